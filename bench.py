@@ -1,0 +1,308 @@
+#!/usr/bin/env python3
+"""Coupling benchmark: IBM coupling cells/s of SolidCloud::interact on one GB300 (and N replicas).
+
+Workload (default): 512^3 uniform hex mesh on [0,1]^3, 16384 spheres / ellipsoids / boxes (lognormal radius,
+median 0.004), FP32 fields resident in HBM (seeded synthetic data).  One step = one interact: sparse reset,
+enumeration of every solid's touched cells, solid fraction, direct forcing and force/torque reduction.
+value = sum over solids of |touched cells| / device time of the step (CUDA events, L2 flushed between steps).
+e2e = the same metric through the host-buffer entry point (U copied in, As/Fs/Ts/Ct + force/torque copied out).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config poly3d_512] [--method refgeo|subsample]
+  python bench.py --impl reference ...   the CPU restatement of the reference's coupling (faithful data
+                                          structures, single thread), timed on a bounded sample of solids
+With N > 1 (torchrun) every rank runs an independent replica: the path has no exchange step on one mesh per GPU
+(replicas only), value = sum over ranks, time = max over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+# algorithmic bytes per unit (one coupling cell = one (solid, touched cell) pair):
+#   U read 12 + As 4 + Fs 12 + Ts 4 + Ct 4 written = 36 B per coupling cell for the whole coupling; per kernel:
+ALG_BYTES = {
+    "couple_kernel": ("coupling_cells", 32.0),   # U read 12, As/Ts/Fs written 20
+    "claim_kernel": ("coupling_cells", 4.0),     # Ct written
+    "finalize_kernel": ("coupling_cells", 8.0),  # Ct and As rewritten for the cells that need it
+    "reset_kernel": ("coupling_cells", 24.0),    # previous cells zeroed
+    "classify_kernel": ("bbox_cells", 1.0),      # one class byte per bbox cell
+    "connect_kernel": ("bbox_cells", 1.0),       # class bytes read once
+}
+METHODS = {"refgeo": 0, "subsample": 1, "learned": 2}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return d, "measured"
+    except Exception:
+        return PEAKS_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(args):
+    from sdfibm_gb300 import abi, workloads
+    w = workloads.CONFIGS[args.config](scale=args.scale)
+    w.opt.fraction_method = METHODS[args.method]
+    return w
+
+
+def cpu_baseline(w, max_solids, max_seconds=25.0):
+    """The oracle (faithful data structures, single thread) on a bounded sample of the workload's solids."""
+    import numpy as np
+
+    from oracle.oracle import OracleCloud
+    S = len(w.solids)
+    rng = np.random.default_rng(123)
+    take = sorted(rng.choice(S, size=min(S, max_solids), replace=False).tolist())
+    sample = []
+    for new_id, s in enumerate(take):
+        d = type(w.solids[s]).from_buffer_copy(w.solids[s])
+        d.id = new_id
+        sample.append(d)
+    U = w.U_numpy().astype(np.float64).reshape(-1)
+    oc = OracleCloud(w.mesh, sample, w.opt, faithful=True)
+    f = oc.new_fields()
+    t0 = time.perf_counter()
+    oc.interact(0.0, w.dt, U, f)
+    wall = time.perf_counter() - t0
+    loop = oc.last_seconds()
+    cells = sum(len(oc.touched(i)[0]) for i in range(len(sample)))
+    return {"value": cells / loop if loop > 0 else None, "unit": "cells/s", "cores": 1, "kind": "port",
+            "sample": "%d of %d solids (random, seed 123) on the full %dx%dx%d mesh, one interact with the "
+                      "reference's data structures (per-solid O(N) cell-type array, std::set, unordered_map "
+                      "phi cache, full-mesh nearest-cell search); timed span = solid loop + checkAlpha as "
+                      "solidcloud.cpp:443-451; %d coupling cells, %.2f s (interact wall %.2f s)"
+                      % (len(sample), S, w.mesh.nx, w.mesh.ny, w.mesh.nz, cells, loop, wall)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    w = make_workload(args)
+    vals = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        info = cpu_baseline(w, args.cpu_solids)
+        if i >= args.warmup:
+            vals.append(info["value"])
+    v = sum(vals) / len(vals)
+    line = {"impl": "reference", "metric": "IBM coupling cells/s", "value": v, "unit": "cells/s", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w.name, "n_cells": w.ncells, "n_solids": len(w.solids), "fraction_method": args.method},
+            "cpu_baseline": dict(info, value=v),
+            "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="poly3d_512")
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--method", default="refgeo", choices=sorted(METHODS))
+    ap.add_argument("--cpu-solids", type=int, default=6)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from sdfibm_gb300 import abi
+    from sdfibm_gb300.cloud import SolidCloud
+
+    w = make_workload(args)
+    w.opt.timing = 1
+    U = w.U_torch()
+    cloud = SolidCloud(w.mesh, w.solids, w.opt)
+    f = cloud.new_fields()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+
+    def step(t):
+        return cloud.interact(t, w.dt, U, f, want_ft=False)
+
+    for i in range(args.warmup):
+        step(i * w.dt)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    cells, kt, bbox, launches = [], {}, [], 0
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        ev0[i].record()
+        step((args.warmup + i) * w.dt)
+        ev1[i].record()
+        st = cloud.stats()  # synchronises
+        cells.append(st["coupling_cells"])
+        bbox.append(st["bbox_cells"])
+        launches += st["launches"]
+        for k, v in cloud.kernel_times().items():
+            kt.setdefault(k, []).append(v)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
+    ms_step = sum(ms) / len(ms)
+    if dist:
+        tt = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_step = float(tt.item())
+    mean_cells = sum(cells) / len(cells)
+    value = mean_cells * world / (ms_step * 1e-3)
+
+    # full time step (interact + evolve + fixInternal), device time
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    step(0.0)
+    cloud.evolve(0.0, w.dt)
+    cloud.fix_internal(f["Ct"], U)
+    e1.record()
+    torch.cuda.synchronize()
+    full_ms = e0.elapsed_time(e1)
+
+    # roofline of the dominant kernel
+    peaks, peaks_kind = load_peaks()
+    kmean = {k: sum(v) / len(v) for k, v in kt.items()}
+    dom = max((k for k in kmean if k in ALG_BYTES), key=lambda k: kmean[k])
+    unit_key, per_unit = ALG_BYTES[dom]
+    units = mean_cells if unit_key == "coupling_cells" else sum(bbox) / len(bbox)
+    achieved = per_unit * units / (kmean[dom] * 1e-3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tfile):
+        try:
+            tr = json.load(open(tfile)).get(args.config, {}).get(args.method, {}).get(dom)
+            if tr:
+                traffic = tr["bytes_per_unit"] * units
+        except Exception:
+            traffic = None
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_kind": peaks_kind,
+                "alg_bytes_per_unit": per_unit, "units": units,
+                "kernel_ms": {k: round(v, 4) for k, v in sorted(kmean.items(), key=lambda x: -x[1])}}
+
+    # end to end through the host-buffer entry point (pinned host fields)
+    e2e = None
+    if not args.no_e2e:
+        N = w.ncells
+        Uh = torch.empty((3, N), dtype=torch.float32, pin_memory=True)
+        Uh.copy_(U)
+        hf = {"As": torch.empty(N, dtype=torch.float32, pin_memory=True),
+              "Fs": torch.empty(3 * N, dtype=torch.float32, pin_memory=True),
+              "Ts": torch.empty(N, dtype=torch.float32, pin_memory=True),
+              "Ct": torch.empty(N, dtype=torch.int32, pin_memory=True)}
+        hn = {k: v.numpy() for k, v in hf.items()}
+        Uhn = Uh.numpy()
+        for i in range(2):
+            cloud.interact_host(0.0, w.dt, Uhn, hn)
+        reps = max(2, min(args.steps, 5))
+        t0 = time.perf_counter()
+        for i in range(reps):
+            cloud.interact_host(i * w.dt, w.dt, Uhn, hn)
+        e2e_s = (time.perf_counter() - t0) / reps
+        e2e = {"value": mean_cells * world / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": 12 * N,
+               "d2h_bytes_per_step": 24 * N + 48 * len(w.solids), "ms_per_step": e2e_s * 1e3}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(w, args.cpu_solids)
+    if rank == 0:
+        line = {"metric": "IBM coupling cells/s", "value": value, "unit": "cells/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 fields, f64 geometry and reductions",
+                "data": "synthetic",
+                "config": {"workload": "%s: %dx%dx%d mesh, %d solids, %s solid fraction, HBM-resident fields"
+                                       % (w.name, w.mesh.nx, w.mesh.ny, w.mesh.nz, len(w.solids), args.method),
+                           "n_cells": w.ncells, "n_solids": len(w.solids), "coupling_cells": mean_cells,
+                           "bbox_cells": sum(bbox) / len(bbox), "fraction_method": args.method,
+                           "l2": "flushed (256 MB write) before every timed step", "full_step_ms": full_ms,
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+                "gpu_launches": launches}
+        print(json.dumps(line))
+    cloud.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,210 @@
+/*
+ * sdfibm_cuda.h — C ABI of the GB300 (sm_103a) fluid–solid coupling library.
+ *
+ * The library is a drop-in for the solid side of sdfibm's time step:
+ *   SolidCloud::interact     src/solidcloud.cpp:435-464  -> sdfibm_cuda_interact
+ *   SolidCloud::evolve       src/solidcloud.cpp:521-562  -> sdfibm_cuda_evolve
+ *   SolidCloud::fixInternal  src/solidcloud.cpp:288-301  -> sdfibm_cuda_fix_internal
+ *   SolidCloud::SolidCloud   src/solidcloud.cpp:209-265  -> sdfibm_cuda_create (after the host has parsed solidDict)
+ *   Solid getters/setters    src/solid.h:58-80           -> sdfibm_cuda_get_solids / sdfibm_cuda_set_solids
+ * The host keeps parsing solidDict with the reference's factories and lowers every Shape / Motion / Forcer /
+ * Material instance into the plain-old-data descriptors below.  No function here exits the process: every entry
+ * point returns an sdfibm_status and sdfibm_cuda_last_error() gives the message.
+ *
+ * Mesh: uniform hexahedral grid (blockMesh single block, simpleGrading 1).  Point (i,j,k) is
+ *   x = origin[0] + i*h[0]  (one multiply, one add; no fused multiply-add), likewise y, z;
+ * cell (i,j,k) has label i + nx*(j + ny*k) and centre origin + (i+0.5)*h.
+ *
+ * Fields (caller-owned, cell-major structure of arrays, device pointers unless stated otherwise):
+ *   U  : float[3][ncells]  (x plane, then y plane, then z plane)
+ *   As : float[ncells], Ts : float[ncells], Fs : float[3][ncells], Ct : int32[ncells]
+ *   FT : double[nsolids][6] = fluid force (3) then fluid torque (3), the values of
+ *        Solid::setFluidForceAndTorque at src/solidcloud.cpp:432.
+ */
+#ifndef SDFIBM_CUDA_H
+#define SDFIBM_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SDFIBM_ABI_VERSION 1
+
+typedef enum sdfibm_status {
+    SDFIBM_OK = 0,
+    SDFIBM_ERR_ARG = 1,       /* bad argument (null pointer, bad size, unknown type id) */
+    SDFIBM_ERR_CAPACITY = 2,  /* a work queue or list outgrew its reserved capacity */
+    SDFIBM_ERR_CUDA = 3,      /* a CUDA runtime call failed */
+    SDFIBM_ERR_TIMEOUT = 4,   /* a bounded device-side wait gave up */
+    SDFIBM_ERR_STATE = 5      /* call out of order (e.g. evolve before any interact) */
+} sdfibm_status;
+
+/* Shape registry of src/libshape/shapefactory.h:11-35 (names kept, ids are this ABI's). */
+typedef enum sdfibm_shape_type {
+    SDFIBM_SHAPE_CIRCLE = 1,          /* circle.h        p = {radius, radiusSQR} */
+    SDFIBM_SHAPE_SPHERE = 2,          /* sphere.h        p = {radius, radiusSQR} */
+    SDFIBM_SHAPE_ELLIPSE = 3,         /* ellipse.h       p = {ra, rb, 1/ra^2, 1/rb^2} */
+    SDFIBM_SHAPE_ELLIPSOID = 4,       /* ellipsoid.h     p = {ra, rb, rc, 1/ra^2, 1/rb^2, 1/rc^2} (com ignored) */
+    SDFIBM_SHAPE_RECTANGLE = 5,       /* rectangle.h     p = {ra, rb} */
+    SDFIBM_SHAPE_BOX = 6,             /* box.h           p = {ra, rb, rc} */
+    SDFIBM_SHAPE_PLANE = 7,           /* plane.h         p = {} ; inside = local y < 0, infinite */
+    SDFIBM_SHAPE_CIRCLE_TAIL = 8,     /* circle_tail.h   p = {radius, ratio, radiusb, radiusSQR, radiusa} */
+    SDFIBM_SHAPE_CIRCLE_TWOTAIL = 9   /* circle_twotail.h p = {radius, ratio, radiusb(=thickness/2), radiusSQR, radiusa} */
+} sdfibm_shape_type;
+
+/* Motion registry of src/libmotion/motionfactory.cpp:33-46 ("free" = none, src/solidcloud.cpp:185). */
+typedef enum sdfibm_motion_type {
+    SDFIBM_MOTION_FREE = 0,
+    SDFIBM_MOTION_000002 = 1,           /* p = {period, omega=2pi/period} */
+    SDFIBM_MOTION_110002 = 2,           /* p = {period, omega} */
+    SDFIBM_MOTION_222000 = 3,           /* p = {u, v, w} */
+    SDFIBM_MOTION_SINEDIRECTIONAL = 4,  /* p = {amplitude, period, omega, dir.x, dir.y, dir.z} */
+    SDFIBM_MOTION_01MASK = 5,           /* p = {vmask.x, vmask.y, vmask.z, omask.x, omask.y, omask.z} */
+    SDFIBM_MOTION_ROTOR = 6,            /* p = {period, omega, radius, theta0, selfom} */
+    SDFIBM_MOTION_OPENCLOSE = 7         /* p = {} */
+} sdfibm_motion_type;
+
+/* Forcer registry of src/libforcer/forcerfactory.h:7-16. */
+typedef enum sdfibm_forcer_type {
+    SDFIBM_FORCER_NONE = 0,
+    SDFIBM_FORCER_CONSTANT = 1,  /* p = {force.xyz, torque.xyz} */
+    SDFIBM_FORCER_SPRING = 2,    /* p = {pivot.xyz, k, l} */
+    SDFIBM_FORCER_MAGNETIC = 3   /* p = {direction.xyz, A, w} */
+} sdfibm_forcer_type;
+
+/* Solid-solid collision handling (src/solidcloud.cpp:477-519, src/libcollision/). */
+typedef enum sdfibm_collision_mode {
+    SDFIBM_COLLISION_OFF = 0,        /* reference HEAD: m_radiusB = -1 (solidcloud.cpp:74) gives an empty grid */
+    SDFIBM_COLLISION_REFERENCE = 1,  /* grid spacing 2*max(radiusB), the reference's SHAPE2ID table and force law */
+    SDFIBM_COLLISION_SPHERES = 2     /* same grid and law, every finite shape treated as its bounding sphere */
+} sdfibm_collision_mode;
+
+/* Cut-cell solid fraction evaluator. */
+typedef enum sdfibm_fraction_method {
+    SDFIBM_FRACTION_REFGEO = 0,     /* GeometricTools::calcCellVolume (geometrictools.cpp:47-116), FP64 */
+    SDFIBM_FRACTION_SUBSAMPLE = 1,  /* stratified midpoint lattice of n^3 (3D) / n^2 (2D) isInside samples */
+    SDFIBM_FRACTION_LEARNED = 2     /* 11-64-64-1 MLP on vertex SDFs, SUBSAMPLE fallback outside the band */
+} sdfibm_fraction_method;
+
+typedef struct sdfibm_mesh_desc {
+    int32_t nx, ny, nz;   /* cells per axis */
+    int32_t twod;         /* on_twod: calcCellVolume puts the cell apex at z = 0 (geometrictools.cpp:57-58) */
+    double origin[3];     /* lowest mesh point */
+    double h[3];          /* cell size per axis */
+} sdfibm_mesh_desc;
+
+typedef struct sdfibm_shape_desc {
+    int32_t type;          /* sdfibm_shape_type */
+    int32_t collision_id;  /* SHAPE2ID of collision.h:11-15: Plane 0, Circle 1, Sphere 2, any other name 0 */
+    double p[8];           /* type parameters, see sdfibm_shape_type */
+    double com[3];         /* IShape::m_com (ignored by Ellipsoid and Plane) */
+    double radiusB;        /* IShape::m_radiusB */
+    double volume;         /* IShape::m_volume */
+    double volume_inv;     /* IShape::m_volumeINV */
+    double moi_inv[9];     /* IShape::m_moiINV = Foam::inv(m_moi), row-major */
+} sdfibm_shape_desc;
+
+typedef struct sdfibm_solid_desc {
+    int32_t id;            /* Solid::id (position in the solids dictionary) */
+    int32_t motion_type;   /* sdfibm_motion_type */
+    int32_t forcer_type;   /* sdfibm_forcer_type */
+    int32_t pad0;
+    sdfibm_shape_desc shape;
+    double motion_p[8];
+    double forcer_p[8];
+    double rho;            /* IMaterial::m_rho */
+    double mass;           /* Solid::mass = m_volume*rho        (solid.h:100) */
+    double mass_inv;       /* Solid::mass_inv = m_volumeINV/rho (solid.h:101) */
+    double moi_inv[9];     /* Solid::moi_inv = m_moiINV/rho     (solid.h:102) */
+    double pos[3];         /* centre */
+    double quat[4];        /* orientation (w, x, y, z) = quaternion(XYZ, euler) */
+    double vel[3];
+    double omega[3];
+} sdfibm_solid_desc;
+
+/* Full dynamic state of one Solid (solid.h:20-44). */
+typedef struct sdfibm_solid_state {
+    double pos[3], quat[4], vel[3], omega[3];
+    double force[3], torque[3];
+    double fluid_force[3], fluid_torque[3], fluid_force_old[3], fluid_torque_old[3];
+    double forcer_force[3], forcer_torque[3], forcer_force_old[3], forcer_torque_old[3];
+    int32_t first_fluid_step, first_forcer_step;
+} sdfibm_solid_state;
+
+typedef struct sdfibm_options {
+    double rho_f;            /* m_rhof: transportProperties rho, 0 when on_fluid is off (solidcloud.cpp:247-251) */
+    double gravity[3];       /* meta.gravity */
+    int32_t collision_mode;  /* sdfibm_collision_mode */
+    int32_t n_subiter;       /* 0: the reference rule (20, or 1 for a single solid: solidcloud.cpp:524-527) */
+    int32_t fraction_method; /* sdfibm_fraction_method */
+    int32_t subsample_n;     /* samples per axis for SUBSAMPLE (0: 10) */
+    int32_t dense_reset;     /* 1: zero the four fields over the whole mesh every interact (solidcloud.cpp:438-441);
+                                0: zero only the cells touched by the previous interact (identical values while
+                                the caller leaves those fields alone between calls) */
+    int32_t exact_forcing;   /* 1: forcing and torque per cell in FP64 exactly as solidcloud.cpp:384-417 (default);
+                                0: FP32 forcing with FP64 force/torque sums */
+    int32_t tile_cells;      /* 0: autotuned.  Cells per (solid, cell-tile) work item otherwise */
+    int32_t timing;          /* 1: record CUDA events around every kernel (sdfibm_cuda_kernel_times) */
+    int32_t reserved[6];
+} sdfibm_options;
+
+typedef struct sdfibm_ctx sdfibm_ctx;
+
+/* Defaults for sdfibm_options (rho_f 1, no gravity, collisions off, REF-GEO, sparse reset, exact forcing). */
+void sdfibm_options_default(sdfibm_options* opt);
+
+/* SolidCloud::SolidCloud (solidcloud.cpp:209-265) minus the dictionary parsing: uploads the descriptors and
+ * reserves device work space.  stream may be NULL (legacy default stream). */
+int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* solids, int32_t nsolids,
+                       const sdfibm_options* opt, void* cuda_stream, sdfibm_ctx** out);
+
+/* SolidCloud::interact (solidcloud.cpp:435-464): resets As/Fs/Ts/Ct, enumerates the touched cells of every solid
+ * (CellEnumerator, cellenumerator.cpp:6-78), computes As (REF-GEO / SUBSAMPLE / LEARNED), the direct forcing
+ * Fs += alpha(U-us)/dt, Ts += alpha, Ct, clamps As to 1 (checkAlpha, :564-570) and reduces the fluid force and
+ * torque of every solid.  U/As/Fs/Ts/Ct are device pointers; FT (may be NULL) is a HOST pointer that receives
+ * the per-solid fluid force and torque (the call then synchronises the stream). */
+int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs, float* Ts,
+                         int32_t* Ct, double* FT);
+
+/* Same as sdfibm_cuda_interact but every field pointer is a HOST pointer: the call copies U in and the four
+ * fields out around the device work (the path an OpenFOAM-resident caller takes). */
+int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs,
+                              float* Ts, int32_t* Ct, double* FT);
+
+/* SolidCloud::evolve (solidcloud.cpp:521-562): n_subiter sub-steps of AB2 forcer and fluid force, buoyancy-reduced
+ * gravity, solid-solid collision and Solid::move (solid.h:181-202), then storeOldForce. */
+int sdfibm_cuda_evolve(sdfibm_ctx* ctx, double time, double dt);
+
+/* SolidCloud::fixInternal (solidcloud.cpp:288-301): U[c] = velocity of solid Ct[c]-4 at the cell centre for every
+ * cell with Ct[c] >= 4.  Visits only the cells the last interact touched. */
+int sdfibm_cuda_fix_internal(sdfibm_ctx* ctx, const int32_t* Ct, float* U);
+
+/* Solid state download / upload for saveState, saveRestart and restarts (solidcloud.cpp:578-665). */
+int sdfibm_cuda_get_solids(sdfibm_ctx* ctx, sdfibm_solid_state* out, int32_t nsolids);
+int sdfibm_cuda_set_solids(sdfibm_ctx* ctx, const sdfibm_solid_state* in, int32_t nsolids);
+
+/* Touched-cell list of one solid from the last interact, as CellEnumerator::intersect would give it: cells sorted
+ * ascending within each type, ALL_INSIDE first, then CENTER_INSIDE, then CENTER_OUTSIDE (solidcloud.cpp:370-374).
+ * types[i] is 1 (ALL_INSIDE), 2 (CENTER_INSIDE) or 3 (CENTER_OUTSIDE).  Returns the count through *n (host). */
+int sdfibm_cuda_touched(sdfibm_ctx* ctx, int32_t solid, int64_t* cells, int8_t* types, int64_t capacity,
+                        int64_t* n);
+
+/* Counters of the last interact (host): [0] coupling cells (sum over solids of |T_s|), [1] cut cells,
+ * [2] bbox cells scanned, [3] vertices re-checked in FP64, [4] work items, [5] kernel launches. */
+int sdfibm_cuda_stats(sdfibm_ctx* ctx, int64_t* out, int32_t n);
+
+/* Per-kernel device time (milliseconds, CUDA events on the context's stream) of the last interact when
+ * options.timing is set: names[i] receives a static kernel name, ms[i] its time; returns the count through *n. */
+int sdfibm_cuda_kernel_times(sdfibm_ctx* ctx, const char** names, double* ms, int32_t capacity, int32_t* n);
+
+const char* sdfibm_cuda_last_error(const sdfibm_ctx* ctx);
+const char* sdfibm_cuda_version(void);
+void sdfibm_cuda_destroy(sdfibm_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SDFIBM_CUDA_H */

@@ -1,0 +1,49 @@
+/*
+ * sdfibm_host.h — host-side lowering of sdfibm's plugin objects into the POD descriptors of sdfibm_cuda.h, and the
+ * solidDict front end.  These replace the reference's construction path:
+ *   ShapeFactory / IShape constructors   src/libshape/shapefactory.h:9-39, src/libshape/{circle,...}.h ctors
+ *   MotionFactory::create                src/libmotion/motionfactory.cpp:23-31 and the motion ctors
+ *   ForcerFactory / IForcer ctors        src/libforcer/forcerfactory.h:7-16, {constant,spring,magnetic}.h ctors
+ *   IMaterial (General) + Solid::setMaterial   src/solidcloud.cpp:127-143, src/solid.h:95-103
+ *   Solid::setOrientation (euler degrees)      src/solidcloud.cpp:176-177, src/solid.h:76-80
+ *   SolidCloud::initFromDictionary             src/solidcloud.cpp:14-206
+ * Every function returns an sdfibm_status; messages go to the caller-provided buffer (never to stdout/exit).
+ */
+#ifndef SDFIBM_HOST_H
+#define SDFIBM_HOST_H
+
+#include "sdfibm_cuda.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* IShape constructor of the given type: raw holds the dictionary scalars in the order of the sdfibm_shape_type
+ * comment (radius | radiusa, radiusb[, radiusc] | radius, ratio, thickness); com may be NULL (zero). */
+int sdfibm_host_make_shape(int32_t type, const double* raw, const double* com, sdfibm_shape_desc* out);
+
+/* Motion constructors: raw holds the dictionary values (period | u,v,w | amplitude, period, direction.xyz |
+ * mask digits as 0/1 | period, radius, theta0, selfom).  The derived parameters are filled in. */
+int sdfibm_host_make_motion(int32_t type, const double* raw, double* motion_p8);
+
+/* Forcer constructors: raw = force.xyz, torque.xyz | pivot.xyz, k, l | direction.xyz, A, w. */
+int sdfibm_host_make_forcer(int32_t type, const double* raw, double* forcer_p8);
+
+/* quaternion(quaternion::XYZ, euler*pi/180) */
+void sdfibm_host_quat_from_euler_deg(const double* euler_deg, double* quat_wxyz);
+
+/* Assemble a solid: shape + material density (Solid::setMaterial) + pose/velocity.  quat may be NULL (use euler). */
+int sdfibm_host_make_solid(int32_t id, const sdfibm_shape_desc* shape, double rho, int32_t motion_type,
+                           const double* motion_p8, int32_t forcer_type, const double* forcer_p8, const double* pos,
+                           const double* euler_deg, const double* vel, const double* omega, sdfibm_solid_desc* out);
+
+/* Parse a solidDict (OpenFOAM dictionary text) into solids and options (meta: on_fluid, on_twod, gravity).
+ * Writes up to capacity solids; *nsolids receives the count.  rho_f is the transportProperties density
+ * (0 is used when on_fluid is off).  msg (may be NULL) receives an error text. */
+int sdfibm_host_parse_soliddict(const char* text, double rho_f, sdfibm_solid_desc* solids, int32_t capacity,
+                                int32_t* nsolids, sdfibm_options* opt, int32_t* on_twod, char* msg, int32_t msg_len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SDFIBM_HOST_H */

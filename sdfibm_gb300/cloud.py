@@ -1,0 +1,126 @@
+"""Python mirror of sdfibm's SolidCloud API (src/solidcloud.h:89-124) on the GB300 coupling library.
+
+    cloud = SolidCloud(mesh, solids, options)          # SolidCloud::SolidCloud after solidDict parsing
+    FT = cloud.interact(t, dt, U, fields)              # SolidCloud::interact   (fields: As, Fs, Ts, Ct)
+    cloud.evolve(t, dt)                                # SolidCloud::evolve
+    cloud.fix_internal(fields["Ct"], U)                # SolidCloud::fixInternal
+    cloud.states() / cloud.set_states(st)              # Solid getters / setters (saveState, saveRestart)
+
+Fields are CUDA tensors in the cell-major layout of include/sdfibm_cuda.h: U and Fs have shape (3, N) float32,
+As and Ts (N,) float32, Ct (N,) int32.  Every call goes through libsdfibm_cuda.so; errors raise CouplingError
+carrying the library's status and message.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from ._lib import load
+
+
+class CouplingError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("sdfibm_cuda status %d: %s" % (status, msg))
+        self.status = status
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+class SolidCloud:
+    def __init__(self, mesh, solids, opt=None, stream=None):
+        self._L = load()
+        self.mesh = mesh
+        self.nsolids = len(solids)
+        self.ncells = int(mesh.nx) * int(mesh.ny) * int(mesh.nz)
+        self._solids = (abi.SolidDesc * max(1, len(solids)))(*solids)
+        self.opt = opt if opt is not None else abi.options()
+        self._h = C.c_void_p()
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        rc = self._L.sdfibm_cuda_create(C.byref(mesh), self._solids, len(solids), C.byref(self.opt), s,
+                                        C.byref(self._h))
+        if rc != abi.OK:
+            raise CouplingError(rc, "create failed")
+
+    def _check(self, rc):
+        if rc != abi.OK:
+            raise CouplingError(rc, self._L.sdfibm_cuda_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.sdfibm_cuda_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def new_fields(self, device="cuda"):
+        import torch
+        N = self.ncells
+        return dict(As=torch.zeros(N, dtype=torch.float32, device=device),
+                    Fs=torch.zeros(3, N, dtype=torch.float32, device=device),
+                    Ts=torch.zeros(N, dtype=torch.float32, device=device),
+                    Ct=torch.zeros(N, dtype=torch.int32, device=device))
+
+    def interact(self, time, dt, U, fields, want_ft=True):
+        FT = np.zeros((max(1, self.nsolids), 6)) if want_ft else None
+        rc = self._L.sdfibm_cuda_interact(self._h, float(time), float(dt), _ptr(U), _ptr(fields["As"]),
+                                          _ptr(fields["Fs"]), _ptr(fields["Ts"]), _ptr(fields["Ct"]),
+                                          FT.ctypes.data_as(C.c_void_p) if want_ft else None)
+        self._check(rc)
+        return FT[:self.nsolids] if want_ft else None
+
+    def interact_host(self, time, dt, U, fields):
+        """Host (numpy) fields: the library copies U in and the fields out (pinned or pageable)."""
+        FT = np.zeros((max(1, self.nsolids), 6))
+        p = lambda a: a.ctypes.data_as(C.c_void_p)
+        rc = self._L.sdfibm_cuda_interact_host(self._h, float(time), float(dt), p(U), p(fields["As"]), p(fields["Fs"]),
+                                               p(fields["Ts"]), p(fields["Ct"]), p(FT))
+        self._check(rc)
+        return FT[:self.nsolids]
+
+    def evolve(self, time, dt):
+        self._check(self._L.sdfibm_cuda_evolve(self._h, float(time), float(dt)))
+
+    def fix_internal(self, Ct, U):
+        self._check(self._L.sdfibm_cuda_fix_internal(self._h, _ptr(Ct), _ptr(U)))
+
+    def states(self):
+        st = (abi.SolidState * max(1, self.nsolids))()
+        self._check(self._L.sdfibm_cuda_get_solids(self._h, st, self.nsolids))
+        return list(st)[:self.nsolids]
+
+    def set_states(self, states):
+        arr = (abi.SolidState * max(1, self.nsolids))(*states)
+        self._check(self._L.sdfibm_cuda_set_solids(self._h, arr, self.nsolids))
+
+    def touched(self, s):
+        n = C.c_int64(0)
+        self._check(self._L.sdfibm_cuda_touched(self._h, int(s), None, None, 0, C.byref(n)))
+        cells = np.zeros(max(1, n.value), np.int64)
+        types = np.zeros(max(1, n.value), np.int8)
+        self._check(self._L.sdfibm_cuda_touched(self._h, int(s), cells.ctypes.data_as(C.c_void_p),
+                                                types.ctypes.data_as(C.c_void_p), n.value, C.byref(n)))
+        return cells[:n.value], types[:n.value]
+
+    def kernel_times(self):
+        """{kernel name: device ms} of the last interact (options.timing must be set)."""
+        names = (C.c_char_p * 32)()
+        ms = (C.c_double * 32)()
+        n = C.c_int32(0)
+        self._check(self._L.sdfibm_cuda_kernel_times(self._h, names, ms, 32, C.byref(n)))
+        out = {}
+        for i in range(n.value):
+            k = names[i].decode()
+            out[k] = out.get(k, 0.0) + ms[i]
+        return out
+
+    def stats(self):
+        out = (C.c_int64 * 6)()
+        self._check(self._L.sdfibm_cuda_stats(self._h, out, 6))
+        keys = ("coupling_cells", "cut_cells", "bbox_cells", "fp64_rechecks", "work_items", "launches")
+        return dict(zip(keys, list(out)))

@@ -1,0 +1,651 @@
+// C ABI of the coupling library (include/sdfibm_cuda.h): context set-up, launch sequencing, error reporting.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sdfibm_cuda.h"
+#include "kernels.cuh"
+
+namespace sdfibm_dev {
+// coupling.cu
+__global__ void plan_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state* st, SolidPlan* plan, int S,
+                            Counters* cnt);
+__global__ void classify_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state* st, SolidPlan* plan,
+                                const int32_t* tile_prefix, int S, int total_tiles, uint8_t* scratch, Counters* cnt);
+__global__ void connect_kernel(MeshK m, const SolidK* sk, SolidPlan* plan, const uint8_t* scratch, uint32_t* gbitmaps,
+                               int32_t* in_cell, int32_t* in_solid, int32_t* cut_cell, int32_t* cut_solid,
+                               int64_t cap_in, int64_t cap_cut, Counters* cnt, int smem_words);
+
+__global__ void couple_kernel(CoupleArgs A);
+__global__ void claim_kernel(const int32_t* in_cell, const int32_t* in_solid, const int32_t* cut_cell,
+                             const int32_t* cut_solid, int32_t* Ct, const Counters* cnt, int64_t N);
+__global__ void finalize_kernel(const int32_t* in_cell, const int32_t* in_solid, const int32_t* cut_cell,
+                                const int32_t* cut_solid, float* As, float* Ts, float* Fs, int32_t* Ct, Counters* cnt,
+                                int64_t N, int32_t* sh_keys, double* sh_vals, const int32_t* sh_used, int32_t sh_mask);
+__global__ void ft_kernel(const double* ftacc, double* ft, int S, double rho_f);
+__global__ void reset_kernel(const int32_t* in_cell, const int32_t* cut_cell, const Counters* cnt, int64_t N,
+                             float* As, float* Fs, float* Ts, int32_t* Ct);
+__global__ void fix_internal_kernel(MeshK m, const sdfibm_solid_state* st, const int32_t* in_cell,
+                                    const int32_t* in_solid, const int32_t* Ct, float* U, const Counters* cnt);
+// evolve.cu
+
+__global__ void evolve_independent_kernel(const SolidK* sk, sdfibm_solid_state* st, int S, int nsub, double time,
+                                          double dt_sub, double rho_f, D3 g);
+__global__ void evolve_pre_kernel(const SolidK* sk, sdfibm_solid_state* st, int S, double time, double rho_f, D3 g,
+                                  GridK gk, int64_t* hashes, int32_t* counts);
+__global__ void grid_scan_kernel(const int32_t* counts, int32_t* start, int32_t* cursor, int64_t ncell);
+__global__ void grid_scatter_kernel(const int64_t* hashes, int32_t* cursor, int32_t* list, int S, int64_t ncell);
+__global__ void collide_kernel(const SolidK* sk, sdfibm_solid_state* st, int S, GridK gk, const int64_t* hashes,
+                               const int32_t* start, const int32_t* list, int mode);
+__global__ void move_kernel(const SolidK* sk, sdfibm_solid_state* st, int S, double time, double dt);
+__global__ void store_old_kernel(sdfibm_solid_state* st, int S);
+__global__ void ft_to_state_kernel(const double* ft, sdfibm_solid_state* st, int S);
+}  // namespace sdfibm_dev
+
+using namespace sdfibm_dev;
+
+// copies this call's fluid force and torque into the solid state (Solid::setFluidForceAndTorque)
+namespace sdfibm_dev {
+__global__ void ft_to_state_kernel(const double* ft, sdfibm_solid_state* st, int S) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    for (int a = 0; a < 3; ++a) {
+        st[s].fluid_force[a] = ft[6 * s + a];
+        st[s].fluid_torque[a] = ft[6 * s + 3 + a];
+    }
+}
+}  // namespace sdfibm_dev
+
+struct sdfibm_ctx {
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    int num_sms = 0;
+    MeshK mesh{};
+    sdfibm_mesh_desc mdesc{};
+    sdfibm_options opt{};
+    int S = 0;
+    int nsub = 20;
+    std::vector<SolidK> hk;
+    SolidK* d_sk = nullptr;
+    sdfibm_solid_state* d_st = nullptr;
+    SolidPlan* d_plan = nullptr;
+    int32_t* d_tile_prefix = nullptr;
+    int total_tiles = 0;
+    uint8_t* d_scratch = nullptr;
+    int64_t scratch_bytes = 0;
+    uint32_t* d_gbitmaps = nullptr;
+    int64_t gbitmap_words = 0;
+    int connect_smem_bytes = 0;
+    int32_t *d_in_cell = nullptr, *d_in_solid = nullptr, *d_cut_cell = nullptr, *d_cut_solid = nullptr;
+    int64_t cap = 0;
+    int32_t* d_sh_keys = nullptr;
+    double* d_sh_vals = nullptr;
+    int32_t* d_sh_used = nullptr;
+    int32_t sh_mask = 0;
+    Counters* d_cnt = nullptr;
+    Counters* h_cnt = nullptr;  // pinned
+    double* d_ftacc = nullptr;
+    double* d_ft = nullptr;
+    double* h_ft = nullptr;  // pinned
+    // collision grid
+    bool grid_active = false;
+    GridK gk{};
+    int64_t* d_hash = nullptr;
+    int32_t *d_gcount = nullptr, *d_gstart = nullptr, *d_gcursor = nullptr, *d_glist = nullptr;
+    // fields seen by the last interact (sparse reset is only valid on the same buffers)
+    const void* last_fields[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool interacted = false;
+    // host staging for sdfibm_cuda_interact_host
+    float *d_U = nullptr, *d_As = nullptr, *d_Fs = nullptr, *d_Ts = nullptr;
+    int32_t* d_Ct = nullptr;
+    int classify_grid = 0, couple_grid = 0;
+    // per-kernel events (options.timing)
+    static constexpr int MAXEV = 24;
+    cudaEvent_t ev[MAXEV + 1] = {};
+    const char* ev_name[MAXEV] = {};
+    int nev = 0;
+    bool ev_ready = false;
+    int launches_last = 0;
+    std::string err;
+};
+
+// event bracketing of each launch when timing is on: mark(ctx, name) after a launch records its end
+static void mark_begin(sdfibm_ctx* ctx) {
+    ctx->nev = 0;
+    if (!ctx->opt.timing) return;
+    if (!ctx->ev_ready) {
+        for (int i = 0; i <= sdfibm_ctx::MAXEV; ++i) cudaEventCreate(&ctx->ev[i]);
+        ctx->ev_ready = true;
+    }
+    cudaEventRecord(ctx->ev[0], ctx->stream);
+}
+static void mark(sdfibm_ctx* ctx, const char* name) {
+    if (!ctx->opt.timing || ctx->nev >= sdfibm_ctx::MAXEV) return;
+    ctx->ev_name[ctx->nev] = name;
+    cudaEventRecord(ctx->ev[ctx->nev + 1], ctx->stream);
+    ++ctx->nev;
+}
+
+static int fail(sdfibm_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+#define CK(call)                                                                                         \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess)                                                                           \
+            return fail(ctx, SDFIBM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
+    } while (0)
+
+template <class T>
+static cudaError_t dalloc(T** p, size_t n) {
+    return cudaMalloc((void**)p, std::max<size_t>(1, n) * sizeof(T));
+}
+
+extern "C" {
+
+const char* sdfibm_cuda_version(void) { return "sdfibm-gb300 1.0 (sm_103a)"; }
+
+const char* sdfibm_cuda_last_error(const sdfibm_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+void sdfibm_options_default(sdfibm_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->rho_f = 1.0;
+    o->collision_mode = SDFIBM_COLLISION_OFF;
+    o->fraction_method = SDFIBM_FRACTION_REFGEO;
+    o->subsample_n = 10;
+    o->exact_forcing = 1;
+}
+
+// radius around -com of a sphere (or, for 2-D shapes, a disc in the local x-y plane) that holds every point the
+// shape's isInside accepts (IShape::m_radiusB is not such a bound for rectangles, boxes and tails)
+static bool bound_radius(const sdfibm_shape_desc& s, double& r, int& prism) {
+    const double* a = s.p;
+    prism = 0;
+    switch (s.type) {
+        case SDFIBM_SHAPE_CIRCLE: r = a[0]; prism = 1; return true;
+        case SDFIBM_SHAPE_SPHERE: r = a[0]; return true;
+        case SDFIBM_SHAPE_ELLIPSE: r = std::max(a[0], a[1]); prism = 1; return true;
+        case SDFIBM_SHAPE_ELLIPSOID: r = std::max({a[0], a[1], a[2]}); return true;
+        case SDFIBM_SHAPE_RECTANGLE: r = std::sqrt(a[0] * a[0] + a[1] * a[1]); prism = 1; return true;
+        case SDFIBM_SHAPE_BOX: r = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); return true;
+        case SDFIBM_SHAPE_CIRCLE_TAIL:
+        case SDFIBM_SHAPE_CIRCLE_TWOTAIL:
+            r = std::max(a[0], std::sqrt(4 * a[4] * a[4] + a[2] * a[2]));
+            prism = 1;
+            return true;
+        case SDFIBM_SHAPE_PLANE: r = 0; return true;
+        default: return false;
+    }
+}
+
+int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* solids, int32_t nsolids,
+                       const sdfibm_options* opt_in, void* cuda_stream, sdfibm_ctx** out) {
+    if (!out) return SDFIBM_ERR_ARG;
+    *out = nullptr;
+    if (!mesh || (nsolids > 0 && !solids) || nsolids < 0 || nsolids > (1 << 28)) return SDFIBM_ERR_ARG;
+    if (mesh->nx <= 0 || mesh->ny <= 0 || mesh->nz <= 0) return SDFIBM_ERR_ARG;
+    if (!(mesh->h[0] > 0 && mesh->h[1] > 0 && mesh->h[2] > 0)) return SDFIBM_ERR_ARG;
+    const int64_t N = (int64_t)mesh->nx * mesh->ny * mesh->nz;
+    if (N >= ((int64_t)1 << 31)) return SDFIBM_ERR_ARG;  // cell labels are stored as int32
+    auto* ctx = new sdfibm_ctx();
+    ctx->mdesc = *mesh;
+    if (opt_in) ctx->opt = *opt_in; else sdfibm_options_default(&ctx->opt);
+    if (ctx->opt.subsample_n <= 0) ctx->opt.subsample_n = 10;
+    ctx->S = nsolids;
+    ctx->nsub = ctx->opt.n_subiter > 0 ? ctx->opt.n_subiter : (nsolids == 1 ? 1 : 20);
+    ctx->stream = (cudaStream_t)cuda_stream;
+    auto bail = [&](int code) {
+        int c = code;
+        sdfibm_cuda_destroy(ctx);
+        return c;
+    };
+    if (cudaGetDevice(&ctx->device) != cudaSuccess) { delete ctx; return SDFIBM_ERR_CUDA; }
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    MeshK& m = ctx->mesh;
+    m.nx = mesh->nx; m.ny = mesh->ny; m.nz = mesh->nz; m.twod = mesh->twod;
+    for (int a = 0; a < 3; ++a) { m.o[a] = mesh->origin[a]; m.h[a] = mesh->h[a]; m.h32[a] = (float)mesh->h[a]; }
+    m.ncells = N;
+    m.V = mesh->h[0] * mesh->h[1] * mesh->h[2];
+    const int32_t n3[3] = {mesh->nx, mesh->ny, mesh->nz};
+
+    // static per-solid records
+    ctx->hk.resize(nsolids);
+    int64_t scratch = 0, gwords = 0, bbox_total = 0;
+    int64_t tiles = 0;
+    int max_smem_words = 0;
+    const int SMEM_CAP_BYTES = 200 * 1024;
+    for (int s = 0; s < nsolids; ++s) {
+        const sdfibm_solid_desc& d = solids[s];
+        SolidK& k = ctx->hk[s];
+        std::memset(&k, 0, sizeof(k));
+        k.shape.type = d.shape.type;
+        for (int i = 0; i < 8; ++i) { k.shape.p[i] = d.shape.p[i]; k.shape.p32[i] = (float)d.shape.p[i]; }
+        for (int i = 0; i < 3; ++i) { k.shape.com[i] = d.shape.com[i]; k.shape.com32[i] = (float)d.shape.com[i]; }
+        double r;
+        int prism;
+        if (!bound_radius(d.shape, r, prism)) { ctx->err = "unknown shape type"; return bail(SDFIBM_ERR_ARG); }
+        k.shape.bound_r = r;
+        k.shape.prism = prism;
+        k.infinite = d.shape.type == SDFIBM_SHAPE_PLANE;
+        const double rr = r * (1.0 + 1e-9) + 1e-12;
+        for (int a = 0; a < 3; ++a) {
+            int64_t e;
+            if (k.infinite || (prism && a == 2)) e = n3[a];
+            else e = (int64_t)std::ceil(2.0 * rr / mesh->h[a]) + 4 + (prism ? 4 : 0);
+            if (!k.infinite && !(prism && a == 2) && e >= (int64_t)n3[a] + 4) e = (int64_t)n3[a] + 4;  // bounded
+            k.ext[a] = (int32_t)e;
+        }
+        if (!k.infinite && prism && !(d.quat[1] == 0.0 && d.quat[2] == 0.0)) {
+            // a 2-D shape that does not rotate about z: its prism may cross the whole mesh
+            for (int a = 0; a < 2; ++a) k.ext[a] = n3[a] + 4;
+        }
+        const int tz = std::min(8, k.ext[2]);
+        k.tdim[2] = tz;
+        k.tdim[0] = tz <= 2 ? 32 : 8;
+        k.tdim[1] = tz <= 2 ? 16 : 8;
+        for (int a = 0; a < 3; ++a) k.ntile[a] = (k.ext[a] + k.tdim[a] - 1) / k.tdim[a];
+        k.tile_base = (int32_t)tiles;
+        tiles += (int64_t)k.ntile[0] * k.ntile[1] * k.ntile[2];
+        const int64_t cells = (int64_t)k.ext[0] * k.ext[1] * k.ext[2];
+        k.scratch_off = scratch;
+        scratch += (cells + 15) & ~(int64_t)15;
+        bbox_total += std::min<int64_t>(cells, N);
+        const int64_t words = 2 * (int64_t)k.ext[1] * k.ext[2] * ((k.ext[0] + 31) / 32);
+        if (words * 4 > SMEM_CAP_BYTES) {
+            k.bitmap_global = 1;
+            k.bitmap_off = gwords;
+            gwords += words;
+        } else {
+            max_smem_words = std::max<int>(max_smem_words, (int)words);
+        }
+        k.motion_type = d.motion_type;
+        k.forcer_type = d.forcer_type;
+        k.collision_id = d.shape.collision_id;
+        k.radiusB = d.shape.radiusB;
+        k.rho = d.rho; k.mass = d.mass; k.mass_inv = d.mass_inv;
+        for (int i = 0; i < 9; ++i) k.moi_inv[i] = d.moi_inv[i];
+        for (int i = 0; i < 8; ++i) { k.motion_p[i] = d.motion_p[i]; k.forcer_p[i] = d.forcer_p[i]; }
+    }
+    if (tiles >= ((int64_t)1 << 31)) { ctx->err = "too many bbox tiles"; return bail(SDFIBM_ERR_CAPACITY); }
+    ctx->total_tiles = (int)tiles;
+    ctx->scratch_bytes = scratch;
+    ctx->gbitmap_words = gwords;
+    ctx->connect_smem_bytes = max_smem_words * 4;
+    ctx->cap = std::max<int64_t>(1, bbox_total);
+
+    {
+        // shared-cell table: a power of two well above the expected count of cells touched by several solids
+        int64_t want = std::max<int64_t>(1 << 12, std::min<int64_t>(ctx->cap, N) / 4);
+        want = std::min<int64_t>(want, (int64_t)1 << 22);
+        int64_t t = 1;
+        while (t < 2 * want) t <<= 1;
+        ctx->sh_mask = (int32_t)(t - 1);
+    }
+    std::vector<int32_t> prefix(nsolids + 1);
+    for (int s = 0; s < nsolids; ++s) prefix[s] = ctx->hk[s].tile_base;
+    prefix[nsolids] = (int32_t)tiles;
+
+    // collision grid (UGrid(bbox of the mesh, 2*max radiusB))
+    if (ctx->opt.collision_mode != SDFIBM_COLLISION_OFF && nsolids > 0) {
+        double rB = -1.0;
+        for (int s = 0; s < nsolids; ++s) rB = std::max(rB, solids[s].shape.radiusB);
+        const double delta = 2 * rB;
+        const double dINV = 1.0 / delta;
+        const double lo[3] = {mesh->origin[0], mesh->origin[1], mesh->origin[2]};
+        const double hi[3] = {mesh->origin[0] + (double)mesh->nx * mesh->h[0],
+                              mesh->origin[1] + (double)mesh->ny * mesh->h[1],
+                              mesh->origin[2] + (double)mesh->nz * mesh->h[2]};
+        if (delta > 0) {
+            const double gx = std::ceil((hi[0] - lo[0]) * dINV), gy = std::ceil((hi[1] - lo[1]) * dINV),
+                         gz = std::ceil((hi[2] - lo[2]) * dINV);
+            if (gx * gy * gz > (double)(1 << 26)) { ctx->err = "collision grid too fine"; return bail(SDFIBM_ERR_CAPACITY); }
+            if (gx > 0 && gy > 0 && gz > 0) {
+                ctx->grid_active = true;
+                GridK& g = ctx->gk;
+                for (int a = 0; a < 3; ++a) g.low[a] = lo[a];
+                g.dINV = dINV;
+                g.nx = (int)gx; g.ny = (int)gy; g.nz = (int)gz;
+                g.nynz = g.ny * g.nz;
+                g.ncell = (int64_t)g.nx * g.ny * g.nz;
+            }
+        }
+    }
+
+    // device allocations
+    if (dalloc(&ctx->d_sk, nsolids) || dalloc(&ctx->d_st, nsolids) || dalloc(&ctx->d_plan, nsolids) ||
+        dalloc(&ctx->d_tile_prefix, nsolids + 1) || dalloc(&ctx->d_scratch, scratch) ||
+        dalloc(&ctx->d_gbitmaps, gwords) || dalloc(&ctx->d_in_cell, ctx->cap) || dalloc(&ctx->d_in_solid, ctx->cap) ||
+        dalloc(&ctx->d_cut_cell, ctx->cap) || dalloc(&ctx->d_cut_solid, ctx->cap) || dalloc(&ctx->d_cnt, 1) ||
+        dalloc(&ctx->d_ftacc, 6 * (size_t)nsolids) || dalloc(&ctx->d_ft, 6 * (size_t)nsolids) ||
+        dalloc(&ctx->d_sh_keys, (size_t)ctx->sh_mask + 1) || dalloc(&ctx->d_sh_vals, 5 * ((size_t)ctx->sh_mask + 1)) ||
+        dalloc(&ctx->d_sh_used, (size_t)ctx->sh_mask + 1) ||
+        cudaMallocHost((void**)&ctx->h_cnt, sizeof(Counters)) != cudaSuccess ||
+        cudaMallocHost((void**)&ctx->h_ft, std::max<size_t>(1, 6 * (size_t)nsolids) * sizeof(double)) != cudaSuccess) {
+        ctx->err = "device allocation failed";
+        return bail(SDFIBM_ERR_CUDA);
+    }
+    if (ctx->grid_active) {
+        if (dalloc(&ctx->d_hash, nsolids) || dalloc(&ctx->d_gcount, ctx->gk.ncell) ||
+            dalloc(&ctx->d_gstart, ctx->gk.ncell + 1) || dalloc(&ctx->d_gcursor, ctx->gk.ncell) ||
+            dalloc(&ctx->d_glist, nsolids)) {
+            ctx->err = "device allocation failed (collision grid)";
+            return bail(SDFIBM_ERR_CUDA);
+        }
+    }
+    std::vector<sdfibm_solid_state> st(nsolids);
+    for (int s = 0; s < nsolids; ++s) {
+        sdfibm_solid_state& x = st[s];
+        std::memset(&x, 0, sizeof(x));
+        for (int a = 0; a < 3; ++a) { x.pos[a] = solids[s].pos[a]; x.vel[a] = solids[s].vel[a]; x.omega[a] = solids[s].omega[a]; }
+        for (int a = 0; a < 4; ++a) x.quat[a] = solids[s].quat[a];
+        x.first_fluid_step = 1;
+        x.first_forcer_step = 1;
+    }
+    sdfibm_ctx* c = ctx;
+    auto up = [&](void* dst, const void* src, size_t bytes) {
+        return bytes ? cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+    };
+    if (up(c->d_sk, c->hk.data(), sizeof(SolidK) * nsolids) || up(c->d_st, st.data(), sizeof(sdfibm_solid_state) * nsolids) ||
+        up(c->d_tile_prefix, prefix.data(), sizeof(int32_t) * (nsolids + 1)) ||
+        cudaMemset(c->d_cnt, 0, sizeof(Counters)) != cudaSuccess ||
+        cudaMemset(c->d_sh_keys, 0xff, sizeof(int32_t) * ((size_t)c->sh_mask + 1)) != cudaSuccess ||
+        cudaMemset(c->d_sh_vals, 0, sizeof(double) * 5 * ((size_t)c->sh_mask + 1)) != cudaSuccess ||
+        up(&c->d_cnt->list_cap, &c->cap, sizeof(int64_t))) {
+        ctx->err = "upload failed";
+        return bail(SDFIBM_ERR_CUDA);
+    }
+    if (ctx->connect_smem_bytes > 48 * 1024) {
+        if (cudaFuncSetAttribute(connect_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 ctx->connect_smem_bytes) != cudaSuccess) {
+            ctx->err = "cannot reserve shared memory for the flood fill";
+            return bail(SDFIBM_ERR_CUDA);
+        }
+    }
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, classify_kernel, 256, 0);
+    ctx->classify_grid = std::max(1, occ) * ctx->num_sms;
+    occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, couple_kernel, 256, 0);
+    ctx->couple_grid = std::max(1, occ) * ctx->num_sms;
+    *out = ctx;
+    return SDFIBM_OK;
+}
+
+static int check_device_error(sdfibm_ctx* ctx) {
+    const int e = ctx->h_cnt->error;
+    if (e == DERR_NONE) return SDFIBM_OK;
+    cudaMemsetAsync(&ctx->d_cnt->error, 0, sizeof(int32_t), ctx->stream);
+    switch (e) {
+        case DERR_CAPACITY: return fail(ctx, SDFIBM_ERR_CAPACITY, "touched-cell list capacity exceeded");
+        case DERR_BBOX: return fail(ctx, SDFIBM_ERR_CAPACITY, "a 2-D shape tilted out of its reserved bounding box");
+        case DERR_FLOOD_LIMIT: return fail(ctx, SDFIBM_ERR_TIMEOUT, "flood fill did not converge within its bound");
+        case DERR_SHARED_TABLE: return fail(ctx, SDFIBM_ERR_CAPACITY, "shared-cell table full");
+        default: return fail(ctx, SDFIBM_ERR_CUDA, "device error " + std::to_string(e));
+    }
+}
+
+static int sync_counters(sdfibm_ctx* ctx) {
+    CK(cudaMemcpyAsync(ctx->h_cnt, ctx->d_cnt, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return check_device_error(ctx);
+}
+
+int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs, float* Ts,
+                         int32_t* Ct, double* FT) {
+    (void)time;
+    if (!ctx) return SDFIBM_ERR_ARG;
+    if (!U || !As || !Fs || !Ts || !Ct) return fail(ctx, SDFIBM_ERR_ARG, "null field pointer");
+    if (!(dt != 0.0)) return fail(ctx, SDFIBM_ERR_ARG, "dt must be nonzero");
+    const int64_t N = ctx->mesh.ncells;
+    const int S = ctx->S;
+    cudaStream_t st = ctx->stream;
+    int launches = 0;
+    mark_begin(ctx);
+    const void* f5[5] = {U, As, Fs, Ts, Ct};
+    bool same = ctx->interacted;
+    for (int i = 1; i < 5; ++i) same = same && f5[i] == ctx->last_fields[i];
+    if (!same || ctx->opt.dense_reset) {
+        // SolidCloud::interact zeroes the four fields over the whole mesh (solidcloud.cpp:438-441)
+        CK(cudaMemsetAsync(As, 0, sizeof(float) * N, st));
+        CK(cudaMemsetAsync(Fs, 0, sizeof(float) * 3 * N, st));
+        CK(cudaMemsetAsync(Ts, 0, sizeof(float) * N, st));
+        CK(cudaMemsetAsync(Ct, 0, sizeof(int32_t) * N, st));
+        mark(ctx, "dense_reset");
+    } else {
+        // only the previous call's cells can be nonzero
+        reset_kernel<<<ctx->num_sms * 4, 256, 0, st>>>(ctx->d_in_cell, ctx->d_cut_cell, ctx->d_cnt, N, As, Fs, Ts, Ct);
+        mark(ctx, "reset_kernel");
+        ++launches;
+    }
+    for (int i = 0; i < 5; ++i) ctx->last_fields[i] = f5[i];
+    // per-call counters (the previous list lengths stay for the reset kernel above, which already ran in order)
+    CK(cudaMemsetAsync(ctx->d_cnt, 0, offsetof(Counters, error), st));
+    CK(cudaMemsetAsync(&ctx->d_cnt->exact_rechecks, 0, 2 * sizeof(unsigned long long), st));
+    if (S > 0) {
+        CK(cudaMemsetAsync(ctx->d_ftacc, 0, sizeof(double) * 6 * S, st));
+        plan_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->mesh, ctx->d_sk, ctx->d_st, ctx->d_plan, S, ctx->d_cnt);
+        mark(ctx, "plan_kernel");
+        classify_kernel<<<ctx->classify_grid, 256, 0, st>>>(ctx->mesh, ctx->d_sk, ctx->d_st, ctx->d_plan,
+                                                            ctx->d_tile_prefix, S, ctx->total_tiles, ctx->d_scratch,
+                                                            ctx->d_cnt);
+        mark(ctx, "classify_kernel");
+        connect_kernel<<<S, 512, ctx->connect_smem_bytes, st>>>(ctx->mesh, ctx->d_sk, ctx->d_plan, ctx->d_scratch,
+                                                                ctx->d_gbitmaps, ctx->d_in_cell, ctx->d_in_solid,
+                                                                ctx->d_cut_cell, ctx->d_cut_solid, ctx->cap, ctx->cap,
+                                                                ctx->d_cnt, ctx->connect_smem_bytes / 4);
+        mark(ctx, "connect_kernel");
+        claim_kernel<<<ctx->num_sms * 4, 256, 0, st>>>(ctx->d_in_cell, ctx->d_in_solid, ctx->d_cut_cell,
+                                                        ctx->d_cut_solid, Ct, ctx->d_cnt, N);
+        mark(ctx, "claim_kernel");
+        CoupleArgs A;
+        A.m = ctx->mesh; A.sk = ctx->d_sk; A.st = ctx->d_st; A.plan = ctx->d_plan;
+        A.in_cell = ctx->d_in_cell; A.in_solid = ctx->d_in_solid; A.cut_cell = ctx->d_cut_cell;
+        A.cut_solid = ctx->d_cut_solid; A.U = U; A.As = As; A.Fs = Fs; A.Ts = Ts; A.Ct = Ct;
+        A.ftacc = ctx->d_ftacc; A.cnt = ctx->d_cnt; A.dtINV = 1.0 / dt;
+        A.method = ctx->opt.fraction_method; A.subsample_n = ctx->opt.subsample_n;
+        A.exact_forcing = ctx->opt.exact_forcing;
+        A.sh_keys = ctx->d_sh_keys; A.sh_vals = ctx->d_sh_vals; A.sh_used = ctx->d_sh_used; A.sh_mask = ctx->sh_mask;
+        couple_kernel<<<ctx->couple_grid, 256, 0, st>>>(A);
+        mark(ctx, "couple_kernel");
+        finalize_kernel<<<ctx->num_sms * 4, 256, 0, st>>>(ctx->d_in_cell, ctx->d_in_solid, ctx->d_cut_cell,
+                                                           ctx->d_cut_solid, As, Ts, Fs, Ct, ctx->d_cnt, N,
+                                                           ctx->d_sh_keys, ctx->d_sh_vals, ctx->d_sh_used, ctx->sh_mask);
+        mark(ctx, "finalize_kernel");
+        ft_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->d_ftacc, ctx->d_ft, S, ctx->opt.rho_f);
+        ft_to_state_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->d_ft, ctx->d_st, S);
+        mark(ctx, "ft_kernel");
+        launches += 8;
+    }
+    CK(cudaGetLastError());
+    ctx->launches_last = launches;
+    ctx->interacted = true;
+    if (FT) {
+        if (S > 0) CK(cudaMemcpyAsync(ctx->h_ft, ctx->d_ft, sizeof(double) * 6 * S, cudaMemcpyDeviceToHost, st));
+        int rc = sync_counters(ctx);
+        if (rc) return rc;
+        std::memcpy(FT, ctx->h_ft, sizeof(double) * 6 * S);
+    }
+    return SDFIBM_OK;
+}
+
+int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs,
+                              float* Ts, int32_t* Ct, double* FT) {
+    if (!ctx) return SDFIBM_ERR_ARG;
+    if (!U || !As || !Fs || !Ts || !Ct) return fail(ctx, SDFIBM_ERR_ARG, "null field pointer");
+    const int64_t N = ctx->mesh.ncells;
+    cudaStream_t st = ctx->stream;
+    if (!ctx->d_U) {
+        if (dalloc(&ctx->d_U, 3 * N) || dalloc(&ctx->d_As, N) || dalloc(&ctx->d_Fs, 3 * N) || dalloc(&ctx->d_Ts, N) ||
+            dalloc(&ctx->d_Ct, N))
+            return fail(ctx, SDFIBM_ERR_CUDA, "staging allocation failed");
+    }
+    CK(cudaMemcpyAsync(ctx->d_U, U, sizeof(float) * 3 * N, cudaMemcpyHostToDevice, st));
+    std::vector<double> ft(6 * (size_t)std::max(1, ctx->S));
+    int rc = sdfibm_cuda_interact(ctx, time, dt, ctx->d_U, ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, nullptr);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(As, ctx->d_As, sizeof(float) * N, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(Fs, ctx->d_Fs, sizeof(float) * 3 * N, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(Ts, ctx->d_Ts, sizeof(float) * N, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(Ct, ctx->d_Ct, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, st));
+    if (ctx->S > 0) CK(cudaMemcpyAsync(ctx->h_ft, ctx->d_ft, sizeof(double) * 6 * ctx->S, cudaMemcpyDeviceToHost, st));
+    rc = sync_counters(ctx);
+    if (rc) return rc;
+    if (FT) std::memcpy(FT, ctx->h_ft, sizeof(double) * 6 * ctx->S);
+    return SDFIBM_OK;
+}
+
+int sdfibm_cuda_evolve(sdfibm_ctx* ctx, double time, double dt) {
+    if (!ctx) return SDFIBM_ERR_ARG;
+    const int S = ctx->S;
+    if (S == 0) return SDFIBM_OK;
+    cudaStream_t st = ctx->stream;
+    const int nsub = ctx->nsub;
+    const double dt_sub = dt / nsub;
+    const D3 g{ctx->opt.gravity[0], ctx->opt.gravity[1], ctx->opt.gravity[2]};
+    const int B = 128, G = (S + B - 1) / B;
+    if (!ctx->grid_active) {
+        evolve_independent_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, nsub, time, dt_sub, ctx->opt.rho_f, g);
+    } else {
+        const GridK& gk = ctx->gk;
+        for (int it = 0; it < nsub; ++it) {
+            CK(cudaMemsetAsync(ctx->d_gcount, 0, sizeof(int32_t) * gk.ncell, st));
+            evolve_pre_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, time, ctx->opt.rho_f, g, gk, ctx->d_hash,
+                                               ctx->d_gcount);
+            grid_scan_kernel<<<1, 1024, 0, st>>>(ctx->d_gcount, ctx->d_gstart, ctx->d_gcursor, gk.ncell);
+            grid_scatter_kernel<<<G, B, 0, st>>>(ctx->d_hash, ctx->d_gcursor, ctx->d_glist, S, gk.ncell);
+            collide_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, gk, ctx->d_hash, ctx->d_gstart, ctx->d_glist,
+                                            ctx->opt.collision_mode);
+            move_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, time, dt_sub);
+        }
+        store_old_kernel<<<G, B, 0, st>>>(ctx->d_st, S);
+    }
+    CK(cudaGetLastError());
+    return SDFIBM_OK;
+}
+
+int sdfibm_cuda_fix_internal(sdfibm_ctx* ctx, const int32_t* Ct, float* U) {
+    if (!ctx) return SDFIBM_ERR_ARG;
+    if (!Ct || !U) return fail(ctx, SDFIBM_ERR_ARG, "null field pointer");
+    if (!ctx->interacted) return fail(ctx, SDFIBM_ERR_STATE, "fix_internal needs a previous interact");
+    fix_internal_kernel<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(ctx->mesh, ctx->d_st, ctx->d_in_cell,
+                                                                    ctx->d_in_solid, Ct, U, ctx->d_cnt);
+    CK(cudaGetLastError());
+    return SDFIBM_OK;
+}
+
+int sdfibm_cuda_get_solids(sdfibm_ctx* ctx, sdfibm_solid_state* out, int32_t n) {
+    if (!ctx) return SDFIBM_ERR_ARG;
+    if (!out || n != ctx->S) return fail(ctx, SDFIBM_ERR_ARG, "state array size must equal the solid count");
+    if (n == 0) return SDFIBM_OK;
+    CK(cudaMemcpyAsync(out, ctx->d_st, sizeof(sdfibm_solid_state) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    return sync_counters(ctx);
+}
+
+int sdfibm_cuda_set_solids(sdfibm_ctx* ctx, const sdfibm_solid_state* in, int32_t n) {
+    if (!ctx) return SDFIBM_ERR_ARG;
+    if (!in || n != ctx->S) return fail(ctx, SDFIBM_ERR_ARG, "state array size must equal the solid count");
+    if (n == 0) return SDFIBM_OK;
+    CK(cudaMemcpyAsync(ctx->d_st, in, sizeof(sdfibm_solid_state) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SDFIBM_OK;
+}
+
+int sdfibm_cuda_touched(sdfibm_ctx* ctx, int32_t solid, int64_t* cells, int8_t* types, int64_t capacity, int64_t* n) {
+    if (!ctx) return SDFIBM_ERR_ARG;
+    if (!n || solid < 0 || solid >= ctx->S) return fail(ctx, SDFIBM_ERR_ARG, "bad solid index");
+    if (!ctx->interacted) return fail(ctx, SDFIBM_ERR_STATE, "no interact yet");
+    int rc = sync_counters(ctx);
+    if (rc) return rc;
+    const int nin = clamp_len(ctx->h_cnt->n_inside, ctx->cap), ncut = clamp_len(ctx->h_cnt->n_cut, ctx->cap);
+    std::vector<int32_t> ic(nin), is(nin), cc(ncut), cs(ncut);
+    if (nin) {
+        CK(cudaMemcpy(ic.data(), ctx->d_in_cell, sizeof(int32_t) * nin, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(is.data(), ctx->d_in_solid, sizeof(int32_t) * nin, cudaMemcpyDeviceToHost));
+    }
+    if (ncut) {
+        CK(cudaMemcpy(cc.data(), ctx->d_cut_cell, sizeof(int32_t) * ncut, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(cs.data(), ctx->d_cut_solid, sizeof(int32_t) * ncut, cudaMemcpyDeviceToHost));
+    }
+    std::vector<int64_t> byType[4];
+    for (int i = 0; i < nin; ++i)
+        if ((is[i] & LIST_SOLID_MASK) == solid) byType[1].push_back(ic[i]);
+    for (int i = 0; i < ncut; ++i)
+        if ((cs[i] & LIST_SOLID_MASK) == solid) {
+            const int t = list_type(cs[i]);
+            if (t < 1 || t > 3) return fail(ctx, SDFIBM_ERR_STATE, "corrupt touched-cell list entry");
+            byType[t].push_back(cc[i]);
+        }
+    int64_t k = 0;
+    for (int t = 1; t <= 3; ++t) {
+        std::sort(byType[t].begin(), byType[t].end());
+        for (int64_t c : byType[t]) {
+            if (k < capacity && cells) { cells[k] = c; if (types) types[k] = (int8_t)t; }
+            ++k;
+        }
+    }
+    *n = k;
+    return SDFIBM_OK;
+}
+
+int sdfibm_cuda_kernel_times(sdfibm_ctx* ctx, const char** names, double* ms, int32_t capacity, int32_t* n) {
+    if (!ctx || !n) return SDFIBM_ERR_ARG;
+    *n = 0;
+    if (!ctx->opt.timing) return fail(ctx, SDFIBM_ERR_STATE, "kernel timing is off (options.timing)");
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < ctx->nev && i < capacity; ++i) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, ctx->ev[i], ctx->ev[i + 1]));
+        if (names) names[i] = ctx->ev_name[i];
+        if (ms) ms[i] = t;
+        *n = i + 1;
+    }
+    return SDFIBM_OK;
+}
+
+int sdfibm_cuda_stats(sdfibm_ctx* ctx, int64_t* out, int32_t n) {
+    if (!ctx || !out) return SDFIBM_ERR_ARG;
+    int rc = sync_counters(ctx);
+    if (rc) return rc;
+    const Counters& c = *ctx->h_cnt;
+    const int64_t v[6] = {(int64_t)c.n_inside + c.n_cut, (int64_t)c.n_cut, (int64_t)c.bbox_cells,
+                          (int64_t)c.exact_rechecks, (int64_t)ctx->total_tiles, (int64_t)ctx->launches_last};
+    for (int i = 0; i < n && i < 6; ++i) out[i] = v[i];
+    return SDFIBM_OK;
+}
+
+void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
+    if (!ctx) return;
+    cudaStreamSynchronize(ctx->stream);
+    void* dev[] = {ctx->d_sk, ctx->d_st, ctx->d_plan, ctx->d_tile_prefix, ctx->d_scratch, ctx->d_gbitmaps,
+                   ctx->d_in_cell, ctx->d_in_solid, ctx->d_cut_cell, ctx->d_cut_solid, ctx->d_cnt, ctx->d_ftacc,
+                   ctx->d_ft, ctx->d_hash, ctx->d_gcount, ctx->d_gstart, ctx->d_gcursor, ctx->d_glist, ctx->d_U,
+                   ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, ctx->d_sh_keys, ctx->d_sh_vals, ctx->d_sh_used};
+    for (void* p : dev)
+        if (p) cudaFree(p);
+    if (ctx->ev_ready)
+        for (int i = 0; i <= sdfibm_ctx::MAXEV; ++i) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->h_cnt) cudaFreeHost(ctx->h_cnt);
+    if (ctx->h_ft) cudaFreeHost(ctx->h_ft);
+    delete ctx;
+}
+
+// sizes of the ABI structs as compiled, for binding checks
+int64_t sdfibm_abi_sizeof(int which) {
+    switch (which) {
+        case 0: return sizeof(sdfibm_mesh_desc);
+        case 1: return sizeof(sdfibm_shape_desc);
+        case 2: return sizeof(sdfibm_solid_desc);
+        case 3: return sizeof(sdfibm_solid_state);
+        case 4: return sizeof(sdfibm_options);
+        default: return -1;
+    }
+}
+
+}  // extern "C"

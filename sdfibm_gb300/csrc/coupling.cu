@@ -1,0 +1,826 @@
+// Coupling kernels: the GB300 replacement of SolidCloud::interact (src/solidcloud.cpp:361-464) and
+// SolidCloud::fixInternal (src/solidcloud.cpp:288-301).
+//
+// Pipeline of one interact (all on one stream, no host round trip until FT is read back):
+//   reset     zero As/Fs/Ts/Ct at the cells the previous call touched (sparse form of solidcloud.cpp:438-441)
+//   plan      per solid: bbox origin in cell indices, FP32 world->local matrix, nearest cell (meshSearch)
+//   classify  persistent CTAs pulling (solid, cell-tile) items from an atomic counter; each tile evaluates the
+//             inside test once per vertex (FP32 with a guard band, FP64 re-check inside the band) and writes one
+//             class byte per cell: 0 no inside vertex, 1 all inside, 2 centre inside, 3 centre outside
+//             (CellEnumerator::_next, cellenumerator.cpp:6-34)
+//   connect   one CTA per solid: bit-parallel flood fill from the seed over cells with an inside vertex
+//             (the BFS of CellEnumerator::intersect with its seed fallback, cellenumerator.cpp:47-78), then
+//             appends the reached cells to the ALL_INSIDE list or the cut-cell list in ascending cell order
+//   couple    persistent CTAs over 256-entry chunks of both lists: alpha (1, REF-GEO, SUBSAMPLE), direct forcing,
+//             field accumulation with atomics, warp then FP64-atomic reduction of force and torque per solid
+//   finalize  Ct key -> Ct value (last solid wins, as the serial loop), As = min(As,1) (checkAlpha), FT = rho_f*sum
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+
+namespace sdfibm_dev {
+
+
+__device__ inline void set_error(Counters* cnt, int32_t code) { atomicCAS(&cnt->error, 0, code); }
+
+// ---- geometry helpers (closed form of the uniform mesh, identical to the oracle's UniformMesh) ----------------------
+__device__ inline double mesh_coord(const MeshK& m, int a, int64_t i) { return m.o[a] + (double)i * m.h[a]; }
+__device__ inline double mesh_centre(const MeshK& m, int a, int64_t i) { return m.o[a] + ((double)i + 0.5) * m.h[a]; }
+__device__ inline D3 mesh_point(const MeshK& m, int64_t i, int64_t j, int64_t k) {
+    return D3{mesh_coord(m, 0, i), mesh_coord(m, 1, j), mesh_coord(m, 2, k)};
+}
+__device__ inline D3 mesh_C(const MeshK& m, int64_t i, int64_t j, int64_t k) {
+    return D3{mesh_centre(m, 0, i), mesh_centre(m, 1, j), mesh_centre(m, 2, k)};
+}
+
+__device__ inline Q4 state_quat(const sdfibm_solid_state& s) { return Q4{s.quat[0], D3{s.quat[1], s.quat[2], s.quat[3]}}; }
+__device__ inline D3 state_pos(const sdfibm_solid_state& s) { return D3{s.pos[0], s.pos[1], s.pos[2]}; }
+
+// ---- plan ---------------------------------------------------------------------------------------------------------
+__global__ void plan_kernel(MeshK m, const SolidK* __restrict__ sk, const sdfibm_solid_state* __restrict__ st,
+                            SolidPlan* __restrict__ plan, int S, Counters* cnt) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const SolidK& k = sk[s];
+    const Q4 q = state_quat(st[s]);
+    const D3 x = state_pos(st[s]);
+    SolidPlan p;
+    // |q|^2 R(q)^T: the linear map of world2local (quaternion::R of OpenFOAM, transposed)
+    {
+        const double w2 = q.w * q.w, x2 = q.v.x * q.v.x, y2 = q.v.y * q.v.y, z2 = q.v.z * q.v.z;
+        const double txy = 2 * q.v.x * q.v.y, twz = 2 * q.w * q.v.z, txz = 2 * q.v.x * q.v.z;
+        const double twy = 2 * q.w * q.v.y, tyz = 2 * q.v.y * q.v.z, twx = 2 * q.w * q.v.x;
+        double R[9] = {w2 + x2 - y2 - z2, txy - twz, txz + twy, txy + twz, w2 - x2 + y2 - z2,
+                       tyz - twx, txz - twy, tyz + twx, w2 - x2 - y2 + z2};
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) p.M[3 * r + c] = (float)R[3 * c + r];
+    }
+    p.err = 0;
+    const int32_t n[3] = {m.nx, m.ny, m.nz};
+    if (k.infinite) {
+        p.lo[0] = p.lo[1] = p.lo[2] = 0;
+    } else {
+        D3 cl{-k.shape.com[0], -k.shape.com[1], -k.shape.com[2]};
+        if (k.shape.type == SDFIBM_SHAPE_ELLIPSOID) cl = D3{0, 0, 0};
+        if (k.shape.prism) cl.z = 0.0;
+        const D3 cw = x + qtransform(q, cl);
+        const double r = k.shape.bound_r * (1.0 + 1e-9) + 1e-12;
+        double rad[3] = {r, r, r};
+        if (k.shape.prism) {
+            // the inside region is a prism along the local z axis a; clip it to the mesh slab in z
+            const double qq = q.w * q.w + magSqr(q.v);
+            const D3 a = qtransform(q, D3{0, 0, 1}) / qq;
+            const double sxy = sqrt(a.x * a.x + a.y * a.y), az = fabs(a.z);
+            if (az < 0.3 && (k.ext[0] < n[0] + 2 || k.ext[1] < n[1] + 2)) p.err = DERR_BBOX;
+            const double zlo = m.o[2], zhi = mesh_coord(m, 2, m.nz);
+            const double zspan = dmax(fabs(zhi - cw.z), fabs(zlo - cw.z));
+            const double rxy = (sxy > 0) ? r + (zspan + r * sxy) / dmax(az, 0.3) * sxy : r;
+            rad[0] = rad[1] = rxy * (1.0 + 1e-9);
+        }
+        const double c3[3] = {cw.x, cw.y, cw.z};
+        for (int a = 0; a < 3; ++a) {
+            if (k.shape.prism && a == 2) { p.lo[2] = 0; continue; }
+            if (k.ext[a] >= n[a] + 2) { p.lo[a] = -1; continue; }  // the window spans the whole axis
+            const double lo = floor((c3[a] - rad[a] - m.o[a]) / m.h[a]) - 1;
+            const double hi = floor((c3[a] + rad[a] - m.o[a]) / m.h[a]) + 1;
+            // only cells 0..n-1 matter: start the window no lower than -1 (this also keeps the int conversion
+            // defined for solids far outside the mesh)
+            const double lo_c = dmin(dmax(lo, -1.0), 1e9), hi_c = dmin(hi, (double)n[a]);
+            p.lo[a] = (int32_t)lo_c;
+            if (hi_c >= lo_c && hi_c - lo_c + 1 > (double)k.ext[a]) p.err = DERR_BBOX;
+        }
+    }
+    if (p.err) set_error(cnt, p.err);
+    // meshSearch::findNearestCell: nearest cell centre, ties to the lowest cell label
+    {
+        const double pc[3] = {x.x, x.y, x.z};
+        int64_t lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+            double t = floor((pc[a] - m.o[a]) / m.h[a]);
+            int64_t e = t < 0 ? 0 : (t > (double)(n[a] - 1) ? n[a] - 1 : (int64_t)t);
+            lo[a] = e > 0 ? e - 1 : 0;
+            hi[a] = e + 1 < n[a] ? e + 1 : n[a] - 1;
+        }
+        int64_t best = -1;
+        double bd = 0;
+        for (int64_t kk = lo[2]; kk <= hi[2]; ++kk)
+            for (int64_t jj = lo[1]; jj <= hi[1]; ++jj)
+                for (int64_t ii = lo[0]; ii <= hi[0]; ++ii) {
+                    const int64_t c = ii + (int64_t)m.nx * (jj + (int64_t)m.ny * kk);
+                    const double d = magSqr(mesh_C(m, ii, jj, kk) - x);
+                    if (best < 0 || d < bd || (d == bd && c < best)) { bd = d; best = c; }
+                }
+        p.seed = best;
+    }
+    p.min_cand = ~0ull;
+    p.n_inside = p.n_cut = 0;
+    plan[s] = p;
+}
+
+// ---- inside test of one world point given as integer lattice offsets ------------------------------------------------
+// base: FP64 (point(I0,J0,K0) - x_s) of the tile; off: FP32 offset of the point from that lattice point.
+// Exact fallback evaluates the point with the mesh formula in FP64, as the oracle does.
+struct TileFrame {
+    float bx, by, bz;  // FP32 of the FP64 base vector
+    float babs;        // |base|_1
+    float e64;         // bound of the FP64 reference's own rounding of point coordinates (large meshes offsets)
+};
+__device__ inline TileFrame make_frame(const D3& b, const D3& p0, const D3& x) {
+    TileFrame tf;
+    tf.bx = (float)b.x; tf.by = (float)b.y; tf.bz = (float)b.z;
+    tf.babs = fabsf(tf.bx) + fabsf(tf.by) + fabsf(tf.bz);
+    tf.e64 = (float)(1e-15 * (fabs(p0.x) + fabs(p0.y) + fabs(p0.z) + fabs(x.x) + fabs(x.y) + fabs(x.z)));
+    return tf;
+}
+
+__device__ inline int classify_point(const ShapeK& sh, const float* M, const TileFrame& tf, float ox, float oy,
+                                     float oz, const D3& p64_exact_world, const D3& x, const Q4& q,
+                                     unsigned long long* rechecks) {
+    const float dx = tf.bx + ox, dy = tf.by + oy, dz = tf.bz + oz;
+    const float lx = __fmaf_rn(M[0], dx, __fmaf_rn(M[1], dy, M[2] * dz));
+    const float ly = __fmaf_rn(M[3], dx, __fmaf_rn(M[4], dy, M[5] * dz));
+    const float lz = __fmaf_rn(M[6], dx, __fmaf_rn(M[7], dy, M[8] * dz));
+    const float dabs = fabsf(dx) + fabsf(dy) + fabsf(dz);
+    const float E = 4.f * U32 * (tf.babs + fabsf(ox) + fabsf(oy) + fabsf(oz) + 2.f * dabs) + tf.e64 + 1e-30f;
+    int r = inside32(sh, lx, ly, lz, E);
+    if (r == 2) {
+        atomicAdd(rechecks, 1ull);
+        r = inside64(sh, world2local(p64_exact_world, x, q)) ? 1 : 0;
+    }
+    return r;
+}
+
+// ---- classify -------------------------------------------------------------------------------------------------------
+constexpr int CLS_THREADS = 256;
+constexpr int MAX_TILE_VERTS = 33 * 17 * 9;  // largest tile: 32 x 16 x 8 cells
+
+__device__ inline int find_solid(const int32_t* prefix, int S, int item) {
+    int lo = 0, hi = S;  // prefix[lo] <= item < prefix[hi]
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (prefix[mid] <= item) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(CLS_THREADS) classify_kernel(MeshK m, const SolidK* __restrict__ sk,
+                                                               const sdfibm_solid_state* __restrict__ st,
+                                                               SolidPlan* __restrict__ plan,
+                                                               const int32_t* __restrict__ tile_prefix, int S,
+                                                               int total_tiles, uint8_t* __restrict__ scratch,
+                                                               Counters* cnt) {
+    __shared__ uint8_t vin[MAX_TILE_VERTS];
+    __shared__ int s_item;
+    __shared__ unsigned long long s_min;
+    __shared__ unsigned long long s_rechecks;
+    __shared__ unsigned int s_valid;
+    __shared__ ShapeK s_shape;
+    __shared__ float s_M[9];
+    __shared__ TileFrame s_tf;
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) {
+            s_item = atomicAdd(&cnt->classify_next, 1);
+            s_min = ~0ull;
+            s_rechecks = 0;
+            s_valid = 0;
+        }
+        __syncthreads();
+        const int item = s_item;
+        if (item >= total_tiles) break;
+        const int s = find_solid(tile_prefix, S, item);
+        const SolidK& k = sk[s];
+        const SolidPlan& pl = plan[s];
+        const int t = item - k.tile_base;
+        const int tx = t % k.ntile[0], ty = (t / k.ntile[0]) % k.ntile[1], tz = t / (k.ntile[0] * k.ntile[1]);
+        const int cx = min(k.tdim[0], k.ext[0] - tx * k.tdim[0]);
+        const int cy = min(k.tdim[1], k.ext[1] - ty * k.tdim[1]);
+        const int cz = min(k.tdim[2], k.ext[2] - tz * k.tdim[2]);
+        const int64_t I0 = (int64_t)pl.lo[0] + tx * k.tdim[0];
+        const int64_t J0 = (int64_t)pl.lo[1] + ty * k.tdim[1];
+        const int64_t K0 = (int64_t)pl.lo[2] + tz * k.tdim[2];
+        const Q4 q = state_quat(st[s]);
+        const D3 x = state_pos(st[s]);
+        if (tid == 0) {
+            s_shape = k.shape;
+            for (int r = 0; r < 9; ++r) s_M[r] = pl.M[r];
+            const D3 p0 = mesh_point(m, I0, J0, K0);
+            s_tf = make_frame(p0 - x, p0, x);
+        }
+        __syncthreads();
+        const int vx = cx + 1, vy = cy + 1, vz = cz + 1, nv = vx * vy * vz;
+        const bool tile_in_mesh = !(I0 + cx <= 0 || J0 + cy <= 0 || K0 + cz <= 0 || I0 >= m.nx || J0 >= m.ny || K0 >= m.nz);
+        if (tile_in_mesh && !pl.err) {
+            for (int v = tid; v < nv; v += CLS_THREADS) {
+                const int a = v % vx, b = (v / vx) % vy, c = v / (vx * vy);
+                const int64_t I = I0 + a, J = J0 + b, K = K0 + c;
+                uint8_t r = 0;
+                if (I >= 0 && J >= 0 && K >= 0 && I <= m.nx && J <= m.ny && K <= m.nz) {
+                    const float ox = (float)a * m.h32[0], oy = (float)b * m.h32[1], oz = (float)c * m.h32[2];
+                    r = (uint8_t)classify_point(s_shape, s_M, s_tf, ox, oy, oz, mesh_point(m, I, J, K), x, q,
+                                                &s_rechecks);
+                }
+                vin[v] = r;
+            }
+        }
+        __syncthreads();
+        const int nc = cx * cy * cz;
+        uint8_t* out = scratch + k.scratch_off;
+        unsigned int local_valid = 0;
+        for (int e = tid; e < nc; e += CLS_THREADS) {
+            const int a = e % cx, b = (e / cx) % cy, c = e / (cx * cy);
+            const int64_t I = I0 + a, J = J0 + b, K = K0 + c;
+            uint8_t cls = 0;
+            if (tile_in_mesh && !pl.err && I >= 0 && J >= 0 && K >= 0 && I < m.nx && J < m.ny && K < m.nz) {
+                ++local_valid;
+                int cntv = 0;
+#pragma unroll
+                for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+                    for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+                        for (int dx = 0; dx < 2; ++dx) cntv += vin[(a + dx) + vx * ((b + dy) + vy * (c + dz))];
+                if (cntv == 8) {
+                    cls = 1;
+                } else if (cntv > 0) {
+                    const float ox = ((float)a + 0.5f) * m.h32[0], oy = ((float)b + 0.5f) * m.h32[1],
+                                oz = ((float)c + 0.5f) * m.h32[2];
+                    const int ci = classify_point(s_shape, s_M, s_tf, ox, oy, oz, mesh_C(m, I, J, K), x, q,
+                                                  &s_rechecks);
+                    cls = ci ? 2 : 3;
+                }
+                if (cls) {
+                    const unsigned long long gidx = (unsigned long long)(I + (int64_t)m.nx * (J + (int64_t)m.ny * K));
+                    atomicMin(&s_min, gidx);
+                }
+            }
+            const int64_t li = (int64_t)(tx * k.tdim[0] + a) +
+                               (int64_t)k.ext[0] * ((ty * k.tdim[1] + b) + (int64_t)k.ext[1] * (tz * k.tdim[2] + c));
+            out[li] = cls;
+        }
+        if (local_valid) atomicAdd(&s_valid, local_valid);
+        __syncthreads();
+        if (tid == 0) {
+            if (s_min != ~0ull) atomicMin(&plan[s].min_cand, s_min);
+            if (s_rechecks) atomicAdd(&cnt->exact_rechecks, s_rechecks);
+            if (s_valid) atomicAdd(&cnt->bbox_cells, (unsigned long long)s_valid);
+        }
+        __syncthreads();
+    }
+}
+
+// ---- connect: bit-parallel flood fill --------------------------------------------------------------------------------
+constexpr int CON_THREADS = 512;
+
+// fill upward (towards higher bits) inside runs of c starting from seeds s (s subset of c)
+__device__ inline uint32_t fill_up(uint32_t c, uint32_t s) { return (((c + s) ^ c) & c) | s; }
+__device__ inline uint32_t fill_down(uint32_t c, uint32_t s) { return __brev(fill_up(__brev(c), __brev(s))); }
+
+__device__ inline int block_excl_scan(int v, int* warp_sums, int& total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int w = lane < nw ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < nw) warp_sums[lane] = w;  // inclusive
+    }
+    __syncthreads();
+    total = warp_sums[nw - 1];
+    const int before = (wid > 0 ? warp_sums[wid - 1] : 0) + x - v;
+    __syncthreads();
+    return before;
+}
+
+__global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const SolidK* __restrict__ sk,
+                                                              SolidPlan* __restrict__ plan,
+                                                              const uint8_t* __restrict__ scratch,
+                                                              uint32_t* __restrict__ gbitmaps,
+                                                              int32_t* __restrict__ in_cell, int32_t* __restrict__ in_solid,
+                                                              int32_t* __restrict__ cut_cell, int32_t* __restrict__ cut_solid,
+                                                              int64_t cap_in, int64_t cap_cut, Counters* cnt,
+                                                              int smem_words) {
+    extern __shared__ uint32_t dsm[];
+    __shared__ int s_seed;  // local cell index of the seed, -1: none
+    __shared__ int warp_sums[32];
+    __shared__ int s_base_in, s_base_cut;
+    const int s = blockIdx.x;
+    const int tid = threadIdx.x;
+    const SolidK& k = sk[s];
+    SolidPlan& pl = plan[s];
+    const int ex = k.ext[0], ey = k.ext[1], ez = k.ext[2];
+    const int W = (ex + 31) >> 5;
+    const int rows = ey * ez;
+    const int nwords = rows * W;
+    uint32_t* C = k.bitmap_global ? gbitmaps + k.bitmap_off : dsm;
+    uint32_t* R = C + nwords;
+    const uint8_t* cls = scratch + k.scratch_off;
+    if (pl.err) {
+        if (tid == 0) { pl.n_inside = 0; pl.n_cut = 0; }
+        return;
+    }
+    // seed: nearest cell when it has an inside vertex, else the lowest-label cell that has one
+    if (tid == 0) {
+        int sl = -1;
+        const int64_t seed = pl.seed;
+        const int64_t si = seed % m.nx, sj = (seed / m.nx) % m.ny, sk2 = seed / ((int64_t)m.nx * m.ny);
+        const int64_t a = si - pl.lo[0], b = sj - pl.lo[1], c = sk2 - pl.lo[2];
+        if (a >= 0 && b >= 0 && c >= 0 && a < ex && b < ey && c < ez) {
+            const int li = (int)(a + (int64_t)ex * (b + (int64_t)ey * c));
+            if (cls[li]) sl = li;
+        }
+        if (sl < 0 && pl.min_cand != ~0ull) {
+            const int64_t g = (int64_t)pl.min_cand;
+            const int64_t gi = g % m.nx, gj = (g / m.nx) % m.ny, gk = g / ((int64_t)m.nx * m.ny);
+            sl = (int)((gi - pl.lo[0]) + (int64_t)ex * ((gj - pl.lo[1]) + (int64_t)ey * (gk - pl.lo[2])));
+        }
+        if (sl >= ex * ey * ez) sl = -1;
+        s_seed = sl;
+    }
+    __syncthreads();
+    if (s_seed < 0) {
+        if (tid == 0) { pl.n_inside = 0; pl.n_cut = 0; }
+        return;
+    }
+    // candidate and reached bitmaps
+    for (int w = tid; w < nwords; w += CON_THREADS) {
+        const int row = w / W, wi = w - row * W;
+        const uint8_t* rp = cls + (int64_t)row * ex;
+        uint32_t bits = 0;
+        const int x0 = wi << 5, x1 = min(ex, x0 + 32);
+        for (int xx = x0; xx < x1; ++xx) bits |= (rp[xx] ? 1u : 0u) << (xx - x0);
+        C[w] = bits;
+        R[w] = 0;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const int sx = s_seed % ex, srow = s_seed / ex;
+        R[srow * W + (sx >> 5)] |= 1u << (sx & 31);
+    }
+    __syncthreads();
+    // directional sweeps until nothing changes
+    const int max_rounds = 8 + 2 * (ex + ey + ez);
+    int round = 0;
+    for (;; ++round) {
+        int changed = 0;
+        // x: carry fill along each row
+        for (int row = tid; row < rows; row += CON_THREADS) {
+            uint32_t* r = R + row * W;
+            const uint32_t* c = C + row * W;
+            uint32_t carry = 0;
+            for (int w = 0; w < W; ++w) {
+                const uint32_t seeds = (r[w] | (carry & 1u)) & c[w];
+                const uint32_t f = fill_up(c[w], seeds);
+                if (f != r[w]) { changed = 1; r[w] = f; }
+                carry = f >> 31;
+            }
+            carry = 0;
+            for (int w = W - 1; w >= 0; --w) {
+                const uint32_t seeds = (r[w] | (carry << 31)) & c[w];
+                const uint32_t f = fill_down(c[w], seeds);
+                if (f != r[w]) { changed = 1; r[w] = f; }
+                carry = f & 1u;
+            }
+        }
+        __syncthreads();
+        // y: forward and backward scans along j for every (k, word)
+        for (int col = tid; col < ez * W; col += CON_THREADS) {
+            const int kk = col / W, w = col - kk * W;
+            uint32_t* r = R + (kk * ey) * W + w;
+            const uint32_t* c = C + (kk * ey) * W + w;
+            for (int j = 1; j < ey; ++j) {
+                const uint32_t f = r[j * W] | (r[(j - 1) * W] & c[j * W]);
+                if (f != r[j * W]) { changed = 1; r[j * W] = f; }
+            }
+            for (int j = ey - 2; j >= 0; --j) {
+                const uint32_t f = r[j * W] | (r[(j + 1) * W] & c[j * W]);
+                if (f != r[j * W]) { changed = 1; r[j * W] = f; }
+            }
+        }
+        __syncthreads();
+        // z: forward and backward scans along k for every (j, word)
+        if (ez > 1) {
+            for (int col = tid; col < ey * W; col += CON_THREADS) {
+                const int jj = col / W, w = col - jj * W;
+                uint32_t* r = R + jj * W + w;
+                const uint32_t* c = C + jj * W + w;
+                const int stride = ey * W;
+                for (int kk = 1; kk < ez; ++kk) {
+                    const uint32_t f = r[kk * stride] | (r[(kk - 1) * stride] & c[kk * stride]);
+                    if (f != r[kk * stride]) { changed = 1; r[kk * stride] = f; }
+                }
+                for (int kk = ez - 2; kk >= 0; --kk) {
+                    const uint32_t f = r[kk * stride] | (r[(kk + 1) * stride] & c[kk * stride]);
+                    if (f != r[kk * stride]) { changed = 1; r[kk * stride] = f; }
+                }
+            }
+        }
+        changed = __syncthreads_or(changed);
+        if (!changed) break;
+        if (round >= max_rounds) {
+            if (tid == 0) set_error(cnt, DERR_FLOOD_LIMIT);
+            break;
+        }
+    }
+    // emit the reached cells in ascending label order: thread t owns rows [t*rpt, (t+1)*rpt)
+    const int rpt = (rows + CON_THREADS - 1) / CON_THREADS;
+    const int r0 = min(rows, tid * rpt), r1 = min(rows, r0 + rpt);
+    int nin = 0, ncut = 0;
+    for (int row = r0; row < r1; ++row)
+        for (int w = 0; w < W; ++w) {
+            uint32_t bits = R[row * W + w];
+            while (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1;
+                const uint8_t cc = cls[(int64_t)row * ex + (w << 5) + b];
+                if (cc == 1) ++nin; else ++ncut;
+            }
+        }
+    int tot_in, tot_cut;
+    const int off_in = block_excl_scan(nin, warp_sums, tot_in);
+    const int off_cut = block_excl_scan(ncut, warp_sums, tot_cut);
+    if (tid == 0) {
+        s_base_in = atomicAdd(&cnt->n_inside, tot_in);
+        s_base_cut = atomicAdd(&cnt->n_cut, tot_cut);
+        pl.n_inside = tot_in;
+        pl.n_cut = tot_cut;
+    }
+    __syncthreads();
+    const int64_t bin = s_base_in, bcut = s_base_cut;
+    if (bin + tot_in > cap_in || bcut + tot_cut > cap_cut) {
+        if (tid == 0) set_error(cnt, DERR_CAPACITY);
+        return;
+    }
+    int64_t pin = bin + off_in, pcut = bcut + off_cut;
+    for (int row = r0; row < r1; ++row) {
+        const int jj = row % ey, kk = row / ey;
+        for (int w = 0; w < W; ++w) {
+            uint32_t bits = R[row * W + w];
+            while (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1;
+                const int xx = (w << 5) + b;
+                const uint8_t cc = cls[(int64_t)row * ex + xx];
+                const int64_t gi = pl.lo[0] + xx, gj = pl.lo[1] + jj, gk = pl.lo[2] + kk;
+                const int32_t cell = (int32_t)(gi + (int64_t)m.nx * (gj + (int64_t)m.ny * gk));
+                if (cc == 1) { in_cell[pin] = cell; in_solid[pin] = list_word(s, 1); ++pin; }
+                else { cut_cell[pcut] = cell; cut_solid[pcut] = list_word(s, cc); ++pcut; }
+            }
+        }
+    }
+}
+
+// ---- REF-GEO: GeometricTools::calcCellVolume (geometrictools.cpp:13-116) in FP64 ----------------------------------------
+// Vertex slots: 0:(i,j,k) 1:(i+1,j,k) 2:(i,j+1,k) 3:(i+1,j+1,k) 4..7 the same at k+1 (ascending point label).
+__constant__ int8_t c_face_slots[9][4] = {
+    {1, 3, 7, 5},  // x-max, owner order (internal +x face and x-max boundary face)
+    {2, 6, 7, 3},  // y-max
+    {4, 5, 7, 6},  // z-max
+    {0, 4, 6, 2},  // x-min boundary face (hex model order)
+    {0, 1, 5, 4},  // y-min boundary face
+    {0, 2, 3, 1},  // z-min boundary face
+    {0, 2, 6, 4},  // -x internal face (owner is the lower neighbour)
+    {0, 4, 5, 1},  // -y internal face
+    {0, 1, 3, 2},  // -z internal face
+};
+
+__device__ inline double line_fraction(double pa, double pb) {
+    if (pa > 0 && pb > 0) return 0;
+    if (pa <= 0 && pb <= 0) return 1;
+    if (pa > 0) return -pb / (pa - pb);
+    return -pa / (pb - pa);
+}
+
+__device__ inline D3 calc_apex(const D3* P, const double* ph, const int8_t* idx, int n) {
+    const D3 A = P[idx[0]];
+    const double phiA = ph[idx[0]];
+    D3 B{0, 0, 0};
+    double phiB = 0.0;
+    for (int i = 1; i < n; ++i) {
+        B = P[idx[i]];
+        phiB = ph[idx[i]];
+        if (phiA * phiB <= 0) break;
+    }
+    return A - fabs(phiA) / (SMALL_D + fabs(phiA) + fabs(phiB)) * (A - B);
+}
+
+__device__ inline double face_area_fraction(const D3* P, const double* ph, const int8_t* f, const D3& Sf) {
+    int sign_sum = 0;
+    for (int i = 0; i < 4; ++i) sign_sum += (ph[f[i]] > 0) ? 1 : -1;
+    if (sign_sum == 4) return 0.0;
+    if (sign_sum == -4) return 1.0;
+    const D3 ap = calc_apex(P, ph, f, 4);
+    double area = 0.0;
+    for (int iseg = 0; iseg < 4; ++iseg) {
+        const int o = f[iseg], a = f[(iseg + 1) & 3];
+        area += fabs(0.5 * mag(cross(P[a] - P[o], ap - P[o]))) * line_fraction(ph[o], ph[a]);
+    }
+    return area / mag(Sf);
+}
+
+__device__ double refgeo_fraction(const MeshK& m, const ShapeK& sh, const D3& x, const Q4& q, int64_t i, int64_t j,
+                                  int64_t k) {
+    D3 P[8];
+    double ph[8];
+    const int8_t order[8] = {0, 1, 2, 3, 4, 5, 6, 7};
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        P[s] = mesh_point(m, i + (s & 1), j + ((s >> 1) & 1), k + ((s >> 2) & 1));
+        ph[s] = sdf64(sh, world2local(P[s], x, q));
+    }
+    D3 ap = calc_apex(P, ph, order, 8);
+    if (m.twod) ap.z = 0.0;
+    const double xc = mesh_centre(m, 0, i), yc = mesh_centre(m, 1, j), zc = mesh_centre(m, 2, k);
+    const double xlo = mesh_coord(m, 0, i), xhi = mesh_coord(m, 0, i + 1);
+    const double ylo = mesh_coord(m, 1, j), yhi = mesh_coord(m, 1, j + 1);
+    const double zlo = mesh_coord(m, 2, k), zhi = mesh_coord(m, 2, k + 1);
+    const D3 Sx{m.h[1] * m.h[2], 0, 0}, Sy{0, m.h[0] * m.h[2], 0}, Sz{0, 0, m.h[0] * m.h[1]};
+    double volume = 0.0;
+    auto acc = [&](int slot, const D3& Cf, const D3& Sf) {
+        const double eps_f = face_area_fraction(P, ph, c_face_slots[slot], Sf);
+        volume += (1.0 / 3.0) * eps_f * fabs(dot(ap - Cf, Sf));
+    };
+    // mesh.cells()[c] order: owned internal (+x,+y,+z), boundary faces by patch, then -z,-y,-x
+    if (i + 1 < m.nx) acc(0, D3{xhi, yc, zc}, Sx);
+    if (j + 1 < m.ny) acc(1, D3{xc, yhi, zc}, Sy);
+    if (k + 1 < m.nz) acc(2, D3{xc, yc, zhi}, Sz);
+    if (i == 0) acc(3, D3{xlo, yc, zc}, Sx);
+    if (i == m.nx - 1) acc(0, D3{xhi, yc, zc}, Sx);
+    if (j == 0) acc(4, D3{xc, ylo, zc}, Sy);
+    if (j == m.ny - 1) acc(1, D3{xc, yhi, zc}, Sy);
+    if (k == 0) acc(5, D3{xc, yc, zlo}, Sz);
+    if (k == m.nz - 1) acc(2, D3{xc, yc, zhi}, Sz);
+    if (k > 0) acc(8, D3{xc, yc, zlo}, Sz);
+    if (j > 0) acc(7, D3{xc, ylo, zc}, Sy);
+    if (i > 0) acc(6, D3{xlo, yc, zc}, Sx);
+    return volume / m.V;
+}
+
+// ---- SUBSAMPLE: n^3 (3-D) or n^2 (2-D) midpoint lattice, isInside per sample -------------------------------------------
+__device__ double subsample_fraction(const MeshK& m, const ShapeK& sh, const float* M, const D3& x, const Q4& q,
+                                     int64_t i, int64_t j, int64_t k, int n, unsigned long long* rechecks) {
+    const D3 p0 = mesh_point(m, i, j, k);
+    const TileFrame tf = make_frame(p0 - x, p0, x);
+    const int nzs = m.twod ? 1 : n;
+    const float inv2n = 1.0f / (float)(2 * n);
+    int cnt = 0;
+    for (int c3 = 0; c3 < nzs; ++c3) {
+        const double tz = m.twod ? 0.5 : (double)(2 * c3 + 1) / (double)(2 * n);
+        const float oz = (m.twod ? 0.5f : (float)(2 * c3 + 1) * inv2n) * m.h32[2];
+        for (int bb = 0; bb < n; ++bb) {
+            const double ty = (double)(2 * bb + 1) / (double)(2 * n);
+            const float oy = (float)(2 * bb + 1) * inv2n * m.h32[1];
+            for (int a = 0; a < n; ++a) {
+                const float ox = (float)(2 * a + 1) * inv2n * m.h32[0];
+                const float dx = tf.bx + ox, dy = tf.by + oy, dz = tf.bz + oz;
+                const float lx = __fmaf_rn(M[0], dx, __fmaf_rn(M[1], dy, M[2] * dz));
+                const float ly = __fmaf_rn(M[3], dx, __fmaf_rn(M[4], dy, M[5] * dz));
+                const float lz = __fmaf_rn(M[6], dx, __fmaf_rn(M[7], dy, M[8] * dz));
+                const float dabs = fabsf(dx) + fabsf(dy) + fabsf(dz);
+                // the FP32 sample offset carries an extra rounding of (2a+1)/(2n) relative to the FP64 formula
+                const float E = 8.f * U32 * (tf.babs + fabsf(ox) + fabsf(oy) + fabsf(oz) + 2.f * dabs) + tf.e64 + 1e-30f;
+                int r = inside32(sh, lx, ly, lz, E);
+                if (r == 2) {
+                    atomicAdd(rechecks, 1ull);
+                    const double ta = (double)(2 * a + 1) / (double)(2 * n);
+                    const D3 p{m.o[0] + ((double)i + ta) * m.h[0], m.o[1] + ((double)j + ty) * m.h[1],
+                               m.o[2] + ((double)k + tz) * m.h[2]};
+                    r = inside64(sh, world2local(p, x, q)) ? 1 : 0;
+                }
+                cnt += r;
+            }
+        }
+    }
+    return (double)cnt / (double)(n * n * nzs);
+}
+
+// ---- shared cells -----------------------------------------------------------------------------------------------------
+// slot of cell c in the shared table, inserting it on first use; -1 (and an error flag) when the table is full
+__device__ inline int shared_slot(const CoupleArgs& A, int32_t c) {
+    uint32_t h = ((uint32_t)c * 2654435761u) & (uint32_t)A.sh_mask;
+    for (int p = 0; p < SHARED_MAX_PROBES; ++p) {
+        const int32_t k = atomicCAS(A.sh_keys + h, -1, c);
+        if (k == -1) {
+            const int u = atomicAdd(&A.cnt->n_shared, 1);
+            if (u <= A.sh_mask) A.sh_used[u] = (int32_t)h;
+            return (int)h;
+        }
+        if (k == c) return (int)h;
+        h = (h + 1) & (uint32_t)A.sh_mask;
+    }
+    set_error(A.cnt, DERR_SHARED_TABLE);
+    return -1;
+}
+
+// claim pass: Ct[c] <- claim word of the touching solid, CT_SHARED with the largest claim when several touch it
+__global__ void claim_kernel(const int32_t* __restrict__ in_cell, const int32_t* __restrict__ in_solid,
+                             const int32_t* __restrict__ cut_cell, const int32_t* __restrict__ cut_solid,
+                             int32_t* __restrict__ Ct, const Counters* cnt, int64_t N) {
+    const int n_in = clamp_len(cnt->n_inside, cnt->list_cap), n_cut = clamp_len(cnt->n_cut, cnt->list_cap);
+    uint32_t* C = reinterpret_cast<uint32_t*>(Ct);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)n_in + n_cut;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const bool cut = e >= n_in;
+        const int64_t ee = cut ? e - n_in : e;
+        const int32_t c = cut ? cut_cell[ee] : in_cell[ee];
+        const int32_t sw = cut ? cut_solid[ee] : in_solid[ee];
+        if (c < 0 || c >= N) continue;
+        const uint32_t key = CT_KEY_BASE | ((uint32_t)(sw & LIST_SOLID_MASK) << 2) | (uint32_t)list_type(sw);
+        const uint32_t v = atomicCAS(C + c, 0u, key);
+        if (v != 0u) {
+            const uint32_t lo = max(key, v & ~CT_SHARED);
+            atomicMax(C + c, lo | CT_SHARED);
+        }
+    }
+}
+
+__device__ inline int32_t decode_claim(uint32_t w) {
+    const uint32_t k = (w & ~CT_SHARED) - CT_KEY_BASE;
+    const int32_t s = (int32_t)(k >> 2), code = (int32_t)(k & 3);
+    return code == 1 ? s + 4 : code;
+}
+
+// ---- couple ---------------------------------------------------------------------------------------------------------
+constexpr int CPL_THREADS = 256;
+
+
+
+__global__ void __launch_bounds__(CPL_THREADS) couple_kernel(CoupleArgs A) {
+    __shared__ int s_item;
+    const MeshK& m = A.m;
+    const int64_t N = m.ncells;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int n_in = clamp_len(A.cnt->n_inside, A.cnt->list_cap), n_cut = clamp_len(A.cnt->n_cut, A.cnt->list_cap);
+    const int in_chunks = (n_in + CPL_THREADS - 1) / CPL_THREADS;
+    const int cut_chunks = (n_cut + CPL_THREADS - 1) / CPL_THREADS;
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(&A.cnt->couple_next, 1);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= in_chunks + cut_chunks) break;
+        const bool is_cut = item >= in_chunks;
+        const int e = (is_cut ? item - in_chunks : item) * CPL_THREADS + tid;
+        const bool valid = e < (is_cut ? n_cut : n_in);
+        int s = -1;
+        double f6[6] = {0, 0, 0, 0, 0, 0};
+        if (valid) {
+            const int32_t c32 = is_cut ? A.cut_cell[e] : A.in_cell[e];
+            const int32_t sw = is_cut ? A.cut_solid[e] : A.in_solid[e];
+            s = sw & LIST_SOLID_MASK;
+            const int type = list_type(sw);
+            const int64_t c = (c32 >= 0 && c32 < N) ? c32 : 0;
+            if (c32 != c) set_error(A.cnt, DERR_CAPACITY);
+            const int64_t i = c % m.nx, j = (c / m.nx) % m.ny, k = c / ((int64_t)m.nx * m.ny);
+            const sdfibm_solid_state& st = A.st[s];
+            const D3 x = state_pos(st);
+            double alpha = 1.0;
+            if (is_cut) {
+                const Q4 q = state_quat(st);
+                if (A.method == SDFIBM_FRACTION_SUBSAMPLE)
+                    alpha = subsample_fraction(m, A.sk[s].shape, A.plan[s].M, x, q, i, j, k, A.subsample_n,
+                                               &A.cnt->exact_rechecks);
+                else
+                    alpha = refgeo_fraction(m, A.sk[s].shape, x, q, i, j, k);
+            }
+            // pcHydrodynamicInteraction (solidcloud.cpp:384-390) and the accumulation of :411-421
+            const D3 cc = mesh_C(m, i, j, k);
+            const D3 vel{st.vel[0], st.vel[1], st.vel[2]}, om{st.omega[0], st.omega[1], st.omega[2]};
+            const D3 uf{(double)A.U[c], (double)A.U[N + c], (double)A.U[2 * N + c]};
+            const D3 us = vel + cross(om, cc - x);
+            const D3 f_ = alpha * (uf - us);
+            const D3 t_ = cross(cc - x, f_);
+            const double cv = m.V;
+            const D3 F = f_ * cv * A.dtINV, T = t_ * cv * A.dtINV;
+            f6[0] = F.x; f6[1] = F.y; f6[2] = F.z; f6[3] = T.x; f6[4] = T.y; f6[5] = T.z;
+            const D3 fs = f_ * A.dtINV;
+            (void)type;
+            const uint32_t claim = reinterpret_cast<const uint32_t*>(A.Ct)[c];
+            if (!(claim & CT_SHARED)) {
+                // the only solid on this cell: As += alpha etc. on zeroed fields is a plain store
+                A.As[c] = (float)alpha;
+                A.Ts[c] = (float)alpha;
+                A.Fs[c] = (float)fs.x;
+                A.Fs[N + c] = (float)fs.y;
+                A.Fs[2 * N + c] = (float)fs.z;
+            } else {
+                const int slot = shared_slot(A, (int32_t)c);
+                if (slot >= 0) {
+                    double* v = A.sh_vals + 5 * (int64_t)slot;
+                    atomicAdd(v + 0, alpha);
+                    atomicAdd(v + 1, alpha);
+                    atomicAdd(v + 2, fs.x);
+                    atomicAdd(v + 3, fs.y);
+                    atomicAdd(v + 4, fs.z);
+                }
+            }
+        }
+        // force/torque: one FP64 atomic per warp when the warp serves a single solid
+        const int s0 = __shfl_sync(0xffffffffu, s, 0);
+        const bool uniform = __all_sync(0xffffffffu, s == s0 || s < 0);
+        if (uniform) {
+#pragma unroll
+            for (int r = 0; r < 6; ++r) {
+                double v = f6[r];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                f6[r] = v;
+            }
+            if (lane == 0 && s0 >= 0)
+                for (int r = 0; r < 6; ++r) atomicAdd(A.ftacc + 6 * s0 + r, f6[r]);
+        } else if (s >= 0) {
+            for (int r = 0; r < 6; ++r) atomicAdd(A.ftacc + 6 * s + r, f6[r]);
+        }
+    }
+}
+
+// ---- finalize ---------------------------------------------------------------------------------------------------------
+__global__ void finalize_kernel(const int32_t* __restrict__ in_cell, const int32_t* __restrict__ in_solid,
+                                const int32_t* __restrict__ cut_cell, const int32_t* __restrict__ cut_solid,
+                                float* __restrict__ As, float* __restrict__ Ts, float* __restrict__ Fs,
+                                int32_t* __restrict__ Ct, Counters* cnt, int64_t N, int32_t* __restrict__ sh_keys,
+                                double* __restrict__ sh_vals, const int32_t* __restrict__ sh_used, int32_t sh_mask) {
+    const int n_in = clamp_len(cnt->n_inside, cnt->list_cap), n_cut = clamp_len(cnt->n_cut, cnt->list_cap);
+    const int n_sh = min(cnt->n_shared, sh_mask + 1);
+    uint32_t* C = reinterpret_cast<uint32_t*>(Ct);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)n_in + n_cut + n_sh;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        if (e < (int64_t)n_in + n_cut) {
+            // cells of one solid: decode the claim, As = min(As, 1) (checkAlpha)
+            const bool cut = e >= n_in;
+            const int64_t ee = cut ? e - n_in : e;
+            const int32_t c = cut ? cut_cell[ee] : in_cell[ee];
+            if (c < 0 || c >= N) continue;
+            const uint32_t v = C[c];
+            if (v < CT_KEY_BASE || (v & CT_SHARED)) continue;
+            Ct[c] = decode_claim(v);
+            As[c] = fminf(As[c], 1.0f);
+        } else {
+            // shared cells: FP64 sums rounded once to the FP32 fields; the slot is cleared for the next call
+            const int slot = sh_used[e - n_in - n_cut];
+            const int32_t c = sh_keys[slot];
+            double* v = sh_vals + 5 * (int64_t)slot;
+            if (c >= 0 && c < N) {
+                Ct[c] = decode_claim(C[c]);
+                As[c] = (float)fmin(v[0], 1.0);
+                Ts[c] = (float)v[1];
+                Fs[c] = (float)v[2];
+                Fs[N + c] = (float)v[3];
+                Fs[2 * N + c] = (float)v[4];
+            }
+            for (int r = 0; r < 5; ++r) v[r] = 0.0;
+            sh_keys[slot] = -1;
+        }
+    }
+}
+
+__global__ void ft_kernel(const double* __restrict__ ftacc, double* __restrict__ ft, int S, double rho_f) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    for (int r = 0; r < 6; ++r) ft[6 * s + r] = ftacc[6 * s + r] * rho_f;
+}
+
+// sparse reset of the previous call's touched cells
+__global__ void reset_kernel(const int32_t* __restrict__ in_cell, const int32_t* __restrict__ cut_cell,
+                             const Counters* cnt, int64_t N, float* As, float* Fs, float* Ts, int32_t* Ct) {
+    const int n_in = clamp_len(cnt->n_inside, cnt->list_cap), n_cut = clamp_len(cnt->n_cut, cnt->list_cap);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)n_in + n_cut;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = e < n_in ? in_cell[e] : cut_cell[e - n_in];
+        if (c < 0 || c >= N) continue;
+        As[c] = 0.f; Ts[c] = 0.f; Ct[c] = 0;
+        Fs[c] = 0.f; Fs[N + c] = 0.f; Fs[2 * N + c] = 0.f;
+    }
+}
+
+// SolidCloud::fixInternal over the ALL_INSIDE list: U = rigid velocity of the solid that owns the cell
+__global__ void fix_internal_kernel(MeshK m, const sdfibm_solid_state* __restrict__ st,
+                                    const int32_t* __restrict__ in_cell, const int32_t* __restrict__ in_solid,
+                                    const int32_t* __restrict__ Ct, float* __restrict__ U, const Counters* cnt) {
+    const int n_in = clamp_len(cnt->n_inside, cnt->list_cap);
+    const int64_t N = m.ncells;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_in; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = in_cell[e];
+        const int32_t s = in_solid[e] & LIST_SOLID_MASK;
+        if (c < 0 || c >= N) continue;
+        if (Ct[c] != s + 4) continue;
+        const int64_t i = c % m.nx, j = (c / m.nx) % m.ny, k = c / ((int64_t)m.nx * m.ny);
+        const sdfibm_solid_state& x = st[s];
+        const D3 vel{x.vel[0], x.vel[1], x.vel[2]}, om{x.omega[0], x.omega[1], x.omega[2]};
+        const D3 u = vel + cross(om, mesh_C(m, i, j, k) - state_pos(x));
+        U[c] = (float)u.x; U[N + c] = (float)u.y; U[2 * N + c] = (float)u.z;
+    }
+}
+
+}  // namespace sdfibm_dev

@@ -1,0 +1,313 @@
+// Rigid-body side of the time step: the GB300 replacement of SolidCloud::evolve (src/solidcloud.cpp:521-562) with
+// Solid::applyForcer / addMidFluidForceAndTorque / addAcceleration / move / storeOldForce (src/solid.h:126-202),
+// addMidEnvironment (solidcloud.cpp:466-475), the motions (src/libmotion) and forcers (src/libforcer), and the
+// uniform-grid collision of solidSolidInteract / solidSolidCollision (solidcloud.cpp:477-519,
+// src/libcollision/ugrid.cpp:5-77, collision.cpp:7-57).
+//
+// Without collisions every solid is independent, so one thread runs all sub-steps of one solid in a single launch.
+// With collisions each sub-step is: forces + grid hash, counting sort of solid ids by grid cell, pair forces
+// (each solid sums its own side of every pair: no atomics, the pair law is evaluated once per side), move.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+
+namespace sdfibm_dev {
+
+__device__ inline D3 ld3(const double* a) { return D3{a[0], a[1], a[2]}; }
+__device__ inline void st3(double* a, const D3& v) { a[0] = v.x; a[1] = v.y; a[2] = v.z; }
+
+// IMotion::constraint of each registered motion
+__device__ inline void motion_constraint(const SolidK& k, double time, D3& velocity, D3& omega) {
+    const double* p = k.motion_p;
+    switch (k.motion_type) {
+        case SDFIBM_MOTION_000002: velocity = D3{0, 0, 0}; omega = D3{0, 0, 0}; omega.z = p[1]; return;
+        case SDFIBM_MOTION_110002: velocity.z = 0.0; omega = D3{0, 0, 0}; omega.z = p[1]; return;
+        case SDFIBM_MOTION_222000: velocity = D3{p[0], p[1], p[2]}; omega = D3{0, 0, 0}; return;
+        case SDFIBM_MOTION_SINEDIRECTIONAL:
+            velocity = p[0] * p[2] * cos(p[2] * time) * D3{p[3], p[4], p[5]};
+            omega = D3{0, 0, 0};
+            return;
+        case SDFIBM_MOTION_01MASK:
+            velocity = D3{velocity.x * p[0], velocity.y * p[1], velocity.z * p[2]};
+            omega = D3{omega.x * p[3], omega.y * p[4], omega.z * p[5]};
+            return;
+        case SDFIBM_MOTION_ROTOR:
+            velocity = D3{0, 0, 0};
+            velocity.x = -p[2] * p[1] * sin(p[1] * time + p[3]);
+            velocity.y = p[2] * p[1] * cos(p[1] * time + p[3]);
+            omega = D3{0, 0, 0};
+            omega.z = p[4];
+            return;
+        case SDFIBM_MOTION_OPENCLOSE: {
+            const double t = fmod(time, 5.0);
+            double v = 0.0;
+            if (t > 1 && t < 2) v = -1.0;
+            if (t > 3 && t < 4) v = 1.0;
+            velocity = D3{0, v, 0};
+            omega = D3{0, 0, 0};
+            return;
+        }
+        default: return;
+    }
+}
+
+// IForcer::generate of each registered forcer
+__device__ inline void forcer_generate(const SolidK& k, const sdfibm_solid_state& s, double time, D3& f, D3& t) {
+    const double* p = k.forcer_p;
+    f = D3{0, 0, 0};
+    t = D3{0, 0, 0};
+    switch (k.forcer_type) {
+        case SDFIBM_FORCER_CONSTANT: f = D3{p[0], p[1], p[2]}; t = D3{p[3], p[4], p[5]}; return;
+        case SDFIBM_FORCER_SPRING: {
+            const D3 r = ld3(s.pos) - D3{p[0], p[1], p[2]};
+            if (mag(r) > SMALL_D) f = -p[3] * r * (1.0 - p[4] / mag(r));
+            return;
+        }
+        case SDFIBM_FORCER_MAGNETIC: {
+            const D3 m_original = (1.0) * (D3{0.0, 0.0, 1.0});
+            const D3 B = p[3] * cos(p[4] * time) * D3{p[0], p[1], p[2]};
+            const Q4 q{s.quat[0], D3{s.quat[1], s.quat[2], s.quat[3]}};
+            const D3 m = qtransform(qconj(q), m_original);
+            t = cross(m, B);
+            return;
+        }
+        default: return;
+    }
+}
+
+// clearForceAndTorque, applyForcer, addMidFluidForceAndTorque, addMidEnvironment for one solid
+__device__ inline void pre_forces(const SolidK& k, sdfibm_solid_state& s, double time, double rho_f, const D3& g) {
+    D3 force{0, 0, 0}, torque{0, 0, 0};
+    if (k.forcer_type != SDFIBM_FORCER_NONE) {
+        D3 f_, t_;
+        forcer_generate(k, s, time, f_, t_);
+        st3(s.forcer_force, f_);
+        st3(s.forcer_torque, t_);
+        if (s.first_forcer_step) {
+            st3(s.forcer_force_old, f_);
+            st3(s.forcer_torque_old, t_);
+            s.first_forcer_step = 0;
+        }
+        force = force + (1.5 * ld3(s.forcer_force) - 0.5 * ld3(s.forcer_force_old));
+        torque = torque + (1.5 * ld3(s.forcer_torque) - 0.5 * ld3(s.forcer_torque_old));
+    }
+    if (s.first_fluid_step) {
+        for (int a = 0; a < 3; ++a) { s.fluid_force_old[a] = s.fluid_force[a]; s.fluid_torque_old[a] = s.fluid_torque[a]; }
+        s.first_fluid_step = 0;
+    }
+    force = force + (1.5 * ld3(s.fluid_force) - 0.5 * ld3(s.fluid_force_old));
+    torque = torque + (1.5 * ld3(s.fluid_torque) - 0.5 * ld3(s.fluid_torque_old));
+    const double rhos = k.rho;
+    const D3 gprime = ((rhos - rho_f) / rhos) * g;
+    force = force + k.mass * gprime;
+    st3(s.force, force);
+    st3(s.torque, torque);
+}
+
+// Solid::move
+__device__ inline void move_solid(const SolidK& k, sdfibm_solid_state& s, double time, double dt) {
+    const D3 velocity_old = ld3(s.vel), omega_old = ld3(s.omega);
+    D3 vel = velocity_old + ld3(s.force) * k.mass_inv * dt;
+    const Q4 q{s.quat[0], D3{s.quat[1], s.quat[2], s.quat[3]}};
+    const double w2 = q.w * q.w, x2 = q.v.x * q.v.x, y2 = q.v.y * q.v.y, z2 = q.v.z * q.v.z;
+    const double txy = 2 * q.v.x * q.v.y, twz = 2 * q.w * q.v.z, txz = 2 * q.v.x * q.v.z;
+    const double twy = 2 * q.w * q.v.y, tyz = 2 * q.v.y * q.v.z, twx = 2 * q.w * q.v.x;
+    const double R[9] = {w2 + x2 - y2 - z2, txy - twz, txz + twy, txy + twz, w2 - x2 + y2 - z2,
+                         tyz - twx, txz - twy, tyz + twx, w2 - x2 - y2 + z2};
+    const double* I = k.moi_inv;
+    double RI[9], W[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) RI[3 * r + c] = R[3 * r] * I[c] + R[3 * r + 1] * I[3 + c] + R[3 * r + 2] * I[6 + c];
+    for (int r = 0; r < 3; ++r)  // (R & I) & R^T
+        for (int c = 0; c < 3; ++c) W[3 * r + c] = RI[3 * r] * R[3 * c] + RI[3 * r + 1] * R[3 * c + 1] + RI[3 * r + 2] * R[3 * c + 2];
+    const D3 T = ld3(s.torque);
+    const D3 WT{W[0] * T.x + W[1] * T.y + W[2] * T.z, W[3] * T.x + W[4] * T.y + W[5] * T.z,
+                W[6] * T.x + W[7] * T.y + W[8] * T.z};
+    D3 om = omega_old + WT * dt;
+    if (k.motion_type != SDFIBM_MOTION_FREE) motion_constraint(k, time, vel, om);
+    const D3 c = ld3(s.pos) + 0.5 * (vel + velocity_old) * dt;
+    const Q4 h{0.5 * 0.0, 0.5 * (0.5 * (om + omega_old))};
+    const Q4 dq0 = qmul(h, q);
+    const Q4 dq{dq0.w * dt, dq0.v * dt};
+    Q4 qn{q.w + dq.w, q.v + dq.v};
+    const double mq = sqrt(qn.w * qn.w + magSqr(qn.v));
+    qn = Q4{qn.w / mq, qn.v / mq};
+    st3(s.vel, vel);
+    st3(s.omega, om);
+    st3(s.pos, c);
+    s.quat[0] = qn.w; s.quat[1] = qn.v.x; s.quat[2] = qn.v.y; s.quat[3] = qn.v.z;
+}
+
+__device__ inline void store_old(sdfibm_solid_state& s) {
+    for (int a = 0; a < 3; ++a) {
+        s.fluid_force_old[a] = s.fluid_force[a];
+        s.fluid_torque_old[a] = s.fluid_torque[a];
+        s.forcer_force_old[a] = s.forcer_force[a];
+        s.forcer_torque_old[a] = s.forcer_torque[a];
+    }
+}
+
+// all sub-steps of one solid (no solid-solid interaction)
+__global__ void evolve_independent_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state* st, int S, int nsub,
+                                          double time, double dt_sub, double rho_f, D3 g) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const SolidK& k = sk[s];
+    sdfibm_solid_state x = st[s];
+    for (int it = 0; it < nsub; ++it) {
+        pre_forces(k, x, time, rho_f, g);
+        move_solid(k, x, time, dt_sub);
+    }
+    store_old(x);
+    st[s] = x;
+}
+
+
+
+__device__ inline int64_t grid_hash(const GridK& gk, const D3& c) {
+    const int i = (int)floor((c.x - gk.low[0]) * gk.dINV);
+    const int j = (int)floor((c.y - gk.low[1]) * gk.dINV);
+    const int k = (int)floor((c.z - gk.low[2]) * gk.dINV);
+    return (int64_t)i * gk.nynz + (int64_t)j * gk.nz + k;
+}
+
+// forces of one sub-step and the UGrid insert (UGrid::insert, ugrid.h:31-34)
+__global__ void evolve_pre_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state* st, int S, double time,
+                                  double rho_f, D3 g, GridK gk, int64_t* __restrict__ hashes,
+                                  int32_t* __restrict__ counts) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    pre_forces(sk[s], st[s], time, rho_f, g);
+    const int64_t h = grid_hash(gk, ld3(st[s].pos));
+    hashes[s] = h;
+    if (h >= 0 && h < gk.ncell) atomicAdd(counts + h, 1);
+}
+
+// exclusive scan of the per-cell counts (single block)
+__global__ void grid_scan_kernel(const int32_t* __restrict__ counts, int32_t* __restrict__ start,
+                                 int32_t* __restrict__ cursor, int64_t ncell) {
+    __shared__ int32_t warp_tot[32];
+    __shared__ int32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int64_t base = 0; base < ncell; base += blockDim.x) {
+        const int64_t i = base + threadIdx.x;
+        const int32_t v = i < ncell ? counts[i] : 0;
+        int32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            int32_t w = lane < nw ? warp_tot[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            if (lane < nw) warp_tot[lane] = w;
+        }
+        __syncthreads();
+        const int32_t excl = carry + (wid > 0 ? warp_tot[wid - 1] : 0) + x - v;
+        if (i < ncell) { start[i] = excl; cursor[i] = excl; }
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warp_tot[nw - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) start[ncell] = carry;
+}
+
+__global__ void grid_scatter_kernel(const int64_t* __restrict__ hashes, int32_t* __restrict__ cursor,
+                                    int32_t* __restrict__ list, int S, int64_t ncell) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const int64_t h = hashes[s];
+    if (h >= 0 && h < ncell) list[atomicAdd(cursor + h, 1)] = s;
+}
+
+// the collision laws of collision.cpp:7-35 (positions of the sub-step start)
+__device__ inline double plane_sphere(const sdfibm_solid_state& p, const sdfibm_solid_state& s, double rB_s, D3& cN) {
+    const Q4 qp{p.quat[0], D3{p.quat[1], p.quat[2], p.quat[3]}};
+    const D3 s_center = qtransform(qconj(qp), ld3(s.pos) - ld3(p.pos));
+    const double p2s = s_center.y;
+    cN = qtransform(qp, D3{0, 1, 0});
+    return rB_s - p2s;
+}
+__device__ inline double sphere_sphere(const sdfibm_solid_state& s1, const sdfibm_solid_state& s2, double r1,
+                                       double r2, D3& cN) {
+    const D3 s2s = ld3(s2.pos) - ld3(s1.pos);
+    const double m = mag(s2s);
+    cN = m < 1e-150 ? D3{0, 0, 0} : s2s / m;
+    return r1 + r2 - mag(s2s);
+}
+
+// contact force on s2 (s1 receives the opposite); returns false when the pair has no law or no overlap
+__device__ inline bool pair_force(const SolidK& k1, const sdfibm_solid_state& s1, int id1, const SolidK& k2,
+                                  const sdfibm_solid_state& s2, int id2, D3& f) {
+    double cd;
+    D3 cN;
+    if ((id1 == 1 || id1 == 2) && id2 == 0) cd = plane_sphere(s2, s1, k1.radiusB, cN);
+    else if (id1 == 0 && (id2 == 1 || id2 == 2)) cd = plane_sphere(s1, s2, k2.radiusB, cN);
+    else if ((id1 == 1 && id2 == 1) || (id1 == 2 && id2 == 2)) cd = sphere_sphere(s1, s2, k1.radiusB, k2.radiusB, cN);
+    else return false;
+    if (cd < 0) return false;
+    f = 1e4 * cd * cN;
+    return true;
+}
+
+__global__ void collide_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state* st, int S, GridK gk,
+                               const int64_t* __restrict__ hashes, const int32_t* __restrict__ start,
+                               const int32_t* __restrict__ list, int mode) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= S) return;
+    const int64_t h = hashes[p];
+    if (h < 0 || h >= gk.ncell) return;
+    const int ci = (int)(h / gk.nynz), cj = (int)((h / gk.nz) % gk.ny), ck = (int)(h % gk.nz);
+    const SolidK& kp = sk[p];
+    const int idp = (mode == SDFIBM_COLLISION_SPHERES) ? (kp.infinite ? 0 : 2) : kp.collision_id;
+    D3 fsum{0, 0, 0};
+    const sdfibm_solid_state sp = st[p];
+    for (int a = ci - 1; a <= ci + 1; ++a) {
+        if (a < 0 || a > gk.nx - 1) continue;
+        for (int b = cj - 1; b <= cj + 1; ++b) {
+            if (b < 0 || b > gk.ny - 1) continue;
+            for (int c = ck - 1; c <= ck + 1; ++c) {
+                if (c < 0 || c > gk.nz - 1) continue;
+                const int64_t nb = (int64_t)a * gk.nynz + (int64_t)b * gk.nz + c;
+                for (int e = start[nb]; e < start[nb + 1]; ++e) {
+                    const int q = list[e];
+                    if (q == p) continue;
+                    const SolidK& kq = sk[q];
+                    const int idq = (mode == SDFIBM_COLLISION_SPHERES) ? (kq.infinite ? 0 : 2) : kq.collision_id;
+                    D3 f;
+                    if (p < q) {
+                        if (pair_force(kp, sp, idp, kq, st[q], idq, f)) fsum = fsum + (-f);
+                    } else {
+                        if (pair_force(kq, st[q], idq, kp, sp, idp, f)) fsum = fsum + f;
+                    }
+                }
+            }
+        }
+    }
+    // force += -f / +f in pair order (reordered sum); torque += -0 leaves it unchanged
+    st[p].force[0] += fsum.x;
+    st[p].force[1] += fsum.y;
+    st[p].force[2] += fsum.z;
+}
+
+__global__ void move_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state* st, int S, double time, double dt) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    move_solid(sk[s], st[s], time, dt);
+}
+
+__global__ void store_old_kernel(sdfibm_solid_state* st, int S) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    store_old(st[s]);
+}
+
+}  // namespace sdfibm_dev

@@ -1,0 +1,528 @@
+// Host-side lowering of shapes / motions / forcers / materials into the C ABI descriptors, and the solidDict front
+// end (include/sdfibm_host.h).  Arithmetic of the constructors follows the reference exactly, so the descriptors
+// carry the same bits as the reference's objects:
+//   shapes     src/libshape/{circle,sphere,ellipse,ellipsoid,rectangle,box,plane,circle_tail,circle_twotail}.h
+//   motions    src/libmotion/motion*.h constructors
+//   forcers    src/libforcer/{constant,spring,magnetic}.h constructors
+//   material   src/libmaterial/imaterial.h, Solid::setMaterial src/solid.h:95-103
+//   euler      Solid::setOrientation src/solid.h:76-80 with OpenFOAM quaternion(XYZ, angles)
+//   dictionary SolidCloud::initFromDictionary src/solidcloud.cpp:14-206
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/sdfibm_host.h"
+
+namespace {
+
+struct T3 {
+    double m[9];
+};
+T3 inv3(const T3& t) {  // Foam::inv(tensor), cofactor formula
+    const double xx = t.m[0], xy = t.m[1], xz = t.m[2], yx = t.m[3], yy = t.m[4], yz = t.m[5], zx = t.m[6],
+                 zy = t.m[7], zz = t.m[8];
+    const double d = xx * yy * zz + xy * yz * zx + xz * yx * zy - xx * yz * zy - xy * yx * zz - xz * yy * zx;
+    return T3{{(yy * zz - zy * yz) / d, (xz * zy - xy * zz) / d, (xy * yz - xz * yy) / d, (zx * yz - yx * zz) / d,
+               (xx * zz - xz * zx) / d, (yx * xz - xx * yz) / d, (yx * zy - zx * yy) / d, (zx * xy - xx * zy) / d,
+               (xx * yy - yx * xy) / d}};
+}
+T3 diag(double a, double b, double c) { return T3{{a, 0, 0, 0, b, 0, 0, 0, c}}; }
+
+struct Qh {
+    double w, x, y, z;
+};
+Qh qmul(const Qh& a, const Qh& b) {
+    // (a.w*b.w - a.v.b.v, a.w*b.v + b.w*a.v + a.v^b.v)
+    const double dotv = a.x * b.x + a.y * b.y + a.z * b.z;
+    const double cx = a.y * b.z - a.z * b.y, cy = a.z * b.x - a.x * b.z, cz = a.x * b.y - a.y * b.x;
+    return Qh{a.w * b.w - dotv, a.w * b.x + b.w * a.x + cx, a.w * b.y + b.w * a.y + cy, a.w * b.z + b.w * a.z + cz};
+}
+Qh axis_angle(double dx, double dy, double dz, double th) {
+    const double c = std::cos(0.5 * th), s = std::sin(0.5 * th);
+    return Qh{c, s * dx, s * dy, s * dz};
+}
+
+}  // namespace
+
+extern "C" {
+
+int sdfibm_host_make_shape(int32_t type, const double* raw, const double* com_in, sdfibm_shape_desc* out) {
+    if (!out || (!raw && type != SDFIBM_SHAPE_PLANE)) return SDFIBM_ERR_ARG;
+    sdfibm_shape_desc s;
+    std::memset(&s, 0, sizeof(s));
+    s.type = type;
+    const double PI = M_PI;
+    T3 moi = diag(1, 1, 1);
+    bool reads_com = true;
+    switch (type) {
+        case SDFIBM_SHAPE_CIRCLE: {
+            const double r = raw[0], r2 = r * r;
+            if (!(r > 0)) return SDFIBM_ERR_ARG;
+            s.p[0] = r; s.p[1] = r2;
+            s.volume = PI * r2;
+            const double tmp = 0.5 * s.volume * r2;
+            moi = diag(tmp, tmp, tmp);
+            s.radiusB = r;
+            break;
+        }
+        case SDFIBM_SHAPE_SPHERE: {
+            const double r = raw[0], r2 = r * r;
+            if (!(r > 0)) return SDFIBM_ERR_ARG;
+            s.p[0] = r; s.p[1] = r2;
+            s.volume = 4.0 / 3.0 * PI * r2 * r;
+            const double tmp = 0.4 * s.volume * r2;
+            moi = diag(tmp, tmp, tmp);
+            s.radiusB = r;
+            break;
+        }
+        case SDFIBM_SHAPE_ELLIPSE: {
+            const double ra = raw[0], rb = raw[1];
+            if (!(ra > 0 && rb > 0)) return SDFIBM_ERR_ARG;
+            s.p[0] = ra; s.p[1] = rb; s.p[2] = 1.0 / (ra * ra); s.p[3] = 1.0 / (rb * rb);
+            s.volume = PI * ra * rb;
+            const double tmp = 0.25 * s.volume * (ra * ra + rb * rb);
+            moi = diag(tmp, tmp, tmp);
+            s.radiusB = std::max(ra, rb);
+            break;
+        }
+        case SDFIBM_SHAPE_ELLIPSOID: {
+            const double ra = raw[0], rb = raw[1], rc = raw[2];
+            if (!(ra > 0 && rb > 0 && rc > 0)) return SDFIBM_ERR_ARG;
+            s.p[0] = ra; s.p[1] = rb; s.p[2] = rc;
+            s.p[3] = 1.0 / (ra * ra); s.p[4] = 1.0 / (rb * rb); s.p[5] = 1.0 / (rc * rc);
+            s.volume = 4.0 / 3.0 * PI * ra * rb * rc;
+            moi = diag(0.2 * s.volume * (rb * rb + rc * rc), 0.2 * s.volume * (ra * ra + rc * rc),
+                       0.2 * s.volume * (ra * ra + rb * rb));
+            s.radiusB = std::max(std::max(ra, rb), rc);
+            reads_com = false;  // the Ellipsoid constructor never reads com
+            break;
+        }
+        case SDFIBM_SHAPE_RECTANGLE: {
+            const double ra = raw[0], rb = raw[1];
+            if (!(ra > 0 && rb > 0)) return SDFIBM_ERR_ARG;
+            s.p[0] = ra; s.p[1] = rb;
+            s.volume = 4.0 * ra * rb;
+            const double tmp = 1.0 / 3.0 * s.volume * (ra * ra + rb * rb);
+            moi = diag(tmp, tmp, tmp);
+            s.radiusB = std::max(ra, rb);
+            break;
+        }
+        case SDFIBM_SHAPE_BOX: {
+            const double ra = raw[0], rb = raw[1], rc = raw[2];
+            if (!(ra > 0 && rb > 0 && rc > 0)) return SDFIBM_ERR_ARG;
+            s.p[0] = ra; s.p[1] = rb; s.p[2] = rc;
+            s.volume = 8.0 * ra * rb * rc;
+            moi = diag(1.0 / 3.0 * s.volume * (rb * rb + rc * rc), 1.0 / 3.0 * s.volume * (ra * ra + rc * rc),
+                       1.0 / 3.0 * s.volume * (rb * rb + ra * ra));
+            s.radiusB = std::max(std::max(ra, rb), rc);
+            break;
+        }
+        case SDFIBM_SHAPE_PLANE:
+            reads_com = false;  // IShape defaults: zero volume, identity moment of inertia, infinite
+            break;
+        case SDFIBM_SHAPE_CIRCLE_TAIL:
+        case SDFIBM_SHAPE_CIRCLE_TWOTAIL: {
+            const double r = raw[0], ratio = raw[1];
+            const double rb = (type == SDFIBM_SHAPE_CIRCLE_TAIL) ? raw[2] : raw[2] * 0.5;
+            if (!(r > 0)) return SDFIBM_ERR_ARG;
+            const double r2 = r * r, ra = (ratio + 1) * 0.5 * r;
+            s.p[0] = r; s.p[1] = ratio; s.p[2] = rb; s.p[3] = r2; s.p[4] = ra;
+            s.volume = PI * r2;
+            const double tmp = 0.5 * s.volume * r2;
+            moi = diag(tmp, tmp, tmp);
+            s.radiusB = 2 * ra;
+            break;
+        }
+        default: return SDFIBM_ERR_ARG;
+    }
+    s.volume_inv = (type == SDFIBM_SHAPE_PLANE) ? 0.0 : 1.0 / s.volume;
+    const T3 mi = (type == SDFIBM_SHAPE_PLANE) ? diag(1, 1, 1) : inv3(moi);
+    std::memcpy(s.moi_inv, mi.m, sizeof(mi.m));
+    if (reads_com && com_in)
+        for (int a = 0; a < 3; ++a) s.com[a] = com_in[a];
+    s.collision_id = (type == SDFIBM_SHAPE_CIRCLE) ? 1 : (type == SDFIBM_SHAPE_SPHERE) ? 2 : 0;
+    *out = s;
+    return SDFIBM_OK;
+}
+
+int sdfibm_host_make_motion(int32_t type, const double* raw, double* p) {
+    if (!p) return SDFIBM_ERR_ARG;
+    for (int i = 0; i < 8; ++i) p[i] = 0;
+    switch (type) {
+        case SDFIBM_MOTION_FREE:
+        case SDFIBM_MOTION_OPENCLOSE: return SDFIBM_OK;
+        case SDFIBM_MOTION_000002:
+        case SDFIBM_MOTION_110002: p[0] = raw[0]; p[1] = 2 * M_PI / raw[0]; return SDFIBM_OK;
+        case SDFIBM_MOTION_222000: p[0] = raw[0]; p[1] = raw[1]; p[2] = raw[2]; return SDFIBM_OK;
+        case SDFIBM_MOTION_SINEDIRECTIONAL:
+            p[0] = raw[0]; p[1] = raw[1]; p[2] = 2 * M_PI / raw[1];
+            p[3] = raw[2]; p[4] = raw[3]; p[5] = raw[4];
+            return SDFIBM_OK;
+        case SDFIBM_MOTION_01MASK:
+            for (int i = 0; i < 6; ++i) {
+                if (raw[i] != 0.0 && raw[i] != 1.0) return SDFIBM_ERR_ARG;
+                p[i] = raw[i];
+            }
+            return SDFIBM_OK;
+        case SDFIBM_MOTION_ROTOR:
+            p[0] = raw[0]; p[1] = 2 * M_PI / raw[0]; p[2] = raw[1]; p[3] = raw[2]; p[4] = raw[3];
+            return SDFIBM_OK;
+        default: return SDFIBM_ERR_ARG;
+    }
+}
+
+int sdfibm_host_make_forcer(int32_t type, const double* raw, double* p) {
+    if (!p) return SDFIBM_ERR_ARG;
+    for (int i = 0; i < 8; ++i) p[i] = 0;
+    switch (type) {
+        case SDFIBM_FORCER_NONE: return SDFIBM_OK;
+        case SDFIBM_FORCER_CONSTANT: for (int i = 0; i < 6; ++i) p[i] = raw[i]; return SDFIBM_OK;
+        case SDFIBM_FORCER_SPRING:
+        case SDFIBM_FORCER_MAGNETIC: for (int i = 0; i < 5; ++i) p[i] = raw[i]; return SDFIBM_OK;
+        default: return SDFIBM_ERR_ARG;
+    }
+}
+
+void sdfibm_host_quat_from_euler_deg(const double* e, double* q) {
+    const double ax = e[0] * M_PI / 180.0, ay = e[1] * M_PI / 180.0, az = e[2] * M_PI / 180.0;
+    Qh r = axis_angle(1, 0, 0, ax);
+    r = qmul(r, axis_angle(0, 1, 0, ay));
+    r = qmul(r, axis_angle(0, 0, 1, az));
+    q[0] = r.w; q[1] = r.x; q[2] = r.y; q[3] = r.z;
+}
+
+int sdfibm_host_make_solid(int32_t id, const sdfibm_shape_desc* shape, double rho, int32_t motion_type,
+                           const double* motion_p8, int32_t forcer_type, const double* forcer_p8, const double* pos,
+                           const double* euler_deg, const double* vel, const double* omega, sdfibm_solid_desc* out) {
+    if (!shape || !out || !pos) return SDFIBM_ERR_ARG;
+    if (!(rho > 0)) return SDFIBM_ERR_ARG;
+    sdfibm_solid_desc d;
+    std::memset(&d, 0, sizeof(d));
+    d.id = id;
+    d.shape = *shape;
+    d.motion_type = motion_type;
+    d.forcer_type = forcer_type;
+    if (motion_p8) std::memcpy(d.motion_p, motion_p8, sizeof(d.motion_p));
+    if (forcer_p8) std::memcpy(d.forcer_p, forcer_p8, sizeof(d.forcer_p));
+    d.rho = rho;
+    d.mass = shape->volume * rho;
+    d.mass_inv = shape->volume_inv / rho;
+    for (int i = 0; i < 9; ++i) d.moi_inv[i] = shape->moi_inv[i] / rho;
+    for (int a = 0; a < 3; ++a) {
+        d.pos[a] = pos[a];
+        d.vel[a] = vel ? vel[a] : 0.0;
+        d.omega[a] = omega ? omega[a] : 0.0;
+    }
+    const double zero[3] = {0, 0, 0};
+    sdfibm_host_quat_from_euler_deg(euler_deg ? euler_deg : zero, d.quat);
+    *out = d;
+    return SDFIBM_OK;
+}
+
+}  // extern "C"
+
+// ---- solidDict front end ----------------------------------------------------------------------------------------------
+namespace {
+
+struct Node {
+    // either a dictionary (ordered entries) or a token list value
+    bool is_dict = false;
+    std::vector<std::pair<std::string, std::shared_ptr<Node>>> entries;
+    std::vector<std::string> tokens;
+
+    const Node* find(const std::string& k) const {
+        for (auto& e : entries)
+            if (e.first == k) return e.second.get();
+        return nullptr;
+    }
+    const Node& sub(const std::string& k) const {
+        const Node* n = find(k);
+        if (!n || !n->is_dict) throw std::runtime_error("missing sub-dictionary " + k);
+        return *n;
+    }
+};
+
+struct Lexer {
+    const std::string& s;
+    size_t i = 0;
+    explicit Lexer(const std::string& t) : s(t) {}
+    void skip() {
+        for (;;) {
+            while (i < s.size() && std::isspace((unsigned char)s[i])) ++i;
+            if (i + 1 < s.size() && s[i] == '/' && s[i + 1] == '/') {
+                while (i < s.size() && s[i] != '\n') ++i;
+            } else if (i + 1 < s.size() && s[i] == '/' && s[i + 1] == '*') {
+                size_t e = s.find("*/", i + 2);
+                i = (e == std::string::npos) ? s.size() : e + 2;
+            } else {
+                return;
+            }
+        }
+    }
+    bool next(std::string& tok) {
+        skip();
+        if (i >= s.size()) return false;
+        const char c = s[i];
+        if (c == '{' || c == '}' || c == '(' || c == ')' || c == ';' || c == '[' || c == ']') {
+            tok = std::string(1, c);
+            ++i;
+            return true;
+        }
+        if (c == '"') {
+            size_t e = s.find('"', i + 1);
+            if (e == std::string::npos) throw std::runtime_error("unterminated string");
+            tok = s.substr(i + 1, e - i - 1);
+            i = e + 1;
+            return true;
+        }
+        size_t b = i;
+        while (i < s.size() && !std::isspace((unsigned char)s[i]) && std::strchr("{}();[]", s[i]) == nullptr) ++i;
+        tok = s.substr(b, i - b);
+        return true;
+    }
+};
+
+std::shared_ptr<Node> parse_dict(Lexer& lx, bool top) {
+    auto n = std::make_shared<Node>();
+    n->is_dict = true;
+    std::string tok;
+    while (lx.next(tok)) {
+        if (tok == "}") {
+            if (top) throw std::runtime_error("unbalanced }");
+            return n;
+        }
+        if (tok == ";") continue;
+        const std::string key = tok;
+        if (!lx.next(tok)) throw std::runtime_error("unexpected end after " + key);
+        if (tok == "{") {
+            n->entries.emplace_back(key, parse_dict(lx, false));
+            continue;
+        }
+        auto v = std::make_shared<Node>();
+        int depth = 0;
+        for (;;) {
+            if (tok == "(" || tok == "[") ++depth;
+            if (tok == ")" || tok == "]") --depth;
+            if (tok == ";" && depth == 0) break;
+            if (tok == "{" || tok == "}") throw std::runtime_error("unexpected brace in value of " + key);
+            v->tokens.push_back(tok);
+            if (!lx.next(tok)) throw std::runtime_error("unexpected end in value of " + key);
+        }
+        n->entries.emplace_back(key, v);
+    }
+    if (!top) throw std::runtime_error("missing }");
+    return n;
+}
+
+double to_num(const std::string& t) {
+    size_t p = 0;
+    double v = std::stod(t, &p);
+    if (p != t.size()) throw std::runtime_error("not a number: " + t);
+    return v;
+}
+double scalar_of(const Node& d, const std::string& k) {
+    const Node* n = d.find(k);
+    if (!n || n->is_dict || n->tokens.empty()) throw std::runtime_error("missing scalar " + k);
+    return to_num(n->tokens.back());  // a dimensioned entry keeps its value last
+}
+bool vector_of(const Node& d, const std::string& k, double out[3]) {
+    const Node* n = d.find(k);
+    if (!n) return false;
+    std::vector<double> v;
+    for (auto& t : n->tokens)
+        if (t != "(" && t != ")") v.push_back(to_num(t));
+    if (v.size() != 3) throw std::runtime_error("bad vector " + k);
+    for (int a = 0; a < 3; ++a) out[a] = v[a];
+    return true;
+}
+std::string word_of(const Node& d, const std::string& k) {
+    const Node* n = d.find(k);
+    if (!n || n->is_dict || n->tokens.size() != 1) throw std::runtime_error("missing word " + k);
+    return n->tokens[0];
+}
+bool bool_of(const Node& d, const std::string& k) {
+    const std::string w = word_of(d, k);
+    if (w == "1" || w == "true" || w == "yes" || w == "on" || w == "y" || w == "t") return true;
+    if (w == "0" || w == "false" || w == "no" || w == "off" || w == "n" || w == "f" || w == "none") return false;
+    throw std::runtime_error("bad bool " + k);
+}
+
+}  // namespace
+
+extern "C" int sdfibm_host_parse_soliddict(const char* text, double rho_f, sdfibm_solid_desc* solids, int32_t capacity,
+                                           int32_t* nsolids, sdfibm_options* opt, int32_t* on_twod, char* msg,
+                                           int32_t msg_len) {
+    auto err = [&](const std::string& m) {
+        if (msg && msg_len > 0) {
+            std::strncpy(msg, m.c_str(), msg_len - 1);
+            msg[msg_len - 1] = 0;
+        }
+        return SDFIBM_ERR_ARG;
+    };
+    if (!text || !nsolids || !opt) return err("null argument");
+    try {
+        const std::string src(text);
+        Lexer lx(src);
+        auto root = parse_dict(lx, true);
+        const Node& meta = root->sub("meta");
+        const bool on_fluid = bool_of(meta, "on_fluid");
+        const bool twod = bool_of(meta, "on_twod");
+        sdfibm_options_default(opt);
+        double g[3] = {0, 0, 0};
+        if (!vector_of(meta, "gravity", g)) throw std::runtime_error("missing meta.gravity");
+        for (int a = 0; a < 3; ++a) opt->gravity[a] = g[a];
+        opt->rho_f = on_fluid ? rho_f : 0.0;
+        if (on_twod) *on_twod = twod ? 1 : 0;
+
+        static const std::map<std::string, int> shape_ids = {
+            {"Circle", SDFIBM_SHAPE_CIRCLE}, {"Sphere", SDFIBM_SHAPE_SPHERE}, {"Ellipse", SDFIBM_SHAPE_ELLIPSE},
+            {"Ellipsoid", SDFIBM_SHAPE_ELLIPSOID}, {"Rectangle", SDFIBM_SHAPE_RECTANGLE}, {"Box", SDFIBM_SHAPE_BOX},
+            {"Plane", SDFIBM_SHAPE_PLANE}, {"Circle_Tail", SDFIBM_SHAPE_CIRCLE_TAIL},
+            {"Circle_TwoTail", SDFIBM_SHAPE_CIRCLE_TWOTAIL}};
+        std::map<std::string, sdfibm_shape_desc> shapes;
+        for (auto& e : root->sub("shapes").entries) {
+            const Node& sd = *e.second;
+            const std::string type = word_of(sd, "type"), name = word_of(sd, "name");
+            auto it = shape_ids.find(type);
+            if (it == shape_ids.end()) throw std::runtime_error("Cannot create unrecognized object: " + type);
+            double raw[8] = {0}, com[3] = {0, 0, 0};
+            switch (it->second) {
+                case SDFIBM_SHAPE_CIRCLE: case SDFIBM_SHAPE_SPHERE: raw[0] = scalar_of(sd, "radius"); break;
+                case SDFIBM_SHAPE_ELLIPSE: case SDFIBM_SHAPE_RECTANGLE:
+                    raw[0] = scalar_of(sd, "radiusa"); raw[1] = scalar_of(sd, "radiusb"); break;
+                case SDFIBM_SHAPE_ELLIPSOID: case SDFIBM_SHAPE_BOX:
+                    raw[0] = scalar_of(sd, "radiusa"); raw[1] = scalar_of(sd, "radiusb"); raw[2] = scalar_of(sd, "radiusc");
+                    break;
+                case SDFIBM_SHAPE_CIRCLE_TAIL: case SDFIBM_SHAPE_CIRCLE_TWOTAIL:
+                    raw[0] = scalar_of(sd, "radius"); raw[1] = scalar_of(sd, "ratio"); raw[2] = scalar_of(sd, "thickness");
+                    break;
+                default: break;
+            }
+            vector_of(sd, "com", com);
+            sdfibm_shape_desc s;
+            if (sdfibm_host_make_shape(it->second, raw, com, &s) != SDFIBM_OK)
+                throw std::runtime_error("bad parameters for shape " + name);
+            shapes[name] = s;  // EntityLibrary::emplace keeps the first of duplicate names
+        }
+        struct Fr { int type; double p[8]; };
+        std::map<std::string, Fr> forcers;
+        if (const Node* fd = root->find("forces")) {
+            for (auto& e : fd->entries) {
+                const Node& d = *e.second;
+                const std::string type = word_of(d, "type"), name = word_of(d, "name");
+                double raw[8] = {0};
+                Fr f{};
+                if (type == "Constant") {
+                    f.type = SDFIBM_FORCER_CONSTANT;
+                    if (!vector_of(d, "force", raw) || !vector_of(d, "torque", raw + 3)) throw std::runtime_error("Constant needs force and torque");
+                } else if (type == "Spring") {
+                    f.type = SDFIBM_FORCER_SPRING;
+                    if (!vector_of(d, "pivot", raw)) throw std::runtime_error("Spring needs pivot");
+                    raw[3] = scalar_of(d, "k"); raw[4] = scalar_of(d, "l");
+                } else if (type == "Magnetic") {
+                    f.type = SDFIBM_FORCER_MAGNETIC;
+                    if (!vector_of(d, "direction", raw)) throw std::runtime_error("Magnetic needs direction");
+                    raw[3] = scalar_of(d, "A"); raw[4] = scalar_of(d, "w");
+                } else {
+                    throw std::runtime_error("Cannot create unrecognized object: " + type);
+                }
+                sdfibm_host_make_forcer(f.type, raw, f.p);
+                if (!forcers.count(name)) forcers[name] = f;
+            }
+        }
+        struct Mo { int type; double p[8]; };
+        std::map<std::string, Mo> motions;
+        for (auto& e : root->sub("motions").entries) {
+            const Node& d = *e.second;
+            const std::string type = word_of(d, "type"), name = word_of(d, "name");
+            double raw[8] = {0};
+            Mo mo{};
+            if (type == "Motion000002" || type == "Motion110002") {
+                mo.type = type == "Motion000002" ? SDFIBM_MOTION_000002 : SDFIBM_MOTION_110002;
+                raw[0] = scalar_of(d, "period");
+            } else if (type == "Motion222000") {
+                mo.type = SDFIBM_MOTION_222000;
+                raw[0] = scalar_of(d, "u"); raw[1] = scalar_of(d, "v"); raw[2] = scalar_of(d, "w");
+            } else if (type == "MotionSineDirectional") {
+                mo.type = SDFIBM_MOTION_SINEDIRECTIONAL;
+                raw[0] = scalar_of(d, "amplitude"); raw[1] = scalar_of(d, "period");
+                if (!vector_of(d, "direction", raw + 2)) throw std::runtime_error("MotionSineDirectional needs direction");
+            } else if (type == "Motion01Mask") {
+                mo.type = SDFIBM_MOTION_01MASK;
+                const std::string mask = word_of(d, "mask");
+                if (mask.empty() || mask[0] != 'b') throw std::runtime_error("Mask starts with b");
+                if (mask.size() != 7) throw std::runtime_error("Mask size != 7");
+                for (int i = 1; i <= 6; ++i) {
+                    if (mask[i] != '0' && mask[i] != '1') throw std::runtime_error("Mask ele != 0 or 1");
+                    raw[i - 1] = mask[i] == '0' ? 0 : 1;
+                }
+            } else if (type == "MotionRotor") {
+                mo.type = SDFIBM_MOTION_ROTOR;
+                raw[0] = scalar_of(d, "period"); raw[1] = scalar_of(d, "radius");
+                raw[2] = scalar_of(d, "theta0"); raw[3] = scalar_of(d, "selfom");
+            } else if (type == "MotionOpenClose") {
+                mo.type = SDFIBM_MOTION_OPENCLOSE;
+            } else {
+                throw std::runtime_error("Unrecognized motion type " + type);
+            }
+            sdfibm_host_make_motion(mo.type, raw, mo.p);
+            motions[name] = mo;
+        }
+        std::map<std::string, double> materials;
+        for (auto& e : root->sub("materials").entries) {
+            const Node& d = *e.second;
+            if (word_of(d, "type") != "General") throw std::runtime_error("Unrecognizable material parameter!");
+            materials[word_of(d, "name")] = scalar_of(d, "rho");
+        }
+        const Node& sol = root->sub("solids");
+        int32_t n = 0;
+        for (auto& e : sol.entries) {
+            const Node& d = *e.second;
+            double pos[3], vel[3] = {0, 0, 0}, euler[3] = {0, 0, 0}, omega[3] = {0, 0, 0};
+            if (!vector_of(d, "pos", pos)) throw std::runtime_error("solid without pos");
+            if (twod && pos[2] != 0)
+                throw std::runtime_error("Solid must has z=0 in 2D simulation, violated by solid # " + std::to_string(n));
+            vector_of(d, "vel", vel);
+            vector_of(d, "euler", euler);
+            vector_of(d, "omega", omega);
+            const std::string mot = word_of(d, "mot_name"), mat = word_of(d, "mat_name"), shp = word_of(d, "shp_name");
+            auto si = shapes.find(shp);
+            if (si == shapes.end()) throw std::runtime_error("unknown shape name " + shp);
+            auto mi = materials.find(mat);
+            if (mi == materials.end()) throw std::runtime_error("unknown material name " + mat);
+            int mtype = SDFIBM_MOTION_FREE;
+            const double* mp = nullptr;
+            if (mot != "free") {
+                // m_libmotion[name] of an unknown name is a null motion, i.e. free (solidcloud.cpp:185-186)
+                auto it = motions.find(mot);
+                if (it != motions.end()) { mtype = it->second.type; mp = it->second.p; }
+            }
+            int ftype = SDFIBM_FORCER_NONE;
+            const double* fp = nullptr;
+            if (d.find("for_name")) {
+                const std::string fn = word_of(d, "for_name");
+                auto it = forcers.find(fn);
+                if (it == forcers.end()) throw std::runtime_error("Unrecognized force name " + fn);
+                ftype = it->second.type;
+                fp = it->second.p;
+            }
+            if (n < capacity && solids) {
+                if (sdfibm_host_make_solid(n, &si->second, mi->second, mtype, mp, ftype, fp, pos, euler, vel, omega,
+                                           &solids[n]) != SDFIBM_OK)
+                    throw std::runtime_error("bad solid " + std::to_string(n));
+            }
+            ++n;
+        }
+        *nsolids = n;
+        if (n > capacity) return err("solid capacity too small");
+    } catch (const std::exception& e) {
+        return err(e.what());
+    }
+    return SDFIBM_OK;
+}

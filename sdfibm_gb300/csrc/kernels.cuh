@@ -1,0 +1,123 @@
+// Internal device-side records shared by the kernels and the C ABI implementation.
+#pragma once
+#include <cstdint>
+
+#include "device_math.cuh"
+
+namespace sdfibm_dev {
+
+struct MeshK {
+    int32_t nx, ny, nz, twod;
+    double o[3], h[3];
+    float h32[3];
+    int64_t ncells;
+    double V;  // hx*hy*hz
+};
+
+// Static per-solid record (built once by sdfibm_cuda_create).
+struct SolidK {
+    ShapeK shape;
+    int32_t infinite;        // Plane: the bbox is the whole mesh
+    int32_t ext[3];          // static bbox extent in cells (per axis)
+    int32_t tdim[3];         // cells per tile per axis
+    int32_t ntile[3];        // tiles per axis
+    int32_t tile_base;       // first work item of this solid in the classify queue
+    int32_t bitmap_global;   // 1: the connect kernel keeps its bitmaps in global memory
+    int64_t scratch_off;     // byte offset of the bbox class array
+    int64_t bitmap_off;      // word offset of the global bitmaps (bitmap_global == 1)
+    int32_t motion_type, forcer_type, collision_id, pad;
+    double radiusB;
+    double rho, mass, mass_inv;
+    double moi_inv[9];
+    double motion_p[8];
+    double forcer_p[8];
+};
+
+// Per-interact record of each solid (written by plan_kernel).
+struct SolidPlan {
+    int32_t lo[3];            // bbox lower cell index (may lie outside the mesh)
+    int32_t err;              // nonzero: bbox too small for the current pose
+    int64_t seed;             // meshSearch::findNearestCell result
+    unsigned long long min_cand;  // lowest cell label with an inside vertex (atomicMin), ~0 when none
+    float M[9];               // FP32 world->local matrix (|q|^2 R^T)
+    int32_t n_inside, n_cut;  // touched cells by kind
+};
+
+// Global counters / flags (one record per context, device memory).
+struct Counters {
+    int32_t classify_next;
+    int32_t couple_next;
+    int32_t finalize_next;
+    int32_t n_inside;         // entries in the ALL_INSIDE list
+    int32_t n_cut;            // entries in the cut-cell list
+    int32_t n_shared;         // cells touched by two or more solids this call (slots used in the shared table)
+    int32_t pad0;
+    int32_t error;            // first error code seen on the device
+    unsigned long long exact_rechecks;  // FP32-undecided points re-evaluated in FP64
+    unsigned long long bbox_cells;
+    int32_t launches;
+    int32_t pad;
+    int64_t list_cap;         // capacity of each touched-cell list (set once at create)
+};
+
+// list lengths clamped to the capacity (a capacity error leaves the counters above what was written)
+__host__ __device__ inline int32_t clamp_len(int32_t n, int64_t cap) { return (int32_t)(n < cap ? n : cap); }
+
+struct CoupleArgs {
+    MeshK m;
+    const SolidK* sk;
+    const sdfibm_solid_state* st;
+    const SolidPlan* plan;
+    const int32_t* in_cell;
+    const int32_t* in_solid;
+    const int32_t* cut_cell;
+    const int32_t* cut_solid;
+    const float* U;
+    float* As;
+    float* Fs;
+    float* Ts;
+    int32_t* Ct;
+    double* ftacc;  // [S][6] sums of f*V/dt and (C-x)^f*V/dt
+    Counters* cnt;
+    double dtINV;
+    int method;
+    int subsample_n;
+    int exact_forcing;
+    // FP64 accumulation of the cells shared by several solids (open addressing, key -1 = empty)
+    int32_t* sh_keys;
+    double* sh_vals;   // [slot][5]: As, Ts, Fs.x, Fs.y, Fs.z
+    int32_t* sh_used;  // slots filled this call
+    int32_t sh_mask;
+};
+
+// Ct during a call holds claim words: CT_KEY_BASE | (solid << 2 | type), with CT_SHARED set once a second solid
+// touched the cell (the low bits then hold the largest claim, i.e. the last solid in the reference's serial order)
+constexpr uint32_t CT_KEY_BASE = 1u << 30;
+constexpr uint32_t CT_SHARED = 1u << 31;
+constexpr int SHARED_MAX_PROBES = 64;
+
+// UGrid (src/libcollision/ugrid.h:14-58): bbox of the mesh, spacing 2*max radiusB, row-major i*ny*nz + j*nz + k
+struct GridK {
+    double low[3];
+    double dINV;
+    int32_t nx, ny, nz, nynz;
+    int64_t ncell;
+};
+
+// list entry word: solid index in bits 0..29, cell type (1 all inside, 2 centre inside, 3 centre outside) in 30..31
+constexpr int LIST_TYPE_SHIFT = 30;
+constexpr int32_t LIST_SOLID_MASK = (1 << LIST_TYPE_SHIFT) - 1;
+__host__ __device__ inline int32_t list_word(int32_t solid, int type) {
+    return (int32_t)((uint32_t)solid | ((uint32_t)type << LIST_TYPE_SHIFT));
+}
+__host__ __device__ inline int list_type(int32_t w) { return (int)((uint32_t)w >> LIST_TYPE_SHIFT); }
+
+enum DeviceError : int32_t {
+    DERR_NONE = 0,
+    DERR_CAPACITY = 1,     // a list outgrew its capacity
+    DERR_BBOX = 2,         // a solid's region left its static bbox (tilted 2-D shape)
+    DERR_FLOOD_LIMIT = 3,  // flood fill hit its iteration bound
+    DERR_SHARED_TABLE = 4  // the shared-cell table is full
+};
+
+}  // namespace sdfibm_dev

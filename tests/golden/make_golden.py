@@ -1,0 +1,76 @@
+"""Regenerates the golden fixtures of tests/golden from the reference checkout (run in a container that has it).
+
+  re200_As.npz          the As field the reference ships for examples/flow_past_cylinder/re200 (0/As, written by
+                        SolidCloud::initialCorrect: a static circle r=1 at the origin, 78400-cell multi-block mesh).
+                        Kept: the 14400 cells of the uniform centre block (h=0.1 on [-6,6]^2, cell offset 20800).
+  falling_ellipse.npz   the oracle run on the reference's own OpenFOAM polyMesh of examples/falling_ellipse
+                        (100x200x1 cells, ellipse 0.3x0.15 at (0.5,3.5), euler z=-45 deg): touched cells, As, forcing.
+                        It pins the uniform-mesh ordering conventions against a real OpenFOAM mesh.
+Usage: python tests/golden/make_golden.py /path/to/reference
+"""
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", ".."))
+
+
+def read_foam_list(path, dtype, ncomp=1):
+    b = open(path, "rb").read()
+    i = b.index(b"}")
+    m = re.compile(rb"\n(\d+)\n\(").search(b, i)
+    n = int(m.group(1))
+    s = m.end()
+    a = np.frombuffer(b[s:s + n * ncomp * np.dtype(dtype).itemsize], dtype=dtype)
+    return (a.reshape(n, ncomp) if ncomp > 1 else a), b[s + n * ncomp * np.dtype(dtype).itemsize:]
+
+
+def read_faces(path):
+    b = open(path, "rb").read()
+    i = b.index(b"}")
+    m = re.compile(rb"\n(\d+)\n\(").search(b, i)
+    n = int(m.group(1))
+    s = m.end()
+    off = np.frombuffer(b[s:s + n * 4], dtype="<i4")
+    rest = b[s + n * 4:]
+    m2 = re.compile(rb"\n(\d+)\n\(").search(rest)
+    n2 = int(m2.group(1))
+    lab = np.frombuffer(rest[m2.end():m2.end() + n2 * 4], dtype="<i4")
+    return off, lab
+
+
+def main(ref):
+    from oracle.oracle import OracleCloud
+    from sdfibm_gb300 import abi
+    from sdfibm_gb300.host import make_shape, make_solid, mask_motion
+    As, _ = read_foam_list(os.path.join(ref, "examples/flow_past_cylinder/re200/0/As"), "<f8")
+    assert len(As) == 78400
+    centre = np.ascontiguousarray(As[20800:20800 + 14400])
+    np.savez_compressed(os.path.join(HERE, "re200_As.npz"), As=centre, nx=120, ny=120,
+                        origin=np.array([-6.0, -6.0, -0.5]), h=np.array([0.1, 0.1, 1.0]))
+    pm = os.path.join(ref, "examples/falling_ellipse/constant/polyMesh")
+    pts, _ = read_foam_list(os.path.join(pm, "points"), "<f8", 3)
+    own, _ = read_foam_list(os.path.join(pm, "owner"), "<i4")
+    nei, _ = read_foam_list(os.path.join(pm, "neighbour"), "<i4")
+    off, lab = read_faces(os.path.join(pm, "faces"))
+    shape = make_shape("Ellipse", radiusa=0.3, radiusb=0.15)
+    solid = make_solid(0, shape, 2.0, (0.5, 3.5, 0.0), (0.0, 0.0, -45.0), motion=mask_motion("b111111"))
+    mesh = abi.mesh_desc((100, 200, 1), (0.0, 0.0, -0.5), (0.02, 0.02, 1.0), twod=1)
+    opt = abi.options(rho_f=1.0)
+    oc = OracleCloud(mesh, [solid], opt, polymesh=(pts, off, lab, own, nei))
+    N = oc.N
+    rng = np.random.default_rng(7)
+    U = (rng.standard_normal((3, N), dtype=np.float32) * np.float32(0.1)).astype(np.float64)
+    f = oc.new_fields()
+    FT = oc.interact(0.0, 0.01, U, f)
+    cells, types = oc.touched(0)
+    np.savez_compressed(os.path.join(HERE, "falling_ellipse.npz"), cells=cells, types=types, As=f["As"][cells],
+                        Fs=f["Fs"].reshape(3, N)[:, cells], FT=FT, U_seed=7, U_std=0.1, dt=0.01)
+    print("re200: %d nonzero; falling_ellipse: %d touched cells, FT=%s" % ((centre > 0).sum(), len(cells), FT))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

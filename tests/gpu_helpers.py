@@ -1,0 +1,96 @@
+"""Shared helpers of the GPU parity tests: run one workload through libsdfibm_cuda.so and through the oracle."""
+import numpy as np
+
+from oracle.oracle import OracleCloud
+from sdfibm_gb300 import abi
+from sdfibm_gb300.cloud import SolidCloud
+
+# tolerances (stated by the coupling contract)
+AS_REL, AS_ABS = 1e-5, 1e-9      # As, Ts and Fs per cell: |d| <= 1e-5 |ref| + 1e-9
+FT_REL = 1e-6                    # force/torque per solid, normwise against the sum of |contributions|
+
+
+def run_pair(torch, w, steps=1, evolve=False, fix=False, U=None):
+    """Runs `steps` interact (+evolve, +fixInternal) on the GPU and on the fast oracle; returns both sides."""
+    Uh = w.U_numpy() if U is None else U
+    gpu = SolidCloud(w.mesh, w.solids, w.opt)
+    orc = OracleCloud(w.mesh, w.solids, w.opt, faithful=False)
+    Ud = torch.from_numpy(Uh).cuda()
+    Uo = Uh.astype(np.float64).reshape(-1).copy()
+    fd = gpu.new_fields()
+    fo = orc.new_fields()
+    out = []
+    t = 0.0
+    for _ in range(steps):
+        FTg = gpu.interact(t, w.dt, Ud, fd)
+        FTo = orc.interact(t, w.dt, Uo, fo)
+        out.append((FTg, FTo))
+        if evolve:
+            gpu.evolve(t, w.dt)
+            orc.evolve(t, w.dt)
+        if fix:
+            gpu.fix_internal(fd["Ct"], Ud)
+            Uo = orc.fix_internal(fo["Ct"], Uo)
+        t += w.dt
+    torch.cuda.synchronize()
+    return dict(gpu=gpu, orc=orc, fd=fd, fo=fo, FT=out, Ud=Ud, Uo=Uo)
+
+
+def ft_scale(w, orc, fo_U, s):
+    """rho_f * V/dt * sum over the solid's cells of |U - u_s| (and of |C-x| |U - u_s| for the torque)."""
+    cells, _ = orc.touched(s)
+    N = orc.N
+    U = fo_U.reshape(3, N)[:, cells]
+    st = orc.get_state()[s]
+    C = np.array([_centre(w.mesh, c) for c in cells]).T if len(cells) else np.zeros((3, 0))
+    x = np.array(st.pos)[:, None]
+    v = np.array(st.vel)[:, None]
+    om = np.array(st.omega)
+    d = C - x
+    us = v + np.cross(om, d.T).T
+    fm = np.linalg.norm(U - us, axis=0) * 1.5  # alpha <= ~1.5 for REF-GEO cut cells
+    V = w.mesh.h[0] * w.mesh.h[1] * w.mesh.h[2]
+    k = w.opt.rho_f * V / w.dt
+    return k * fm.sum() + 1e-300, k * (np.linalg.norm(d, axis=0) * fm).sum() + 1e-300
+
+
+def _centre(m, c):
+    i = c % m.nx
+    j = (c // m.nx) % m.ny
+    k = c // (m.nx * m.ny)
+    return (m.origin[0] + (i + 0.5) * m.h[0], m.origin[1] + (j + 0.5) * m.h[1], m.origin[2] + (k + 0.5) * m.h[2])
+
+
+def check_interact(w, r, U_used=None):
+    """Asserts the coupling contract on the last interact of run_pair; returns a summary dict."""
+    gpu, orc, fd, fo = r["gpu"], r["orc"], r["fd"], r["fo"]
+    N = orc.N
+    S = len(w.solids)
+    ncells = 0
+    for s in range(S):
+        cg, tg = gpu.touched(s)
+        co, to = orc.touched(s)
+        assert np.array_equal(cg, co), "touched cells of solid %d differ (%d vs %d)" % (s, len(cg), len(co))
+        assert np.array_equal(tg, to), "cell types of solid %d differ" % s
+        ncells += len(co)
+    Ct = fd["Ct"].cpu().numpy()
+    assert np.array_equal(Ct, fo["Ct"]), "Ct differs in %d cells" % int((Ct != fo["Ct"]).sum())
+    for key in ("As", "Ts"):
+        g = fd[key].cpu().numpy().astype(np.float64)
+        o = fo[key]
+        bad = np.abs(g - o) > AS_REL * np.abs(o) + AS_ABS
+        assert not bad.any(), "%s differs in %d cells, worst %g vs %g" % (key, bad.sum(), g[bad][0], o[bad][0])
+    g = fd["Fs"].cpu().numpy().astype(np.float64).reshape(-1)
+    o = fo["Fs"]
+    bad = np.abs(g - o) > AS_REL * np.abs(o) + AS_ABS
+    assert not bad.any(), "Fs differs in %d entries" % bad.sum()
+    FTg, FTo = r["FT"][-1]
+    Uo = r["Uo"] if U_used is None else U_used
+    worst = 0.0
+    for s in range(S):
+        sf, st = ft_scale(w, orc, Uo, s)
+        ef = np.linalg.norm(FTg[s, :3] - FTo[s, :3]) / sf
+        et = np.linalg.norm(FTg[s, 3:] - FTo[s, 3:]) / st
+        worst = max(worst, ef, et)
+        assert ef <= FT_REL and et <= FT_REL, "solid %d force/torque error %g %g" % (s, ef, et)
+    return dict(coupling_cells=ncells, ft_err=worst)

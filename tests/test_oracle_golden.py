@@ -1,0 +1,63 @@
+"""The oracle pinned against the reference's shipped artefacts (CPU)."""
+import numpy as np
+
+from conftest import golden
+from oracle.oracle import OracleCloud
+from sdfibm_gb300 import abi
+from sdfibm_gb300.host import make_shape, make_solid, mask_motion
+
+# cell (j=50, i=57) of the re200 centre block holds 1.0 in the shipped field while the shipped serial algorithm gives
+# 0.6685 for every possible vertex order: it is excluded and reported (see the fixture script).
+RE200_FLAGGED = [(50, 57)]
+
+
+def re200_case(faithful=True):
+    g = golden("re200_As.npz")
+    mesh = abi.mesh_desc((120, 120, 1), g["origin"], g["h"], twod=1)
+    solid = make_solid(0, make_shape("Circle", radius=1.0), 1.0, (0, 0, 0), motion=mask_motion("b000000"))
+    oc = OracleCloud(mesh, [solid], abi.options(rho_f=1.0), faithful=faithful)
+    f = oc.new_fields()
+    oc.interact(0.0, 1.0, np.zeros(3 * oc.N), f)   # SolidCloud::initialCorrect = interact(0, 1)
+    return g["As"].reshape(120, 120), f["As"].reshape(120, 120)
+
+
+def test_re200_golden_As():
+    ref, got = re200_case()
+    mask = np.ones_like(ref, dtype=bool)
+    for j, i in RE200_FLAGGED:
+        mask[j, i] = False
+    d = np.abs(ref - got)
+    # 346 cells bit-for-bit up to 1e-12; 5 cells where blockMesh's point coordinates put a vertex on the circle to
+    # rounding hold As < 1e-9 in the shipped field and 0 here
+    assert d[mask].max() < 1e-9
+    assert (d[mask] < 1e-12).sum() >= 346
+    assert (got > 0).sum() == 346 and (ref > 0).sum() == 352
+    assert (got == 1).sum() == 276 and (ref == 1).sum() == 276
+    # the flagged cell is a genuine cut cell in the serial algorithm
+    assert 0.6 < got[50, 57] < 0.7 and ref[50, 57] == 1.0
+
+
+def test_re200_total_area():
+    ref, got = re200_case()
+    assert abs((got * 0.01).sum() - 3.1352207447) < 1e-9
+    assert abs((ref * 0.01).sum() - 3.1385353449) < 1e-9
+
+
+def test_falling_ellipse_uniform_matches_polymesh():
+    """The implicit uniform mesh (closed-form geometry, OpenFOAM ordering) reproduces the oracle run on the
+    reference's own OpenFOAM polyMesh of examples/falling_ellipse."""
+    g = golden("falling_ellipse.npz")
+    shape = make_shape("Ellipse", radiusa=0.3, radiusb=0.15)
+    solid = make_solid(0, shape, 2.0, (0.5, 3.5, 0.0), (0.0, 0.0, -45.0), motion=mask_motion("b111111"))
+    mesh = abi.mesh_desc((100, 200, 1), (0.0, 0.0, -0.5), (0.02, 0.02, 1.0), twod=1)
+    oc = OracleCloud(mesh, [solid], abi.options(rho_f=1.0), faithful=False)
+    N = oc.N
+    rng = np.random.default_rng(int(g["U_seed"]))
+    U = (rng.standard_normal((3, N), dtype=np.float32) * np.float32(g["U_std"])).astype(np.float64)
+    f = oc.new_fields()
+    FT = oc.interact(0.0, float(g["dt"]), U, f)
+    cells, types = oc.touched(0)
+    assert np.array_equal(cells, g["cells"]) and np.array_equal(types, g["types"])
+    assert np.abs(f["As"][cells] - g["As"]).max() < 1e-12
+    assert np.abs(f["Fs"].reshape(3, N)[:, cells] - g["Fs"]).max() < 1e-9
+    assert np.abs(FT - g["FT"]).max() < 1e-12 * np.abs(g["FT"]).max() + 1e-15
