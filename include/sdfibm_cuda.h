@@ -192,6 +192,20 @@ int sdfibm_cuda_set_solids(sdfibm_ctx* ctx, const sdfibm_solid_state* in, int32_
 int sdfibm_cuda_touched(sdfibm_ctx* ctx, int32_t solid, int64_t* cells, int8_t* types, int64_t capacity,
                         int64_t* n);
 
+/* No counterpart in the reference.  The touched cells of ONE solid (the same list and order as sdfibm_cuda_touched
+ * returns after an interact) computed without allocating any device memory, for callers that cannot call
+ * cudaMalloc: hosts whose device memory is owned entirely by their own pool allocator, or latency-critical loops
+ * that cannot afford the device-wide synchronisation of cudaMalloc/cudaFree.  The work space is one file-scope
+ * device array of about 10 MiB, reserved on every GPU that loads the library until the process exits.
+ * Limit: the solid's bounding box may hold at most 524288 cells (and 262144 flood-fill bitmap words); larger solids
+ * are rejected with SDFIBM_ERR_CAPACITY.  The first call on a device looks up the array's address with that device
+ * current: make it before any stream capture.  Calls share the array, so calls that overlap on the GPU race; issue
+ * them on one stream.  cells (int32) and types (int8, 1/2/3) are device buffers of `capacity` entries; *n_device
+ * (device int64) receives the full count, or -(status) when the enumeration failed on the device.  Asynchronous on
+ * cuda_stream (NULL: the legacy default stream). */
+int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* solid, void* cuda_stream,
+                                int32_t* cells, int8_t* types, int64_t capacity, int64_t* n_device);
+
 /* Counters of the last interact (host): [0] coupling cells (sum over solids of |T_s|), [1] cut cells,
  * [2] bbox cells scanned, [3] vertices re-checked in FP64, [4] work items, [5] kernel launches. */
 int sdfibm_cuda_stats(sdfibm_ctx* ctx, int64_t* out, int32_t n);

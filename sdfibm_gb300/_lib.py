@@ -17,7 +17,7 @@ CUDA_SYMBOLS = [
     "sdfibm_cuda_evolve", "sdfibm_cuda_fix_internal", "sdfibm_cuda_get_solids", "sdfibm_cuda_set_solids",
     "sdfibm_cuda_touched", "sdfibm_cuda_stats", "sdfibm_cuda_kernel_times", "sdfibm_cuda_last_error",
     "sdfibm_cuda_version",
-    "sdfibm_cuda_destroy",
+    "sdfibm_cuda_destroy", "sdfibm_cuda_touched_noalloc",
 ]
 HOST_SYMBOLS = [
     "sdfibm_host_make_shape", "sdfibm_host_make_motion", "sdfibm_host_make_forcer", "sdfibm_host_quat_from_euler_deg",
@@ -50,6 +50,7 @@ def load():
     L.sdfibm_cuda_touched.argtypes = [vp, i32, vp, vp, i64, P(i64)]
     L.sdfibm_cuda_stats.argtypes = [vp, P(i64), i32]
     L.sdfibm_cuda_kernel_times.argtypes = [vp, P(C.c_char_p), P(dbl), i32, P(i32)]
+    L.sdfibm_cuda_touched_noalloc.argtypes = [P(abi.MeshDesc), P(abi.SolidDesc), vp, vp, vp, i64, vp]
     L.sdfibm_cuda_last_error.argtypes = [vp]
     L.sdfibm_cuda_last_error.restype = C.c_char_p
     L.sdfibm_cuda_version.restype = C.c_char_p
