@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libsdfibm_cuda.so")
 BUILD_DIR = os.path.join(HERE, "_build")
-CU_SOURCES = ["coupling.cu", "evolve.cu", "capi.cu", "noalloc.cu"]
+CU_SOURCES = ["classify.cu", "coupling.cu", "evolve.cu", "capi.cu", "noalloc.cu"]
 CXX_SOURCES = ["host.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -27,7 +27,7 @@ def nvcc():
 
 
 def _sources():
-    return [os.path.join(CSRC, f) for f in CU_SOURCES + CXX_SOURCES + ["device_math.cuh", "kernels.cuh"]] + [
+    return [os.path.join(CSRC, f) for f in CU_SOURCES + CXX_SOURCES + ["device_math.cuh", "kernels.cuh", "common.cuh"]] + [
         os.path.join(HERE, "..", "include", h) for h in ("sdfibm_cuda.h", "sdfibm_host.h")]
 
 

@@ -15,8 +15,7 @@ namespace sdfibm_dev {
 // coupling.cu
 __global__ void plan_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state* st, SolidPlan* plan, int S,
                             Counters* cnt);
-__global__ void classify_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state* st, SolidPlan* plan,
-                                const int32_t* tile_prefix, int S, int total_tiles, uint8_t* scratch, Counters* cnt);
+__global__ void classify_kernel(ClassifyArgs A);
 __global__ void connect_kernel(MeshK m, const SolidK* sk, SolidPlan* plan, const uint8_t* scratch, uint32_t* gbitmaps,
                                int32_t* in_cell, int32_t* in_solid, int32_t* cut_cell, int32_t* cut_solid,
                                int64_t cap_in, int64_t cap_cut, Counters* cnt, int smem_words);
@@ -77,6 +76,7 @@ struct sdfibm_ctx {
     int32_t* d_tile_prefix = nullptr;
     int total_tiles = 0;
     uint8_t* d_scratch = nullptr;
+    float* d_alpha = nullptr;  // solid fraction per bbox cell (same indexing as d_scratch)
     int64_t scratch_bytes = 0;
     uint32_t* d_gbitmaps = nullptr;
     int64_t gbitmap_words = 0;
@@ -246,10 +246,11 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
             // a 2-D shape that does not rotate about z: its prism may cross the whole mesh
             for (int a = 0; a < 2; ++a) k.ext[a] = n3[a] + 4;
         }
-        const int tz = std::min(8, k.ext[2]);
-        k.tdim[2] = tz;
-        k.tdim[0] = tz <= 2 ? 32 : 8;
-        k.tdim[1] = tz <= 2 ? 16 : 8;
+        // warp tiles: 4x4x4 cells, or 8x8 x (1 or 2) on one- and two-layer meshes
+        const int tz = std::min(4, k.ext[2]);
+        k.tdim[2] = tz <= 2 ? tz : 4;
+        k.tdim[0] = tz <= 2 ? 8 : 4;
+        k.tdim[1] = tz <= 2 ? 8 : 4;
         for (int a = 0; a < 3; ++a) k.ntile[a] = (k.ext[a] + k.tdim[a] - 1) / k.tdim[a];
         k.tile_base = (int32_t)tiles;
         tiles += (int64_t)k.ntile[0] * k.ntile[1] * k.ntile[2];
@@ -320,7 +321,7 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
 
     // device allocations
     if (dalloc(&ctx->d_sk, nsolids) || dalloc(&ctx->d_st, nsolids) || dalloc(&ctx->d_plan, nsolids) ||
-        dalloc(&ctx->d_tile_prefix, nsolids + 1) || dalloc(&ctx->d_scratch, scratch) ||
+        dalloc(&ctx->d_tile_prefix, nsolids + 1) || dalloc(&ctx->d_scratch, scratch) || dalloc(&ctx->d_alpha, scratch) ||
         dalloc(&ctx->d_gbitmaps, gwords) || dalloc(&ctx->d_in_cell, ctx->cap) || dalloc(&ctx->d_in_solid, ctx->cap) ||
         dalloc(&ctx->d_cut_cell, ctx->cap) || dalloc(&ctx->d_cut_solid, ctx->cap) || dalloc(&ctx->d_cnt, 1) ||
         dalloc(&ctx->d_ftacc, 6 * (size_t)nsolids) || dalloc(&ctx->d_ft, 6 * (size_t)nsolids) ||
@@ -432,9 +433,11 @@ int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U
         CK(cudaMemsetAsync(ctx->d_ftacc, 0, sizeof(double) * 6 * S, st));
         plan_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->mesh, ctx->d_sk, ctx->d_st, ctx->d_plan, S, ctx->d_cnt);
         mark(ctx, "plan_kernel");
-        classify_kernel<<<ctx->classify_grid, 256, 0, st>>>(ctx->mesh, ctx->d_sk, ctx->d_st, ctx->d_plan,
-                                                            ctx->d_tile_prefix, S, ctx->total_tiles, ctx->d_scratch,
-                                                            ctx->d_cnt);
+        ClassifyArgs CA;
+        CA.m = ctx->mesh; CA.sk = ctx->d_sk; CA.st = ctx->d_st; CA.plan = ctx->d_plan; CA.tile_prefix = ctx->d_tile_prefix;
+        CA.S = S; CA.total_tiles = ctx->total_tiles; CA.cls = ctx->d_scratch; CA.alpha = ctx->d_alpha; CA.cnt = ctx->d_cnt;
+        CA.method = ctx->opt.fraction_method; CA.subsample_n = ctx->opt.subsample_n;
+        classify_kernel<<<ctx->classify_grid, 256, 0, st>>>(CA);
         mark(ctx, "classify_kernel");
         connect_kernel<<<S, 512, ctx->connect_smem_bytes, st>>>(ctx->mesh, ctx->d_sk, ctx->d_plan, ctx->d_scratch,
                                                                 ctx->d_gbitmaps, ctx->d_in_cell, ctx->d_in_solid,
@@ -447,7 +450,7 @@ int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U
         CoupleArgs A;
         A.m = ctx->mesh; A.sk = ctx->d_sk; A.st = ctx->d_st; A.plan = ctx->d_plan;
         A.in_cell = ctx->d_in_cell; A.in_solid = ctx->d_in_solid; A.cut_cell = ctx->d_cut_cell;
-        A.cut_solid = ctx->d_cut_solid; A.U = U; A.As = As; A.Fs = Fs; A.Ts = Ts; A.Ct = Ct;
+        A.cut_solid = ctx->d_cut_solid; A.alpha = ctx->d_alpha; A.U = U; A.As = As; A.Fs = Fs; A.Ts = Ts; A.Ct = Ct;
         A.ftacc = ctx->d_ftacc; A.cnt = ctx->d_cnt; A.dtINV = 1.0 / dt;
         A.method = ctx->opt.fraction_method; A.subsample_n = ctx->opt.subsample_n;
         A.exact_forcing = ctx->opt.exact_forcing;
@@ -626,7 +629,7 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
     void* dev[] = {ctx->d_sk, ctx->d_st, ctx->d_plan, ctx->d_tile_prefix, ctx->d_scratch, ctx->d_gbitmaps,
                    ctx->d_in_cell, ctx->d_in_solid, ctx->d_cut_cell, ctx->d_cut_solid, ctx->d_cnt, ctx->d_ftacc,
                    ctx->d_ft, ctx->d_hash, ctx->d_gcount, ctx->d_gstart, ctx->d_gcursor, ctx->d_glist, ctx->d_U,
-                   ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, ctx->d_sh_keys, ctx->d_sh_vals, ctx->d_sh_used};
+                   ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, ctx->d_alpha, ctx->d_sh_keys, ctx->d_sh_vals, ctx->d_sh_used};
     for (void* p : dev)
         if (p) cudaFree(p);
     if (ctx->ev_ready)

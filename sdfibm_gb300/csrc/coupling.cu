@@ -17,27 +17,14 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-#include "kernels.cuh"
+#include "common.cuh"
 
 namespace sdfibm_dev {
 
 
-__device__ inline void set_error(Counters* cnt, int32_t code) { atomicCAS(&cnt->error, 0, code); }
-
-// ---- geometry helpers (closed form of the uniform mesh, identical to the oracle's UniformMesh) ----------------------
-__device__ inline double mesh_coord(const MeshK& m, int a, int64_t i) { return m.o[a] + (double)i * m.h[a]; }
-__device__ inline double mesh_centre(const MeshK& m, int a, int64_t i) { return m.o[a] + ((double)i + 0.5) * m.h[a]; }
-__device__ inline D3 mesh_point(const MeshK& m, int64_t i, int64_t j, int64_t k) {
-    return D3{mesh_coord(m, 0, i), mesh_coord(m, 1, j), mesh_coord(m, 2, k)};
-}
-__device__ inline D3 mesh_C(const MeshK& m, int64_t i, int64_t j, int64_t k) {
-    return D3{mesh_centre(m, 0, i), mesh_centre(m, 1, j), mesh_centre(m, 2, k)};
-}
-
-__device__ inline Q4 state_quat(const sdfibm_solid_state& s) { return Q4{s.quat[0], D3{s.quat[1], s.quat[2], s.quat[3]}}; }
-__device__ inline D3 state_pos(const sdfibm_solid_state& s) { return D3{s.pos[0], s.pos[1], s.pos[2]}; }
-
 // ---- plan ---------------------------------------------------------------------------------------------------------
+__device__ inline int32_t n3v(const MeshK& m, int a) { return a == 0 ? m.nx : (a == 1 ? m.ny : m.nz); }
+
 __global__ void plan_kernel(MeshK m, const SolidK* __restrict__ sk, const sdfibm_solid_state* __restrict__ st,
                             SolidPlan* __restrict__ plan, int S, Counters* cnt) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -58,6 +45,9 @@ __global__ void plan_kernel(MeshK m, const SolidK* __restrict__ sk, const sdfibm
     }
     p.err = 0;
     const int32_t n[3] = {m.nx, m.ny, m.nz};
+    p.cw[0] = p.cw[1] = p.cw[2] = 0.0;
+    p.rcull = 0.0;
+    for (int a = 0; a < 3; ++a) { p.vlo[a] = 0; p.vhi[a] = n3v(m, a); }
     if (k.infinite) {
         p.lo[0] = p.lo[1] = p.lo[2] = 0;
     } else {
@@ -77,6 +67,32 @@ __global__ void plan_kernel(MeshK m, const SolidK* __restrict__ sk, const sdfibm
             const double zspan = dmax(fabs(zhi - cw.z), fabs(zlo - cw.z));
             const double rxy = (sxy > 0) ? r + (zspan + r * sxy) / dmax(az, 0.3) * sxy : r;
             rad[0] = rad[1] = rxy * (1.0 + 1e-9);
+        }
+        p.cw[0] = cw.x; p.cw[1] = cw.y; p.cw[2] = cw.z;
+        p.rcull = rad[0];
+        // oriented bounding box of the inside region: half extents along the world axes
+        {
+            const double qq = q.w * q.w + magSqr(q.v);
+            const D3 ex = qtransform(q, D3{1, 0, 0}) / qq, ey = qtransform(q, D3{0, 1, 0}) / qq,
+                     ez = qtransform(q, D3{0, 0, 1}) / qq;  // columns of the unit rotation
+            const double Rm[3][3] = {{ex.x, ey.x, ez.x}, {ex.y, ey.y, ez.y}, {ex.z, ey.z, ez.z}};
+            double e[3] = {rad[0], rad[1], rad[2]};
+            const double* sp = k.shape.p;
+            if (k.shape.type == SDFIBM_SHAPE_ELLIPSOID) {
+                for (int a = 0; a < 3; ++a)
+                    e[a] = sqrt(Rm[a][0] * Rm[a][0] * sp[0] * sp[0] + Rm[a][1] * Rm[a][1] * sp[1] * sp[1] +
+                                Rm[a][2] * Rm[a][2] * sp[2] * sp[2]);
+            } else if (k.shape.type == SDFIBM_SHAPE_BOX) {
+                for (int a = 0; a < 3; ++a) e[a] = fabs(Rm[a][0]) * sp[0] + fabs(Rm[a][1]) * sp[1] + fabs(Rm[a][2]) * sp[2];
+            }
+            const double c3v[3] = {cw.x, cw.y, cw.z};
+            for (int a = 0; a < 3; ++a) {
+                if (k.shape.prism && a == 2) continue;  // all layers
+                const double ea = dmin(e[a], rad[a]) * (1.0 + 1e-9) + 1e-12;
+                const double l = ceil((c3v[a] - ea - m.o[a]) / m.h[a]) - 1, u = floor((c3v[a] + ea - m.o[a]) / m.h[a]) + 1;
+                p.vlo[a] = (int32_t)dmin(dmax(l, -1.0), (double)n3v(m, a) + 1);
+                p.vhi[a] = (int32_t)dmin(dmax(u, -1.0), (double)n3v(m, a) + 1);
+            }
         }
         const double c3[3] = {cw.x, cw.y, cw.z};
         for (int a = 0; a < 3; ++a) {
@@ -116,158 +132,6 @@ __global__ void plan_kernel(MeshK m, const SolidK* __restrict__ sk, const sdfibm
     p.min_cand = ~0ull;
     p.n_inside = p.n_cut = 0;
     plan[s] = p;
-}
-
-// ---- inside test of one world point given as integer lattice offsets ------------------------------------------------
-// base: FP64 (point(I0,J0,K0) - x_s) of the tile; off: FP32 offset of the point from that lattice point.
-// Exact fallback evaluates the point with the mesh formula in FP64, as the oracle does.
-struct TileFrame {
-    float bx, by, bz;  // FP32 of the FP64 base vector
-    float babs;        // |base|_1
-    float e64;         // bound of the FP64 reference's own rounding of point coordinates (large meshes offsets)
-};
-__device__ inline TileFrame make_frame(const D3& b, const D3& p0, const D3& x) {
-    TileFrame tf;
-    tf.bx = (float)b.x; tf.by = (float)b.y; tf.bz = (float)b.z;
-    tf.babs = fabsf(tf.bx) + fabsf(tf.by) + fabsf(tf.bz);
-    tf.e64 = (float)(1e-15 * (fabs(p0.x) + fabs(p0.y) + fabs(p0.z) + fabs(x.x) + fabs(x.y) + fabs(x.z)));
-    return tf;
-}
-
-__device__ inline int classify_point(const ShapeK& sh, const float* M, const TileFrame& tf, float ox, float oy,
-                                     float oz, const D3& p64_exact_world, const D3& x, const Q4& q,
-                                     unsigned long long* rechecks) {
-    const float dx = tf.bx + ox, dy = tf.by + oy, dz = tf.bz + oz;
-    const float lx = __fmaf_rn(M[0], dx, __fmaf_rn(M[1], dy, M[2] * dz));
-    const float ly = __fmaf_rn(M[3], dx, __fmaf_rn(M[4], dy, M[5] * dz));
-    const float lz = __fmaf_rn(M[6], dx, __fmaf_rn(M[7], dy, M[8] * dz));
-    const float dabs = fabsf(dx) + fabsf(dy) + fabsf(dz);
-    const float E = 4.f * U32 * (tf.babs + fabsf(ox) + fabsf(oy) + fabsf(oz) + 2.f * dabs) + tf.e64 + 1e-30f;
-    int r = inside32(sh, lx, ly, lz, E);
-    if (r == 2) {
-        atomicAdd(rechecks, 1ull);
-        r = inside64(sh, world2local(p64_exact_world, x, q)) ? 1 : 0;
-    }
-    return r;
-}
-
-// ---- classify -------------------------------------------------------------------------------------------------------
-constexpr int CLS_THREADS = 256;
-constexpr int MAX_TILE_VERTS = 33 * 17 * 9;  // largest tile: 32 x 16 x 8 cells
-
-__device__ inline int find_solid(const int32_t* prefix, int S, int item) {
-    int lo = 0, hi = S;  // prefix[lo] <= item < prefix[hi]
-    while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (prefix[mid] <= item) lo = mid; else hi = mid;
-    }
-    return lo;
-}
-
-__global__ void __launch_bounds__(CLS_THREADS) classify_kernel(MeshK m, const SolidK* __restrict__ sk,
-                                                               const sdfibm_solid_state* __restrict__ st,
-                                                               SolidPlan* __restrict__ plan,
-                                                               const int32_t* __restrict__ tile_prefix, int S,
-                                                               int total_tiles, uint8_t* __restrict__ scratch,
-                                                               Counters* cnt) {
-    __shared__ uint8_t vin[MAX_TILE_VERTS];
-    __shared__ int s_item;
-    __shared__ unsigned long long s_min;
-    __shared__ unsigned long long s_rechecks;
-    __shared__ unsigned int s_valid;
-    __shared__ ShapeK s_shape;
-    __shared__ float s_M[9];
-    __shared__ TileFrame s_tf;
-    const int tid = threadIdx.x;
-    for (;;) {
-        if (tid == 0) {
-            s_item = atomicAdd(&cnt->classify_next, 1);
-            s_min = ~0ull;
-            s_rechecks = 0;
-            s_valid = 0;
-        }
-        __syncthreads();
-        const int item = s_item;
-        if (item >= total_tiles) break;
-        const int s = find_solid(tile_prefix, S, item);
-        const SolidK& k = sk[s];
-        const SolidPlan& pl = plan[s];
-        const int t = item - k.tile_base;
-        const int tx = t % k.ntile[0], ty = (t / k.ntile[0]) % k.ntile[1], tz = t / (k.ntile[0] * k.ntile[1]);
-        const int cx = min(k.tdim[0], k.ext[0] - tx * k.tdim[0]);
-        const int cy = min(k.tdim[1], k.ext[1] - ty * k.tdim[1]);
-        const int cz = min(k.tdim[2], k.ext[2] - tz * k.tdim[2]);
-        const int64_t I0 = (int64_t)pl.lo[0] + tx * k.tdim[0];
-        const int64_t J0 = (int64_t)pl.lo[1] + ty * k.tdim[1];
-        const int64_t K0 = (int64_t)pl.lo[2] + tz * k.tdim[2];
-        const Q4 q = state_quat(st[s]);
-        const D3 x = state_pos(st[s]);
-        if (tid == 0) {
-            s_shape = k.shape;
-            for (int r = 0; r < 9; ++r) s_M[r] = pl.M[r];
-            const D3 p0 = mesh_point(m, I0, J0, K0);
-            s_tf = make_frame(p0 - x, p0, x);
-        }
-        __syncthreads();
-        const int vx = cx + 1, vy = cy + 1, vz = cz + 1, nv = vx * vy * vz;
-        const bool tile_in_mesh = !(I0 + cx <= 0 || J0 + cy <= 0 || K0 + cz <= 0 || I0 >= m.nx || J0 >= m.ny || K0 >= m.nz);
-        if (tile_in_mesh && !pl.err) {
-            for (int v = tid; v < nv; v += CLS_THREADS) {
-                const int a = v % vx, b = (v / vx) % vy, c = v / (vx * vy);
-                const int64_t I = I0 + a, J = J0 + b, K = K0 + c;
-                uint8_t r = 0;
-                if (I >= 0 && J >= 0 && K >= 0 && I <= m.nx && J <= m.ny && K <= m.nz) {
-                    const float ox = (float)a * m.h32[0], oy = (float)b * m.h32[1], oz = (float)c * m.h32[2];
-                    r = (uint8_t)classify_point(s_shape, s_M, s_tf, ox, oy, oz, mesh_point(m, I, J, K), x, q,
-                                                &s_rechecks);
-                }
-                vin[v] = r;
-            }
-        }
-        __syncthreads();
-        const int nc = cx * cy * cz;
-        uint8_t* out = scratch + k.scratch_off;
-        unsigned int local_valid = 0;
-        for (int e = tid; e < nc; e += CLS_THREADS) {
-            const int a = e % cx, b = (e / cx) % cy, c = e / (cx * cy);
-            const int64_t I = I0 + a, J = J0 + b, K = K0 + c;
-            uint8_t cls = 0;
-            if (tile_in_mesh && !pl.err && I >= 0 && J >= 0 && K >= 0 && I < m.nx && J < m.ny && K < m.nz) {
-                ++local_valid;
-                int cntv = 0;
-#pragma unroll
-                for (int dz = 0; dz < 2; ++dz)
-#pragma unroll
-                    for (int dy = 0; dy < 2; ++dy)
-#pragma unroll
-                        for (int dx = 0; dx < 2; ++dx) cntv += vin[(a + dx) + vx * ((b + dy) + vy * (c + dz))];
-                if (cntv == 8) {
-                    cls = 1;
-                } else if (cntv > 0) {
-                    const float ox = ((float)a + 0.5f) * m.h32[0], oy = ((float)b + 0.5f) * m.h32[1],
-                                oz = ((float)c + 0.5f) * m.h32[2];
-                    const int ci = classify_point(s_shape, s_M, s_tf, ox, oy, oz, mesh_C(m, I, J, K), x, q,
-                                                  &s_rechecks);
-                    cls = ci ? 2 : 3;
-                }
-                if (cls) {
-                    const unsigned long long gidx = (unsigned long long)(I + (int64_t)m.nx * (J + (int64_t)m.ny * K));
-                    atomicMin(&s_min, gidx);
-                }
-            }
-            const int64_t li = (int64_t)(tx * k.tdim[0] + a) +
-                               (int64_t)k.ext[0] * ((ty * k.tdim[1] + b) + (int64_t)k.ext[1] * (tz * k.tdim[2] + c));
-            out[li] = cls;
-        }
-        if (local_valid) atomicAdd(&s_valid, local_valid);
-        __syncthreads();
-        if (tid == 0) {
-            if (s_min != ~0ull) atomicMin(&plan[s].min_cand, s_min);
-            if (s_rechecks) atomicAdd(&cnt->exact_rechecks, s_rechecks);
-            if (s_valid) atomicAdd(&cnt->bbox_cells, (unsigned long long)s_valid);
-        }
-        __syncthreads();
-    }
 }
 
 // ---- connect: bit-parallel flood fill --------------------------------------------------------------------------------
@@ -481,130 +345,6 @@ __global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const Sol
     }
 }
 
-// ---- REF-GEO: GeometricTools::calcCellVolume (geometrictools.cpp:13-116) in FP64 ----------------------------------------
-// Vertex slots: 0:(i,j,k) 1:(i+1,j,k) 2:(i,j+1,k) 3:(i+1,j+1,k) 4..7 the same at k+1 (ascending point label).
-__constant__ int8_t c_face_slots[9][4] = {
-    {1, 3, 7, 5},  // x-max, owner order (internal +x face and x-max boundary face)
-    {2, 6, 7, 3},  // y-max
-    {4, 5, 7, 6},  // z-max
-    {0, 4, 6, 2},  // x-min boundary face (hex model order)
-    {0, 1, 5, 4},  // y-min boundary face
-    {0, 2, 3, 1},  // z-min boundary face
-    {0, 2, 6, 4},  // -x internal face (owner is the lower neighbour)
-    {0, 4, 5, 1},  // -y internal face
-    {0, 1, 3, 2},  // -z internal face
-};
-
-__device__ inline double line_fraction(double pa, double pb) {
-    if (pa > 0 && pb > 0) return 0;
-    if (pa <= 0 && pb <= 0) return 1;
-    if (pa > 0) return -pb / (pa - pb);
-    return -pa / (pb - pa);
-}
-
-__device__ inline D3 calc_apex(const D3* P, const double* ph, const int8_t* idx, int n) {
-    const D3 A = P[idx[0]];
-    const double phiA = ph[idx[0]];
-    D3 B{0, 0, 0};
-    double phiB = 0.0;
-    for (int i = 1; i < n; ++i) {
-        B = P[idx[i]];
-        phiB = ph[idx[i]];
-        if (phiA * phiB <= 0) break;
-    }
-    return A - fabs(phiA) / (SMALL_D + fabs(phiA) + fabs(phiB)) * (A - B);
-}
-
-__device__ inline double face_area_fraction(const D3* P, const double* ph, const int8_t* f, const D3& Sf) {
-    int sign_sum = 0;
-    for (int i = 0; i < 4; ++i) sign_sum += (ph[f[i]] > 0) ? 1 : -1;
-    if (sign_sum == 4) return 0.0;
-    if (sign_sum == -4) return 1.0;
-    const D3 ap = calc_apex(P, ph, f, 4);
-    double area = 0.0;
-    for (int iseg = 0; iseg < 4; ++iseg) {
-        const int o = f[iseg], a = f[(iseg + 1) & 3];
-        area += fabs(0.5 * mag(cross(P[a] - P[o], ap - P[o]))) * line_fraction(ph[o], ph[a]);
-    }
-    return area / mag(Sf);
-}
-
-__device__ double refgeo_fraction(const MeshK& m, const ShapeK& sh, const D3& x, const Q4& q, int64_t i, int64_t j,
-                                  int64_t k) {
-    D3 P[8];
-    double ph[8];
-    const int8_t order[8] = {0, 1, 2, 3, 4, 5, 6, 7};
-#pragma unroll
-    for (int s = 0; s < 8; ++s) {
-        P[s] = mesh_point(m, i + (s & 1), j + ((s >> 1) & 1), k + ((s >> 2) & 1));
-        ph[s] = sdf64(sh, world2local(P[s], x, q));
-    }
-    D3 ap = calc_apex(P, ph, order, 8);
-    if (m.twod) ap.z = 0.0;
-    const double xc = mesh_centre(m, 0, i), yc = mesh_centre(m, 1, j), zc = mesh_centre(m, 2, k);
-    const double xlo = mesh_coord(m, 0, i), xhi = mesh_coord(m, 0, i + 1);
-    const double ylo = mesh_coord(m, 1, j), yhi = mesh_coord(m, 1, j + 1);
-    const double zlo = mesh_coord(m, 2, k), zhi = mesh_coord(m, 2, k + 1);
-    const D3 Sx{m.h[1] * m.h[2], 0, 0}, Sy{0, m.h[0] * m.h[2], 0}, Sz{0, 0, m.h[0] * m.h[1]};
-    double volume = 0.0;
-    auto acc = [&](int slot, const D3& Cf, const D3& Sf) {
-        const double eps_f = face_area_fraction(P, ph, c_face_slots[slot], Sf);
-        volume += (1.0 / 3.0) * eps_f * fabs(dot(ap - Cf, Sf));
-    };
-    // mesh.cells()[c] order: owned internal (+x,+y,+z), boundary faces by patch, then -z,-y,-x
-    if (i + 1 < m.nx) acc(0, D3{xhi, yc, zc}, Sx);
-    if (j + 1 < m.ny) acc(1, D3{xc, yhi, zc}, Sy);
-    if (k + 1 < m.nz) acc(2, D3{xc, yc, zhi}, Sz);
-    if (i == 0) acc(3, D3{xlo, yc, zc}, Sx);
-    if (i == m.nx - 1) acc(0, D3{xhi, yc, zc}, Sx);
-    if (j == 0) acc(4, D3{xc, ylo, zc}, Sy);
-    if (j == m.ny - 1) acc(1, D3{xc, yhi, zc}, Sy);
-    if (k == 0) acc(5, D3{xc, yc, zlo}, Sz);
-    if (k == m.nz - 1) acc(2, D3{xc, yc, zhi}, Sz);
-    if (k > 0) acc(8, D3{xc, yc, zlo}, Sz);
-    if (j > 0) acc(7, D3{xc, ylo, zc}, Sy);
-    if (i > 0) acc(6, D3{xlo, yc, zc}, Sx);
-    return volume / m.V;
-}
-
-// ---- SUBSAMPLE: n^3 (3-D) or n^2 (2-D) midpoint lattice, isInside per sample -------------------------------------------
-__device__ double subsample_fraction(const MeshK& m, const ShapeK& sh, const float* M, const D3& x, const Q4& q,
-                                     int64_t i, int64_t j, int64_t k, int n, unsigned long long* rechecks) {
-    const D3 p0 = mesh_point(m, i, j, k);
-    const TileFrame tf = make_frame(p0 - x, p0, x);
-    const int nzs = m.twod ? 1 : n;
-    const float inv2n = 1.0f / (float)(2 * n);
-    int cnt = 0;
-    for (int c3 = 0; c3 < nzs; ++c3) {
-        const double tz = m.twod ? 0.5 : (double)(2 * c3 + 1) / (double)(2 * n);
-        const float oz = (m.twod ? 0.5f : (float)(2 * c3 + 1) * inv2n) * m.h32[2];
-        for (int bb = 0; bb < n; ++bb) {
-            const double ty = (double)(2 * bb + 1) / (double)(2 * n);
-            const float oy = (float)(2 * bb + 1) * inv2n * m.h32[1];
-            for (int a = 0; a < n; ++a) {
-                const float ox = (float)(2 * a + 1) * inv2n * m.h32[0];
-                const float dx = tf.bx + ox, dy = tf.by + oy, dz = tf.bz + oz;
-                const float lx = __fmaf_rn(M[0], dx, __fmaf_rn(M[1], dy, M[2] * dz));
-                const float ly = __fmaf_rn(M[3], dx, __fmaf_rn(M[4], dy, M[5] * dz));
-                const float lz = __fmaf_rn(M[6], dx, __fmaf_rn(M[7], dy, M[8] * dz));
-                const float dabs = fabsf(dx) + fabsf(dy) + fabsf(dz);
-                // the FP32 sample offset carries an extra rounding of (2a+1)/(2n) relative to the FP64 formula
-                const float E = 8.f * U32 * (tf.babs + fabsf(ox) + fabsf(oy) + fabsf(oz) + 2.f * dabs) + tf.e64 + 1e-30f;
-                int r = inside32(sh, lx, ly, lz, E);
-                if (r == 2) {
-                    atomicAdd(rechecks, 1ull);
-                    const double ta = (double)(2 * a + 1) / (double)(2 * n);
-                    const D3 p{m.o[0] + ((double)i + ta) * m.h[0], m.o[1] + ((double)j + ty) * m.h[1],
-                               m.o[2] + ((double)k + tz) * m.h[2]};
-                    r = inside64(sh, world2local(p, x, q)) ? 1 : 0;
-                }
-                cnt += r;
-            }
-        }
-    }
-    return (double)cnt / (double)(n * n * nzs);
-}
-
 // ---- shared cells -----------------------------------------------------------------------------------------------------
 // slot of cell c in the shared table, inserting it on first use; -1 (and an error flag) when the table is full
 __device__ inline int shared_slot(const CoupleArgs& A, int32_t c) {
@@ -687,12 +427,11 @@ __global__ void __launch_bounds__(CPL_THREADS) couple_kernel(CoupleArgs A) {
             const D3 x = state_pos(st);
             double alpha = 1.0;
             if (is_cut) {
-                const Q4 q = state_quat(st);
-                if (A.method == SDFIBM_FRACTION_SUBSAMPLE)
-                    alpha = subsample_fraction(m, A.sk[s].shape, A.plan[s].M, x, q, i, j, k, A.subsample_n,
-                                               &A.cnt->exact_rechecks);
-                else
-                    alpha = refgeo_fraction(m, A.sk[s].shape, x, q, i, j, k);
+                // computed by the classify pass for every cut candidate of the solid's bbox
+                const SolidK& ks = A.sk[s];
+                const int32_t* lo = A.plan[s].lo;
+                const int64_t li = (i - lo[0]) + (int64_t)ks.ext[0] * ((j - lo[1]) + (int64_t)ks.ext[1] * (k - lo[2]));
+                alpha = (double)A.alpha[ks.scratch_off + li];
             }
             // pcHydrodynamicInteraction (solidcloud.cpp:384-390) and the accumulation of :411-421
             const D3 cc = mesh_C(m, i, j, k);

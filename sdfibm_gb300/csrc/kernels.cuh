@@ -41,6 +41,10 @@ struct SolidPlan {
     unsigned long long min_cand;  // lowest cell label with an inside vertex (atomicMin), ~0 when none
     float M[9];               // FP32 world->local matrix (|q|^2 R^T)
     int32_t n_inside, n_cut;  // touched cells by kind
+    double cw[3];             // centre of the bounding sphere (2-D shapes: of the bounding disc)
+    double rcull;             // its radius
+    int32_t vlo[3], vhi[3];   // mesh-vertex index box of the solid's oriented bounding box: vertices outside it are
+                              // outside the solid (vlo > vhi on some axis: no vertex can be inside)
 };
 
 // Global counters / flags (one record per context, device memory).
@@ -72,6 +76,7 @@ struct CoupleArgs {
     const int32_t* in_solid;
     const int32_t* cut_cell;
     const int32_t* cut_solid;
+    const float* alpha;  // per bbox cell, from the classify pass
     const float* U;
     float* As;
     float* Fs;
@@ -95,6 +100,21 @@ struct CoupleArgs {
 constexpr uint32_t CT_KEY_BASE = 1u << 30;
 constexpr uint32_t CT_SHARED = 1u << 31;
 constexpr int SHARED_MAX_PROBES = 64;
+
+struct ClassifyArgs {
+    MeshK m;
+    const SolidK* sk;
+    const sdfibm_solid_state* st;
+    SolidPlan* plan;
+    const int32_t* tile_prefix;
+    int S;
+    int total_tiles;
+    uint8_t* cls;      // class byte per bbox cell
+    float* alpha;      // solid fraction per bbox cell (cut candidates only)
+    Counters* cnt;
+    int method;        // sdfibm_fraction_method, or -1: classification only
+    int subsample_n;
+};
 
 // UGrid (src/libcollision/ugrid.h:14-58): bbox of the mesh, spacing 2*max radiusB, row-major i*ny*nz + j*nz + k
 struct GridK {

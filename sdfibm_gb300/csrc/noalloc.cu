@@ -28,8 +28,7 @@
 namespace sdfibm_dev {
 __global__ void plan_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state* st, SolidPlan* plan, int S,
                             Counters* cnt);
-__global__ void classify_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state* st, SolidPlan* plan,
-                                const int32_t* tile_prefix, int S, int total_tiles, uint8_t* scratch, Counters* cnt);
+__global__ void classify_kernel(ClassifyArgs A);
 __global__ void connect_kernel(MeshK m, const SolidK* sk, SolidPlan* plan, const uint8_t* scratch, uint32_t* gbitmaps,
                                int32_t* in_cell, int32_t* in_solid, int32_t* cut_cell, int32_t* cut_solid,
                                int64_t cap_in, int64_t cap_cut, Counters* cnt, int smem_words);
@@ -126,10 +125,10 @@ bool solid_record(const sdfibm_mesh_desc& mesh, const sdfibm_solid_desc& d, Soli
     }
     if (!k.infinite && prism && !(d.quat[1] == 0.0 && d.quat[2] == 0.0))
         for (int a = 0; a < 2; ++a) k.ext[a] = n3[a] + 4;
-    const int tz = k.ext[2] < 8 ? k.ext[2] : 8;
-    k.tdim[2] = tz;
-    k.tdim[0] = tz <= 2 ? 32 : 8;
-    k.tdim[1] = tz <= 2 ? 16 : 8;
+    const int tz = k.ext[2] < 4 ? k.ext[2] : 4;
+    k.tdim[2] = tz <= 2 ? tz : 4;
+    k.tdim[0] = tz <= 2 ? 8 : 4;
+    k.tdim[1] = tz <= 2 ? 8 : 4;
     for (int a = 0; a < 3; ++a) k.ntile[a] = (k.ext[a] + k.tdim[a] - 1) / k.tdim[a];
     k.tile_base = 0;
     k.scratch_off = 0;
@@ -267,7 +266,10 @@ extern "C" int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc* mesh, const s
     if (cudaGetDevice(&dev) != cudaSuccess) return SDFIBM_ERR_CUDA;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int grid = ntiles < 4 * (sms > 0 ? sms : 1) ? ntiles : 4 * (sms > 0 ? sms : 1);
-    classify_kernel<<<grid, 256, 0, st>>>(m, d_sk, d_st, d_plan, d_prefix, 1, ntiles, b + OFF_CLS, d_cnt);
+    ClassifyArgs CA;
+    CA.m = m; CA.sk = d_sk; CA.st = d_st; CA.plan = d_plan; CA.tile_prefix = d_prefix; CA.S = 1; CA.total_tiles = ntiles;
+    CA.cls = b + OFF_CLS; CA.alpha = nullptr; CA.cnt = d_cnt; CA.method = -1; CA.subsample_n = 0;
+    classify_kernel<<<grid, 256, 0, st>>>(CA);
     connect_kernel<<<1, 512, 0, st>>>(m, d_sk, d_plan, b + OFF_CLS, reinterpret_cast<uint32_t*>(b + OFF_BITMAP),
                                       reinterpret_cast<int32_t*>(b + OFF_IN_CELL), reinterpret_cast<int32_t*>(b + OFF_IN_SOLID),
                                       reinterpret_cast<int32_t*>(b + OFF_CUT_CELL), reinterpret_cast<int32_t*>(b + OFF_CUT_SOLID),

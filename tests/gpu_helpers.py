@@ -80,9 +80,29 @@ def check_interact(w, r, U_used=None):
         o = fo[key]
         bad = np.abs(g - o) > AS_REL * np.abs(o) + AS_ABS
         assert not bad.any(), "%s differs in %d cells, worst %g vs %g" % (key, bad.sum(), g[bad][0], o[bad][0])
-    g = fd["Fs"].cpu().numpy().astype(np.float64).reshape(-1)
-    o = fo["Fs"]
-    bad = np.abs(g - o) > AS_REL * np.abs(o) + AS_ABS
+    g = fd["Fs"].cpu().numpy().astype(np.float64).reshape(3, N)
+    o = fo["Fs"].reshape(3, N)
+    # Fs is relative-accurate per contribution; where several solids touch one cell their contributions can cancel,
+    # so there the bound is taken against the sum of the contributions' magnitudes
+    scale = np.abs(o).copy()
+    owners = {}
+    for s in range(S):
+        for c in orc.touched(s)[0]:
+            owners.setdefault(int(c), []).append(s)
+    Uo = r["Uo"].reshape(3, N) if U_used is None else U_used.reshape(3, N)
+    st = orc.get_state()
+    for c, ss in owners.items():
+        if len(ss) < 2:
+            continue
+        C = np.array(_centre(w.mesh, c))
+        mag = np.zeros(3)
+        for s in ss:
+            al = orc.cell_fraction(s, c, int(w.opt.fraction_method))  # the solid's own fraction of the cell
+            x = np.array(st[s].pos)
+            us = np.array(st[s].vel) + np.cross(np.array(st[s].omega), C - x)
+            mag += al * np.abs(Uo[:, c] - us) / w.dt
+        scale[:, c] = np.maximum(scale[:, c], mag)
+    bad = np.abs(g - o) > AS_REL * scale + AS_ABS
     assert not bad.any(), "Fs differs in %d entries" % bad.sum()
     FTg, FTo = r["FT"][-1]
     Uo = r["Uo"] if U_used is None else U_used
