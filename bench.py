@@ -103,6 +103,7 @@ def make_workload(args):
     from sdfibm_gb300 import abi, workloads
     w = workloads.CONFIGS[args.config](scale=args.scale)
     w.opt.fraction_method = METHODS[args.method]
+    w.opt.exact_forcing = 0 if getattr(args, "fp32_forcing", False) else 1
     return w
 
 
@@ -167,6 +168,8 @@ def main():
     ap.add_argument("--cpu-solids", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--fp32-forcing", action="store_true",
+                    help="FP32 direct forcing with FP64 force/torque sums (the fast paths' precision)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -289,8 +292,9 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 fields, f64 geometry and reductions",
                 "data": "synthetic",
-                "config": {"workload": "%s: %dx%dx%d mesh, %d solids, %s solid fraction, HBM-resident fields"
-                                       % (w.name, w.mesh.nx, w.mesh.ny, w.mesh.nz, len(w.solids), args.method),
+                "config": {"workload": "%s: %dx%dx%d mesh, %d solids, %s solid fraction, %s forcing, HBM-resident fields"
+                                       % (w.name, w.mesh.nx, w.mesh.ny, w.mesh.nz, len(w.solids), args.method,
+                                          "FP32" if args.fp32_forcing else "FP64"),
                            "n_cells": w.ncells, "n_solids": len(w.solids), "coupling_cells": mean_cells,
                            "bbox_cells": sum(bbox) / len(bbox), "fraction_method": args.method,
                            "l2": "flushed (256 MB write) before every timed step", "full_step_ms": full_ms,

@@ -15,17 +15,18 @@ namespace sdfibm_dev {
 // coupling.cu
 __global__ void plan_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state* st, SolidPlan* plan, int S,
                             Counters* cnt);
-__global__ void classify_kernel(ClassifyArgs A);
+__global__ void classify_kernel_3d(ClassifyArgs A);
+__global__ void classify_kernel_2d(ClassifyArgs A);
 __global__ void connect_kernel(MeshK m, const SolidK* sk, SolidPlan* plan, const uint8_t* scratch, uint32_t* gbitmaps,
                                int32_t* in_cell, int32_t* in_solid, int32_t* cut_cell, int32_t* cut_solid,
                                int64_t cap_in, int64_t cap_cut, Counters* cnt, int smem_words);
 
 __global__ void couple_kernel(CoupleArgs A);
+__global__ void finalize_kernel(float* As, float* Ts, float* Fs, int32_t* Ct, const Counters* cnt, int64_t N,
+                                int32_t* sh_keys, double* sh_vals, const int32_t* sh_used, int32_t sh_mask);
+__global__ void begin_kernel(Counters* cnt);
 __global__ void claim_kernel(const int32_t* in_cell, const int32_t* in_solid, const int32_t* cut_cell,
                              const int32_t* cut_solid, int32_t* Ct, const Counters* cnt, int64_t N);
-__global__ void finalize_kernel(const int32_t* in_cell, const int32_t* in_solid, const int32_t* cut_cell,
-                                const int32_t* cut_solid, float* As, float* Ts, float* Fs, int32_t* Ct, Counters* cnt,
-                                int64_t N, int32_t* sh_keys, double* sh_vals, const int32_t* sh_used, int32_t sh_mask);
 __global__ void ft_kernel(const double* ftacc, double* ft, int S, double rho_f);
 __global__ void reset_kernel(const int32_t* in_cell, const int32_t* cut_cell, const Counters* cnt, int64_t N,
                              float* As, float* Fs, float* Ts, int32_t* Ct);
@@ -73,7 +74,8 @@ struct sdfibm_ctx {
     SolidK* d_sk = nullptr;
     sdfibm_solid_state* d_st = nullptr;
     SolidPlan* d_plan = nullptr;
-    int32_t* d_tile_prefix = nullptr;
+    int2* d_chunks = nullptr;  // classify work items: (solid, first tile)
+    int total_chunks = 0;
     int total_tiles = 0;
     uint8_t* d_scratch = nullptr;
     float* d_alpha = nullptr;  // solid fraction per bbox cell (same indexing as d_scratch)
@@ -81,7 +83,13 @@ struct sdfibm_ctx {
     uint32_t* d_gbitmaps = nullptr;
     int64_t gbitmap_words = 0;
     int connect_smem_bytes = 0;
-    int32_t *d_in_cell = nullptr, *d_in_solid = nullptr, *d_cut_cell = nullptr, *d_cut_solid = nullptr;
+    // touched-cell lists, double buffered: [cur] is this call's, [cur ^ 1] the previous call's (sparse reset)
+    int32_t* d_lists[2][4] = {{nullptr, nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr, nullptr}};
+    int cur = 0;
+    int32_t* in_cell() const { return d_lists[cur][0]; }
+    int32_t* in_solid() const { return d_lists[cur][1]; }
+    int32_t* cut_cell() const { return d_lists[cur][2]; }
+    int32_t* cut_solid() const { return d_lists[cur][3]; }
     int64_t cap = 0;
     int32_t* d_sh_keys = nullptr;
     double* d_sh_vals = nullptr;
@@ -246,11 +254,11 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
             // a 2-D shape that does not rotate about z: its prism may cross the whole mesh
             for (int a = 0; a < 2; ++a) k.ext[a] = n3[a] + 4;
         }
-        // warp tiles: 4x4x4 cells, or 8x8 x (1 or 2) on one- and two-layer meshes
-        const int tz = std::min(4, k.ext[2]);
-        k.tdim[2] = tz <= 2 ? tz : 4;
-        k.tdim[0] = tz <= 2 ? 8 : 4;
-        k.tdim[1] = tz <= 2 ? 8 : 4;
+        // warp tiles: 4x4x4 cells, or 8x8x2 on one- and two-layer meshes
+        const bool layer = mesh->nz <= 2;
+        k.tdim[0] = layer ? 8 : 4;
+        k.tdim[1] = layer ? 8 : 4;
+        k.tdim[2] = layer ? 2 : 4;
         for (int a = 0; a < 3; ++a) k.ntile[a] = (k.ext[a] + k.tdim[a] - 1) / k.tdim[a];
         k.tile_base = (int32_t)tiles;
         tiles += (int64_t)k.ntile[0] * k.ntile[1] * k.ntile[2];
@@ -289,9 +297,13 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         while (t < 2 * want) t <<= 1;
         ctx->sh_mask = (int32_t)(t - 1);
     }
-    std::vector<int32_t> prefix(nsolids + 1);
-    for (int s = 0; s < nsolids; ++s) prefix[s] = ctx->hk[s].tile_base;
-    prefix[nsolids] = (int32_t)tiles;
+    std::vector<int2> chunks;
+    for (int s = 0; s < nsolids; ++s) {
+        const SolidK& k = ctx->hk[s];
+        const int nt = k.ntile[0] * k.ntile[1] * k.ntile[2];
+        for (int t0 = 0; t0 < nt; t0 += CHUNK_TILES) chunks.push_back(make_int2(s, t0));
+    }
+    ctx->total_chunks = (int)chunks.size();
 
     // collision grid (UGrid(bbox of the mesh, 2*max radiusB))
     if (ctx->opt.collision_mode != SDFIBM_COLLISION_OFF && nsolids > 0) {
@@ -321,9 +333,11 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
 
     // device allocations
     if (dalloc(&ctx->d_sk, nsolids) || dalloc(&ctx->d_st, nsolids) || dalloc(&ctx->d_plan, nsolids) ||
-        dalloc(&ctx->d_tile_prefix, nsolids + 1) || dalloc(&ctx->d_scratch, scratch) || dalloc(&ctx->d_alpha, scratch) ||
-        dalloc(&ctx->d_gbitmaps, gwords) || dalloc(&ctx->d_in_cell, ctx->cap) || dalloc(&ctx->d_in_solid, ctx->cap) ||
-        dalloc(&ctx->d_cut_cell, ctx->cap) || dalloc(&ctx->d_cut_solid, ctx->cap) || dalloc(&ctx->d_cnt, 1) ||
+        dalloc(&ctx->d_chunks, chunks.size()) || dalloc(&ctx->d_scratch, scratch) || dalloc(&ctx->d_alpha, scratch) ||
+        dalloc(&ctx->d_gbitmaps, gwords) || dalloc(&ctx->d_lists[0][0], ctx->cap) || dalloc(&ctx->d_lists[0][1], ctx->cap) ||
+        dalloc(&ctx->d_lists[0][2], ctx->cap) || dalloc(&ctx->d_lists[0][3], ctx->cap) ||
+        dalloc(&ctx->d_lists[1][0], ctx->cap) || dalloc(&ctx->d_lists[1][1], ctx->cap) ||
+        dalloc(&ctx->d_lists[1][2], ctx->cap) || dalloc(&ctx->d_lists[1][3], ctx->cap) || dalloc(&ctx->d_cnt, 1) ||
         dalloc(&ctx->d_ftacc, 6 * (size_t)nsolids) || dalloc(&ctx->d_ft, 6 * (size_t)nsolids) ||
         dalloc(&ctx->d_sh_keys, (size_t)ctx->sh_mask + 1) || dalloc(&ctx->d_sh_vals, 5 * ((size_t)ctx->sh_mask + 1)) ||
         dalloc(&ctx->d_sh_used, (size_t)ctx->sh_mask + 1) ||
@@ -354,7 +368,7 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         return bytes ? cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
     };
     if (up(c->d_sk, c->hk.data(), sizeof(SolidK) * nsolids) || up(c->d_st, st.data(), sizeof(sdfibm_solid_state) * nsolids) ||
-        up(c->d_tile_prefix, prefix.data(), sizeof(int32_t) * (nsolids + 1)) ||
+        up(c->d_chunks, chunks.data(), sizeof(int2) * chunks.size()) ||
         cudaMemset(c->d_cnt, 0, sizeof(Counters)) != cudaSuccess ||
         cudaMemset(c->d_sh_keys, 0xff, sizeof(int32_t) * ((size_t)c->sh_mask + 1)) != cudaSuccess ||
         cudaMemset(c->d_sh_vals, 0, sizeof(double) * 5 * ((size_t)c->sh_mask + 1)) != cudaSuccess ||
@@ -370,7 +384,7 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         }
     }
     int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, classify_kernel, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mesh->nz <= 2 ? classify_kernel_2d : classify_kernel_3d, 256, 0);
     ctx->classify_grid = std::max(1, occ) * ctx->num_sms;
     occ = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, couple_kernel, 256, 0);
@@ -412,59 +426,65 @@ int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U
     const void* f5[5] = {U, As, Fs, Ts, Ct};
     bool same = ctx->interacted;
     for (int i = 1; i < 5; ++i) same = same && f5[i] == ctx->last_fields[i];
-    if (!same || ctx->opt.dense_reset) {
+    const bool dense = !same || ctx->opt.dense_reset;
+    for (int i = 0; i < 5; ++i) ctx->last_fields[i] = f5[i];
+    ctx->cur ^= 1;  // this call's lists; the other buffer holds the previous call's touched cells
+    begin_kernel<<<1, 1, 0, st>>>(ctx->d_cnt);
+    ++launches;
+    if (dense) {
         // SolidCloud::interact zeroes the four fields over the whole mesh (solidcloud.cpp:438-441)
         CK(cudaMemsetAsync(As, 0, sizeof(float) * N, st));
         CK(cudaMemsetAsync(Fs, 0, sizeof(float) * 3 * N, st));
         CK(cudaMemsetAsync(Ts, 0, sizeof(float) * N, st));
         CK(cudaMemsetAsync(Ct, 0, sizeof(int32_t) * N, st));
         mark(ctx, "dense_reset");
-    } else {
-        // only the previous call's cells can be nonzero
-        reset_kernel<<<ctx->num_sms * 4, 256, 0, st>>>(ctx->d_in_cell, ctx->d_cut_cell, ctx->d_cnt, N, As, Fs, Ts, Ct);
-        mark(ctx, "reset_kernel");
-        ++launches;
     }
-    for (int i = 0; i < 5; ++i) ctx->last_fields[i] = f5[i];
-    // per-call counters (the previous list lengths stay for the reset kernel above, which already ran in order)
-    CK(cudaMemsetAsync(ctx->d_cnt, 0, offsetof(Counters, error), st));
-    CK(cudaMemsetAsync(&ctx->d_cnt->exact_rechecks, 0, 2 * sizeof(unsigned long long), st));
     if (S > 0) {
         CK(cudaMemsetAsync(ctx->d_ftacc, 0, sizeof(double) * 6 * S, st));
         plan_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->mesh, ctx->d_sk, ctx->d_st, ctx->d_plan, S, ctx->d_cnt);
         mark(ctx, "plan_kernel");
         ClassifyArgs CA;
-        CA.m = ctx->mesh; CA.sk = ctx->d_sk; CA.st = ctx->d_st; CA.plan = ctx->d_plan; CA.tile_prefix = ctx->d_tile_prefix;
-        CA.S = S; CA.total_tiles = ctx->total_tiles; CA.cls = ctx->d_scratch; CA.alpha = ctx->d_alpha; CA.cnt = ctx->d_cnt;
+        CA.m = ctx->mesh; CA.sk = ctx->d_sk; CA.st = ctx->d_st; CA.plan = ctx->d_plan; CA.chunks = ctx->d_chunks;
+        CA.total_chunks = ctx->total_chunks; CA.cls = ctx->d_scratch; CA.alpha = ctx->d_alpha; CA.cnt = ctx->d_cnt;
         CA.method = ctx->opt.fraction_method; CA.subsample_n = ctx->opt.subsample_n;
-        classify_kernel<<<ctx->classify_grid, 256, 0, st>>>(CA);
+        if (ctx->mesh.nz <= 2) classify_kernel_2d<<<ctx->classify_grid, 256, 0, st>>>(CA);
+        else classify_kernel_3d<<<ctx->classify_grid, 256, 0, st>>>(CA);
         mark(ctx, "classify_kernel");
         connect_kernel<<<S, 512, ctx->connect_smem_bytes, st>>>(ctx->mesh, ctx->d_sk, ctx->d_plan, ctx->d_scratch,
-                                                                ctx->d_gbitmaps, ctx->d_in_cell, ctx->d_in_solid,
-                                                                ctx->d_cut_cell, ctx->d_cut_solid, ctx->cap, ctx->cap,
+                                                                ctx->d_gbitmaps, ctx->in_cell(), ctx->in_solid(),
+                                                                ctx->cut_cell(), ctx->cut_solid(), ctx->cap, ctx->cap,
                                                                 ctx->d_cnt, ctx->connect_smem_bytes / 4);
         mark(ctx, "connect_kernel");
-        claim_kernel<<<ctx->num_sms * 4, 256, 0, st>>>(ctx->d_in_cell, ctx->d_in_solid, ctx->d_cut_cell,
-                                                        ctx->d_cut_solid, Ct, ctx->d_cnt, N);
+        claim_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(ctx->in_cell(), ctx->in_solid(), ctx->cut_cell(),
+                                                        ctx->cut_solid(), Ct, ctx->d_cnt, N);
         mark(ctx, "claim_kernel");
+        launches += 4;
+    }
+    if (!dense) {
+        const int p = ctx->cur ^ 1;
+        reset_kernel<<<ctx->num_sms * 4, 256, 0, st>>>(ctx->d_lists[p][0], ctx->d_lists[p][2], ctx->d_cnt, N, As, Fs,
+                                                        Ts, Ct);
+        mark(ctx, "reset_kernel");
+        ++launches;
+    }
+    if (S > 0) {
         CoupleArgs A;
         A.m = ctx->mesh; A.sk = ctx->d_sk; A.st = ctx->d_st; A.plan = ctx->d_plan;
-        A.in_cell = ctx->d_in_cell; A.in_solid = ctx->d_in_solid; A.cut_cell = ctx->d_cut_cell;
-        A.cut_solid = ctx->d_cut_solid; A.alpha = ctx->d_alpha; A.U = U; A.As = As; A.Fs = Fs; A.Ts = Ts; A.Ct = Ct;
+        A.in_cell = ctx->in_cell(); A.in_solid = ctx->in_solid(); A.cut_cell = ctx->cut_cell();
+        A.cut_solid = ctx->cut_solid(); A.alpha = ctx->d_alpha; A.U = U; A.As = As; A.Fs = Fs; A.Ts = Ts; A.Ct = Ct;
         A.ftacc = ctx->d_ftacc; A.cnt = ctx->d_cnt; A.dtINV = 1.0 / dt;
         A.method = ctx->opt.fraction_method; A.subsample_n = ctx->opt.subsample_n;
         A.exact_forcing = ctx->opt.exact_forcing;
         A.sh_keys = ctx->d_sh_keys; A.sh_vals = ctx->d_sh_vals; A.sh_used = ctx->d_sh_used; A.sh_mask = ctx->sh_mask;
         couple_kernel<<<ctx->couple_grid, 256, 0, st>>>(A);
         mark(ctx, "couple_kernel");
-        finalize_kernel<<<ctx->num_sms * 4, 256, 0, st>>>(ctx->d_in_cell, ctx->d_in_solid, ctx->d_cut_cell,
-                                                           ctx->d_cut_solid, As, Ts, Fs, Ct, ctx->d_cnt, N,
-                                                           ctx->d_sh_keys, ctx->d_sh_vals, ctx->d_sh_used, ctx->sh_mask);
+        finalize_kernel<<<ctx->num_sms, 256, 0, st>>>(As, Ts, Fs, Ct, ctx->d_cnt, N, ctx->d_sh_keys, ctx->d_sh_vals,
+                                                       ctx->d_sh_used, ctx->sh_mask);
         mark(ctx, "finalize_kernel");
         ft_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->d_ftacc, ctx->d_ft, S, ctx->opt.rho_f);
         ft_to_state_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->d_ft, ctx->d_st, S);
         mark(ctx, "ft_kernel");
-        launches += 8;
+        launches += 4;
     }
     CK(cudaGetLastError());
     ctx->launches_last = launches;
@@ -537,8 +557,8 @@ int sdfibm_cuda_fix_internal(sdfibm_ctx* ctx, const int32_t* Ct, float* U) {
     if (!ctx) return SDFIBM_ERR_ARG;
     if (!Ct || !U) return fail(ctx, SDFIBM_ERR_ARG, "null field pointer");
     if (!ctx->interacted) return fail(ctx, SDFIBM_ERR_STATE, "fix_internal needs a previous interact");
-    fix_internal_kernel<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(ctx->mesh, ctx->d_st, ctx->d_in_cell,
-                                                                    ctx->d_in_solid, Ct, U, ctx->d_cnt);
+    fix_internal_kernel<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(ctx->mesh, ctx->d_st, ctx->in_cell(),
+                                                                    ctx->in_solid(), Ct, U, ctx->d_cnt);
     CK(cudaGetLastError());
     return SDFIBM_OK;
 }
@@ -569,12 +589,12 @@ int sdfibm_cuda_touched(sdfibm_ctx* ctx, int32_t solid, int64_t* cells, int8_t* 
     const int nin = clamp_len(ctx->h_cnt->n_inside, ctx->cap), ncut = clamp_len(ctx->h_cnt->n_cut, ctx->cap);
     std::vector<int32_t> ic(nin), is(nin), cc(ncut), cs(ncut);
     if (nin) {
-        CK(cudaMemcpy(ic.data(), ctx->d_in_cell, sizeof(int32_t) * nin, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(is.data(), ctx->d_in_solid, sizeof(int32_t) * nin, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(ic.data(), ctx->in_cell(), sizeof(int32_t) * nin, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(is.data(), ctx->in_solid(), sizeof(int32_t) * nin, cudaMemcpyDeviceToHost));
     }
     if (ncut) {
-        CK(cudaMemcpy(cc.data(), ctx->d_cut_cell, sizeof(int32_t) * ncut, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(cs.data(), ctx->d_cut_solid, sizeof(int32_t) * ncut, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(cc.data(), ctx->cut_cell(), sizeof(int32_t) * ncut, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(cs.data(), ctx->cut_solid(), sizeof(int32_t) * ncut, cudaMemcpyDeviceToHost));
     }
     std::vector<int64_t> byType[4];
     for (int i = 0; i < nin; ++i)
@@ -618,7 +638,7 @@ int sdfibm_cuda_stats(sdfibm_ctx* ctx, int64_t* out, int32_t n) {
     if (rc) return rc;
     const Counters& c = *ctx->h_cnt;
     const int64_t v[6] = {(int64_t)c.n_inside + c.n_cut, (int64_t)c.n_cut, (int64_t)c.bbox_cells,
-                          (int64_t)c.exact_rechecks, (int64_t)ctx->total_tiles, (int64_t)ctx->launches_last};
+                          (int64_t)c.exact_rechecks, (int64_t)ctx->total_chunks, (int64_t)ctx->launches_last};
     for (int i = 0; i < n && i < 6; ++i) out[i] = v[i];
     return SDFIBM_OK;
 }
@@ -626,8 +646,9 @@ int sdfibm_cuda_stats(sdfibm_ctx* ctx, int64_t* out, int32_t n) {
 void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
     if (!ctx) return;
     cudaStreamSynchronize(ctx->stream);
-    void* dev[] = {ctx->d_sk, ctx->d_st, ctx->d_plan, ctx->d_tile_prefix, ctx->d_scratch, ctx->d_gbitmaps,
-                   ctx->d_in_cell, ctx->d_in_solid, ctx->d_cut_cell, ctx->d_cut_solid, ctx->d_cnt, ctx->d_ftacc,
+    void* dev[] = {ctx->d_sk, ctx->d_st, ctx->d_plan, ctx->d_chunks, ctx->d_scratch, ctx->d_gbitmaps,
+                   ctx->d_lists[0][0], ctx->d_lists[0][1], ctx->d_lists[0][2], ctx->d_lists[0][3],
+                   ctx->d_lists[1][0], ctx->d_lists[1][1], ctx->d_lists[1][2], ctx->d_lists[1][3], ctx->d_cnt, ctx->d_ftacc,
                    ctx->d_ft, ctx->d_hash, ctx->d_gcount, ctx->d_gstart, ctx->d_gcursor, ctx->d_glist, ctx->d_U,
                    ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, ctx->d_alpha, ctx->d_sh_keys, ctx->d_sh_vals, ctx->d_sh_used};
     for (void* p : dev)

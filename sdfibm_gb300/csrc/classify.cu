@@ -7,11 +7,11 @@
 //      (CellEnumerator::_next, src/cellenumerator.cpp:6-34): 0 no inside vertex, 1 all inside, 2 centre inside,
 //      3 centre outside;
 //   3. computes the solid fraction of every cut candidate (class 2/3) and writes it to the alpha scratch:
-//      REF-GEO   GeometricTools::calcCellVolume (src/geometrictools.cpp:13-116): the vertex signed distances come
-//                from the reference's FP64 Solid::phi, evaluated once per tile vertex next to a cut cell and kept in
-//                shared memory; the apex/pyramid geometry then runs in FP32 in cell-local coordinates (vertices on
-//                {0,1}^3), where on an axis-aligned hexahedron every term is a product of non-negative factors and
-//                no subtraction cancels, so the result keeps ~1e-7 relative accuracy;
+//      REF-GEO   GeometricTools::calcCellVolume (src/geometrictools.cpp:13-116): the vertex signed distances are
+//                evaluated once per tile vertex next to a cut cell (FP64 wherever a difference can cancel, see
+//                sdf_mixed) and kept in shared memory; the apex/pyramid geometry then runs in FP32 in cell-local
+//                coordinates (vertices on {0,1}^3), where on an axis-aligned hexahedron every term is a product of
+//                non-negative factors and no subtraction cancels, so the result keeps ~1e-7 relative accuracy;
 //      SUBSAMPLE one warp per cut cell, n^3 (3-D) or n^2 (2-D) midpoint samples, each with the same exact inside
 //                test as the vertices.
 // Candidates that the flood fill later leaves out simply have their alpha ignored.
@@ -104,7 +104,7 @@ __device__ inline float face_fraction32(const float* ph, const int8_t* f, int ax
 
 // GeometricTools::calcCellVolume / V.  apz/apz1: local z of the 2-D apex plane and 1 minus it
 // (geometrictools.cpp:57-58), unused in 3-D.
-__device__ float refgeo32(const MeshK& m, const float* ph, int64_t i, int64_t j, int64_t k, float apz, float apz1) {
+static __device__ __noinline__ float refgeo32(const MeshK& m, const float* ph, int64_t i, int64_t j, int64_t k, float apz, float apz1) {
     const int8_t order[8] = {0, 1, 2, 3, 4, 5, 6, 7};
     ApexPair ap = apex_pair(ph, order, 8);
     if (m.twod) { ap.v[2] = apz; ap.w[2] = apz1; }
@@ -129,54 +129,154 @@ __device__ float refgeo32(const MeshK& m, const float* ph, int64_t i, int64_t j,
     return vol;
 }
 
-// ---- SUBSAMPLE: one warp per cut cell -----------------------------------------------------------------------------------
-__device__ float subsample_warp(const MeshK& m, const ShapeK& sh, const float* M, const D3& x, const Q4& q, int64_t i,
-                                int64_t j, int64_t k, int n, unsigned long long* rechecks) {
+// the oracle's FP64 sample point (i + (2a+1)/(2n), ...) and the reference's inside test, out of line (see
+// exact_inside_point)
+static __device__ __noinline__ int exact_inside_sample(const ShapeK& sh, const MeshK& m, int64_t i, int64_t j, int64_t k,
+                                                int a, int b, int c3, int n, const D3& x, const Q4& q) {
+    const double ta64 = (double)(2 * a + 1) / (double)(2 * n), tb64 = (double)(2 * b + 1) / (double)(2 * n);
+    const double tc64 = m.twod ? 0.5 : (double)(2 * c3 + 1) / (double)(2 * n);
+    const D3 p{m.o[0] + ((double)i + ta64) * m.h[0], m.o[1] + ((double)j + tb64) * m.h[1],
+               m.o[2] + ((double)k + tc64) * m.h[2]};
+    return inside64(sh, world2local(p, x, q)) ? 1 : 0;
+}
+
+// the reference's FP64 Solid::phi of mesh point (I,J,K), out of line
+static __device__ __noinline__ float exact_phi_point(const ShapeK& sh, const MeshK& m, int64_t I, int64_t J, int64_t K,
+                                              const D3& x, const Q4& q) {
+    const D3 p{m.o[0] + (double)I * m.h[0], m.o[1] + (double)J * m.h[1], m.o[2] + (double)K * m.h[2]};
+    return (float)sdf64(sh, world2local(p, x, q));
+}
+
+// ---- SUBSAMPLE: one warp per cut cell ----------------------------------------------------------------------------------
+// Each lane owns (a,b) columns of the n x n x n midpoint lattice and walks its column in z.  Local coordinates step by
+// three precomputed vectors (the columns of the world->local map times h), and one error bound covers every sample
+// of the cell; undecided samples are re-evaluated with the oracle's FP64 point formula.
+static __device__ __noinline__ float subsample_warp(const MeshK& m, const ShapeK& sh, const float* M, const TileFrame& tf, int a0, int b0,
+                                int c0, const D3& x, const Q4& q, int64_t i, int64_t j, int64_t k, int n,
+                                unsigned long long* rechecks) {
     const int lane = threadIdx.x & 31;
-    const D3 p0 = mesh_point(m, i, j, k);
-    const TileFrame tf = make_frame(p0 - x, p0, x);
+    const float hx = m.h32[0], hy = m.h32[1], hz = m.h32[2];
+    const float ox = (float)a0 * hx, oy = (float)b0 * hy, oz = (float)c0 * hz;  // cell corner within the tile
+    const float dx = tf.bx + ox, dy = tf.by + oy, dz = tf.bz + oz;
+    const float px = __fmaf_rn(M[0], dx, __fmaf_rn(M[1], dy, M[2] * dz));
+    const float py = __fmaf_rn(M[3], dx, __fmaf_rn(M[4], dy, M[5] * dz));
+    const float pz = __fmaf_rn(M[6], dx, __fmaf_rn(M[7], dy, M[8] * dz));
+    const float sxx = M[0] * hx, sxy = M[3] * hx, sxz = M[6] * hx;
+    const float syx = M[1] * hy, syy = M[4] * hy, syz = M[7] * hy;
+    const float szx = M[2] * hz, szy = M[5] * hz, szz = M[8] * hz;
+    const float hsum = hx + hy + hz;
+    const float E = 8.f * U32 * (tf.babs + fabsf(ox) + fabsf(oy) + fabsf(oz) + 2.f * (fabsf(dx) + fabsf(dy) + fabsf(dz)) +
+                                 3.f * hsum) +
+                    8.f * U32 * (fabsf(px) + fabsf(py) + fabsf(pz) + fabsf(sxx) + fabsf(sxy) + fabsf(sxz) + fabsf(syx) +
+                                 fabsf(syy) + fabsf(syz) + fabsf(szx) + fabsf(szy) + fabsf(szz)) +
+                    tf.e64 + 1e-30f;
     const int nzs = m.twod ? 1 : n;
-    const int K = n * n * nzs;
     const float inv2n = 1.0f / (float)(2 * n);
     int cnt = 0;
-    for (int sidx = lane; sidx < K; sidx += 32) {
-        const int a = sidx % n, b = (sidx / n) % n, c3 = sidx / (n * n);
-        const float ox = (float)(2 * a + 1) * inv2n * m.h32[0];
-        const float oy = (float)(2 * b + 1) * inv2n * m.h32[1];
-        const float oz = (m.twod ? 0.5f : (float)(2 * c3 + 1) * inv2n) * m.h32[2];
-        // the FP32 sample offset carries an extra rounding of (2a+1)/(2n); doubled bound
-        const float dx = tf.bx + ox, dy = tf.by + oy, dz = tf.bz + oz;
-        const float lx = __fmaf_rn(M[0], dx, __fmaf_rn(M[1], dy, M[2] * dz));
-        const float ly = __fmaf_rn(M[3], dx, __fmaf_rn(M[4], dy, M[5] * dz));
-        const float lz = __fmaf_rn(M[6], dx, __fmaf_rn(M[7], dy, M[8] * dz));
-        const float dabs = fabsf(dx) + fabsf(dy) + fabsf(dz);
-        const float E = 8.f * U32 * (tf.babs + fabsf(ox) + fabsf(oy) + fabsf(oz) + 2.f * dabs) + tf.e64 + 1e-30f;
-        int r = inside32(sh, lx, ly, lz, E);
-        if (r == 2) {
-            ++*rechecks;
-            const double ta = (double)(2 * a + 1) / (double)(2 * n), tb = (double)(2 * b + 1) / (double)(2 * n);
-            const double tz = m.twod ? 0.5 : (double)(2 * c3 + 1) / (double)(2 * n);
-            const D3 p{m.o[0] + ((double)i + ta) * m.h[0], m.o[1] + ((double)j + tb) * m.h[1],
-                       m.o[2] + ((double)k + tz) * m.h[2]};
-            r = inside64(sh, world2local(p, x, q)) ? 1 : 0;
+    for (int col = lane; col < n * n; col += 32) {
+        const int a = col % n, b = col / n;
+        const float ta = (float)(2 * a + 1) * inv2n, tb = (float)(2 * b + 1) * inv2n;
+        const float bx = __fmaf_rn(tb, syx, __fmaf_rn(ta, sxx, px));
+        const float by = __fmaf_rn(tb, syy, __fmaf_rn(ta, sxy, py));
+        const float bz = __fmaf_rn(tb, syz, __fmaf_rn(ta, sxz, pz));
+        for (int c3 = 0; c3 < nzs; ++c3) {
+            const float tc = m.twod ? 0.5f : (float)(2 * c3 + 1) * inv2n;
+            int r = inside32(sh, __fmaf_rn(tc, szx, bx), __fmaf_rn(tc, szy, by), __fmaf_rn(tc, szz, bz), E);
+            if (r == 2) {
+                ++*rechecks;
+                r = exact_inside_sample(sh, m, i, j, k, a, b, c3, n, x, q);
+            }
+            cnt += r;
         }
-        cnt += r;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    return (float)((double)cnt / (double)K);
+    return (float)((double)cnt / (double)(n * n * nzs));
 }
 
-// ---- the tile kernel: one warp per (solid, cell-tile) item ---------------------------------------------------------------
-constexpr int CLS_WARPS = 8;
-constexpr int WT_VERTS = 9 * 9 * 3;  // largest warp tile: 8 x 8 x 2 cells
-constexpr int WT_CELLS = 8 * 8 * 2;
+// ---- signed distance for REF-GEO: FP64 where it decides, FP32 where it only scales ------------------------------------
+// The geometry consumes phi in FP32, so phi needs ~1e-7 relative accuracy and the reference's exact sign and filter
+// (|phi| < 1e-8 -> -1e-8).  The local point and every cancelling difference (|p|^2 - r^2, |x| - a, ...) are FP64; the
+// square roots and the final division only scale a non-cancelling quantity and run in FP32.  Values within 1e-6 of
+// the filter threshold are recomputed with the reference's full FP64 sequence by the caller.
+__device__ inline float rect_mixed(double x, double y, double ra, double rb) {
+    const double dx = fabs(x) - ra, dy = fabs(y) - rb;
+    const double dxp = dmax(0.0, dx), dyp = dmax(0.0, dy);
+    return sqrtf((float)(dxp * dxp + dyp * dyp)) + (float)dmin(0.0, dmax(dx, dy));
+}
+static __device__ __noinline__ float sdf_mixed(const ShapeK& s, const D3& p) {
+    const double* a = s.p;
+    const D3 com{s.com[0], s.com[1], s.com[2]};
+    switch (s.type) {
+        case SDFIBM_SHAPE_CIRCLE: {
+            const D3 q = com + D3{p.x, p.y, 0.0};
+            const double qq = magSqr(q);
+            return (float)(qq - a[1]) / (sqrtf((float)qq) + (float)a[0]);
+        }
+        case SDFIBM_SHAPE_SPHERE: {
+            const D3 q = com + p;
+            const double qq = magSqr(q);
+            return (float)(qq - a[1]) / (sqrtf((float)qq) + (float)a[0]);
+        }
+        case SDFIBM_SHAPE_ELLIPSE: {
+            const D3 q = com + p;
+            const double xa = q.x * q.x * a[2], yb = q.y * q.y * a[3];
+            return (float)(0.5 * (xa + yb - 1.0)) / sqrtf((float)(xa * a[2] + yb * a[3]));
+        }
+        case SDFIBM_SHAPE_ELLIPSOID: {
+            const double xa = p.x * p.x * a[3], yb = p.y * p.y * a[4], zc = p.z * p.z * a[5];
+            return (float)(0.5 * (xa + yb + zc - 1.0)) / sqrtf((float)(xa * a[3] + yb * a[4] + zc * a[5]));
+        }
+        case SDFIBM_SHAPE_RECTANGLE: {
+            const D3 q = com + p;
+            return rect_mixed(q.x, q.y, a[0], a[1]);
+        }
+        case SDFIBM_SHAPE_BOX: {
+            const D3 q = com + p;
+            const double dx = fabs(q.x) - a[0], dy = fabs(q.y) - a[1], dz = fabs(q.z) - a[2];
+            const double dxp = dmax(0.0, dx), dyp = dmax(0.0, dy), dzp = dmax(0.0, dz);
+            return sqrtf((float)(dxp * dxp + dyp * dyp + dzp * dzp)) + (float)dmin(0.0, dmax(dz, dmax(dx, dy)));
+        }
+        case SDFIBM_SHAPE_PLANE: return (float)p.y;
+        case SDFIBM_SHAPE_CIRCLE_TAIL: {
+            const D3 q = com + p;
+            const double qq = q.x * q.x + q.y * q.y;
+            const float d1 = (float)(qq - a[3]) / (sqrtf((float)qq) + (float)a[0]);
+            const float d2 = rect_mixed(q.x - a[4], q.y, a[4], a[2]);
+            return fminf(d1, d2);
+        }
+        case SDFIBM_SHAPE_CIRCLE_TWOTAIL: {
+            const D3 q = com + p;
+            const double qq = q.x * q.x + q.y * q.y;
+            const float dc = (float)(qq - a[3]) / (sqrtf((float)qq) + (float)a[0]);
+            const D3 r1 = rot30_64(D3{q.x, q.y, 0.0}), r2 = rot30_64(D3{q.x, -q.y, 0.0});
+            const float d1 = rect_mixed(r1.x - a[4], r1.y, a[4], a[2]);
+            const float d2 = rect_mixed(r2.x - a[4], r2.y, a[4], a[2]);
+            return fminf(dc, fminf(d1, d2));
+        }
+    }
+    return 0.f;
+}
 
-__global__ void __launch_bounds__(CLS_WARPS * 32) classify_kernel(ClassifyArgs A) {
-    __shared__ uint8_t s_vin[CLS_WARPS][WT_VERTS];
-    __shared__ uint8_t s_need[CLS_WARPS][WT_VERTS];
-    __shared__ float s_phi[CLS_WARPS][WT_VERTS];
-    __shared__ uint8_t s_cut[CLS_WARPS][WT_CELLS];
+// filter of sdf.h:147-150 applied to the mixed value; *exact_needed set when the value sits on the threshold
+__device__ inline float filter_mixed(const ShapeK& s, float phi, bool* exact_needed) {
+    if (s.type == SDFIBM_SHAPE_PLANE) return phi;  // the plane's distance is unfiltered and exact
+    const float a = fabsf(phi);
+    if (fabsf(a - 1e-8f) <= 1e-14f) *exact_needed = true;
+    return a < 1e-8f ? -1e-8f : phi;
+}
+
+// ---- the tile kernel: one warp per chunk of up to CHUNK_TILES tiles of one solid ------------------------------------------
+constexpr int CLS_WARPS = 8;
+
+template <int TX, int TY, int TZ>
+__device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
+    constexpr int VX = TX + 1, VY = TY + 1, VZ = TZ + 1, NV = VX * VY * VZ, NC = TX * TY * TZ;
+    __shared__ uint8_t s_vin[CLS_WARPS][NV];
+    __shared__ uint8_t s_need[CLS_WARPS][NV];
+    __shared__ float s_phi[CLS_WARPS][NV];
+    __shared__ uint8_t s_cut[CLS_WARPS][NC];
+    __shared__ uint8_t s_vlist[CLS_WARPS][NV];
     const MeshK& m = A.m;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -186,152 +286,169 @@ __global__ void __launch_bounds__(CLS_WARPS * 32) classify_kernel(ClassifyArgs A
     uint8_t* cutlist = s_cut[w];
     unsigned long long rechecks = 0, valid_cells = 0;
     for (;;) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(&A.cnt->classify_next, 1);
-        item = __shfl_sync(FULL, item, 0);
-        if (item >= A.total_tiles) break;
-        const int s = find_solid(A.tile_prefix, A.S, item);
+        int chunk = 0;
+        if (lane == 0) chunk = atomicAdd(&A.cnt->classify_next, 1);
+        chunk = __shfl_sync(FULL, chunk, 0);
+        if (chunk >= A.total_chunks) break;
+        const int2 ch = A.chunks[chunk];
+        const int s = ch.x;
         const SolidK& k = A.sk[s];
         const SolidPlan& pl = A.plan[s];
-        const int t = item - k.tile_base;
-        const int tx = t % k.ntile[0], ty = (t / k.ntile[0]) % k.ntile[1], tz = t / (k.ntile[0] * k.ntile[1]);
-        const int cx = min(k.tdim[0], k.ext[0] - tx * k.tdim[0]);
-        const int cy = min(k.tdim[1], k.ext[1] - ty * k.tdim[1]);
-        const int cz = min(k.tdim[2], k.ext[2] - tz * k.tdim[2]);
-        const int64_t I0 = (int64_t)pl.lo[0] + tx * k.tdim[0];
-        const int64_t J0 = (int64_t)pl.lo[1] + ty * k.tdim[1];
-        const int64_t K0 = (int64_t)pl.lo[2] + tz * k.tdim[2];
-        const int nc = cx * cy * cz;
-        uint8_t* out = A.cls + k.scratch_off;
-        auto local_index = [&](int a, int b, int c) {
-            return (int64_t)(tx * k.tdim[0] + a) +
-                   (int64_t)k.ext[0] * ((ty * k.tdim[1] + b) + (int64_t)k.ext[1] * (tz * k.tdim[2] + c));
-        };
-        // whole tile outside the mesh or outside the solid's oriented bounding box: no cell has an inside vertex
-        const bool cull = pl.err != 0 || I0 + cx <= 0 || J0 + cy <= 0 || K0 + cz <= 0 || I0 >= m.nx || J0 >= m.ny ||
-                          K0 >= m.nz || I0 + cx < pl.vlo[0] || I0 > pl.vhi[0] || J0 + cy < pl.vlo[1] ||
-                          J0 > pl.vhi[1] || K0 + cz < pl.vlo[2] || K0 > pl.vhi[2];
-        if (cull) {
-            for (int e = lane; e < nc; e += 32) {
-                const int a = e % cx, b = (e / cx) % cy, c = e / (cx * cy);
-                out[local_index(a, b, c)] = 0;
-            }
-            continue;
-        }
+        const int ntile_all = k.ntile[0] * k.ntile[1] * k.ntile[2];
+        const int t_end = min(ch.y + CHUNK_TILES, ntile_all);
         const Q4 q = state_quat(A.st[s]);
         const D3 x = state_pos(A.st[s]);
-        TileFrame tf;
-        {
-            float f5[5] = {0, 0, 0, 0, 0};
-            if (lane == 0) {
-                const D3 p0 = mesh_point(m, I0, J0, K0);
-                tf = make_frame(p0 - x, p0, x);
-                f5[0] = tf.bx; f5[1] = tf.by; f5[2] = tf.bz; f5[3] = tf.babs; f5[4] = tf.e64;
-            }
-#pragma unroll
-            for (int r = 0; r < 5; ++r) f5[r] = __shfl_sync(FULL, f5[r], 0);
-            tf.bx = f5[0]; tf.by = f5[1]; tf.bz = f5[2]; tf.babs = f5[3]; tf.e64 = f5[4];
-        }
         const ShapeK& sh = k.shape;
-        const float* M = pl.M;
-        const int vx = cx + 1, vy = cy + 1, vz = cz + 1, nv = vx * vy * vz;
-        for (int v = lane; v < nv; v += 32) {
-            const int a = v % vx, b = (v / vx) % vy, c = v / (vx * vy);
-            const int64_t I = I0 + a, J = J0 + b, K = K0 + c;
-            uint8_t r = 0;
-            if (I >= pl.vlo[0] && I <= pl.vhi[0] && J >= pl.vlo[1] && J <= pl.vhi[1] && K >= pl.vlo[2] &&
-                K <= pl.vhi[2] && I >= 0 && J >= 0 && K >= 0 && I <= m.nx && J <= m.ny && K <= m.nz) {
-                const float ox = (float)a * m.h32[0], oy = (float)b * m.h32[1], oz = (float)c * m.h32[2];
-                r = (uint8_t)classify_point(sh, M, tf, ox, oy, oz, [&] { return mesh_point(m, I, J, K); }, x, q,
-                                            &rechecks);
-            }
-            vin[v] = r;
-            vneed[v] = 0;
-        }
-        __syncwarp();
+        float M[9];
+#pragma unroll
+        for (int r = 0; r < 9; ++r) M[r] = pl.M[r];
+        const int32_t vlo0 = pl.vlo[0], vlo1 = pl.vlo[1], vlo2 = pl.vlo[2];
+        const int32_t vhi0 = pl.vhi[0], vhi1 = pl.vhi[1], vhi2 = pl.vhi[2];
+        uint8_t* out = A.cls + k.scratch_off;
+        float* alpha = A.alpha + k.scratch_off;
         unsigned long long wmin = ~0ull;
-        int ncut = 0;
-        for (int base = 0; base < nc; base += 32) {
-            const int e = base + lane;
-            uint8_t cls = 0;
-            int a = 0, b = 0, c = 0;
-            if (e < nc) {
-                a = e % cx; b = (e / cx) % cy; c = e / (cx * cy);
+        const float sb[3] = {(float)pl.base[0], (float)pl.base[1], (float)pl.base[2]};
+        for (int t = ch.y; t < t_end; ++t) {
+            const int tx = t % k.ntile[0], ty = (t / k.ntile[0]) % k.ntile[1], tz = t / (k.ntile[0] * k.ntile[1]);
+            const int cx = min(TX, k.ext[0] - tx * TX);
+            const int cy = min(TY, k.ext[1] - ty * TY);
+            const int cz = min(TZ, k.ext[2] - tz * TZ);
+            const int64_t I0 = (int64_t)pl.lo[0] + tx * TX;
+            const int64_t J0 = (int64_t)pl.lo[1] + ty * TY;
+            const int64_t K0 = (int64_t)pl.lo[2] + tz * TZ;
+            auto local_index = [&](int a, int b, int c) {
+                return (int64_t)(tx * TX + a) + (int64_t)k.ext[0] * ((ty * TY + b) + (int64_t)k.ext[1] * (tz * TZ + c));
+            };
+            // whole tile outside the mesh or outside the solid's oriented bounding box: no cell has an inside vertex
+            const bool cull = pl.err != 0 || I0 + cx <= 0 || J0 + cy <= 0 || K0 + cz <= 0 || I0 >= m.nx ||
+                              J0 >= m.ny || K0 >= m.nz || I0 + cx < vlo0 || I0 > vhi0 || J0 + cy < vlo1 ||
+                              J0 > vhi1 || K0 + cz < vlo2 || K0 > vhi2;
+            if (cull) {
+                for (int e = lane; e < NC; e += 32) {
+                    const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
+                    if (a < cx && b < cy && c < cz) out[local_index(a, b, c)] = 0;
+                }
+                continue;
+            }
+            // tile frame in FP32: the solid's FP64 base plus the tile's cell offset; babs covers both roundings
+            TileFrame tf;
+            {
+                const float ofx = (float)(tx * TX) * m.h32[0], ofy = (float)(ty * TY) * m.h32[1],
+                            ofz = (float)(tz * TZ) * m.h32[2];
+                tf.bx = sb[0] + ofx; tf.by = sb[1] + ofy; tf.bz = sb[2] + ofz;
+                tf.babs = fabsf(sb[0]) + fabsf(sb[1]) + fabsf(sb[2]) + 2.f * (fabsf(ofx) + fabsf(ofy) + fabsf(ofz)) +
+                          fabsf(tf.bx) + fabsf(tf.by) + fabsf(tf.bz);
+                tf.e64 = pl.e64;
+            }
+            for (int v = lane; v < NV; v += 32) {
+                const int a = v % VX, b = (v / VX) % VY, c = v / (VX * VY);
                 const int64_t I = I0 + a, J = J0 + b, K = K0 + c;
-                if (I >= 0 && J >= 0 && K >= 0 && I < m.nx && J < m.ny && K < m.nz) {
-                    ++valid_cells;
-                    int cntv = 0;
-#pragma unroll
-                    for (int dz = 0; dz < 2; ++dz)
-#pragma unroll
-                        for (int dy = 0; dy < 2; ++dy)
-#pragma unroll
-                            for (int dx = 0; dx < 2; ++dx) cntv += vin[(a + dx) + vx * ((b + dy) + vy * (c + dz))];
-                    if (cntv == 8) {
-                        cls = 1;
-                    } else if (cntv > 0) {
-                        const float ox = ((float)a + 0.5f) * m.h32[0], oy = ((float)b + 0.5f) * m.h32[1],
-                                    oz = ((float)c + 0.5f) * m.h32[2];
-                        const int ci = classify_point(sh, M, tf, ox, oy, oz, [&] { return mesh_C(m, I, J, K); }, x, q,
-                                                      &rechecks);
-                        cls = ci ? 2 : 3;
+                uint8_t r = 0;
+                if (a <= cx && b <= cy && c <= cz && I >= vlo0 && I <= vhi0 && J >= vlo1 && J <= vhi1 && K >= vlo2 &&
+                    K <= vhi2 && I >= 0 && J >= 0 && K >= 0 && I <= m.nx && J <= m.ny && K <= m.nz) {
+                    const float ox = (float)a * m.h32[0], oy = (float)b * m.h32[1], oz = (float)c * m.h32[2];
+                    r = (uint8_t)classify_point(sh, M, tf, ox, oy, oz, m, I, J, K, 0, x, q, &rechecks);
+                }
+                vin[v] = r;
+                vneed[v] = 0;
+            }
+            __syncwarp();
+            int ncut = 0;
+#pragma unroll 1
+            for (int base = 0; base < NC; base += 32) {
+                const int e = base + lane;
+                const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
+                uint8_t cls = 0;
+                const bool in_tile = e < NC && a < cx && b < cy && c < cz;
+                if (in_tile) {
+                    const int64_t I = I0 + a, J = J0 + b, K = K0 + c;
+                    if (I >= 0 && J >= 0 && K >= 0 && I < m.nx && J < m.ny && K < m.nz) {
+                        ++valid_cells;
+                        const int v0 = a + VX * (b + VY * c);
+                        const int cntv = vin[v0] + vin[v0 + 1] + vin[v0 + VX] + vin[v0 + VX + 1] + vin[v0 + VX * VY] +
+                                         vin[v0 + VX * VY + 1] + vin[v0 + VX * VY + VX] + vin[v0 + VX * VY + VX + 1];
+                        if (cntv == 8) {
+                            cls = 1;
+                        } else if (cntv > 0) {
+                            const float ox = ((float)a + 0.5f) * m.h32[0], oy = ((float)b + 0.5f) * m.h32[1],
+                                        oz = ((float)c + 0.5f) * m.h32[2];
+                            const int ci = classify_point(sh, M, tf, ox, oy, oz, m, I, J, K, 1, x, q, &rechecks);
+                            cls = ci ? 2 : 3;
+                        }
+                        if (cls) wmin = min(wmin, (unsigned long long)(I + (int64_t)m.nx * (J + (int64_t)m.ny * K)));
                     }
-                    if (cls) wmin = min(wmin, (unsigned long long)(I + (int64_t)m.nx * (J + (int64_t)m.ny * K)));
+                    out[local_index(a, b, c)] = cls;
                 }
-                out[local_index(a, b, c)] = cls;
+                // compact the cut candidates of this round
+                const bool is_cut = (cls == 2 || cls == 3) && A.method >= 0;
+                const unsigned bal = __ballot_sync(FULL, is_cut);
+                if (is_cut) {
+                    cutlist[ncut + __popc(bal & ((1u << lane) - 1u))] = (uint8_t)e;
+                    if (A.method == SDFIBM_FRACTION_REFGEO) {
+                        const int v0 = a + VX * (b + VY * c);
+                        vneed[v0] = 1; vneed[v0 + 1] = 1; vneed[v0 + VX] = 1; vneed[v0 + VX + 1] = 1;
+                        vneed[v0 + VX * VY] = 1; vneed[v0 + VX * VY + 1] = 1; vneed[v0 + VX * VY + VX] = 1;
+                        vneed[v0 + VX * VY + VX + 1] = 1;
+                    }
+                }
+                ncut += __popc(bal);
             }
-            // compact the cut candidates of this round
-            const bool is_cut = (cls == 2 || cls == 3) && A.method >= 0;
-            const unsigned bal = __ballot_sync(FULL, is_cut);
-            if (is_cut) {
-                cutlist[ncut + __popc(bal & ((1u << lane) - 1u))] = (uint8_t)e;
-                if (A.method == SDFIBM_FRACTION_REFGEO) {
-#pragma unroll
-                    for (int dz = 0; dz < 2; ++dz)
-#pragma unroll
-                        for (int dy = 0; dy < 2; ++dy)
-#pragma unroll
-                            for (int dx = 0; dx < 2; ++dx) vneed[(a + dx) + vx * ((b + dy) + vy * (c + dz))] = 1;
+            if (ncut == 0) continue;
+            __syncwarp();
+            if (A.method == SDFIBM_FRACTION_REFGEO) {
+                // Solid::phi once per vertex next to a cut candidate.  The needed vertices are compacted first so
+                // every FP64 instruction runs on a full warp; the local point is the solid's FP64 local map applied to
+                // small integer offsets from the bbox corner.
+                uint8_t* vlist = s_vlist[w];
+                int nneed = 0;
+                for (int base = 0; base < NV; base += 32) {
+                    const int v = base + lane;
+                    const bool need = v < NV && vneed[v];
+                    const unsigned bal = __ballot_sync(FULL, need);
+                    if (need) vlist[nneed + __popc(bal & ((1u << lane) - 1u))] = (uint8_t)v;
+                    nneed += __popc(bal);
+                }
+                __syncwarp();
+                const double* L = pl.lmap;
+                for (int u = lane; u < nneed; u += 32) {
+                    const int v = vlist[u];
+                    const int a = v % VX, b = (v / VX) % VY, c = v / (VX * VY);
+                    const double da = (double)(tx * TX + a), db = (double)(ty * TY + b), dc = (double)(tz * TZ + c);
+                    const D3 plc{L[0] + da * L[3] + db * L[6] + dc * L[9], L[1] + da * L[4] + db * L[7] + dc * L[10],
+                                 L[2] + da * L[5] + db * L[8] + dc * L[11]};
+                    bool exact = false;
+                    float ph = filter_mixed(sh, sdf_mixed(sh, plc), &exact);
+                    if (exact || sh.type == SDFIBM_SHAPE_PLANE) ph = exact_phi_point(sh, m, I0 + a, J0 + b, K0 + c, x, q);
+                    vphi[v] = ph;
+                }
+                __syncwarp();
+                for (int u = lane; u < ncut; u += 32) {
+                    const int e = cutlist[u];
+                    const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
+                    const int v0 = a + VX * (b + VY * c);
+                    const float ph[8] = {vphi[v0], vphi[v0 + 1], vphi[v0 + VX], vphi[v0 + VX + 1],
+                                         vphi[v0 + VX * VY], vphi[v0 + VX * VY + 1], vphi[v0 + VX * VY + VX],
+                                         vphi[v0 + VX * VY + VX + 1]};
+                    const int64_t K = K0 + c;
+                    const float apz = m.twod ? (float)((0.0 - mesh_coord(m, 2, K)) / m.h[2]) : 0.f;
+                    const float apz1 = m.twod ? (float)((mesh_coord(m, 2, K + 1) - 0.0) / m.h[2]) : 0.f;
+                    alpha[local_index(a, b, c)] = refgeo32(m, ph, I0 + a, J0 + b, K, apz, apz1);
+                }
+            } else {
+                // SUBSAMPLE (and the fallback of LEARNED): the warp shares the samples of one cut cell
+                for (int u = 0; u < ncut; ++u) {
+                    const int e = cutlist[u];
+                    const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
+                    const float al = subsample_warp(m, sh, M, tf, a, b, c, x, q, I0 + a, J0 + b, K0 + c,
+                                                    A.subsample_n, &rechecks);
+                    if (lane == 0) alpha[local_index(a, b, c)] = al;
                 }
             }
-            ncut += __popc(bal);
+            __syncwarp();
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) wmin = min(wmin, __shfl_xor_sync(FULL, wmin, o));
         if (lane == 0 && wmin != ~0ull) atomicMin(&A.plan[s].min_cand, wmin);
-        if (ncut == 0) continue;
-        __syncwarp();
-        float* alpha = A.alpha + k.scratch_off;
-        if (A.method == SDFIBM_FRACTION_REFGEO) {
-            // Solid::phi (FP64) once per vertex next to a cut candidate
-            for (int v = lane; v < nv; v += 32) {
-                if (!vneed[v]) continue;
-                const int a = v % vx, b = (v / vx) % vy, c = v / (vx * vy);
-                vphi[v] = (float)sdf64(sh, world2local(mesh_point(m, I0 + a, J0 + b, K0 + c), x, q));
-            }
-            __syncwarp();
-            for (int u = lane; u < ncut; u += 32) {
-                const int e = cutlist[u];
-                const int a = e % cx, b = (e / cx) % cy, c = e / (cx * cy);
-                float ph[8];
-#pragma unroll
-                for (int sl = 0; sl < 8; ++sl)
-                    ph[sl] = vphi[(a + (sl & 1)) + vx * ((b + ((sl >> 1) & 1)) + vy * (c + ((sl >> 2) & 1)))];
-                const int64_t K = K0 + c;
-                const float apz = m.twod ? (float)((0.0 - mesh_coord(m, 2, K)) / m.h[2]) : 0.f;
-                const float apz1 = m.twod ? (float)((mesh_coord(m, 2, K + 1) - 0.0) / m.h[2]) : 0.f;
-                alpha[local_index(a, b, c)] = refgeo32(m, ph, I0 + a, J0 + b, K, apz, apz1);
-            }
-        } else {
-            // SUBSAMPLE (and the fallback of LEARNED): the warp shares the samples of one cut cell
-            for (int u = 0; u < ncut; ++u) {
-                const int e = cutlist[u];
-                const int a = e % cx, b = (e / cx) % cy, c = e / (cx * cy);
-                const float al = subsample_warp(m, sh, M, x, q, I0 + a, J0 + b, K0 + c, A.subsample_n, &rechecks);
-                if (lane == 0) alpha[local_index(a, b, c)] = al;
-            }
-        }
-        __syncwarp();
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -343,5 +460,9 @@ __global__ void __launch_bounds__(CLS_WARPS * 32) classify_kernel(ClassifyArgs A
         if (valid_cells) atomicAdd(&A.cnt->bbox_cells, valid_cells);
     }
 }
+
+// 3-D meshes: 4x4x4-cell tiles; one- and two-layer meshes: 8x8x2
+__global__ void __launch_bounds__(CLS_WARPS * 32) classify_kernel_3d(ClassifyArgs A) { classify_body<4, 4, 4>(A); }
+__global__ void __launch_bounds__(CLS_WARPS * 32) classify_kernel_2d(ClassifyArgs A) { classify_body<8, 8, 2>(A); }
 
 }  // namespace sdfibm_dev

@@ -39,11 +39,21 @@ __device__ inline TileFrame make_frame(const D3& b, const D3& p0, const D3& x) {
     return tf;
 }
 
-// p_exact is only evaluated (FP64, with the oracle's point formula) when the FP32 test cannot decide
-template <class ExactPoint>
+// The reference's FP64 inside test of mesh point (I,J,K) (centre: of cell (I,J,K)).  Kept out of line so the
+// compiler cannot evaluate it speculatively on the FP32 fast path: it only runs for undecided points.
+static __device__ __noinline__ int exact_inside_point(const ShapeK& sh, const MeshK& m, int64_t I, int64_t J, int64_t K,
+                                               int centre, const D3& x, const Q4& q) {
+    const D3 p = centre ? D3{m.o[0] + ((double)I + 0.5) * m.h[0], m.o[1] + ((double)J + 0.5) * m.h[1],
+                             m.o[2] + ((double)K + 0.5) * m.h[2]}
+                        : D3{m.o[0] + (double)I * m.h[0], m.o[1] + (double)J * m.h[1], m.o[2] + (double)K * m.h[2]};
+    return inside64(sh, world2local(p, x, q)) ? 1 : 0;
+}
+
+// FP32 inside test of a point given by its offset (ox,oy,oz) from the tile frame's base point, with the FP64
+// re-check inside the guard band
 __device__ inline int classify_point(const ShapeK& sh, const float* M, const TileFrame& tf, float ox, float oy,
-                                     float oz, const ExactPoint& p_exact, const D3& x, const Q4& q,
-                                     unsigned long long* rechecks) {
+                                     float oz, const MeshK& m, int64_t I, int64_t J, int64_t K, int centre,
+                                     const D3& x, const Q4& q, unsigned long long* rechecks) {
     const float dx = tf.bx + ox, dy = tf.by + oy, dz = tf.bz + oz;
     const float lx = __fmaf_rn(M[0], dx, __fmaf_rn(M[1], dy, M[2] * dz));
     const float ly = __fmaf_rn(M[3], dx, __fmaf_rn(M[4], dy, M[5] * dz));
@@ -53,7 +63,7 @@ __device__ inline int classify_point(const ShapeK& sh, const float* M, const Til
     int r = inside32(sh, lx, ly, lz, E);
     if (r == 2) {
         ++*rechecks;  // caller-local counter
-        r = inside64(sh, world2local(p_exact(), x, q)) ? 1 : 0;
+        r = exact_inside_point(sh, m, I, J, K, centre, x, q);
     }
     return r;
 }

@@ -128,10 +128,67 @@ __global__ void plan_kernel(MeshK m, const SolidK* __restrict__ sk, const sdfibm
                     if (best < 0 || d < bd || (d == bd && c < best)) { bd = d; best = c; }
                 }
         p.seed = best;
+        const int64_t si = best % m.nx, sj = (best / m.nx) % m.ny, sk3 = best / ((int64_t)m.nx * m.ny);
+        p.seed_ijk[0] = (int32_t)si; p.seed_ijk[1] = (int32_t)sj; p.seed_ijk[2] = (int32_t)sk3;
+        p.pad1 = 0;
+        const D3 cb = mesh_C(m, si, sj, sk3) - x;
+        p.cbase[0] = cb.x; p.cbase[1] = cb.y; p.cbase[2] = cb.z;
+    }
+    // FP64 origin of the tile frames and the local map (world2local of the bbox corner plus the images of the cell
+    // edge vectors), so tiles build their frames without per-tile FP64 work
+    {
+        const D3 p0 = mesh_point(m, p.lo[0], p.lo[1], p.lo[2]);
+        const D3 b = p0 - x;
+        p.base[0] = b.x; p.base[1] = b.y; p.base[2] = b.z;
+        const D3 cl = world2local(p0, x, q);
+        const Q4 qc = qconj(q);
+        const D3 lx = qtransform(qc, D3{m.h[0], 0, 0}), ly = qtransform(qc, D3{0, m.h[1], 0}),
+                 lz = qtransform(qc, D3{0, 0, m.h[2]});
+        const double l12[12] = {cl.x, cl.y, cl.z, lx.x, lx.y, lx.z, ly.x, ly.y, ly.z, lz.x, lz.y, lz.z};
+        for (int r = 0; r < 12; ++r) p.lmap[r] = l12[r];
+        const D3 pf = mesh_point(m, (int64_t)p.lo[0] + k.ext[0], (int64_t)p.lo[1] + k.ext[1], (int64_t)p.lo[2] + k.ext[2]);
+        p.e64 = (float)(2e-15 * (fabs(p0.x) + fabs(p0.y) + fabs(p0.z) + fabs(pf.x) + fabs(pf.y) + fabs(pf.z) + fabs(x.x) +
+                                 fabs(x.y) + fabs(x.z)));
+        p.pad2 = 0.f;
     }
     p.min_cand = ~0ull;
     p.n_inside = p.n_cut = 0;
     plan[s] = p;
+}
+
+// ---- claims ----------------------------------------------------------------------------------------------------------
+// Ct during a call holds claim words CT_KEY_BASE | (solid << 2 | type); CT_SHARED is set once a second solid touches
+// the cell and the low bits then keep the largest claim (the last solid of the reference's serial loop).  Any value
+// below CT_KEY_BASE -- zero, or the decoded Ct a previous call left -- is an unclaimed cell.
+// One atomicMax claims the cell (any previous value is below every claim word); seeing another claim of this call
+// in its return value, the claimer raises the word to the larger claim with CT_SHARED set.
+__device__ inline void claim_cell(int32_t* Ct, int32_t cell, int32_t s, int type) {
+    uint32_t* C = reinterpret_cast<uint32_t*>(Ct) + cell;
+    const uint32_t key = CT_KEY_BASE | ((uint32_t)s << 2) | (uint32_t)type;
+    const uint32_t old = atomicMax(C, key);
+    if (old >= CT_KEY_BASE) atomicMax(C, max(key, old & ~CT_SHARED) | CT_SHARED);
+}
+
+// claim pass over this call's lists
+__global__ void claim_kernel(const int32_t* __restrict__ in_cell, const int32_t* __restrict__ in_solid,
+                             const int32_t* __restrict__ cut_cell, const int32_t* __restrict__ cut_solid,
+                             int32_t* __restrict__ Ct, const Counters* cnt, int64_t N) {
+    const int n_in = clamp_len(cnt->n_inside, cnt->list_cap), n_cut = clamp_len(cnt->n_cut, cnt->list_cap);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)n_in + n_cut;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const bool cut = e >= n_in;
+        const int64_t ee = cut ? e - n_in : e;
+        const int32_t c = cut ? cut_cell[ee] : in_cell[ee];
+        const int32_t sw = cut ? cut_solid[ee] : in_solid[ee];
+        if (c < 0 || c >= N) continue;
+        claim_cell(Ct, c, sw & LIST_SOLID_MASK, list_type(sw));
+    }
+}
+
+__device__ inline int32_t decode_claim(uint32_t w) {
+    const uint32_t k = (w & ~CT_SHARED) - CT_KEY_BASE;
+    const int32_t s = (int32_t)(k >> 2), code = (int32_t)(k & 3);
+    return code == 1 ? s + 4 : code;
 }
 
 // ---- connect: bit-parallel flood fill --------------------------------------------------------------------------------
@@ -363,34 +420,6 @@ __device__ inline int shared_slot(const CoupleArgs& A, int32_t c) {
     return -1;
 }
 
-// claim pass: Ct[c] <- claim word of the touching solid, CT_SHARED with the largest claim when several touch it
-__global__ void claim_kernel(const int32_t* __restrict__ in_cell, const int32_t* __restrict__ in_solid,
-                             const int32_t* __restrict__ cut_cell, const int32_t* __restrict__ cut_solid,
-                             int32_t* __restrict__ Ct, const Counters* cnt, int64_t N) {
-    const int n_in = clamp_len(cnt->n_inside, cnt->list_cap), n_cut = clamp_len(cnt->n_cut, cnt->list_cap);
-    uint32_t* C = reinterpret_cast<uint32_t*>(Ct);
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)n_in + n_cut;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const bool cut = e >= n_in;
-        const int64_t ee = cut ? e - n_in : e;
-        const int32_t c = cut ? cut_cell[ee] : in_cell[ee];
-        const int32_t sw = cut ? cut_solid[ee] : in_solid[ee];
-        if (c < 0 || c >= N) continue;
-        const uint32_t key = CT_KEY_BASE | ((uint32_t)(sw & LIST_SOLID_MASK) << 2) | (uint32_t)list_type(sw);
-        const uint32_t v = atomicCAS(C + c, 0u, key);
-        if (v != 0u) {
-            const uint32_t lo = max(key, v & ~CT_SHARED);
-            atomicMax(C + c, lo | CT_SHARED);
-        }
-    }
-}
-
-__device__ inline int32_t decode_claim(uint32_t w) {
-    const uint32_t k = (w & ~CT_SHARED) - CT_KEY_BASE;
-    const int32_t s = (int32_t)(k >> 2), code = (int32_t)(k & 3);
-    return code == 1 ? s + 4 : code;
-}
-
 // ---- couple ---------------------------------------------------------------------------------------------------------
 constexpr int CPL_THREADS = 256;
 
@@ -434,25 +463,46 @@ __global__ void __launch_bounds__(CPL_THREADS) couple_kernel(CoupleArgs A) {
                 alpha = (double)A.alpha[ks.scratch_off + li];
             }
             // pcHydrodynamicInteraction (solidcloud.cpp:384-390) and the accumulation of :411-421
-            const D3 cc = mesh_C(m, i, j, k);
-            const D3 vel{st.vel[0], st.vel[1], st.vel[2]}, om{st.omega[0], st.omega[1], st.omega[2]};
-            const D3 uf{(double)A.U[c], (double)A.U[N + c], (double)A.U[2 * N + c]};
-            const D3 us = vel + cross(om, cc - x);
-            const D3 f_ = alpha * (uf - us);
-            const D3 t_ = cross(cc - x, f_);
-            const double cv = m.V;
-            const D3 F = f_ * cv * A.dtINV, T = t_ * cv * A.dtINV;
-            f6[0] = F.x; f6[1] = F.y; f6[2] = F.z; f6[3] = T.x; f6[4] = T.y; f6[5] = T.z;
-            const D3 fs = f_ * A.dtINV;
-            (void)type;
+            const float Ux = A.U[c], Uy = A.U[N + c], Uz = A.U[2 * N + c];
+            D3 fs;
+            if (A.exact_forcing) {
+                // the reference's FP64 sequence
+                const D3 cc = mesh_C(m, i, j, k);
+                const D3 vel{st.vel[0], st.vel[1], st.vel[2]}, om{st.omega[0], st.omega[1], st.omega[2]};
+                const D3 uf{(double)Ux, (double)Uy, (double)Uz};
+                const D3 us = vel + cross(om, cc - x);
+                const D3 f_ = alpha * (uf - us);
+                const D3 t_ = cross(cc - x, f_);
+                const double cv = m.V;
+                const D3 F = f_ * cv * A.dtINV, T = t_ * cv * A.dtINV;
+                f6[0] = F.x; f6[1] = F.y; f6[2] = F.z; f6[3] = T.x; f6[4] = T.y; f6[5] = T.z;
+                fs = f_ * A.dtINV;
+            } else {
+                // FP32: the offset C - x is the solid's FP64 seed offset plus a small integer number of cells
+                const SolidPlan& pl = A.plan[s];
+                const float dx = __fmaf_rn((float)(i - pl.seed_ijk[0]), m.h32[0], (float)pl.cbase[0]);
+                const float dy = __fmaf_rn((float)(j - pl.seed_ijk[1]), m.h32[1], (float)pl.cbase[1]);
+                const float dz = __fmaf_rn((float)(k - pl.seed_ijk[2]), m.h32[2], (float)pl.cbase[2]);
+                const float ox = (float)st.omega[0], oy = (float)st.omega[1], oz = (float)st.omega[2];
+                const float usx = (float)st.vel[0] + (oy * dz - oz * dy);
+                const float usy = (float)st.vel[1] + (oz * dx - ox * dz);
+                const float usz = (float)st.vel[2] + (ox * dy - oy * dx);
+                const float al = (float)alpha;
+                const float fx = al * (Ux - usx), fy = al * (Uy - usy), fz = al * (Uz - usz);
+                const float k1 = (float)(m.V * A.dtINV), di = (float)A.dtINV;
+                f6[0] = fx * k1; f6[1] = fy * k1; f6[2] = fz * k1;
+                f6[3] = (dy * fz - dz * fy) * k1; f6[4] = (dz * fx - dx * fz) * k1; f6[5] = (dx * fy - dy * fx) * k1;
+                fs = D3{fx * di, fy * di, fz * di};
+            }
             const uint32_t claim = reinterpret_cast<const uint32_t*>(A.Ct)[c];
             if (!(claim & CT_SHARED)) {
-                // the only solid on this cell: As += alpha etc. on zeroed fields is a plain store
-                A.As[c] = (float)alpha;
+                // the only solid on this cell: the final values (As += alpha on a zeroed field, checkAlpha, Ct)
+                A.As[c] = fminf((float)alpha, 1.0f);
                 A.Ts[c] = (float)alpha;
                 A.Fs[c] = (float)fs.x;
                 A.Fs[N + c] = (float)fs.y;
                 A.Fs[2 * N + c] = (float)fs.z;
+                A.Ct[c] = type == 1 ? s + 4 : type;
             } else {
                 const int slot = shared_slot(A, (int32_t)c);
                 if (slot >= 0) {
@@ -484,44 +534,38 @@ __global__ void __launch_bounds__(CPL_THREADS) couple_kernel(CoupleArgs A) {
     }
 }
 
-// ---- finalize ---------------------------------------------------------------------------------------------------------
-__global__ void finalize_kernel(const int32_t* __restrict__ in_cell, const int32_t* __restrict__ in_solid,
-                                const int32_t* __restrict__ cut_cell, const int32_t* __restrict__ cut_solid,
-                                float* __restrict__ As, float* __restrict__ Ts, float* __restrict__ Fs,
-                                int32_t* __restrict__ Ct, Counters* cnt, int64_t N, int32_t* __restrict__ sh_keys,
+// ---- finalize: cells shared by several solids ---------------------------------------------------------------------------
+// FP64 sums rounded once to the FP32 fields, Ct decoded from the largest claim, As = min(As, 1) (checkAlpha); the slot
+// is cleared for the next call.
+__global__ void finalize_kernel(float* __restrict__ As, float* __restrict__ Ts, float* __restrict__ Fs,
+                                int32_t* __restrict__ Ct, const Counters* cnt, int64_t N, int32_t* __restrict__ sh_keys,
                                 double* __restrict__ sh_vals, const int32_t* __restrict__ sh_used, int32_t sh_mask) {
-    const int n_in = clamp_len(cnt->n_inside, cnt->list_cap), n_cut = clamp_len(cnt->n_cut, cnt->list_cap);
     const int n_sh = min(cnt->n_shared, sh_mask + 1);
     uint32_t* C = reinterpret_cast<uint32_t*>(Ct);
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)n_in + n_cut + n_sh;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        if (e < (int64_t)n_in + n_cut) {
-            // cells of one solid: decode the claim, As = min(As, 1) (checkAlpha)
-            const bool cut = e >= n_in;
-            const int64_t ee = cut ? e - n_in : e;
-            const int32_t c = cut ? cut_cell[ee] : in_cell[ee];
-            if (c < 0 || c >= N) continue;
-            const uint32_t v = C[c];
-            if (v < CT_KEY_BASE || (v & CT_SHARED)) continue;
-            Ct[c] = decode_claim(v);
-            As[c] = fminf(As[c], 1.0f);
-        } else {
-            // shared cells: FP64 sums rounded once to the FP32 fields; the slot is cleared for the next call
-            const int slot = sh_used[e - n_in - n_cut];
-            const int32_t c = sh_keys[slot];
-            double* v = sh_vals + 5 * (int64_t)slot;
-            if (c >= 0 && c < N) {
-                Ct[c] = decode_claim(C[c]);
-                As[c] = (float)fmin(v[0], 1.0);
-                Ts[c] = (float)v[1];
-                Fs[c] = (float)v[2];
-                Fs[N + c] = (float)v[3];
-                Fs[2 * N + c] = (float)v[4];
-            }
-            for (int r = 0; r < 5; ++r) v[r] = 0.0;
-            sh_keys[slot] = -1;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_sh; e += (int64_t)gridDim.x * blockDim.x) {
+        const int slot = sh_used[e];
+        const int32_t c = sh_keys[slot];
+        double* v = sh_vals + 5 * (int64_t)slot;
+        if (c >= 0 && c < N) {
+            Ct[c] = decode_claim(C[c]);
+            As[c] = (float)fmin(v[0], 1.0);
+            Ts[c] = (float)v[1];
+            Fs[c] = (float)v[2];
+            Fs[N + c] = (float)v[3];
+            Fs[2 * N + c] = (float)v[4];
         }
+        for (int r = 0; r < 5; ++r) v[r] = 0.0;
+        sh_keys[slot] = -1;
     }
+}
+
+// per-call counters: the previous lengths are kept for the sparse reset
+__global__ void begin_kernel(Counters* cnt) {
+    cnt->prev_n_inside = cnt->n_inside;
+    cnt->prev_n_cut = cnt->n_cut;
+    cnt->classify_next = 0; cnt->couple_next = 0; cnt->finalize_next = 0;
+    cnt->n_inside = 0; cnt->n_cut = 0; cnt->n_shared = 0;
+    cnt->exact_rechecks = 0; cnt->bbox_cells = 0;
 }
 
 __global__ void ft_kernel(const double* __restrict__ ftacc, double* __restrict__ ft, int S, double rho_f) {
@@ -530,14 +574,16 @@ __global__ void ft_kernel(const double* __restrict__ ftacc, double* __restrict__
     for (int r = 0; r < 6; ++r) ft[6 * s + r] = ftacc[6 * s + r] * rho_f;
 }
 
-// sparse reset of the previous call's touched cells
-__global__ void reset_kernel(const int32_t* __restrict__ in_cell, const int32_t* __restrict__ cut_cell,
+// sparse reset: the cells the previous call touched and this call does not (after this call's claims, before the
+// couple pass writes the claimed cells) go back to zero -- the sparse form of solidcloud.cpp:438-441
+__global__ void reset_kernel(const int32_t* __restrict__ prev_in_cell, const int32_t* __restrict__ prev_cut_cell,
                              const Counters* cnt, int64_t N, float* As, float* Fs, float* Ts, int32_t* Ct) {
-    const int n_in = clamp_len(cnt->n_inside, cnt->list_cap), n_cut = clamp_len(cnt->n_cut, cnt->list_cap);
+    const int n_in = clamp_len(cnt->prev_n_inside, cnt->list_cap), n_cut = clamp_len(cnt->prev_n_cut, cnt->list_cap);
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)n_in + n_cut;
          e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t c = e < n_in ? in_cell[e] : cut_cell[e - n_in];
+        const int64_t c = e < n_in ? prev_in_cell[e] : prev_cut_cell[e - n_in];
         if (c < 0 || c >= N) continue;
+        if (reinterpret_cast<const uint32_t*>(Ct)[c] >= CT_KEY_BASE) continue;  // claimed now: rewritten below
         As[c] = 0.f; Ts[c] = 0.f; Ct[c] = 0;
         Fs[c] = 0.f; Fs[N + c] = 0.f; Fs[2 * N + c] = 0.f;
     }

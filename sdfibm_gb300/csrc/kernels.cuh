@@ -41,6 +41,13 @@ struct SolidPlan {
     unsigned long long min_cand;  // lowest cell label with an inside vertex (atomicMin), ~0 when none
     float M[9];               // FP32 world->local matrix (|q|^2 R^T)
     int32_t n_inside, n_cut;  // touched cells by kind
+    int32_t seed_ijk[3];      // cell indices of the seed cell
+    int32_t pad1;
+    double cbase[3];          // centre of the seed cell minus the solid centre (FP64), origin of FP32 cell offsets
+    double base[3];           // mesh point (lo) minus the solid centre: FP64 origin of the FP32 tile frames
+    double lmap[12];          // world2local of mesh point (lo), then the local images of h_x e_x, h_y e_y, h_z e_z
+    float e64;                // bound of the FP64 rounding of point coordinates (see TileFrame)
+    float pad2;
     double cw[3];             // centre of the bounding sphere (2-D shapes: of the bounding disc)
     double rcull;             // its radius
     int32_t vlo[3], vhi[3];   // mesh-vertex index box of the solid's oriented bounding box: vertices outside it are
@@ -52,11 +59,13 @@ struct Counters {
     int32_t classify_next;
     int32_t couple_next;
     int32_t finalize_next;
-    int32_t n_inside;         // entries in the ALL_INSIDE list
-    int32_t n_cut;            // entries in the cut-cell list
+    int32_t n_inside;         // entries in the ALL_INSIDE list of this call
+    int32_t n_cut;            // entries in the cut-cell list of this call
     int32_t n_shared;         // cells touched by two or more solids this call (slots used in the shared table)
-    int32_t pad0;
+    int32_t prev_n_inside;    // list lengths of the previous call (its lists stay for the sparse reset)
+    int32_t prev_n_cut;
     int32_t error;            // first error code seen on the device
+    int32_t pad0;
     unsigned long long exact_rechecks;  // FP32-undecided points re-evaluated in FP64
     unsigned long long bbox_cells;
     int32_t launches;
@@ -101,14 +110,16 @@ constexpr uint32_t CT_KEY_BASE = 1u << 30;
 constexpr uint32_t CT_SHARED = 1u << 31;
 constexpr int SHARED_MAX_PROBES = 64;
 
+// classify work items: up to CHUNK_TILES consecutive tiles of one solid
+constexpr int CHUNK_TILES = 8;
+
 struct ClassifyArgs {
     MeshK m;
     const SolidK* sk;
     const sdfibm_solid_state* st;
     SolidPlan* plan;
-    const int32_t* tile_prefix;
-    int S;
-    int total_tiles;
+    const int2* chunks;  // (solid, first tile)
+    int total_chunks;
     uint8_t* cls;      // class byte per bbox cell
     float* alpha;      // solid fraction per bbox cell (cut candidates only)
     Counters* cnt;

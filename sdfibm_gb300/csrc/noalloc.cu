@@ -28,7 +28,8 @@
 namespace sdfibm_dev {
 __global__ void plan_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state* st, SolidPlan* plan, int S,
                             Counters* cnt);
-__global__ void classify_kernel(ClassifyArgs A);
+__global__ void classify_kernel_3d(ClassifyArgs A);
+__global__ void classify_kernel_2d(ClassifyArgs A);
 __global__ void connect_kernel(MeshK m, const SolidK* sk, SolidPlan* plan, const uint8_t* scratch, uint32_t* gbitmaps,
                                int32_t* in_cell, int32_t* in_solid, int32_t* cut_cell, int32_t* cut_solid,
                                int64_t cap_in, int64_t cap_cut, Counters* cnt, int smem_words);
@@ -46,8 +47,9 @@ constexpr size_t OFF_SK = 0;
 constexpr size_t OFF_ST = OFF_SK + na_align(sizeof(SolidK));
 constexpr size_t OFF_PLAN = OFF_ST + na_align(sizeof(sdfibm_solid_state));
 constexpr size_t OFF_CNT = OFF_PLAN + na_align(sizeof(SolidPlan));
-constexpr size_t OFF_PREFIX = OFF_CNT + na_align(sizeof(Counters));
-constexpr size_t OFF_CLS = OFF_PREFIX + 256;
+constexpr int64_t NA_MAX_CHUNKS = 8192;           // classify work items of the one solid
+constexpr size_t OFF_CHUNKS = OFF_CNT + na_align(sizeof(Counters));
+constexpr size_t OFF_CLS = OFF_CHUNKS + na_align(sizeof(int2) * NA_MAX_CHUNKS);
 constexpr size_t OFF_BITMAP = OFF_CLS + na_align(NA_MAX_BBOX_CELLS);
 constexpr size_t LIST_BYTES = na_align(4 * NA_MAX_BBOX_CELLS);
 constexpr size_t OFF_IN_CELL = OFF_BITMAP + na_align(4 * NA_MAX_BITMAP_WORDS);
@@ -125,10 +127,10 @@ bool solid_record(const sdfibm_mesh_desc& mesh, const sdfibm_solid_desc& d, Soli
     }
     if (!k.infinite && prism && !(d.quat[1] == 0.0 && d.quat[2] == 0.0))
         for (int a = 0; a < 2; ++a) k.ext[a] = n3[a] + 4;
-    const int tz = k.ext[2] < 4 ? k.ext[2] : 4;
-    k.tdim[2] = tz <= 2 ? tz : 4;
-    k.tdim[0] = tz <= 2 ? 8 : 4;
-    k.tdim[1] = tz <= 2 ? 8 : 4;
+    const bool layer = mesh.nz <= 2;
+    k.tdim[0] = layer ? 8 : 4;
+    k.tdim[1] = layer ? 8 : 4;
+    k.tdim[2] = layer ? 2 : 4;
     for (int a = 0; a < 3; ++a) k.ntile[a] = (k.ext[a] + k.tdim[a] - 1) / k.tdim[a];
     k.tile_base = 0;
     k.scratch_off = 0;
@@ -144,6 +146,12 @@ bool solid_record(const sdfibm_mesh_desc& mesh, const sdfibm_solid_desc& d, Soli
 }  // namespace
 
 namespace sdfibm_dev {
+
+// classify work items of the single solid: (0, first tile of each chunk)
+__global__ void noalloc_chunks_kernel(int2* chunks, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) chunks[i] = make_int2(0, i * CHUNK_TILES);
+}
 
 // Writes the enumeration result in the order of sdfibm_cuda_touched: ALL_INSIDE cells ascending, then
 // CENTER_INSIDE ascending, then CENTER_OUTSIDE ascending (a stable partition of the cut list by type).  *n receives
@@ -229,6 +237,8 @@ extern "C" int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc* mesh, const s
     const int64_t words = 2 * (int64_t)k.ext[1] * k.ext[2] * ((k.ext[0] + 31) / 32);
     if (bbox > NA_MAX_BBOX_CELLS || words > NA_MAX_BITMAP_WORDS) return SDFIBM_ERR_CAPACITY;
     const int ntiles = k.ntile[0] * k.ntile[1] * k.ntile[2];
+    const int nchunks = (ntiles + CHUNK_TILES - 1) / CHUNK_TILES;
+    if (nchunks > NA_MAX_CHUNKS) return SDFIBM_ERR_CAPACITY;
 
     void* base = nullptr;
     if (scratch_address(&base) != cudaSuccess) return SDFIBM_ERR_CUDA;
@@ -249,27 +259,27 @@ extern "C" int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc* mesh, const s
     Counters c0;
     std::memset(&c0, 0, sizeof(c0));
     c0.list_cap = NA_MAX_BBOX_CELLS;  // counters start from zero on every call
-    const int32_t prefix[2] = {0, ntiles};
 
     SolidK* d_sk = reinterpret_cast<SolidK*>(b + OFF_SK);
     sdfibm_solid_state* d_st = reinterpret_cast<sdfibm_solid_state*>(b + OFF_ST);
     SolidPlan* d_plan = reinterpret_cast<SolidPlan*>(b + OFF_PLAN);
     Counters* d_cnt = reinterpret_cast<Counters*>(b + OFF_CNT);
-    int32_t* d_prefix = reinterpret_cast<int32_t*>(b + OFF_PREFIX);
+    int2* d_chunks = reinterpret_cast<int2*>(b + OFF_CHUNKS);
     if (cudaMemcpyAsync(d_sk, &k, sizeof(k), cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemcpyAsync(d_st, &x, sizeof(x), cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaMemcpyAsync(d_cnt, &c0, sizeof(c0), cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaMemcpyAsync(d_prefix, prefix, sizeof(prefix), cudaMemcpyHostToDevice, st) != cudaSuccess)
+        cudaMemcpyAsync(d_cnt, &c0, sizeof(c0), cudaMemcpyHostToDevice, st) != cudaSuccess)
         return SDFIBM_ERR_CUDA;
+    noalloc_chunks_kernel<<<(nchunks + 255) / 256, 256, 0, st>>>(d_chunks, nchunks);
     plan_kernel<<<1, 32, 0, st>>>(m, d_sk, d_st, d_plan, 1, d_cnt);
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return SDFIBM_ERR_CUDA;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int grid = ntiles < 4 * (sms > 0 ? sms : 1) ? ntiles : 4 * (sms > 0 ? sms : 1);
+    const int grid = nchunks < 4 * (sms > 0 ? sms : 1) ? nchunks : 4 * (sms > 0 ? sms : 1);
     ClassifyArgs CA;
-    CA.m = m; CA.sk = d_sk; CA.st = d_st; CA.plan = d_plan; CA.tile_prefix = d_prefix; CA.S = 1; CA.total_tiles = ntiles;
+    CA.m = m; CA.sk = d_sk; CA.st = d_st; CA.plan = d_plan; CA.chunks = d_chunks; CA.total_chunks = nchunks;
     CA.cls = b + OFF_CLS; CA.alpha = nullptr; CA.cnt = d_cnt; CA.method = -1; CA.subsample_n = 0;
-    classify_kernel<<<grid, 256, 0, st>>>(CA);
+    if (m.nz <= 2) classify_kernel_2d<<<grid, 256, 0, st>>>(CA);
+    else classify_kernel_3d<<<grid, 256, 0, st>>>(CA);
     connect_kernel<<<1, 512, 0, st>>>(m, d_sk, d_plan, b + OFF_CLS, reinterpret_cast<uint32_t*>(b + OFF_BITMAP),
                                       reinterpret_cast<int32_t*>(b + OFF_IN_CELL), reinterpret_cast<int32_t*>(b + OFF_IN_SOLID),
                                       reinterpret_cast<int32_t*>(b + OFF_CUT_CELL), reinterpret_cast<int32_t*>(b + OFF_CUT_SOLID),
