@@ -7,7 +7,11 @@ enumeration of every solid's touched cells, solid fraction, direct forcing and f
 value = sum over solids of |touched cells| / device time of the step (CUDA events, L2 flushed between steps).
 e2e = the same metric through the host-buffer entry point (U copied in, As/Fs/Ts/Ct + force/torque copied out).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--config poly3d_512] [--method refgeo|subsample]
+The default method is the learned cut-cell fraction (network + SUBSAMPLE(16^3) fallback outside its band).  The
+same run times the plain SUBSAMPLE(10^3) path ("plain") and measures the learned As and per-solid force against a
+SUBSAMPLE(16^3) step ("accuracy"; that evaluator's classifications equal the FP64 oracle's).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config poly3d_512] [--method learned|subsample|refgeo]
   python bench.py --impl reference ...   the CPU restatement of the reference's coupling (faithful data
                                           structures, single thread), timed on a bounded sample of solids
 With N > 1 (torchrun) every rank runs an independent replica: the path has no exchange step on one mesh per GPU
@@ -103,8 +107,83 @@ def make_workload(args):
     from sdfibm_gb300 import abi, workloads
     w = workloads.CONFIGS[args.config](scale=args.scale)
     w.opt.fraction_method = METHODS[args.method]
-    w.opt.exact_forcing = 0 if getattr(args, "fp32_forcing", False) else 1
+    w.opt.exact_forcing = 1 if getattr(args, "exact_forcing", False) else 0
+    if args.method == "learned":
+        w.opt.learned_fallback_n = 16
+    elif args.method == "subsample":
+        w.opt.subsample_n = 10
     return w
+
+
+def make_cloud(w, method, subsample_n=None):
+    """A coupling context of workload w with the given fraction method (the learned model loaded if needed)."""
+    import copy
+
+    from sdfibm_gb300 import abi, learned
+    from sdfibm_gb300.cloud import SolidCloud
+    opt = copy.copy(w.opt)
+    opt.fraction_method = METHODS[method]
+    if subsample_n:
+        opt.subsample_n = subsample_n
+    opt.timing = 1
+    cloud = SolidCloud(w.mesh, w.solids, opt)
+    if method == "learned":
+        params, tt, tg, _ = learned.load_model()
+        cloud.set_fraction_model(params, tt, tg)
+    return cloud
+
+
+def time_steps(torch, cloud, w, U, f, steps, warmup, flush):
+    """warmup + steps interacts; device time per step (CUDA events around each step, L2 flushed before it)."""
+    for i in range(warmup):
+        cloud.interact(i * w.dt, w.dt, U, f, want_ft=False)
+    torch.cuda.synchronize()
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    cells, bbox, kt, launches, st = [], [], {}, 0, {}
+    for i in range(steps):
+        flush.fill_(float(i))
+        ev0[i].record()
+        cloud.interact((warmup + i) * w.dt, w.dt, U, f, want_ft=False)
+        ev1[i].record()
+        st = cloud.stats()  # synchronises
+        cells.append(st["coupling_cells"])
+        bbox.append(st["bbox_cells"])
+        launches += st["launches"]
+        for k, v in cloud.kernel_times().items():
+            kt.setdefault(k, []).append(v)
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
+    return dict(ms_step=sum(ms) / len(ms), cells=sum(cells) / len(cells), bbox=sum(bbox) / len(bbox),
+                launches=launches, kernel_ms={k: sum(v) / len(v) for k, v in kt.items()}, stats=st)
+
+
+def accuracy(torch, w, cloud, U):
+    """Learned As and per-solid force against SUBSAMPLE(16^3) on the same step."""
+    import numpy as np
+    ref = make_cloud(w, "subsample", subsample_n=16)
+    fr, fl = ref.new_fields(), cloud.new_fields()
+    FTr = ref.interact(0.0, w.dt, U, fr)
+    FTl = cloud.interact(0.0, w.dt, U, fl)
+    ref.close()
+    touched = fr["Ct"] != 0
+    cut = touched & ~((fr["As"] == 1.0) & (fl["As"] == 1.0))
+    err = (fl["As"] - fr["As"]).abs()[cut].double()
+    q = torch.quantile(err[: 1 << 24], torch.tensor([0.5, 0.99, 0.999], dtype=torch.float64, device=err.device))
+    # force error per solid, normwise against rho_f / dt * volume * (|U| rms + |v| + |omega| r): the magnitude of the
+    # sum of the cell contributions
+    u_rms = float(U.square().mean().sqrt())
+    rel = []
+    for s, d in enumerate(w.solids):
+        v = np.linalg.norm(np.array(d.vel[:])) + np.linalg.norm(np.array(d.omega[:])) * d.shape.radiusB
+        scale = w.opt.rho_f / w.dt * d.shape.volume * (u_rms + v)
+        rel.append(np.linalg.norm(FTl[s, :3] - FTr[s, :3]) / scale)
+    rel = np.array(rel)
+    return {"reference": "SUBSAMPLE 16^3 (4096 samples), same step", "cut_cells": int(cut.sum()),
+            "as_abs_err_mean": float(err.mean()), "as_abs_err_p50": float(q[0]), "as_abs_err_p99": float(q[1]),
+            "as_abs_err_p999": float(q[2]), "as_abs_err_max": float(err.max()),
+            "force_rel_err_median": float(np.median(rel)), "force_rel_err_p90": float(np.percentile(rel, 90)),
+            "force_rel_err_max": float(rel.max())}
 
 
 def cpu_baseline(w, max_solids, max_seconds=25.0):
@@ -164,12 +243,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="poly3d_512")
     ap.add_argument("--scale", type=float, default=1.0)
-    ap.add_argument("--method", default="refgeo", choices=sorted(METHODS))
+    ap.add_argument("--method", default="learned", choices=sorted(METHODS))
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain SUBSAMPLE timing and the accuracy step")
     ap.add_argument("--cpu-solids", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--fp32-forcing", action="store_true",
-                    help="FP32 direct forcing with FP64 force/torque sums (the fast paths' precision)")
+    ap.add_argument("--exact-forcing", action="store_true",
+                    help="the reference's FP64 forcing sequence per cell (default: FP64 for the rigid-body "
+                         "velocity and U - us, FP32 after it, FP64 force/torque sums)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -189,9 +270,8 @@ def main():
     from sdfibm_gb300.cloud import SolidCloud
 
     w = make_workload(args)
-    w.opt.timing = 1
     U = w.U_torch()
-    cloud = SolidCloud(w.mesh, w.solids, w.opt)
+    cloud = make_cloud(w, args.method)
     f = cloud.new_fields()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
 
@@ -206,30 +286,34 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    cells, kt, bbox, launches = [], {}, [], 0
-    for i in range(args.steps):
-        flush.fill_(float(i))
-        ev0[i].record()
-        step((args.warmup + i) * w.dt)
-        ev1[i].record()
-        st = cloud.stats()  # synchronises
-        cells.append(st["coupling_cells"])
-        bbox.append(st["bbox_cells"])
-        launches += st["launches"]
-        for k, v in cloud.kernel_times().items():
-            kt.setdefault(k, []).append(v)
-    torch.cuda.synchronize()
+    tm = time_steps(torch, cloud, w, U, f, args.steps, 0, flush)
     clk = clocks.stop()
-    ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
-    ms_step = sum(ms) / len(ms)
+    ms_step = tm["ms_step"]
     if dist:
         tt = torch.tensor([ms_step], device="cuda")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         ms_step = float(tt.item())
-    mean_cells = sum(cells) / len(cells)
+    mean_cells = tm["cells"]
     value = mean_cells * world / (ms_step * 1e-3)
+    launches = tm["launches"]
+    bbox = [tm["bbox"]]
+    kt = {k: [v] for k, v in tm["kernel_ms"].items()}
+
+    compare = None
+    if args.method == "learned" and not args.no_compare:
+        plain = make_cloud(w, "subsample", subsample_n=10)
+        fp = plain.new_fields()
+        tp = time_steps(torch, plain, w, U, fp, args.steps, args.warmup, flush)
+        plain.close()
+        del fp
+        acc = accuracy(torch, w, cloud, U)
+        st = tm["stats"]
+        compare = {"plain": {"method": "SUBSAMPLE 10^3 samples per cut cell", "ms_per_step": tp["ms_step"],
+                             "value": tp["cells"] * world / (tp["ms_step"] * 1e-3),
+                             "kernel_ms": {k: round(v, 4) for k, v in tp["kernel_ms"].items()}},
+                   "speedup_vs_plain": tp["ms_step"] / tm["ms_step"],
+                   "learned_cells": st.get("learned_cells"), "fallback_cells": st.get("learned_fallback_cells"),
+                   "accuracy": acc}
 
     # full time step (interact + evolve + fixInternal), device time
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -294,13 +378,13 @@ def main():
                 "data": "synthetic",
                 "config": {"workload": "%s: %dx%dx%d mesh, %d solids, %s solid fraction, %s forcing, HBM-resident fields"
                                        % (w.name, w.mesh.nx, w.mesh.ny, w.mesh.nz, len(w.solids), args.method,
-                                          "FP32" if args.fp32_forcing else "FP64"),
+                                          "FP64" if args.exact_forcing else "mixed FP64/FP32"),
                            "n_cells": w.ncells, "n_solids": len(w.solids), "coupling_cells": mean_cells,
                            "bbox_cells": sum(bbox) / len(bbox), "fraction_method": args.method,
                            "l2": "flushed (256 MB write) before every timed step", "full_step_ms": full_ms,
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-                "gpu_launches": launches}
+                "gpu_launches": launches, "learned_vs_plain": compare}
         print(json.dumps(line))
     cloud.close()
     if dist:

@@ -148,7 +148,9 @@ typedef struct sdfibm_options {
                                 0: FP32 forcing with FP64 force/torque sums */
     int32_t tile_cells;      /* 0: autotuned.  Cells per (solid, cell-tile) work item otherwise */
     int32_t timing;          /* 1: record CUDA events around every kernel (sdfibm_cuda_kernel_times) */
-    int32_t reserved[6];
+    int32_t learned_fallback_n; /* LEARNED: samples per axis of the SUBSAMPLE evaluation of the cells outside the
+                                   network's confidence band (0: 16, the lattice the network was trained on) */
+    int32_t reserved[5];
 } sdfibm_options;
 
 typedef struct sdfibm_ctx sdfibm_ctx;
@@ -207,8 +209,17 @@ int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc* mesh, const sdfibm_solid
                                 int32_t* cells, int8_t* types, int64_t capacity, int64_t* n_device);
 
 /* Counters of the last interact (host): [0] coupling cells (sum over solids of |T_s|), [1] cut cells,
- * [2] bbox cells scanned, [3] vertices re-checked in FP64, [4] work items, [5] kernel launches. */
+ * [2] bbox cells scanned, [3] vertices re-checked in FP64, [4] work items, [5] kernel launches,
+ * [6] cut cells given to the learned fraction model, [7] of those, cells outside its band (SUBSAMPLE fallback). */
 int sdfibm_cuda_stats(sdfibm_ctx* ctx, int64_t* out, int32_t n);
+
+/* No counterpart in the reference (which has only the apex/pyramid fraction).  Installs the learned cut-cell
+ * fraction model used when options.fraction_method is SDFIBM_FRACTION_LEARNED: params is a HOST array of
+ * SDFIBM_MLP_NPARAM floats in the layout of include/sdfibm_mlp.h; cells whose features fall outside the band
+ * (face twist sum > tau_twist or | |trilinear gradient| - 1 | > tau_grad) are evaluated by SUBSAMPLE with
+ * options.learned_fallback_n samples per axis (a negative limit closes the band: every cut cell falls back).
+ * Reserves the per-cell feature buffers on first use. */
+int sdfibm_cuda_set_fraction_model(sdfibm_ctx* ctx, const float* params, float tau_twist, float tau_grad);
 
 /* Per-kernel device time (milliseconds, CUDA events on the context's stream) of the last interact when
  * options.timing is set: names[i] receives a static kernel name, ms[i] its time; returns the count through *n. */

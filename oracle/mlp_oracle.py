@@ -1,0 +1,200 @@
+"""CPU oracle of the learned cut-cell fraction model: TEST INFRASTRUCTURE ONLY.
+
+Only tests, the smoke check and the bench's CPU legs import this module, as the checker of the GPU kernels in
+sdfibm_gb300/csrc/mlp.cu.  It has no counterpart in the reference, which computes As only with the apex/pyramid
+geometry (geometrictools.cpp:47-116).  It restates the model so that the GPU forward pass, backward pass and
+trainer can be compared term by term:
+
+* features of a cut cell (11): the signed distance at its 8 vertices divided by the cell size, in the vertex
+  order of OpenFOAM's cellPoints for a hex, (i,j,k) (i+1,j,k) (i,j+1,k) (i+1,j+1,k), then the same at k+1; then
+  the trilinear gradient of those 8 values at the cell centre, normalised to unit length;
+* network 11 -> 64 -> 64 -> 1 with SiLU hidden activations and a sigmoid output;
+* numerics of the GPU kernels: the two hidden layers are BF16 x BF16 tensor-core products with FP32
+  accumulation, W1 and W2 are rounded to BF16, and the features and the first hidden activations are carried
+  as a hi + lo pair of BF16 values (so they keep ~16 significant bits); biases, the 64 -> 1 output layer and
+  the sigmoid are FP32;
+* the loss is the mean squared error of the predicted fraction; the backward pass rounds the operands of its
+  tensor-core products (dZ2, dZ1, H1, X) to BF16 and sums the bias gradients and the output layer in FP32.
+
+The pure-Python parts are vectorised numpy; sizes used by the tests are a few thousand cells.
+"""
+import numpy as np
+
+N_IN = 11
+N_H = 64
+N_PARAM = N_H * N_IN + N_H + N_H * N_H + N_H + N_H + 1  # 4993
+
+# flat parameter layout, shared with include/sdfibm_mlp.h
+OFF_W1 = 0                        # W1[64][11], row = hidden unit
+OFF_B1 = OFF_W1 + N_H * N_IN      # b1[64]
+OFF_W2 = OFF_B1 + N_H             # W2[64][64], row = output unit
+OFF_B2 = OFF_W2 + N_H * N_H       # b2[64]
+OFF_W3 = OFF_B2 + N_H             # w3[64]
+OFF_B3 = OFF_W3 + N_H             # b3
+
+
+def unpack(p):
+    p = np.asarray(p, dtype=np.float32)
+    assert p.shape == (N_PARAM,)
+    W1 = p[OFF_W1:OFF_B1].reshape(N_H, N_IN)
+    b1 = p[OFF_B1:OFF_W2]
+    W2 = p[OFF_W2:OFF_B2].reshape(N_H, N_H)
+    b2 = p[OFF_B2:OFF_W3]
+    w3 = p[OFF_W3:OFF_B3]
+    b3 = p[OFF_B3]
+    return W1, b1, W2, b2, w3, b3
+
+
+def pack(W1, b1, W2, b2, w3, b3):
+    return np.concatenate([np.ravel(W1), b1, np.ravel(W2), b2, w3, [b3]]).astype(np.float32)
+
+
+def init_params(seed=0):
+    """He-style initialisation used by the trainer (uniform, fan-in scaled)."""
+    rng = np.random.default_rng(seed)
+    W1 = rng.uniform(-1, 1, (N_H, N_IN)) * np.sqrt(3.0 / N_IN)
+    W2 = rng.uniform(-1, 1, (N_H, N_H)) * np.sqrt(3.0 / N_H)
+    w3 = rng.uniform(-1, 1, N_H) * np.sqrt(3.0 / N_H)
+    return pack(W1, np.zeros(N_H), W2, np.zeros(N_H), w3, 0.0)
+
+
+def bf16(x):
+    """Round float32 values to bfloat16 (nearest, ties to even); returned as float32."""
+    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def split(x):
+    hi = bf16(x)
+    lo = bf16(np.asarray(x, np.float32) - hi)
+    return hi, lo
+
+
+def sigmoid(z):
+    with np.errstate(over="ignore"):
+        return 1.0 / (1.0 + np.exp(-z))
+
+
+def silu(z):
+    return z * sigmoid(z)
+
+
+def dsilu(z):
+    s = sigmoid(z)
+    return s * (1.0 + z * (1.0 - s))
+
+
+def features(phi, inv_h):
+    """phi: [n, 8] float32 vertex signed distances; inv_h: float32 1/h.  Returns [n, 11] float32.
+
+    Same FP32 operation order as the device function cell_features in mlp.cu."""
+    f = (np.asarray(phi, np.float32) * np.float32(inv_h)).astype(np.float32)
+    q = np.float32(0.25)
+    gx = q * (((f[:, 1] - f[:, 0]) + (f[:, 3] - f[:, 2])) + ((f[:, 5] - f[:, 4]) + (f[:, 7] - f[:, 6])))
+    gy = q * (((f[:, 2] - f[:, 0]) + (f[:, 3] - f[:, 1])) + ((f[:, 6] - f[:, 4]) + (f[:, 7] - f[:, 5])))
+    gz = q * (((f[:, 4] - f[:, 0]) + (f[:, 5] - f[:, 1])) + ((f[:, 6] - f[:, 2]) + (f[:, 7] - f[:, 3])))
+    gn = np.sqrt(gx * gx + gy * gy + gz * gz).astype(np.float32)
+    ok = gn > np.float32(1e-12)
+    den = np.where(ok, gn, np.float32(1.0)).astype(np.float32)
+    g = np.stack([np.where(ok, gx / den, 0), np.where(ok, gy / den, 0), np.where(ok, gz / den, 0)], 1)
+    return np.concatenate([f, g.astype(np.float32)], 1).astype(np.float32)
+
+
+def band_scores(feat):
+    """Confidence-band scores of a cell from its features: (twist, |grad| - 1).
+
+    twist = sum over the 6 faces of |f_a - f_b - f_c + f_d| (zero for a linear field); the gradient magnitude of
+    the trilinear interpolant is 1 for a true distance field away from edges and the medial axis."""
+    f = np.asarray(feat, np.float32)[:, :8]
+    tw = (np.abs(f[:, 0] - f[:, 1] - f[:, 2] + f[:, 3]) + np.abs(f[:, 4] - f[:, 5] - f[:, 6] + f[:, 7]) +
+          np.abs(f[:, 0] - f[:, 1] - f[:, 4] + f[:, 5]) + np.abs(f[:, 2] - f[:, 3] - f[:, 6] + f[:, 7]) +
+          np.abs(f[:, 0] - f[:, 2] - f[:, 4] + f[:, 6]) + np.abs(f[:, 1] - f[:, 3] - f[:, 5] + f[:, 7]))
+    q = 0.25
+    gx = q * (((f[:, 1] - f[:, 0]) + (f[:, 3] - f[:, 2])) + ((f[:, 5] - f[:, 4]) + (f[:, 7] - f[:, 6])))
+    gy = q * (((f[:, 2] - f[:, 0]) + (f[:, 3] - f[:, 1])) + ((f[:, 6] - f[:, 4]) + (f[:, 7] - f[:, 5])))
+    gz = q * (((f[:, 4] - f[:, 0]) + (f[:, 5] - f[:, 1])) + ((f[:, 6] - f[:, 2]) + (f[:, 7] - f[:, 3])))
+    return tw, np.abs(np.sqrt(gx * gx + gy * gy + gz * gz) - 1.0)
+
+
+def forward(p, X, return_all=False, exact=False):
+    """Predicted fraction of each cell.  X: [n, 11] float32.  FP64 accumulation of the FP32-exact products.
+
+    exact=True drops every rounding (FP64 throughout): the plain function, used to check the backward algebra."""
+    W1, b1, W2, b2, w3, b3 = unpack(p) if not exact else [np.asarray(t, np.float64) for t in unpack_f64(p)]
+    if exact:
+        z1 = np.asarray(X, np.float64) @ W1.T + b1
+        h1 = silu(z1)
+        z2 = h1 @ W2.T + b2
+        h2 = silu(z2)
+        o = h2 @ w3 + b3
+        a = sigmoid(o)
+        if return_all:
+            return dict(z1=z1, h1=h1, z2=z2, h2=h2, o=o, a=a)
+        return a
+    W1b = bf16(W1).astype(np.float64)
+    W2b = bf16(W2).astype(np.float64)
+    xh, xl = split(X)
+    z1 = (xh.astype(np.float64) + xl.astype(np.float64)) @ W1b.T + b1
+    h1 = silu(z1.astype(np.float32)).astype(np.float32)
+    hh, hl = split(h1)
+    z2 = (hh.astype(np.float64) + hl.astype(np.float64)) @ W2b.T + b2
+    z2 = z2.astype(np.float32)
+    h2 = silu(z2).astype(np.float32)
+    o = h2.astype(np.float64) @ w3.astype(np.float64) + b3
+    a = sigmoid(o)
+    if return_all:
+        return dict(z1=z1.astype(np.float32), h1=h1, z2=z2, h2=h2, o=o, a=a)
+    return a
+
+
+def unpack_f64(p):
+    p = np.asarray(p, dtype=np.float64)
+    return (p[OFF_W1:OFF_B1].reshape(N_H, N_IN), p[OFF_B1:OFF_W2], p[OFF_W2:OFF_B2].reshape(N_H, N_H),
+            p[OFF_B2:OFF_W3], p[OFF_W3:OFF_B3], p[OFF_B3])
+
+
+def loss_grad(p, X, y, exact=False):
+    """Loss = mean((a - y)^2) and its gradient; returns (loss, grad[N_PARAM]).
+
+    exact=True: the FP64 gradient of the unrounded function (checked against finite differences)."""
+    if exact:
+        W1, b1, W2, b2, w3, b3 = unpack_f64(p)
+        n = X.shape[0]
+        r = forward(p, X, return_all=True, exact=True)
+        a = r["a"]
+        d = a - y
+        dz3 = (2.0 / n) * d * a * (1.0 - a)
+        dZ2 = dz3[:, None] * w3[None, :] * dsilu(r["z2"])
+        dZ1 = (dZ2 @ W2) * dsilu(r["z1"])
+        g = np.concatenate([(dZ1.T @ np.asarray(X, np.float64)).ravel(), dZ1.sum(0), (dZ2.T @ r["h1"]).ravel(),
+                            dZ2.sum(0), r["h2"].T @ dz3, [dz3.sum()]])
+        return float(np.mean(d * d)), g
+    W1, b1, W2, b2, w3, b3 = unpack(p)
+    n = X.shape[0]
+    r = forward(p, X, return_all=True)
+    a = r["a"]
+    d = a - y
+    loss = float(np.mean(d * d))
+    dz3 = (2.0 / n) * d * a * (1.0 - a)                                   # [n]
+    dw3 = r["h2"].astype(np.float64).T @ dz3
+    db3 = dz3.sum()
+    dZ2 = (dz3[:, None] * w3[None, :].astype(np.float64) * dsilu(r["z2"].astype(np.float64))).astype(np.float32)
+    db2 = dZ2.astype(np.float64).sum(0)
+    dZ2b = bf16(dZ2).astype(np.float64)
+    dW2 = dZ2b.T @ bf16(r["h1"]).astype(np.float64)
+    dH1 = dZ2b @ bf16(W2).astype(np.float64)
+    dZ1 = (dH1 * dsilu(r["z1"].astype(np.float64))).astype(np.float32)
+    db1 = dZ1.astype(np.float64).sum(0)
+    dW1 = bf16(dZ1).astype(np.float64).T @ bf16(X).astype(np.float64)
+    g = np.concatenate([dW1.ravel(), db1, dW2.ravel(), db2, dw3, [db3]])
+    return loss, g
+
+
+def adam_step(p, g, m, v, t, lr, b1=0.9, b2=0.999, eps=1e-8):
+    """One Adam update (t counts from 1), FP32 state as in the device kernel."""
+    m = (b1 * m + (1 - b1) * g).astype(np.float32)
+    v = (b2 * v + (1 - b2) * g * g).astype(np.float32)
+    mh = m / (1 - b1 ** t)
+    vh = v / (1 - b2 ** t)
+    return (p - lr * mh / (np.sqrt(vh) + eps)).astype(np.float32), m, v

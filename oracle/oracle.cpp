@@ -884,4 +884,27 @@ double oracle_phi(const sdfibm_solid_desc* s, const double* p) {
     return shapeSDF(s->shape, world2local(arr3(p), arr3(s->pos), Quat{s->quat[0], arr3(s->quat + 1)}));
 }
 
+// One labelled training cell of the learned fraction (sdfibm_mlp_dataset): the shape at the origin with rotation q4,
+// the cell [o, o + h]^3; writes the filtered signed distance at the 8 vertices (cellPoints order) and returns the
+// number of n^3 midpoint-lattice samples inside.
+int64_t oracle_sample_cell(const sdfibm_shape_desc* s, const double* q4, const double* o, double h, int n,
+                           double* phi8) {
+    const Quat q{q4[0], V3{q4[1], q4[2], q4[3]}};
+    const V3 zero{0.0, 0.0, 0.0};
+    for (int v = 0; v < 8; ++v) {
+        const V3 p{o[0] + (double)(v & 1) * h, o[1] + (double)((v >> 1) & 1) * h, o[2] + (double)((v >> 2) & 1) * h};
+        phi8[v] = shapeSDF(*s, world2local(p, zero, q));
+    }
+    int64_t cnt = 0;
+    for (int c = 0; c < n; ++c)
+        for (int b = 0; b < n; ++b)
+            for (int a = 0; a < n; ++a) {
+                const double ta = (double)(2 * a + 1) / (double)(2 * n), tb = (double)(2 * b + 1) / (double)(2 * n),
+                             tc = (double)(2 * c + 1) / (double)(2 * n);
+                const V3 p{o[0] + ta * h, o[1] + tb * h, o[2] + tc * h};
+                cnt += shapeInside(*s, world2local(p, zero, q)) ? 1 : 0;
+            }
+    return cnt;
+}
+
 }  // extern "C"

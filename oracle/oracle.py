@@ -60,6 +60,8 @@ def lib():
         L.oracle_phi01.argtypes = [C.POINTER(abi.SolidDesc), vp]
         L.oracle_phi.restype = C.c_double
         L.oracle_phi.argtypes = [C.POINTER(abi.SolidDesc), vp]
+        L.oracle_sample_cell.restype = C.c_int64
+        L.oracle_sample_cell.argtypes = [C.POINTER(abi.ShapeDesc), vp, vp, C.c_double, C.c_int, vp]
         _lib = L
     return _lib
 
@@ -76,6 +78,21 @@ def make_shape(type_id, raw, com=(0.0, 0.0, 0.0)):
     if lib().oracle_make_shape(type_id, _p(r), _p(c), C.byref(s)) != 0:
         raise ValueError("bad shape")
     return s
+
+
+def sample_cell(recipe, n_sub):
+    """Recomputes one generated training cell from its FP64 recipe (the 20-value record of sdfibm_mlp_dataset):
+    returns (phi at the 8 vertices, inside count of the n_sub^3 lattice)."""
+    r = np.asarray(recipe, dtype=np.float64)
+    s = abi.ShapeDesc()
+    s.type = int(r[0])
+    for k in range(8):
+        s.p[k] = r[1 + k]
+    q = np.ascontiguousarray(r[9:13])
+    o = np.ascontiguousarray(r[13:16])
+    phi = np.zeros(8)
+    cnt = lib().oracle_sample_cell(C.byref(s), _p(q), _p(o), float(r[16]), int(n_sub), _p(phi))
+    return phi, int(cnt)
 
 
 def quat_from_euler_deg(euler_deg):

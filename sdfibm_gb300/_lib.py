@@ -17,7 +17,10 @@ CUDA_SYMBOLS = [
     "sdfibm_cuda_evolve", "sdfibm_cuda_fix_internal", "sdfibm_cuda_get_solids", "sdfibm_cuda_set_solids",
     "sdfibm_cuda_touched", "sdfibm_cuda_stats", "sdfibm_cuda_kernel_times", "sdfibm_cuda_last_error",
     "sdfibm_cuda_version",
-    "sdfibm_cuda_destroy", "sdfibm_cuda_touched_noalloc",
+    "sdfibm_cuda_destroy", "sdfibm_cuda_touched_noalloc", "sdfibm_cuda_set_fraction_model",
+]
+MLP_SYMBOLS = [
+    "sdfibm_mlp_dataset", "sdfibm_mlp_forward", "sdfibm_mlp_loss_grad", "sdfibm_mlp_adam", "sdfibm_mlp_train",
 ]
 HOST_SYMBOLS = [
     "sdfibm_host_make_shape", "sdfibm_host_make_motion", "sdfibm_host_make_forcer", "sdfibm_host_quat_from_euler_deg",
@@ -49,6 +52,7 @@ def load():
     L.sdfibm_cuda_set_solids.argtypes = [vp, P(abi.SolidState), i32]
     L.sdfibm_cuda_touched.argtypes = [vp, i32, vp, vp, i64, P(i64)]
     L.sdfibm_cuda_stats.argtypes = [vp, P(i64), i32]
+    L.sdfibm_cuda_set_fraction_model.argtypes = [vp, vp, C.c_float, C.c_float]
     L.sdfibm_cuda_kernel_times.argtypes = [vp, P(C.c_char_p), P(dbl), i32, P(i32)]
     L.sdfibm_cuda_touched_noalloc.argtypes = [P(abi.MeshDesc), P(abi.SolidDesc), vp, vp, vp, i64, vp]
     L.sdfibm_cuda_last_error.argtypes = [vp]
@@ -56,6 +60,11 @@ def load():
     L.sdfibm_cuda_version.restype = C.c_char_p
     L.sdfibm_cuda_destroy.argtypes = [vp]
     L.sdfibm_cuda_destroy.restype = None
+    L.sdfibm_mlp_dataset.argtypes = [C.c_uint64, i64, P(abi.MlpDataDesc), vp, vp, vp, vp]
+    L.sdfibm_mlp_forward.argtypes = [vp, vp, i64, i64, vp, vp]
+    L.sdfibm_mlp_loss_grad.argtypes = [vp, vp, vp, i64, i64, vp, vp]
+    L.sdfibm_mlp_adam.argtypes = [vp, vp, vp, vp, i32, C.c_float, vp]
+    L.sdfibm_mlp_train.argtypes = [vp, vp, vp, i64, P(abi.MlpTrainDesc), vp, vp]
     L.sdfibm_abi_sizeof.argtypes = [C.c_int]
     L.sdfibm_abi_sizeof.restype = i64
     L.sdfibm_host_make_shape.argtypes = [i32, vp, vp, P(abi.ShapeDesc)]

@@ -58,7 +58,23 @@ class Options(C.Structure):
     _fields_ = [("rho_f", C.c_double), ("gravity", C.c_double * 3), ("collision_mode", C.c_int32),
                 ("n_subiter", C.c_int32), ("fraction_method", C.c_int32), ("subsample_n", C.c_int32),
                 ("dense_reset", C.c_int32), ("exact_forcing", C.c_int32), ("tile_cells", C.c_int32),
-                ("timing", C.c_int32), ("reserved", C.c_int32 * 6)]
+                ("timing", C.c_int32), ("learned_fallback_n", C.c_int32), ("reserved", C.c_int32 * 5)]
+
+
+class MlpDataDesc(C.Structure):
+    """sdfibm_mlp_data_desc (include/sdfibm_mlp.h)."""
+    _fields_ = [("hr_min", C.c_double), ("hr_max", C.c_double), ("families", C.c_int32), ("n_sub", C.c_int32),
+                ("z_axis_frac", C.c_double)]
+
+
+class MlpTrainDesc(C.Structure):
+    """sdfibm_mlp_train_desc (include/sdfibm_mlp.h)."""
+    _fields_ = [("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float), ("lr_final_frac", C.c_float),
+                ("warmup_steps", C.c_int32), ("reserved", C.c_int32)]
+
+
+MLP_NPARAM = 4993
+MLP_SPHERE, MLP_ELLIPSOID, MLP_BOX, MLP_PLANE, MLP_CYLINDER, MLP_ELLIPTIC_CYL = 1, 2, 4, 8, 16, 32
 
 
 def mesh_desc(n, origin, h, twod=0):

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libsdfibm_cuda.so")
 BUILD_DIR = os.path.join(HERE, "_build")
-CU_SOURCES = ["classify.cu", "coupling.cu", "evolve.cu", "capi.cu", "noalloc.cu"]
+CU_SOURCES = ["classify.cu", "coupling.cu", "evolve.cu", "capi.cu", "noalloc.cu", "mlp.cu"]
 CXX_SOURCES = ["host.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -120,7 +120,16 @@ class SolidCloud:
         return out
 
     def stats(self):
-        out = (C.c_int64 * 6)()
-        self._check(self._L.sdfibm_cuda_stats(self._h, out, 6))
-        keys = ("coupling_cells", "cut_cells", "bbox_cells", "fp64_rechecks", "work_items", "launches")
+        out = (C.c_int64 * 8)()
+        self._check(self._L.sdfibm_cuda_stats(self._h, out, 8))
+        keys = ("coupling_cells", "cut_cells", "bbox_cells", "fp64_rechecks", "work_items", "launches",
+                "learned_cells", "learned_fallback_cells")
         return dict(zip(keys, list(out)))
+
+    def set_fraction_model(self, params, tau_twist, tau_grad):
+        """Installs the learned cut-cell fraction model (options.fraction_method = FRACTION_LEARNED)."""
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.shape != (abi.MLP_NPARAM,):
+            raise ValueError("fraction model needs %d parameters" % abi.MLP_NPARAM)
+        self._check(self._L.sdfibm_cuda_set_fraction_model(self._h, p.ctypes.data_as(C.c_void_p),
+                                                           C.c_float(tau_twist), C.c_float(tau_grad)))

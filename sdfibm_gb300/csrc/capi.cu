@@ -10,6 +10,8 @@
 
 #include "../../include/sdfibm_cuda.h"
 #include "kernels.cuh"
+#include "mlp.cuh"
+#include "../../include/sdfibm_mlp.h"
 
 namespace sdfibm_dev {
 // coupling.cu
@@ -17,6 +19,7 @@ __global__ void plan_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state*
                             Counters* cnt);
 __global__ void classify_kernel_3d(ClassifyArgs A);
 __global__ void classify_kernel_2d(ClassifyArgs A);
+__global__ void learned_fallback_kernel(FallbackArgs A);
 __global__ void connect_kernel(MeshK m, const SolidK* sk, SolidPlan* plan, const uint8_t* scratch, uint32_t* gbitmaps,
                                int32_t* in_cell, int32_t* in_solid, int32_t* cut_cell, int32_t* cut_solid,
                                int64_t cap_in, int64_t cap_cut, Counters* cnt, int smem_words);
@@ -27,7 +30,7 @@ __global__ void finalize_kernel(float* As, float* Ts, float* Fs, int32_t* Ct, co
 __global__ void begin_kernel(Counters* cnt);
 __global__ void claim_kernel(const int32_t* in_cell, const int32_t* in_solid, const int32_t* cut_cell,
                              const int32_t* cut_solid, int32_t* Ct, const Counters* cnt, int64_t N);
-__global__ void ft_kernel(const double* ftacc, double* ft, int S, double rho_f);
+__global__ void ft_kernel(const double* ftacc, double* ft, int S, double scale);
 __global__ void reset_kernel(const int32_t* in_cell, const int32_t* cut_cell, const Counters* cnt, int64_t N,
                              float* As, float* Fs, float* Ts, int32_t* Ct);
 __global__ void fix_internal_kernel(MeshK m, const sdfibm_solid_state* st, const int32_t* in_cell,
@@ -116,6 +119,15 @@ struct sdfibm_ctx {
     static constexpr int MAXEV = 24;
     cudaEvent_t ev[MAXEV + 1] = {};
     const char* ev_name[MAXEV] = {};
+    // learned fraction (SDFIBM_FRACTION_LEARNED): model and per-cut-cell feature buffers
+    float* d_mlp = nullptr;
+    float tau_twist = 0.f, tau_grad = 0.f;
+    bool model_set = false;
+    float* d_feat = nullptr;  // [11][feat_cap]
+    int64_t feat_cap = 0;
+    int32_t* d_fref_solid = nullptr;
+    int64_t* d_fref_index = nullptr;
+    int32_t* d_fb = nullptr;
     int nev = 0;
     bool ev_ready = false;
     int launches_last = 0;
@@ -221,6 +233,7 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
     for (int a = 0; a < 3; ++a) { m.o[a] = mesh->origin[a]; m.h[a] = mesh->h[a]; m.h32[a] = (float)mesh->h[a]; }
     m.ncells = N;
     m.V = mesh->h[0] * mesh->h[1] * mesh->h[2];
+    mesh_fastdiv(m);
     const int32_t n3[3] = {mesh->nx, mesh->ny, mesh->nz};
 
     // static per-solid records
@@ -402,6 +415,7 @@ static int check_device_error(sdfibm_ctx* ctx) {
         case DERR_BBOX: return fail(ctx, SDFIBM_ERR_CAPACITY, "a 2-D shape tilted out of its reserved bounding box");
         case DERR_FLOOD_LIMIT: return fail(ctx, SDFIBM_ERR_TIMEOUT, "flood fill did not converge within its bound");
         case DERR_SHARED_TABLE: return fail(ctx, SDFIBM_ERR_CAPACITY, "shared-cell table full");
+        case DERR_MMA_TIMEOUT: return fail(ctx, SDFIBM_ERR_TIMEOUT, "learned fraction: tensor-core wait timed out");
         default: return fail(ctx, SDFIBM_ERR_CUDA, "device error " + std::to_string(e));
     }
 }
@@ -427,6 +441,8 @@ int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U
     bool same = ctx->interacted;
     for (int i = 1; i < 5; ++i) same = same && f5[i] == ctx->last_fields[i];
     const bool dense = !same || ctx->opt.dense_reset;
+    if (ctx->opt.fraction_method == SDFIBM_FRACTION_LEARNED && !ctx->model_set)
+        return fail(ctx, SDFIBM_ERR_STATE, "LEARNED fraction without a model: call sdfibm_cuda_set_fraction_model");
     for (int i = 0; i < 5; ++i) ctx->last_fields[i] = f5[i];
     ctx->cur ^= 1;  // this call's lists; the other buffer holds the previous call's touched cells
     begin_kernel<<<1, 1, 0, st>>>(ctx->d_cnt);
@@ -447,9 +463,32 @@ int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U
         CA.m = ctx->mesh; CA.sk = ctx->d_sk; CA.st = ctx->d_st; CA.plan = ctx->d_plan; CA.chunks = ctx->d_chunks;
         CA.total_chunks = ctx->total_chunks; CA.cls = ctx->d_scratch; CA.alpha = ctx->d_alpha; CA.cnt = ctx->d_cnt;
         CA.method = ctx->opt.fraction_method; CA.subsample_n = ctx->opt.subsample_n;
+        const bool learned = ctx->opt.fraction_method == SDFIBM_FRACTION_LEARNED;
+        if (learned) {
+            CA.feat = ctx->d_feat; CA.feat_cap = ctx->feat_cap; CA.fref_solid = ctx->d_fref_solid;
+            CA.fref_index = ctx->d_fref_index; CA.inv_h = (float)(1.0 / ctx->mdesc.h[0]);
+        }
         if (ctx->mesh.nz <= 2) classify_kernel_2d<<<ctx->classify_grid, 256, 0, st>>>(CA);
         else classify_kernel_3d<<<ctx->classify_grid, 256, 0, st>>>(CA);
         mark(ctx, "classify_kernel");
+        if (learned) {
+            // network on every cut cell, SUBSAMPLE on the cells outside its band
+            MlpInferArgs ia{};
+            ia.params = ctx->d_mlp; ia.feat = ctx->d_feat; ia.stride = ctx->feat_cap; ia.n_dev = &ctx->d_cnt->n_feat;
+            ia.ref_solid = ctx->d_fref_solid; ia.ref_index = ctx->d_fref_index; ia.alpha = ctx->d_alpha;
+            ia.fb_list = ctx->d_fb; ia.fb_count = &ctx->d_cnt->n_fb; ia.tau_twist = ctx->tau_twist;
+            ia.tau_grad = ctx->tau_grad; ia.error = &ctx->d_cnt->error;
+            launch_mlp_infer(ia, 4 * ctx->num_sms, st);
+            mark(ctx, "mlp_infer_kernel");
+            FallbackArgs fa;
+            fa.m = ctx->mesh; fa.sk = ctx->d_sk; fa.st = ctx->d_st; fa.plan = ctx->d_plan; fa.fb_list = ctx->d_fb;
+            fa.fref_solid = ctx->d_fref_solid; fa.fref_index = ctx->d_fref_index; fa.cap = ctx->feat_cap;
+            fa.alpha = ctx->d_alpha; fa.cnt = ctx->d_cnt;
+            fa.n = ctx->opt.learned_fallback_n > 0 ? ctx->opt.learned_fallback_n : 16;
+            learned_fallback_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(fa);
+            mark(ctx, "learned_fallback_kernel");
+            launches += 2;
+        }
         connect_kernel<<<S, 512, ctx->connect_smem_bytes, st>>>(ctx->mesh, ctx->d_sk, ctx->d_plan, ctx->d_scratch,
                                                                 ctx->d_gbitmaps, ctx->in_cell(), ctx->in_solid(),
                                                                 ctx->cut_cell(), ctx->cut_solid(), ctx->cap, ctx->cap,
@@ -481,7 +520,7 @@ int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U
         finalize_kernel<<<ctx->num_sms, 256, 0, st>>>(As, Ts, Fs, Ct, ctx->d_cnt, N, ctx->d_sh_keys, ctx->d_sh_vals,
                                                        ctx->d_sh_used, ctx->sh_mask);
         mark(ctx, "finalize_kernel");
-        ft_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->d_ftacc, ctx->d_ft, S, ctx->opt.rho_f);
+        ft_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->d_ftacc, ctx->d_ft, S, ctx->opt.rho_f * ctx->mesh.V / dt);
         ft_to_state_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->d_ft, ctx->d_st, S);
         mark(ctx, "ft_kernel");
         launches += 4;
@@ -632,14 +671,37 @@ int sdfibm_cuda_kernel_times(sdfibm_ctx* ctx, const char** names, double* ms, in
     return SDFIBM_OK;
 }
 
+int sdfibm_cuda_set_fraction_model(sdfibm_ctx* ctx, const float* params, float tau_twist, float tau_grad) {
+    if (!ctx) return SDFIBM_ERR_ARG;
+    if (!params) return fail(ctx, SDFIBM_ERR_ARG, "null model parameters");
+    if (std::isnan(tau_twist) || std::isnan(tau_grad)) return fail(ctx, SDFIBM_ERR_ARG, "band limits are NaN");
+    for (int i = 0; i < SDFIBM_MLP_NPARAM; ++i)
+        if (!std::isfinite(params[i])) return fail(ctx, SDFIBM_ERR_ARG, "non-finite model parameter");
+    if (!ctx->d_mlp) {
+        // one feature record per bbox cell: every cut cell of a call fits
+        ctx->feat_cap = std::max<int64_t>(1, ctx->scratch_bytes);
+        if (dalloc(&ctx->d_mlp, SDFIBM_MLP_NPARAM) || dalloc(&ctx->d_feat, (size_t)SDFIBM_MLP_NIN * ctx->feat_cap) ||
+            dalloc(&ctx->d_fref_solid, ctx->feat_cap) || dalloc(&ctx->d_fref_index, ctx->feat_cap) ||
+            dalloc(&ctx->d_fb, ctx->feat_cap))
+            return fail(ctx, SDFIBM_ERR_CUDA, "allocation of the learned-fraction buffers failed");
+    }
+    CK(cudaMemcpyAsync(ctx->d_mlp, params, sizeof(float) * SDFIBM_MLP_NPARAM, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->tau_twist = tau_twist;
+    ctx->tau_grad = tau_grad;
+    ctx->model_set = true;
+    return SDFIBM_OK;
+}
+
 int sdfibm_cuda_stats(sdfibm_ctx* ctx, int64_t* out, int32_t n) {
     if (!ctx || !out) return SDFIBM_ERR_ARG;
     int rc = sync_counters(ctx);
     if (rc) return rc;
     const Counters& c = *ctx->h_cnt;
-    const int64_t v[6] = {(int64_t)c.n_inside + c.n_cut, (int64_t)c.n_cut, (int64_t)c.bbox_cells,
-                          (int64_t)c.exact_rechecks, (int64_t)ctx->total_chunks, (int64_t)ctx->launches_last};
-    for (int i = 0; i < n && i < 6; ++i) out[i] = v[i];
+    const int64_t v[8] = {(int64_t)c.n_inside + c.n_cut, (int64_t)c.n_cut, (int64_t)c.bbox_cells,
+                          (int64_t)c.exact_rechecks, (int64_t)ctx->total_chunks, (int64_t)ctx->launches_last,
+                          (int64_t)c.n_feat, (int64_t)c.n_fb};
+    for (int i = 0; i < n && i < 8; ++i) out[i] = v[i];
     return SDFIBM_OK;
 }
 
@@ -650,7 +712,8 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
                    ctx->d_lists[0][0], ctx->d_lists[0][1], ctx->d_lists[0][2], ctx->d_lists[0][3],
                    ctx->d_lists[1][0], ctx->d_lists[1][1], ctx->d_lists[1][2], ctx->d_lists[1][3], ctx->d_cnt, ctx->d_ftacc,
                    ctx->d_ft, ctx->d_hash, ctx->d_gcount, ctx->d_gstart, ctx->d_gcursor, ctx->d_glist, ctx->d_U,
-                   ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, ctx->d_alpha, ctx->d_sh_keys, ctx->d_sh_vals, ctx->d_sh_used};
+                   ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, ctx->d_alpha, ctx->d_sh_keys, ctx->d_sh_vals, ctx->d_sh_used,
+                   ctx->d_mlp, ctx->d_feat, ctx->d_fref_solid, ctx->d_fref_index, ctx->d_fb};
     for (void* p : dev)
         if (p) cudaFree(p);
     if (ctx->ev_ready)
@@ -668,6 +731,8 @@ int64_t sdfibm_abi_sizeof(int which) {
         case 2: return sizeof(sdfibm_solid_desc);
         case 3: return sizeof(sdfibm_solid_state);
         case 4: return sizeof(sdfibm_options);
+        case 5: return sizeof(sdfibm_mlp_data_desc);
+        case 6: return sizeof(sdfibm_mlp_train_desc);
         default: return -1;
     }
 }

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "mlp.cuh"
 
 namespace sdfibm_dev {
 
@@ -149,49 +150,136 @@ static __device__ __noinline__ float exact_phi_point(const ShapeK& sh, const Mes
 
 // ---- SUBSAMPLE: one warp per cut cell ----------------------------------------------------------------------------------
 // Each lane owns (a,b) columns of the n x n x n midpoint lattice and walks its column in z.  Local coordinates step by
-// three precomputed vectors (the columns of the world->local map times h), and one error bound covers every sample
-// of the cell; undecided samples are re-evaluated with the oracle's FP64 point formula.
-static __device__ __noinline__ float subsample_warp(const MeshK& m, const ShapeK& sh, const float* M, const TileFrame& tf, int a0, int b0,
-                                int c0, const D3& x, const Q4& q, int64_t i, int64_t j, int64_t k, int n,
-                                unsigned long long* rechecks) {
+// three precomputed vectors (the columns of the world->local map times h).  One error bound E covers every sample
+// coordinate of the cell; for the convex shapes the bound of the inside function is also taken once per cell, from
+// the largest coordinate any sample can have, so a sample costs a few FMAs and two compares.  Undecided samples are
+// re-evaluated with the oracle's FP64 point formula.
+
+// sample frame of one cell: corner point p (shape centre offset folded in for the convex shapes), steps s*, bounds
+struct SampleFrame {
+    float px, py, pz;
+    float sxx, sxy, sxz, syx, syy, syz, szx, szy, szz;
+    float E;   // bound of |computed - exact| of every sample coordinate (without the folded offset)
+    float Eg;  // bound of |computed - exact| of the inside function (convex shapes, offset folded)
+    float k0, k1, k2, k3;  // quadric X^2 k0 + Y^2 k1 + Z^2 k2 - k3, or box half extents k0..k2
+};
+
+__device__ __forceinline__ int band(float g, float Eg) { return g < -Eg ? 1 : (g > Eg ? 0 : 2); }
+
+constexpr int SS_QUADRIC = 0, SS_BOX = 1, SS_GENERIC = 2;
+
+template <int T>
+__device__ __forceinline__ int sample_inside(const ShapeK& sh, const SampleFrame& f, float X, float Y, float Z) {
+    if (T == SS_QUADRIC) return band(__fmaf_rn(X * X, f.k0, __fmaf_rn(Y * Y, f.k1, (Z * Z) * f.k2)) - f.k3, f.Eg);
+    if (T == SS_BOX) return band(fmaxf(fmaxf(fabsf(X) - f.k0, fabsf(Y) - f.k1), fabsf(Z) - f.k2), f.Eg);
+    return inside32(sh, X, Y, Z, f.E);  // tails and planes: the general test with its per-sample bound
+}
+
+template <int T>
+__device__ __forceinline__ int subsample_count(const MeshK& m, const ShapeK& sh, const SampleFrame& f, int64_t i,
+                                               int64_t j, int64_t k, int n, const D3& x, const Q4& q,
+                                               unsigned long long* rechecks) {
     const int lane = threadIdx.x & 31;
-    const float hx = m.h32[0], hy = m.h32[1], hz = m.h32[2];
-    const float ox = (float)a0 * hx, oy = (float)b0 * hy, oz = (float)c0 * hz;  // cell corner within the tile
-    const float dx = tf.bx + ox, dy = tf.by + oy, dz = tf.bz + oz;
-    const float px = __fmaf_rn(M[0], dx, __fmaf_rn(M[1], dy, M[2] * dz));
-    const float py = __fmaf_rn(M[3], dx, __fmaf_rn(M[4], dy, M[5] * dz));
-    const float pz = __fmaf_rn(M[6], dx, __fmaf_rn(M[7], dy, M[8] * dz));
-    const float sxx = M[0] * hx, sxy = M[3] * hx, sxz = M[6] * hx;
-    const float syx = M[1] * hy, syy = M[4] * hy, syz = M[7] * hy;
-    const float szx = M[2] * hz, szy = M[5] * hz, szz = M[8] * hz;
-    const float hsum = hx + hy + hz;
-    const float E = 8.f * U32 * (tf.babs + fabsf(ox) + fabsf(oy) + fabsf(oz) + 2.f * (fabsf(dx) + fabsf(dy) + fabsf(dz)) +
-                                 3.f * hsum) +
-                    8.f * U32 * (fabsf(px) + fabsf(py) + fabsf(pz) + fabsf(sxx) + fabsf(sxy) + fabsf(sxz) + fabsf(syx) +
-                                 fabsf(syy) + fabsf(syz) + fabsf(szx) + fabsf(szy) + fabsf(szz)) +
-                    tf.e64 + 1e-30f;
     const int nzs = m.twod ? 1 : n;
     const float inv2n = 1.0f / (float)(2 * n);
     int cnt = 0;
+#pragma unroll 1
     for (int col = lane; col < n * n; col += 32) {
-        const int a = col % n, b = col / n;
-        const float ta = (float)(2 * a + 1) * inv2n, tb = (float)(2 * b + 1) * inv2n;
-        const float bx = __fmaf_rn(tb, syx, __fmaf_rn(ta, sxx, px));
-        const float by = __fmaf_rn(tb, syy, __fmaf_rn(ta, sxy, py));
-        const float bz = __fmaf_rn(tb, syz, __fmaf_rn(ta, sxz, pz));
+        const int ia = col % n, ib = col / n;
+        const float ta = (float)(2 * ia + 1) * inv2n, tb = (float)(2 * ib + 1) * inv2n;
+        const float bx = __fmaf_rn(tb, f.syx, __fmaf_rn(ta, f.sxx, f.px));
+        const float by = __fmaf_rn(tb, f.syy, __fmaf_rn(ta, f.sxy, f.py));
+        const float bz = __fmaf_rn(tb, f.syz, __fmaf_rn(ta, f.sxz, f.pz));
+        float odd = 1.f;  // 2*c3 + 1, exact
+#pragma unroll 2
         for (int c3 = 0; c3 < nzs; ++c3) {
-            const float tc = m.twod ? 0.5f : (float)(2 * c3 + 1) * inv2n;
-            int r = inside32(sh, __fmaf_rn(tc, szx, bx), __fmaf_rn(tc, szy, by), __fmaf_rn(tc, szz, bz), E);
+            const float tc = m.twod ? 0.5f : odd * inv2n;
+            odd += 2.f;
+            int r = sample_inside<T>(sh, f, __fmaf_rn(tc, f.szx, bx), __fmaf_rn(tc, f.szy, by),
+                                     __fmaf_rn(tc, f.szz, bz));
             if (r == 2) {
                 ++*rechecks;
-                r = exact_inside_sample(sh, m, i, j, k, a, b, c3, n, x, q);
+                r = exact_inside_sample(sh, m, i, j, k, ia, ib, c3, n, x, q);
             }
             cnt += r;
         }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    return (float)((double)cnt / (double)(n * n * nzs));
+    return cnt;
+}
+
+static __device__ __noinline__ float subsample_warp(const MeshK& m, const ShapeK& sh, const float* M, const TileFrame& tf,
+                                                    int a0, int b0, int c0, const D3& x, const Q4& q, int64_t i,
+                                                    int64_t j, int64_t k, int n, unsigned long long* rechecks) {
+    const float u = U32;
+    const float hx = m.h32[0], hy = m.h32[1], hz = m.h32[2];
+    const float ox = (float)a0 * hx, oy = (float)b0 * hy, oz = (float)c0 * hz;  // cell corner within the tile
+    const float dx = tf.bx + ox, dy = tf.by + oy, dz = tf.bz + oz;
+    SampleFrame f;
+    f.px = __fmaf_rn(M[0], dx, __fmaf_rn(M[1], dy, M[2] * dz));
+    f.py = __fmaf_rn(M[3], dx, __fmaf_rn(M[4], dy, M[5] * dz));
+    f.pz = __fmaf_rn(M[6], dx, __fmaf_rn(M[7], dy, M[8] * dz));
+    f.sxx = M[0] * hx; f.sxy = M[3] * hx; f.sxz = M[6] * hx;
+    f.syx = M[1] * hy; f.syy = M[4] * hy; f.syz = M[7] * hy;
+    f.szx = M[2] * hz; f.szy = M[5] * hz; f.szz = M[8] * hz;
+    const float sabs = fabsf(f.sxx) + fabsf(f.sxy) + fabsf(f.sxz) + fabsf(f.syx) + fabsf(f.syy) + fabsf(f.syz) +
+                       fabsf(f.szx) + fabsf(f.szy) + fabsf(f.szz);
+    f.E = 8.f * u * (tf.babs + fabsf(ox) + fabsf(oy) + fabsf(oz) + 2.f * (fabsf(dx) + fabsf(dy) + fabsf(dz)) +
+                     3.f * (hx + hy + hz)) +
+          8.f * u * (fabsf(f.px) + fabsf(f.py) + fabsf(f.pz) + sabs) + tf.e64 + 1e-30f;
+    const int type = sh.type;
+    const bool prism = sh.prism;
+    const float* a = sh.p32;
+    int kind = SS_GENERIC;
+    if (type == SDFIBM_SHAPE_CIRCLE || type == SDFIBM_SHAPE_SPHERE || type == SDFIBM_SHAPE_ELLIPSE ||
+        type == SDFIBM_SHAPE_ELLIPSOID)
+        kind = SS_QUADRIC;
+    else if (type == SDFIBM_SHAPE_RECTANGLE || type == SDFIBM_SHAPE_BOX)
+        kind = SS_BOX;
+    float Ep = f.E;
+    if (kind != SS_GENERIC) {
+        // sample = (corner + com) + steps: one more rounding of the corner, the conversion of com to FP32, and the
+        // stepping FMAs now run at magnitudes up to |com| larger (the ellipsoid ignores com, as the reference does)
+        const bool use_com = type != SDFIBM_SHAPE_ELLIPSOID;
+        const float c0x = use_com ? sh.com32[0] : 0.f, c0y = use_com ? sh.com32[1] : 0.f;
+        f.px += c0x;
+        f.py += c0y;
+        if (prism) {
+            // 2-D shapes: the local z is the FP32 com z for every sample (exact steps of zero)
+            f.pz = sh.com32[2];
+            f.sxz = 0.f; f.syz = 0.f; f.szz = 0.f;
+        } else if (use_com) {
+            f.pz += sh.com32[2];
+        }
+        const float cabs = use_com ? fabsf(sh.com32[0]) + fabsf(sh.com32[1]) + fabsf(sh.com32[2]) : 0.f;
+        Ep = f.E + 2.f * u * (fabsf(f.px) + fabsf(f.py) + fabsf(f.pz) + sabs) + 5.f * u * cabs;
+    }
+    // largest |coordinate| any sample of the cell can reach
+    const float mx = fabsf(f.px) + fabsf(f.sxx) + fabsf(f.syx) + fabsf(f.szx) + Ep;
+    const float my = fabsf(f.py) + fabsf(f.sxy) + fabsf(f.syy) + fabsf(f.szy) + Ep;
+    const float mz = fabsf(f.pz) + fabsf(f.sxz) + fabsf(f.syz) + fabsf(f.szz) + Ep;
+    int cnt;
+    if (kind == SS_QUADRIC) {
+        switch (type) {
+            case SDFIBM_SHAPE_CIRCLE:
+            case SDFIBM_SHAPE_SPHERE: f.k0 = 1.f; f.k1 = 1.f; f.k2 = 1.f; f.k3 = a[1]; break;
+            case SDFIBM_SHAPE_ELLIPSE: f.k0 = a[2]; f.k1 = a[3]; f.k2 = 0.f; f.k3 = 1.f; break;
+            default: f.k0 = a[3]; f.k1 = a[4]; f.k2 = a[5]; f.k3 = 1.f; break;
+        }
+        f.Eg = (2.f * (mx * f.k0 + my * f.k1 + mz * f.k2) + Ep * (f.k0 + f.k1 + f.k2)) * Ep +
+               10.f * u * (mx * mx * f.k0 + my * my * f.k1 + mz * mz * f.k2 + f.k3);
+        cnt = subsample_count<SS_QUADRIC>(m, sh, f, i, j, k, n, x, q, rechecks);
+    } else if (kind == SS_BOX) {
+        f.k0 = a[0]; f.k1 = a[1];
+        f.k2 = prism ? INFINITY : a[2];  // the rectangle has no z extent
+        f.Eg = Ep + 2.f * u * (fmaxf(mx, fmaxf(my, prism ? 0.f : mz)) + fmaxf(a[0], fmaxf(a[1], prism ? 0.f : a[2])));
+        cnt = subsample_count<SS_BOX>(m, sh, f, i, j, k, n, x, q, rechecks);
+    } else {
+        cnt = subsample_count<SS_GENERIC>(m, sh, f, i, j, k, n, x, q, rechecks);
+    }
+    const int nzs = m.twod ? 1 : n;
+    return __fdiv_rn((float)cnt, (float)(n * n * nzs));  // cnt and n^3 are exact in FP32: one correct rounding
 }
 
 // ---- signed distance for REF-GEO: FP64 where it decides, FP32 where it only scales ------------------------------------
@@ -384,7 +472,7 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                 const unsigned bal = __ballot_sync(FULL, is_cut);
                 if (is_cut) {
                     cutlist[ncut + __popc(bal & ((1u << lane) - 1u))] = (uint8_t)e;
-                    if (A.method == SDFIBM_FRACTION_REFGEO) {
+                    if (A.method == SDFIBM_FRACTION_REFGEO || A.method == SDFIBM_FRACTION_LEARNED) {
                         const int v0 = a + VX * (b + VY * c);
                         vneed[v0] = 1; vneed[v0 + 1] = 1; vneed[v0 + VX] = 1; vneed[v0 + VX + 1] = 1;
                         vneed[v0 + VX * VY] = 1; vneed[v0 + VX * VY + 1] = 1; vneed[v0 + VX * VY + VX] = 1;
@@ -395,7 +483,7 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
             }
             if (ncut == 0) continue;
             __syncwarp();
-            if (A.method == SDFIBM_FRACTION_REFGEO) {
+            if (A.method == SDFIBM_FRACTION_REFGEO || A.method == SDFIBM_FRACTION_LEARNED) {
                 // Solid::phi once per vertex next to a cut candidate.  The needed vertices are compacted first so
                 // every FP64 instruction runs on a full warp; the local point is the solid's FP64 local map applied to
                 // small integer offsets from the bbox corner.
@@ -422,6 +510,36 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                     vphi[v] = ph;
                 }
                 __syncwarp();
+                if (A.method == SDFIBM_FRACTION_LEARNED) {
+                    // features of every cut cell into the network's input buffer; the fraction comes later
+                    for (int u0 = 0; u0 < ncut; u0 += 32) {
+                        int base = 0;
+                        if (lane == 0) base = atomicAdd(&A.cnt->n_feat, min(32, ncut - u0));
+                        base = __shfl_sync(FULL, base, 0);
+                        const int u = u0 + lane;
+                        if (u < ncut) {
+                            const int e = cutlist[u];
+                            const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
+                            const int v0 = a + VX * (b + VY * c);
+                            const float ph[8] = {vphi[v0], vphi[v0 + 1], vphi[v0 + VX], vphi[v0 + VX + 1],
+                                                 vphi[v0 + VX * VY], vphi[v0 + VX * VY + 1],
+                                                 vphi[v0 + VX * VY + VX], vphi[v0 + VX * VY + VX + 1]};
+                            float fe[MLP_IN];
+                            cell_features(ph, A.inv_h, fe);
+                            const int64_t slot = (int64_t)base + lane;
+                            if (slot < A.feat_cap) {
+#pragma unroll
+                                for (int q2 = 0; q2 < MLP_IN; ++q2) A.feat[q2 * A.feat_cap + slot] = fe[q2];
+                                A.fref_solid[slot] = s;
+                                A.fref_index[slot] = k.scratch_off + local_index(a, b, c);
+                            } else {
+                                set_error(A.cnt, DERR_CAPACITY);
+                            }
+                        }
+                    }
+                    __syncwarp();
+                    continue;
+                }
                 for (int u = lane; u < ncut; u += 32) {
                     const int e = cutlist[u];
                     const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
@@ -459,6 +577,41 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
         if (rechecks) atomicAdd(&A.cnt->exact_rechecks, rechecks);
         if (valid_cells) atomicAdd(&A.cnt->bbox_cells, valid_cells);
     }
+}
+
+// LEARNED fallback: one warp per cell outside the network's band, SUBSAMPLE from the cell's own FP32 frame
+__global__ void __launch_bounds__(256) learned_fallback_kernel(FallbackArgs A) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nfb = min((int64_t)A.cnt->n_fb, A.cap);
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    unsigned long long rechecks = 0;
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nfb; w += warps) {
+        const int32_t slot = A.fb_list[w];
+        const int s = A.fref_solid[slot];
+        const int64_t idx = A.fref_index[slot];
+        const SolidK& k = A.sk[s];
+        const SolidPlan& pl = A.plan[s];
+        const int64_t local = idx - k.scratch_off;
+        const int64_t la = local % k.ext[0], lb = (local / k.ext[0]) % k.ext[1], lc = local / ((int64_t)k.ext[0] * k.ext[1]);
+        TileFrame tf;
+        tf.bx = (float)(pl.base[0] + (double)la * A.m.h[0]);
+        tf.by = (float)(pl.base[1] + (double)lb * A.m.h[1]);
+        tf.bz = (float)(pl.base[2] + (double)lc * A.m.h[2]);
+        tf.babs = 2.f * (fabsf(tf.bx) + fabsf(tf.by) + fabsf(tf.bz)) +
+                  (float)(fabs(pl.base[0]) + fabs(pl.base[1]) + fabs(pl.base[2]));
+        tf.e64 = pl.e64;
+        float M[9];
+#pragma unroll
+        for (int r = 0; r < 9; ++r) M[r] = pl.M[r];
+        const Q4 q = state_quat(A.st[s]);
+        const D3 x = state_pos(A.st[s]);
+        const float al = subsample_warp(A.m, k.shape, M, tf, 0, 0, 0, x, q, pl.lo[0] + la, pl.lo[1] + lb,
+                                        pl.lo[2] + lc, A.n, &rechecks);
+        if (lane == 0) A.alpha[idx] = al;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);
+    if (lane == 0 && rechecks) atomicAdd(&A.cnt->exact_rechecks, rechecks);
 }
 
 // 3-D meshes: 4x4x4-cell tiles; one- and two-layer meshes: 8x8x2

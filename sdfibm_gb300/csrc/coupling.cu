@@ -425,6 +425,42 @@ constexpr int CPL_THREADS = 256;
 
 
 
+// Reduce-scatter of 8 values over the warp in three xor steps: afterwards each lane holds slot (lane >> 2) & 7 summed
+// over the 8 lanes that share its bits 0..1; warp_total4 then adds the 4 lanes that differ in those bits.
+template <typename T>
+__device__ __forceinline__ T reduce_scatter8(T* v, int lane) {
+    {
+        const bool up = (lane & 16) != 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const T send = up ? v[i] : v[i + 4];
+            const T keep = up ? v[i + 4] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        }
+    }
+    {
+        const bool up = (lane & 8) != 0;
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const T send = up ? v[i] : v[i + 2];
+            const T keep = up ? v[i + 2] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+        }
+    }
+    const bool up = (lane & 4) != 0;
+    const T send = up ? v[0] : v[1];
+    const T keep = up ? v[1] : v[0];
+    return keep + __shfl_xor_sync(0xffffffffu, send, 4);
+}
+// sum over the 4 lanes that differ in bits 0..1 (FP64)
+__device__ __forceinline__ double warp_total4(double x) {
+    x += __shfl_xor_sync(0xffffffffu, x, 2);
+    x += __shfl_xor_sync(0xffffffffu, x, 1);
+    return x;
+}
+
+// Per-cell forcing (pcHydrodynamicInteraction, solidcloud.cpp:384-390) and the force/torque sums (:411-421).
+// ftacc receives sum f and sum (C - x) x f; ft_kernel applies rho_f * V / dt once per solid.
 __global__ void __launch_bounds__(CPL_THREADS) couple_kernel(CoupleArgs A) {
     __shared__ int s_item;
     const MeshK& m = A.m;
@@ -433,6 +469,7 @@ __global__ void __launch_bounds__(CPL_THREADS) couple_kernel(CoupleArgs A) {
     const int n_in = clamp_len(A.cnt->n_inside, A.cnt->list_cap), n_cut = clamp_len(A.cnt->n_cut, A.cnt->list_cap);
     const int in_chunks = (n_in + CPL_THREADS - 1) / CPL_THREADS;
     const int cut_chunks = (n_cut + CPL_THREADS - 1) / CPL_THREADS;
+    const float dtINV32 = (float)A.dtINV;
     for (;;) {
         if (tid == 0) s_item = atomicAdd(&A.cnt->couple_next, 1);
         __syncthreads();
@@ -443,7 +480,8 @@ __global__ void __launch_bounds__(CPL_THREADS) couple_kernel(CoupleArgs A) {
         const int e = (is_cut ? item - in_chunks : item) * CPL_THREADS + tid;
         const bool valid = e < (is_cut ? n_cut : n_in);
         int s = -1;
-        double f6[6] = {0, 0, 0, 0, 0, 0};
+        double f6[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        float g6[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (valid) {
             const int32_t c32 = is_cut ? A.cut_cell[e] : A.in_cell[e];
             const int32_t sw = is_cut ? A.cut_solid[e] : A.in_solid[e];
@@ -451,85 +489,82 @@ __global__ void __launch_bounds__(CPL_THREADS) couple_kernel(CoupleArgs A) {
             const int type = list_type(sw);
             const int64_t c = (c32 >= 0 && c32 < N) ? c32 : 0;
             if (c32 != c) set_error(A.cnt, DERR_CAPACITY);
-            const int64_t i = c % m.nx, j = (c / m.nx) % m.ny, k = c / ((int64_t)m.nx * m.ny);
+            int i, j, k;
+            cell_ijk(m, c, i, j, k);
             const sdfibm_solid_state& st = A.st[s];
-            const D3 x = state_pos(st);
-            double alpha = 1.0;
+            float alpha = 1.f;
             if (is_cut) {
                 // computed by the classify pass for every cut candidate of the solid's bbox
                 const SolidK& ks = A.sk[s];
                 const int32_t* lo = A.plan[s].lo;
                 const int64_t li = (i - lo[0]) + (int64_t)ks.ext[0] * ((j - lo[1]) + (int64_t)ks.ext[1] * (k - lo[2]));
-                alpha = (double)A.alpha[ks.scratch_off + li];
+                alpha = A.alpha[ks.scratch_off + li];
             }
-            // pcHydrodynamicInteraction (solidcloud.cpp:384-390) and the accumulation of :411-421
             const float Ux = A.U[c], Uy = A.U[N + c], Uz = A.U[2 * N + c];
-            D3 fs;
+            float fsx, fsy, fsz;
             if (A.exact_forcing) {
                 // the reference's FP64 sequence
+                const D3 x = state_pos(st);
                 const D3 cc = mesh_C(m, i, j, k);
                 const D3 vel{st.vel[0], st.vel[1], st.vel[2]}, om{st.omega[0], st.omega[1], st.omega[2]};
                 const D3 uf{(double)Ux, (double)Uy, (double)Uz};
                 const D3 us = vel + cross(om, cc - x);
-                const D3 f_ = alpha * (uf - us);
+                const D3 f_ = (double)alpha * (uf - us);
                 const D3 t_ = cross(cc - x, f_);
-                const double cv = m.V;
-                const D3 F = f_ * cv * A.dtINV, T = t_ * cv * A.dtINV;
-                f6[0] = F.x; f6[1] = F.y; f6[2] = F.z; f6[3] = T.x; f6[4] = T.y; f6[5] = T.z;
-                fs = f_ * A.dtINV;
+                f6[0] = f_.x; f6[1] = f_.y; f6[2] = f_.z; f6[3] = t_.x; f6[4] = t_.y; f6[5] = t_.z;
+                fsx = (float)(f_.x * A.dtINV); fsy = (float)(f_.y * A.dtINV); fsz = (float)(f_.z * A.dtINV);
             } else {
-                // FP32: the offset C - x is the solid's FP64 seed offset plus a small integer number of cells
+                // FP64 for the rigid-body velocity and U - us (the difference can cancel), FP32 after it.  C - x is
+                // the solid's FP64 seed offset plus a whole number of cells.
                 const SolidPlan& pl = A.plan[s];
-                const float dx = __fmaf_rn((float)(i - pl.seed_ijk[0]), m.h32[0], (float)pl.cbase[0]);
-                const float dy = __fmaf_rn((float)(j - pl.seed_ijk[1]), m.h32[1], (float)pl.cbase[1]);
-                const float dz = __fmaf_rn((float)(k - pl.seed_ijk[2]), m.h32[2], (float)pl.cbase[2]);
-                const float ox = (float)st.omega[0], oy = (float)st.omega[1], oz = (float)st.omega[2];
-                const float usx = (float)st.vel[0] + (oy * dz - oz * dy);
-                const float usy = (float)st.vel[1] + (oz * dx - ox * dz);
-                const float usz = (float)st.vel[2] + (ox * dy - oy * dx);
-                const float al = (float)alpha;
-                const float fx = al * (Ux - usx), fy = al * (Uy - usy), fz = al * (Uz - usz);
-                const float k1 = (float)(m.V * A.dtINV), di = (float)A.dtINV;
-                f6[0] = fx * k1; f6[1] = fy * k1; f6[2] = fz * k1;
-                f6[3] = (dy * fz - dz * fy) * k1; f6[4] = (dz * fx - dx * fz) * k1; f6[5] = (dx * fy - dy * fx) * k1;
-                fs = D3{fx * di, fy * di, fz * di};
+                const D3 d{pl.cbase[0] + (double)(i - pl.seed_ijk[0]) * m.h[0],
+                           pl.cbase[1] + (double)(j - pl.seed_ijk[1]) * m.h[1],
+                           pl.cbase[2] + (double)(k - pl.seed_ijk[2]) * m.h[2]};
+                const D3 vel{st.vel[0], st.vel[1], st.vel[2]}, om{st.omega[0], st.omega[1], st.omega[2]};
+                const D3 us = vel + cross(om, d);
+                const float fx = alpha * (float)((double)Ux - us.x), fy = alpha * (float)((double)Uy - us.y),
+                            fz = alpha * (float)((double)Uz - us.z);
+                const float dx = (float)d.x, dy = (float)d.y, dz = (float)d.z;
+                g6[0] = fx; g6[1] = fy; g6[2] = fz;
+                g6[3] = dy * fz - dz * fy; g6[4] = dz * fx - dx * fz; g6[5] = dx * fy - dy * fx;
+                fsx = fx * dtINV32; fsy = fy * dtINV32; fsz = fz * dtINV32;
             }
             const uint32_t claim = reinterpret_cast<const uint32_t*>(A.Ct)[c];
             if (!(claim & CT_SHARED)) {
                 // the only solid on this cell: the final values (As += alpha on a zeroed field, checkAlpha, Ct)
-                A.As[c] = fminf((float)alpha, 1.0f);
-                A.Ts[c] = (float)alpha;
-                A.Fs[c] = (float)fs.x;
-                A.Fs[N + c] = (float)fs.y;
-                A.Fs[2 * N + c] = (float)fs.z;
+                A.As[c] = fminf(alpha, 1.0f);
+                A.Ts[c] = alpha;
+                A.Fs[c] = fsx;
+                A.Fs[N + c] = fsy;
+                A.Fs[2 * N + c] = fsz;
                 A.Ct[c] = type == 1 ? s + 4 : type;
             } else {
                 const int slot = shared_slot(A, (int32_t)c);
                 if (slot >= 0) {
                     double* v = A.sh_vals + 5 * (int64_t)slot;
-                    atomicAdd(v + 0, alpha);
-                    atomicAdd(v + 1, alpha);
-                    atomicAdd(v + 2, fs.x);
-                    atomicAdd(v + 3, fs.y);
-                    atomicAdd(v + 4, fs.z);
+                    atomicAdd(v + 0, (double)alpha);
+                    atomicAdd(v + 1, (double)alpha);
+                    atomicAdd(v + 2, (double)fsx);
+                    atomicAdd(v + 3, (double)fsy);
+                    atomicAdd(v + 4, (double)fsz);
                 }
             }
         }
-        // force/torque: one FP64 atomic per warp when the warp serves a single solid
+        // force/torque: a reduce-scatter over the warp and one FP64 atomic per (solid, component) when the warp
+        // serves a single solid
         const int s0 = __shfl_sync(0xffffffffu, s, 0);
         const bool uniform = __all_sync(0xffffffffu, s == s0 || s < 0);
         if (uniform) {
-#pragma unroll
-            for (int r = 0; r < 6; ++r) {
-                double v = f6[r];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                f6[r] = v;
+            double v;
+            if (A.exact_forcing) {
+                v = warp_total4(reduce_scatter8(f6, lane));
+            } else {
+                v = warp_total4((double)reduce_scatter8(g6, lane));
             }
-            if (lane == 0 && s0 >= 0)
-                for (int r = 0; r < 6; ++r) atomicAdd(A.ftacc + 6 * s0 + r, f6[r]);
+            const int slot = lane >> 2;
+            if ((lane & 3) == 0 && slot < 6 && s0 >= 0) atomicAdd(A.ftacc + 6 * s0 + slot, v);
         } else if (s >= 0) {
-            for (int r = 0; r < 6; ++r) atomicAdd(A.ftacc + 6 * s + r, f6[r]);
+            for (int r = 0; r < 6; ++r) atomicAdd(A.ftacc + 6 * s + r, A.exact_forcing ? f6[r] : (double)g6[r]);
         }
     }
 }
@@ -566,12 +601,14 @@ __global__ void begin_kernel(Counters* cnt) {
     cnt->classify_next = 0; cnt->couple_next = 0; cnt->finalize_next = 0;
     cnt->n_inside = 0; cnt->n_cut = 0; cnt->n_shared = 0;
     cnt->exact_rechecks = 0; cnt->bbox_cells = 0;
+    cnt->n_feat = 0; cnt->n_fb = 0;
 }
 
-__global__ void ft_kernel(const double* __restrict__ ftacc, double* __restrict__ ft, int S, double rho_f) {
+// F = rho_f * V / dt * sum f, T = rho_f * V / dt * sum (C - x) x f  (solidcloud.cpp:411-421)
+__global__ void ft_kernel(const double* __restrict__ ftacc, double* __restrict__ ft, int S, double scale) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= S) return;
-    for (int r = 0; r < 6; ++r) ft[6 * s + r] = ftacc[6 * s + r] * rho_f;
+    for (int r = 0; r < 6; ++r) ft[6 * s + r] = ftacc[6 * s + r] * scale;
 }
 
 // sparse reset: the cells the previous call touched and this call does not (after this call's claims, before the
@@ -600,7 +637,8 @@ __global__ void fix_internal_kernel(MeshK m, const sdfibm_solid_state* __restric
         const int32_t s = in_solid[e] & LIST_SOLID_MASK;
         if (c < 0 || c >= N) continue;
         if (Ct[c] != s + 4) continue;
-        const int64_t i = c % m.nx, j = (c / m.nx) % m.ny, k = c / ((int64_t)m.nx * m.ny);
+        int i, j, k;
+        cell_ijk(m, c, i, j, k);
         const sdfibm_solid_state& x = st[s];
         const D3 vel{x.vel[0], x.vel[1], x.vel[2]}, om{x.omega[0], x.omega[1], x.omega[2]};
         const D3 u = vel + cross(om, mesh_C(m, i, j, k) - state_pos(x));

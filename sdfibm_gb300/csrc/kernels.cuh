@@ -6,13 +6,43 @@
 
 namespace sdfibm_dev {
 
+// Division of a cell label (< 2^31) by a fixed divisor: q = (n * mul) >> shift with mul = ceil(2^shift / d),
+// shift = 32 + ceil(log2 d) (Granlund and Montgomery, "Division by invariant integers using multiplication", 1994).
+struct FastDiv {
+    uint64_t mul;
+    uint32_t shift;
+    uint32_t d;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+    uint32_t l = 0;
+    while ((1ull << l) < d) ++l;
+    const unsigned __int128 p = (unsigned __int128)1 << (32 + l);
+    return FastDiv{(uint64_t)((p + d - 1) / d), 32 + l, d};
+}
+__host__ __device__ inline uint32_t fdiv(uint32_t n, const FastDiv& f) { return (uint32_t)(((uint64_t)n * f.mul) >> f.shift); }
+
 struct MeshK {
     int32_t nx, ny, nz, twod;
     double o[3], h[3];
     float h32[3];
     int64_t ncells;
     double V;  // hx*hy*hz
+    FastDiv div_x, div_xy;  // by nx and by nx*ny
 };
+inline void mesh_fastdiv(MeshK& m) {
+    m.div_x = make_fastdiv((uint32_t)m.nx);
+    m.div_xy = make_fastdiv((uint32_t)((int64_t)m.nx * m.ny));
+}
+// (i, j, k) of cell label c (0 <= c < ncells < 2^31)
+__device__ inline void cell_ijk(const MeshK& m, int64_t c, int& i, int& j, int& k) {
+    const uint32_t u = (uint32_t)c;
+    const uint32_t kk = fdiv(u, m.div_xy);
+    const uint32_t r = u - kk * m.div_xy.d;
+    const uint32_t jj = fdiv(r, m.div_x);
+    i = (int)(r - jj * m.div_x.d);
+    j = (int)jj;
+    k = (int)kk;
+}
 
 // Static per-solid record (built once by sdfibm_cuda_create).
 struct SolidK {
@@ -71,6 +101,8 @@ struct Counters {
     int32_t launches;
     int32_t pad;
     int64_t list_cap;         // capacity of each touched-cell list (set once at create)
+    int32_t n_feat;           // LEARNED: cut cells whose features the classify pass wrote this call
+    int32_t n_fb;             // LEARNED: of those, cells outside the model's band (SUBSAMPLE fallback)
 };
 
 // list lengths clamped to the capacity (a capacity error leaves the counters above what was written)
@@ -125,6 +157,27 @@ struct ClassifyArgs {
     Counters* cnt;
     int method;        // sdfibm_fraction_method, or -1: classification only
     int subsample_n;
+    // LEARNED: features of every cut cell ([11][feat_cap]) and where its fraction goes
+    float* feat;
+    int64_t feat_cap;
+    int32_t* fref_solid;
+    int64_t* fref_index;  // index into alpha
+    float inv_h;          // 1 / h (x spacing) of the feature scaling
+};
+
+// LEARNED: cells left to SUBSAMPLE by the network's confidence band
+struct FallbackArgs {
+    MeshK m;
+    const SolidK* sk;
+    const sdfibm_solid_state* st;
+    const SolidPlan* plan;
+    const int32_t* fb_list;    // positions into the feature buffer
+    const int32_t* fref_solid;
+    const int64_t* fref_index;
+    int64_t cap;
+    float* alpha;
+    Counters* cnt;
+    int n;                     // samples per axis
 };
 
 // UGrid (src/libcollision/ugrid.h:14-58): bbox of the mesh, spacing 2*max radiusB, row-major i*ny*nz + j*nz + k
@@ -148,7 +201,8 @@ enum DeviceError : int32_t {
     DERR_CAPACITY = 1,     // a list outgrew its capacity
     DERR_BBOX = 2,         // a solid's region left its static bbox (tilted 2-D shape)
     DERR_FLOOD_LIMIT = 3,  // flood fill hit its iteration bound
-    DERR_SHARED_TABLE = 4  // the shared-cell table is full
+    DERR_SHARED_TABLE = 4, // the shared-cell table is full
+    DERR_MMA_TIMEOUT = 7   // a tensor-core completion was not observed in time (SDFIBM_MLP_ERR_TIMEOUT)
 };
 
 }  // namespace sdfibm_dev

@@ -251,6 +251,7 @@ extern "C" int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc* mesh, const s
     for (int a = 0; a < 3; ++a) { m.o[a] = mesh->origin[a]; m.h[a] = mesh->h[a]; m.h32[a] = (float)mesh->h[a]; }
     m.ncells = N;
     m.V = mesh->h[0] * mesh->h[1] * mesh->h[2];
+    mesh_fastdiv(m);
 
     sdfibm_solid_state x;
     std::memset(&x, 0, sizeof(x));

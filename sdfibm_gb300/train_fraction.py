@@ -1,0 +1,106 @@
+"""Trains the learned cut-cell fraction model on the GPU and writes sdfibm_gb300/data/fraction_mlp.npz.
+
+    python -m sdfibm_gb300.train_fraction [--train 10000000] [--test 1000000] [--epochs 40] [--out PATH]
+
+Steps, all through libsdfibm_cuda.so:
+  1. labelled cut cells (sdfibm_mlp_dataset): random spheres, ellipsoids, boxes, planes, circle and ellipse
+     prisms under random rotation and translation, cell size / radius log-uniform in [hr_min, hr_max], label =
+     fraction of a 16^3 lattice of isInside samples (SUBSAMPLE with 4096 samples);
+  2. Adam on the mean squared error, every gradient from the tensor-core forward + backward kernels
+     (sdfibm_mlp_train);
+  3. the confidence band: on held-out cells, the largest (tau_twist, tau_grad) box whose accepted cells keep the
+     mean absolute error at most --band-mean and the 99.9th percentile at most --band-p999;
+  4. the model file, with the training record (data description, losses, held-out errors, timings) in `meta`.
+"""
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import learned
+
+
+def band_scores(torch, feat):
+    """(twist sum, | |trilinear gradient| - 1 |) of every cell; the formulas of in_band in mlp.cuh."""
+    f = feat[:8]
+    tw = ((f[0] - f[1] - f[2] + f[3]).abs() + (f[4] - f[5] - f[6] + f[7]).abs() + (f[0] - f[1] - f[4] + f[5]).abs() +
+          (f[2] - f[3] - f[6] + f[7]).abs() + (f[0] - f[2] - f[4] + f[6]).abs() + (f[1] - f[3] - f[5] + f[7]).abs())
+    gx = 0.25 * (((f[1] - f[0]) + (f[3] - f[2])) + ((f[5] - f[4]) + (f[7] - f[6])))
+    gy = 0.25 * (((f[2] - f[0]) + (f[3] - f[1])) + ((f[6] - f[4]) + (f[7] - f[5])))
+    gz = 0.25 * (((f[4] - f[0]) + (f[5] - f[1])) + ((f[6] - f[2]) + (f[7] - f[3])))
+    return tw, ((gx * gx + gy * gy + gz * gz).sqrt() - 1.0).abs()
+
+
+def calibrate(torch, err, tw, gd, mean_max, p999_max):
+    """Largest accepted fraction over a grid of (tau_twist, tau_grad) quantiles meeting both error limits."""
+    qs = torch.tensor([0.5, 0.6, 0.7, 0.8, 0.85, 0.9, 0.93, 0.95, 0.97, 0.98, 0.99, 0.995, 0.999, 1.0],
+                      device=err.device)
+    tws = torch.quantile(tw[:1 << 20].double(), qs.double()).float()
+    gds = torch.quantile(gd[:1 << 20].double(), qs.double()).float()
+    best = (0.0, 0.0, 0.0, float("nan"), float("nan"))
+    for a in tws.tolist():
+        for b in gds.tolist():
+            acc = (tw <= a) & (gd <= b)
+            frac = acc.float().mean().item()
+            if frac <= best[0]:
+                continue
+            e = err[acc]
+            if e.numel() == 0:
+                continue
+            m = e.mean().item()
+            p = torch.quantile(e[:1 << 22].double(), 0.999).item()
+            if m <= mean_max and p <= p999_max:
+                best = (frac, a, b, m, p)
+    return best
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--train", type=int, default=10_000_000)
+    ap.add_argument("--test", type=int, default=1_000_000)
+    ap.add_argument("--epochs", type=int, default=40)
+    ap.add_argument("--batch", type=int, default=32768)
+    ap.add_argument("--lr", type=float, default=3e-3)
+    ap.add_argument("--hr-min", type=float, default=0.01)
+    ap.add_argument("--hr-max", type=float, default=1.5)
+    ap.add_argument("--n-sub", type=int, default=16)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--band-mean", type=float, default=3e-4)
+    ap.add_argument("--band-p999", type=float, default=5e-3)
+    ap.add_argument("--out", default=learned.MODEL_PATH)
+    a = ap.parse_args(argv)
+    import torch
+    torch.cuda.init()
+    dkw = dict(hr=(a.hr_min, a.hr_max), n_sub=a.n_sub)
+    t0 = time.time()
+    feat, label, _ = learned.make_dataset(torch, a.train, seed=a.seed, **dkw)
+    tf, tl, _ = learned.make_dataset(torch, a.test, seed=a.seed + 1, **dkw)
+    torch.cuda.synchronize()
+    t_data = time.time() - t0
+    p = torch.from_numpy(learned.init_params(a.seed)).cuda()
+    t0 = time.time()
+    losses = learned.train(torch, p, feat, label, epochs=a.epochs, batch=a.batch, lr=a.lr,
+                           warmup_steps=min(500, a.train // a.batch))
+    torch.cuda.synchronize()
+    t_train = time.time() - t0
+    pred = learned.forward(torch, p, tf)
+    err = (pred - tl).abs()
+    tw, gd = band_scores(torch, tf)
+    frac, tau_tw, tau_gd, m_acc, p_acc = calibrate(torch, err, tw, gd, a.band_mean, a.band_p999)
+    q = torch.quantile(err[:1 << 22].double(), torch.tensor([0.5, 0.9, 0.99, 0.999], dtype=torch.float64,
+                                                            device=err.device)).tolist()
+    meta = dict(data=dict(train=a.train, test=a.test, seed=a.seed, hr=[a.hr_min, a.hr_max], n_sub=a.n_sub,
+                          families="sphere ellipsoid box plane circle-prism ellipse-prism", z_axis_frac=0.25),
+                train=dict(epochs=a.epochs, batch=a.batch, lr=a.lr, loss_per_epoch=[float(x) for x in losses],
+                           seconds=t_train, data_seconds=t_data),
+                test=dict(mean_abs=err.mean().item(), max_abs=err.max().item(), q50=q[0], q90=q[1], q99=q[2],
+                          q999=q[3]),
+                band=dict(tau_twist=tau_tw, tau_grad=tau_gd, accepted=frac, accepted_mean_abs=m_acc,
+                          accepted_q999=p_acc, limits=dict(mean=a.band_mean, q999=a.band_p999)))
+    learned.save_model(p.cpu().numpy(), tau_tw, tau_gd, meta, a.out)
+    print(json.dumps(meta))
+
+
+if __name__ == "__main__":
+    main()

@@ -10,10 +10,15 @@ AS_REL, AS_ABS = 1e-5, 1e-9      # As, Ts and Fs per cell: |d| <= 1e-5 |ref| + 1
 FT_REL = 1e-6                    # force/torque per solid, normwise against the sum of |contributions|
 
 
-def run_pair(torch, w, steps=1, evolve=False, fix=False, U=None):
-    """Runs `steps` interact (+evolve, +fixInternal) on the GPU and on the fast oracle; returns both sides."""
+def run_pair(torch, w, steps=1, evolve=False, fix=False, U=None, gpu_opt=None, gpu_setup=None):
+    """Runs `steps` interact (+evolve, +fixInternal) on the GPU and on the fast oracle; returns both sides.
+
+    gpu_opt: options of the GPU side when they differ from the oracle's (w.opt); gpu_setup(cloud) runs after
+    the GPU cloud is created."""
     Uh = w.U_numpy() if U is None else U
-    gpu = SolidCloud(w.mesh, w.solids, w.opt)
+    gpu = SolidCloud(w.mesh, w.solids, gpu_opt if gpu_opt is not None else w.opt)
+    if gpu_setup is not None:
+        gpu_setup(gpu)
     orc = OracleCloud(w.mesh, w.solids, w.opt, faithful=False)
     Ud = torch.from_numpy(Uh).cuda()
     Uo = Uh.astype(np.float64).reshape(-1).copy()

@@ -1,0 +1,86 @@
+"""Coupling with the learned cut-cell fraction (options.fraction_method = LEARNED) against the FP64 oracle running
+SUBSAMPLE with the 16^3 lattice the network is trained on and falls back to."""
+import copy
+import os
+
+import numpy as np
+import pytest
+
+from gpu_helpers import check_interact, run_pair
+from sdfibm_gb300 import abi, learned, workloads
+
+pytestmark = pytest.mark.gpu
+
+AS_MEAN = 1e-3   # learned path: mean |As - As_SUBSAMPLE(4096)| over the cut cells
+F_REL = 1e-4     # learned path: per-solid force, normwise against the sum of |contributions|
+
+
+def _learned_pair(torch, w, params, tau_twist, tau_grad):
+    orc_w = copy.copy(w)
+    orc_w.opt = abi.options(rho_f=w.opt.rho_f, collision_mode=w.opt.collision_mode,
+                            fraction_method=abi.FRACTION_SUBSAMPLE, subsample_n=16)
+    gpu_opt = abi.options(rho_f=w.opt.rho_f, collision_mode=w.opt.collision_mode,
+                          fraction_method=abi.FRACTION_LEARNED, learned_fallback_n=16)
+    r = run_pair(torch, orc_w, gpu_opt=gpu_opt,
+                 gpu_setup=lambda c: c.set_fraction_model(params, tau_twist, tau_grad))
+    return orc_w, r
+
+
+def test_band_closed_is_subsample16(cuda_lib, torch_cuda):
+    """With the band closed every cut cell takes the SUBSAMPLE fallback: the contract of the plain method holds."""
+    w = workloads.poly3d_256(scale=0.25)
+    orc_w, r = _learned_pair(torch_cuda, w, learned.init_params(0), -1.0, -1.0)
+    check_interact(orc_w, r)
+    st = r["gpu"].stats()
+    assert st["learned_cells"] == st["cut_cells"] > 0
+    assert st["learned_fallback_cells"] == st["learned_cells"]
+
+
+def test_band_open_predicts_every_cut_cell(cuda_lib, torch_cuda):
+    """With the band open the network gives every cut cell its fraction; enumeration and inside cells are exact."""
+    w = workloads.poly3d_256(scale=0.25)
+    orc_w, r = _learned_pair(torch_cuda, w, learned.init_params(1), 1e30, 1e30)
+    gpu, orc, fd, fo = r["gpu"], r["orc"], r["fd"], r["fo"]
+    st = gpu.stats()
+    assert st["learned_fallback_cells"] == 0 and st["learned_cells"] == st["cut_cells"] > 0
+    for s in range(len(w.solids)):
+        cg, tg = gpu.touched(s)
+        co, to = orc.touched(s)
+        assert np.array_equal(cg, co) and np.array_equal(tg, to)
+    assert np.array_equal(fd["Ct"].cpu().numpy(), fo["Ct"])
+    As = fd["As"].cpu().numpy()
+    for s in range(len(w.solids)):
+        cells, types = orc.touched(s)
+        assert np.all(As[cells[types == 1]] == 1.0)   # ALL_INSIDE cells take alpha = 1
+    touched = fo["Ct"] != 0
+    assert np.all((As[touched] > 0) & (As[touched] <= 1))
+
+
+@pytest.mark.skipif(not os.path.exists(learned.MODEL_PATH), reason="no trained fraction model")
+@pytest.mark.parametrize("cfg", ["poly3d_256", "poly3d_512"])
+def test_trained_model_accuracy(cuda_lib, torch_cuda, cfg):
+    """The shipped model with its band: As and per-solid force against SUBSAMPLE(4096) in FP64."""
+    params, tt, tg, meta = learned.load_model()
+    w = workloads.poly3d_256(scale=0.25) if cfg == "poly3d_256" else workloads.poly3d_512(scale=0.125,
+                                                                                          collision=abi.COLLISION_OFF)
+    orc_w, r = _learned_pair(torch_cuda, w, params, tt, tg)
+    gpu, orc, fd, fo = r["gpu"], r["orc"], r["fd"], r["fo"]
+    assert np.array_equal(fd["Ct"].cpu().numpy(), fo["Ct"])
+    As = fd["As"].cpu().numpy().astype(np.float64)
+    cut = (fo["Ct"] != 0) & ~((fo["As"] == 1.0) & (As == 1.0))
+    err = np.abs(As - fo["As"])[cut]
+    assert err.mean() <= AS_MEAN, "mean |As error| %g over %d cut cells" % (err.mean(), cut.sum())
+    FTg, FTo = r["FT"][-1]
+    N = orc.N
+    V = w.mesh.h[0] * w.mesh.h[1] * w.mesh.h[2]
+    Uo = r["Uo"].reshape(3, N)
+    rel = []
+    for s in range(len(w.solids)):
+        cells, _ = orc.touched(s)
+        if len(cells) == 0:
+            continue
+        st = orc.get_state()[s]
+        fm = np.linalg.norm(Uo[:, cells] - np.array(st.vel)[:, None], axis=0).sum() * w.opt.rho_f * V / w.dt
+        rel.append(np.linalg.norm(FTg[s, :3] - FTo[s, :3]) / (fm + 1e-300))
+    rel = np.array(rel)
+    assert np.median(rel) <= F_REL, "median per-solid force error %g" % np.median(rel)

@@ -1,0 +1,115 @@
+"""Learned cut-cell fraction on the GPU (tcgen05 kernels of mlp.cu through include/sdfibm_mlp.h) against the CPU
+oracle of the model (oracle/mlp_oracle.py) and of the training cells (oracle_sample_cell)."""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as MO
+from oracle import oracle as O
+from sdfibm_gb300 import abi, learned
+
+pytestmark = pytest.mark.gpu
+
+FWD_ABS = 2e-5      # predicted fraction, GPU vs oracle (same roundings; FP32 accumulation order, fast exp)
+GRAD_REL = 2e-2     # normwise per parameter block (BF16 roundings of dZ can flip by one unit in the last place)
+
+
+def _params(seed, bias=0.1):
+    p = learned.init_params(seed)
+    rng = np.random.default_rng(seed + 100)
+    p[MO.OFF_B1:MO.OFF_W2] = rng.normal(0, bias, 64)
+    p[MO.OFF_B2:MO.OFF_W3] = rng.normal(0, bias, 64)
+    p[MO.OFF_B3] = 0.3
+    return p
+
+
+def test_dataset_matches_oracle(cuda_lib, torch_cuda):
+    torch = torch_cuda
+    n = 2048  # 64 warps: every family drawn (the family is chosen per warp)
+    feat, label, rec = learned.make_dataset(torch, n, seed=7, recipe=True, n_sub=8)
+    feat, label, rec = feat.cpu().numpy(), label.cpu().numpy(), rec.cpu().numpy()
+    types = set()
+    for i in range(n):
+        phi, cnt = O.sample_cell(rec[i], 8)
+        assert 0 < rec[i, 17] < 8, "cell %d is not cut" % i
+        assert label[i] == np.float32(cnt / 512.0), "label of cell %d: %r vs %r" % (i, label[i], cnt / 512.0)
+        f = MO.features(phi.astype(np.float32)[None, :], np.float32(1.0))[0]
+        np.testing.assert_array_equal(feat[:, i], f)
+        types.add(int(rec[i, 0]))
+    assert types == {abi.SHAPE_SPHERE, abi.SHAPE_ELLIPSOID, abi.SHAPE_BOX, abi.SHAPE_PLANE, abi.SHAPE_CIRCLE,
+                     abi.SHAPE_ELLIPSE}
+
+
+def test_forward_matches_oracle(cuda_lib, torch_cuda):
+    torch = torch_cuda
+    n = 1000  # 8 tiles, the last one partial
+    feat, _, _ = learned.make_dataset(torch, n, seed=11)
+    p = _params(3)
+    out = learned.forward(torch, torch.from_numpy(p).cuda(), feat).cpu().numpy()
+    ref = MO.forward(p, feat.cpu().numpy().T)
+    err = np.abs(out - ref)
+    assert err.max() <= FWD_ABS, "max |GPU - oracle| = %g at cell %d" % (err.max(), int(err.argmax()))
+    # the hi/lo split matters: a single-BF16 forward is far off
+    lo = MO.forward(p, MO.bf16(feat.cpu().numpy().T))
+    assert np.abs(lo - ref).max() > FWD_ABS
+
+
+def test_forward_strided_features(cuda_lib, torch_cuda):
+    torch = torch_cuda
+    feat, _, _ = learned.make_dataset(torch, 4096, seed=12)
+    p = torch.from_numpy(_params(4)).cuda()
+    full = learned.forward(torch, p, feat)
+    part = learned.forward(torch, p, feat[:, 100:1300])  # stride 4096, 1200 cells
+    assert torch.equal(full[100:1300], part)
+
+
+def test_loss_grad_matches_oracle(cuda_lib, torch_cuda):
+    torch = torch_cuda
+    n = 1000
+    feat, label, _ = learned.make_dataset(torch, n, seed=13)
+    p = _params(5)
+    loss, g = learned.loss_grad(torch, torch.from_numpy(p).cuda(), feat, label)
+    lref, gref = MO.loss_grad(p, feat.cpu().numpy().T, label.cpu().numpy().astype(np.float64))
+    assert abs(loss - lref) <= 1e-5 * (1 + lref)
+    blocks = {"W1": (MO.OFF_W1, MO.OFF_B1), "b1": (MO.OFF_B1, MO.OFF_W2), "W2": (MO.OFF_W2, MO.OFF_B2),
+              "b2": (MO.OFF_B2, MO.OFF_W3), "w3": (MO.OFF_W3, MO.OFF_B3), "b3": (MO.OFF_B3, MO.N_PARAM)}
+    for name, (a, b) in blocks.items():
+        rel = np.linalg.norm(g[a:b] - gref[a:b]) / (np.linalg.norm(gref[a:b]) + 1e-30)
+        assert rel <= GRAD_REL, "%s gradient: relative error %g" % (name, rel)
+
+
+def test_gradient_of_many_tiles_per_cta(cuda_lib, torch_cuda):
+    """More tiles than SMs: each CTA accumulates several tiles in tensor memory before its single flush."""
+    torch = torch_cuda
+    n = 128 * 700
+    feat, label, _ = learned.make_dataset(torch, n, seed=14, n_sub=4)
+    p = _params(6)
+    loss, g = learned.loss_grad(torch, torch.from_numpy(p).cuda(), feat, label)
+    lref, gref = MO.loss_grad(p, feat.cpu().numpy().T, label.cpu().numpy().astype(np.float64))
+    assert abs(loss - lref) <= 1e-4 * (1 + lref)
+    assert np.linalg.norm(g - gref) / np.linalg.norm(gref) <= GRAD_REL
+
+
+def test_adam_step_matches_oracle(cuda_lib, torch_cuda):
+    torch = torch_cuda
+    rng = np.random.default_rng(2)
+    p = _params(7)
+    g = rng.normal(0, 1e-2, MO.N_PARAM + 1).astype(np.float32)
+    m = rng.normal(0, 1e-3, MO.N_PARAM).astype(np.float32)
+    v = np.abs(rng.normal(0, 1e-4, MO.N_PARAM)).astype(np.float32)
+    pd, gd, md, vd = (torch.from_numpy(x.copy()).cuda() for x in (p, g, m, v))
+    learned.adam(torch, pd, gd, md, vd, 3, 1e-3)
+    pr, mr, vr = MO.adam_step(p, g[:-1], m, v, 3, 1e-3)
+    np.testing.assert_allclose(pd.cpu().numpy(), pr, rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(md.cpu().numpy(), mr, rtol=1e-6, atol=1e-9)
+
+
+def test_training_lowers_the_error(cuda_lib, torch_cuda):
+    torch = torch_cuda
+    feat, label, _ = learned.make_dataset(torch, 1 << 17, seed=21, n_sub=8)
+    tf, tl, _ = learned.make_dataset(torch, 1 << 14, seed=22, n_sub=8)
+    p = torch.from_numpy(learned.init_params(1)).cuda()
+    before = (learned.forward(torch, p, tf) - tl).abs().mean().item()
+    losses = learned.train(torch, p, feat, label, epochs=4, batch=8192, lr=3e-3, warmup_steps=20)
+    after = (learned.forward(torch, p, tf) - tl).abs().mean().item()
+    assert np.all(np.isfinite(losses)) and losses[-1] < losses[0]
+    assert after < 0.5 * before and after < 0.05, (before, after, losses)

@@ -91,6 +91,21 @@ def test_shape_zoo(cuda_lib, torch_cuda, twod, method):
     check_interact(w, r)
 
 
+@pytest.mark.parametrize("cfg", ["poly3d_256", "sedimentation2d", "zoo3", "zoo2"])
+def test_mixed_precision_forcing(cuda_lib, torch_cuda, cfg):
+    """exact_forcing = 0: FP64 only for the rigid-body velocity and U - us, FP32 after; same contract."""
+    if cfg == "poly3d_256":
+        w = workloads.poly3d_256(scale=0.25)
+    elif cfg == "sedimentation2d":
+        w = workloads.sedimentation2d(scale=0.25)
+    else:
+        w = _zoo(cfg == "zoo2", 13)
+    w.opt.exact_forcing = 0
+    w.opt.fraction_method = abi.FRACTION_SUBSAMPLE
+    r = run_pair(torch_cuda, w)
+    check_interact(w, r)
+
+
 def test_sparse_reset_and_repeat(cuda_lib, torch_cuda):
     """Three interacts with motion in between: the sparse reset leaves exactly the fields a dense reset gives."""
     w = workloads.sedimentation2d(scale=0.125, ncircles=12)
