@@ -115,8 +115,9 @@ def make_workload(args):
     return w
 
 
-def make_cloud(w, method, subsample_n=None):
-    """A coupling context of workload w with the given fraction method (the learned model loaded if needed)."""
+def make_cloud(w, method, subsample_n=None, stream=None, timing=False):
+    """A coupling context of workload w with the given fraction method (the learned model loaded if needed).
+    With a stream the context replays CUDA graphs of its steps; with timing it records per-kernel events instead."""
     import copy
 
     from sdfibm_gb300 import abi, learned
@@ -125,34 +126,39 @@ def make_cloud(w, method, subsample_n=None):
     opt.fraction_method = METHODS[method]
     if subsample_n:
         opt.subsample_n = subsample_n
-    opt.timing = 1
-    cloud = SolidCloud(w.mesh, w.solids, opt)
+    opt.timing = 1 if timing else 0
+    opt.graphs = 0 if timing else 1
+    cloud = SolidCloud(w.mesh, w.solids, opt, stream=stream)
     if method == "learned":
         params, tt, tg, _ = learned.load_model()
         cloud.set_fraction_model(params, tt, tg)
     return cloud
 
 
-def time_steps(torch, cloud, w, U, f, steps, warmup, flush):
-    """warmup + steps interacts; device time per step (CUDA events around each step, L2 flushed before it)."""
-    for i in range(warmup):
-        cloud.interact(i * w.dt, w.dt, U, f, want_ft=False)
-    torch.cuda.synchronize()
-    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
-    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
-    cells, bbox, kt, launches, st = [], [], {}, 0, {}
-    for i in range(steps):
-        flush.fill_(float(i))
-        ev0[i].record()
-        cloud.interact((warmup + i) * w.dt, w.dt, U, f, want_ft=False)
-        ev1[i].record()
-        st = cloud.stats()  # synchronises
-        cells.append(st["coupling_cells"])
-        bbox.append(st["bbox_cells"])
-        launches += st["launches"]
-        for k, v in cloud.kernel_times().items():
-            kt.setdefault(k, []).append(v)
-    torch.cuda.synchronize()
+def time_steps(torch, cloud, w, U, f, steps, warmup, flush, stream=None, kernel_times=False):
+    """warmup + steps interacts on `stream`; device time per step (CUDA events on that stream around each step, L2
+    flushed before it by a 256 MB write on the same stream)."""
+    stream = stream or torch.cuda.current_stream()
+    with torch.cuda.stream(stream):
+        for i in range(warmup):
+            cloud.interact(i * w.dt, w.dt, U, f, want_ft=False)
+        stream.synchronize()
+        ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        cells, bbox, kt, launches, st = [], [], {}, 0, {}
+        for i in range(steps):
+            flush.fill_(float(i))
+            ev0[i].record(stream)
+            cloud.interact((warmup + i) * w.dt, w.dt, U, f, want_ft=False)
+            ev1[i].record(stream)
+            st = cloud.stats()  # synchronises
+            cells.append(st["coupling_cells"])
+            bbox.append(st["bbox_cells"])
+            launches += st["launches"]
+            if kernel_times:
+                for k, v in cloud.kernel_times().items():
+                    kt.setdefault(k, []).append(v)
+        stream.synchronize()
     ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
     return dict(ms_step=sum(ms) / len(ms), cells=sum(cells) / len(cells), bbox=sum(bbox) / len(bbox),
                 launches=launches, kernel_ms={k: sum(v) / len(v) for k, v in kt.items()}, stats=st)
@@ -186,51 +192,78 @@ def accuracy(torch, w, cloud, U):
             "force_rel_err_max": float(rel.max())}
 
 
-def cpu_baseline(w, max_solids, max_seconds=25.0):
-    """The oracle (faithful data structures, single thread) on a bounded sample of the workload's solids."""
-    import numpy as np
+class CpuReference:
+    """The oracle with the reference's data structures and its REF-GEO fraction (the reference's own algorithm for
+    this path) on a bounded sample of the workload's solids, the solid loop spread over all host threads (solid i
+    on thread i % threads)."""
 
-    from oracle.oracle import OracleCloud
-    S = len(w.solids)
-    rng = np.random.default_rng(123)
-    take = sorted(rng.choice(S, size=min(S, max_solids), replace=False).tolist())
-    sample = []
-    for new_id, s in enumerate(take):
-        d = type(w.solids[s]).from_buffer_copy(w.solids[s])
-        d.id = new_id
-        sample.append(d)
-    U = w.U_numpy().astype(np.float64).reshape(-1)
-    oc = OracleCloud(w.mesh, sample, w.opt, faithful=True)
-    f = oc.new_fields()
-    t0 = time.perf_counter()
-    oc.interact(0.0, w.dt, U, f)
-    wall = time.perf_counter() - t0
-    loop = oc.last_seconds()
-    cells = sum(len(oc.touched(i)[0]) for i in range(len(sample)))
-    return {"value": cells / loop if loop > 0 else None, "unit": "cells/s", "cores": 1, "kind": "port",
-            "sample": "%d of %d solids (random, seed 123) on the full %dx%dx%d mesh, one interact with the "
-                      "reference's data structures (per-solid O(N) cell-type array, std::set, unordered_map "
-                      "phi cache, full-mesh nearest-cell search); timed span = solid loop + checkAlpha as "
-                      "solidcloud.cpp:443-451; %d coupling cells, %.2f s (interact wall %.2f s)"
-                      % (len(sample), S, w.mesh.nx, w.mesh.ny, w.mesh.nz, cells, loop, wall)}
+    def __init__(self, w, solids_per_thread, threads=None):
+        import copy
+
+        import numpy as np
+
+        from oracle.oracle import OracleCloud
+        self.w = w
+        self.threads = threads or os.cpu_count() or 1
+        S = len(w.solids)
+        rng = np.random.default_rng(123)
+        take = sorted(rng.choice(S, size=min(S, solids_per_thread * self.threads), replace=False).tolist())
+        sample = []
+        for new_id, s in enumerate(take):
+            d = type(w.solids[s]).from_buffer_copy(w.solids[s])
+            d.id = new_id
+            sample.append(d)
+        self.nsample, self.S = len(sample), S
+        opt = copy.copy(w.opt)
+        opt.fraction_method = 0  # REF-GEO
+        self.U = w.U_numpy().astype(np.float64).reshape(-1)
+        self.oc = OracleCloud(w.mesh, sample, opt, faithful=True)
+        self.f = self.oc.new_fields()
+
+    def step(self):
+        """One interact; returns (coupling cells, seconds of the timed span, wall seconds)."""
+        t0 = time.perf_counter()
+        self.oc.interact_threads(self.w.dt, self.U, self.f, self.threads)
+        wall = time.perf_counter() - t0
+        cells = sum(len(self.oc.touched(i)[0]) for i in range(self.nsample))
+        return cells, self.oc.last_seconds(), wall
+
+    def describe(self, value, cells, loop, wall):
+        w = self.w
+        return {"value": value, "unit": "cells/s", "cores": self.threads, "kind": "port",
+                "sample": "%d of %d solids (random, seed 123) on the full %dx%dx%d mesh, interact with the "
+                          "reference's data structures (per-solid O(N) cell-type array, std::set, unordered_map "
+                          "phi cache, full-mesh nearest-cell search) and its REF-GEO fraction, solids spread over "
+                          "%d threads; timed span = solid loop + checkAlpha as solidcloud.cpp:443-451; %d coupling "
+                          "cells per step, %.2f s (interact wall %.2f s)"
+                          % (self.nsample, self.S, w.mesh.nx, w.mesh.ny, w.mesh.nz, self.threads, cells, loop, wall)}
+
+
+def cpu_baseline(w, solids_per_thread, threads=None):
+    ref = CpuReference(w, solids_per_thread, threads)
+    cells, loop, wall = ref.step()
+    return ref.describe(cells / loop if loop > 0 else None, cells, loop, wall)
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
     w = make_workload(args)
+    ref = CpuReference(w, args.cpu_solids)
     vals = []
-    info = None
+    last = None
     for i in range(args.warmup + args.steps):
-        info = cpu_baseline(w, args.cpu_solids)
+        cells, loop, wall = ref.step()
+        last = (cells, loop, wall)
         if i >= args.warmup:
-            vals.append(info["value"])
+            vals.append(cells / loop)
     v = sum(vals) / len(vals)
     line = {"impl": "reference", "metric": "IBM coupling cells/s", "value": v, "unit": "cells/s", "n_gpus": 0,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": w.name, "n_cells": w.ncells, "n_solids": len(w.solids), "fraction_method": args.method},
-            "cpu_baseline": dict(info, value=v),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": last[1] * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w.name, "n_cells": w.ncells, "n_solids": len(w.solids),
+                       "fraction_method": "refgeo (the reference's apex/pyramid fraction)"},
+            "cpu_baseline": ref.describe(v, *last),
             "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -245,7 +278,7 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--method", default="learned", choices=sorted(METHODS))
     ap.add_argument("--no-compare", action="store_true", help="skip the plain SUBSAMPLE timing and the accuracy step")
-    ap.add_argument("--cpu-solids", type=int, default=6)
+    ap.add_argument("--cpu-solids", type=int, default=2, help="solids per host thread in the CPU timing sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--exact-forcing", action="store_true",
@@ -271,23 +304,34 @@ def main():
 
     w = make_workload(args)
     U = w.U_torch()
-    cloud = make_cloud(w, args.method)
-    f = cloud.new_fields()
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+    stream = torch.cuda.Stream()
+    cloud = make_cloud(w, args.method, stream=stream)
+    with torch.cuda.stream(stream):
+        f = cloud.new_fields()
+        flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+    torch.cuda.synchronize()
 
     def step(t):
         return cloud.interact(t, w.dt, U, f, want_ft=False)
 
-    for i in range(args.warmup):
-        step(i * w.dt)
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            step(i * w.dt)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    tm = time_steps(torch, cloud, w, U, f, args.steps, 0, flush)
+    tm = time_steps(torch, cloud, w, U, f, args.steps, 0, flush, stream=stream)
     clk = clocks.stop()
+    # per-kernel device times from a second context that records events around every launch (no graphs)
+    ct = make_cloud(w, args.method, timing=True)
+    ft_ = ct.new_fields()
+    tk = time_steps(torch, ct, w, U, ft_, min(args.steps, 3), 2, flush, kernel_times=True)
+    ct.close()
+    del ft_
+    tm["kernel_ms"] = tk["kernel_ms"]
     ms_step = tm["ms_step"]
     if dist:
         tt = torch.tensor([ms_step], device="cuda")
@@ -301,11 +345,17 @@ def main():
 
     compare = None
     if args.method == "learned" and not args.no_compare:
-        plain = make_cloud(w, "subsample", subsample_n=10)
-        fp = plain.new_fields()
-        tp = time_steps(torch, plain, w, U, fp, args.steps, args.warmup, flush)
+        plain = make_cloud(w, "subsample", subsample_n=10, stream=stream)
+        with torch.cuda.stream(stream):
+            fp = plain.new_fields()
+        tp = time_steps(torch, plain, w, U, fp, args.steps, args.warmup, flush, stream=stream)
         plain.close()
         del fp
+        pt = make_cloud(w, "subsample", subsample_n=10, timing=True)
+        fpt = pt.new_fields()
+        tp["kernel_ms"] = time_steps(torch, pt, w, U, fpt, min(args.steps, 3), 2, flush, kernel_times=True)["kernel_ms"]
+        pt.close()
+        del fpt
         acc = accuracy(torch, w, cloud, U)
         st = tm["stats"]
         compare = {"plain": {"method": "SUBSAMPLE 10^3 samples per cut cell", "ms_per_step": tp["ms_step"],
@@ -315,15 +365,22 @@ def main():
                    "learned_cells": st.get("learned_cells"), "fallback_cells": st.get("learned_fallback_cells"),
                    "accuracy": acc}
 
-    # full time step (interact + evolve + fixInternal), device time
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    step(0.0)
-    cloud.evolve(0.0, w.dt)
-    cloud.fix_internal(f["Ct"], U)
-    e1.record()
-    torch.cuda.synchronize()
-    full_ms = e0.elapsed_time(e1)
+    # full time step (interact + evolve with its sub-steps and collisions + fixInternal), device time, graphs
+    with torch.cuda.stream(stream):
+        for i in range(2):
+            step(i * w.dt)
+            cloud.evolve(i * w.dt, w.dt)
+            cloud.fix_internal(f["Ct"], U)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        step(2 * w.dt)
+        e1.record(stream)
+        cloud.evolve(2 * w.dt, w.dt)
+        cloud.fix_internal(f["Ct"], U)
+        e2.record(stream)
+        stream.synchronize()
+    full_ms = e0.elapsed_time(e2)
+    evolve_ms = e1.elapsed_time(e2)
 
     # roofline of the dominant kernel
     peaks, peaks_kind = load_peaks()
@@ -382,6 +439,7 @@ def main():
                            "n_cells": w.ncells, "n_solids": len(w.solids), "coupling_cells": mean_cells,
                            "bbox_cells": sum(bbox) / len(bbox), "fraction_method": args.method,
                            "l2": "flushed (256 MB write) before every timed step", "full_step_ms": full_ms,
+                           "evolve_fix_ms": evolve_ms, "cuda_graphs": True,
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
                 "gpu_launches": launches, "learned_vs_plain": compare}

@@ -146,11 +146,14 @@ typedef struct sdfibm_options {
                                 the caller leaves those fields alone between calls) */
     int32_t exact_forcing;   /* 1: forcing and torque per cell in FP64 exactly as solidcloud.cpp:384-417 (default);
                                 0: FP32 forcing with FP64 force/torque sums */
-    int32_t tile_cells;      /* 0: autotuned.  Cells per (solid, cell-tile) work item otherwise */
+    int32_t tile_cells;      /* cells per (solid, cell-tile) work item of the classify queue; 0: 8 tiles (512 cells
+                                in 3-D), or what sdfibm_cuda_autotune chose */
     int32_t timing;          /* 1: record CUDA events around every kernel (sdfibm_cuda_kernel_times) */
     int32_t learned_fallback_n; /* LEARNED: samples per axis of the SUBSAMPLE evaluation of the cells outside the
                                    network's confidence band (0: 16, the lattice the network was trained on) */
-    int32_t reserved[5];
+    int32_t graphs;          /* 1: capture interact and evolve as CUDA graphs on the first call and replay them
+                                (needs a non-NULL stream; ignored while timing is on) */
+    int32_t reserved[4];
 } sdfibm_options;
 
 typedef struct sdfibm_ctx sdfibm_ctx;
@@ -212,6 +215,13 @@ int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc* mesh, const sdfibm_solid
  * [2] bbox cells scanned, [3] vertices re-checked in FP64, [4] work items, [5] kernel launches,
  * [6] cut cells given to the learned fraction model, [7] of those, cells outside its band (SUBSAMPLE fallback). */
 int sdfibm_cuda_stats(sdfibm_ctx* ctx, int64_t* out, int32_t n);
+
+/* No counterpart in the reference.  Autotuner of the classify work queue: times a few dense interacts (on the given
+ * device fields, which it overwrites) with each candidate work-item size (2, 4, 8, 16 or 32 tiles of one solid per
+ * item) and keeps the fastest; results do not depend on the choice.  *chosen_tiles (host, may be NULL) receives it
+ * and options.tile_cells reports it in cells.  Captured graphs are re-captured on their next use.  Synchronises. */
+int sdfibm_cuda_autotune(sdfibm_ctx* ctx, double dt, const float* U, float* As, float* Fs, float* Ts, int32_t* Ct,
+                         int32_t* chosen_tiles);
 
 /* No counterpart in the reference (which has only the apex/pyramid fraction).  Installs the learned cut-cell
  * fraction model used when options.fraction_method is SDFIBM_FRACTION_LEARNED: params is a HOST array of

@@ -4,4 +4,4 @@
 set -e
 cd "$(dirname "$0")"
 ${CXX:-g++} -std=c++17 -O2 -ffp-contract=off -fno-fast-math -fPIC -shared -Wall -Wno-unused-function \
-    -o liboracle.so oracle.cpp
+    -o liboracle.so oracle.cpp -pthread

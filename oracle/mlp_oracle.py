@@ -8,7 +8,10 @@ trainer can be compared term by term:
 * features of a cut cell (11): the signed distance at its 8 vertices divided by the cell size, in the vertex
   order of OpenFOAM's cellPoints for a hex, (i,j,k) (i+1,j,k) (i,j+1,k) (i+1,j+1,k), then the same at k+1; then
   the trilinear gradient of those 8 values at the cell centre, normalised to unit length;
-* network 11 -> 64 -> 64 -> 1 with SiLU hidden activations and a sigmoid output;
+* network 11 -> 64 -> 64 -> 1 with SiLU hidden activations; the predicted fraction is
+  sigmoid(logit(clamp(P, 1e-4, 1 - 1e-4)) + g * o) with o the network output, P the exact solid fraction of the cell
+  under the plane fitted to its vertex distances (Scardovelli & Zaleski, J. Comput. Phys. 164 (2000), cube-plane
+  volume) and g = tw / (1 + tw), tw the sum of the six face twists of the vertex distances;
 * numerics of the GPU kernels: the two hidden layers are BF16 x BF16 tensor-core products with FP32
   accumulation, W1 and W2 are rounded to BF16, and the features and the first hidden activations are carried
   as a hi + lo pair of BF16 values (so they keep ~16 significant bits); biases, the 64 -> 1 output layer and
@@ -117,6 +120,57 @@ def band_scores(feat):
     return tw, np.abs(np.sqrt(gx * gx + gy * gy + gz * gz) - 1.0)
 
 
+PRIOR_CLAMP = 1e-4
+
+
+def plane_fraction(X):
+    """Exact solid fraction under the plane fitted to the vertex distances (FP64, vectorised)."""
+    f = np.asarray(X, np.float64)[:, :8]
+    n = np.stack([0.25 * (((f[:, 1] - f[:, 0]) + (f[:, 3] - f[:, 2])) + ((f[:, 5] - f[:, 4]) + (f[:, 7] - f[:, 6]))),
+                  0.25 * (((f[:, 2] - f[:, 0]) + (f[:, 3] - f[:, 1])) + ((f[:, 6] - f[:, 4]) + (f[:, 7] - f[:, 5]))),
+                  0.25 * (((f[:, 4] - f[:, 0]) + (f[:, 5] - f[:, 1])) + ((f[:, 6] - f[:, 2]) + (f[:, 7] - f[:, 3])))],
+                 1)
+    d = 0.5 * n.sum(1) - f.mean(1)
+    d = d - np.minimum(n, 0).sum(1)
+    m = np.abs(n)
+    s = m.sum(1)
+    out = np.where(d > 0, 1.0, 0.0)
+    ok = s > 0
+    with np.errstate(divide="ignore", invalid="ignore"):
+        a = np.where(ok, d / np.where(ok, s, 1.0), 0.0)
+        ms = np.sort(m / np.where(ok, s, 1.0)[:, None], 1)
+        flip = a > 0.5
+        al = np.where(flip, 1 - a, a)
+        m1, m2, m3 = ms[:, 0], ms[:, 1], ms[:, 2]
+        m12 = m1 + m2
+        r1 = al ** 3 / (6 * m1 * m2 * m3)
+        r2 = al * (al - m1) / (2 * m2 * m3) + m1 * m1 / (6 * m2 * m3)
+        r3 = (al * al * (3 * m12 - al) + m1 * m1 * (m1 - 3 * al) + m2 * m2 * (m2 - 3 * al)) / (6 * m1 * m2 * m3)
+        r4 = (al * al * (3 - 2 * al) + m1 * m1 * (m1 - 3 * al) + m2 * m2 * (m2 - 3 * al) +
+              m3 * m3 * (m3 - 3 * al)) / (6 * m1 * m2 * m3)
+        r5 = (2 * al - m12) / (2 * m3)
+        v = np.where(al < m1, r1, np.where(al < m2, r2, np.where(al < np.minimum(m3, m12), r3,
+                                                                  np.where(m3 < m12, r4, r5))))
+        v = np.clip(v, 0.0, 1.0)
+        v = np.where(flip, 1 - v, v)
+    v = np.where(a <= 0, 0.0, np.where(a >= 1, 1.0, v))
+    return np.where(ok, v, out)
+
+
+def face_twist(X):
+    f = np.asarray(X, np.float64)[:, :8]
+    return (np.abs(f[:, 0] - f[:, 1] - f[:, 2] + f[:, 3]) + np.abs(f[:, 4] - f[:, 5] - f[:, 6] + f[:, 7]) +
+            np.abs(f[:, 0] - f[:, 1] - f[:, 4] + f[:, 5]) + np.abs(f[:, 2] - f[:, 3] - f[:, 6] + f[:, 7]) +
+            np.abs(f[:, 0] - f[:, 2] - f[:, 4] + f[:, 6]) + np.abs(f[:, 1] - f[:, 3] - f[:, 5] + f[:, 7]))
+
+
+def prior(X):
+    """(logit of the clamped planar fraction, gate) of every cell."""
+    v = np.clip(plane_fraction(X), PRIOR_CLAMP, 1 - PRIOR_CLAMP)
+    tw = face_twist(X)
+    return np.log(v / (1 - v)), tw / (1 + tw)
+
+
 def forward(p, X, return_all=False, exact=False):
     """Predicted fraction of each cell.  X: [n, 11] float32.  FP64 accumulation of the FP32-exact products.
 
@@ -128,9 +182,10 @@ def forward(p, X, return_all=False, exact=False):
         z2 = h1 @ W2.T + b2
         h2 = silu(z2)
         o = h2 @ w3 + b3
-        a = sigmoid(o)
+        pl, g = prior(X)
+        a = sigmoid(pl + g * o)
         if return_all:
-            return dict(z1=z1, h1=h1, z2=z2, h2=h2, o=o, a=a)
+            return dict(z1=z1, h1=h1, z2=z2, h2=h2, o=o, a=a, gate=g)
         return a
     W1b = bf16(W1).astype(np.float64)
     W2b = bf16(W2).astype(np.float64)
@@ -142,9 +197,10 @@ def forward(p, X, return_all=False, exact=False):
     z2 = z2.astype(np.float32)
     h2 = silu(z2).astype(np.float32)
     o = h2.astype(np.float64) @ w3.astype(np.float64) + b3
-    a = sigmoid(o)
+    pl, g = prior(X)
+    a = sigmoid(pl + g * o)
     if return_all:
-        return dict(z1=z1.astype(np.float32), h1=h1, z2=z2, h2=h2, o=o, a=a)
+        return dict(z1=z1.astype(np.float32), h1=h1, z2=z2, h2=h2, o=o, a=a, gate=g)
     return a
 
 
@@ -164,7 +220,7 @@ def loss_grad(p, X, y, exact=False):
         r = forward(p, X, return_all=True, exact=True)
         a = r["a"]
         d = a - y
-        dz3 = (2.0 / n) * d * a * (1.0 - a)
+        dz3 = (2.0 / n) * d * a * (1.0 - a) * r["gate"]
         dZ2 = dz3[:, None] * w3[None, :] * dsilu(r["z2"])
         dZ1 = (dZ2 @ W2) * dsilu(r["z1"])
         g = np.concatenate([(dZ1.T @ np.asarray(X, np.float64)).ravel(), dZ1.sum(0), (dZ2.T @ r["h1"]).ravel(),
@@ -176,7 +232,7 @@ def loss_grad(p, X, y, exact=False):
     a = r["a"]
     d = a - y
     loss = float(np.mean(d * d))
-    dz3 = (2.0 / n) * d * a * (1.0 - a)                                   # [n]
+    dz3 = (2.0 / n) * d * a * (1.0 - a) * r["gate"]                       # [n]
     dw3 = r["h2"].astype(np.float64).T @ dz3
     db3 = dz3.sum()
     dZ2 = (dz3[:, None] * w3[None, :].astype(np.float64) * dsilu(r["z2"].astype(np.float64))).astype(np.float32)

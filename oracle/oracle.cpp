@@ -30,6 +30,7 @@
 #include <queue>
 #include <set>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -124,6 +125,8 @@ struct CloudBase {
     virtual ~CloudBase() = default;
     virtual int interact(double time, double dt, const double* U, double* As, double* Fs, double* Ts, int32_t* Ct,
                          double* FT) = 0;
+    virtual int interactThreads(double dt, const double* U, double* As, double* Fs, double* Ts, int32_t* Ct,
+                                double* FT, int nthreads) = 0;
     virtual int64_t touched(int s, int64_t* cells, int8_t* types, int64_t cap) const = 0;
     virtual int fixInternal(const int32_t* Ct, double* U) const = 0;
     virtual int64_t nCells() const = 0;
@@ -528,9 +531,21 @@ struct Cloud : CloudBase {
         return geo.cellVolume(c, s, twod != 0) / vol(c);
     }
 
-    // SolidCloud::solidFluidInteract (solidcloud.cpp:361-433)
+    // FP64 += that is safe when several threads add to one cell (the threaded timing variant)
+    static void atomicAdd(double* a, double v) {
+        uint64_t old = __atomic_load_n(reinterpret_cast<uint64_t*>(a), __ATOMIC_RELAXED), nw;
+        do {
+            double cur;
+            std::memcpy(&cur, &old, 8);
+            cur += v;
+            std::memcpy(&nw, &cur, 8);
+        } while (!__atomic_compare_exchange_n(reinterpret_cast<uint64_t*>(a), &old, nw, true, __ATOMIC_RELAXED,
+                                              __ATOMIC_RELAXED));
+    }
+
+    // SolidCloud::solidFluidInteract (solidcloud.cpp:361-433); shared = the fields are updated by several threads
     void solidFluidInteract(int si, double dt, const double* U, double* As, double* Fs, double* Ts, int32_t* Ct,
-                            int64_t N) {
+                            int64_t N, bool shared = false) {
         Solid& s = solids[si];
         std::vector<int64_t> ins, cin, cout;
         enumerate(s, ins, cin, cout);
@@ -561,7 +576,7 @@ struct Cloud : CloudBase {
                 if (opt.fraction_method == SDFIBM_FRACTION_SUBSAMPLE) alpha = subsampleFraction(c, s);
                 else alpha = geo.cellVolume(c, s, twod != 0) / vol(c);
             }
-            As[c] += alpha;
+            if (shared) atomicAdd(As + c, alpha); else As[c] += alpha;
             V3 cc = centre(c);
             V3 uf{U[c], U[N + c], U[2 * N + c]};
             V3 us = s.evalPointVelocity(cc);
@@ -571,8 +586,13 @@ struct Cloud : CloudBase {
             force += f_ * cv * dtINV;
             torque += t_ * cv * dtINV;
             V3 fs = f_ * dtINV;
-            Fs[c] += fs.x; Fs[N + c] += fs.y; Fs[2 * N + c] += fs.z;
-            Ts[c] += alpha;
+            if (shared) {
+                atomicAdd(Fs + c, fs.x); atomicAdd(Fs + N + c, fs.y); atomicAdd(Fs + 2 * N + c, fs.z);
+                atomicAdd(Ts + c, alpha);
+            } else {
+                Fs[c] += fs.x; Fs[N + c] += fs.y; Fs[2 * N + c] += fs.z;
+                Ts[c] += alpha;
+            }
         }
         force *= opt.rho_f;
         torque *= opt.rho_f;
@@ -599,6 +619,35 @@ struct Cloud : CloudBase {
         } else {
             for (auto& v : touched_cells) for (int64_t c : v) As[c] = std::min(As[c], 1.0);
         }
+        auto t2 = std::chrono::steady_clock::now();
+        last_seconds = std::chrono::duration<double>(t2 - t1).count();
+        if (FT) {
+            for (size_t si = 0; si < solids.size(); ++si) {
+                put3(FT + 6 * si, solids[si].fluid_force);
+                put3(FT + 6 * si + 3, solids[si].fluid_torque);
+            }
+        }
+        return 0;
+    }
+
+    // The same interact with the solids spread over nthreads host threads (solid si on thread si % nthreads), for
+    // the CPU timing on all cores: as many independent solid loops as the reference would run on that many
+    // single-solid-loop ranks.  Cells shared by several solids are summed atomically; Ct keeps the last writer.
+    int interactThreads(double dt, const double* U, double* As, double* Fs, double* Ts, int32_t* Ct, double* FT,
+                        int nthreads) override {
+        const int64_t N = mesh.nCells();
+        std::fill(As, As + N, 0.0); std::fill(Fs, Fs + 3 * N, 0.0);
+        std::fill(Ts, Ts + N, 0.0); std::fill(Ct, Ct + N, 0);
+        auto t1 = std::chrono::steady_clock::now();
+        const int T = std::max(1, nthreads);
+        std::vector<std::thread> pool;
+        for (int t = 0; t < T; ++t)
+            pool.emplace_back([&, t] {
+                for (size_t si = (size_t)t; si < solids.size(); si += (size_t)T)
+                    solidFluidInteract((int)si, dt, U, As, Fs, Ts, Ct, N, true);
+            });
+        for (auto& th : pool) th.join();
+        for (int64_t c = 0; c < N; ++c) As[c] = std::min(As[c], 1.0);
         auto t2 = std::chrono::steady_clock::now();
         last_seconds = std::chrono::duration<double>(t2 - t1).count();
         if (FT) {
@@ -842,6 +891,10 @@ int oracle_interact(void* h, double time, double dt, const double* U, double* As
     try { return static_cast<CloudBase*>(h)->interact(time, dt, U, As, Fs, Ts, Ct, FT); } catch (...) { return 1; }
 }
 double oracle_last_seconds(void* h) { return static_cast<CloudBase*>(h)->last_seconds; }
+int oracle_interact_threads(void* h, double dt, const double* U, double* As, double* Fs, double* Ts, int32_t* Ct,
+                            double* FT, int nthreads) {
+    return static_cast<CloudBase*>(h)->interactThreads(dt, U, As, Fs, Ts, Ct, FT, nthreads);
+}
 int64_t oracle_last_pairs(void* h) { return static_cast<CloudBase*>(h)->last_pairs; }
 
 int64_t oracle_touched(void* h, int s, int64_t* cells, int8_t* types, int64_t cap) {

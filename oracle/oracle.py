@@ -60,6 +60,7 @@ def lib():
         L.oracle_phi01.argtypes = [C.POINTER(abi.SolidDesc), vp]
         L.oracle_phi.restype = C.c_double
         L.oracle_phi.argtypes = [C.POINTER(abi.SolidDesc), vp]
+        L.oracle_interact_threads.argtypes = [vp, C.c_double] + [vp] * 6 + [C.c_int]
         L.oracle_sample_cell.restype = C.c_int64
         L.oracle_sample_cell.argtypes = [C.POINTER(abi.ShapeDesc), vp, vp, C.c_double, C.c_int, vp]
         _lib = L
@@ -138,6 +139,16 @@ class OracleCloud:
         FT = np.zeros(6 * self.nsolids)
         rc = lib().oracle_interact(self.h, time, dt, _p(U), _p(fields["As"]), _p(fields["Fs"]), _p(fields["Ts"]),
                                    _p(fields["Ct"]), _p(FT))
+        if rc != 0:
+            raise RuntimeError("oracle interact failed")
+        return FT.reshape(self.nsolids, 6)
+
+    def interact_threads(self, dt, U, fields, nthreads):
+        """interact with the solids spread over nthreads host threads (CPU timing on all cores)."""
+        U = np.ascontiguousarray(U, dtype=np.float64).reshape(-1)
+        FT = np.zeros(6 * self.nsolids)
+        rc = lib().oracle_interact_threads(self.h, dt, _p(U), _p(fields["As"]), _p(fields["Fs"]), _p(fields["Ts"]),
+                                           _p(fields["Ct"]), _p(FT), int(nthreads))
         if rc != 0:
             raise RuntimeError("oracle interact failed")
         return FT.reshape(self.nsolids, 6)

@@ -17,7 +17,7 @@ CUDA_SYMBOLS = [
     "sdfibm_cuda_evolve", "sdfibm_cuda_fix_internal", "sdfibm_cuda_get_solids", "sdfibm_cuda_set_solids",
     "sdfibm_cuda_touched", "sdfibm_cuda_stats", "sdfibm_cuda_kernel_times", "sdfibm_cuda_last_error",
     "sdfibm_cuda_version",
-    "sdfibm_cuda_destroy", "sdfibm_cuda_touched_noalloc", "sdfibm_cuda_set_fraction_model",
+    "sdfibm_cuda_destroy", "sdfibm_cuda_touched_noalloc", "sdfibm_cuda_set_fraction_model", "sdfibm_cuda_autotune",
 ]
 MLP_SYMBOLS = [
     "sdfibm_mlp_dataset", "sdfibm_mlp_forward", "sdfibm_mlp_loss_grad", "sdfibm_mlp_adam", "sdfibm_mlp_train",
@@ -53,6 +53,7 @@ def load():
     L.sdfibm_cuda_touched.argtypes = [vp, i32, vp, vp, i64, P(i64)]
     L.sdfibm_cuda_stats.argtypes = [vp, P(i64), i32]
     L.sdfibm_cuda_set_fraction_model.argtypes = [vp, vp, C.c_float, C.c_float]
+    L.sdfibm_cuda_autotune.argtypes = [vp, dbl, vp, vp, vp, vp, vp, P(i32)]
     L.sdfibm_cuda_kernel_times.argtypes = [vp, P(C.c_char_p), P(dbl), i32, P(i32)]
     L.sdfibm_cuda_touched_noalloc.argtypes = [P(abi.MeshDesc), P(abi.SolidDesc), vp, vp, vp, i64, vp]
     L.sdfibm_cuda_last_error.argtypes = [vp]

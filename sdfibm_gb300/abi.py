@@ -58,7 +58,8 @@ class Options(C.Structure):
     _fields_ = [("rho_f", C.c_double), ("gravity", C.c_double * 3), ("collision_mode", C.c_int32),
                 ("n_subiter", C.c_int32), ("fraction_method", C.c_int32), ("subsample_n", C.c_int32),
                 ("dense_reset", C.c_int32), ("exact_forcing", C.c_int32), ("tile_cells", C.c_int32),
-                ("timing", C.c_int32), ("learned_fallback_n", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("timing", C.c_int32), ("learned_fallback_n", C.c_int32), ("graphs", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 class MlpDataDesc(C.Structure):

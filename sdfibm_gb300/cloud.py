@@ -126,6 +126,13 @@ class SolidCloud:
                 "learned_cells", "learned_fallback_cells")
         return dict(zip(keys, list(out)))
 
+    def autotune(self, dt, U, fields):
+        """Chooses the classify work-item size by timing dense interacts on these fields; returns tiles per item."""
+        out = C.c_int32(0)
+        self._check(self._L.sdfibm_cuda_autotune(self._h, float(dt), _ptr(U), _ptr(fields["As"]), _ptr(fields["Fs"]),
+                                                 _ptr(fields["Ts"]), _ptr(fields["Ct"]), C.byref(out)))
+        return out.value
+
     def set_fraction_model(self, params, tau_twist, tau_grad):
         """Installs the learned cut-cell fraction model (options.fraction_method = FRACTION_LEARNED)."""
         p = np.ascontiguousarray(params, dtype=np.float32)

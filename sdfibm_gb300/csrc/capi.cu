@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -30,22 +31,28 @@ __global__ void finalize_kernel(float* As, float* Ts, float* Fs, int32_t* Ct, co
 __global__ void begin_kernel(Counters* cnt);
 __global__ void claim_kernel(const int32_t* in_cell, const int32_t* in_solid, const int32_t* cut_cell,
                              const int32_t* cut_solid, int32_t* Ct, const Counters* cnt, int64_t N);
-__global__ void ft_kernel(const double* ftacc, double* ft, int S, double scale);
+__global__ void ft_kernel(const double* ftacc, double* ft, int S, const StepParams* step);
+__global__ void set_step_kernel(StepParams* p, double time, double dt, int nsub, double rho_V);
 __global__ void reset_kernel(const int32_t* in_cell, const int32_t* cut_cell, const Counters* cnt, int64_t N,
                              float* As, float* Fs, float* Ts, int32_t* Ct);
 __global__ void fix_internal_kernel(MeshK m, const sdfibm_solid_state* st, const int32_t* in_cell,
                                     const int32_t* in_solid, const int32_t* Ct, float* U, const Counters* cnt);
 // evolve.cu
 
-__global__ void evolve_independent_kernel(const SolidK* sk, sdfibm_solid_state* st, int S, int nsub, double time,
-                                          double dt_sub, double rho_f, D3 g);
-__global__ void evolve_pre_kernel(const SolidK* sk, sdfibm_solid_state* st, int S, double time, double rho_f, D3 g,
-                                  GridK gk, int64_t* hashes, int32_t* counts);
+__global__ void evolve_independent_kernel(const SolidK* sk, sdfibm_solid_state* st, int S, int nsub,
+                                          const StepParams* step, double rho_f, D3 g);
+__global__ void evolve_pre_kernel(const SolidK* sk, sdfibm_solid_state* st, int S, const StepParams* step, double rho_f, D3 g,
+                                  GridK gk, int64_t* hashes, int32_t* counts, FineGridK fg, int32_t* fcounts, int mode,
+                                  int coarse_needed);
+__global__ void fine_scatter_kernel(const SolidK* sk, const sdfibm_solid_state* st, int S, GridK gk,
+                                    const int64_t* hashes, FineGridK fg, int32_t* fcursor, int32_t* flist, int mode,
+                                    Counters* cnt);
 __global__ void grid_scan_kernel(const int32_t* counts, int32_t* start, int32_t* cursor, int64_t ncell);
 __global__ void grid_scatter_kernel(const int64_t* hashes, int32_t* cursor, int32_t* list, int S, int64_t ncell);
 __global__ void collide_kernel(const SolidK* sk, sdfibm_solid_state* st, int S, GridK gk, const int64_t* hashes,
-                               const int32_t* start, const int32_t* list, int mode);
-__global__ void move_kernel(const SolidK* sk, sdfibm_solid_state* st, int S, double time, double dt);
+                               const int32_t* start, const int32_t* list, int mode, FineGridK fg, const int32_t* fstart,
+                               const int32_t* flist, const int32_t* planes, int nplanes);
+__global__ void move_kernel(const SolidK* sk, sdfibm_solid_state* st, int S, const StepParams* step);
 __global__ void store_old_kernel(sdfibm_solid_state* st, int S);
 __global__ void ft_to_state_kernel(const double* ft, sdfibm_solid_state* st, int S);
 }  // namespace sdfibm_dev
@@ -79,6 +86,8 @@ struct sdfibm_ctx {
     SolidPlan* d_plan = nullptr;
     int2* d_chunks = nullptr;  // classify work items: (solid, first tile)
     int total_chunks = 0;
+    int chunk_tiles = CHUNK_TILES;
+    int64_t chunks_cap = 0;    // entries reserved in d_chunks
     int total_tiles = 0;
     uint8_t* d_scratch = nullptr;
     float* d_alpha = nullptr;  // solid fraction per bbox cell (same indexing as d_scratch)
@@ -108,6 +117,10 @@ struct sdfibm_ctx {
     GridK gk{};
     int64_t* d_hash = nullptr;
     int32_t *d_gcount = nullptr, *d_gstart = nullptr, *d_gcursor = nullptr, *d_glist = nullptr;
+    // fine broad phase of the sphere-like solids and the list of plane-like ones (contact law id 0)
+    FineGridK fg{};
+    int32_t *d_fcount = nullptr, *d_fstart = nullptr, *d_fcursor = nullptr, *d_flist = nullptr, *d_planes = nullptr;
+    int nplanes = 0;
     // fields seen by the last interact (sparse reset is only valid on the same buffers)
     const void* last_fields[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     bool interacted = false;
@@ -132,6 +145,21 @@ struct sdfibm_ctx {
     bool ev_ready = false;
     int launches_last = 0;
     std::string err;
+    // time-step parameters on the device ([0] interact, [1] evolve) and the captured graphs
+    StepParams* d_step = nullptr;
+    struct Graph {
+        bool valid = false;
+        cudaGraphExec_t exec = nullptr;
+        cudaGraphNode_t step_node = nullptr;
+        cudaKernelNodeParams step_params{};
+        int cur = -1, dense = -1;
+        const void* fields[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+        int launches = 0;
+    };
+    Graph igraph[4];
+    Graph egraph;
+    bool graphs_failed = false;
+    std::vector<cudaGraph_t> graphs_keep;
 };
 
 // event bracketing of each launch when timing is on: mark(ctx, name) after a launch records its end
@@ -161,6 +189,17 @@ static int fail(sdfibm_ctx* ctx, int code, const std::string& msg) {
         if (e_ != cudaSuccess)                                                                           \
             return fail(ctx, SDFIBM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
     } while (0)
+
+// classify work items: chunks of up to chunk_tiles consecutive tiles of each solid
+static std::vector<int2> make_chunks(const std::vector<SolidK>& hk, int chunk_tiles) {
+    std::vector<int2> chunks;
+    for (size_t s = 0; s < hk.size(); ++s) {
+        const SolidK& k = hk[s];
+        const int nt = k.ntile[0] * k.ntile[1] * k.ntile[2];
+        for (int t0 = 0; t0 < nt; t0 += chunk_tiles) chunks.push_back(make_int2((int)s, t0));
+    }
+    return chunks;
+}
 
 template <class T>
 static cudaError_t dalloc(T** p, size_t n) {
@@ -297,6 +336,7 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
     }
     if (tiles >= ((int64_t)1 << 31)) { ctx->err = "too many bbox tiles"; return bail(SDFIBM_ERR_CAPACITY); }
     ctx->total_tiles = (int)tiles;
+    ctx->chunks_cap = tiles;
     ctx->scratch_bytes = scratch;
     ctx->gbitmap_words = gwords;
     ctx->connect_smem_bytes = max_smem_words * 4;
@@ -310,12 +350,12 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         while (t < 2 * want) t <<= 1;
         ctx->sh_mask = (int32_t)(t - 1);
     }
-    std::vector<int2> chunks;
-    for (int s = 0; s < nsolids; ++s) {
-        const SolidK& k = ctx->hk[s];
-        const int nt = k.ntile[0] * k.ntile[1] * k.ntile[2];
-        for (int t0 = 0; t0 < nt; t0 += CHUNK_TILES) chunks.push_back(make_int2(s, t0));
+    ctx->chunk_tiles = CHUNK_TILES;
+    if (ctx->opt.tile_cells > 0) {
+        const int cells_per_tile = mesh->nz <= 2 ? 8 * 8 * 2 : 4 * 4 * 4;
+        ctx->chunk_tiles = std::max(1, std::min(255, ctx->opt.tile_cells / cells_per_tile));
     }
+    std::vector<int2> chunks = make_chunks(ctx->hk, ctx->chunk_tiles);
     ctx->total_chunks = (int)chunks.size();
 
     // collision grid (UGrid(bbox of the mesh, 2*max radiusB))
@@ -340,20 +380,65 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
                 g.nx = (int)gx; g.ny = (int)gy; g.nz = (int)gz;
                 g.nynz = g.ny * g.nz;
                 g.ncell = (int64_t)g.nx * g.ny * g.nz;
+                // fine grid: about 8 cells per sphere-like solid over the same box
+                std::vector<int32_t> planes;
+                int64_t nsph = 0;
+                for (int s = 0; s < nsolids; ++s) {
+                    const bool infinite = ctx->hk[s].infinite != 0;
+                    const int id = ctx->opt.collision_mode == SDFIBM_COLLISION_SPHERES ? (infinite ? 0 : 2)
+                                                                                      : ctx->hk[s].collision_id;
+                    if (id == 0) planes.push_back(s);
+                    else if (id == 1 || id == 2) ++nsph;
+                }
+                ctx->nplanes = (int)planes.size();
+                FineGridK& f = ctx->fg;
+                const double vol = (hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2]);
+                double c = std::cbrt(vol / (8.0 * (double)std::max<int64_t>(1, nsph)));
+                for (;;) {
+                    int64_t nc = 1;
+                    for (int a = 0; a < 3; ++a) {
+                        f.n[a] = (int32_t)std::max(1.0, std::ceil((hi[a] - lo[a]) / c));
+                        nc *= f.n[a];
+                    }
+                    if (nc <= (1 << 22)) { f.ncell = nc; break; }
+                    c *= 1.25;
+                }
+                for (int a = 0; a < 3; ++a) f.low[a] = lo[a];
+                f.inv = 1.0 / c;
+                int64_t cap = 0;
+                for (int s = 0; s < nsolids; ++s) {
+                    const bool infinite = ctx->hk[s].infinite != 0;
+                    const int id = ctx->opt.collision_mode == SDFIBM_COLLISION_SPHERES ? (infinite ? 0 : 2)
+                                                                                      : ctx->hk[s].collision_id;
+                    if (id != 1 && id != 2) continue;
+                    const double span = 2.0 * std::max(0.0, solids[s].shape.radiusB) * f.inv + 2.0;
+                    int64_t e = 1;
+                    for (int a = 0; a < 3; ++a) e *= std::min<int64_t>(f.n[a], (int64_t)span);
+                    cap += e;
+                }
+                f.cap = std::max<int64_t>(1, cap);
+                if (dalloc(&ctx->d_planes, planes.size()) ||
+                    (planes.size() && cudaMemcpy(ctx->d_planes, planes.data(), sizeof(int32_t) * planes.size(),
+                                                 cudaMemcpyHostToDevice) != cudaSuccess) ||
+                    dalloc(&ctx->d_fcount, f.ncell) || dalloc(&ctx->d_fstart, f.ncell + 1) ||
+                    dalloc(&ctx->d_fcursor, f.ncell) || dalloc(&ctx->d_flist, f.cap)) {
+                    ctx->err = "device allocation failed (fine collision grid)";
+                    return bail(SDFIBM_ERR_CUDA);
+                }
             }
         }
     }
 
     // device allocations
     if (dalloc(&ctx->d_sk, nsolids) || dalloc(&ctx->d_st, nsolids) || dalloc(&ctx->d_plan, nsolids) ||
-        dalloc(&ctx->d_chunks, chunks.size()) || dalloc(&ctx->d_scratch, scratch) || dalloc(&ctx->d_alpha, scratch) ||
+        dalloc(&ctx->d_chunks, (size_t)ctx->total_tiles) || dalloc(&ctx->d_scratch, scratch) || dalloc(&ctx->d_alpha, scratch) ||
         dalloc(&ctx->d_gbitmaps, gwords) || dalloc(&ctx->d_lists[0][0], ctx->cap) || dalloc(&ctx->d_lists[0][1], ctx->cap) ||
         dalloc(&ctx->d_lists[0][2], ctx->cap) || dalloc(&ctx->d_lists[0][3], ctx->cap) ||
         dalloc(&ctx->d_lists[1][0], ctx->cap) || dalloc(&ctx->d_lists[1][1], ctx->cap) ||
         dalloc(&ctx->d_lists[1][2], ctx->cap) || dalloc(&ctx->d_lists[1][3], ctx->cap) || dalloc(&ctx->d_cnt, 1) ||
         dalloc(&ctx->d_ftacc, 6 * (size_t)nsolids) || dalloc(&ctx->d_ft, 6 * (size_t)nsolids) ||
         dalloc(&ctx->d_sh_keys, (size_t)ctx->sh_mask + 1) || dalloc(&ctx->d_sh_vals, 5 * ((size_t)ctx->sh_mask + 1)) ||
-        dalloc(&ctx->d_sh_used, (size_t)ctx->sh_mask + 1) ||
+        dalloc(&ctx->d_sh_used, (size_t)ctx->sh_mask + 1) || dalloc(&ctx->d_step, 2) ||
         cudaMallocHost((void**)&ctx->h_cnt, sizeof(Counters)) != cudaSuccess ||
         cudaMallocHost((void**)&ctx->h_ft, std::max<size_t>(1, 6 * (size_t)nsolids) * sizeof(double)) != cudaSuccess) {
         ctx->err = "device allocation failed";
@@ -426,25 +511,14 @@ static int sync_counters(sdfibm_ctx* ctx) {
     return check_device_error(ctx);
 }
 
-int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs, float* Ts,
-                         int32_t* Ct, double* FT) {
-    (void)time;
-    if (!ctx) return SDFIBM_ERR_ARG;
-    if (!U || !As || !Fs || !Ts || !Ct) return fail(ctx, SDFIBM_ERR_ARG, "null field pointer");
-    if (!(dt != 0.0)) return fail(ctx, SDFIBM_ERR_ARG, "dt must be nonzero");
+// The device work of one interact on the context's stream: what a captured graph holds.
+static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs, float* Ts,
+                            int32_t* Ct, bool dense, int& launches) {
     const int64_t N = ctx->mesh.ncells;
     const int S = ctx->S;
     cudaStream_t st = ctx->stream;
-    int launches = 0;
-    mark_begin(ctx);
-    const void* f5[5] = {U, As, Fs, Ts, Ct};
-    bool same = ctx->interacted;
-    for (int i = 1; i < 5; ++i) same = same && f5[i] == ctx->last_fields[i];
-    const bool dense = !same || ctx->opt.dense_reset;
-    if (ctx->opt.fraction_method == SDFIBM_FRACTION_LEARNED && !ctx->model_set)
-        return fail(ctx, SDFIBM_ERR_STATE, "LEARNED fraction without a model: call sdfibm_cuda_set_fraction_model");
-    for (int i = 0; i < 5; ++i) ctx->last_fields[i] = f5[i];
-    ctx->cur ^= 1;  // this call's lists; the other buffer holds the previous call's touched cells
+    set_step_kernel<<<1, 1, 0, st>>>(ctx->d_step, time, dt, 1, ctx->opt.rho_f * ctx->mesh.V);
+    ++launches;
     begin_kernel<<<1, 1, 0, st>>>(ctx->d_cnt);
     ++launches;
     if (dense) {
@@ -462,6 +536,7 @@ int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U
         ClassifyArgs CA;
         CA.m = ctx->mesh; CA.sk = ctx->d_sk; CA.st = ctx->d_st; CA.plan = ctx->d_plan; CA.chunks = ctx->d_chunks;
         CA.total_chunks = ctx->total_chunks; CA.cls = ctx->d_scratch; CA.alpha = ctx->d_alpha; CA.cnt = ctx->d_cnt;
+        CA.chunk_tiles = ctx->chunk_tiles;
         CA.method = ctx->opt.fraction_method; CA.subsample_n = ctx->opt.subsample_n;
         const bool learned = ctx->opt.fraction_method == SDFIBM_FRACTION_LEARNED;
         if (learned) {
@@ -511,7 +586,7 @@ int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U
         A.m = ctx->mesh; A.sk = ctx->d_sk; A.st = ctx->d_st; A.plan = ctx->d_plan;
         A.in_cell = ctx->in_cell(); A.in_solid = ctx->in_solid(); A.cut_cell = ctx->cut_cell();
         A.cut_solid = ctx->cut_solid(); A.alpha = ctx->d_alpha; A.U = U; A.As = As; A.Fs = Fs; A.Ts = Ts; A.Ct = Ct;
-        A.ftacc = ctx->d_ftacc; A.cnt = ctx->d_cnt; A.dtINV = 1.0 / dt;
+        A.ftacc = ctx->d_ftacc; A.cnt = ctx->d_cnt; A.step = ctx->d_step;
         A.method = ctx->opt.fraction_method; A.subsample_n = ctx->opt.subsample_n;
         A.exact_forcing = ctx->opt.exact_forcing;
         A.sh_keys = ctx->d_sh_keys; A.sh_vals = ctx->d_sh_vals; A.sh_used = ctx->d_sh_used; A.sh_mask = ctx->sh_mask;
@@ -520,18 +595,122 @@ int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U
         finalize_kernel<<<ctx->num_sms, 256, 0, st>>>(As, Ts, Fs, Ct, ctx->d_cnt, N, ctx->d_sh_keys, ctx->d_sh_vals,
                                                        ctx->d_sh_used, ctx->sh_mask);
         mark(ctx, "finalize_kernel");
-        ft_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->d_ftacc, ctx->d_ft, S, ctx->opt.rho_f * ctx->mesh.V / dt);
+        ft_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->d_ftacc, ctx->d_ft, S, ctx->d_step);
         ft_to_state_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->d_ft, ctx->d_st, S);
         mark(ctx, "ft_kernel");
         launches += 4;
     }
     CK(cudaGetLastError());
+    return SDFIBM_OK;
+}
+
+// Runs `enqueue` as a CUDA graph: captured on first use (or when `key_changed`), then replayed after updating the
+// arguments of its set_step_kernel node.  Returns a status, or -1 when capture is not possible (the caller then
+// launches directly).
+static int run_graph(sdfibm_ctx* ctx, sdfibm_ctx::Graph& g, bool key_changed, const std::function<int()>& enqueue,
+                     StepParams* step, double time, double dt, int nsub, double rho_V) {
+    cudaStream_t st = ctx->stream;
+    if (!g.valid || key_changed) {
+        if (g.valid) {
+            cudaGraphExecDestroy(g.exec);
+            g.valid = false;
+        }
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            return -1;
+        }
+        const int rc = enqueue();
+        const cudaError_t e = cudaStreamEndCapture(st, &graph);
+        if (rc != SDFIBM_OK || e != cudaSuccess || !graph) {
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            return -1;
+        }
+        size_t n = 0;
+        cudaGraphGetNodes(graph, nullptr, &n);
+        std::vector<cudaGraphNode_t> nodes(n);
+        cudaGraphGetNodes(graph, nodes.data(), &n);
+        g.step_node = nullptr;
+        for (cudaGraphNode_t nd : nodes) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nd, &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
+            cudaKernelNodeParams kp;
+            if (cudaGraphKernelNodeGetParams(nd, &kp) == cudaSuccess && kp.func == (void*)set_step_kernel) {
+                g.step_node = nd;
+                g.step_params = kp;
+                break;
+            }
+        }
+        if (!g.step_node || cudaGraphInstantiate(&g.exec, graph, 0) != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            cudaGetLastError();
+            return -1;
+        }
+        // the graph is kept alive: its node handle addresses the instantiated copy
+        ctx->graphs_keep.push_back(graph);
+        g.valid = true;
+    }
+    void* args[5] = {&step, &time, &dt, &nsub, &rho_V};
+    cudaKernelNodeParams kp = g.step_params;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    CK(cudaGraphExecKernelNodeSetParams(g.exec, g.step_node, &kp));
+    CK(cudaGraphLaunch(g.exec, st));
+    return SDFIBM_OK;
+}
+
+static bool graphs_on(const sdfibm_ctx* ctx) {
+    return ctx->opt.graphs && ctx->stream != nullptr && !ctx->opt.timing && !ctx->graphs_failed;
+}
+
+int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs, float* Ts,
+                         int32_t* Ct, double* FT) {
+    if (!ctx) return SDFIBM_ERR_ARG;
+    if (!U || !As || !Fs || !Ts || !Ct) return fail(ctx, SDFIBM_ERR_ARG, "null field pointer");
+    if (!(dt != 0.0)) return fail(ctx, SDFIBM_ERR_ARG, "dt must be nonzero");
+    const int S = ctx->S;
+    cudaStream_t st = ctx->stream;
+    int launches = 0;
+    mark_begin(ctx);
+    const void* f5[5] = {U, As, Fs, Ts, Ct};
+    bool same = ctx->interacted;
+    for (int i = 1; i < 5; ++i) same = same && f5[i] == ctx->last_fields[i];
+    const bool dense = !same || ctx->opt.dense_reset;
+    if (ctx->opt.fraction_method == SDFIBM_FRACTION_LEARNED && !ctx->model_set)
+        return fail(ctx, SDFIBM_ERR_STATE, "LEARNED fraction without a model: call sdfibm_cuda_set_fraction_model");
+    for (int i = 0; i < 5; ++i) ctx->last_fields[i] = f5[i];
+    ctx->cur ^= 1;  // this call's lists; the other buffer holds the previous call's touched cells
+    int rc = -1;
+    if (graphs_on(ctx)) {
+        sdfibm_ctx::Graph& g = ctx->igraph[ctx->cur * 2 + (dense ? 1 : 0)];
+        bool changed = g.cur != ctx->cur || g.dense != (int)dense;
+        for (int i = 0; i < 5; ++i) changed = changed || g.fields[i] != f5[i];
+        int counted = 0;
+        rc = run_graph(ctx, g, changed,
+                       [&] {
+                           counted = 0;
+                           return enqueue_interact(ctx, time, dt, U, As, Fs, Ts, Ct, dense, counted);
+                       },
+                       ctx->d_step, time, dt, 1, ctx->opt.rho_f * ctx->mesh.V);
+        if (rc == -1) {
+            ctx->graphs_failed = true;
+        } else {
+            g.cur = ctx->cur;
+            g.dense = (int)dense;
+            for (int i = 0; i < 5; ++i) g.fields[i] = f5[i];
+            if (counted) g.launches = counted;
+            launches = g.launches;
+        }
+    }
+    if (rc == -1) rc = enqueue_interact(ctx, time, dt, U, As, Fs, Ts, Ct, dense, launches);
+    if (rc) return rc;
     ctx->launches_last = launches;
     ctx->interacted = true;
     if (FT) {
         if (S > 0) CK(cudaMemcpyAsync(ctx->h_ft, ctx->d_ft, sizeof(double) * 6 * S, cudaMemcpyDeviceToHost, st));
-        int rc = sync_counters(ctx);
-        if (rc) return rc;
+        const int rs = sync_counters(ctx);
+        if (rs) return rs;
         std::memcpy(FT, ctx->h_ft, sizeof(double) * 6 * S);
     }
     return SDFIBM_OK;
@@ -563,33 +742,54 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
     return SDFIBM_OK;
 }
 
-int sdfibm_cuda_evolve(sdfibm_ctx* ctx, double time, double dt) {
-    if (!ctx) return SDFIBM_ERR_ARG;
+// The device work of one evolve (all sub-steps) on the context's stream: what a captured graph holds.
+static int enqueue_evolve(sdfibm_ctx* ctx, double time, double dt) {
     const int S = ctx->S;
-    if (S == 0) return SDFIBM_OK;
     cudaStream_t st = ctx->stream;
     const int nsub = ctx->nsub;
-    const double dt_sub = dt / nsub;
+    StepParams* step = ctx->d_step + 1;
     const D3 g{ctx->opt.gravity[0], ctx->opt.gravity[1], ctx->opt.gravity[2]};
     const int B = 128, G = (S + B - 1) / B;
+    set_step_kernel<<<1, 1, 0, st>>>(step, time, dt, nsub, 0.0);
     if (!ctx->grid_active) {
-        evolve_independent_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, nsub, time, dt_sub, ctx->opt.rho_f, g);
+        evolve_independent_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, nsub, step, ctx->opt.rho_f, g);
     } else {
         const GridK& gk = ctx->gk;
+        const FineGridK& fg = ctx->fg;
+        const int mode = ctx->opt.collision_mode;
+        const int coarse = ctx->nplanes > 0;  // the coarse lists serve only the plane-like solids
         for (int it = 0; it < nsub; ++it) {
-            CK(cudaMemsetAsync(ctx->d_gcount, 0, sizeof(int32_t) * gk.ncell, st));
-            evolve_pre_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, time, ctx->opt.rho_f, g, gk, ctx->d_hash,
-                                               ctx->d_gcount);
-            grid_scan_kernel<<<1, 1024, 0, st>>>(ctx->d_gcount, ctx->d_gstart, ctx->d_gcursor, gk.ncell);
-            grid_scatter_kernel<<<G, B, 0, st>>>(ctx->d_hash, ctx->d_gcursor, ctx->d_glist, S, gk.ncell);
-            collide_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, gk, ctx->d_hash, ctx->d_gstart, ctx->d_glist,
-                                            ctx->opt.collision_mode);
-            move_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, time, dt_sub);
+            if (coarse) CK(cudaMemsetAsync(ctx->d_gcount, 0, sizeof(int32_t) * gk.ncell, st));
+            CK(cudaMemsetAsync(ctx->d_fcount, 0, sizeof(int32_t) * fg.ncell, st));
+            evolve_pre_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, step, ctx->opt.rho_f, g, gk, ctx->d_hash,
+                                               ctx->d_gcount, fg, ctx->d_fcount, mode, coarse);
+            if (coarse) {
+                grid_scan_kernel<<<1, 1024, 0, st>>>(ctx->d_gcount, ctx->d_gstart, ctx->d_gcursor, gk.ncell);
+                grid_scatter_kernel<<<G, B, 0, st>>>(ctx->d_hash, ctx->d_gcursor, ctx->d_glist, S, gk.ncell);
+            }
+            grid_scan_kernel<<<1, 1024, 0, st>>>(ctx->d_fcount, ctx->d_fstart, ctx->d_fcursor, fg.ncell);
+            fine_scatter_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, gk, ctx->d_hash, fg, ctx->d_fcursor,
+                                                 ctx->d_flist, mode, ctx->d_cnt);
+            collide_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, gk, ctx->d_hash, ctx->d_gstart, ctx->d_glist, mode,
+                                            fg, ctx->d_fstart, ctx->d_flist, ctx->d_planes, ctx->nplanes);
+            move_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, step);
         }
         store_old_kernel<<<G, B, 0, st>>>(ctx->d_st, S);
     }
     CK(cudaGetLastError());
     return SDFIBM_OK;
+}
+
+int sdfibm_cuda_evolve(sdfibm_ctx* ctx, double time, double dt) {
+    if (!ctx) return SDFIBM_ERR_ARG;
+    if (ctx->S == 0) return SDFIBM_OK;
+    if (graphs_on(ctx)) {
+        const int rc = run_graph(ctx, ctx->egraph, false, [&] { return enqueue_evolve(ctx, time, dt); },
+                                 ctx->d_step + 1, time, dt, ctx->nsub, 0.0);
+        if (rc != -1) return rc;
+        ctx->graphs_failed = true;
+    }
+    return enqueue_evolve(ctx, time, dt);
 }
 
 int sdfibm_cuda_fix_internal(sdfibm_ctx* ctx, const int32_t* Ct, float* U) {
@@ -671,6 +871,60 @@ int sdfibm_cuda_kernel_times(sdfibm_ctx* ctx, const char** names, double* ms, in
     return SDFIBM_OK;
 }
 
+int sdfibm_cuda_autotune(sdfibm_ctx* ctx, double dt, const float* U, float* As, float* Fs, float* Ts, int32_t* Ct,
+                         int32_t* chosen_tiles) {
+    if (!ctx) return SDFIBM_ERR_ARG;
+    if (!U || !As || !Fs || !Ts || !Ct) return fail(ctx, SDFIBM_ERR_ARG, "null field pointer");
+    if (ctx->S == 0) return SDFIBM_OK;
+    if (ctx->opt.fraction_method == SDFIBM_FRACTION_LEARNED && !ctx->model_set)
+        return fail(ctx, SDFIBM_ERR_STATE, "LEARNED fraction without a model: call sdfibm_cuda_set_fraction_model");
+    static const int cand[] = {2, 4, 8, 16, 32};
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const int saved_timing = ctx->opt.timing;
+    ctx->opt.timing = 0;
+    int best = ctx->chunk_tiles;
+    float best_ms = 1e30f;
+    int rc = SDFIBM_OK;
+    for (int ci = 0; ci < (int)(sizeof(cand) / sizeof(cand[0])) && rc == SDFIBM_OK; ++ci) {
+        std::vector<int2> ch = make_chunks(ctx->hk, cand[ci]);
+        if ((int64_t)ch.size() > ctx->chunks_cap) continue;
+        if (cudaMemcpy(ctx->d_chunks, ch.data(), sizeof(int2) * ch.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+            rc = fail(ctx, SDFIBM_ERR_CUDA, "chunk table upload failed");
+            break;
+        }
+        ctx->chunk_tiles = cand[ci];
+        ctx->total_chunks = (int)ch.size();
+        float ms = 1e30f;
+        for (int rep = 0; rep < 3 && rc == SDFIBM_OK; ++rep) {
+            cudaEventRecord(e0, ctx->stream);
+            int launches = 0;
+            rc = enqueue_interact(ctx, 0.0, dt, U, As, Fs, Ts, Ct, true, launches);
+            cudaEventRecord(e1, ctx->stream);
+            if (cudaEventSynchronize(e1) != cudaSuccess) rc = fail(ctx, SDFIBM_ERR_CUDA, "autotune timing failed");
+            float t = 0.f;
+            cudaEventElapsedTime(&t, e0, e1);
+            if (rep > 0) ms = std::min(ms, t);  // the first run of each size is a warm-up
+        }
+        if (ms < best_ms) { best_ms = ms; best = cand[ci]; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->opt.timing = saved_timing;
+    if (rc != SDFIBM_OK) return rc;
+    std::vector<int2> ch = make_chunks(ctx->hk, best);
+    CK(cudaMemcpy(ctx->d_chunks, ch.data(), sizeof(int2) * ch.size(), cudaMemcpyHostToDevice));
+    ctx->chunk_tiles = best;
+    ctx->total_chunks = (int)ch.size();
+    ctx->opt.tile_cells = best * (ctx->mesh.nz <= 2 ? 8 * 8 * 2 : 4 * 4 * 4);
+    for (auto& g : ctx->igraph) g.cur = -1;  // captured graphs hold the old table size: recapture on next use
+    // the fields hold a complete dense interact of the current state; the next call starts from the same buffers
+    ctx->interacted = false;
+    if (chosen_tiles) *chosen_tiles = best;
+    return sync_counters(ctx);
+}
+
 int sdfibm_cuda_set_fraction_model(sdfibm_ctx* ctx, const float* params, float tau_twist, float tau_grad) {
     if (!ctx) return SDFIBM_ERR_ARG;
     if (!params) return fail(ctx, SDFIBM_ERR_ARG, "null model parameters");
@@ -685,6 +939,7 @@ int sdfibm_cuda_set_fraction_model(sdfibm_ctx* ctx, const float* params, float t
             dalloc(&ctx->d_fb, ctx->feat_cap))
             return fail(ctx, SDFIBM_ERR_CUDA, "allocation of the learned-fraction buffers failed");
     }
+    mlp_prepare();
     CK(cudaMemcpyAsync(ctx->d_mlp, params, sizeof(float) * SDFIBM_MLP_NPARAM, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->tau_twist = tau_twist;
@@ -713,9 +968,15 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
                    ctx->d_lists[1][0], ctx->d_lists[1][1], ctx->d_lists[1][2], ctx->d_lists[1][3], ctx->d_cnt, ctx->d_ftacc,
                    ctx->d_ft, ctx->d_hash, ctx->d_gcount, ctx->d_gstart, ctx->d_gcursor, ctx->d_glist, ctx->d_U,
                    ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, ctx->d_alpha, ctx->d_sh_keys, ctx->d_sh_vals, ctx->d_sh_used,
-                   ctx->d_mlp, ctx->d_feat, ctx->d_fref_solid, ctx->d_fref_index, ctx->d_fb};
+                   ctx->d_mlp, ctx->d_feat, ctx->d_fref_solid, ctx->d_fref_index, ctx->d_fb, ctx->d_fcount,
+                   ctx->d_fstart, ctx->d_fcursor, ctx->d_flist, ctx->d_planes};
     for (void* p : dev)
         if (p) cudaFree(p);
+    if (ctx->d_step) cudaFree(ctx->d_step);
+    for (auto& g : ctx->igraph)
+        if (g.valid) cudaGraphExecDestroy(g.exec);
+    if (ctx->egraph.valid) cudaGraphExecDestroy(ctx->egraph.exec);
+    for (cudaGraph_t gr : ctx->graphs_keep) cudaGraphDestroy(gr);
     if (ctx->ev_ready)
         for (int i = 0; i <= sdfibm_ctx::MAXEV; ++i) cudaEventDestroy(ctx->ev[i]);
     if (ctx->h_cnt) cudaFreeHost(ctx->h_cnt);

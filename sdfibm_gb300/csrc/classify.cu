@@ -354,7 +354,40 @@ __device__ inline float filter_mixed(const ShapeK& s, float phi, bool* exact_nee
     return a < 1e-8f ? -1e-8f : phi;
 }
 
-// ---- the tile kernel: one warp per chunk of up to CHUNK_TILES tiles of one solid ------------------------------------------
+// LEARNED: the features of the tile's cut cells (one warp), appended to the network's input buffer with the index of
+// the cell's fraction; out of line to keep the tile loop small.  tile0 = fraction index of the tile's cell (0,0,0).
+template <int TX, int TY, int TZ>
+static __device__ __noinline__ void write_features(const ClassifyArgs& A, const uint8_t* cutlist, int ncut,
+                                                   const float* vphi, int s, int64_t tile0, int ext0, int ext1) {
+    constexpr int VX = TX + 1, VY = TY + 1;
+    const int lane = threadIdx.x & 31;
+    for (int u0 = 0; u0 < ncut; u0 += 32) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&A.cnt->n_feat, min(32, ncut - u0));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const int u = u0 + lane;
+        if (u < ncut) {
+            const int e = cutlist[u];
+            const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
+            const int v0 = a + VX * (b + VY * c);
+            const float ph[8] = {vphi[v0], vphi[v0 + 1], vphi[v0 + VX], vphi[v0 + VX + 1], vphi[v0 + VX * VY],
+                                 vphi[v0 + VX * VY + 1], vphi[v0 + VX * VY + VX], vphi[v0 + VX * VY + VX + 1]};
+            float fe[MLP_IN];
+            cell_features(ph, A.inv_h, fe);
+            const int64_t slot = (int64_t)base + lane;
+            if (slot < A.feat_cap) {
+#pragma unroll
+                for (int q = 0; q < MLP_IN; ++q) A.feat[q * A.feat_cap + slot] = fe[q];
+                A.fref_solid[slot] = s;
+                A.fref_index[slot] = tile0 + a + (int64_t)ext0 * (b + (int64_t)ext1 * c);
+            } else {
+                set_error(A.cnt, DERR_CAPACITY);
+            }
+        }
+    }
+}
+
+// ---- the tile kernel: one warp per chunk of up to chunk_tiles tiles of one solid ------------------------------------------
 constexpr int CLS_WARPS = 8;
 
 template <int TX, int TY, int TZ>
@@ -383,7 +416,7 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
         const SolidK& k = A.sk[s];
         const SolidPlan& pl = A.plan[s];
         const int ntile_all = k.ntile[0] * k.ntile[1] * k.ntile[2];
-        const int t_end = min(ch.y + CHUNK_TILES, ntile_all);
+        const int t_end = min(ch.y + A.chunk_tiles, ntile_all);
         const Q4 q = state_quat(A.st[s]);
         const D3 x = state_pos(A.st[s]);
         const ShapeK& sh = k.shape;
@@ -512,31 +545,8 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                 __syncwarp();
                 if (A.method == SDFIBM_FRACTION_LEARNED) {
                     // features of every cut cell into the network's input buffer; the fraction comes later
-                    for (int u0 = 0; u0 < ncut; u0 += 32) {
-                        int base = 0;
-                        if (lane == 0) base = atomicAdd(&A.cnt->n_feat, min(32, ncut - u0));
-                        base = __shfl_sync(FULL, base, 0);
-                        const int u = u0 + lane;
-                        if (u < ncut) {
-                            const int e = cutlist[u];
-                            const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
-                            const int v0 = a + VX * (b + VY * c);
-                            const float ph[8] = {vphi[v0], vphi[v0 + 1], vphi[v0 + VX], vphi[v0 + VX + 1],
-                                                 vphi[v0 + VX * VY], vphi[v0 + VX * VY + 1],
-                                                 vphi[v0 + VX * VY + VX], vphi[v0 + VX * VY + VX + 1]};
-                            float fe[MLP_IN];
-                            cell_features(ph, A.inv_h, fe);
-                            const int64_t slot = (int64_t)base + lane;
-                            if (slot < A.feat_cap) {
-#pragma unroll
-                                for (int q2 = 0; q2 < MLP_IN; ++q2) A.feat[q2 * A.feat_cap + slot] = fe[q2];
-                                A.fref_solid[slot] = s;
-                                A.fref_index[slot] = k.scratch_off + local_index(a, b, c);
-                            } else {
-                                set_error(A.cnt, DERR_CAPACITY);
-                            }
-                        }
-                    }
+                    write_features<TX, TY, TZ>(A, cutlist, ncut, vphi, s,
+                                               k.scratch_off + local_index(0, 0, 0), k.ext[0], k.ext[1]);
                     __syncwarp();
                     continue;
                 }

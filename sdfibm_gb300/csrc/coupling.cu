@@ -469,7 +469,8 @@ __global__ void __launch_bounds__(CPL_THREADS) couple_kernel(CoupleArgs A) {
     const int n_in = clamp_len(A.cnt->n_inside, A.cnt->list_cap), n_cut = clamp_len(A.cnt->n_cut, A.cnt->list_cap);
     const int in_chunks = (n_in + CPL_THREADS - 1) / CPL_THREADS;
     const int cut_chunks = (n_cut + CPL_THREADS - 1) / CPL_THREADS;
-    const float dtINV32 = (float)A.dtINV;
+    const double dtINV = A.step->dtINV;
+    const float dtINV32 = (float)dtINV;
     for (;;) {
         if (tid == 0) s_item = atomicAdd(&A.cnt->couple_next, 1);
         __syncthreads();
@@ -512,7 +513,7 @@ __global__ void __launch_bounds__(CPL_THREADS) couple_kernel(CoupleArgs A) {
                 const D3 f_ = (double)alpha * (uf - us);
                 const D3 t_ = cross(cc - x, f_);
                 f6[0] = f_.x; f6[1] = f_.y; f6[2] = f_.z; f6[3] = t_.x; f6[4] = t_.y; f6[5] = t_.z;
-                fsx = (float)(f_.x * A.dtINV); fsy = (float)(f_.y * A.dtINV); fsz = (float)(f_.z * A.dtINV);
+                fsx = (float)(f_.x * dtINV); fsy = (float)(f_.y * dtINV); fsz = (float)(f_.z * dtINV);
             } else {
                 // FP64 for the rigid-body velocity and U - us (the difference can cancel), FP32 after it.  C - x is
                 // the solid's FP64 seed offset plus a whole number of cells.
@@ -605,10 +606,19 @@ __global__ void begin_kernel(Counters* cnt) {
 }
 
 // F = rho_f * V / dt * sum f, T = rho_f * V / dt * sum (C - x) x f  (solidcloud.cpp:411-421)
-__global__ void ft_kernel(const double* __restrict__ ftacc, double* __restrict__ ft, int S, double scale) {
+__global__ void ft_kernel(const double* __restrict__ ftacc, double* __restrict__ ft, int S, const StepParams* step) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= S) return;
+    const double scale = step->ft_scale;
     for (int r = 0; r < 6; ++r) ft[6 * s + r] = ftacc[6 * s + r] * scale;
+}
+
+__global__ void set_step_kernel(StepParams* p, double time, double dt, int nsub, double rho_V) {
+    p->time = time;
+    p->dt = dt;
+    p->dt_sub = dt / nsub;
+    p->dtINV = 1.0 / dt;
+    p->ft_scale = rho_V / dt;
 }
 
 // sparse reset: the cells the previous call touched and this call does not (after this call's claims, before the

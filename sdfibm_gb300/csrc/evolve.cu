@@ -10,7 +10,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-#include "kernels.cuh"
+#include "common.cuh"
 
 namespace sdfibm_dev {
 
@@ -150,9 +150,10 @@ __device__ inline void store_old(sdfibm_solid_state& s) {
 
 // all sub-steps of one solid (no solid-solid interaction)
 __global__ void evolve_independent_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state* st, int S, int nsub,
-                                          double time, double dt_sub, double rho_f, D3 g) {
+                                          const StepParams* step, double rho_f, D3 g) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= S) return;
+    const double time = step->time, dt_sub = step->dt_sub;
     const SolidK& k = sk[s];
     sdfibm_solid_state x = st[s];
     for (int it = 0; it < nsub; ++it) {
@@ -172,16 +173,67 @@ __device__ inline int64_t grid_hash(const GridK& gk, const D3& c) {
     return (int64_t)i * gk.nynz + (int64_t)j * gk.nz + k;
 }
 
-// forces of one sub-step and the UGrid insert (UGrid::insert, ugrid.h:31-34)
-__global__ void evolve_pre_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state* st, int S, double time,
-                                  double rho_f, D3 g, GridK gk, int64_t* __restrict__ hashes,
-                                  int32_t* __restrict__ counts) {
+// collision id of the pair-law table: SPHERES mode treats every non-plane solid as its bounding sphere
+__device__ inline int coll_id(const SolidK& k, int mode) {
+    return mode == SDFIBM_COLLISION_SPHERES ? (k.infinite ? 0 : 2) : k.collision_id;
+}
+
+// fine-grid cell range of a bounding box, clamped to the grid
+__device__ inline void fine_range(const FineGridK& fg, const D3& c, double r, int lo[3], int hi[3]) {
+    const double cc[3] = {c.x, c.y, c.z};
+    for (int a = 0; a < 3; ++a) {
+        const double l = floor((cc[a] - r - fg.low[a]) * fg.inv), h = floor((cc[a] + r - fg.low[a]) * fg.inv);
+        lo[a] = (int)fmin(fmax(l, 0.0), (double)(fg.n[a] - 1));
+        hi[a] = (int)fmin(fmax(h, 0.0), (double)(fg.n[a] - 1));
+    }
+}
+__device__ inline int64_t fine_index(const FineGridK& fg, int i, int j, int k) {
+    return (int64_t)i + (int64_t)fg.n[0] * ((int64_t)j + (int64_t)fg.n[1] * k);
+}
+
+// forces of one sub-step, the UGrid key of every solid (UGrid::insert, ugrid.h:31-34) with the coarse counts (only
+// needed by plane-like solids, which search their 27 coarse neighbours), and the fine-grid counts of the sphere-like
+// solids whose key is on the grid (the reference never pairs the others)
+__global__ void evolve_pre_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state* st, int S,
+                                  const StepParams* step, double rho_f, D3 g, GridK gk, int64_t* __restrict__ hashes,
+                                  int32_t* __restrict__ counts, FineGridK fg, int32_t* __restrict__ fcounts, int mode,
+                                  int coarse_needed) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= S) return;
-    pre_forces(sk[s], st[s], time, rho_f, g);
-    const int64_t h = grid_hash(gk, ld3(st[s].pos));
+    pre_forces(sk[s], st[s], step->time, rho_f, g);
+    const D3 c = ld3(st[s].pos);
+    const int64_t h = grid_hash(gk, c);
     hashes[s] = h;
-    if (h >= 0 && h < gk.ncell) atomicAdd(counts + h, 1);
+    if (h < 0 || h >= gk.ncell) return;
+    if (coarse_needed) atomicAdd(counts + h, 1);
+    const int id = coll_id(sk[s], mode);
+    if (id != 1 && id != 2) return;
+    int lo[3], hi[3];
+    fine_range(fg, c, sk[s].radiusB, lo, hi);
+    for (int k = lo[2]; k <= hi[2]; ++k)
+        for (int j = lo[1]; j <= hi[1]; ++j)
+            for (int i = lo[0]; i <= hi[0]; ++i) atomicAdd(fcounts + fine_index(fg, i, j, k), 1);
+}
+
+__global__ void fine_scatter_kernel(const SolidK* __restrict__ sk, const sdfibm_solid_state* __restrict__ st, int S,
+                                    GridK gk, const int64_t* __restrict__ hashes, FineGridK fg,
+                                    int32_t* __restrict__ fcursor, int32_t* __restrict__ flist, int mode,
+                                    Counters* cnt) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const int64_t h = hashes[s];
+    if (h < 0 || h >= gk.ncell) return;
+    const int id = coll_id(sk[s], mode);
+    if (id != 1 && id != 2) return;
+    int lo[3], hi[3];
+    fine_range(fg, ld3(st[s].pos), sk[s].radiusB, lo, hi);
+    for (int k = lo[2]; k <= hi[2]; ++k)
+        for (int j = lo[1]; j <= hi[1]; ++j)
+            for (int i = lo[0]; i <= hi[0]; ++i) {
+                const int32_t e = atomicAdd(fcursor + fine_index(fg, i, j, k), 1);
+                if (e < fg.cap) flist[e] = s;
+                else set_error(cnt, DERR_CAPACITY);
+            }
 }
 
 // exclusive scan of the per-cell counts (single block)
@@ -258,35 +310,81 @@ __device__ inline bool pair_force(const SolidK& k1, const sdfibm_solid_state& s1
     return true;
 }
 
+// the 27 coarse cells around key a contain key b (the neighbour loops of ugrid.cpp:50-77)
+__device__ inline bool coarse_neighbours(const GridK& gk, int64_t a, int64_t b) {
+    const int64_t ai = a / gk.nynz, aj = (a / gk.nz) % gk.ny, ak = a % gk.nz;
+    const int64_t bi = b / gk.nynz, bj = (b / gk.nz) % gk.ny, bk = b % gk.nz;
+    return llabs(ai - bi) <= 1 && llabs(aj - bj) <= 1 && llabs(ak - bk) <= 1;
+}
+
+// Pair forces of one sub-step, each solid summing its own side of every pair the reference's UGrid would form
+// (27 coarse neighbours of its key, keys on the grid) that has a contact law and overlaps.  Sphere-like pairs come
+// from the fine grid: a pair is taken in the one fine cell holding the corner max(lo_p, lo_q) of the two bounding
+// boxes' intersection, then kept only when the coarse keys are neighbours, so the contacts are exactly the
+// reference's.  Plane-like solids (law id 0) search the coarse grid; sphere-like solids test the plane list.
 __global__ void collide_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state* st, int S, GridK gk,
                                const int64_t* __restrict__ hashes, const int32_t* __restrict__ start,
-                               const int32_t* __restrict__ list, int mode) {
+                               const int32_t* __restrict__ list, int mode, FineGridK fg,
+                               const int32_t* __restrict__ fstart, const int32_t* __restrict__ flist,
+                               const int32_t* __restrict__ planes, int nplanes) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= S) return;
     const int64_t h = hashes[p];
     if (h < 0 || h >= gk.ncell) return;
-    const int ci = (int)(h / gk.nynz), cj = (int)((h / gk.nz) % gk.ny), ck = (int)(h % gk.nz);
     const SolidK& kp = sk[p];
-    const int idp = (mode == SDFIBM_COLLISION_SPHERES) ? (kp.infinite ? 0 : 2) : kp.collision_id;
+    const int idp = coll_id(kp, mode);
     D3 fsum{0, 0, 0};
-    const sdfibm_solid_state sp = st[p];
-    for (int a = ci - 1; a <= ci + 1; ++a) {
-        if (a < 0 || a > gk.nx - 1) continue;
-        for (int b = cj - 1; b <= cj + 1; ++b) {
-            if (b < 0 || b > gk.ny - 1) continue;
-            for (int c = ck - 1; c <= ck + 1; ++c) {
-                if (c < 0 || c > gk.nz - 1) continue;
-                const int64_t nb = (int64_t)a * gk.nynz + (int64_t)b * gk.nz + c;
-                for (int e = start[nb]; e < start[nb + 1]; ++e) {
-                    const int q = list[e];
-                    if (q == p) continue;
-                    const SolidK& kq = sk[q];
-                    const int idq = (mode == SDFIBM_COLLISION_SPHERES) ? (kq.infinite ? 0 : 2) : kq.collision_id;
-                    D3 f;
-                    if (p < q) {
-                        if (pair_force(kp, sp, idp, kq, st[q], idq, f)) fsum = fsum + (-f);
-                    } else {
-                        if (pair_force(kq, st[q], idq, kp, sp, idp, f)) fsum = fsum + f;
+    const sdfibm_solid_state& sp = st[p];
+    auto add_pair = [&](int q, int idq) {
+        D3 f;
+        if (p < q) {
+            if (pair_force(kp, sp, idp, sk[q], st[q], idq, f)) fsum = fsum + (-f);
+        } else {
+            if (pair_force(sk[q], st[q], idq, kp, sp, idp, f)) fsum = fsum + f;
+        }
+    };
+    if (idp == 1 || idp == 2) {
+        int lo[3], hi[3];
+        fine_range(fg, ld3(sp.pos), kp.radiusB, lo, hi);
+        for (int k = lo[2]; k <= hi[2]; ++k)
+            for (int j = lo[1]; j <= hi[1]; ++j)
+                for (int i = lo[0]; i <= hi[0]; ++i) {
+                    const int64_t cell = fine_index(fg, i, j, k);
+                    for (int e = fstart[cell]; e < fstart[cell + 1]; ++e) {
+                        const int q = flist[e];
+                        if (q == p) continue;
+                        const SolidK& kq = sk[q];
+                        if (coll_id(kq, mode) != idp) continue;  // (1,1) and (2,2) have a law, (1,2) has none
+                        // the pair's home cell: the corner max(lo_p, lo_q) of the two cell ranges' intersection
+                        // (both solids compute it from the same indices, so exactly one of p's and one of q's
+                        // visits holds the pair)
+                        int ql[3], qh[3];
+                        fine_range(fg, ld3(st[q].pos), kq.radiusB, ql, qh);
+                        if (max(lo[0], ql[0]) != i || max(lo[1], ql[1]) != j || max(lo[2], ql[2]) != k) continue;
+                        if (i > qh[0] || j > qh[1] || k > qh[2]) continue;  // ranges do not intersect
+                        const int64_t hq = hashes[q];
+                        if (!coarse_neighbours(gk, h, hq)) continue;
+                        add_pair(q, idp);
+                    }
+                }
+        for (int e = 0; e < nplanes; ++e) {
+            const int q = planes[e];
+            const int64_t hq = hashes[q];
+            if (hq < 0 || hq >= gk.ncell || !coarse_neighbours(gk, h, hq)) continue;
+            add_pair(q, 0);
+        }
+    } else {
+        const int ci = (int)(h / gk.nynz), cj = (int)((h / gk.nz) % gk.ny), ck = (int)(h % gk.nz);
+        for (int a = ci - 1; a <= ci + 1; ++a) {
+            if (a < 0 || a > gk.nx - 1) continue;
+            for (int b = cj - 1; b <= cj + 1; ++b) {
+                if (b < 0 || b > gk.ny - 1) continue;
+                for (int c = ck - 1; c <= ck + 1; ++c) {
+                    if (c < 0 || c > gk.nz - 1) continue;
+                    const int64_t nb = (int64_t)a * gk.nynz + (int64_t)b * gk.nz + c;
+                    for (int e = start[nb]; e < start[nb + 1]; ++e) {
+                        const int q = list[e];
+                        if (q != p) add_pair(q, coll_id(sk[q], mode));
                     }
                 }
             }
@@ -298,10 +396,10 @@ __global__ void collide_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state
     st[p].force[2] += fsum.z;
 }
 
-__global__ void move_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state* st, int S, double time, double dt) {
+__global__ void move_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state* st, int S, const StepParams* step) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= S) return;
-    move_solid(sk[s], st[s], time, dt);
+    move_solid(sk[s], st[s], step->time, step->dt_sub);
 }
 
 __global__ void store_old_kernel(sdfibm_solid_state* st, int S) {

@@ -108,6 +108,16 @@ struct Counters {
 // list lengths clamped to the capacity (a capacity error leaves the counters above what was written)
 __host__ __device__ inline int32_t clamp_len(int32_t n, int64_t cap) { return (int32_t)(n < cap ? n : cap); }
 
+// Time-step parameters the kernels read from device memory; set_step_kernel writes them at the head of a call, so a
+// captured graph replays with new values after one kernel-node update.
+struct StepParams {
+    double time;
+    double dt;
+    double dt_sub;    // evolve: dt / sub-steps
+    double dtINV;     // interact: 1 / dt
+    double ft_scale;  // interact: rho_f * V / dt
+};
+
 struct CoupleArgs {
     MeshK m;
     const SolidK* sk;
@@ -125,7 +135,7 @@ struct CoupleArgs {
     int32_t* Ct;
     double* ftacc;  // [S][6] sums of f*V/dt and (C-x)^f*V/dt
     Counters* cnt;
-    double dtINV;
+    const StepParams* step;
     int method;
     int subsample_n;
     int exact_forcing;
@@ -142,7 +152,7 @@ constexpr uint32_t CT_KEY_BASE = 1u << 30;
 constexpr uint32_t CT_SHARED = 1u << 31;
 constexpr int SHARED_MAX_PROBES = 64;
 
-// classify work items: up to CHUNK_TILES consecutive tiles of one solid
+// classify work items: up to chunk_tiles consecutive tiles of one solid (default below; the autotuner may change it)
 constexpr int CHUNK_TILES = 8;
 
 struct ClassifyArgs {
@@ -152,6 +162,7 @@ struct ClassifyArgs {
     SolidPlan* plan;
     const int2* chunks;  // (solid, first tile)
     int total_chunks;
+    int chunk_tiles;     // tiles per work item
     uint8_t* cls;      // class byte per bbox cell
     float* alpha;      // solid fraction per bbox cell (cut candidates only)
     Counters* cnt;
@@ -186,6 +197,17 @@ struct GridK {
     double dINV;
     int32_t nx, ny, nz, nynz;
     int64_t ncell;
+};
+
+// Fine broad-phase grid of the sphere-like solids: about 8 cells per solid, each solid listed in every cell its
+// bounding box [x - r_B, x + r_B] overlaps (indices clamped to the grid).
+struct FineGridK {
+    double low[3];
+    double inv;              // 1 / cell size
+    int32_t n[3];
+    int32_t pad;
+    int64_t ncell;
+    int64_t cap;             // entries reserved for the cell lists
 };
 
 // list entry word: solid index in bits 0..29, cell type (1 all inside, 2 centre inside, 3 centre outside) in 30..31

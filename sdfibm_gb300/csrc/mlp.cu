@@ -1,6 +1,7 @@
 // Learned cut-cell fraction on the Blackwell tensor cores: inference, training (forward + backward), Adam, and the
 // generator of labelled training cells.  Parameter layout, features and numerics: include/sdfibm_mlp.h.
 //
+// Model output: a = sigmoid(logit(planar fraction) + gate * network), see model_prior in mlp.cuh.
 // One CTA of 128 threads works on tiles of 128 cells; thread t owns cell t of the tile, row t of every M = 128
 // operand and lane t of tensor memory.  Thread 0 issues the tcgen05.mma instructions and commits them to one
 // mbarrier; every wait on it is bounded and a timeout ends the CTA's work with an error code.
@@ -200,7 +201,9 @@ __global__ void __launch_bounds__(MLP_THREADS) mlp_infer_kernel(MlpInferArgs A) 
             const float zz = z[j] + sb2[j];
             o += sw3[j] * (zz * sigm(zz));
         }
-        const float a = sigm(o);
+        float prior, gate;
+        model_prior(x, prior, gate);
+        const float a = sigm(prior + gate * o);
         if (valid) {
             if (!A.ref_solid) {
                 A.out[c] = a;
@@ -340,9 +343,11 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) mlp_grad_kernel(MlpGradArgs A)
             const float zz = v[j] + sb2[j];
             o += sw3[j] * (zz * sigm(zz));
         }
-        const float a = sigm(o);
+        float prior, gate;
+        model_prior(x, prior, gate);
+        const float a = sigm(prior + gate * o);
         const float d = valid ? a - y : 0.f;
-        const float dz3 = A.scale * d * a * (1.f - a);
+        const float dz3 = A.scale * d * a * (1.f - a) * gate;
         float w[64];
 #pragma unroll
         for (int j = 0; j < 64; ++j) {
@@ -624,15 +629,22 @@ int mlp_sm_count() {
     return g_smcount;
 }
 
-void launch_mlp_infer(const MlpInferArgs& a, int grid, cudaStream_t st) {
+// shared-memory reservations of the MLP kernels (outside any stream capture: set before the first launch)
+void mlp_prepare() {
     static std::once_flag once;
-    std::call_once(once, [] { cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, INF_SMEM); });
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, INF_SMEM);
+        cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TR_SMEM);
+    });
+}
+
+void launch_mlp_infer(const MlpInferArgs& a, int grid, cudaStream_t st) {
+    mlp_prepare();
     mlp_infer_kernel<<<grid, MLP_THREADS, INF_SMEM, st>>>(a);
 }
 
 void launch_mlp_grad(const MlpGradArgs& a, int grid, cudaStream_t st) {
-    static std::once_flag once;
-    std::call_once(once, [] { cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TR_SMEM); });
+    mlp_prepare();
     mlp_grad_kernel<<<grid, MLP_THREADS, TR_SMEM, st>>>(a);
 }
 

@@ -97,7 +97,7 @@ def init_params(seed=0):
     rng = np.random.default_rng(seed)
     W1 = rng.uniform(-1, 1, (64, 11)) * np.sqrt(3.0 / 11)
     W2 = rng.uniform(-1, 1, (64, 64)) * np.sqrt(3.0 / 64)
-    w3 = rng.uniform(-1, 1, 64) * np.sqrt(3.0 / 64)
+    w3 = rng.uniform(-1, 1, 64) * np.sqrt(3.0 / 64) * 0.1  # start near the planar prior
     return np.concatenate([W1.ravel(), np.zeros(64), W2.ravel(), np.zeros(64), w3, [0.0]]).astype(np.float32)
 
 

