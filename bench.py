@@ -109,13 +109,14 @@ def make_workload(args):
     w.opt.fraction_method = METHODS[args.method]
     w.opt.exact_forcing = 1 if getattr(args, "exact_forcing", False) else 0
     if args.method == "learned":
-        w.opt.learned_fallback_n = 16
+        from sdfibm_gb300 import learned
+        w.opt.learned_fallback_n = int(learned.load_model()[3].get("band", {}).get("fallback_n", 16))
     elif args.method == "subsample":
         w.opt.subsample_n = 10
     return w
 
 
-def make_cloud(w, method, subsample_n=None, stream=None, timing=False):
+def make_cloud(w, method, subsample_n=None, stream=None, timing=False, band=None):
     """A coupling context of workload w with the given fraction method (the learned model loaded if needed).
     With a stream the context replays CUDA graphs of its steps; with timing it records per-kernel events instead."""
     import copy
@@ -130,7 +131,9 @@ def make_cloud(w, method, subsample_n=None, stream=None, timing=False):
     opt.graphs = 0 if timing else 1
     cloud = SolidCloud(w.mesh, w.solids, opt, stream=stream)
     if method == "learned":
-        params, tt, tg, _ = learned.load_model()
+        params, tt, tg, meta = learned.load_model()
+        if band is not None:
+            tt, tg = band[0], band[1]
         cloud.set_fraction_model(params, tt, tg)
     return cloud
 
@@ -164,14 +167,22 @@ def time_steps(torch, cloud, w, U, f, steps, warmup, flush, stream=None, kernel_
                 launches=launches, kernel_ms={k: sum(v) / len(v) for k, v in kt.items()}, stats=st)
 
 
-def accuracy(torch, w, cloud, U):
+def reference16(w, U):
+    """Fields and forces of one SUBSAMPLE(16^3) step (its classifications equal the FP64 oracle's)."""
+    ref = make_cloud(w, "subsample", subsample_n=16)
+    fr = ref.new_fields()
+    FTr = ref.interact(0.0, w.dt, U, fr)
+    ref.close()
+    return fr, FTr
+
+
+def accuracy(torch, w, cloud, U, ref):
     """Learned As and per-solid force against SUBSAMPLE(16^3) on the same step."""
     import numpy as np
-    ref = make_cloud(w, "subsample", subsample_n=16)
-    fr, fl = ref.new_fields(), cloud.new_fields()
-    FTr = ref.interact(0.0, w.dt, U, fr)
+    fr, FTr = ref
+    fl = cloud.new_fields()
+    torch.cuda.synchronize()  # the fields are zeroed on torch's stream; the context may run on another
     FTl = cloud.interact(0.0, w.dt, U, fl)
-    ref.close()
     touched = fr["Ct"] != 0
     cut = touched & ~((fr["As"] == 1.0) & (fl["As"] == 1.0))
     err = (fl["As"] - fr["As"]).abs()[cut].double()
@@ -345,10 +356,12 @@ def main():
 
     compare = None
     if args.method == "learned" and not args.no_compare:
+        ref = reference16(w, U)
         plain = make_cloud(w, "subsample", subsample_n=10, stream=stream)
         with torch.cuda.stream(stream):
             fp = plain.new_fields()
         tp = time_steps(torch, plain, w, U, fp, args.steps, args.warmup, flush, stream=stream)
+        acc_plain = accuracy(torch, w, plain, U, ref)
         plain.close()
         del fp
         pt = make_cloud(w, "subsample", subsample_n=10, timing=True)
@@ -356,14 +369,38 @@ def main():
         tp["kernel_ms"] = time_steps(torch, pt, w, U, fpt, min(args.steps, 3), 2, flush, kernel_times=True)["kernel_ms"]
         pt.close()
         del fpt
-        acc = accuracy(torch, w, cloud, U)
+        acc = accuracy(torch, w, cloud, U, ref)
         st = tm["stats"]
+        # other operating points of the same model: the open band and the 10^3 fallback
+        points = []
+        for label, band, fb in (("open band (network on every cut cell)", (1e30, 1e30), None),
+                                ("tau_twist 0.1, tau_grad 0.05, SUBSAMPLE 10^3 fallback", (0.1, 0.05), 10)):
+            import copy
+            w2 = copy.copy(w)
+            w2.opt = copy.copy(w.opt)
+            if fb:
+                w2.opt.learned_fallback_n = fb
+            c2 = make_cloud(w2, "learned", stream=stream, band=band)
+            with torch.cuda.stream(stream):
+                f2 = c2.new_fields()
+            t2 = time_steps(torch, c2, w2, U, f2, args.steps, args.warmup, flush, stream=stream)
+            a2 = accuracy(torch, w2, c2, U, ref)
+            points.append({"band": label, "ms_per_step": t2["ms_step"],
+                           "value": t2["cells"] * world / (t2["ms_step"] * 1e-3),
+                           "fallback_cells": t2["stats"].get("learned_fallback_cells"),
+                           "as_abs_err_mean": a2["as_abs_err_mean"], "as_abs_err_p99": a2["as_abs_err_p99"],
+                           "force_rel_err_median": a2["force_rel_err_median"]})
+            c2.close()
+            del f2
+        del ref
         compare = {"plain": {"method": "SUBSAMPLE 10^3 samples per cut cell", "ms_per_step": tp["ms_step"],
                              "value": tp["cells"] * world / (tp["ms_step"] * 1e-3),
+                             "as_abs_err_mean": acc_plain["as_abs_err_mean"],
+                             "as_abs_err_p99": acc_plain["as_abs_err_p99"],
                              "kernel_ms": {k: round(v, 4) for k, v in tp["kernel_ms"].items()}},
                    "speedup_vs_plain": tp["ms_step"] / tm["ms_step"],
                    "learned_cells": st.get("learned_cells"), "fallback_cells": st.get("learned_fallback_cells"),
-                   "accuracy": acc}
+                   "accuracy": acc, "other_operating_points": points}
 
     # full time step (interact + evolve with its sub-steps and collisions + fixInternal), device time, graphs
     with torch.cuda.stream(stream):

@@ -23,7 +23,11 @@ __global__ void classify_kernel_2d(ClassifyArgs A);
 __global__ void learned_fallback_kernel(FallbackArgs A);
 __global__ void connect_kernel(MeshK m, const SolidK* sk, SolidPlan* plan, const uint8_t* scratch, uint32_t* gbitmaps,
                                int32_t* in_cell, int32_t* in_solid, int32_t* cut_cell, int32_t* cut_solid,
-                               int64_t cap_in, int64_t cap_cut, Counters* cnt, int smem_words);
+                               int64_t cap_in, int64_t cap_cut, Counters* cnt, int smem_words, const int32_t* solids);
+__global__ void connect_small_kernel(MeshK m, const SolidK* sk, SolidPlan* plan, const uint8_t* scratch,
+                                     int32_t* in_cell, int32_t* in_solid, int32_t* cut_cell, int32_t* cut_solid,
+                                     int64_t cap_in, int64_t cap_cut, Counters* cnt, const int32_t* solids,
+                                     int nsolids);
 
 __global__ void couple_kernel(CoupleArgs A);
 __global__ void finalize_kernel(float* As, float* Ts, float* Fs, int32_t* Ct, const Counters* cnt, int64_t N,
@@ -95,6 +99,9 @@ struct sdfibm_ctx {
     uint32_t* d_gbitmaps = nullptr;
     int64_t gbitmap_words = 0;
     int connect_smem_bytes = 0;
+    // flood-fill work: solids with small bbox bitmaps (one warp each) and the others (one CTA each)
+    int32_t *d_small = nullptr, *d_big = nullptr;
+    int n_small = 0, n_big = 0;
     // touched-cell lists, double buffered: [cur] is this call's, [cur ^ 1] the previous call's (sparse reset)
     int32_t* d_lists[2][4] = {{nullptr, nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr, nullptr}};
     int cur = 0;
@@ -277,6 +284,7 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
 
     // static per-solid records
     ctx->hk.resize(nsolids);
+    std::vector<int32_t> small_solids, big_solids;
     int64_t scratch = 0, gwords = 0, bbox_total = 0;
     int64_t tiles = 0;
     int max_smem_words = 0;
@@ -319,12 +327,16 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         scratch += (cells + 15) & ~(int64_t)15;
         bbox_total += std::min<int64_t>(cells, N);
         const int64_t words = 2 * (int64_t)k.ext[1] * k.ext[2] * ((k.ext[0] + 31) / 32);
-        if (words * 4 > SMEM_CAP_BYTES) {
+        if (words / 2 <= 256) {
+            small_solids.push_back(s);  // warp-per-solid flood fill (connect_small_kernel)
+        } else if (words * 4 > SMEM_CAP_BYTES) {
             k.bitmap_global = 1;
             k.bitmap_off = gwords;
             gwords += words;
+            big_solids.push_back(s);
         } else {
             max_smem_words = std::max<int>(max_smem_words, (int)words);
+            big_solids.push_back(s);
         }
         k.motion_type = d.motion_type;
         k.forcer_type = d.forcer_type;
@@ -340,6 +352,8 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
     ctx->scratch_bytes = scratch;
     ctx->gbitmap_words = gwords;
     ctx->connect_smem_bytes = max_smem_words * 4;
+    ctx->n_small = (int)small_solids.size();
+    ctx->n_big = (int)big_solids.size();
     ctx->cap = std::max<int64_t>(1, bbox_total);
 
     {
@@ -439,6 +453,7 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         dalloc(&ctx->d_ftacc, 6 * (size_t)nsolids) || dalloc(&ctx->d_ft, 6 * (size_t)nsolids) ||
         dalloc(&ctx->d_sh_keys, (size_t)ctx->sh_mask + 1) || dalloc(&ctx->d_sh_vals, 5 * ((size_t)ctx->sh_mask + 1)) ||
         dalloc(&ctx->d_sh_used, (size_t)ctx->sh_mask + 1) || dalloc(&ctx->d_step, 2) ||
+        dalloc(&ctx->d_small, small_solids.size()) || dalloc(&ctx->d_big, big_solids.size()) ||
         cudaMallocHost((void**)&ctx->h_cnt, sizeof(Counters)) != cudaSuccess ||
         cudaMallocHost((void**)&ctx->h_ft, std::max<size_t>(1, 6 * (size_t)nsolids) * sizeof(double)) != cudaSuccess) {
         ctx->err = "device allocation failed";
@@ -467,6 +482,8 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
     };
     if (up(c->d_sk, c->hk.data(), sizeof(SolidK) * nsolids) || up(c->d_st, st.data(), sizeof(sdfibm_solid_state) * nsolids) ||
         up(c->d_chunks, chunks.data(), sizeof(int2) * chunks.size()) ||
+        up(c->d_small, small_solids.data(), sizeof(int32_t) * small_solids.size()) ||
+        up(c->d_big, big_solids.data(), sizeof(int32_t) * big_solids.size()) ||
         cudaMemset(c->d_cnt, 0, sizeof(Counters)) != cudaSuccess ||
         cudaMemset(c->d_sh_keys, 0xff, sizeof(int32_t) * ((size_t)c->sh_mask + 1)) != cudaSuccess ||
         cudaMemset(c->d_sh_vals, 0, sizeof(double) * 5 * ((size_t)c->sh_mask + 1)) != cudaSuccess ||
@@ -564,10 +581,15 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             mark(ctx, "learned_fallback_kernel");
             launches += 2;
         }
-        connect_kernel<<<S, 512, ctx->connect_smem_bytes, st>>>(ctx->mesh, ctx->d_sk, ctx->d_plan, ctx->d_scratch,
-                                                                ctx->d_gbitmaps, ctx->in_cell(), ctx->in_solid(),
-                                                                ctx->cut_cell(), ctx->cut_solid(), ctx->cap, ctx->cap,
-                                                                ctx->d_cnt, ctx->connect_smem_bytes / 4);
+        if (ctx->n_small > 0)
+            connect_small_kernel<<<(ctx->n_small + 7) / 8, 256, 0, st>>>(
+                ctx->mesh, ctx->d_sk, ctx->d_plan, ctx->d_scratch, ctx->in_cell(), ctx->in_solid(), ctx->cut_cell(),
+                ctx->cut_solid(), ctx->cap, ctx->cap, ctx->d_cnt, ctx->d_small, ctx->n_small);
+        if (ctx->n_big > 0)
+            connect_kernel<<<ctx->n_big, 512, ctx->connect_smem_bytes, st>>>(
+                ctx->mesh, ctx->d_sk, ctx->d_plan, ctx->d_scratch, ctx->d_gbitmaps, ctx->in_cell(), ctx->in_solid(),
+                ctx->cut_cell(), ctx->cut_solid(), ctx->cap, ctx->cap, ctx->d_cnt, ctx->connect_smem_bytes / 4,
+                ctx->d_big);
         mark(ctx, "connect_kernel");
         claim_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(ctx->in_cell(), ctx->in_solid(), ctx->cut_cell(),
                                                         ctx->cut_solid(), Ct, ctx->d_cnt, N);
@@ -973,6 +995,8 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
     for (void* p : dev)
         if (p) cudaFree(p);
     if (ctx->d_step) cudaFree(ctx->d_step);
+    if (ctx->d_small) cudaFree(ctx->d_small);
+    if (ctx->d_big) cudaFree(ctx->d_big);
     for (auto& g : ctx->igraph)
         if (g.valid) cudaGraphExecDestroy(g.exec);
     if (ctx->egraph.valid) cudaGraphExecDestroy(ctx->egraph.exec);

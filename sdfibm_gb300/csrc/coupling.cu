@@ -224,6 +224,26 @@ __device__ inline int block_excl_scan(int v, int* warp_sums, int& total) {
     return before;
 }
 
+// local cell index of the flood-fill seed: the nearest cell when it has an inside vertex, else the lowest-label cell
+// that has one (the seed fallback scan of cellenumerator.cpp:52-63); -1 when the solid touches no cell
+__device__ inline int seed_local(const MeshK& m, const SolidPlan& pl, const uint8_t* cls, int ex, int ey, int ez) {
+    int sl = -1;
+    const int64_t seed = pl.seed;
+    const int64_t si = seed % m.nx, sj = (seed / m.nx) % m.ny, sk2 = seed / ((int64_t)m.nx * m.ny);
+    const int64_t a = si - pl.lo[0], b = sj - pl.lo[1], c = sk2 - pl.lo[2];
+    if (a >= 0 && b >= 0 && c >= 0 && a < ex && b < ey && c < ez) {
+        const int li = (int)(a + (int64_t)ex * (b + (int64_t)ey * c));
+        if (cls[li]) sl = li;
+    }
+    if (sl < 0 && pl.min_cand != ~0ull) {
+        const int64_t g = (int64_t)pl.min_cand;
+        const int64_t gi = g % m.nx, gj = (g / m.nx) % m.ny, gk = g / ((int64_t)m.nx * m.ny);
+        sl = (int)((gi - pl.lo[0]) + (int64_t)ex * ((gj - pl.lo[1]) + (int64_t)ey * (gk - pl.lo[2])));
+    }
+    if (sl >= ex * ey * ez) sl = -1;
+    return sl;
+}
+
 __global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const SolidK* __restrict__ sk,
                                                               SolidPlan* __restrict__ plan,
                                                               const uint8_t* __restrict__ scratch,
@@ -231,12 +251,12 @@ __global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const Sol
                                                               int32_t* __restrict__ in_cell, int32_t* __restrict__ in_solid,
                                                               int32_t* __restrict__ cut_cell, int32_t* __restrict__ cut_solid,
                                                               int64_t cap_in, int64_t cap_cut, Counters* cnt,
-                                                              int smem_words) {
+                                                              int smem_words, const int32_t* __restrict__ solids) {
     extern __shared__ uint32_t dsm[];
     __shared__ int s_seed;  // local cell index of the seed, -1: none
     __shared__ int warp_sums[32];
     __shared__ int s_base_in, s_base_cut;
-    const int s = blockIdx.x;
+    const int s = solids ? solids[blockIdx.x] : blockIdx.x;
     const int tid = threadIdx.x;
     const SolidK& k = sk[s];
     SolidPlan& pl = plan[s];
@@ -253,21 +273,7 @@ __global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const Sol
     }
     // seed: nearest cell when it has an inside vertex, else the lowest-label cell that has one
     if (tid == 0) {
-        int sl = -1;
-        const int64_t seed = pl.seed;
-        const int64_t si = seed % m.nx, sj = (seed / m.nx) % m.ny, sk2 = seed / ((int64_t)m.nx * m.ny);
-        const int64_t a = si - pl.lo[0], b = sj - pl.lo[1], c = sk2 - pl.lo[2];
-        if (a >= 0 && b >= 0 && c >= 0 && a < ex && b < ey && c < ez) {
-            const int li = (int)(a + (int64_t)ex * (b + (int64_t)ey * c));
-            if (cls[li]) sl = li;
-        }
-        if (sl < 0 && pl.min_cand != ~0ull) {
-            const int64_t g = (int64_t)pl.min_cand;
-            const int64_t gi = g % m.nx, gj = (g / m.nx) % m.ny, gk = g / ((int64_t)m.nx * m.ny);
-            sl = (int)((gi - pl.lo[0]) + (int64_t)ex * ((gj - pl.lo[1]) + (int64_t)ey * (gk - pl.lo[2])));
-        }
-        if (sl >= ex * ey * ez) sl = -1;
-        s_seed = sl;
+        s_seed = seed_local(m, pl, cls, ex, ey, ez);
     }
     __syncthreads();
     if (s_seed < 0) {
@@ -384,6 +390,168 @@ __global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const Sol
         return;
     }
     int64_t pin = bin + off_in, pcut = bcut + off_cut;
+    for (int row = r0; row < r1; ++row) {
+        const int jj = row % ey, kk = row / ey;
+        for (int w = 0; w < W; ++w) {
+            uint32_t bits = R[row * W + w];
+            while (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1;
+                const int xx = (w << 5) + b;
+                const uint8_t cc = cls[(int64_t)row * ex + xx];
+                const int64_t gi = pl.lo[0] + xx, gj = pl.lo[1] + jj, gk = pl.lo[2] + kk;
+                const int32_t cell = (int32_t)(gi + (int64_t)m.nx * (gj + (int64_t)m.ny * gk));
+                if (cc == 1) { in_cell[pin] = cell; in_solid[pin] = list_word(s, 1); ++pin; }
+                else { cut_cell[pcut] = cell; cut_solid[pcut] = list_word(s, cc); ++pcut; }
+            }
+        }
+    }
+}
+
+// The same connected component for solids whose bbox bitmap has at most CON_SMALL_WORDS words: one warp per solid,
+// eight solids per CTA, bitmaps in shared memory, warp-synchronous sweeps.
+constexpr int CON_SMALL_WORDS = 256;
+constexpr int CON_SMALL_WARPS = 8;
+
+__global__ void __launch_bounds__(CON_SMALL_WARPS * 32) connect_small_kernel(
+    MeshK m, const SolidK* __restrict__ sk, SolidPlan* __restrict__ plan, const uint8_t* __restrict__ scratch,
+    int32_t* __restrict__ in_cell, int32_t* __restrict__ in_solid, int32_t* __restrict__ cut_cell,
+    int32_t* __restrict__ cut_solid, int64_t cap_in, int64_t cap_cut, Counters* cnt, const int32_t* __restrict__ solids,
+    int nsolids) {
+    __shared__ uint32_t s_bits[CON_SMALL_WARPS][2 * CON_SMALL_WORDS];
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int item = blockIdx.x * CON_SMALL_WARPS + wid;
+    if (item >= nsolids) return;
+    const int s = solids[item];
+    const SolidK& k = sk[s];
+    SolidPlan& pl = plan[s];
+    const int ex = k.ext[0], ey = k.ext[1], ez = k.ext[2];
+    const int W = (ex + 31) >> 5;
+    const int rows = ey * ez;
+    const int nwords = rows * W;
+    uint32_t* C = s_bits[wid];
+    uint32_t* R = C + CON_SMALL_WORDS;
+    const uint8_t* cls = scratch + k.scratch_off;
+    if (pl.err) {
+        if (lane == 0) { pl.n_inside = 0; pl.n_cut = 0; }
+        return;
+    }
+    int sl = 0;
+    if (lane == 0) sl = seed_local(m, pl, cls, ex, ey, ez);
+    sl = __shfl_sync(FULL, sl, 0);
+    if (sl < 0) {
+        if (lane == 0) { pl.n_inside = 0; pl.n_cut = 0; }
+        return;
+    }
+    for (int w = lane; w < nwords; w += 32) {
+        const int row = w / W, wi = w - row * W;
+        const uint8_t* rp = cls + (int64_t)row * ex;
+        uint32_t bits = 0;
+        const int x0 = wi << 5, x1 = min(ex, x0 + 32);
+        for (int xx = x0; xx < x1; ++xx) bits |= (rp[xx] ? 1u : 0u) << (xx - x0);
+        C[w] = bits;
+        R[w] = 0;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        const int sx = sl % ex, srow = sl / ex;
+        R[srow * W + (sx >> 5)] |= 1u << (sx & 31);
+    }
+    __syncwarp();
+    const int max_rounds = 8 + 2 * (ex + ey + ez);
+    for (int round = 0;; ++round) {
+        int changed = 0;
+        for (int row = lane; row < rows; row += 32) {
+            uint32_t* r = R + row * W;
+            const uint32_t* c = C + row * W;
+            uint32_t carry = 0;
+            for (int w = 0; w < W; ++w) {
+                const uint32_t seeds = (r[w] | (carry & 1u)) & c[w];
+                const uint32_t f = fill_up(c[w], seeds);
+                if (f != r[w]) { changed = 1; r[w] = f; }
+                carry = f >> 31;
+            }
+            carry = 0;
+            for (int w = W - 1; w >= 0; --w) {
+                const uint32_t seeds = (r[w] | (carry << 31)) & c[w];
+                const uint32_t f = fill_down(c[w], seeds);
+                if (f != r[w]) { changed = 1; r[w] = f; }
+                carry = f & 1u;
+            }
+        }
+        __syncwarp();
+        for (int col = lane; col < ez * W; col += 32) {
+            const int kk = col / W, w = col - kk * W;
+            uint32_t* r = R + (kk * ey) * W + w;
+            const uint32_t* c = C + (kk * ey) * W + w;
+            for (int j = 1; j < ey; ++j) {
+                const uint32_t f = r[j * W] | (r[(j - 1) * W] & c[j * W]);
+                if (f != r[j * W]) { changed = 1; r[j * W] = f; }
+            }
+            for (int j = ey - 2; j >= 0; --j) {
+                const uint32_t f = r[j * W] | (r[(j + 1) * W] & c[j * W]);
+                if (f != r[j * W]) { changed = 1; r[j * W] = f; }
+            }
+        }
+        __syncwarp();
+        if (ez > 1) {
+            for (int col = lane; col < ey * W; col += 32) {
+                const int jj = col / W, w = col - jj * W;
+                uint32_t* r = R + jj * W + w;
+                const uint32_t* c = C + jj * W + w;
+                const int stride = ey * W;
+                for (int kk = 1; kk < ez; ++kk) {
+                    const uint32_t f = r[kk * stride] | (r[(kk - 1) * stride] & c[kk * stride]);
+                    if (f != r[kk * stride]) { changed = 1; r[kk * stride] = f; }
+                }
+                for (int kk = ez - 2; kk >= 0; --kk) {
+                    const uint32_t f = r[kk * stride] | (r[(kk + 1) * stride] & c[kk * stride]);
+                    if (f != r[kk * stride]) { changed = 1; r[kk * stride] = f; }
+                }
+            }
+        }
+        __syncwarp();
+        if (!__any_sync(FULL, changed)) break;
+        if (round >= max_rounds) {
+            if (lane == 0) set_error(cnt, DERR_FLOOD_LIMIT);
+            break;
+        }
+    }
+    // emit in ascending label order: lane t owns rows [t*rpt, (t+1)*rpt)
+    const int rpt = (rows + 31) / 32;
+    const int r0 = min(rows, lane * rpt), r1 = min(rows, r0 + rpt);
+    int nin = 0, ncut = 0;
+    for (int row = r0; row < r1; ++row)
+        for (int w = 0; w < W; ++w) {
+            uint32_t bits = R[row * W + w];
+            while (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1;
+                if (cls[(int64_t)row * ex + (w << 5) + b] == 1) ++nin; else ++ncut;
+            }
+        }
+    int xin = nin, xcut = ncut;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int a = __shfl_up_sync(FULL, xin, o), b = __shfl_up_sync(FULL, xcut, o);
+        if (lane >= o) { xin += a; xcut += b; }
+    }
+    const int tot_in = __shfl_sync(FULL, xin, 31), tot_cut = __shfl_sync(FULL, xcut, 31);
+    int bin = 0, bcut = 0;
+    if (lane == 0) {
+        bin = atomicAdd(&cnt->n_inside, tot_in);
+        bcut = atomicAdd(&cnt->n_cut, tot_cut);
+        pl.n_inside = tot_in;
+        pl.n_cut = tot_cut;
+    }
+    bin = __shfl_sync(FULL, bin, 0);
+    bcut = __shfl_sync(FULL, bcut, 0);
+    if ((int64_t)bin + tot_in > cap_in || (int64_t)bcut + tot_cut > cap_cut) {
+        if (lane == 0) set_error(cnt, DERR_CAPACITY);
+        return;
+    }
+    int64_t pin = (int64_t)bin + xin - nin, pcut = (int64_t)bcut + xcut - ncut;
     for (int row = r0; row < r1; ++row) {
         const int jj = row % ey, kk = row / ey;
         for (int w = 0; w < W; ++w) {

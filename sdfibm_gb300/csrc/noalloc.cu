@@ -32,7 +32,7 @@ __global__ void classify_kernel_3d(ClassifyArgs A);
 __global__ void classify_kernel_2d(ClassifyArgs A);
 __global__ void connect_kernel(MeshK m, const SolidK* sk, SolidPlan* plan, const uint8_t* scratch, uint32_t* gbitmaps,
                                int32_t* in_cell, int32_t* in_solid, int32_t* cut_cell, int32_t* cut_solid,
-                               int64_t cap_in, int64_t cap_cut, Counters* cnt, int smem_words);
+                               int64_t cap_in, int64_t cap_cut, Counters* cnt, int smem_words, const int32_t* solids);
 }  // namespace sdfibm_dev
 
 using namespace sdfibm_dev;
@@ -284,7 +284,7 @@ extern "C" int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc* mesh, const s
     connect_kernel<<<1, 512, 0, st>>>(m, d_sk, d_plan, b + OFF_CLS, reinterpret_cast<uint32_t*>(b + OFF_BITMAP),
                                       reinterpret_cast<int32_t*>(b + OFF_IN_CELL), reinterpret_cast<int32_t*>(b + OFF_IN_SOLID),
                                       reinterpret_cast<int32_t*>(b + OFF_CUT_CELL), reinterpret_cast<int32_t*>(b + OFF_CUT_SOLID),
-                                      NA_MAX_BBOX_CELLS, NA_MAX_BBOX_CELLS, d_cnt, 0);
+                                      NA_MAX_BBOX_CELLS, NA_MAX_BBOX_CELLS, d_cnt, 0, nullptr);
     noalloc_order_kernel<<<1, 1024, 0, st>>>(cells, types, capacity, n_device);
     return cudaGetLastError() == cudaSuccess ? SDFIBM_OK : SDFIBM_ERR_CUDA;
 }

@@ -65,6 +65,8 @@ def main(argv=None):
     ap.add_argument("--hr-min", type=float, default=0.01)
     ap.add_argument("--hr-max", type=float, default=1.5)
     ap.add_argument("--n-sub", type=int, default=16)
+    ap.add_argument("--families", default="all", help="all, or a comma list of sphere,ellipsoid,box,plane,cylinder,"
+                                                        "elliptic_cylinder")
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--band-mean", type=float, default=7e-4)
     ap.add_argument("--band-p99", type=float, default=1e-2)
@@ -72,7 +74,11 @@ def main(argv=None):
     a = ap.parse_args(argv)
     import torch
     torch.cuda.init()
-    dkw = dict(hr=(a.hr_min, a.hr_max), n_sub=a.n_sub)
+    from . import abi
+    names = dict(sphere=abi.MLP_SPHERE, ellipsoid=abi.MLP_ELLIPSOID, box=abi.MLP_BOX, plane=abi.MLP_PLANE,
+                 cylinder=abi.MLP_CYLINDER, elliptic_cylinder=abi.MLP_ELLIPTIC_CYL)
+    fam = learned.ALL_FAMILIES if a.families == "all" else sum(names[x] for x in a.families.split(","))
+    dkw = dict(hr=(a.hr_min, a.hr_max), n_sub=a.n_sub, families=fam)
     t0 = time.time()
     feat, label, _ = learned.make_dataset(torch, a.train, seed=a.seed, **dkw)
     tf, tl, _ = learned.make_dataset(torch, a.test, seed=a.seed + 1, **dkw)
@@ -104,7 +110,7 @@ def main(argv=None):
     q = torch.quantile(err[:1 << 22].double(), torch.tensor([0.5, 0.9, 0.99, 0.999], dtype=torch.float64,
                                                             device=err.device)).tolist()
     meta = dict(data=dict(train=a.train, test=a.test, seed=a.seed, hr=[a.hr_min, a.hr_max], n_sub=a.n_sub,
-                          families="sphere ellipsoid box plane circle-prism ellipse-prism", z_axis_frac=0.25),
+                          families=a.families, z_axis_frac=0.25),
                 train=dict(epochs=a.epochs, batch=a.batch, lr=a.lr, loss_per_epoch=[float(x) for x in losses],
                            seconds=t_train, data_seconds=t_data),
                 test=dict(mean_abs=err.mean().item(), max_abs=err.max().item(), q50=q[0], q90=q[1], q99=q[2],
