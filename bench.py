@@ -32,13 +32,23 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # algorithmic bytes per unit (one coupling cell = one (solid, touched cell) pair):
 #   U read 12 + As 4 + Fs 12 + Ts 4 + Ct 4 written = 36 B per coupling cell for the whole coupling; per kernel:
 ALG_BYTES = {
-    "couple_kernel": ("coupling_cells", 32.0),   # U read 12, As/Ts/Fs written 20
-    "claim_kernel": ("coupling_cells", 4.0),     # Ct written
-    "finalize_kernel": ("coupling_cells", 8.0),  # Ct and As rewritten for the cells that need it
-    "reset_kernel": ("coupling_cells", 24.0),    # previous cells zeroed
-    "classify_kernel": ("bbox_cells", 1.0),      # one class byte per bbox cell
-    "connect_kernel": ("bbox_cells", 1.0),       # class bytes read once
+    "couple_kernel": ("coupling_cells", 32.0),     # U read 12, As/Ts/Fs written 20
+    "claim_kernel": ("coupling_cells", 4.0),       # Ct written
+    "finalize_kernel": ("coupling_cells", 8.0),    # Ct and As rewritten for the cells that need it
+    "reset_kernel": ("coupling_cells", 24.0),      # previous cells zeroed
+    "classify_kernel": ("bbox_cells", 1.0),        # one class byte per bbox cell (+ the cut-cell outputs below)
+    "connect_kernel": ("bbox_cells", 1.0),         # class bytes read once
+    "mlp_infer_kernel": ("learned_cells", 56.0),   # 11 features + destination read, fraction written
+    "learned_fallback_kernel": ("fallback_cells", 16.0),  # destination read, fraction written
 }
+# DRAM bytes per unit measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum of one launch / its units) on the
+# 256^3 / 2048-solid learned workload; profiles/<kernel>_poly3d_256_learned.md records the captures
+NCU_BYTES_PER_UNIT = {
+    "couple_kernel": 219.2,    # 292.0 MB for 1,332,670 coupling cells: short x-runs of scattered cells in 6 field planes
+    "classify_kernel": 3.16,   # 24.7 MB for 7,825,801 bbox cells
+}
+# FLOPs of the two tensor-core layers per predicted cell: hi and lo BF16 halves of an 11(16)x64 and a 64x64 product
+MLP_FLOPS_PER_CELL = 2 * (2 * 16 * 64) + 2 * (2 * 64 * 64)
 METHODS = {"refgeo": 0, "subsample": 1, "learned": 2}
 
 
@@ -422,23 +432,31 @@ def main():
     # roofline of the dominant kernel
     peaks, peaks_kind = load_peaks()
     kmean = {k: sum(v) / len(v) for k, v in kt.items()}
-    dom = max((k for k in kmean if k in ALG_BYTES), key=lambda k: kmean[k])
-    unit_key, per_unit = ALG_BYTES[dom]
-    units = mean_cells if unit_key == "coupling_cells" else sum(bbox) / len(bbox)
+    dom = max(kmean, key=lambda k: kmean[k])
+    st = tm["stats"]
+    unit_counts = {"coupling_cells": mean_cells, "bbox_cells": sum(bbox) / len(bbox),
+                   "learned_cells": st.get("learned_cells", 0), "fallback_cells": st.get("learned_fallback_cells", 0)}
+    unit_key, per_unit = ALG_BYTES.get(dom, ("coupling_cells", 0.0))
+    units = unit_counts[unit_key]
     achieved = per_unit * units / (kmean[dom] * 1e-3) / 1e9
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    if os.path.exists(tfile):
-        try:
-            tr = json.load(open(tfile)).get(args.config, {}).get(args.method, {}).get(dom)
-            if tr:
-                traffic = tr["bytes_per_unit"] * units
-        except Exception:
-            traffic = None
+    traffic = NCU_BYTES_PER_UNIT[dom] * units if dom in NCU_BYTES_PER_UNIT else None
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_kind": peaks_kind,
-                "alg_bytes_per_unit": per_unit, "units": units,
+                "alg_bytes_per_unit": per_unit, "unit_of_work": unit_key, "units": units,
+                "note": "classify and the SUBSAMPLE fallback are FP32-ALU-bound (lattice inside tests), so their "
+                        "HBM fraction is small by construction; couple is the HBM-bound kernel",
                 "kernel_ms": {k: round(v, 4) for k, v in sorted(kmean.items(), key=lambda x: -x[1])}}
+    # the HBM-bound kernel of the step and the tensor-core kernel, each against its own peak
+    if "couple_kernel" in kmean:
+        a = ALG_BYTES["couple_kernel"][1] * mean_cells / (kmean["couple_kernel"] * 1e-3) / 1e9
+        roofline["couple_kernel"] = {"bound": "hbm", "achieved": a, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                                     "frac": a / peaks["hbm_gbs"],
+                                     "traffic": NCU_BYTES_PER_UNIT["couple_kernel"] * mean_cells
+                                     if "couple_kernel" in NCU_BYTES_PER_UNIT else None}
+    if "mlp_infer_kernel" in kmean and unit_counts["learned_cells"]:
+        tf = MLP_FLOPS_PER_CELL * unit_counts["learned_cells"] / (kmean["mlp_infer_kernel"] * 1e-3) / 1e12
+        roofline["mlp_infer_kernel"] = {"bound": "tensor", "achieved": tf, "peak": peaks["bf16_tflops"],
+                                        "unit": "TFLOP/s", "frac": tf / peaks["bf16_tflops"]}
 
     # end to end through the host-buffer entry point (pinned host fields)
     e2e = None

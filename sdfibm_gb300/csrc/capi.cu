@@ -18,8 +18,8 @@ namespace sdfibm_dev {
 // coupling.cu
 __global__ void plan_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state* st, SolidPlan* plan, int S,
                             Counters* cnt);
-__global__ void classify_kernel_3d(ClassifyArgs A);
-__global__ void classify_kernel_2d(ClassifyArgs A);
+void launch_classify(const ClassifyArgs& A, bool flat, int grid, cudaStream_t st);
+int classify_occupancy(int method, bool flat);
 __global__ void learned_fallback_kernel(FallbackArgs A);
 __global__ void connect_kernel(MeshK m, const SolidK* sk, SolidPlan* plan, const uint8_t* scratch, uint32_t* gbitmaps,
                                int32_t* in_cell, int32_t* in_solid, int32_t* cut_cell, int32_t* cut_solid,
@@ -499,7 +499,7 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         }
     }
     int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mesh->nz <= 2 ? classify_kernel_2d : classify_kernel_3d, 256, 0);
+    occ = classify_occupancy(ctx->opt.fraction_method, mesh->nz <= 2);
     ctx->classify_grid = std::max(1, occ) * ctx->num_sms;
     occ = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, couple_kernel, 256, 0);
@@ -560,8 +560,7 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             CA.feat = ctx->d_feat; CA.feat_cap = ctx->feat_cap; CA.fref_solid = ctx->d_fref_solid;
             CA.fref_index = ctx->d_fref_index; CA.inv_h = (float)(1.0 / ctx->mdesc.h[0]);
         }
-        if (ctx->mesh.nz <= 2) classify_kernel_2d<<<ctx->classify_grid, 256, 0, st>>>(CA);
-        else classify_kernel_3d<<<ctx->classify_grid, 256, 0, st>>>(CA);
+        launch_classify(CA, ctx->mesh.nz <= 2, ctx->classify_grid, st);
         mark(ctx, "classify_kernel");
         if (learned) {
             // network on every cut cell, SUBSAMPLE on the cells outside its band

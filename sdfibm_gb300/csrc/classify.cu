@@ -209,6 +209,104 @@ __device__ __forceinline__ int subsample_count(const MeshK& m, const ShapeK& sh,
     return cnt;
 }
 
+// Block-skipping count for the quadrics and boxes: the lattice is split into B x B x B blocks (B x B x 1 on one-layer
+// meshes).  For each block the inside function is bounded over the box of local coordinates that holds the block's
+// samples (centre +- half the block's span along the three step vectors, widened by the coordinate error bound Ep);
+// a block whose upper bound is below -Eg has every sample inside in the reference's FP64 evaluation, one whose
+// lower bound is above Eg has none, and only the remaining blocks are sampled, with the same coordinate sequence
+// and per-sample bound as subsample_count.  The count is therefore the exhaustive lattice count.
+template <int T>
+__device__ __forceinline__ void block_bounds(const SampleFrame& f, float X, float Y, float Z, float hx, float hy,
+                                             float hz, float& gmin, float& gmax) {
+    const float xl = X - hx, xh = X + hx, yl = Y - hy, yh = Y + hy, zl = Z - hz, zh = Z + hz;
+    const float ax = fmaxf(fabsf(xl), fabsf(xh)), ay = fmaxf(fabsf(yl), fabsf(yh)), az = fmaxf(fabsf(zl), fabsf(zh));
+    const float bx = (xl <= 0.f && xh >= 0.f) ? 0.f : fminf(fabsf(xl), fabsf(xh));
+    const float by = (yl <= 0.f && yh >= 0.f) ? 0.f : fminf(fabsf(yl), fabsf(yh));
+    const float bz = (zl <= 0.f && zh >= 0.f) ? 0.f : fminf(fabsf(zl), fabsf(zh));
+    if (T == SS_QUADRIC) {
+        gmax = __fmaf_rn(ax * ax, f.k0, __fmaf_rn(ay * ay, f.k1, (az * az) * f.k2)) - f.k3;
+        gmin = __fmaf_rn(bx * bx, f.k0, __fmaf_rn(by * by, f.k1, (bz * bz) * f.k2)) - f.k3;
+    } else {
+        gmax = fmaxf(fmaxf(ax - f.k0, ay - f.k1), az - f.k2);
+        gmin = fmaxf(fmaxf(bx - f.k0, by - f.k1), bz - f.k2);
+    }
+}
+
+template <int T>
+__device__ __noinline__ int subsample_blocks(const MeshK& m, const ShapeK& sh, const SampleFrame& f, int64_t i,
+                                             int64_t j, int64_t k, int n, int lb, float Ep, const D3& x, const Q4& q,
+                                             unsigned long long* rechecks) {
+    __shared__ uint8_t s_und[8][128];  // undecided block ids of each warp (blocks of 256 threads, at most 128 blocks)
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    uint8_t* list = s_und[(threadIdx.x >> 5) & 7];
+    const bool flat = m.twod != 0;
+    const int B = 1 << lb, nb = n >> lb, nbz = flat ? 1 : nb;
+    const int lsz = flat ? 2 * lb : 3 * lb;  // log2 of the samples per block
+    const int nblocks = nb * nb * nbz;
+    const float inv2n = 1.0f / (float)(2 * n);
+    // half span of a block along each step vector (t from its first to its last sample), widened by a relative 1e-6
+    const float half = 0.5f * (float)(2 * (B - 1)) * inv2n * 1.000001f;
+    const float halfz = flat ? 0.f : half;
+    const float hx = half * (fabsf(f.sxx) + fabsf(f.syx)) + halfz * fabsf(f.szx) + Ep;
+    const float hy = half * (fabsf(f.sxy) + fabsf(f.syy)) + halfz * fabsf(f.szy) + Ep;
+    const float hz = half * (fabsf(f.sxz) + fabsf(f.syz)) + halfz * fabsf(f.szz) + Ep + U32 * fabsf(f.pz);
+    int cnt = 0, nund = 0;
+    for (int base = 0; base < nblocks; base += 32) {
+        const int blk = base + lane;
+        bool undecided = false;
+        if (blk < nblocks) {
+            const int ba = blk % nb, bb = (blk / nb) % nb, bc = blk / (nb * nb);
+            const float ta = (float)(2 * ba * B + B) * inv2n, tb = (float)(2 * bb * B + B) * inv2n;
+            const float tc = flat ? 0.5f : (float)(2 * bc * B + B) * inv2n;
+            const float X = __fmaf_rn(tc, f.szx, __fmaf_rn(tb, f.syx, __fmaf_rn(ta, f.sxx, f.px)));
+            const float Y = __fmaf_rn(tc, f.szy, __fmaf_rn(tb, f.syy, __fmaf_rn(ta, f.sxy, f.py)));
+            const float Z = __fmaf_rn(tc, f.szz, __fmaf_rn(tb, f.syz, __fmaf_rn(ta, f.sxz, f.pz)));
+            float gmin, gmax;
+            block_bounds<T>(f, X, Y, Z, hx, hy, hz, gmin, gmax);
+            if (gmax < -f.Eg) cnt += 1 << lsz;
+            else if (!(gmin > f.Eg)) undecided = true;
+        }
+        const unsigned mask = __ballot_sync(FULL, undecided);
+        if (undecided) list[nund + __popc(mask & ((1u << lane) - 1u))] = (uint8_t)blk;
+        nund += __popc(mask);
+    }
+    __syncwarp();
+    const int slots = nund << lsz;
+    for (int e = lane; e < slots; e += 32) {
+        const int blk = list[e >> lsz], sidx = e & ((1 << lsz) - 1);
+        const int ba = blk % nb, bb = (blk / nb) % nb, bc = blk / (nb * nb);
+        const int ia = (ba << lb) + (sidx & (B - 1)), ib = (bb << lb) + ((sidx >> lb) & (B - 1));
+        const int ic = flat ? 0 : (bc << lb) + (sidx >> (2 * lb));
+        const float ta = (float)(2 * ia + 1) * inv2n, tb = (float)(2 * ib + 1) * inv2n;
+        const float tc = flat ? 0.5f : (float)(2 * ic + 1) * inv2n;
+        const float bx = __fmaf_rn(tb, f.syx, __fmaf_rn(ta, f.sxx, f.px));
+        const float by = __fmaf_rn(tb, f.syy, __fmaf_rn(ta, f.sxy, f.py));
+        const float bz = __fmaf_rn(tb, f.syz, __fmaf_rn(ta, f.sxz, f.pz));
+        int res = sample_inside<T>(sh, f, __fmaf_rn(tc, f.szx, bx), __fmaf_rn(tc, f.szy, by), __fmaf_rn(tc, f.szz, bz));
+        if (res == 2) {
+            ++*rechecks;
+            res = exact_inside_sample(sh, m, i, j, k, ia, ib, ic, n, x, q);
+        }
+        cnt += res;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(FULL, cnt, o);
+    return cnt;
+}
+
+// log2 of the block edge for block skipping (power of two dividing n, at most 128 blocks), 0: sample every point
+__device__ inline int block_log2(int n, bool flat) {
+    for (int lb = 1; lb <= 3; ++lb) {
+        const int B = 1 << lb;
+        if (n % B) continue;
+        const int nb = n / B;
+        if ((flat ? nb * nb : nb * nb * nb) <= 128) return lb;
+    }
+    return 0;
+}
+
 static __device__ __noinline__ float subsample_warp(const MeshK& m, const ShapeK& sh, const float* M, const TileFrame& tf,
                                                     int a0, int b0, int c0, const D3& x, const Q4& q, int64_t i,
                                                     int64_t j, int64_t k, int n, unsigned long long* rechecks) {
@@ -269,12 +367,16 @@ static __device__ __noinline__ float subsample_warp(const MeshK& m, const ShapeK
         }
         f.Eg = (2.f * (mx * f.k0 + my * f.k1 + mz * f.k2) + Ep * (f.k0 + f.k1 + f.k2)) * Ep +
                10.f * u * (mx * mx * f.k0 + my * my * f.k1 + mz * mz * f.k2 + f.k3);
-        cnt = subsample_count<SS_QUADRIC>(m, sh, f, i, j, k, n, x, q, rechecks);
+        const int lb = block_log2(n, m.twod != 0);
+        cnt = lb ? subsample_blocks<SS_QUADRIC>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks)
+                 : subsample_count<SS_QUADRIC>(m, sh, f, i, j, k, n, x, q, rechecks);
     } else if (kind == SS_BOX) {
         f.k0 = a[0]; f.k1 = a[1];
         f.k2 = prism ? INFINITY : a[2];  // the rectangle has no z extent
         f.Eg = Ep + 2.f * u * (fmaxf(mx, fmaxf(my, prism ? 0.f : mz)) + fmaxf(a[0], fmaxf(a[1], prism ? 0.f : a[2])));
-        cnt = subsample_count<SS_BOX>(m, sh, f, i, j, k, n, x, q, rechecks);
+        const int lb = block_log2(n, m.twod != 0);
+        cnt = lb ? subsample_blocks<SS_BOX>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks)
+                 : subsample_count<SS_BOX>(m, sh, f, i, j, k, n, x, q, rechecks);
     } else {
         cnt = subsample_count<SS_GENERIC>(m, sh, f, i, j, k, n, x, q, rechecks);
     }
@@ -390,7 +492,7 @@ static __device__ __noinline__ void write_features(const ClassifyArgs& A, const 
 // ---- the tile kernel: one warp per chunk of up to chunk_tiles tiles of one solid ------------------------------------------
 constexpr int CLS_WARPS = 8;
 
-template <int TX, int TY, int TZ>
+template <int TX, int TY, int TZ, int METHOD>
 __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
     constexpr int VX = TX + 1, VY = TY + 1, VZ = TZ + 1, NV = VX * VY * VZ, NC = TX * TY * TZ;
     __shared__ uint8_t s_vin[CLS_WARPS][NV];
@@ -501,11 +603,11 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                     out[local_index(a, b, c)] = cls;
                 }
                 // compact the cut candidates of this round
-                const bool is_cut = (cls == 2 || cls == 3) && A.method >= 0;
+                const bool is_cut = (cls == 2 || cls == 3) && METHOD >= 0;
                 const unsigned bal = __ballot_sync(FULL, is_cut);
                 if (is_cut) {
                     cutlist[ncut + __popc(bal & ((1u << lane) - 1u))] = (uint8_t)e;
-                    if (A.method == SDFIBM_FRACTION_REFGEO || A.method == SDFIBM_FRACTION_LEARNED) {
+                    if (METHOD == SDFIBM_FRACTION_REFGEO || METHOD == SDFIBM_FRACTION_LEARNED) {
                         const int v0 = a + VX * (b + VY * c);
                         vneed[v0] = 1; vneed[v0 + 1] = 1; vneed[v0 + VX] = 1; vneed[v0 + VX + 1] = 1;
                         vneed[v0 + VX * VY] = 1; vneed[v0 + VX * VY + 1] = 1; vneed[v0 + VX * VY + VX] = 1;
@@ -516,7 +618,7 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
             }
             if (ncut == 0) continue;
             __syncwarp();
-            if (A.method == SDFIBM_FRACTION_REFGEO || A.method == SDFIBM_FRACTION_LEARNED) {
+            if (METHOD == SDFIBM_FRACTION_REFGEO || METHOD == SDFIBM_FRACTION_LEARNED) {
                 // Solid::phi once per vertex next to a cut candidate.  The needed vertices are compacted first so
                 // every FP64 instruction runs on a full warp; the local point is the solid's FP64 local map applied to
                 // small integer offsets from the bbox corner.
@@ -534,6 +636,16 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                 for (int u = lane; u < nneed; u += 32) {
                     const int v = vlist[u];
                     const int a = v % VX, b = (v / VX) % VY, c = v / (VX * VY);
+                    if (METHOD == SDFIBM_FRACTION_LEARNED) {
+                        // the network's features need ~1e-6 relative accuracy: FP32 local point and distance
+                        const float dx = tf.bx + (float)a * m.h32[0], dy = tf.by + (float)b * m.h32[1],
+                                    dz = tf.bz + (float)c * m.h32[2];
+                        const float lx = __fmaf_rn(M[0], dx, __fmaf_rn(M[1], dy, M[2] * dz));
+                        const float ly = __fmaf_rn(M[3], dx, __fmaf_rn(M[4], dy, M[5] * dz));
+                        const float lz = __fmaf_rn(M[6], dx, __fmaf_rn(M[7], dy, M[8] * dz));
+                        vphi[v] = sdf32(sh, lx, ly, lz);
+                        continue;
+                    }
                     const double da = (double)(tx * TX + a), db = (double)(ty * TY + b), dc = (double)(tz * TZ + c);
                     const D3 plc{L[0] + da * L[3] + db * L[6] + dc * L[9], L[1] + da * L[4] + db * L[7] + dc * L[10],
                                  L[2] + da * L[5] + db * L[8] + dc * L[11]};
@@ -543,7 +655,7 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                     vphi[v] = ph;
                 }
                 __syncwarp();
-                if (A.method == SDFIBM_FRACTION_LEARNED) {
+                if (METHOD == SDFIBM_FRACTION_LEARNED) {
                     // features of every cut cell into the network's input buffer; the fraction comes later
                     write_features<TX, TY, TZ>(A, cutlist, ncut, vphi, s,
                                                k.scratch_off + local_index(0, 0, 0), k.ext[0], k.ext[1]);
@@ -601,15 +713,18 @@ __global__ void __launch_bounds__(256) learned_fallback_kernel(FallbackArgs A) {
         const int64_t idx = A.fref_index[slot];
         const SolidK& k = A.sk[s];
         const SolidPlan& pl = A.plan[s];
-        const int64_t local = idx - k.scratch_off;
-        const int64_t la = local % k.ext[0], lb = (local / k.ext[0]) % k.ext[1], lc = local / ((int64_t)k.ext[0] * k.ext[1]);
+        const int local = (int)(idx - k.scratch_off);  // < bbox cells of one solid
+        const int la = local % k.ext[0], lb = (local / k.ext[0]) % k.ext[1], lc = local / (k.ext[0] * k.ext[1]);
+        // the cell's FP32 frame as the classify pass builds a tile's: rounded base plus a whole number of cells
         TileFrame tf;
-        tf.bx = (float)(pl.base[0] + (double)la * A.m.h[0]);
-        tf.by = (float)(pl.base[1] + (double)lb * A.m.h[1]);
-        tf.bz = (float)(pl.base[2] + (double)lc * A.m.h[2]);
-        tf.babs = 2.f * (fabsf(tf.bx) + fabsf(tf.by) + fabsf(tf.bz)) +
-                  (float)(fabs(pl.base[0]) + fabs(pl.base[1]) + fabs(pl.base[2]));
-        tf.e64 = pl.e64;
+        {
+            const float sbx = (float)pl.base[0], sby = (float)pl.base[1], sbz = (float)pl.base[2];
+            const float ofx = (float)la * A.m.h32[0], ofy = (float)lb * A.m.h32[1], ofz = (float)lc * A.m.h32[2];
+            tf.bx = sbx + ofx; tf.by = sby + ofy; tf.bz = sbz + ofz;
+            tf.babs = fabsf(sbx) + fabsf(sby) + fabsf(sbz) + 2.f * (fabsf(ofx) + fabsf(ofy) + fabsf(ofz)) +
+                      fabsf(tf.bx) + fabsf(tf.by) + fabsf(tf.bz);
+            tf.e64 = pl.e64;
+        }
         float M[9];
 #pragma unroll
         for (int r = 0; r < 9; ++r) M[r] = pl.M[r];
@@ -625,7 +740,57 @@ __global__ void __launch_bounds__(256) learned_fallback_kernel(FallbackArgs A) {
 }
 
 // 3-D meshes: 4x4x4-cell tiles; one- and two-layer meshes: 8x8x2
-__global__ void __launch_bounds__(CLS_WARPS * 32) classify_kernel_3d(ClassifyArgs A) { classify_body<4, 4, 4>(A); }
-__global__ void __launch_bounds__(CLS_WARPS * 32) classify_kernel_2d(ClassifyArgs A) { classify_body<8, 8, 2>(A); }
+// one instantiation per fraction method (-1: classification only), so each kernel carries only its own path
+template <int METHOD>
+__global__ void __launch_bounds__(CLS_WARPS * 32) classify_kernel_3d(ClassifyArgs A) { classify_body<4, 4, 4, METHOD>(A); }
+template <int METHOD>
+__global__ void __launch_bounds__(CLS_WARPS * 32) classify_kernel_2d(ClassifyArgs A) { classify_body<8, 8, 2, METHOD>(A); }
+template __global__ void classify_kernel_3d<-1>(ClassifyArgs);
+template __global__ void classify_kernel_3d<SDFIBM_FRACTION_REFGEO>(ClassifyArgs);
+template __global__ void classify_kernel_3d<SDFIBM_FRACTION_SUBSAMPLE>(ClassifyArgs);
+template __global__ void classify_kernel_3d<SDFIBM_FRACTION_LEARNED>(ClassifyArgs);
+template __global__ void classify_kernel_2d<-1>(ClassifyArgs);
+template __global__ void classify_kernel_2d<SDFIBM_FRACTION_REFGEO>(ClassifyArgs);
+template __global__ void classify_kernel_2d<SDFIBM_FRACTION_SUBSAMPLE>(ClassifyArgs);
+template __global__ void classify_kernel_2d<SDFIBM_FRACTION_LEARNED>(ClassifyArgs);
+
+// host side: the instantiation for a method and a tile shape
+void launch_classify(const ClassifyArgs& A, bool flat, int grid, cudaStream_t st) {
+    switch (A.method) {
+        case SDFIBM_FRACTION_REFGEO:
+            if (flat) classify_kernel_2d<SDFIBM_FRACTION_REFGEO><<<grid, CLS_WARPS * 32, 0, st>>>(A);
+            else classify_kernel_3d<SDFIBM_FRACTION_REFGEO><<<grid, CLS_WARPS * 32, 0, st>>>(A);
+            break;
+        case SDFIBM_FRACTION_SUBSAMPLE:
+            if (flat) classify_kernel_2d<SDFIBM_FRACTION_SUBSAMPLE><<<grid, CLS_WARPS * 32, 0, st>>>(A);
+            else classify_kernel_3d<SDFIBM_FRACTION_SUBSAMPLE><<<grid, CLS_WARPS * 32, 0, st>>>(A);
+            break;
+        case SDFIBM_FRACTION_LEARNED:
+            if (flat) classify_kernel_2d<SDFIBM_FRACTION_LEARNED><<<grid, CLS_WARPS * 32, 0, st>>>(A);
+            else classify_kernel_3d<SDFIBM_FRACTION_LEARNED><<<grid, CLS_WARPS * 32, 0, st>>>(A);
+            break;
+        default:
+            if (flat) classify_kernel_2d<-1><<<grid, CLS_WARPS * 32, 0, st>>>(A);
+            else classify_kernel_3d<-1><<<grid, CLS_WARPS * 32, 0, st>>>(A);
+            break;
+    }
+}
+
+// resident CTAs per SM of the instantiation a launch would use
+int classify_occupancy(int method, bool flat) {
+    int occ = 0;
+    const void* f = nullptr;
+    switch (method) {
+        case SDFIBM_FRACTION_REFGEO: f = flat ? (const void*)classify_kernel_2d<SDFIBM_FRACTION_REFGEO>
+                                              : (const void*)classify_kernel_3d<SDFIBM_FRACTION_REFGEO>; break;
+        case SDFIBM_FRACTION_SUBSAMPLE: f = flat ? (const void*)classify_kernel_2d<SDFIBM_FRACTION_SUBSAMPLE>
+                                                 : (const void*)classify_kernel_3d<SDFIBM_FRACTION_SUBSAMPLE>; break;
+        case SDFIBM_FRACTION_LEARNED: f = flat ? (const void*)classify_kernel_2d<SDFIBM_FRACTION_LEARNED>
+                                               : (const void*)classify_kernel_3d<SDFIBM_FRACTION_LEARNED>; break;
+        default: f = flat ? (const void*)classify_kernel_2d<-1> : (const void*)classify_kernel_3d<-1>; break;
+    }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f, CLS_WARPS * 32, 0);
+    return occ;
+}
 
 }  // namespace sdfibm_dev

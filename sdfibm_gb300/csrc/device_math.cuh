@@ -75,6 +75,53 @@ __device__ inline double rect64(const D3& p, double ra, double rb) {
 __device__ inline D3 rot30_64(const D3& p) { return D3{ROT30_C * p.x + 0.5 * p.y, ROT30_C * p.y - 0.5 * p.x, 0.0}; }
 __device__ inline double filter64(double phi) { return (fabs(phi) < SDF_TOL) ? -SDF_TOL : phi; }
 
+// Shape::signedDistance (local frame) in FP32, for the learned fraction's features (which need only ~1e-6
+// relative accuracy): the same formulas as sdf64 below, the reference's filter included.
+__device__ inline float filter32(float phi) { return fabsf(phi) < 1e-8f ? -1e-8f : phi; }
+__device__ inline float rect32(float x, float y, float ra, float rb) {
+    const float dx = fabsf(x) - ra, dy = fabsf(y) - rb;
+    const float dxp = fmaxf(0.f, dx), dyp = fmaxf(0.f, dy);
+    return sqrtf(dxp * dxp + dyp * dyp) + fminf(0.f, fmaxf(dx, dy));
+}
+__device__ inline float sdf32(const ShapeK& s, float px, float py, float pz) {
+    const float* a = s.p32;
+    const float cx = px + s.com32[0], cy = py + s.com32[1], cz = pz + s.com32[2];
+    switch (s.type) {
+        case SDFIBM_SHAPE_CIRCLE: {
+            const float z = s.com32[2];
+            return filter32(sqrtf(cx * cx + cy * cy + z * z) - a[0]);
+        }
+        case SDFIBM_SHAPE_SPHERE: return filter32(sqrtf(cx * cx + cy * cy + cz * cz) - a[0]);
+        case SDFIBM_SHAPE_ELLIPSE: {
+            const float xa = cx * cx * a[2], yb = cy * cy * a[3];
+            return filter32(0.5f * (xa + yb - 1.f) / sqrtf(xa * a[2] + yb * a[3]));
+        }
+        case SDFIBM_SHAPE_ELLIPSOID: {
+            const float xa = px * px * a[3], yb = py * py * a[4], zc = pz * pz * a[5];
+            return filter32(0.5f * (xa + yb + zc - 1.f) / sqrtf(xa * a[3] + yb * a[4] + zc * a[5]));
+        }
+        case SDFIBM_SHAPE_RECTANGLE: return filter32(rect32(cx, cy, a[0], a[1]));
+        case SDFIBM_SHAPE_BOX: {
+            const float dx = fabsf(cx) - a[0], dy = fabsf(cy) - a[1], dz = fabsf(cz) - a[2];
+            const float dxp = fmaxf(0.f, dx), dyp = fmaxf(0.f, dy), dzp = fmaxf(0.f, dz);
+            return filter32(sqrtf(dxp * dxp + dyp * dyp + dzp * dzp) + fminf(0.f, fmaxf(dz, fmaxf(dx, dy))));
+        }
+        case SDFIBM_SHAPE_PLANE: return py;
+        case SDFIBM_SHAPE_CIRCLE_TAIL: {
+            const float d1 = sqrtf(cx * cx + cy * cy) - a[0];
+            return filter32(fminf(d1, rect32(cx - a[4], cy, a[4], a[2])));
+        }
+        case SDFIBM_SHAPE_CIRCLE_TWOTAIL: {
+            const float c = (float)ROT30_C;
+            const float dc = sqrtf(cx * cx + cy * cy) - a[0];
+            const float d1 = rect32(c * cx + 0.5f * cy - a[4], c * cy - 0.5f * cx, a[4], a[2]);
+            const float d2 = rect32(c * cx - 0.5f * cy - a[4], -c * cy - 0.5f * cx, a[4], a[2]);
+            return filter32(fminf(dc, fminf(d1, d2)));
+        }
+    }
+    return 0.f;
+}
+
 // Shape::isInside (local frame), FP64
 __device__ inline bool inside64(const ShapeK& s, const D3& p) {
     const double* a = s.p;

@@ -28,8 +28,8 @@
 namespace sdfibm_dev {
 __global__ void plan_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state* st, SolidPlan* plan, int S,
                             Counters* cnt);
-__global__ void classify_kernel_3d(ClassifyArgs A);
-__global__ void classify_kernel_2d(ClassifyArgs A);
+void launch_classify(const ClassifyArgs& A, bool flat, int grid, cudaStream_t st);
+int classify_occupancy(int method, bool flat);
 __global__ void connect_kernel(MeshK m, const SolidK* sk, SolidPlan* plan, const uint8_t* scratch, uint32_t* gbitmaps,
                                int32_t* in_cell, int32_t* in_solid, int32_t* cut_cell, int32_t* cut_solid,
                                int64_t cap_in, int64_t cap_cut, Counters* cnt, int smem_words, const int32_t* solids);
@@ -279,8 +279,7 @@ extern "C" int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc* mesh, const s
     ClassifyArgs CA;
     CA.m = m; CA.sk = d_sk; CA.st = d_st; CA.plan = d_plan; CA.chunks = d_chunks; CA.total_chunks = nchunks; CA.chunk_tiles = CHUNK_TILES;
     CA.cls = b + OFF_CLS; CA.alpha = nullptr; CA.cnt = d_cnt; CA.method = -1; CA.subsample_n = 0;
-    if (m.nz <= 2) classify_kernel_2d<<<grid, 256, 0, st>>>(CA);
-    else classify_kernel_3d<<<grid, 256, 0, st>>>(CA);
+    launch_classify(CA, m.nz <= 2, grid, st);
     connect_kernel<<<1, 512, 0, st>>>(m, d_sk, d_plan, b + OFF_CLS, reinterpret_cast<uint32_t*>(b + OFF_BITMAP),
                                       reinterpret_cast<int32_t*>(b + OFF_IN_CELL), reinterpret_cast<int32_t*>(b + OFF_IN_SOLID),
                                       reinterpret_cast<int32_t*>(b + OFF_CUT_CELL), reinterpret_cast<int32_t*>(b + OFF_CUT_SOLID),
