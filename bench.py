@@ -493,6 +493,9 @@ def main():
                                           "FP64" if args.exact_forcing else "mixed FP64/FP32"),
                            "n_cells": w.ncells, "n_solids": len(w.solids), "coupling_cells": mean_cells,
                            "bbox_cells": sum(bbox) / len(bbox), "fraction_method": args.method,
+                           "fp64_rechecks": tm["stats"].get("fp64_rechecks"),
+                           "learned_cells": tm["stats"].get("learned_cells"),
+                           "fallback_cells": tm["stats"].get("learned_fallback_cells"),
                            "l2": "flushed (256 MB write) before every timed step", "full_step_ms": full_ms,
                            "evolve_fix_ms": evolve_ms, "cuda_graphs": True,
                            "parallelism": "replicas" if world > 1 else "single GPU"},

@@ -236,10 +236,10 @@ template <int T>
 __device__ __noinline__ int subsample_blocks(const MeshK& m, const ShapeK& sh, const SampleFrame& f, int64_t i,
                                              int64_t j, int64_t k, int n, int lb, float Ep, const D3& x, const Q4& q,
                                              unsigned long long* rechecks) {
-    __shared__ uint8_t s_und[8][128];  // undecided block ids of each warp (blocks of 256 threads, at most 128 blocks)
+    __shared__ uint16_t s_und[8][128];  // undecided blocks of each warp, (ba, bb, bc) packed 5 bits each
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    uint8_t* list = s_und[(threadIdx.x >> 5) & 7];
+    uint16_t* list = s_und[(threadIdx.x >> 5) & 7];
     const bool flat = m.twod != 0;
     const int B = 1 << lb, nb = n >> lb, nbz = flat ? 1 : nb;
     const int lsz = flat ? 2 * lb : 3 * lb;  // log2 of the samples per block
@@ -255,8 +255,10 @@ __device__ __noinline__ int subsample_blocks(const MeshK& m, const ShapeK& sh, c
     for (int base = 0; base < nblocks; base += 32) {
         const int blk = base + lane;
         bool undecided = false;
+        int packed = 0;
         if (blk < nblocks) {
             const int ba = blk % nb, bb = (blk / nb) % nb, bc = blk / (nb * nb);
+            packed = ba | (bb << 5) | (bc << 10);
             const float ta = (float)(2 * ba * B + B) * inv2n, tb = (float)(2 * bb * B + B) * inv2n;
             const float tc = flat ? 0.5f : (float)(2 * bc * B + B) * inv2n;
             const float X = __fmaf_rn(tc, f.szx, __fmaf_rn(tb, f.syx, __fmaf_rn(ta, f.sxx, f.px)));
@@ -268,27 +270,33 @@ __device__ __noinline__ int subsample_blocks(const MeshK& m, const ShapeK& sh, c
             else if (!(gmin > f.Eg)) undecided = true;
         }
         const unsigned mask = __ballot_sync(FULL, undecided);
-        if (undecided) list[nund + __popc(mask & ((1u << lane) - 1u))] = (uint8_t)blk;
+        if (undecided) list[nund + __popc(mask & ((1u << lane) - 1u))] = (uint16_t)packed;
         nund += __popc(mask);
     }
     __syncwarp();
-    const int slots = nund << lsz;
+    // the undecided blocks' columns: one (block, a, b) column per slot, walked along c as subsample_count does
+    const int lcol = 2 * lb;  // log2 of the columns per block
+    const int slots = nund << lcol;
+    const int Bz = flat ? 1 : B;
     for (int e = lane; e < slots; e += 32) {
-        const int blk = list[e >> lsz], sidx = e & ((1 << lsz) - 1);
-        const int ba = blk % nb, bb = (blk / nb) % nb, bc = blk / (nb * nb);
-        const int ia = (ba << lb) + (sidx & (B - 1)), ib = (bb << lb) + ((sidx >> lb) & (B - 1));
-        const int ic = flat ? 0 : (bc << lb) + (sidx >> (2 * lb));
+        const int pk = list[e >> lcol], col = e & ((1 << lcol) - 1);
+        const int ia = ((pk & 31) << lb) + (col & (B - 1)), ib = (((pk >> 5) & 31) << lb) + (col >> lb);
+        const int ic0 = ((pk >> 10) & 31) << lb;
         const float ta = (float)(2 * ia + 1) * inv2n, tb = (float)(2 * ib + 1) * inv2n;
-        const float tc = flat ? 0.5f : (float)(2 * ic + 1) * inv2n;
         const float bx = __fmaf_rn(tb, f.syx, __fmaf_rn(ta, f.sxx, f.px));
         const float by = __fmaf_rn(tb, f.syy, __fmaf_rn(ta, f.sxy, f.py));
         const float bz = __fmaf_rn(tb, f.syz, __fmaf_rn(ta, f.sxz, f.pz));
-        int res = sample_inside<T>(sh, f, __fmaf_rn(tc, f.szx, bx), __fmaf_rn(tc, f.szy, by), __fmaf_rn(tc, f.szz, bz));
-        if (res == 2) {
-            ++*rechecks;
-            res = exact_inside_sample(sh, m, i, j, k, ia, ib, ic, n, x, q);
+        float odd = (float)(2 * ic0 + 1);  // 2*ic + 1, exact
+        for (int dc = 0; dc < Bz; ++dc, odd += 2.f) {
+            const float tc = flat ? 0.5f : odd * inv2n;
+            int res = sample_inside<T>(sh, f, __fmaf_rn(tc, f.szx, bx), __fmaf_rn(tc, f.szy, by),
+                                       __fmaf_rn(tc, f.szz, bz));
+            if (res == 2) {
+                ++*rechecks;
+                res = exact_inside_sample(sh, m, i, j, k, ia, ib, flat ? 0 : ic0 + dc, n, x, q);
+            }
+            cnt += res;
         }
-        cnt += res;
     }
     __syncwarp();
 #pragma unroll
