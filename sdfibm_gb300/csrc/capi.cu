@@ -21,6 +21,8 @@ __global__ void plan_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state*
 void launch_classify(const ClassifyArgs& A, bool flat, int grid, cudaStream_t st);
 int classify_occupancy(int method, bool flat);
 __global__ void learned_fallback_kernel(FallbackArgs A);
+__global__ void recheck_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state* st, const SolidPlan* plan,
+                               const Recheck* rq, int64_t cap, Counters* cnt, float* alpha);
 __global__ void connect_kernel(MeshK m, const SolidK* sk, SolidPlan* plan, const uint8_t* scratch, uint32_t* gbitmaps,
                                int32_t* in_cell, int32_t* in_solid, int32_t* cut_cell, int32_t* cut_solid,
                                int64_t cap_in, int64_t cap_cut, Counters* cnt, int smem_words, const int32_t* solids);
@@ -102,6 +104,9 @@ struct sdfibm_ctx {
     // flood-fill work: solids with small bbox bitmaps (one warp each) and the others (one CTA each)
     int32_t *d_small = nullptr, *d_big = nullptr;
     int n_small = 0, n_big = 0;
+    // SUBSAMPLE points whose FP32 test was undecided, re-evaluated in FP64 on full warps by recheck_kernel
+    Recheck* d_rq = nullptr;
+    int64_t rq_cap = 0;
     // touched-cell lists, double buffered: [cur] is this call's, [cur ^ 1] the previous call's (sparse reset)
     int32_t* d_lists[2][4] = {{nullptr, nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr, nullptr}};
     int cur = 0;
@@ -131,9 +136,13 @@ struct sdfibm_ctx {
     // fields seen by the last interact (sparse reset is only valid on the same buffers)
     const void* last_fields[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     bool interacted = false;
-    // host staging for sdfibm_cuda_interact_host
+    // host staging for sdfibm_cuda_interact_host: U is uploaded on its own copy stream while the enumeration runs
+    // (only couple reads U), the four fields come back on four copy streams
     float *d_U = nullptr, *d_As = nullptr, *d_Fs = nullptr, *d_Ts = nullptr;
     int32_t* d_Ct = nullptr;
+    cudaStream_t copy_st[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev_entry = nullptr, ev_u = nullptr, ev_done = nullptr;
+    cudaEvent_t u_wait = nullptr;  // set while interact_host runs: couple waits for the upload
     int classify_grid = 0, couple_grid = 0;
     // per-kernel events (options.timing)
     static constexpr int MAXEV = 24;
@@ -354,6 +363,7 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
     ctx->connect_smem_bytes = max_smem_words * 4;
     ctx->n_small = (int)small_solids.size();
     ctx->n_big = (int)big_solids.size();
+    ctx->rq_cap = std::min<int64_t>(std::max<int64_t>(scratch / 8, 1 << 20), 1 << 25);
     ctx->cap = std::max<int64_t>(1, bbox_total);
 
     {
@@ -454,6 +464,7 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         dalloc(&ctx->d_sh_keys, (size_t)ctx->sh_mask + 1) || dalloc(&ctx->d_sh_vals, 5 * ((size_t)ctx->sh_mask + 1)) ||
         dalloc(&ctx->d_sh_used, (size_t)ctx->sh_mask + 1) || dalloc(&ctx->d_step, 2) ||
         dalloc(&ctx->d_small, small_solids.size()) || dalloc(&ctx->d_big, big_solids.size()) ||
+        dalloc(&ctx->d_rq, (size_t)ctx->rq_cap) ||
         cudaMallocHost((void**)&ctx->h_cnt, sizeof(Counters)) != cudaSuccess ||
         cudaMallocHost((void**)&ctx->h_ft, std::max<size_t>(1, 6 * (size_t)nsolids) * sizeof(double)) != cudaSuccess) {
         ctx->err = "device allocation failed";
@@ -550,12 +561,14 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
         CK(cudaMemsetAsync(ctx->d_ftacc, 0, sizeof(double) * 6 * S, st));
         plan_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->mesh, ctx->d_sk, ctx->d_st, ctx->d_plan, S, ctx->d_cnt);
         mark(ctx, "plan_kernel");
-        ClassifyArgs CA;
+        ClassifyArgs CA{};
         CA.m = ctx->mesh; CA.sk = ctx->d_sk; CA.st = ctx->d_st; CA.plan = ctx->d_plan; CA.chunks = ctx->d_chunks;
         CA.total_chunks = ctx->total_chunks; CA.cls = ctx->d_scratch; CA.alpha = ctx->d_alpha; CA.cnt = ctx->d_cnt;
         CA.chunk_tiles = ctx->chunk_tiles;
         CA.method = ctx->opt.fraction_method; CA.subsample_n = ctx->opt.subsample_n;
         const bool learned = ctx->opt.fraction_method == SDFIBM_FRACTION_LEARNED;
+        const bool subsample = ctx->opt.fraction_method == SDFIBM_FRACTION_SUBSAMPLE;
+        if (subsample) { CA.rq = ctx->d_rq; CA.rq_cap = ctx->rq_cap; }
         if (learned) {
             CA.feat = ctx->d_feat; CA.feat_cap = ctx->feat_cap; CA.fref_solid = ctx->d_fref_solid;
             CA.fref_index = ctx->d_fref_index; CA.inv_h = (float)(1.0 / ctx->mdesc.h[0]);
@@ -571,14 +584,21 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             ia.tau_grad = ctx->tau_grad; ia.error = &ctx->d_cnt->error;
             launch_mlp_infer(ia, 4 * ctx->num_sms, st);
             mark(ctx, "mlp_infer_kernel");
-            FallbackArgs fa;
+            FallbackArgs fa{};
             fa.m = ctx->mesh; fa.sk = ctx->d_sk; fa.st = ctx->d_st; fa.plan = ctx->d_plan; fa.fb_list = ctx->d_fb;
             fa.fref_solid = ctx->d_fref_solid; fa.fref_index = ctx->d_fref_index; fa.cap = ctx->feat_cap;
             fa.alpha = ctx->d_alpha; fa.cnt = ctx->d_cnt;
             fa.n = ctx->opt.learned_fallback_n > 0 ? ctx->opt.learned_fallback_n : 16;
+            fa.rq = ctx->d_rq; fa.rq_cap = ctx->rq_cap;
             learned_fallback_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(fa);
             mark(ctx, "learned_fallback_kernel");
             launches += 2;
+        }
+        if (learned || subsample) {
+            recheck_kernel<<<ctx->num_sms * 4, 256, 0, st>>>(ctx->mesh, ctx->d_sk, ctx->d_st, ctx->d_plan, ctx->d_rq,
+                                                              ctx->rq_cap, ctx->d_cnt, ctx->d_alpha);
+            mark(ctx, "recheck_kernel");
+            ++launches;
         }
         if (ctx->n_small > 0)
             connect_small_kernel<<<(ctx->n_small + 7) / 8, 256, 0, st>>>(
@@ -602,14 +622,21 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
         mark(ctx, "reset_kernel");
         ++launches;
     }
+    if (ctx->u_wait) CK(cudaStreamWaitEvent(st, ctx->u_wait, 0));  // U staged on a copy stream (interact_host)
     if (S > 0) {
-        CoupleArgs A;
+        CoupleArgs A{};
         A.m = ctx->mesh; A.sk = ctx->d_sk; A.st = ctx->d_st; A.plan = ctx->d_plan;
         A.in_cell = ctx->in_cell(); A.in_solid = ctx->in_solid(); A.cut_cell = ctx->cut_cell();
         A.cut_solid = ctx->cut_solid(); A.alpha = ctx->d_alpha; A.U = U; A.As = As; A.Fs = Fs; A.Ts = Ts; A.Ct = Ct;
         A.ftacc = ctx->d_ftacc; A.cnt = ctx->d_cnt; A.step = ctx->d_step;
         A.method = ctx->opt.fraction_method; A.subsample_n = ctx->opt.subsample_n;
         A.exact_forcing = ctx->opt.exact_forcing;
+        {
+            const int nc = ctx->opt.fraction_method == SDFIBM_FRACTION_LEARNED
+                               ? (ctx->opt.learned_fallback_n > 0 ? ctx->opt.learned_fallback_n : 16)
+                               : ctx->opt.subsample_n;
+            A.count_samples = nc * nc * (ctx->mesh.twod ? 1 : nc);
+        }
         A.sh_keys = ctx->d_sh_keys; A.sh_vals = ctx->d_sh_vals; A.sh_used = ctx->d_sh_used; A.sh_mask = ctx->sh_mask;
         couple_kernel<<<ctx->couple_grid, 256, 0, st>>>(A);
         mark(ctx, "couple_kernel");
@@ -682,7 +709,7 @@ static int run_graph(sdfibm_ctx* ctx, sdfibm_ctx::Graph& g, bool key_changed, co
 }
 
 static bool graphs_on(const sdfibm_ctx* ctx) {
-    return ctx->opt.graphs && ctx->stream != nullptr && !ctx->opt.timing && !ctx->graphs_failed;
+    return ctx->opt.graphs && ctx->stream != nullptr && !ctx->opt.timing && !ctx->graphs_failed && !ctx->u_wait;
 }
 
 int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs, float* Ts,
@@ -748,16 +775,32 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
             dalloc(&ctx->d_Ct, N))
             return fail(ctx, SDFIBM_ERR_CUDA, "staging allocation failed");
     }
-    CK(cudaMemcpyAsync(ctx->d_U, U, sizeof(float) * 3 * N, cudaMemcpyHostToDevice, st));
-    std::vector<double> ft(6 * (size_t)std::max(1, ctx->S));
+    if (!ctx->ev_u) {
+        for (auto& c : ctx->copy_st) CK(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&ctx->ev_entry, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ctx->ev_u, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming));
+    }
+    // upload U once the previous work on the stream (which may still read d_U) is done; couple waits for it
+    CK(cudaEventRecord(ctx->ev_entry, st));
+    CK(cudaStreamWaitEvent(ctx->copy_st[0], ctx->ev_entry, 0));
+    CK(cudaMemcpyAsync(ctx->d_U, U, sizeof(float) * 3 * N, cudaMemcpyHostToDevice, ctx->copy_st[0]));
+    CK(cudaEventRecord(ctx->ev_u, ctx->copy_st[0]));
+    ctx->u_wait = ctx->ev_u;
     int rc = sdfibm_cuda_interact(ctx, time, dt, ctx->d_U, ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, nullptr);
+    ctx->u_wait = nullptr;
     if (rc) return rc;
-    CK(cudaMemcpyAsync(As, ctx->d_As, sizeof(float) * N, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(Fs, ctx->d_Fs, sizeof(float) * 3 * N, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(Ts, ctx->d_Ts, sizeof(float) * N, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(Ct, ctx->d_Ct, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, st));
+    CK(cudaEventRecord(ctx->ev_done, st));
+    void* dst[4] = {As, Fs, Ts, Ct};
+    const void* src[4] = {ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct};
+    const size_t bytes[4] = {sizeof(float) * N, sizeof(float) * 3 * N, sizeof(float) * N, sizeof(int32_t) * N};
+    for (int i = 0; i < 4; ++i) {
+        CK(cudaStreamWaitEvent(ctx->copy_st[i], ctx->ev_done, 0));
+        CK(cudaMemcpyAsync(dst[i], src[i], bytes[i], cudaMemcpyDeviceToHost, ctx->copy_st[i]));
+    }
     if (ctx->S > 0) CK(cudaMemcpyAsync(ctx->h_ft, ctx->d_ft, sizeof(double) * 6 * ctx->S, cudaMemcpyDeviceToHost, st));
     rc = sync_counters(ctx);
+    for (auto& c : ctx->copy_st) CK(cudaStreamSynchronize(c));
     if (rc) return rc;
     if (FT) std::memcpy(FT, ctx->h_ft, sizeof(double) * 6 * ctx->S);
     return SDFIBM_OK;
@@ -995,6 +1038,12 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
         if (p) cudaFree(p);
     if (ctx->d_step) cudaFree(ctx->d_step);
     if (ctx->d_small) cudaFree(ctx->d_small);
+    if (ctx->d_rq) cudaFree(ctx->d_rq);
+    for (auto& c : ctx->copy_st)
+        if (c) cudaStreamDestroy(c);
+    if (ctx->ev_entry) cudaEventDestroy(ctx->ev_entry);
+    if (ctx->ev_u) cudaEventDestroy(ctx->ev_u);
+    if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
     if (ctx->d_big) cudaFree(ctx->d_big);
     for (auto& g : ctx->igraph)
         if (g.valid) cudaGraphExecDestroy(g.exec);

@@ -141,6 +141,29 @@ static __device__ __noinline__ int exact_inside_sample(const ShapeK& sh, const M
     return inside64(sh, world2local(p, x, q)) ? 1 : 0;
 }
 
+// Where an undecided SUBSAMPLE point goes: appended to the recheck list (counted later by recheck_kernel) when there
+// is room, else re-evaluated here.
+struct Defer {
+    Recheck* rq;
+    int64_t cap;
+    int32_t* count;
+    int64_t idx;
+    int32_t solid;
+};
+static __device__ __forceinline__ int undecided_sample(const Defer* df, const ShapeK& sh, const MeshK& m, int64_t i,
+                                                       int64_t j, int64_t k, int a, int b, int c3, int n, const D3& x,
+                                                       const Q4& q) {
+    if (df) {
+        const int slot = atomicAdd(df->count, 1);
+        if (slot < df->cap) {
+            df->rq[slot] = Recheck{df->idx, df->solid,
+                                   (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)c3 << 16) | ((uint32_t)n << 24)};
+            return 0;
+        }
+    }
+    return exact_inside_sample(sh, m, i, j, k, a, b, c3, n, x, q);
+}
+
 // the reference's FP64 Solid::phi of mesh point (I,J,K), out of line
 static __device__ __noinline__ float exact_phi_point(const ShapeK& sh, const MeshK& m, int64_t I, int64_t J, int64_t K,
                                               const D3& x, const Q4& q) {
@@ -178,7 +201,7 @@ __device__ __forceinline__ int sample_inside(const ShapeK& sh, const SampleFrame
 template <int T>
 __device__ __forceinline__ int subsample_count(const MeshK& m, const ShapeK& sh, const SampleFrame& f, int64_t i,
                                                int64_t j, int64_t k, int n, const D3& x, const Q4& q,
-                                               unsigned long long* rechecks) {
+                                               unsigned long long* rechecks, const Defer* df) {
     const int lane = threadIdx.x & 31;
     const int nzs = m.twod ? 1 : n;
     const float inv2n = 1.0f / (float)(2 * n);
@@ -199,7 +222,7 @@ __device__ __forceinline__ int subsample_count(const MeshK& m, const ShapeK& sh,
                                      __fmaf_rn(tc, f.szz, bz));
             if (r == 2) {
                 ++*rechecks;
-                r = exact_inside_sample(sh, m, i, j, k, ia, ib, c3, n, x, q);
+                r = undecided_sample(df, sh, m, i, j, k, ia, ib, c3, n, x, q);
             }
             cnt += r;
         }
@@ -235,7 +258,7 @@ __device__ __forceinline__ void block_bounds(const SampleFrame& f, float X, floa
 template <int T>
 __device__ __noinline__ int subsample_blocks(const MeshK& m, const ShapeK& sh, const SampleFrame& f, int64_t i,
                                              int64_t j, int64_t k, int n, int lb, float Ep, const D3& x, const Q4& q,
-                                             unsigned long long* rechecks) {
+                                             unsigned long long* rechecks, const Defer* df) {
     __shared__ uint16_t s_und[8][128];  // undecided blocks of each warp, (ba, bb, bc) packed 5 bits each
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -293,7 +316,7 @@ __device__ __noinline__ int subsample_blocks(const MeshK& m, const ShapeK& sh, c
                                        __fmaf_rn(tc, f.szz, bz));
             if (res == 2) {
                 ++*rechecks;
-                res = exact_inside_sample(sh, m, i, j, k, ia, ib, flat ? 0 : ic0 + dc, n, x, q);
+                res = undecided_sample(df, sh, m, i, j, k, ia, ib, flat ? 0 : ic0 + dc, n, x, q);
             }
             cnt += res;
         }
@@ -304,9 +327,10 @@ __device__ __noinline__ int subsample_blocks(const MeshK& m, const ShapeK& sh, c
     return cnt;
 }
 
-// log2 of the block edge for block skipping (power of two dividing n, at most 128 blocks), 0: sample every point
+// log2 of the block edge for block skipping (power of two of at least 4 dividing n, at most 128 blocks), 0: sample
+// every point (blocks of 2 samples per axis cost more to test than they save)
 __device__ inline int block_log2(int n, bool flat) {
-    for (int lb = 1; lb <= 3; ++lb) {
+    for (int lb = 2; lb <= 3; ++lb) {
         const int B = 1 << lb;
         if (n % B) continue;
         const int nb = n / B;
@@ -315,9 +339,12 @@ __device__ inline int block_log2(int n, bool flat) {
     return 0;
 }
 
-static __device__ __noinline__ float subsample_warp(const MeshK& m, const ShapeK& sh, const float* M, const TileFrame& tf,
-                                                    int a0, int b0, int c0, const D3& x, const Q4& q, int64_t i,
-                                                    int64_t j, int64_t k, int n, unsigned long long* rechecks) {
+// Inside count of the cell's n^3 (n^2 on one-layer meshes) lattice; with a Defer the undecided points are not counted
+// here but appended to the recheck list.
+static __device__ __noinline__ int subsample_warp(const MeshK& m, const ShapeK& sh, const float* M, const TileFrame& tf,
+                                                  int a0, int b0, int c0, const D3& x, const Q4& q, int64_t i,
+                                                  int64_t j, int64_t k, int n, unsigned long long* rechecks,
+                                                  const Defer* df) {
     const float u = U32;
     const float hx = m.h32[0], hy = m.h32[1], hz = m.h32[2];
     const float ox = (float)a0 * hx, oy = (float)b0 * hy, oz = (float)c0 * hz;  // cell corner within the tile
@@ -376,20 +403,24 @@ static __device__ __noinline__ float subsample_warp(const MeshK& m, const ShapeK
         f.Eg = (2.f * (mx * f.k0 + my * f.k1 + mz * f.k2) + Ep * (f.k0 + f.k1 + f.k2)) * Ep +
                10.f * u * (mx * mx * f.k0 + my * my * f.k1 + mz * mz * f.k2 + f.k3);
         const int lb = block_log2(n, m.twod != 0);
-        cnt = lb ? subsample_blocks<SS_QUADRIC>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks)
-                 : subsample_count<SS_QUADRIC>(m, sh, f, i, j, k, n, x, q, rechecks);
+        cnt = lb ? subsample_blocks<SS_QUADRIC>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks, df)
+                 : subsample_count<SS_QUADRIC>(m, sh, f, i, j, k, n, x, q, rechecks, df);
     } else if (kind == SS_BOX) {
         f.k0 = a[0]; f.k1 = a[1];
         f.k2 = prism ? INFINITY : a[2];  // the rectangle has no z extent
         f.Eg = Ep + 2.f * u * (fmaxf(mx, fmaxf(my, prism ? 0.f : mz)) + fmaxf(a[0], fmaxf(a[1], prism ? 0.f : a[2])));
         const int lb = block_log2(n, m.twod != 0);
-        cnt = lb ? subsample_blocks<SS_BOX>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks)
-                 : subsample_count<SS_BOX>(m, sh, f, i, j, k, n, x, q, rechecks);
+        cnt = lb ? subsample_blocks<SS_BOX>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks, df)
+                 : subsample_count<SS_BOX>(m, sh, f, i, j, k, n, x, q, rechecks, df);
     } else {
-        cnt = subsample_count<SS_GENERIC>(m, sh, f, i, j, k, n, x, q, rechecks);
+        cnt = subsample_count<SS_GENERIC>(m, sh, f, i, j, k, n, x, q, rechecks, df);
     }
-    const int nzs = m.twod ? 1 : n;
-    return __fdiv_rn((float)cnt, (float)(n * n * nzs));  // cnt and n^3 are exact in FP32: one correct rounding
+    return cnt;
+}
+
+// the fraction of a complete count (cnt and n^3 are exact in FP32: one correct rounding)
+__device__ inline float count_fraction(const MeshK& m, int cnt, int n) {
+    return __fdiv_rn((float)cnt, (float)(n * n * (m.twod ? 1 : n)));
 }
 
 // ---- signed distance for REF-GEO: FP64 where it decides, FP32 where it only scales ------------------------------------
@@ -687,9 +718,11 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                 for (int u = 0; u < ncut; ++u) {
                     const int e = cutlist[u];
                     const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
-                    const float al = subsample_warp(m, sh, M, tf, a, b, c, x, q, I0 + a, J0 + b, K0 + c,
-                                                    A.subsample_n, &rechecks);
-                    if (lane == 0) alpha[local_index(a, b, c)] = al;
+                    const int64_t li = local_index(a, b, c);
+                    const Defer df{A.rq, A.rq_cap, &A.cnt->n_recheck, k.scratch_off + li, s};
+                    const int cnt = subsample_warp(m, sh, M, tf, a, b, c, x, q, I0 + a, J0 + b, K0 + c,
+                                                   A.subsample_n, &rechecks, A.rq ? &df : nullptr);
+                    if (lane == 0) alpha[li] = A.rq ? -1.f - (float)cnt : count_fraction(m, cnt, A.subsample_n);
                 }
             }
             __syncwarp();
@@ -738,13 +771,35 @@ __global__ void __launch_bounds__(256) learned_fallback_kernel(FallbackArgs A) {
         for (int r = 0; r < 9; ++r) M[r] = pl.M[r];
         const Q4 q = state_quat(A.st[s]);
         const D3 x = state_pos(A.st[s]);
-        const float al = subsample_warp(A.m, k.shape, M, tf, 0, 0, 0, x, q, pl.lo[0] + la, pl.lo[1] + lb,
-                                        pl.lo[2] + lc, A.n, &rechecks);
-        if (lane == 0) A.alpha[idx] = al;
+        const Defer df{A.rq, A.rq_cap, &A.cnt->n_recheck, idx, s};
+        const int cnt = subsample_warp(A.m, k.shape, M, tf, 0, 0, 0, x, q, pl.lo[0] + la, pl.lo[1] + lb,
+                                       pl.lo[2] + lc, A.n, &rechecks, A.rq ? &df : nullptr);
+        if (lane == 0) A.alpha[idx] = A.rq ? -1.f - (float)cnt : count_fraction(A.m, cnt, A.n);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);
     if (lane == 0 && rechecks) atomicAdd(&A.cnt->exact_rechecks, rechecks);
+}
+
+// The deferred SUBSAMPLE points: one per thread, the reference's FP64 point and inside test, an inside point lowers the
+// cell's encoded count (-(1 + count)) by one.
+__global__ void __launch_bounds__(256) recheck_kernel(MeshK m, const SolidK* __restrict__ sk,
+                                                      const sdfibm_solid_state* __restrict__ st,
+                                                      const SolidPlan* __restrict__ plan,
+                                                      const Recheck* __restrict__ rq, int64_t cap, Counters* cnt,
+                                                      float* __restrict__ alpha) {
+    const int64_t n = min((int64_t)cnt->n_recheck, cap);
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const Recheck r = rq[e];
+        const SolidK& k = sk[r.solid];
+        const SolidPlan& pl = plan[r.solid];
+        const int local = (int)(r.idx - k.scratch_off);
+        const int la = local % k.ext[0], lb = (local / k.ext[0]) % k.ext[1], lc = local / (k.ext[0] * k.ext[1]);
+        const int a = r.sample & 255, b = (r.sample >> 8) & 255, c = (r.sample >> 16) & 255, ns = r.sample >> 24;
+        const int in = exact_inside_sample(k.shape, m, pl.lo[0] + la, pl.lo[1] + lb, pl.lo[2] + lc, a, b, c, ns,
+                                           state_pos(st[r.solid]), state_quat(st[r.solid]));
+        if (in) atomicAdd(alpha + r.idx, -1.f);
+    }
 }
 
 // 3-D meshes: 4x4x4-cell tiles; one- and two-layer meshes: 8x8x2

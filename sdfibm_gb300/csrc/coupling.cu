@@ -668,6 +668,8 @@ __global__ void __launch_bounds__(CPL_THREADS) couple_kernel(CoupleArgs A) {
                 const int32_t* lo = A.plan[s].lo;
                 const int64_t li = (i - lo[0]) + (int64_t)ks.ext[0] * ((j - lo[1]) + (int64_t)ks.ext[1] * (k - lo[2]));
                 alpha = A.alpha[ks.scratch_off + li];
+                // a SUBSAMPLE count whose undecided points were rechecked on full warps
+                if (alpha < 0.f) alpha = __fdiv_rn(-alpha - 1.f, (float)A.count_samples);
             }
             const float Ux = A.U[c], Uy = A.U[N + c], Uz = A.U[2 * N + c];
             float fsx, fsy, fsz;
@@ -770,7 +772,7 @@ __global__ void begin_kernel(Counters* cnt) {
     cnt->classify_next = 0; cnt->couple_next = 0; cnt->finalize_next = 0;
     cnt->n_inside = 0; cnt->n_cut = 0; cnt->n_shared = 0;
     cnt->exact_rechecks = 0; cnt->bbox_cells = 0;
-    cnt->n_feat = 0; cnt->n_fb = 0;
+    cnt->n_feat = 0; cnt->n_fb = 0; cnt->n_recheck = 0;
 }
 
 // F = rho_f * V / dt * sum f, T = rho_f * V / dt * sum (C - x) x f  (solidcloud.cpp:411-421)

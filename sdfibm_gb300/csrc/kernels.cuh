@@ -103,10 +103,20 @@ struct Counters {
     int64_t list_cap;         // capacity of each touched-cell list (set once at create)
     int32_t n_feat;           // LEARNED: cut cells whose features the classify pass wrote this call
     int32_t n_fb;             // LEARNED: of those, cells outside the model's band (SUBSAMPLE fallback)
+    int32_t n_recheck;        // SUBSAMPLE points left to recheck_kernel this call
+    int32_t pad3;
 };
 
 // list lengths clamped to the capacity (a capacity error leaves the counters above what was written)
 __host__ __device__ inline int32_t clamp_len(int32_t n, int64_t cap) { return (int32_t)(n < cap ? n : cap); }
+
+// A SUBSAMPLE point whose FP32 test was undecided, left for recheck_kernel: the FP64 re-evaluations then run on full
+// warps instead of one lane at a time.  sample = ia | ib << 8 | ic << 16 | n << 24.
+struct Recheck {
+    int64_t idx;     // index into the fraction array (which holds -(1 + decided inside count) meanwhile)
+    int32_t solid;
+    uint32_t sample;
+};
 
 // Time-step parameters the kernels read from device memory; set_step_kernel writes them at the head of a call, so a
 // captured graph replays with new values after one kernel-node update.
@@ -136,6 +146,7 @@ struct CoupleArgs {
     double* ftacc;  // [S][6] sums of f*V/dt and (C-x)^f*V/dt
     Counters* cnt;
     const StepParams* step;
+    int count_samples;   // a negative alpha is -(1 + inside count) out of this many SUBSAMPLE points
     int method;
     int subsample_n;
     int exact_forcing;
@@ -174,6 +185,8 @@ struct ClassifyArgs {
     int32_t* fref_solid;
     int64_t* fref_index;  // index into alpha
     float inv_h;          // 1 / h (x spacing) of the feature scaling
+    Recheck* rq;          // deferred SUBSAMPLE rechecks (nullptr: re-evaluate in place)
+    int64_t rq_cap;
 };
 
 // LEARNED: cells left to SUBSAMPLE by the network's confidence band
@@ -189,6 +202,8 @@ struct FallbackArgs {
     float* alpha;
     Counters* cnt;
     int n;                     // samples per axis
+    Recheck* rq;
+    int64_t rq_cap;
 };
 
 // UGrid (src/libcollision/ugrid.h:14-58): bbox of the mesh, spacing 2*max radiusB, row-major i*ny*nz + j*nz + k

@@ -276,7 +276,7 @@ extern "C" int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc* mesh, const s
     if (cudaGetDevice(&dev) != cudaSuccess) return SDFIBM_ERR_CUDA;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int grid = nchunks < 4 * (sms > 0 ? sms : 1) ? nchunks : 4 * (sms > 0 ? sms : 1);
-    ClassifyArgs CA;
+    ClassifyArgs CA{};
     CA.m = m; CA.sk = d_sk; CA.st = d_st; CA.plan = d_plan; CA.chunks = d_chunks; CA.total_chunks = nchunks; CA.chunk_tiles = CHUNK_TILES;
     CA.cls = b + OFF_CLS; CA.alpha = nullptr; CA.cnt = d_cnt; CA.method = -1; CA.subsample_n = 0;
     launch_classify(CA, m.nz <= 2, grid, st);
