@@ -49,15 +49,17 @@ __global__ void evolve_independent_kernel(const SolidK* sk, sdfibm_solid_state* 
                                           const StepParams* step, double rho_f, D3 g);
 __global__ void evolve_pre_kernel(const SolidK* sk, sdfibm_solid_state* st, int S, const StepParams* step, double rho_f, D3 g,
                                   GridK gk, int64_t* hashes, int32_t* counts, FineGridK fg, int32_t* fcounts, int mode,
-                                  int coarse_needed);
-__global__ void fine_scatter_kernel(const SolidK* sk, const sdfibm_solid_state* st, int S, GridK gk,
-                                    const int64_t* hashes, FineGridK fg, int32_t* fcursor, int32_t* flist, int mode,
+                                  int coarse_needed, CollRec* recs);
+__global__ void fine_scatter_kernel(const CollRec* recs, int S, FineGridK fg, int32_t* fcursor, int32_t* flist,
                                     Counters* cnt);
 __global__ void grid_scan_kernel(const int32_t* counts, int32_t* start, int32_t* cursor, int64_t ncell);
+__global__ void scan_blocks_kernel(const int32_t* counts, int32_t* start, int32_t* sums, int64_t ncell);
+__global__ void scan_add_kernel(int32_t* start, int32_t* cursor, const int32_t* sums_excl, int64_t ncell,
+                                int64_t nblocks);
 __global__ void grid_scatter_kernel(const int64_t* hashes, int32_t* cursor, int32_t* list, int S, int64_t ncell);
 __global__ void collide_kernel(const SolidK* sk, sdfibm_solid_state* st, int S, GridK gk, const int64_t* hashes,
                                const int32_t* start, const int32_t* list, int mode, FineGridK fg, const int32_t* fstart,
-                               const int32_t* flist, const int32_t* planes, int nplanes);
+                               const int32_t* flist, const int32_t* planes, int nplanes, const CollRec* recs);
 __global__ void move_kernel(const SolidK* sk, sdfibm_solid_state* st, int S, const StepParams* step);
 __global__ void store_old_kernel(sdfibm_solid_state* st, int S);
 __global__ void ft_to_state_kernel(const double* ft, sdfibm_solid_state* st, int S);
@@ -128,10 +130,12 @@ struct sdfibm_ctx {
     bool grid_active = false;
     GridK gk{};
     int64_t* d_hash = nullptr;
+    CollRec* d_recs = nullptr;  // per-solid collision records of the current sub-step
     int32_t *d_gcount = nullptr, *d_gstart = nullptr, *d_gcursor = nullptr, *d_glist = nullptr;
     // fine broad phase of the sphere-like solids and the list of plane-like ones (contact law id 0)
     FineGridK fg{};
     int32_t *d_fcount = nullptr, *d_fstart = nullptr, *d_fcursor = nullptr, *d_flist = nullptr, *d_planes = nullptr;
+    int32_t *d_fsums = nullptr, *d_fsums_excl = nullptr;  // block sums of the multi-block scans of the two grids
     int nplanes = 0;
     // fields seen by the last interact (sparse reset is only valid on the same buffers)
     const void* last_fields[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -471,9 +475,11 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         return bail(SDFIBM_ERR_CUDA);
     }
     if (ctx->grid_active) {
-        if (dalloc(&ctx->d_hash, nsolids) || dalloc(&ctx->d_gcount, ctx->gk.ncell) ||
+        if (dalloc(&ctx->d_hash, nsolids) || dalloc(&ctx->d_recs, nsolids) || dalloc(&ctx->d_gcount, ctx->gk.ncell) ||
             dalloc(&ctx->d_gstart, ctx->gk.ncell + 1) || dalloc(&ctx->d_gcursor, ctx->gk.ncell) ||
-            dalloc(&ctx->d_glist, nsolids)) {
+            dalloc(&ctx->d_glist, nsolids) ||
+            dalloc(&ctx->d_fsums, std::max(ctx->gk.ncell, ctx->fg.ncell) / 1024 + 2) ||
+            dalloc(&ctx->d_fsums_excl, std::max(ctx->gk.ncell, ctx->fg.ncell) / 1024 + 2)) {
             ctx->err = "device allocation failed (collision grid)";
             return bail(SDFIBM_ERR_CUDA);
         }
@@ -806,6 +812,20 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
     return SDFIBM_OK;
 }
 
+// Exclusive scan of per-cell counts into start (ncell + 1 entries, the total last) and cursor: one block for small
+// grids, else per-1024-cell block scans, one block over their sums, and the block offsets added back.
+static void scan_counts(sdfibm_ctx* ctx, const int32_t* counts, int32_t* start, int32_t* cursor, int64_t ncell) {
+    cudaStream_t st = ctx->stream;
+    if (ncell <= 16384) {
+        grid_scan_kernel<<<1, 1024, 0, st>>>(counts, start, cursor, ncell);
+        return;
+    }
+    const int64_t nb = (ncell + 1023) / 1024;
+    scan_blocks_kernel<<<(unsigned)nb, 1024, 0, st>>>(counts, start, ctx->d_fsums, ncell);
+    grid_scan_kernel<<<1, 1024, 0, st>>>(ctx->d_fsums, ctx->d_fsums_excl, ctx->d_fsums_excl, nb);
+    scan_add_kernel<<<(unsigned)nb, 1024, 0, st>>>(start, cursor, ctx->d_fsums_excl, ncell, nb);
+}
+
 // The device work of one evolve (all sub-steps) on the context's stream: what a captured graph holds.
 static int enqueue_evolve(sdfibm_ctx* ctx, double time, double dt) {
     const int S = ctx->S;
@@ -813,7 +833,8 @@ static int enqueue_evolve(sdfibm_ctx* ctx, double time, double dt) {
     const int nsub = ctx->nsub;
     StepParams* step = ctx->d_step + 1;
     const D3 g{ctx->opt.gravity[0], ctx->opt.gravity[1], ctx->opt.gravity[2]};
-    const int B = 128, G = (S + B - 1) / B;
+    // thread-per-solid kernels are FP64-pipe bound: small blocks spread a few thousand solids over every SM
+    const int B = S <= ctx->num_sms * 4 * 64 ? 32 : 128, G = (S + B - 1) / B;
     set_step_kernel<<<1, 1, 0, st>>>(step, time, dt, nsub, 0.0);
     if (!ctx->grid_active) {
         evolve_independent_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, nsub, step, ctx->opt.rho_f, g);
@@ -826,16 +847,17 @@ static int enqueue_evolve(sdfibm_ctx* ctx, double time, double dt) {
             if (coarse) CK(cudaMemsetAsync(ctx->d_gcount, 0, sizeof(int32_t) * gk.ncell, st));
             CK(cudaMemsetAsync(ctx->d_fcount, 0, sizeof(int32_t) * fg.ncell, st));
             evolve_pre_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, step, ctx->opt.rho_f, g, gk, ctx->d_hash,
-                                               ctx->d_gcount, fg, ctx->d_fcount, mode, coarse);
+                                               ctx->d_gcount, fg, ctx->d_fcount, mode, coarse, ctx->d_recs);
             if (coarse) {
-                grid_scan_kernel<<<1, 1024, 0, st>>>(ctx->d_gcount, ctx->d_gstart, ctx->d_gcursor, gk.ncell);
+                scan_counts(ctx, ctx->d_gcount, ctx->d_gstart, ctx->d_gcursor, gk.ncell);
                 grid_scatter_kernel<<<G, B, 0, st>>>(ctx->d_hash, ctx->d_gcursor, ctx->d_glist, S, gk.ncell);
             }
-            grid_scan_kernel<<<1, 1024, 0, st>>>(ctx->d_fcount, ctx->d_fstart, ctx->d_fcursor, fg.ncell);
-            fine_scatter_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, gk, ctx->d_hash, fg, ctx->d_fcursor,
-                                                 ctx->d_flist, mode, ctx->d_cnt);
-            collide_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, gk, ctx->d_hash, ctx->d_gstart, ctx->d_glist, mode,
-                                            fg, ctx->d_fstart, ctx->d_flist, ctx->d_planes, ctx->nplanes);
+            scan_counts(ctx, ctx->d_fcount, ctx->d_fstart, ctx->d_fcursor, fg.ncell);
+            const unsigned GW = (unsigned)(((int64_t)S * 32 + 255) / 256);  // one warp per solid
+            fine_scatter_kernel<<<GW, 256, 0, st>>>(ctx->d_recs, S, fg, ctx->d_fcursor, ctx->d_flist, ctx->d_cnt);
+            collide_kernel<<<GW, 256, 0, st>>>(
+                ctx->d_sk, ctx->d_st, S, gk, ctx->d_hash, ctx->d_gstart, ctx->d_glist, mode, fg, ctx->d_fstart,
+                ctx->d_flist, ctx->d_planes, ctx->nplanes, ctx->d_recs);
             move_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, step);
         }
         store_old_kernel<<<G, B, 0, st>>>(ctx->d_st, S);
@@ -1039,6 +1061,9 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
     if (ctx->d_step) cudaFree(ctx->d_step);
     if (ctx->d_small) cudaFree(ctx->d_small);
     if (ctx->d_rq) cudaFree(ctx->d_rq);
+    if (ctx->d_fsums) cudaFree(ctx->d_fsums);
+    if (ctx->d_recs) cudaFree(ctx->d_recs);
+    if (ctx->d_fsums_excl) cudaFree(ctx->d_fsums_excl);
     for (auto& c : ctx->copy_st)
         if (c) cudaStreamDestroy(c);
     if (ctx->ev_entry) cudaEventDestroy(ctx->ev_entry);

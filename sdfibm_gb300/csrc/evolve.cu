@@ -192,48 +192,53 @@ __device__ inline int64_t fine_index(const FineGridK& fg, int i, int j, int k) {
 }
 
 // forces of one sub-step, the UGrid key of every solid (UGrid::insert, ugrid.h:31-34) with the coarse counts (only
-// needed by plane-like solids, which search their 27 coarse neighbours), and the fine-grid counts of the sphere-like
-// solids whose key is on the grid (the reference never pairs the others)
+// needed by plane-like solids, which search their 27 coarse neighbours), the fine-grid counts of the sphere-like
+// solids whose key is on the grid (the reference never pairs the others) and the solid's collision record
 __global__ void evolve_pre_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state* st, int S,
                                   const StepParams* step, double rho_f, D3 g, GridK gk, int64_t* __restrict__ hashes,
                                   int32_t* __restrict__ counts, FineGridK fg, int32_t* __restrict__ fcounts, int mode,
-                                  int coarse_needed) {
+                                  int coarse_needed, CollRec* __restrict__ recs) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= S) return;
     pre_forces(sk[s], st[s], step->time, rho_f, g);
     const D3 c = ld3(st[s].pos);
     const int64_t h = grid_hash(gk, c);
     hashes[s] = h;
-    if (h < 0 || h >= gk.ncell) return;
-    if (coarse_needed) atomicAdd(counts + h, 1);
-    const int id = coll_id(sk[s], mode);
-    if (id != 1 && id != 2) return;
-    int lo[3], hi[3];
-    fine_range(fg, c, sk[s].radiusB, lo, hi);
-    for (int k = lo[2]; k <= hi[2]; ++k)
-        for (int j = lo[1]; j <= hi[1]; ++j)
-            for (int i = lo[0]; i <= hi[0]; ++i) atomicAdd(fcounts + fine_index(fg, i, j, k), 1);
+    CollRec rec{};
+    rec.id = -1;
+    if (h >= 0 && h < gk.ncell) {
+        if (coarse_needed) atomicAdd(counts + h, 1);
+        const double rB = sk[s].radiusB;
+        rec.id = coll_id(sk[s], mode);
+        rec.c[0] = (int32_t)(h / gk.nynz);
+        rec.c[1] = (int32_t)((h / gk.nz) % gk.ny);
+        rec.c[2] = (int32_t)(h % gk.nz);
+        rec.x = (float)c.x; rec.y = (float)c.y; rec.z = (float)c.z; rec.r = (float)rB;
+        if (rec.id == 1 || rec.id == 2) {
+            fine_range(fg, c, rB, rec.lo, rec.hi);
+            for (int k = rec.lo[2]; k <= rec.hi[2]; ++k)
+                for (int j = rec.lo[1]; j <= rec.hi[1]; ++j)
+                    for (int i = rec.lo[0]; i <= rec.hi[0]; ++i) atomicAdd(fcounts + fine_index(fg, i, j, k), 1);
+        }
+    }
+    recs[s] = rec;
 }
 
-__global__ void fine_scatter_kernel(const SolidK* __restrict__ sk, const sdfibm_solid_state* __restrict__ st, int S,
-                                    GridK gk, const int64_t* __restrict__ hashes, FineGridK fg,
-                                    int32_t* __restrict__ fcursor, int32_t* __restrict__ flist, int mode,
-                                    Counters* cnt) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void fine_scatter_kernel(const CollRec* __restrict__ recs, int S, FineGridK fg, int32_t* __restrict__ fcursor,
+                                    int32_t* __restrict__ flist, Counters* cnt) {
+    // one warp per solid: the lanes split its fine cells, so a large solid's claims do not run one after another
+    const int lane = threadIdx.x & 31;
+    const int s = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     if (s >= S) return;
-    const int64_t h = hashes[s];
-    if (h < 0 || h >= gk.ncell) return;
-    const int id = coll_id(sk[s], mode);
-    if (id != 1 && id != 2) return;
-    int lo[3], hi[3];
-    fine_range(fg, ld3(st[s].pos), sk[s].radiusB, lo, hi);
-    for (int k = lo[2]; k <= hi[2]; ++k)
-        for (int j = lo[1]; j <= hi[1]; ++j)
-            for (int i = lo[0]; i <= hi[0]; ++i) {
-                const int32_t e = atomicAdd(fcursor + fine_index(fg, i, j, k), 1);
-                if (e < fg.cap) flist[e] = s;
-                else set_error(cnt, DERR_CAPACITY);
-            }
+    const CollRec& r = recs[s];
+    if (r.id != 1 && r.id != 2) return;
+    const int nx = r.hi[0] - r.lo[0] + 1, ny = r.hi[1] - r.lo[1] + 1, nz = r.hi[2] - r.lo[2] + 1;
+    for (int e = lane; e < nx * ny * nz; e += 32) {
+        const int i = r.lo[0] + e % nx, j = r.lo[1] + (e / nx) % ny, k = r.lo[2] + e / (nx * ny);
+        const int32_t slot = atomicAdd(fcursor + fine_index(fg, i, j, k), 1);
+        if (slot < fg.cap) flist[slot] = s;
+        else set_error(cnt, DERR_CAPACITY);
+    }
 }
 
 // exclusive scan of the per-cell counts (single block)
@@ -270,6 +275,45 @@ __global__ void grid_scan_kernel(const int32_t* __restrict__ counts, int32_t* __
         __syncthreads();
     }
     if (threadIdx.x == 0) start[ncell] = carry;
+}
+
+// exclusive scan of large count arrays in three launches: per-1024-block scans, a scan of the block sums, offsets
+__global__ void __launch_bounds__(1024) scan_blocks_kernel(const int32_t* __restrict__ counts, int32_t* __restrict__ start,
+                                                           int32_t* __restrict__ sums, int64_t ncell) {
+    __shared__ int32_t warp_tot[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+    const int32_t v = i < ncell ? counts[i] : 0;
+    int32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int32_t w = warp_tot[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        warp_tot[lane] = w;
+    }
+    __syncthreads();
+    if (i < ncell) start[i] = (wid > 0 ? warp_tot[wid - 1] : 0) + x - v;
+    if (threadIdx.x == 1023) sums[blockIdx.x] = warp_tot[31];
+}
+
+__global__ void __launch_bounds__(1024) scan_add_kernel(int32_t* __restrict__ start, int32_t* __restrict__ cursor,
+                                                        const int32_t* __restrict__ sums_excl, int64_t ncell,
+                                                        int64_t nblocks) {
+    const int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+    if (i < ncell) {
+        const int32_t v = start[i] + sums_excl[blockIdx.x];
+        start[i] = v;
+        cursor[i] = v;
+    }
+    if (i == 0) start[ncell] = sums_excl[nblocks];  // the scan of the sums holds the total at nblocks
 }
 
 __global__ void grid_scatter_kernel(const int64_t* __restrict__ hashes, int32_t* __restrict__ cursor,
@@ -316,6 +360,19 @@ __device__ inline bool coarse_neighbours(const GridK& gk, int64_t a, int64_t b) 
     const int64_t bi = b / gk.nynz, bj = (b / gk.nz) % gk.ny, bk = b % gk.nz;
     return llabs(ai - bi) <= 1 && llabs(aj - bj) <= 1 && llabs(ak - bk) <= 1;
 }
+__device__ inline bool coarse_neighbours(const CollRec& a, const CollRec& b) {
+    return abs(a.c[0] - b.c[0]) <= 1 && abs(a.c[1] - b.c[1]) <= 1 && abs(a.c[2] - b.c[2]) <= 1;
+}
+
+// FP32 screen of a sphere pair: false only when the bounding spheres are certainly apart, i.e. the FP64 contact depth
+// r1 + r2 - |x2 - x1| is negative.  The FP32 values carry relative errors of a few 2^-24; the margin is 2^-16 of the
+// magnitudes involved, far above them.
+__device__ inline bool sphere_screen(const CollRec& a, const CollRec& b) {
+    const float dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
+    const float mag = fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fabsf(a.z)) + fmaxf(fmaxf(fabsf(b.x), fabsf(b.y)), fabsf(b.z));
+    const float reach = a.r + b.r + 1.52587890625e-5f * (mag + a.r + b.r);
+    return dx * dx + dy * dy + dz * dz <= reach * reach;
+}
 
 // Pair forces of one sub-step, each solid summing its own side of every pair the reference's UGrid would form
 // (27 coarse neighbours of its key, keys on the grid) that has a contact law and overlaps.  Sphere-like pairs come
@@ -326,13 +383,16 @@ __global__ void collide_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state
                                const int64_t* __restrict__ hashes, const int32_t* __restrict__ start,
                                const int32_t* __restrict__ list, int mode, FineGridK fg,
                                const int32_t* __restrict__ fstart, const int32_t* __restrict__ flist,
-                               const int32_t* __restrict__ planes, int nplanes) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+                               const int32_t* __restrict__ planes, int nplanes, const CollRec* __restrict__ recs) {
+    // one warp per solid: lanes split the solid's fine cells (a large solid spans thousands), the plane list, or the
+    // entries of its coarse cells; the warp sums the force
+    const int lane = threadIdx.x & 31;
+    const int p = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     if (p >= S) return;
-    const int64_t h = hashes[p];
-    if (h < 0 || h >= gk.ncell) return;
+    const CollRec rp = recs[p];
+    if (rp.id < 0) return;
     const SolidK& kp = sk[p];
-    const int idp = coll_id(kp, mode);
+    const int idp = rp.id;
     D3 fsum{0, 0, 0};
     const sdfibm_solid_state& sp = st[p];
     auto add_pair = [&](int q, int idq) {
@@ -344,37 +404,33 @@ __global__ void collide_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state
         }
     };
     if (idp == 1 || idp == 2) {
-        int lo[3], hi[3];
-        fine_range(fg, ld3(sp.pos), kp.radiusB, lo, hi);
-        for (int k = lo[2]; k <= hi[2]; ++k)
-            for (int j = lo[1]; j <= hi[1]; ++j)
-                for (int i = lo[0]; i <= hi[0]; ++i) {
-                    const int64_t cell = fine_index(fg, i, j, k);
-                    for (int e = fstart[cell]; e < fstart[cell + 1]; ++e) {
-                        const int q = flist[e];
-                        if (q == p) continue;
-                        const SolidK& kq = sk[q];
-                        if (coll_id(kq, mode) != idp) continue;  // (1,1) and (2,2) have a law, (1,2) has none
-                        // the pair's home cell: the corner max(lo_p, lo_q) of the two cell ranges' intersection
-                        // (both solids compute it from the same indices, so exactly one of p's and one of q's
-                        // visits holds the pair)
-                        int ql[3], qh[3];
-                        fine_range(fg, ld3(st[q].pos), kq.radiusB, ql, qh);
-                        if (max(lo[0], ql[0]) != i || max(lo[1], ql[1]) != j || max(lo[2], ql[2]) != k) continue;
-                        if (i > qh[0] || j > qh[1] || k > qh[2]) continue;  // ranges do not intersect
-                        const int64_t hq = hashes[q];
-                        if (!coarse_neighbours(gk, h, hq)) continue;
-                        add_pair(q, idp);
-                    }
-                }
-        for (int e = 0; e < nplanes; ++e) {
+        const int nx = rp.hi[0] - rp.lo[0] + 1, ny = rp.hi[1] - rp.lo[1] + 1, nz = rp.hi[2] - rp.lo[2] + 1;
+        const int ncells = nx * ny * nz;
+        for (int e = lane; e < ncells; e += 32) {
+            const int i = rp.lo[0] + e % nx, j = rp.lo[1] + (e / nx) % ny, k = rp.lo[2] + e / (nx * ny);
+            const int64_t cell = fine_index(fg, i, j, k);
+            for (int f = fstart[cell]; f < fstart[cell + 1]; ++f) {
+                const int q = flist[f];
+                if (q == p) continue;
+                const CollRec rq = recs[q];
+                if (rq.id != idp) continue;  // (1,1) and (2,2) have a law, (1,2) has none
+                // the pair's home cell: the corner max(lo_p, lo_q) of the two cell ranges' intersection (both solids
+                // compute it from the same indices, so exactly one of p's and one of q's visits holds the pair)
+                if (max(rp.lo[0], rq.lo[0]) != i || max(rp.lo[1], rq.lo[1]) != j || max(rp.lo[2], rq.lo[2]) != k)
+                    continue;
+                if (i > rq.hi[0] || j > rq.hi[1] || k > rq.hi[2]) continue;  // ranges do not intersect
+                if (!coarse_neighbours(rp, rq) || !sphere_screen(rp, rq)) continue;
+                add_pair(q, idp);
+            }
+        }
+        for (int e = lane; e < nplanes; e += 32) {
             const int q = planes[e];
-            const int64_t hq = hashes[q];
-            if (hq < 0 || hq >= gk.ncell || !coarse_neighbours(gk, h, hq)) continue;
+            const CollRec& rq = recs[q];
+            if (rq.id < 0 || !coarse_neighbours(rp, rq)) continue;
             add_pair(q, 0);
         }
     } else {
-        const int ci = (int)(h / gk.nynz), cj = (int)((h / gk.nz) % gk.ny), ck = (int)(h % gk.nz);
+        const int ci = rp.c[0], cj = rp.c[1], ck = rp.c[2];
         for (int a = ci - 1; a <= ci + 1; ++a) {
             if (a < 0 || a > gk.nx - 1) continue;
             for (int b = cj - 1; b <= cj + 1; ++b) {
@@ -382,18 +438,26 @@ __global__ void collide_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state
                 for (int c = ck - 1; c <= ck + 1; ++c) {
                     if (c < 0 || c > gk.nz - 1) continue;
                     const int64_t nb = (int64_t)a * gk.nynz + (int64_t)b * gk.nz + c;
-                    for (int e = start[nb]; e < start[nb + 1]; ++e) {
+                    for (int e = start[nb] + lane; e < start[nb + 1]; e += 32) {
                         const int q = list[e];
-                        if (q != p) add_pair(q, coll_id(sk[q], mode));
+                        if (q != p) add_pair(q, recs[q].id);
                     }
                 }
             }
         }
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        fsum.x += __shfl_xor_sync(0xffffffffu, fsum.x, o);
+        fsum.y += __shfl_xor_sync(0xffffffffu, fsum.y, o);
+        fsum.z += __shfl_xor_sync(0xffffffffu, fsum.z, o);
+    }
     // force += -f / +f in pair order (reordered sum); torque += -0 leaves it unchanged
-    st[p].force[0] += fsum.x;
-    st[p].force[1] += fsum.y;
-    st[p].force[2] += fsum.z;
+    if (lane == 0) {
+        st[p].force[0] += fsum.x;
+        st[p].force[1] += fsum.y;
+        st[p].force[2] += fsum.z;
+    }
 }
 
 __global__ void move_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state* st, int S, const StepParams* step) {

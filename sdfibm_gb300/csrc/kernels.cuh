@@ -225,6 +225,18 @@ struct FineGridK {
     int64_t cap;             // entries reserved for the cell lists
 };
 
+// Per-solid record of one collision sub-step, written with the UGrid key: the integer data the pair search needs, so
+// that it runs without FP64 work until a pair survives the FP32 screen.
+struct alignas(16) CollRec {
+    int32_t lo[3];
+    int32_t id;      // contact-law id; -1 when the key is off the grid (the solid is never paired)
+    int32_t hi[3];   // fine cell range [lo, hi] of the bounding box (sphere-like solids)
+    int32_t pad0;
+    int32_t c[3];    // the key decomposed as the UGrid neighbour loops do: key / nynz, (key / nz) % ny, key % nz
+    int32_t pad1;
+    float x, y, z, r;  // centre and bounding radius rounded to FP32 (the screen of sphere pairs)
+};
+
 // list entry word: solid index in bits 0..29, cell type (1 all inside, 2 centre inside, 3 centre outside) in 30..31
 constexpr int LIST_TYPE_SHIFT = 30;
 constexpr int32_t LIST_SOLID_MASK = (1 << LIST_TYPE_SHIFT) - 1;
