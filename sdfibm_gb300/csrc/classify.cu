@@ -191,10 +191,16 @@ __device__ __forceinline__ int band(float g, float Eg) { return g < -Eg ? 1 : (g
 
 constexpr int SS_QUADRIC = 0, SS_BOX = 1, SS_GENERIC = 2;
 
+// inside function of the convex shapes at a local point (negative inside), within f.Eg of its exact value
+template <int T>
+__device__ __forceinline__ float sample_g(const SampleFrame& f, float X, float Y, float Z) {
+    if (T == SS_QUADRIC) return __fmaf_rn(X * X, f.k0, __fmaf_rn(Y * Y, f.k1, (Z * Z) * f.k2)) - f.k3;
+    return fmaxf(fmaxf(fabsf(X) - f.k0, fabsf(Y) - f.k1), fabsf(Z) - f.k2);
+}
+
 template <int T>
 __device__ __forceinline__ int sample_inside(const ShapeK& sh, const SampleFrame& f, float X, float Y, float Z) {
-    if (T == SS_QUADRIC) return band(__fmaf_rn(X * X, f.k0, __fmaf_rn(Y * Y, f.k1, (Z * Z) * f.k2)) - f.k3, f.Eg);
-    if (T == SS_BOX) return band(fmaxf(fmaxf(fabsf(X) - f.k0, fabsf(Y) - f.k1), fabsf(Z) - f.k2), f.Eg);
+    if (T == SS_QUADRIC || T == SS_BOX) return band(sample_g<T>(f, X, Y, Z), f.Eg);
     return inside32(sh, X, Y, Z, f.E);  // tails and planes: the general test with its per-sample bound
 }
 
@@ -339,6 +345,136 @@ __device__ inline int block_log2(int n, bool flat) {
     return 0;
 }
 
+// Run counting for the convex shapes (3-D): the inside samples of a lattice column (a, b) are one run, since the
+// exact inside function q is convex along the column's line.  The run's ends come from the FP32 intersection of the
+// line with the shape (any error there only costs time); a few samples, computed and bounded exactly as the walk
+// computes them, then decide the whole column:
+//   run [c1, c2] found: c1 and c2 inside, c1 - 1 and c2 + 1 outside (or off the column).  Every sample between the
+//     ends is inside (q there is at most its value at the ends) and every sample past c2 + 1 outside (q grows past a
+//     rise from an inside to an outside sample), and likewise before c1 - 1;
+//   no sample in the interval: the sample cv nearest the closest approach and its neighbours outside, with q
+//     certified to rise from cv to each neighbour (computed rise of at least 2 Eg, each value being within Eg of
+//     exact); every sample past a neighbour is then outside.
+// A column that does not verify (an undecided sample, a run end off by one, a flat approach) is walked sample by
+// sample.  The count is therefore the exhaustive lattice count.
+template <int T>
+__device__ __noinline__ int subsample_runs(const MeshK& m, const ShapeK& sh, const SampleFrame& f, int64_t i,
+                                           int64_t j, int64_t k, int n, const D3& x, const Q4& q,
+                                           unsigned long long* rechecks, const Defer* df) {
+    __shared__ uint16_t s_walk[8][128];  // columns of each warp left to the sample-by-sample walk
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    uint16_t* walk_list = s_walk[(threadIdx.x >> 5) & 7];
+    const float inv2n = 1.0f / (float)(2 * n), nf = (float)n, invn = 1.0f / nf;
+    const float rise = 2.0001f * f.Eg;
+    // quadric along the column: q(t) = A t^2 + 2 B t + C, t the column coordinate of the samples (2c + 1) / (2n);
+    // box: slab of axis a between t = (-k_a - b_a) / s_a and (k_a - b_a) / s_a
+    const float A = f.k0 * f.szx * f.szx + f.k1 * f.szy * f.szy + f.k2 * f.szz * f.szz;
+    const float invA = 1.0f / A;
+    const float isx = 1.0f / f.szx, isy = 1.0f / f.szy, isz = 1.0f / f.szz;
+    auto column_base = [&](int col, int& ia, int& ib, float& bx, float& by, float& bz) {
+        ib = __float2int_rz(((float)col + 0.5f) * invn);
+        ia = col - ib * n;
+        const float ta = (float)(2 * ia + 1) * inv2n, tb = (float)(2 * ib + 1) * inv2n;
+        bx = __fmaf_rn(tb, f.syx, __fmaf_rn(ta, f.sxx, f.px));
+        by = __fmaf_rn(tb, f.syy, __fmaf_rn(ta, f.sxy, f.py));
+        bz = __fmaf_rn(tb, f.syz, __fmaf_rn(ta, f.sxz, f.pz));
+    };
+    // the walk's sample: the same coordinates, bound and deferral as subsample_count
+    auto walk_sample = [&](int ia, int ib, int c3, float bx, float by, float bz) {
+        const float tc = (float)(2 * c3 + 1) * inv2n;
+        int r = band(sample_g<T>(f, __fmaf_rn(tc, f.szx, bx), __fmaf_rn(tc, f.szy, by), __fmaf_rn(tc, f.szz, bz)),
+                     f.Eg);
+        if (r == 2) {
+            ++*rechecks;
+            r = undecided_sample(df, sh, m, i, j, k, ia, ib, c3, n, x, q);
+        }
+        return r;
+    };
+    int cnt = 0, nwalk = 0;
+#pragma unroll 1
+    for (int base = 0; base < n * n; base += 32) {
+        const int col = base + lane;
+        int res = 0;
+        int ia = 0, ib = 0;
+        float bx = 0.f, by = 0.f, bz = 0.f;
+        if (col < n * n) {
+            column_base(col, ia, ib, bx, by, bz);
+            auto g_at = [&](int c3) {
+                const float tc = (float)(2 * c3 + 1) * inv2n;
+                return sample_g<T>(f, __fmaf_rn(tc, f.szx, bx), __fmaf_rn(tc, f.szy, by), __fmaf_rn(tc, f.szz, bz));
+            };
+            float tl, tr;
+            if (T == SS_QUADRIC) {
+                const float B = f.k0 * bx * f.szx + f.k1 * by * f.szy + f.k2 * bz * f.szz;
+                const float C = f.k0 * bx * bx + f.k1 * by * by + f.k2 * bz * bz - f.k3;
+                const float disc = B * B - A * C;
+                const float sq = disc > 0.f ? sqrtf(disc) : 0.f;
+                tl = (-B - sq) * invA;
+                tr = disc > 0.f ? (-B + sq) * invA : tl - 1.f;  // empty: tl marks the closest approach
+            } else {
+                const float lx = (-f.k0 - bx) * isx, rx = (f.k0 - bx) * isx;
+                const float ly = (-f.k1 - by) * isy, ry = (f.k1 - by) * isy;
+                const float lz = (-f.k2 - bz) * isz, rz = (f.k2 - bz) * isz;
+                tl = fmaxf(fmaxf(fminf(lx, rx), fminf(ly, ry)), fminf(lz, rz));
+                tr = fminf(fminf(fmaxf(lx, rx), fmaxf(ly, ry)), fmaxf(lz, rz));
+            }
+            // sample indices c with t_c in [tl, tr]: t_c n - 1/2 = c (clamped before the conversion: inf / NaN safe)
+            const float ul = fminf(fmaxf(tl * nf - 0.5f, -2.f), nf + 1.f);
+            const float ur = fminf(fmaxf(tr * nf - 0.5f, -2.f), nf + 1.f);
+            const int c1 = max((int)ceilf(ul), 0), c2 = min((int)floorf(ur), n - 1);
+            res = -1;
+            if (tl <= tr && c1 <= c2) {
+                const int r1 = band(g_at(c1), f.Eg), r2 = c2 == c1 ? r1 : band(g_at(c2), f.Eg);
+                const int rl = c1 > 0 ? band(g_at(c1 - 1), f.Eg) : 0, rr = c2 < n - 1 ? band(g_at(c2 + 1), f.Eg) : 0;
+                if (r1 == 1 && r2 == 1 && rl == 0 && rr == 0) res = c2 - c1 + 1;
+            } else {
+                const float um = (T == SS_QUADRIC && !(tl <= tr)) ? ul : 0.5f * (ul + ur);
+                const int cv = min(max(__float2int_rn(fminf(fmaxf(um, 0.f), nf - 1.f)), 0), n - 1);
+                const float g0 = g_at(cv);
+                bool ok = band(g0, f.Eg) == 0;
+                if (ok && cv + 1 < n) {
+                    const float g1 = g_at(cv + 1);
+                    ok = band(g1, f.Eg) == 0 && (cv + 2 >= n || g1 - g0 >= rise);
+                }
+                if (ok && cv > 0) {
+                    const float g1 = g_at(cv - 1);
+                    ok = band(g1, f.Eg) == 0 && (cv < 2 || g1 - g0 >= rise);
+                }
+                if (ok) res = 0;
+            }
+        }
+        const bool walk = res < 0;
+        const unsigned mask = __ballot_sync(FULL, walk);
+        const int pos = nwalk + __popc(mask & ((1u << lane) - 1u));
+        nwalk += __popc(mask);
+        if (walk) {
+            if (pos < 128) {
+                walk_list[pos] = (uint16_t)col;
+            } else {  // list full: walk here
+                for (int c3 = 0; c3 < n; ++c3) cnt += walk_sample(ia, ib, c3, bx, by, bz);
+            }
+        } else {
+            cnt += res;
+        }
+    }
+    __syncwarp();
+    // the listed columns' samples spread over the lanes
+    const int listed = min(nwalk, 128);
+#pragma unroll 1
+    for (int e = lane; e < listed * n; e += 32) {
+        const int w = __float2int_rz(((float)e + 0.5f) * invn), c3 = e - w * n;
+        int ia, ib;
+        float bx, by, bz;
+        column_base(walk_list[w], ia, ib, bx, by, bz);
+        cnt += walk_sample(ia, ib, c3, bx, by, bz);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(FULL, cnt, o);
+    return cnt;
+}
+
 // Inside count of the cell's n^3 (n^2 on one-layer meshes) lattice; with a Defer the undecided points are not counted
 // here but appended to the recheck list.
 static __device__ __noinline__ int subsample_warp(const MeshK& m, const ShapeK& sh, const float* M, const TileFrame& tf,
@@ -392,6 +528,8 @@ static __device__ __noinline__ int subsample_warp(const MeshK& m, const ShapeK& 
     const float mx = fabsf(f.px) + fabsf(f.sxx) + fabsf(f.syx) + fabsf(f.szx) + Ep;
     const float my = fabsf(f.py) + fabsf(f.sxy) + fabsf(f.syy) + fabsf(f.szy) + Ep;
     const float mz = fabsf(f.pz) + fabsf(f.sxz) + fabsf(f.syz) + fabsf(f.szz) + Ep;
+    // lattices of at least 5 per axis without 4 x 4 x 4 blocks count runs along columns (3-D, convex shapes)
+    const bool use_runs = !m.twod && !prism && n >= 5;
     int cnt;
     if (kind == SS_QUADRIC) {
         switch (type) {
@@ -404,14 +542,16 @@ static __device__ __noinline__ int subsample_warp(const MeshK& m, const ShapeK& 
                10.f * u * (mx * mx * f.k0 + my * my * f.k1 + mz * mz * f.k2 + f.k3);
         const int lb = block_log2(n, m.twod != 0);
         cnt = lb ? subsample_blocks<SS_QUADRIC>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks, df)
-                 : subsample_count<SS_QUADRIC>(m, sh, f, i, j, k, n, x, q, rechecks, df);
+              : use_runs ? subsample_runs<SS_QUADRIC>(m, sh, f, i, j, k, n, x, q, rechecks, df)
+                         : subsample_count<SS_QUADRIC>(m, sh, f, i, j, k, n, x, q, rechecks, df);
     } else if (kind == SS_BOX) {
         f.k0 = a[0]; f.k1 = a[1];
         f.k2 = prism ? INFINITY : a[2];  // the rectangle has no z extent
         f.Eg = Ep + 2.f * u * (fmaxf(mx, fmaxf(my, prism ? 0.f : mz)) + fmaxf(a[0], fmaxf(a[1], prism ? 0.f : a[2])));
         const int lb = block_log2(n, m.twod != 0);
         cnt = lb ? subsample_blocks<SS_BOX>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks, df)
-                 : subsample_count<SS_BOX>(m, sh, f, i, j, k, n, x, q, rechecks, df);
+              : use_runs ? subsample_runs<SS_BOX>(m, sh, f, i, j, k, n, x, q, rechecks, df)
+                         : subsample_count<SS_BOX>(m, sh, f, i, j, k, n, x, q, rechecks, df);
     } else {
         cnt = subsample_count<SS_GENERIC>(m, sh, f, i, j, k, n, x, q, rechecks, df);
     }
@@ -748,33 +888,44 @@ __global__ void __launch_bounds__(256) learned_fallback_kernel(FallbackArgs A) {
     const int64_t nfb = min((int64_t)A.cnt->n_fb, A.cap);
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     unsigned long long rechecks = 0;
-    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nfb; w += warps) {
-        const int32_t slot = A.fb_list[w];
-        const int s = A.fref_solid[slot];
-        const int64_t idx = A.fref_index[slot];
-        const SolidK& k = A.sk[s];
-        const SolidPlan& pl = A.plan[s];
-        const int local = (int)(idx - k.scratch_off);  // < bbox cells of one solid
-        const int la = local % k.ext[0], lb = (local / k.ext[0]) % k.ext[1], lc = local / (k.ext[0] * k.ext[1]);
-        // the cell's FP32 frame as the classify pass builds a tile's: rounded base plus a whole number of cells
-        TileFrame tf;
-        {
-            const float sbx = (float)pl.base[0], sby = (float)pl.base[1], sbz = (float)pl.base[2];
-            const float ofx = (float)la * A.m.h32[0], ofy = (float)lb * A.m.h32[1], ofz = (float)lc * A.m.h32[2];
-            tf.bx = sbx + ofx; tf.by = sby + ofy; tf.bz = sbz + ofz;
-            tf.babs = fabsf(sbx) + fabsf(sby) + fabsf(sbz) + 2.f * (fabsf(ofx) + fabsf(ofy) + fabsf(ofz)) +
-                      fabsf(tf.bx) + fabsf(tf.by) + fabsf(tf.bz);
-            tf.e64 = pl.e64;
+    // each warp takes 32 consecutive list entries: the 32 lanes load their (solid, index) pairs at once, then the
+    // warp counts the cells one after the other
+    for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < nfb; base += warps * 32) {
+        int s_l = 0;
+        int64_t idx_l = 0;
+        if (base + lane < nfb) {
+            const int32_t slot = A.fb_list[base + lane];
+            s_l = A.fref_solid[slot];
+            idx_l = A.fref_index[slot];
         }
-        float M[9];
+        const int batch = (int)min((int64_t)32, nfb - base);
+        for (int t = 0; t < batch; ++t) {
+            const int s = __shfl_sync(0xffffffffu, s_l, t);
+            const int64_t idx = __shfl_sync(0xffffffffu, idx_l, t);
+            const SolidK& k = A.sk[s];
+            const SolidPlan& pl = A.plan[s];
+            const int local = (int)(idx - k.scratch_off);  // < bbox cells of one solid
+            const int la = local % k.ext[0], lb = (local / k.ext[0]) % k.ext[1], lc = local / (k.ext[0] * k.ext[1]);
+            // the cell's FP32 frame as the classify pass builds a tile's: rounded base plus a whole number of cells
+            TileFrame tf;
+            {
+                const float sbx = (float)pl.base[0], sby = (float)pl.base[1], sbz = (float)pl.base[2];
+                const float ofx = (float)la * A.m.h32[0], ofy = (float)lb * A.m.h32[1], ofz = (float)lc * A.m.h32[2];
+                tf.bx = sbx + ofx; tf.by = sby + ofy; tf.bz = sbz + ofz;
+                tf.babs = fabsf(sbx) + fabsf(sby) + fabsf(sbz) + 2.f * (fabsf(ofx) + fabsf(ofy) + fabsf(ofz)) +
+                          fabsf(tf.bx) + fabsf(tf.by) + fabsf(tf.bz);
+                tf.e64 = pl.e64;
+            }
+            float M[9];
 #pragma unroll
-        for (int r = 0; r < 9; ++r) M[r] = pl.M[r];
-        const Q4 q = state_quat(A.st[s]);
-        const D3 x = state_pos(A.st[s]);
-        const Defer df{A.rq, A.rq_cap, &A.cnt->n_recheck, idx, s};
-        const int cnt = subsample_warp(A.m, k.shape, M, tf, 0, 0, 0, x, q, pl.lo[0] + la, pl.lo[1] + lb,
-                                       pl.lo[2] + lc, A.n, &rechecks, A.rq ? &df : nullptr);
-        if (lane == 0) A.alpha[idx] = A.rq ? -1.f - (float)cnt : count_fraction(A.m, cnt, A.n);
+            for (int r = 0; r < 9; ++r) M[r] = pl.M[r];
+            const Q4 q = state_quat(A.st[s]);
+            const D3 x = state_pos(A.st[s]);
+            const Defer df{A.rq, A.rq_cap, &A.cnt->n_recheck, idx, s};
+            const int cnt = subsample_warp(A.m, k.shape, M, tf, 0, 0, 0, x, q, pl.lo[0] + la, pl.lo[1] + lb,
+                                           pl.lo[2] + lc, A.n, &rechecks, A.rq ? &df : nullptr);
+            if (lane == 0) A.alpha[idx] = A.rq ? -1.f - (float)cnt : count_fraction(A.m, cnt, A.n);
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);
