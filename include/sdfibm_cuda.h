@@ -153,7 +153,11 @@ typedef struct sdfibm_options {
                                    network's confidence band (0: 16, the lattice the network was trained on) */
     int32_t graphs;          /* 1: capture interact and evolve as CUDA graphs on the first call and replay them
                                 (needs a non-NULL stream; ignored while timing is on) */
-    int32_t reserved[4];
+    int32_t recheck_cap;     /* SUBSAMPLE / LEARNED: entries of the list of FP32-undecided sample points re-evaluated
+                                in FP64 after the sampling pass (0: one per 8 bbox cells, at least 2^20, at most
+                                2^25); points beyond it are re-evaluated in place (cells of the LEARNED fallback are
+                                then recounted whole) */
+    int32_t reserved[3];
 } sdfibm_options;
 
 typedef struct sdfibm_ctx sdfibm_ctx;

@@ -59,7 +59,7 @@ class Options(C.Structure):
                 ("n_subiter", C.c_int32), ("fraction_method", C.c_int32), ("subsample_n", C.c_int32),
                 ("dense_reset", C.c_int32), ("exact_forcing", C.c_int32), ("tile_cells", C.c_int32),
                 ("timing", C.c_int32), ("learned_fallback_n", C.c_int32), ("graphs", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("recheck_cap", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class MlpDataDesc(C.Structure):

@@ -21,6 +21,7 @@ __global__ void plan_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state*
 void launch_classify(const ClassifyArgs& A, bool flat, int grid, cudaStream_t st);
 int classify_occupancy(int method, bool flat);
 __global__ void learned_fallback_kernel(FallbackArgs A);
+__global__ void recount_kernel(FallbackArgs A);
 __global__ void recheck_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state* st, const SolidPlan* plan,
                                const Recheck* rq, int64_t cap, Counters* cnt, float* alpha);
 __global__ void connect_kernel(MeshK m, const SolidK* sk, SolidPlan* plan, const uint8_t* scratch, uint32_t* gbitmaps,
@@ -109,6 +110,9 @@ struct sdfibm_ctx {
     // SUBSAMPLE points whose FP32 test was undecided, re-evaluated in FP64 on full warps by recheck_kernel
     Recheck* d_rq = nullptr;
     int64_t rq_cap = 0;
+    // LEARNED: fallback cells whose points overflowed the recheck list, recounted with FP64 in place
+    Recheck* d_ovf = nullptr;
+    int64_t ovf_cap = 0;
     // touched-cell lists, double buffered: [cur] is this call's, [cur ^ 1] the previous call's (sparse reset)
     int32_t* d_lists[2][4] = {{nullptr, nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr, nullptr}};
     int cur = 0;
@@ -367,7 +371,9 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
     ctx->connect_smem_bytes = max_smem_words * 4;
     ctx->n_small = (int)small_solids.size();
     ctx->n_big = (int)big_solids.size();
-    ctx->rq_cap = std::min<int64_t>(std::max<int64_t>(scratch / 8, 1 << 20), 1 << 25);
+    ctx->rq_cap = ctx->opt.recheck_cap > 0 ? (int64_t)ctx->opt.recheck_cap
+                                            : std::min<int64_t>(std::max<int64_t>(scratch / 8, 1 << 20), 1 << 25);
+    ctx->ovf_cap = std::max<int64_t>(ctx->rq_cap / 16, std::min<int64_t>(scratch, 1 << 16));
     ctx->cap = std::max<int64_t>(1, bbox_total);
 
     {
@@ -468,7 +474,7 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         dalloc(&ctx->d_sh_keys, (size_t)ctx->sh_mask + 1) || dalloc(&ctx->d_sh_vals, 5 * ((size_t)ctx->sh_mask + 1)) ||
         dalloc(&ctx->d_sh_used, (size_t)ctx->sh_mask + 1) || dalloc(&ctx->d_step, 2) ||
         dalloc(&ctx->d_small, small_solids.size()) || dalloc(&ctx->d_big, big_solids.size()) ||
-        dalloc(&ctx->d_rq, (size_t)ctx->rq_cap) ||
+        dalloc(&ctx->d_rq, (size_t)ctx->rq_cap) || dalloc(&ctx->d_ovf, (size_t)ctx->ovf_cap) ||
         cudaMallocHost((void**)&ctx->h_cnt, sizeof(Counters)) != cudaSuccess ||
         cudaMallocHost((void**)&ctx->h_ft, std::max<size_t>(1, 6 * (size_t)nsolids) * sizeof(double)) != cudaSuccess) {
         ctx->err = "device allocation failed";
@@ -581,6 +587,7 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
         }
         launch_classify(CA, ctx->mesh.nz <= 2, ctx->classify_grid, st);
         mark(ctx, "classify_kernel");
+        FallbackArgs fa{};
         if (learned) {
             // network on every cut cell, SUBSAMPLE on the cells outside its band
             MlpInferArgs ia{};
@@ -590,12 +597,12 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             ia.tau_grad = ctx->tau_grad; ia.error = &ctx->d_cnt->error;
             launch_mlp_infer(ia, 4 * ctx->num_sms, st);
             mark(ctx, "mlp_infer_kernel");
-            FallbackArgs fa{};
             fa.m = ctx->mesh; fa.sk = ctx->d_sk; fa.st = ctx->d_st; fa.plan = ctx->d_plan; fa.fb_list = ctx->d_fb;
             fa.fref_solid = ctx->d_fref_solid; fa.fref_index = ctx->d_fref_index; fa.cap = ctx->feat_cap;
             fa.alpha = ctx->d_alpha; fa.cnt = ctx->d_cnt;
             fa.n = ctx->opt.learned_fallback_n > 0 ? ctx->opt.learned_fallback_n : 16;
             fa.rq = ctx->d_rq; fa.rq_cap = ctx->rq_cap;
+            fa.ovf = ctx->d_ovf; fa.ovf_cap = ctx->ovf_cap;
             learned_fallback_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(fa);
             mark(ctx, "learned_fallback_kernel");
             launches += 2;
@@ -604,6 +611,11 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             recheck_kernel<<<ctx->num_sms * 4, 256, 0, st>>>(ctx->mesh, ctx->d_sk, ctx->d_st, ctx->d_plan, ctx->d_rq,
                                                               ctx->rq_cap, ctx->d_cnt, ctx->d_alpha);
             mark(ctx, "recheck_kernel");
+            ++launches;
+        }
+        if (learned) {
+            recount_kernel<<<ctx->num_sms * 2, 256, 0, st>>>(fa);
+            mark(ctx, "recount_kernel");
             ++launches;
         }
         if (ctx->n_small > 0)
@@ -1061,6 +1073,7 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
     if (ctx->d_step) cudaFree(ctx->d_step);
     if (ctx->d_small) cudaFree(ctx->d_small);
     if (ctx->d_rq) cudaFree(ctx->d_rq);
+    if (ctx->d_ovf) cudaFree(ctx->d_ovf);
     if (ctx->d_fsums) cudaFree(ctx->d_fsums);
     if (ctx->d_recs) cudaFree(ctx->d_recs);
     if (ctx->d_fsums_excl) cudaFree(ctx->d_fsums_excl);

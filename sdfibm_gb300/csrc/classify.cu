@@ -142,14 +142,17 @@ static __device__ __noinline__ int exact_inside_sample(const ShapeK& sh, const M
 }
 
 // Where an undecided SUBSAMPLE point goes: appended to the recheck list (counted later by recheck_kernel) when there
-// is room, else re-evaluated here.
+// is room, else re-evaluated here.  DEFER_ONLY kernels carry no FP64 path: a point the full list cannot take sets the
+// warp's overflow flag instead, and the cell is recounted by recount_kernel.
 struct Defer {
     Recheck* rq;
     int64_t cap;
     int32_t* count;
     int64_t idx;
     int32_t solid;
+    int32_t* overflow;  // DEFER_ONLY: the warp's flag in shared memory
 };
+template <bool DEFER_ONLY>
 static __device__ __forceinline__ int undecided_sample(const Defer* df, const ShapeK& sh, const MeshK& m, int64_t i,
                                                        int64_t j, int64_t k, int a, int b, int c3, int n, const D3& x,
                                                        const Q4& q) {
@@ -160,7 +163,12 @@ static __device__ __forceinline__ int undecided_sample(const Defer* df, const Sh
                                    (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)c3 << 16) | ((uint32_t)n << 24)};
             return 0;
         }
+        if (DEFER_ONLY) {
+            *(volatile int32_t*)df->overflow = 1;
+            return 0;
+        }
     }
+    if (DEFER_ONLY) return 0;  // DEFER_ONLY callers always pass a Defer
     return exact_inside_sample(sh, m, i, j, k, a, b, c3, n, x, q);
 }
 
@@ -204,7 +212,7 @@ __device__ __forceinline__ int sample_inside(const ShapeK& sh, const SampleFrame
     return inside32(sh, X, Y, Z, f.E);  // tails and planes: the general test with its per-sample bound
 }
 
-template <int T>
+template <int T, bool DEFER_ONLY>
 __device__ __forceinline__ int subsample_count(const MeshK& m, const ShapeK& sh, const SampleFrame& f, int64_t i,
                                                int64_t j, int64_t k, int n, const D3& x, const Q4& q,
                                                unsigned long long* rechecks, const Defer* df) {
@@ -228,7 +236,7 @@ __device__ __forceinline__ int subsample_count(const MeshK& m, const ShapeK& sh,
                                      __fmaf_rn(tc, f.szz, bz));
             if (r == 2) {
                 ++*rechecks;
-                r = undecided_sample(df, sh, m, i, j, k, ia, ib, c3, n, x, q);
+                r = undecided_sample<DEFER_ONLY>(df, sh, m, i, j, k, ia, ib, c3, n, x, q);
             }
             cnt += r;
         }
@@ -261,7 +269,7 @@ __device__ __forceinline__ void block_bounds(const SampleFrame& f, float X, floa
     }
 }
 
-template <int T>
+template <int T, bool DEFER_ONLY>
 __device__ __noinline__ int subsample_blocks(const MeshK& m, const ShapeK& sh, const SampleFrame& f, int64_t i,
                                              int64_t j, int64_t k, int n, int lb, float Ep, const D3& x, const Q4& q,
                                              unsigned long long* rechecks, const Defer* df) {
@@ -322,7 +330,7 @@ __device__ __noinline__ int subsample_blocks(const MeshK& m, const ShapeK& sh, c
                                        __fmaf_rn(tc, f.szz, bz));
             if (res == 2) {
                 ++*rechecks;
-                res = undecided_sample(df, sh, m, i, j, k, ia, ib, flat ? 0 : ic0 + dc, n, x, q);
+                res = undecided_sample<DEFER_ONLY>(df, sh, m, i, j, k, ia, ib, flat ? 0 : ic0 + dc, n, x, q);
             }
             cnt += res;
         }
@@ -357,7 +365,7 @@ __device__ inline int block_log2(int n, bool flat) {
 //     exact); every sample past a neighbour is then outside.
 // A column that does not verify (an undecided sample, a run end off by one, a flat approach) is walked sample by
 // sample.  The count is therefore the exhaustive lattice count.
-template <int T>
+template <int T, bool DEFER_ONLY>
 __device__ __noinline__ int subsample_runs(const MeshK& m, const ShapeK& sh, const SampleFrame& f, int64_t i,
                                            int64_t j, int64_t k, int n, const D3& x, const Q4& q,
                                            unsigned long long* rechecks, const Defer* df) {
@@ -387,7 +395,7 @@ __device__ __noinline__ int subsample_runs(const MeshK& m, const ShapeK& sh, con
                      f.Eg);
         if (r == 2) {
             ++*rechecks;
-            r = undecided_sample(df, sh, m, i, j, k, ia, ib, c3, n, x, q);
+            r = undecided_sample<DEFER_ONLY>(df, sh, m, i, j, k, ia, ib, c3, n, x, q);
         }
         return r;
     };
@@ -477,6 +485,7 @@ __device__ __noinline__ int subsample_runs(const MeshK& m, const ShapeK& sh, con
 
 // Inside count of the cell's n^3 (n^2 on one-layer meshes) lattice; with a Defer the undecided points are not counted
 // here but appended to the recheck list.
+template <bool DEFER_ONLY>
 static __device__ __noinline__ int subsample_warp(const MeshK& m, const ShapeK& sh, const float* M, const TileFrame& tf,
                                                   int a0, int b0, int c0, const D3& x, const Q4& q, int64_t i,
                                                   int64_t j, int64_t k, int n, unsigned long long* rechecks,
@@ -528,8 +537,8 @@ static __device__ __noinline__ int subsample_warp(const MeshK& m, const ShapeK& 
     const float mx = fabsf(f.px) + fabsf(f.sxx) + fabsf(f.syx) + fabsf(f.szx) + Ep;
     const float my = fabsf(f.py) + fabsf(f.sxy) + fabsf(f.syy) + fabsf(f.szy) + Ep;
     const float mz = fabsf(f.pz) + fabsf(f.sxz) + fabsf(f.syz) + fabsf(f.szz) + Ep;
-    // lattices of at least 5 per axis without 4 x 4 x 4 blocks count runs along columns (3-D, convex shapes)
-    const bool use_runs = !m.twod && !prism && n >= 5;
+    // 3-D convex shapes: lattices of 5 to 15 per axis count runs along columns, larger ones skip 4 x 4 x 4 blocks
+    const bool use_runs = !m.twod && !prism && n >= 5 && n < 16;
     int cnt;
     if (kind == SS_QUADRIC) {
         switch (type) {
@@ -541,19 +550,19 @@ static __device__ __noinline__ int subsample_warp(const MeshK& m, const ShapeK& 
         f.Eg = (2.f * (mx * f.k0 + my * f.k1 + mz * f.k2) + Ep * (f.k0 + f.k1 + f.k2)) * Ep +
                10.f * u * (mx * mx * f.k0 + my * my * f.k1 + mz * mz * f.k2 + f.k3);
         const int lb = block_log2(n, m.twod != 0);
-        cnt = lb ? subsample_blocks<SS_QUADRIC>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks, df)
-              : use_runs ? subsample_runs<SS_QUADRIC>(m, sh, f, i, j, k, n, x, q, rechecks, df)
-                         : subsample_count<SS_QUADRIC>(m, sh, f, i, j, k, n, x, q, rechecks, df);
+        cnt = lb ? subsample_blocks<SS_QUADRIC, DEFER_ONLY>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks, df)
+              : use_runs ? subsample_runs<SS_QUADRIC, DEFER_ONLY>(m, sh, f, i, j, k, n, x, q, rechecks, df)
+                         : subsample_count<SS_QUADRIC, DEFER_ONLY>(m, sh, f, i, j, k, n, x, q, rechecks, df);
     } else if (kind == SS_BOX) {
         f.k0 = a[0]; f.k1 = a[1];
         f.k2 = prism ? INFINITY : a[2];  // the rectangle has no z extent
         f.Eg = Ep + 2.f * u * (fmaxf(mx, fmaxf(my, prism ? 0.f : mz)) + fmaxf(a[0], fmaxf(a[1], prism ? 0.f : a[2])));
         const int lb = block_log2(n, m.twod != 0);
-        cnt = lb ? subsample_blocks<SS_BOX>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks, df)
-              : use_runs ? subsample_runs<SS_BOX>(m, sh, f, i, j, k, n, x, q, rechecks, df)
-                         : subsample_count<SS_BOX>(m, sh, f, i, j, k, n, x, q, rechecks, df);
+        cnt = lb ? subsample_blocks<SS_BOX, DEFER_ONLY>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks, df)
+              : use_runs ? subsample_runs<SS_BOX, DEFER_ONLY>(m, sh, f, i, j, k, n, x, q, rechecks, df)
+                         : subsample_count<SS_BOX, DEFER_ONLY>(m, sh, f, i, j, k, n, x, q, rechecks, df);
     } else {
-        cnt = subsample_count<SS_GENERIC>(m, sh, f, i, j, k, n, x, q, rechecks, df);
+        cnt = subsample_count<SS_GENERIC, DEFER_ONLY>(m, sh, f, i, j, k, n, x, q, rechecks, df);
     }
     return cnt;
 }
@@ -859,8 +868,8 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                     const int e = cutlist[u];
                     const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
                     const int64_t li = local_index(a, b, c);
-                    const Defer df{A.rq, A.rq_cap, &A.cnt->n_recheck, k.scratch_off + li, s};
-                    const int cnt = subsample_warp(m, sh, M, tf, a, b, c, x, q, I0 + a, J0 + b, K0 + c,
+                    const Defer df{A.rq, A.rq_cap, &A.cnt->n_recheck, k.scratch_off + li, s, nullptr};
+                    const int cnt = subsample_warp<false>(m, sh, M, tf, a, b, c, x, q, I0 + a, J0 + b, K0 + c,
                                                    A.subsample_n, &rechecks, A.rq ? &df : nullptr);
                     if (lane == 0) alpha[li] = A.rq ? -1.f - (float)cnt : count_fraction(m, cnt, A.subsample_n);
                 }
@@ -882,12 +891,45 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
     }
 }
 
-// LEARNED fallback: one warp per cell outside the network's band, SUBSAMPLE from the cell's own FP32 frame
-__global__ void __launch_bounds__(256) learned_fallback_kernel(FallbackArgs A) {
+// SUBSAMPLE count of one listed cell (bbox index idx of solid s) from the cell's own FP32 frame, built as the classify
+// pass builds a tile's: the solid's rounded base plus a whole number of cells.
+template <bool DEFER_ONLY>
+__device__ __forceinline__ int count_listed_cell(const FallbackArgs& A, int s, int64_t idx, unsigned long long* rechecks,
+                                                 const Defer* df) {
+    const SolidK& k = A.sk[s];
+    const SolidPlan& pl = A.plan[s];
+    const int local = (int)(idx - k.scratch_off);  // < bbox cells of one solid
+    const int la = local % k.ext[0], lb = (local / k.ext[0]) % k.ext[1], lc = local / (k.ext[0] * k.ext[1]);
+    TileFrame tf;
+    {
+        const float sbx = (float)pl.base[0], sby = (float)pl.base[1], sbz = (float)pl.base[2];
+        const float ofx = (float)la * A.m.h32[0], ofy = (float)lb * A.m.h32[1], ofz = (float)lc * A.m.h32[2];
+        tf.bx = sbx + ofx; tf.by = sby + ofy; tf.bz = sbz + ofz;
+        tf.babs = fabsf(sbx) + fabsf(sby) + fabsf(sbz) + 2.f * (fabsf(ofx) + fabsf(ofy) + fabsf(ofz)) +
+                  fabsf(tf.bx) + fabsf(tf.by) + fabsf(tf.bz);
+        tf.e64 = pl.e64;
+    }
+    float M[9];
+#pragma unroll
+    for (int r = 0; r < 9; ++r) M[r] = pl.M[r];
+    const Q4 q = state_quat(A.st[s]);
+    const D3 x = state_pos(A.st[s]);
+    return subsample_warp<DEFER_ONLY>(A.m, k.shape, M, tf, 0, 0, 0, x, q, pl.lo[0] + la, pl.lo[1] + lb,
+                                      pl.lo[2] + lc, A.n, rechecks, df);
+}
+
+// LEARNED fallback: one warp per cell outside the network's band.  Undecided points always go to the recheck list
+// (this kernel holds no FP64 path, which keeps its register count and so its occupancy); a cell some of whose points
+// found the list full is listed for recount_kernel.
+__global__ void __launch_bounds__(256, 4) learned_fallback_kernel(FallbackArgs A) {
+    __shared__ int32_t s_overflow[8];
     const int lane = threadIdx.x & 31;
+    int32_t* overflow = s_overflow + ((threadIdx.x >> 5) & 7);
     const int64_t nfb = min((int64_t)A.cnt->n_fb, A.cap);
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     unsigned long long rechecks = 0;
+    if (lane == 0) *overflow = 0;
+    __syncwarp();
     // each warp takes 32 consecutive list entries: the 32 lanes load their (solid, index) pairs at once, then the
     // warp counts the cells one after the other
     for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < nfb; base += warps * 32) {
@@ -902,30 +944,37 @@ __global__ void __launch_bounds__(256) learned_fallback_kernel(FallbackArgs A) {
         for (int t = 0; t < batch; ++t) {
             const int s = __shfl_sync(0xffffffffu, s_l, t);
             const int64_t idx = __shfl_sync(0xffffffffu, idx_l, t);
-            const SolidK& k = A.sk[s];
-            const SolidPlan& pl = A.plan[s];
-            const int local = (int)(idx - k.scratch_off);  // < bbox cells of one solid
-            const int la = local % k.ext[0], lb = (local / k.ext[0]) % k.ext[1], lc = local / (k.ext[0] * k.ext[1]);
-            // the cell's FP32 frame as the classify pass builds a tile's: rounded base plus a whole number of cells
-            TileFrame tf;
-            {
-                const float sbx = (float)pl.base[0], sby = (float)pl.base[1], sbz = (float)pl.base[2];
-                const float ofx = (float)la * A.m.h32[0], ofy = (float)lb * A.m.h32[1], ofz = (float)lc * A.m.h32[2];
-                tf.bx = sbx + ofx; tf.by = sby + ofy; tf.bz = sbz + ofz;
-                tf.babs = fabsf(sbx) + fabsf(sby) + fabsf(sbz) + 2.f * (fabsf(ofx) + fabsf(ofy) + fabsf(ofz)) +
-                          fabsf(tf.bx) + fabsf(tf.by) + fabsf(tf.bz);
-                tf.e64 = pl.e64;
+            const Defer df{A.rq, A.rq_cap, &A.cnt->n_recheck, idx, s, overflow};
+            const int cnt = count_listed_cell<true>(A, s, idx, &rechecks, &df);
+            __syncwarp();
+            if (lane == 0) {
+                A.alpha[idx] = -1.f - (float)cnt;
+                if (*(volatile int32_t*)overflow) {
+                    *overflow = 0;
+                    const int slot = atomicAdd(&A.cnt->n_ovf, 1);
+                    if (slot < A.ovf_cap) A.ovf[slot] = Recheck{idx, s, 0u};
+                    else set_error(A.cnt, DERR_CAPACITY);
+                }
             }
-            float M[9];
-#pragma unroll
-            for (int r = 0; r < 9; ++r) M[r] = pl.M[r];
-            const Q4 q = state_quat(A.st[s]);
-            const D3 x = state_pos(A.st[s]);
-            const Defer df{A.rq, A.rq_cap, &A.cnt->n_recheck, idx, s};
-            const int cnt = subsample_warp(A.m, k.shape, M, tf, 0, 0, 0, x, q, pl.lo[0] + la, pl.lo[1] + lb,
-                                           pl.lo[2] + lc, A.n, &rechecks, A.rq ? &df : nullptr);
-            if (lane == 0) A.alpha[idx] = A.rq ? -1.f - (float)cnt : count_fraction(A.m, cnt, A.n);
+            __syncwarp();
         }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);
+    if (lane == 0 && rechecks) atomicAdd(&A.cnt->exact_rechecks, rechecks);
+}
+
+// Cells of the fallback whose undecided points overflowed the recheck list: counted again from scratch, undecided
+// points in FP64 in place, after recheck_kernel (whose updates of these cells the new count replaces).
+__global__ void __launch_bounds__(256) recount_kernel(FallbackArgs A) {
+    const int lane = threadIdx.x & 31;
+    const int64_t n = min((int64_t)A.cnt->n_ovf, A.ovf_cap);
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    unsigned long long rechecks = 0;
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n; w += warps) {
+        const Recheck r = A.ovf[w];
+        const int cnt = count_listed_cell<false>(A, r.solid, r.idx, &rechecks, nullptr);
+        if (lane == 0) A.alpha[r.idx] = -1.f - (float)cnt;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);

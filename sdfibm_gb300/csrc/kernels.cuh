@@ -104,7 +104,7 @@ struct Counters {
     int32_t n_feat;           // LEARNED: cut cells whose features the classify pass wrote this call
     int32_t n_fb;             // LEARNED: of those, cells outside the model's band (SUBSAMPLE fallback)
     int32_t n_recheck;        // SUBSAMPLE points left to recheck_kernel this call
-    int32_t pad3;
+    int32_t n_ovf;            // LEARNED: fallback cells whose points overflowed the recheck list (recount_kernel)
 };
 
 // list lengths clamped to the capacity (a capacity error leaves the counters above what was written)
@@ -204,6 +204,8 @@ struct FallbackArgs {
     int n;                     // samples per axis
     Recheck* rq;
     int64_t rq_cap;
+    Recheck* ovf;              // cells to recount (idx, solid), see recount_kernel
+    int64_t ovf_cap;
 };
 
 // UGrid (src/libcollision/ugrid.h:14-58): bbox of the mesh, spacing 2*max radiusB, row-major i*ny*nz + j*nz + k

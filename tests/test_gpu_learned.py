@@ -15,25 +15,29 @@ AS_MEAN = 1e-3   # learned path: mean |As - As_SUBSAMPLE(4096)| over the cut cel
 F_REL = 1e-4     # learned path: per-solid force, normwise against the sum of |contributions|
 
 
-def _learned_pair(torch, w, params, tau_twist, tau_grad):
+def _learned_pair(torch, w, params, tau_twist, tau_grad, recheck_cap=0):
     orc_w = copy.copy(w)
     orc_w.opt = abi.options(rho_f=w.opt.rho_f, collision_mode=w.opt.collision_mode,
                             fraction_method=abi.FRACTION_SUBSAMPLE, subsample_n=16)
     gpu_opt = abi.options(rho_f=w.opt.rho_f, collision_mode=w.opt.collision_mode,
-                          fraction_method=abi.FRACTION_LEARNED, learned_fallback_n=16)
+                          fraction_method=abi.FRACTION_LEARNED, learned_fallback_n=16, recheck_cap=recheck_cap)
     r = run_pair(torch, orc_w, gpu_opt=gpu_opt,
                  gpu_setup=lambda c: c.set_fraction_model(params, tau_twist, tau_grad))
     return orc_w, r
 
 
-def test_band_closed_is_subsample16(cuda_lib, torch_cuda):
-    """With the band closed every cut cell takes the SUBSAMPLE fallback: the contract of the plain method holds."""
+@pytest.mark.parametrize("recheck_cap", [0, 50])
+def test_band_closed_is_subsample16(cuda_lib, torch_cuda, recheck_cap):
+    """With the band closed every cut cell takes the SUBSAMPLE fallback: the contract of the plain method holds.
+    A recheck list of 50 entries overflows at once: the cells whose points it could not take are recounted."""
     w = workloads.poly3d_256(scale=0.25)
-    orc_w, r = _learned_pair(torch_cuda, w, learned.init_params(0), -1.0, -1.0)
+    orc_w, r = _learned_pair(torch_cuda, w, learned.init_params(0), -1.0, -1.0, recheck_cap)
     check_interact(orc_w, r)
     st = r["gpu"].stats()
     assert st["learned_cells"] == st["cut_cells"] > 0
     assert st["learned_fallback_cells"] == st["learned_cells"]
+    if recheck_cap:
+        assert st["fp64_rechecks"] > 2 * recheck_cap
 
 
 def test_band_open_predicts_every_cut_cell(cuda_lib, torch_cuda):

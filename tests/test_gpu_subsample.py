@@ -51,3 +51,15 @@ def test_convex_lattice_counts(cuda_lib, torch_cuda, n):
     r = run_pair(torch_cuda, w)
     s = check_interact(w, r)
     assert s["coupling_cells"] > 1000
+
+
+def test_recheck_list_overflow(cuda_lib, torch_cuda):
+    """A recheck list of 20 entries: the undecided points it cannot take are re-evaluated in place."""
+    import copy
+    w = _convex_zoo(40)
+    w.opt.subsample_n = 10
+    gpu_opt = copy.copy(w.opt)
+    gpu_opt.recheck_cap = 20
+    r = run_pair(torch_cuda, w, gpu_opt=gpu_opt)
+    check_interact(w, r)
+    assert r["gpu"].stats()["fp64_rechecks"] > 40
