@@ -354,32 +354,40 @@ __device__ inline int block_log2(int n, bool flat) {
 }
 
 // Run counting for the convex shapes (3-D): the inside samples of a lattice column (a, b) are one run, since the
-// exact inside function q is convex along the column's line.  The run's ends come from the FP32 intersection of the
-// line with the shape (any error there only costs time); a few samples, computed and bounded exactly as the walk
-// computes them, then decide the whole column:
+// exact inside function q is convex along the column's line.  Along the column the local coordinates are
+// w + c d (c the sample index), so the quadric is the polynomial A c^2 + 2 B c + C and the box the maximum of three
+// |w + c d| - k.  The run's ends come from their FP32 roots (any error there only costs time); the polynomial values
+// at a few samples, within Egh of q there, then decide the whole column:
 //   run [c1, c2] found: c1 and c2 inside, c1 - 1 and c2 + 1 outside (or off the column).  Every sample between the
 //     ends is inside (q there is at most its value at the ends) and every sample past c2 + 1 outside (q grows past a
 //     rise from an inside to an outside sample), and likewise before c1 - 1;
 //   no sample in the interval: the sample cv nearest the closest approach and its neighbours outside, with q
-//     certified to rise from cv to each neighbour (computed rise of at least 2 Eg, each value being within Eg of
-//     exact); every sample past a neighbour is then outside.
-// A column that does not verify (an undecided sample, a run end off by one, a flat approach) is walked sample by
-// sample.  The count is therefore the exhaustive lattice count.
+//     certified to rise from cv to each neighbour (computed rise of at least 2 Egh); every sample past a neighbour
+//     is then outside.
+// A column that does not verify (a value within Egh of zero, a run end off by one, a flat approach) is walked sample
+// by sample with the coordinates, bound and deferral of subsample_count.  The count is therefore the exhaustive
+// lattice count.
+//
+// Egh: the polynomial's value differs from the walk's coordinates-then-shape evaluation by the roundings of w, d,
+// the coefficients and the Horner steps, each a few units of roundoff of the magnitudes sum k X^2 + k3 (quadric) or
+// max |X| + max k (box) over the cell; the caller adds 64 (quadric) or 32 (box) units of roundoff of those sums to Eg.
 template <int T, bool DEFER_ONLY>
-__device__ __noinline__ int subsample_runs(const MeshK& m, const ShapeK& sh, const SampleFrame& f, int64_t i,
-                                           int64_t j, int64_t k, int n, const D3& x, const Q4& q,
+__device__ __noinline__ int subsample_runs(const MeshK& m, const ShapeK& sh, const SampleFrame& f, float Egh,
+                                           int64_t i, int64_t j, int64_t k, int n, const D3& x, const Q4& q,
                                            unsigned long long* rechecks, const Defer* df) {
     __shared__ uint16_t s_walk[8][128];  // columns of each warp left to the sample-by-sample walk
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     uint16_t* walk_list = s_walk[(threadIdx.x >> 5) & 7];
     const float inv2n = 1.0f / (float)(2 * n), nf = (float)n, invn = 1.0f / nf;
-    const float rise = 2.0001f * f.Eg;
-    // quadric along the column: q(t) = A t^2 + 2 B t + C, t the column coordinate of the samples (2c + 1) / (2n);
-    // box: slab of axis a between t = (-k_a - b_a) / s_a and (k_a - b_a) / s_a
-    const float A = f.k0 * f.szx * f.szx + f.k1 * f.szy * f.szy + f.k2 * f.szz * f.szz;
+    const float rise = 2.0001f * Egh;
+    // per-sample step along the column and the per-cell parts of the polynomial
+    const float dx = f.szx * invn, dy = f.szy * invn, dz = f.szz * invn;
+    const float kdx = f.k0 * dx, kdy = f.k1 * dy, kdz = f.k2 * dz;
+    const float A = __fmaf_rn(dx, kdx, __fmaf_rn(dy, kdy, dz * kdz));
     const float invA = 1.0f / A;
-    const float isx = 1.0f / f.szx, isy = 1.0f / f.szy, isz = 1.0f / f.szz;
+    const float idx_ = 1.0f / dx, idy = 1.0f / dy, idz = 1.0f / dz;
+    const float kx0 = f.k0 * idx_, ky0 = f.k1 * idy, kz0 = f.k2 * idz;
     auto column_base = [&](int col, int& ia, int& ib, float& bx, float& by, float& bz) {
         ib = __float2int_rz(((float)col + 0.5f) * invn);
         ia = col - ib * n;
@@ -408,46 +416,52 @@ __device__ __noinline__ int subsample_runs(const MeshK& m, const ShapeK& sh, con
         float bx = 0.f, by = 0.f, bz = 0.f;
         if (col < n * n) {
             column_base(col, ia, ib, bx, by, bz);
-            auto g_at = [&](int c3) {
-                const float tc = (float)(2 * c3 + 1) * inv2n;
-                return sample_g<T>(f, __fmaf_rn(tc, f.szx, bx), __fmaf_rn(tc, f.szy, by), __fmaf_rn(tc, f.szz, bz));
-            };
-            float tl, tr;
+            // coordinates of sample c: w + c d
+            const float wx = __fmaf_rn(f.szx, inv2n, bx), wy = __fmaf_rn(f.szy, inv2n, by),
+                        wz = __fmaf_rn(f.szz, inv2n, bz);
+            float B2 = 0.f, C = 0.f;
+            float cl, cr;
             if (T == SS_QUADRIC) {
-                const float B = f.k0 * bx * f.szx + f.k1 * by * f.szy + f.k2 * bz * f.szz;
-                const float C = f.k0 * bx * bx + f.k1 * by * by + f.k2 * bz * bz - f.k3;
-                const float disc = B * B - A * C;
-                const float sq = disc > 0.f ? sqrtf(disc) : 0.f;
-                tl = (-B - sq) * invA;
-                tr = disc > 0.f ? (-B + sq) * invA : tl - 1.f;  // empty: tl marks the closest approach
+                const float B = __fmaf_rn(wx, kdx, __fmaf_rn(wy, kdy, wz * kdz));
+                C = __fmaf_rn(wx * wx, f.k0, __fmaf_rn(wy * wy, f.k1, (wz * wz) * f.k2)) - f.k3;
+                B2 = 2.f * B;
+                const float disc = __fmaf_rn(B, B, -A * C);
+                const float sq = disc > 0.f ? disc * rsqrtf(disc) : 0.f;  // approximate: only locates the run
+                cl = (-B - sq) * invA;
+                cr = disc > 0.f ? (-B + sq) * invA : cl - 1.f;  // empty: cl marks the closest approach
             } else {
-                const float lx = (-f.k0 - bx) * isx, rx = (f.k0 - bx) * isx;
-                const float ly = (-f.k1 - by) * isy, ry = (f.k1 - by) * isy;
-                const float lz = (-f.k2 - bz) * isz, rz = (f.k2 - bz) * isz;
-                tl = fmaxf(fmaxf(fminf(lx, rx), fminf(ly, ry)), fminf(lz, rz));
-                tr = fminf(fminf(fmaxf(lx, rx), fmaxf(ly, ry)), fmaxf(lz, rz));
+                const float lx = __fmaf_rn(-wx, idx_, -kx0), rx = __fmaf_rn(-wx, idx_, kx0);
+                const float ly = __fmaf_rn(-wy, idy, -ky0), ry = __fmaf_rn(-wy, idy, ky0);
+                const float lz = __fmaf_rn(-wz, idz, -kz0), rz = __fmaf_rn(-wz, idz, kz0);
+                cl = fmaxf(fmaxf(fminf(lx, rx), fminf(ly, ry)), fminf(lz, rz));
+                cr = fminf(fminf(fmaxf(lx, rx), fmaxf(ly, ry)), fmaxf(lz, rz));
             }
-            // sample indices c with t_c in [tl, tr]: t_c n - 1/2 = c (clamped before the conversion: inf / NaN safe)
-            const float ul = fminf(fmaxf(tl * nf - 0.5f, -2.f), nf + 1.f);
-            const float ur = fminf(fmaxf(tr * nf - 0.5f, -2.f), nf + 1.f);
+            auto g_at = [&](int c3) {
+                const float c = (float)c3;
+                if (T == SS_QUADRIC) return __fmaf_rn(__fmaf_rn(A, c, B2), c, C);
+                return fmaxf(fmaxf(fabsf(__fmaf_rn(c, dx, wx)) - f.k0, fabsf(__fmaf_rn(c, dy, wy)) - f.k1),
+                             fabsf(__fmaf_rn(c, dz, wz)) - f.k2);
+            };
+            // clamped before the conversions (inf / NaN safe)
+            const float ul = fminf(fmaxf(cl, -2.f), nf + 1.f), ur = fminf(fmaxf(cr, -2.f), nf + 1.f);
             const int c1 = max((int)ceilf(ul), 0), c2 = min((int)floorf(ur), n - 1);
             res = -1;
-            if (tl <= tr && c1 <= c2) {
-                const int r1 = band(g_at(c1), f.Eg), r2 = c2 == c1 ? r1 : band(g_at(c2), f.Eg);
-                const int rl = c1 > 0 ? band(g_at(c1 - 1), f.Eg) : 0, rr = c2 < n - 1 ? band(g_at(c2 + 1), f.Eg) : 0;
+            if (cl <= cr && c1 <= c2) {
+                const int r1 = band(g_at(c1), Egh), r2 = c2 == c1 ? r1 : band(g_at(c2), Egh);
+                const int rl = c1 > 0 ? band(g_at(c1 - 1), Egh) : 0, rr = c2 < n - 1 ? band(g_at(c2 + 1), Egh) : 0;
                 if (r1 == 1 && r2 == 1 && rl == 0 && rr == 0) res = c2 - c1 + 1;
             } else {
-                const float um = (T == SS_QUADRIC && !(tl <= tr)) ? ul : 0.5f * (ul + ur);
+                const float um = (T == SS_QUADRIC && !(cl <= cr)) ? ul : 0.5f * (ul + ur);
                 const int cv = min(max(__float2int_rn(fminf(fmaxf(um, 0.f), nf - 1.f)), 0), n - 1);
                 const float g0 = g_at(cv);
-                bool ok = band(g0, f.Eg) == 0;
+                bool ok = band(g0, Egh) == 0;
                 if (ok && cv + 1 < n) {
                     const float g1 = g_at(cv + 1);
-                    ok = band(g1, f.Eg) == 0 && (cv + 2 >= n || g1 - g0 >= rise);
+                    ok = band(g1, Egh) == 0 && (cv + 2 >= n || g1 - g0 >= rise);
                 }
                 if (ok && cv > 0) {
                     const float g1 = g_at(cv - 1);
-                    ok = band(g1, f.Eg) == 0 && (cv < 2 || g1 - g0 >= rise);
+                    ok = band(g1, Egh) == 0 && (cv < 2 || g1 - g0 >= rise);
                 }
                 if (ok) res = 0;
             }
@@ -549,17 +563,19 @@ static __device__ __noinline__ int subsample_warp(const MeshK& m, const ShapeK& 
         }
         f.Eg = (2.f * (mx * f.k0 + my * f.k1 + mz * f.k2) + Ep * (f.k0 + f.k1 + f.k2)) * Ep +
                10.f * u * (mx * mx * f.k0 + my * my * f.k1 + mz * mz * f.k2 + f.k3);
+        const float Egh = f.Eg + 64.f * u * (mx * mx * f.k0 + my * my * f.k1 + mz * mz * f.k2 + f.k3);
         const int lb = block_log2(n, m.twod != 0);
         cnt = lb ? subsample_blocks<SS_QUADRIC, DEFER_ONLY>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks, df)
-              : use_runs ? subsample_runs<SS_QUADRIC, DEFER_ONLY>(m, sh, f, i, j, k, n, x, q, rechecks, df)
+              : use_runs ? subsample_runs<SS_QUADRIC, DEFER_ONLY>(m, sh, f, Egh, i, j, k, n, x, q, rechecks, df)
                          : subsample_count<SS_QUADRIC, DEFER_ONLY>(m, sh, f, i, j, k, n, x, q, rechecks, df);
     } else if (kind == SS_BOX) {
         f.k0 = a[0]; f.k1 = a[1];
         f.k2 = prism ? INFINITY : a[2];  // the rectangle has no z extent
         f.Eg = Ep + 2.f * u * (fmaxf(mx, fmaxf(my, prism ? 0.f : mz)) + fmaxf(a[0], fmaxf(a[1], prism ? 0.f : a[2])));
+        const float Egh = f.Eg + 32.f * u * (fmaxf(mx, fmaxf(my, mz)) + fmaxf(a[0], fmaxf(a[1], a[2])));
         const int lb = block_log2(n, m.twod != 0);
         cnt = lb ? subsample_blocks<SS_BOX, DEFER_ONLY>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks, df)
-              : use_runs ? subsample_runs<SS_BOX, DEFER_ONLY>(m, sh, f, i, j, k, n, x, q, rechecks, df)
+              : use_runs ? subsample_runs<SS_BOX, DEFER_ONLY>(m, sh, f, Egh, i, j, k, n, x, q, rechecks, df)
                          : subsample_count<SS_BOX, DEFER_ONLY>(m, sh, f, i, j, k, n, x, q, rechecks, df);
     } else {
         cnt = subsample_count<SS_GENERIC, DEFER_ONLY>(m, sh, f, i, j, k, n, x, q, rechecks, df);
