@@ -372,9 +372,9 @@ __device__ inline int block_log2(int n, bool flat) {
 // the coefficients and the Horner steps, each a few units of roundoff of the magnitudes sum k X^2 + k3 (quadric) or
 // max |X| + max k (box) over the cell; the caller adds 64 (quadric) or 32 (box) units of roundoff of those sums to Eg.
 template <int T, bool DEFER_ONLY>
-__device__ __noinline__ int subsample_runs(const MeshK& m, const ShapeK& sh, const SampleFrame& f, float Egh,
-                                           int64_t i, int64_t j, int64_t k, int n, const D3& x, const Q4& q,
-                                           unsigned long long* rechecks, const Defer* df) {
+__device__ __forceinline__ int subsample_runs_body(const MeshK& m, const ShapeK& sh, const SampleFrame& f, float Egh,
+                                                   int64_t i, int64_t j, int64_t k, int n, const D3& x, const Q4& q,
+                                                   unsigned long long* rechecks, const Defer* df) {
     __shared__ uint16_t s_walk[8][128];  // columns of each warp left to the sample-by-sample walk
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -497,13 +497,21 @@ __device__ __noinline__ int subsample_runs(const MeshK& m, const ShapeK& sh, con
     return cnt;
 }
 
+// out of line for the classify pass; the fallback kernel inlines the body (DEFER_ONLY, no FP64 path)
+template <int T, bool DEFER_ONLY>
+__device__ __noinline__ int subsample_runs(const MeshK& m, const ShapeK& sh, const SampleFrame& f, float Egh, int64_t i,
+                                           int64_t j, int64_t k, int n, const D3& x, const Q4& q,
+                                           unsigned long long* rechecks, const Defer* df) {
+    return subsample_runs_body<T, DEFER_ONLY>(m, sh, f, Egh, i, j, k, n, x, q, rechecks, df);
+}
+
 // Inside count of the cell's n^3 (n^2 on one-layer meshes) lattice; with a Defer the undecided points are not counted
-// here but appended to the recheck list.
+// here but appended to the recheck list.  DEFER_ONLY: x, q and (i, j, k) only feed the FP64 path, which it lacks.
 template <bool DEFER_ONLY>
-static __device__ __noinline__ int subsample_warp(const MeshK& m, const ShapeK& sh, const float* M, const TileFrame& tf,
-                                                  int a0, int b0, int c0, const D3& x, const Q4& q, int64_t i,
-                                                  int64_t j, int64_t k, int n, unsigned long long* rechecks,
-                                                  const Defer* df) {
+static __device__ __forceinline__ int subsample_warp_body(const MeshK& m, const ShapeK& sh, const float* M,
+                                                          const TileFrame& tf, int a0, int b0, int c0, const D3& x,
+                                                          const Q4& q, int64_t i, int64_t j, int64_t k, int n,
+                                                          unsigned long long* rechecks, const Defer* df) {
     const float u = U32;
     const float hx = m.h32[0], hy = m.h32[1], hz = m.h32[2];
     const float ox = (float)a0 * hx, oy = (float)b0 * hy, oz = (float)c0 * hz;  // cell corner within the tile
@@ -551,8 +559,9 @@ static __device__ __noinline__ int subsample_warp(const MeshK& m, const ShapeK& 
     const float mx = fabsf(f.px) + fabsf(f.sxx) + fabsf(f.syx) + fabsf(f.szx) + Ep;
     const float my = fabsf(f.py) + fabsf(f.sxy) + fabsf(f.syy) + fabsf(f.szy) + Ep;
     const float mz = fabsf(f.pz) + fabsf(f.sxz) + fabsf(f.syz) + fabsf(f.szz) + Ep;
-    // 3-D convex shapes: lattices of 5 to 15 per axis count runs along columns, larger ones skip 4 x 4 x 4 blocks
-    const bool use_runs = !m.twod && !prism && n >= 5 && n < 16;
+    // 3-D convex shapes count runs along columns from 5 samples per axis; out of line (the classify pass), lattices
+    // of 16 and more skip 4 x 4 x 4 blocks instead
+    const bool use_runs = !m.twod && !prism && n >= 5 && (DEFER_ONLY || n < 16);
     int cnt;
     if (kind == SS_QUADRIC) {
         switch (type) {
@@ -565,22 +574,40 @@ static __device__ __noinline__ int subsample_warp(const MeshK& m, const ShapeK& 
                10.f * u * (mx * mx * f.k0 + my * my * f.k1 + mz * mz * f.k2 + f.k3);
         const float Egh = f.Eg + 64.f * u * (mx * mx * f.k0 + my * my * f.k1 + mz * mz * f.k2 + f.k3);
         const int lb = block_log2(n, m.twod != 0);
-        cnt = lb ? subsample_blocks<SS_QUADRIC, DEFER_ONLY>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks, df)
-              : use_runs ? subsample_runs<SS_QUADRIC, DEFER_ONLY>(m, sh, f, Egh, i, j, k, n, x, q, rechecks, df)
-                         : subsample_count<SS_QUADRIC, DEFER_ONLY>(m, sh, f, i, j, k, n, x, q, rechecks, df);
+        if (use_runs && DEFER_ONLY)
+            cnt = subsample_runs_body<SS_QUADRIC, true>(m, sh, f, Egh, i, j, k, n, x, q, rechecks, df);
+        else if (use_runs)
+            cnt = subsample_runs<SS_QUADRIC, DEFER_ONLY>(m, sh, f, Egh, i, j, k, n, x, q, rechecks, df);
+        else if (lb)
+            cnt = subsample_blocks<SS_QUADRIC, DEFER_ONLY>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks, df);
+        else
+            cnt = subsample_count<SS_QUADRIC, DEFER_ONLY>(m, sh, f, i, j, k, n, x, q, rechecks, df);
     } else if (kind == SS_BOX) {
         f.k0 = a[0]; f.k1 = a[1];
         f.k2 = prism ? INFINITY : a[2];  // the rectangle has no z extent
         f.Eg = Ep + 2.f * u * (fmaxf(mx, fmaxf(my, prism ? 0.f : mz)) + fmaxf(a[0], fmaxf(a[1], prism ? 0.f : a[2])));
         const float Egh = f.Eg + 32.f * u * (fmaxf(mx, fmaxf(my, mz)) + fmaxf(a[0], fmaxf(a[1], a[2])));
         const int lb = block_log2(n, m.twod != 0);
-        cnt = lb ? subsample_blocks<SS_BOX, DEFER_ONLY>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks, df)
-              : use_runs ? subsample_runs<SS_BOX, DEFER_ONLY>(m, sh, f, Egh, i, j, k, n, x, q, rechecks, df)
-                         : subsample_count<SS_BOX, DEFER_ONLY>(m, sh, f, i, j, k, n, x, q, rechecks, df);
+        if (use_runs && DEFER_ONLY)
+            cnt = subsample_runs_body<SS_BOX, true>(m, sh, f, Egh, i, j, k, n, x, q, rechecks, df);
+        else if (use_runs)
+            cnt = subsample_runs<SS_BOX, DEFER_ONLY>(m, sh, f, Egh, i, j, k, n, x, q, rechecks, df);
+        else if (lb)
+            cnt = subsample_blocks<SS_BOX, DEFER_ONLY>(m, sh, f, i, j, k, n, lb, Ep, x, q, rechecks, df);
+        else
+            cnt = subsample_count<SS_BOX, DEFER_ONLY>(m, sh, f, i, j, k, n, x, q, rechecks, df);
     } else {
         cnt = subsample_count<SS_GENERIC, DEFER_ONLY>(m, sh, f, i, j, k, n, x, q, rechecks, df);
     }
     return cnt;
+}
+
+// the out-of-line form of the classify pass and of the recount (FP64 path included)
+static __device__ __noinline__ int subsample_warp(const MeshK& m, const ShapeK& sh, const float* M, const TileFrame& tf,
+                                                  int a0, int b0, int c0, const D3& x, const Q4& q, int64_t i,
+                                                  int64_t j, int64_t k, int n, unsigned long long* rechecks,
+                                                  const Defer* df) {
+    return subsample_warp_body<false>(m, sh, M, tf, a0, b0, c0, x, q, i, j, k, n, rechecks, df);
 }
 
 // the fraction of a complete count (cnt and n^3 are exact in FP32: one correct rounding)
@@ -885,7 +912,7 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                     const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
                     const int64_t li = local_index(a, b, c);
                     const Defer df{A.rq, A.rq_cap, &A.cnt->n_recheck, k.scratch_off + li, s, nullptr};
-                    const int cnt = subsample_warp<false>(m, sh, M, tf, a, b, c, x, q, I0 + a, J0 + b, K0 + c,
+                    const int cnt = subsample_warp(m, sh, M, tf, a, b, c, x, q, I0 + a, J0 + b, K0 + c,
                                                    A.subsample_n, &rechecks, A.rq ? &df : nullptr);
                     if (lane == 0) alpha[li] = A.rq ? -1.f - (float)cnt : count_fraction(m, cnt, A.subsample_n);
                 }
@@ -915,7 +942,8 @@ __device__ __forceinline__ int count_listed_cell(const FallbackArgs& A, int s, i
     const SolidK& k = A.sk[s];
     const SolidPlan& pl = A.plan[s];
     const int local = (int)(idx - k.scratch_off);  // < bbox cells of one solid
-    const int la = local % k.ext[0], lb = (local / k.ext[0]) % k.ext[1], lc = local / (k.ext[0] * k.ext[1]);
+    const int row = local / k.ext[0], lc = row / k.ext[1];
+    const int la = local - row * k.ext[0], lb = row - lc * k.ext[1];
     TileFrame tf;
     {
         const float sbx = (float)pl.base[0], sby = (float)pl.base[1], sbz = (float)pl.base[2];
@@ -928,10 +956,14 @@ __device__ __forceinline__ int count_listed_cell(const FallbackArgs& A, int s, i
     float M[9];
 #pragma unroll
     for (int r = 0; r < 9; ++r) M[r] = pl.M[r];
+    if (DEFER_ONLY) {  // inlined; the FP64 state is not needed
+        return subsample_warp_body<true>(A.m, k.shape, M, tf, 0, 0, 0, D3{0, 0, 0}, Q4{1, D3{0, 0, 0}}, 0, 0, 0, A.n,
+                                         rechecks, df);
+    }
     const Q4 q = state_quat(A.st[s]);
     const D3 x = state_pos(A.st[s]);
-    return subsample_warp<DEFER_ONLY>(A.m, k.shape, M, tf, 0, 0, 0, x, q, pl.lo[0] + la, pl.lo[1] + lb,
-                                      pl.lo[2] + lc, A.n, rechecks, df);
+    return subsample_warp(A.m, k.shape, M, tf, 0, 0, 0, x, q, pl.lo[0] + la, pl.lo[1] + lb, pl.lo[2] + lc, A.n,
+                          rechecks, df);
 }
 
 // LEARNED fallback: one warp per cell outside the network's band.  Undecided points always go to the recheck list
