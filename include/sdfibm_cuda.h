@@ -178,8 +178,12 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
 int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs, float* Ts,
                          int32_t* Ct, double* FT);
 
-/* Same as sdfibm_cuda_interact but every field pointer is a HOST pointer: the call copies U in and the four
- * fields out around the device work (the path an OpenFOAM-resident caller takes). */
+/* Same as sdfibm_cuda_interact but every field pointer is a HOST pointer (the path an OpenFOAM-resident caller
+ * takes).  U is copied in on a second stream while the enumeration and fraction kernels run.  Page-locked fields
+ * (cudaHostAlloc / cudaHostRegister) are written in place with the cells this call or the previous one touched,
+ * while the call gets the same five buffers as the previous one and the caller leaves the four fields alone in
+ * between (the first call, other buffers, or dense_reset copy the whole fields); other host memory receives
+ * whole-field copies. */
 int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs,
                               float* Ts, int32_t* Ct, double* FT);
 
@@ -217,7 +221,9 @@ int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc* mesh, const sdfibm_solid
 
 /* Counters of the last interact (host): [0] coupling cells (sum over solids of |T_s|), [1] cut cells,
  * [2] bbox cells scanned, [3] vertices re-checked in FP64, [4] work items, [5] kernel launches,
- * [6] cut cells given to the learned fraction model, [7] of those, cells outside its band (SUBSAMPLE fallback). */
+ * [6] cut cells given to the learned fraction model, [7] of those, cells outside its band (SUBSAMPLE fallback),
+ * [8] / [9] bytes the last sdfibm_cuda_interact_host moved host to device / device to host, [10] 1 when it wrote
+ * the touched cells only.  n: entries of out (at most 11 are written). */
 int sdfibm_cuda_stats(sdfibm_ctx* ctx, int64_t* out, int32_t n);
 
 /* No counterpart in the reference.  Autotuner of the classify work queue: times a few dense interacts (on the given

@@ -75,7 +75,9 @@ class SolidCloud:
         return FT[:self.nsolids] if want_ft else None
 
     def interact_host(self, time, dt, U, fields):
-        """Host (numpy) fields: the library copies U in and the fields out (pinned or pageable)."""
+        """Host (numpy) fields.  Page-locked field arrays (e.g. numpy views of torch pin_memory tensors) receive only
+        the cells that changed since the previous call on the same arrays, written in place; other arrays receive
+        whole-field copies."""
         FT = np.zeros((max(1, self.nsolids), 6))
         p = lambda a: a.ctypes.data_as(C.c_void_p)
         rc = self._L.sdfibm_cuda_interact_host(self._h, float(time), float(dt), p(U), p(fields["As"]), p(fields["Fs"]),
@@ -120,10 +122,10 @@ class SolidCloud:
         return out
 
     def stats(self):
-        out = (C.c_int64 * 8)()
-        self._check(self._L.sdfibm_cuda_stats(self._h, out, 8))
+        out = (C.c_int64 * 11)()
+        self._check(self._L.sdfibm_cuda_stats(self._h, out, 11))
         keys = ("coupling_cells", "cut_cells", "bbox_cells", "fp64_rechecks", "work_items", "launches",
-                "learned_cells", "learned_fallback_cells")
+                "learned_cells", "learned_fallback_cells", "host_h2d_bytes", "host_d2h_bytes", "host_sparse")
         return dict(zip(keys, list(out)))
 
     def autotune(self, dt, U, fields):

@@ -40,6 +40,10 @@ __global__ void claim_kernel(const int32_t* in_cell, const int32_t* in_solid, co
                              const int32_t* cut_solid, int32_t* Ct, const Counters* cnt, int64_t N);
 __global__ void ft_kernel(const double* ftacc, double* ft, int S, const StepParams* step);
 __global__ void set_step_kernel(StepParams* p, double time, double dt, int nsub, double rho_V);
+__global__ void mark_export_kernel(const int32_t* in_cell, const int32_t* cut_cell, const int32_t* prev_in_cell,
+                                   const int32_t* prev_cut_cell, const Counters* cnt, int64_t N, uint32_t* dirty);
+__global__ void export_kernel(Counters* cnt, int64_t N, uint32_t* dirty, const float* As, const float* Fs,
+                              const float* Ts, const int32_t* Ct, float* hAs, float* hFs, float* hTs, int32_t* hCt);
 __global__ void reset_kernel(const int32_t* in_cell, const int32_t* cut_cell, const Counters* cnt, int64_t N,
                              float* As, float* Fs, float* Ts, int32_t* Ct);
 __global__ void fix_internal_kernel(MeshK m, const sdfibm_solid_state* st, const int32_t* in_cell,
@@ -151,6 +155,13 @@ struct sdfibm_ctx {
     cudaStream_t copy_st[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t ev_entry = nullptr, ev_u = nullptr, ev_done = nullptr;
     cudaEvent_t u_wait = nullptr;  // set while interact_host runs: couple waits for the upload
+    // interact_host on page-locked host fields: the host buffers of the last such call (their cells equal the device
+    // fields after it) and the bytes the last interact_host moved each way
+    const void* host_fields[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool host_synced = false;
+    bool host_sparse = false;  // the last interact_host exported the touched cells only
+    int64_t host_h2d = 0, host_d2h = 0;
+    uint32_t* d_dirty = nullptr;  // changed 8-cell chunks of the fields, one bit each (cleared by export_kernel)
     int classify_grid = 0, couple_grid = 0;
     // per-kernel events (options.timing)
     static constexpr int MAXEV = 24;
@@ -740,6 +751,7 @@ int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U
     int launches = 0;
     mark_begin(ctx);
     const void* f5[5] = {U, As, Fs, Ts, Ct};
+    if (As != ctx->d_As) ctx->host_synced = false;  // the touched-cell lists no longer follow the host fields
     bool same = ctx->interacted;
     for (int i = 1; i < 5; ++i) same = same && f5[i] == ctx->last_fields[i];
     const bool dense = !same || ctx->opt.dense_reset;
@@ -782,28 +794,84 @@ int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U
     return SDFIBM_OK;
 }
 
+// device address of a page-locked host buffer (nullptr for any other memory)
+static void* mapped_host(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs,
                               float* Ts, int32_t* Ct, double* FT) {
     if (!ctx) return SDFIBM_ERR_ARG;
     if (!U || !As || !Fs || !Ts || !Ct) return fail(ctx, SDFIBM_ERR_ARG, "null field pointer");
     const int64_t N = ctx->mesh.ncells;
     cudaStream_t st = ctx->stream;
-    if (!ctx->d_U) {
-        if (dalloc(&ctx->d_U, 3 * N) || dalloc(&ctx->d_As, N) || dalloc(&ctx->d_Fs, 3 * N) || dalloc(&ctx->d_Ts, N) ||
-            dalloc(&ctx->d_Ct, N))
-            return fail(ctx, SDFIBM_ERR_CUDA, "staging allocation failed");
-    }
+    if (!ctx->d_U && dalloc(&ctx->d_U, 3 * N)) return fail(ctx, SDFIBM_ERR_CUDA, "staging allocation failed");
     if (!ctx->ev_u) {
         for (auto& c : ctx->copy_st) CK(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&ctx->ev_entry, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&ctx->ev_u, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming));
     }
-    // upload U once the previous work on the stream (which may still read d_U) is done; couple waits for it
+    if (!ctx->d_As) {
+        if (dalloc(&ctx->d_As, N) || dalloc(&ctx->d_Fs, 3 * N) || dalloc(&ctx->d_Ts, N) || dalloc(&ctx->d_Ct, N) ||
+            dalloc(&ctx->d_dirty, (N + 255) / 256) ||
+            cudaMemsetAsync(ctx->d_dirty, 0, sizeof(uint32_t) * ((N + 255) / 256), st) != cudaSuccess)
+            return fail(ctx, SDFIBM_ERR_CUDA, "staging allocation failed");
+    }
+    // upload U on a copy stream once the previous work on the stream (which may still read d_U) is done; the
+    // enumeration and fraction kernels run meanwhile and the coupling kernel waits for it
     CK(cudaEventRecord(ctx->ev_entry, st));
     CK(cudaStreamWaitEvent(ctx->copy_st[0], ctx->ev_entry, 0));
     CK(cudaMemcpyAsync(ctx->d_U, U, sizeof(float) * 3 * N, cudaMemcpyHostToDevice, ctx->copy_st[0]));
     CK(cudaEventRecord(ctx->ev_u, ctx->copy_st[0]));
+    // page-locked host fields take the cells that changed since the previous call, written in place (all of them on
+    // the first call, after a change of buffers, and with dense_reset); other memory gets whole-field copies
+    void* const hp[4] = {mapped_host(As), mapped_host(Fs), mapped_host(Ts), mapped_host(Ct)};
+    if (hp[0] && hp[1] && hp[2] && hp[3]) {
+        const void* f5[5] = {U, As, Fs, Ts, Ct};
+        bool same = ctx->host_synced && !ctx->opt.dense_reset;
+        for (int i = 0; i < 5; ++i) same = same && f5[i] == ctx->host_fields[i];
+        ctx->host_synced = false;
+        ctx->u_wait = ctx->ev_u;
+        int rc = sdfibm_cuda_interact(ctx, time, dt, ctx->d_U, ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, nullptr);
+        ctx->u_wait = nullptr;
+        if (rc) return rc;
+        if (same) {
+            const int p = ctx->cur ^ 1;
+            CK(cudaMemsetAsync(&ctx->d_cnt->n_export, 0, sizeof(int32_t), st));
+            mark_export_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(ctx->in_cell(), ctx->cut_cell(), ctx->d_lists[p][0],
+                                                                  ctx->d_lists[p][2], ctx->d_cnt, N, ctx->d_dirty);
+            export_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(
+                ctx->d_cnt, N, ctx->d_dirty, ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, static_cast<float*>(hp[0]),
+                static_cast<float*>(hp[1]), static_cast<float*>(hp[2]), static_cast<int32_t*>(hp[3]));
+            CK(cudaGetLastError());
+            mark(ctx, "export_kernel");
+        } else {
+            CK(cudaMemcpyAsync(As, ctx->d_As, sizeof(float) * N, cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(Fs, ctx->d_Fs, sizeof(float) * 3 * N, cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(Ts, ctx->d_Ts, sizeof(float) * N, cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(Ct, ctx->d_Ct, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, st));
+            mark(ctx, "host_copies");
+        }
+        if (ctx->S > 0)
+            CK(cudaMemcpyAsync(ctx->h_ft, ctx->d_ft, sizeof(double) * 6 * ctx->S, cudaMemcpyDeviceToHost, st));
+        rc = sync_counters(ctx);
+        if (rc) return rc;
+        const Counters& c = *ctx->h_cnt;
+        ctx->host_h2d = 12 * N;
+        ctx->host_d2h = (same ? 24 * 8 * (int64_t)c.n_export : 24 * N) + 48 * ctx->S;
+        ctx->host_sparse = same;
+        for (int i = 0; i < 5; ++i) ctx->host_fields[i] = f5[i];
+        ctx->host_synced = true;
+        if (FT) std::memcpy(FT, ctx->h_ft, sizeof(double) * 6 * ctx->S);
+        return SDFIBM_OK;
+    }
+    ctx->host_synced = false;
     ctx->u_wait = ctx->ev_u;
     int rc = sdfibm_cuda_interact(ctx, time, dt, ctx->d_U, ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, nullptr);
     ctx->u_wait = nullptr;
@@ -820,6 +888,9 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
     rc = sync_counters(ctx);
     for (auto& c : ctx->copy_st) CK(cudaStreamSynchronize(c));
     if (rc) return rc;
+    ctx->host_h2d = 12 * N;
+    ctx->host_d2h = 24 * N + 48 * ctx->S;
+    ctx->host_sparse = false;
     if (FT) std::memcpy(FT, ctx->h_ft, sizeof(double) * 6 * ctx->S);
     return SDFIBM_OK;
 }
@@ -1051,10 +1122,11 @@ int sdfibm_cuda_stats(sdfibm_ctx* ctx, int64_t* out, int32_t n) {
     int rc = sync_counters(ctx);
     if (rc) return rc;
     const Counters& c = *ctx->h_cnt;
-    const int64_t v[8] = {(int64_t)c.n_inside + c.n_cut, (int64_t)c.n_cut, (int64_t)c.bbox_cells,
-                          (int64_t)c.exact_rechecks, (int64_t)ctx->total_chunks, (int64_t)ctx->launches_last,
-                          (int64_t)c.n_feat, (int64_t)c.n_fb};
-    for (int i = 0; i < n && i < 8; ++i) out[i] = v[i];
+    const int64_t v[11] = {(int64_t)c.n_inside + c.n_cut, (int64_t)c.n_cut, (int64_t)c.bbox_cells,
+                           (int64_t)c.exact_rechecks, (int64_t)ctx->total_chunks, (int64_t)ctx->launches_last,
+                           (int64_t)c.n_feat, (int64_t)c.n_fb, ctx->host_h2d, ctx->host_d2h,
+                           (int64_t)ctx->host_sparse};
+    for (int i = 0; i < n && i < 11; ++i) out[i] = v[i];
     return SDFIBM_OK;
 }
 
@@ -1074,6 +1146,7 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
     if (ctx->d_small) cudaFree(ctx->d_small);
     if (ctx->d_rq) cudaFree(ctx->d_rq);
     if (ctx->d_ovf) cudaFree(ctx->d_ovf);
+    if (ctx->d_dirty) cudaFree(ctx->d_dirty);
     if (ctx->d_fsums) cudaFree(ctx->d_fsums);
     if (ctx->d_recs) cudaFree(ctx->d_recs);
     if (ctx->d_fsums_excl) cudaFree(ctx->d_fsums_excl);

@@ -806,6 +806,54 @@ __global__ void reset_kernel(const int32_t* __restrict__ prev_in_cell, const int
     }
 }
 
+// interact_host on page-locked host fields.  The host fields held the previous call's values; the cells this call or
+// the previous one touched (the current and the previous lists) are the ones that changed.  mark_export_kernel sets
+// their 8-cell chunks in a bitmap (one bit per chunk, one word per 256 cells); export_kernel then copies every marked
+// chunk from the device fields to the host fields through the mapped host pointers, a warp per bitmap word so that
+// each store instruction covers 32 consecutive cells (whole 32-byte sectors of the host arrays), and clears the word.
+__global__ void mark_export_kernel(const int32_t* __restrict__ in_cell, const int32_t* __restrict__ cut_cell,
+                                   const int32_t* __restrict__ prev_in_cell, const int32_t* __restrict__ prev_cut_cell,
+                                   const Counters* cnt, int64_t N, uint32_t* __restrict__ dirty) {
+    const int64_t n0 = clamp_len(cnt->n_inside, cnt->list_cap), n1 = clamp_len(cnt->n_cut, cnt->list_cap);
+    const int64_t n2 = clamp_len(cnt->prev_n_inside, cnt->list_cap), n3 = clamp_len(cnt->prev_n_cut, cnt->list_cap);
+    const int64_t total = n0 + n1 + n2 + n3;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        int64_t c;
+        if (e < n0) c = in_cell[e];
+        else if (e < n0 + n1) c = cut_cell[e - n0];
+        else if (e < n0 + n1 + n2) c = prev_in_cell[e - n0 - n1];
+        else c = prev_cut_cell[e - n0 - n1 - n2];
+        if (c < 0 || c >= N) continue;
+        const uint32_t bit = 1u << ((c >> 3) & 31);
+        if (!(dirty[c >> 8] & bit)) atomicOr(dirty + (c >> 8), bit);
+    }
+}
+
+__global__ void export_kernel(Counters* cnt, int64_t N, uint32_t* __restrict__ dirty, const float* __restrict__ As,
+                              const float* __restrict__ Fs, const float* __restrict__ Ts,
+                              const int32_t* __restrict__ Ct, float* hAs, float* hFs, float* hTs, int32_t* hCt) {
+    const int lane = threadIdx.x & 31;
+    const int64_t words = (N + 255) >> 8;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    int chunks = 0;
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += nw) {
+        const uint32_t word = dirty[w];
+        if (!word) continue;
+        chunks += __popc(word);
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int64_t c = (w << 8) + 32 * t + lane;
+            if (((word >> ((32 * t + lane) >> 3)) & 1u) && c < N) {
+                hAs[c] = As[c]; hTs[c] = Ts[c]; hCt[c] = Ct[c];
+                hFs[c] = Fs[c]; hFs[N + c] = Fs[N + c]; hFs[2 * N + c] = Fs[2 * N + c];
+            }
+        }
+        __syncwarp();
+        if (lane == 0) dirty[w] = 0u;
+    }
+    if (lane == 0 && chunks) atomicAdd(&cnt->n_export, chunks);
+}
+
 // SolidCloud::fixInternal over the ALL_INSIDE list: U = rigid velocity of the solid that owns the cell
 __global__ void fix_internal_kernel(MeshK m, const sdfibm_solid_state* __restrict__ st,
                                     const int32_t* __restrict__ in_cell, const int32_t* __restrict__ in_solid,

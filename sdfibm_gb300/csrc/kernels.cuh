@@ -99,7 +99,7 @@ struct Counters {
     unsigned long long exact_rechecks;  // FP32-undecided points re-evaluated in FP64
     unsigned long long bbox_cells;
     int32_t launches;
-    int32_t pad;
+    int32_t n_export;         // interact_host: 8-cell chunks written to the page-locked host fields
     int64_t list_cap;         // capacity of each touched-cell list (set once at create)
     int32_t n_feat;           // LEARNED: cut cells whose features the classify pass wrote this call
     int32_t n_fb;             // LEARNED: of those, cells outside the model's band (SUBSAMPLE fallback)

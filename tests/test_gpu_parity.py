@@ -137,3 +137,43 @@ def test_interact_host_matches_device(cuda_lib, torch_cuda):
     assert np.array_equal(fd["As"].cpu().numpy(), fh["As"])
     assert np.array_equal(fd["Ct"].cpu().numpy(), fh["Ct"])
     assert np.allclose(FTa, FTb, rtol=1e-12, atol=1e-14)
+    assert b.stats()["host_sparse"] == 0
+
+
+@pytest.mark.parametrize("cfg", ["poly3d_512", "sedimentation2d"])
+def test_interact_host_pinned_in_place(cuda_lib, torch_cuda, cfg):
+    """Page-locked host fields over several moving steps: only the changed cells are written back; the host fields
+    equal the device path's after every step, and a buffer change falls back to a whole copy."""
+    from sdfibm_gb300.cloud import SolidCloud
+    torch = torch_cuda
+    w = workloads.poly3d_512(scale=0.0625) if cfg == "poly3d_512" else workloads.sedimentation2d(scale=0.125)
+    N = w.ncells
+    U = torch.from_numpy(w.U_numpy()).pin_memory()
+    a = SolidCloud(w.mesh, w.solids, w.opt)
+    b = SolidCloud(w.mesh, w.solids, w.opt)
+    fd = a.new_fields()
+    Ud = U.cuda()
+
+    def pinned():
+        return {"As": torch.full((N,), 7.0).pin_memory(), "Fs": torch.full((3 * N,), 7.0).pin_memory(),
+                "Ts": torch.full((N,), 7.0).pin_memory(), "Ct": torch.full((N,), 7, dtype=torch.int32).pin_memory()}
+
+    fh = pinned()
+    hn = {k: v.numpy() for k, v in fh.items()}
+    t = 0.0
+    for step in range(4):
+        if step == 3:  # other host buffers: one whole copy
+            fh = pinned()
+            hn = {k: v.numpy() for k, v in fh.items()}
+        FTa = a.interact(t, w.dt, Ud, fd)
+        FTb = b.interact_host(t, w.dt, U.numpy(), hn)
+        for k in ("As", "Fs", "Ts", "Ct"):
+            assert np.array_equal(fd[k].cpu().numpy().reshape(-1), hn[k]), (step, k)
+        assert np.allclose(FTa, FTb, rtol=1e-12, atol=1e-14)
+        st = b.stats()
+        assert st["host_sparse"] == (1 if step in (1, 2) else 0), step
+        if st["host_sparse"]:
+            assert 0 < st["host_d2h_bytes"] < 24 * N and st["host_h2d_bytes"] == 12 * N
+        a.evolve(t, w.dt)
+        b.evolve(t, w.dt)
+        t += w.dt
