@@ -133,6 +133,23 @@ __global__ void plan_kernel(MeshK m, const SolidK* __restrict__ sk, const sdfibm
         p.pad1 = 0;
         const D3 cb = mesh_C(m, si, sj, sk3) - x;
         p.cbase[0] = cb.x; p.cbase[1] = cb.y; p.cbase[2] = cb.z;
+        // us at a cell (i, j, k) = us0 + omega x ((i, j, k) - seed) h: us0 and the six per-step terms, split into
+        // FP32 pairs (the couple kernel evaluates U - us in two-float arithmetic)
+        const D3 vel{st[s].vel[0], st[s].vel[1], st[s].vel[2]}, om{st[s].omega[0], st[s].omega[1], st[s].omega[2]};
+        const D3 us0 = vel + cross(om, cb);
+        const double u3[3] = {us0.x, us0.y, us0.z};
+        const double d6[6] = {-om.z * m.h[1], om.y * m.h[2], om.z * m.h[0], -om.x * m.h[2], -om.y * m.h[0],
+                              om.x * m.h[1]};
+        for (int a = 0; a < 3; ++a) {
+            p.us_hi[a] = (float)u3[a];
+            p.us_lo[a] = (float)(u3[a] - (double)p.us_hi[a]);
+            p.cb32[a] = (float)p.cbase[a];
+        }
+        for (int r = 0; r < 6; ++r) {
+            p.ds_hi[r] = (float)d6[r];
+            p.ds_lo[r] = (float)(d6[r] - (double)p.ds_hi[r]);
+        }
+        p.pad3 = 0.f;
     }
     // FP64 origin of the tile frames and the local map (world2local of the bbox corner plus the images of the cell
     // edge vectors), so tiles build their frames without per-tile FP64 work
@@ -627,6 +644,29 @@ __device__ __forceinline__ double warp_total4(double x) {
     return x;
 }
 
+// Two-float arithmetic (Dekker / Knuth): a + b = s + e and a * b = p + e exactly, with explicit rounding intrinsics
+// so that nothing is contracted or reassociated.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// U - (u0 + a p + b q) with u0, p, q given as FP32 pairs hi + lo and a, b small integers, rounded once to FP32 after
+// an error of about 2^-46 of the magnitudes
+__device__ __forceinline__ float ff_u_minus_us(float U, float u0h, float u0l, float a, float ph, float pl, float b,
+                                               float qh, float ql) {
+    const float t1 = __fmul_rn(a, ph), e1 = __fmaf_rn(a, ph, -t1);
+    const float t2 = __fmul_rn(b, qh), e2 = __fmaf_rn(b, qh, -t2);
+    float s1, f1, s2, f2;
+    two_sum(u0h, t1, s1, f1);
+    two_sum(s1, t2, s2, f2);
+    const float lo = __fadd_rn(__fadd_rn(__fadd_rn(u0l, __fadd_rn(e1, e2)), __fadd_rn(f1, f2)),
+                               __fmaf_rn(a, pl, __fmul_rn(b, ql)));
+    float d, g;
+    two_sum(U, -s2, d, g);
+    return __fadd_rn(d, __fsub_rn(g, lo));
+}
+
 // Per-cell forcing (pcHydrodynamicInteraction, solidcloud.cpp:384-390) and the force/torque sums (:411-421).
 // ftacc receives sum f and sum (C - x) x f; ft_kernel applies rho_f * V / dt once per solid.
 __global__ void __launch_bounds__(CPL_THREADS) couple_kernel(CoupleArgs A) {
@@ -685,17 +725,20 @@ __global__ void __launch_bounds__(CPL_THREADS) couple_kernel(CoupleArgs A) {
                 f6[0] = f_.x; f6[1] = f_.y; f6[2] = f_.z; f6[3] = t_.x; f6[4] = t_.y; f6[5] = t_.z;
                 fsx = (float)(f_.x * dtINV); fsy = (float)(f_.y * dtINV); fsz = (float)(f_.z * dtINV);
             } else {
-                // FP64 for the rigid-body velocity and U - us (the difference can cancel), FP32 after it.  C - x is
-                // the solid's FP64 seed offset plus a whole number of cells.
+                // U - us in two-float arithmetic (the difference can cancel; about 2^-46 of the magnitudes, against
+                // 2^-24 of the difference for the FP32 rounding that follows), FP32 after it.  The cell offsets from
+                // the seed are exact small integers.
                 const SolidPlan& pl = A.plan[s];
-                const D3 d{pl.cbase[0] + (double)(i - pl.seed_ijk[0]) * m.h[0],
-                           pl.cbase[1] + (double)(j - pl.seed_ijk[1]) * m.h[1],
-                           pl.cbase[2] + (double)(k - pl.seed_ijk[2]) * m.h[2]};
-                const D3 vel{st.vel[0], st.vel[1], st.vel[2]}, om{st.omega[0], st.omega[1], st.omega[2]};
-                const D3 us = vel + cross(om, d);
-                const float fx = alpha * (float)((double)Ux - us.x), fy = alpha * (float)((double)Uy - us.y),
-                            fz = alpha * (float)((double)Uz - us.z);
-                const float dx = (float)d.x, dy = (float)d.y, dz = (float)d.z;
+                const float di = (float)(i - pl.seed_ijk[0]), dj = (float)(j - pl.seed_ijk[1]),
+                            dk = (float)(k - pl.seed_ijk[2]);
+                const float fx = alpha * ff_u_minus_us(Ux, pl.us_hi[0], pl.us_lo[0], dj, pl.ds_hi[0], pl.ds_lo[0], dk,
+                                                       pl.ds_hi[1], pl.ds_lo[1]);
+                const float fy = alpha * ff_u_minus_us(Uy, pl.us_hi[1], pl.us_lo[1], di, pl.ds_hi[2], pl.ds_lo[2], dk,
+                                                       pl.ds_hi[3], pl.ds_lo[3]);
+                const float fz = alpha * ff_u_minus_us(Uz, pl.us_hi[2], pl.us_lo[2], di, pl.ds_hi[4], pl.ds_lo[4], dj,
+                                                       pl.ds_hi[5], pl.ds_lo[5]);
+                const float dx = __fmaf_rn(di, m.h32[0], pl.cb32[0]), dy = __fmaf_rn(dj, m.h32[1], pl.cb32[1]),
+                            dz = __fmaf_rn(dk, m.h32[2], pl.cb32[2]);
                 g6[0] = fx; g6[1] = fy; g6[2] = fz;
                 g6[3] = dy * fz - dz * fy; g6[4] = dz * fx - dx * fz; g6[5] = dx * fy - dy * fx;
                 fsx = fx * dtINV32; fsy = fy * dtINV32; fsz = fz * dtINV32;

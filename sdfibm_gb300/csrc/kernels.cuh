@@ -82,6 +82,12 @@ struct SolidPlan {
     double rcull;             // its radius
     int32_t vlo[3], vhi[3];   // mesh-vertex index box of the solid's oriented bounding box: vertices outside it are
                               // outside the solid (vlo > vhi on some axis: no vertex can be inside)
+    // mixed forcing: the rigid-body velocity at the seed cell centre and its change per cell step (components
+    // x: dj, dk; y: di, dk; z: di, dj) as FP32 pairs hi + lo, and cbase rounded to FP32
+    float us_hi[3], us_lo[3];
+    float ds_hi[6], ds_lo[6];
+    float cb32[3];
+    float pad3;
 };
 
 // Global counters / flags (one record per context, device memory).
