@@ -221,7 +221,8 @@ int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc* mesh, const sdfibm_solid
 
 /* Counters of the last interact (host): [0] coupling cells (sum over solids of |T_s|), [1] cut cells,
  * [2] bbox cells scanned, [3] vertices re-checked in FP64, [4] work items, [5] kernel launches,
- * [6] cut cells given to the learned fraction model, [7] of those, cells outside its band (SUBSAMPLE fallback),
+ * [6] cut cells listed for the fraction pass (LEARNED: given to the model; SUBSAMPLE: sampled from the list),
+ * [7] LEARNED: of those, cells outside the model's band (SUBSAMPLE fallback),
  * [8] / [9] bytes the last sdfibm_cuda_interact_host moved host to device / device to host, [10] 1 when it wrote
  * the touched cells only.  n: entries of out (at most 11 are written). */
 int sdfibm_cuda_stats(sdfibm_ctx* ctx, int64_t* out, int32_t n);

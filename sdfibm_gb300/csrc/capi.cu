@@ -20,7 +20,7 @@ __global__ void plan_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state*
                             Counters* cnt);
 void launch_classify(const ClassifyArgs& A, bool flat, int grid, cudaStream_t st);
 int classify_occupancy(int method, bool flat);
-__global__ void learned_fallback_kernel(FallbackArgs A);
+__global__ void subsample_cells_kernel(FallbackArgs A);
 __global__ void recount_kernel(FallbackArgs A);
 __global__ void recheck_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state* st, const SolidPlan* plan,
                                const Recheck* rq, int64_t cap, Counters* cnt, float* alpha);
@@ -486,6 +486,9 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         dalloc(&ctx->d_sh_used, (size_t)ctx->sh_mask + 1) || dalloc(&ctx->d_step, 2) ||
         dalloc(&ctx->d_small, small_solids.size()) || dalloc(&ctx->d_big, big_solids.size()) ||
         dalloc(&ctx->d_rq, (size_t)ctx->rq_cap) || dalloc(&ctx->d_ovf, (size_t)ctx->ovf_cap) ||
+        (ctx->opt.fraction_method == SDFIBM_FRACTION_SUBSAMPLE &&
+         (dalloc(&ctx->d_fref_solid, (size_t)(ctx->feat_cap = std::max<int64_t>(1, scratch))) ||
+          dalloc(&ctx->d_fref_index, (size_t)ctx->feat_cap))) ||
         cudaMallocHost((void**)&ctx->h_cnt, sizeof(Counters)) != cudaSuccess ||
         cudaMallocHost((void**)&ctx->h_ft, std::max<size_t>(1, 6 * (size_t)nsolids) * sizeof(double)) != cudaSuccess) {
         ctx->err = "device allocation failed";
@@ -591,7 +594,11 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
         CA.method = ctx->opt.fraction_method; CA.subsample_n = ctx->opt.subsample_n;
         const bool learned = ctx->opt.fraction_method == SDFIBM_FRACTION_LEARNED;
         const bool subsample = ctx->opt.fraction_method == SDFIBM_FRACTION_SUBSAMPLE;
-        if (subsample) { CA.rq = ctx->d_rq; CA.rq_cap = ctx->rq_cap; }
+        if (subsample) {
+            // cut cells listed by the classify pass, sampled by subsample_cells_kernel
+            CA.rq = ctx->d_rq; CA.rq_cap = ctx->rq_cap;
+            CA.feat_cap = ctx->feat_cap; CA.fref_solid = ctx->d_fref_solid; CA.fref_index = ctx->d_fref_index;
+        }
         if (learned) {
             CA.feat = ctx->d_feat; CA.feat_cap = ctx->feat_cap; CA.fref_solid = ctx->d_fref_solid;
             CA.fref_index = ctx->d_fref_index; CA.inv_h = (float)(1.0 / ctx->mdesc.h[0]);
@@ -614,9 +621,19 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             fa.n = ctx->opt.learned_fallback_n > 0 ? ctx->opt.learned_fallback_n : 16;
             fa.rq = ctx->d_rq; fa.rq_cap = ctx->rq_cap;
             fa.ovf = ctx->d_ovf; fa.ovf_cap = ctx->ovf_cap;
-            learned_fallback_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(fa);
-            mark(ctx, "learned_fallback_kernel");
+            subsample_cells_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(fa);
+            mark(ctx, "subsample_cells_kernel");
             launches += 2;
+        } else if (subsample) {
+            fa.m = ctx->mesh; fa.sk = ctx->d_sk; fa.st = ctx->d_st; fa.plan = ctx->d_plan; fa.fb_list = nullptr;
+            fa.fref_solid = ctx->d_fref_solid; fa.fref_index = ctx->d_fref_index; fa.cap = ctx->feat_cap;
+            fa.alpha = ctx->d_alpha; fa.cnt = ctx->d_cnt;
+            fa.n = ctx->opt.subsample_n;
+            fa.rq = ctx->d_rq; fa.rq_cap = ctx->rq_cap;
+            fa.ovf = ctx->d_ovf; fa.ovf_cap = ctx->ovf_cap;
+            subsample_cells_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(fa);
+            mark(ctx, "subsample_cells_kernel");
+            ++launches;
         }
         if (learned || subsample) {
             recheck_kernel<<<ctx->num_sms * 4, 256, 0, st>>>(ctx->mesh, ctx->d_sk, ctx->d_st, ctx->d_plan, ctx->d_rq,
@@ -624,7 +641,7 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             mark(ctx, "recheck_kernel");
             ++launches;
         }
-        if (learned) {
+        if (learned || subsample) {
             recount_kernel<<<ctx->num_sms * 2, 256, 0, st>>>(fa);
             mark(ctx, "recount_kernel");
             ++launches;
@@ -1104,8 +1121,8 @@ int sdfibm_cuda_set_fraction_model(sdfibm_ctx* ctx, const float* params, float t
         // one feature record per bbox cell: every cut cell of a call fits
         ctx->feat_cap = std::max<int64_t>(1, ctx->scratch_bytes);
         if (dalloc(&ctx->d_mlp, SDFIBM_MLP_NPARAM) || dalloc(&ctx->d_feat, (size_t)SDFIBM_MLP_NIN * ctx->feat_cap) ||
-            dalloc(&ctx->d_fref_solid, ctx->feat_cap) || dalloc(&ctx->d_fref_index, ctx->feat_cap) ||
-            dalloc(&ctx->d_fb, ctx->feat_cap))
+            (!ctx->d_fref_solid && dalloc(&ctx->d_fref_solid, ctx->feat_cap)) ||
+            (!ctx->d_fref_index && dalloc(&ctx->d_fref_index, ctx->feat_cap)) || dalloc(&ctx->d_fb, ctx->feat_cap))
             return fail(ctx, SDFIBM_ERR_CUDA, "allocation of the learned-fraction buffers failed");
     }
     mlp_prepare();

@@ -720,6 +720,30 @@ static __device__ __noinline__ void write_features(const ClassifyArgs& A, const 
     }
 }
 
+// SUBSAMPLE: the tile's cut cells (one warp) appended to the cell list as (solid, fraction index)
+template <int TX, int TY, int TZ>
+static __device__ __noinline__ void write_cut_list(const ClassifyArgs& A, const uint8_t* cutlist, int ncut, int s,
+                                                   int64_t tile0, int ext0, int ext1) {
+    const int lane = threadIdx.x & 31;
+    for (int u0 = 0; u0 < ncut; u0 += 32) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&A.cnt->n_feat, min(32, ncut - u0));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const int u = u0 + lane;
+        if (u < ncut) {
+            const int e = cutlist[u];
+            const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
+            const int64_t slot = (int64_t)base + lane;
+            if (slot < A.feat_cap) {
+                A.fref_solid[slot] = s;
+                A.fref_index[slot] = tile0 + a + (int64_t)ext0 * (b + (int64_t)ext1 * c);
+            } else {
+                set_error(A.cnt, DERR_CAPACITY);
+            }
+        }
+    }
+}
+
 // ---- the tile kernel: one warp per chunk of up to chunk_tiles tiles of one solid ------------------------------------------
 constexpr int CLS_WARPS = 8;
 
@@ -905,8 +929,12 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                     const float apz1 = m.twod ? (float)((mesh_coord(m, 2, K + 1) - 0.0) / m.h[2]) : 0.f;
                     alpha[local_index(a, b, c)] = refgeo32(m, ph, I0 + a, J0 + b, K, apz, apz1);
                 }
+            } else if (A.fref_index) {
+                // SUBSAMPLE: the cut cells are listed; subsample_cells_kernel samples them, a warp per cell
+                write_cut_list<TX, TY, TZ>(A, cutlist, ncut, s, k.scratch_off + local_index(0, 0, 0), k.ext[0],
+                                           k.ext[1]);
             } else {
-                // SUBSAMPLE (and the fallback of LEARNED): the warp shares the samples of one cut cell
+                // SUBSAMPLE without a cell list (allocation-free entry): the warp shares the samples of one cut cell
                 for (int u = 0; u < ncut; ++u) {
                     const int e = cutlist[u];
                     const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
@@ -966,14 +994,15 @@ __device__ __forceinline__ int count_listed_cell(const FallbackArgs& A, int s, i
                           rechecks, df);
 }
 
-// LEARNED fallback: one warp per cell outside the network's band.  Undecided points always go to the recheck list
-// (this kernel holds no FP64 path, which keeps its register count and so its occupancy); a cell some of whose points
-// found the list full is listed for recount_kernel.
-__global__ void __launch_bounds__(256, 4) learned_fallback_kernel(FallbackArgs A) {
+// SUBSAMPLE of listed cells, one warp per cell: the cut cells of the classify pass (SUBSAMPLE, fb_list == nullptr)
+// or the cells outside the network's band (LEARNED fallback).  Undecided points always go to the recheck list (this
+// kernel holds no FP64 path, which keeps its register count and so its occupancy); a cell some of whose points found
+// the list full is listed for recount_kernel.
+__global__ void __launch_bounds__(256, 4) subsample_cells_kernel(FallbackArgs A) {
     __shared__ int32_t s_overflow[8];
     const int lane = threadIdx.x & 31;
     int32_t* overflow = s_overflow + ((threadIdx.x >> 5) & 7);
-    const int64_t nfb = min((int64_t)A.cnt->n_fb, A.cap);
+    const int64_t nfb = min((int64_t)(A.fb_list ? A.cnt->n_fb : A.cnt->n_feat), A.cap);
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     unsigned long long rechecks = 0;
     if (lane == 0) *overflow = 0;
@@ -984,7 +1013,7 @@ __global__ void __launch_bounds__(256, 4) learned_fallback_kernel(FallbackArgs A
         int s_l = 0;
         int64_t idx_l = 0;
         if (base + lane < nfb) {
-            const int32_t slot = A.fb_list[base + lane];
+            const int32_t slot = A.fb_list ? A.fb_list[base + lane] : (int32_t)(base + lane);
             s_l = A.fref_solid[slot];
             idx_l = A.fref_index[slot];
         }

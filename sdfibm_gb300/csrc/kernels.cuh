@@ -195,13 +195,14 @@ struct ClassifyArgs {
     int64_t rq_cap;
 };
 
-// LEARNED: cells left to SUBSAMPLE by the network's confidence band
+// SUBSAMPLE of listed cells: every listed cut cell (fb_list == nullptr), or the LEARNED cells left to SUBSAMPLE by
+// the network's confidence band
 struct FallbackArgs {
     MeshK m;
     const SolidK* sk;
     const sdfibm_solid_state* st;
     const SolidPlan* plan;
-    const int32_t* fb_list;    // positions into the feature buffer
+    const int32_t* fb_list;    // positions into the feature buffer (nullptr: every listed cell)
     const int32_t* fref_solid;
     const int64_t* fref_index;
     int64_t cap;
