@@ -122,7 +122,7 @@ def make_workload(args):
         from sdfibm_gb300 import learned
         w.opt.learned_fallback_n = int(learned.load_model()[3].get("band", {}).get("fallback_n", 16))
     elif args.method == "subsample":
-        w.opt.subsample_n = 10
+        w.opt.subsample_n = args.subsample_n
     return w
 
 
@@ -299,6 +299,7 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--method", default="learned", choices=sorted(METHODS))
     ap.add_argument("--no-compare", action="store_true", help="skip the plain SUBSAMPLE timing and the accuracy step")
+    ap.add_argument("--subsample-n", type=int, default=10, help="samples per axis of --method subsample")
     ap.add_argument("--cpu-solids", type=int, default=2, help="solids per host thread in the CPU timing sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
