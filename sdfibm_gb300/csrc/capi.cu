@@ -40,6 +40,7 @@ __global__ void claim_kernel(const int32_t* in_cell, const int32_t* in_solid, co
                              const int32_t* cut_solid, int32_t* Ct, const Counters* cnt, int64_t N);
 __global__ void ft_kernel(const double* ftacc, double* ft, int S, const StepParams* step);
 __global__ void set_step_kernel(StepParams* p, double time, double dt, int nsub, double rho_V);
+int export_chunk_cells();
 __global__ void mark_export_kernel(const int32_t* in_cell, const int32_t* cut_cell, const int32_t* prev_in_cell,
                                    const int32_t* prev_cut_cell, const Counters* cnt, int64_t N, uint32_t* dirty);
 __global__ void export_kernel(Counters* cnt, int64_t N, uint32_t* dirty, const float* As, const float* Fs,
@@ -835,9 +836,11 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
         CK(cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming));
     }
     if (!ctx->d_As) {
+        // one bit per chunk of export_chunk_cells() cells, 32 chunks per word
+        const int64_t words = (N + 32 * (int64_t)export_chunk_cells() - 1) / (32 * (int64_t)export_chunk_cells());
         if (dalloc(&ctx->d_As, N) || dalloc(&ctx->d_Fs, 3 * N) || dalloc(&ctx->d_Ts, N) || dalloc(&ctx->d_Ct, N) ||
-            dalloc(&ctx->d_dirty, (N + 255) / 256) ||
-            cudaMemsetAsync(ctx->d_dirty, 0, sizeof(uint32_t) * ((N + 255) / 256), st) != cudaSuccess)
+            dalloc(&ctx->d_dirty, words) ||
+            cudaMemsetAsync(ctx->d_dirty, 0, sizeof(uint32_t) * words, st) != cudaSuccess)
             return fail(ctx, SDFIBM_ERR_CUDA, "staging allocation failed");
     }
     // upload U on a copy stream once the previous work on the stream (which may still read d_U) is done; the
@@ -881,7 +884,7 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
         if (rc) return rc;
         const Counters& c = *ctx->h_cnt;
         ctx->host_h2d = 12 * N;
-        ctx->host_d2h = (same ? 24 * 8 * (int64_t)c.n_export : 24 * N) + 48 * ctx->S;
+        ctx->host_d2h = (same ? 24 * (int64_t)export_chunk_cells() * c.n_export : 24 * N) + 48 * ctx->S;
         ctx->host_sparse = same;
         for (int i = 0; i < 5; ++i) ctx->host_fields[i] = f5[i];
         ctx->host_synced = true;

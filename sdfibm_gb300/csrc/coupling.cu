@@ -851,9 +851,13 @@ __global__ void reset_kernel(const int32_t* __restrict__ prev_in_cell, const int
 
 // interact_host on page-locked host fields.  The host fields held the previous call's values; the cells this call or
 // the previous one touched (the current and the previous lists) are the ones that changed.  mark_export_kernel sets
-// their 8-cell chunks in a bitmap (one bit per chunk, one word per 256 cells); export_kernel then copies every marked
-// chunk from the device fields to the host fields through the mapped host pointers, a warp per bitmap word so that
-// each store instruction covers 32 consecutive cells (whole 32-byte sectors of the host arrays), and clears the word.
+// their chunks of EXPORT_CHUNK consecutive cells in a bitmap (one bit per chunk); export_kernel then copies every
+// marked chunk from the device fields to the host fields through the mapped host pointers, a warp per bitmap word so
+// that each store instruction covers 32 consecutive cells of a host array, and clears the word.
+constexpr int EXPORT_LG = 3;  // log2 of the cells per chunk
+constexpr int EXPORT_CHUNK = 1 << EXPORT_LG;
+int export_chunk_cells() { return EXPORT_CHUNK; }
+
 __global__ void mark_export_kernel(const int32_t* __restrict__ in_cell, const int32_t* __restrict__ cut_cell,
                                    const int32_t* __restrict__ prev_in_cell, const int32_t* __restrict__ prev_cut_cell,
                                    const Counters* cnt, int64_t N, uint32_t* __restrict__ dirty) {
@@ -867,8 +871,9 @@ __global__ void mark_export_kernel(const int32_t* __restrict__ in_cell, const in
         else if (e < n0 + n1 + n2) c = prev_in_cell[e - n0 - n1];
         else c = prev_cut_cell[e - n0 - n1 - n2];
         if (c < 0 || c >= N) continue;
-        const uint32_t bit = 1u << ((c >> 3) & 31);
-        if (!(dirty[c >> 8] & bit)) atomicOr(dirty + (c >> 8), bit);
+        const uint32_t bit = 1u << ((c >> EXPORT_LG) & 31);
+        uint32_t* word = dirty + (c >> (EXPORT_LG + 5));
+        if (!(*word & bit)) atomicOr(word, bit);
     }
 }
 
@@ -876,7 +881,7 @@ __global__ void export_kernel(Counters* cnt, int64_t N, uint32_t* __restrict__ d
                               const float* __restrict__ Fs, const float* __restrict__ Ts,
                               const int32_t* __restrict__ Ct, float* hAs, float* hFs, float* hTs, int32_t* hCt) {
     const int lane = threadIdx.x & 31;
-    const int64_t words = (N + 255) >> 8;
+    const int64_t words = (N + 32 * EXPORT_CHUNK - 1) >> (EXPORT_LG + 5);
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
     int chunks = 0;
     for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += nw) {
@@ -884,9 +889,9 @@ __global__ void export_kernel(Counters* cnt, int64_t N, uint32_t* __restrict__ d
         if (!word) continue;
         chunks += __popc(word);
 #pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            const int64_t c = (w << 8) + 32 * t + lane;
-            if (((word >> ((32 * t + lane) >> 3)) & 1u) && c < N) {
+        for (int t = 0; t < EXPORT_CHUNK; ++t) {
+            const int64_t c = (w << (EXPORT_LG + 5)) + 32 * t + lane;
+            if (((word >> ((32 * t + lane) >> EXPORT_LG)) & 1u) && c < N) {
                 hAs[c] = As[c]; hTs[c] = Ts[c]; hCt[c] = Ct[c];
                 hFs[c] = Fs[c]; hFs[N + c] = Fs[N + c]; hFs[2 * N + c] = Fs[2 * N + c];
             }
