@@ -445,23 +445,25 @@ __device__ __forceinline__ int subsample_runs_body(const MeshK& m, const ShapeK&
             // clamped before the conversions (inf / NaN safe)
             const float ul = fminf(fmaxf(cl, -2.f), nf + 1.f), ur = fminf(fmaxf(cr, -2.f), nf + 1.f);
             const int c1 = max((int)ceilf(ul), 0), c2 = min((int)floorf(ur), n - 1);
+            // inside: g < -Egh, outside: g > Egh (band() of the walk, as plain comparisons)
             res = -1;
             if (cl <= cr && c1 <= c2) {
-                const int r1 = band(g_at(c1), Egh), r2 = c2 == c1 ? r1 : band(g_at(c2), Egh);
-                const int rl = c1 > 0 ? band(g_at(c1 - 1), Egh) : 0, rr = c2 < n - 1 ? band(g_at(c2 + 1), Egh) : 0;
-                if (r1 == 1 && r2 == 1 && rl == 0 && rr == 0) res = c2 - c1 + 1;
+                bool ok = g_at(c1) < -Egh && (c2 == c1 || g_at(c2) < -Egh);
+                if (ok && c1 > 0) ok = g_at(c1 - 1) > Egh;
+                if (ok && c2 < n - 1) ok = g_at(c2 + 1) > Egh;
+                if (ok) res = c2 - c1 + 1;
             } else {
                 const float um = (T == SS_QUADRIC && !(cl <= cr)) ? ul : 0.5f * (ul + ur);
                 const int cv = min(max(__float2int_rn(fminf(fmaxf(um, 0.f), nf - 1.f)), 0), n - 1);
                 const float g0 = g_at(cv);
-                bool ok = band(g0, Egh) == 0;
+                bool ok = g0 > Egh;
                 if (ok && cv + 1 < n) {
                     const float g1 = g_at(cv + 1);
-                    ok = band(g1, Egh) == 0 && (cv + 2 >= n || g1 - g0 >= rise);
+                    ok = g1 > Egh && (cv + 2 >= n || g1 - g0 >= rise);
                 }
                 if (ok && cv > 0) {
                     const float g1 = g_at(cv - 1);
-                    ok = band(g1, Egh) == 0 && (cv < 2 || g1 - g0 >= rise);
+                    ok = g1 > Egh && (cv < 2 || g1 - g0 >= rise);
                 }
                 if (ok) res = 0;
             }
