@@ -44,8 +44,9 @@ ALG_BYTES = {
 # DRAM bytes per unit measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum of one launch / its units) on the
 # 256^3 / 2048-solid learned workload; profiles/<kernel>_poly3d_256_learned.md records the captures
 NCU_BYTES_PER_UNIT = {
-    "couple_kernel": 219.2,    # 292.0 MB for 1,332,670 coupling cells: short x-runs of scattered cells in 6 field planes
-    "classify_kernel": 3.16,   # 24.7 MB for 7,825,801 bbox cells
+    "couple_kernel": 220.1,    # 293.3 MB for 1,332,670 coupling cells: short x-runs of scattered cells in 6 field planes
+    "classify_kernel": 1.40,   # 11.0 MB for 7,825,801 bbox cells (the learned features stay in L2 for the network)
+    "subsample_cells_kernel": 39.6,  # 18.2 MB for 460,073 sampled cells
 }
 # FLOPs of the two tensor-core layers per predicted cell: hi and lo BF16 halves of an 11(16)x64 and a 64x64 product
 MLP_FLOPS_PER_CELL = 2 * (2 * 16 * 64) + 2 * (2 * 64 * 64)
