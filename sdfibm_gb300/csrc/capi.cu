@@ -349,6 +349,8 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         k.tdim[1] = layer ? 8 : 4;
         k.tdim[2] = layer ? 2 : 4;
         for (int a = 0; a < 3; ++a) k.ntile[a] = (k.ext[a] + k.tdim[a] - 1) / k.tdim[a];
+        k.div_e0 = make_fastdiv((uint32_t)k.ext[0]);
+        k.div_e01 = make_fastdiv((uint32_t)((int64_t)k.ext[0] * k.ext[1]));
         k.tile_base = (int32_t)tiles;
         tiles += (int64_t)k.ntile[0] * k.ntile[1] * k.ntile[2];
         const int64_t cells = (int64_t)k.ext[0] * k.ext[1] * k.ext[2];

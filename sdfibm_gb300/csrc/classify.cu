@@ -379,14 +379,15 @@ __device__ __forceinline__ int subsample_runs_body(const MeshK& m, const ShapeK&
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     uint16_t* walk_list = s_walk[(threadIdx.x >> 5) & 7];
-    const float inv2n = 1.0f / (float)(2 * n), nf = (float)n, invn = 1.0f / nf;
+    // correctly rounded reciprocals (the same values as 1.0f / x, without the division sequence)
+    const float inv2n = __frcp_rn((float)(2 * n)), nf = (float)n, invn = __frcp_rn(nf);
     const float rise = 2.0001f * Egh;
     // per-sample step along the column and the per-cell parts of the polynomial
     const float dx = f.szx * invn, dy = f.szy * invn, dz = f.szz * invn;
     const float kdx = f.k0 * dx, kdy = f.k1 * dy, kdz = f.k2 * dz;
     const float A = __fmaf_rn(dx, kdx, __fmaf_rn(dy, kdy, dz * kdz));
-    const float invA = 1.0f / A;
-    const float idx_ = 1.0f / dx, idy = 1.0f / dy, idz = 1.0f / dz;
+    const float invA = __frcp_rn(A);
+    const float idx_ = __frcp_rn(dx), idy = __frcp_rn(dy), idz = __frcp_rn(dz);
     const float kx0 = f.k0 * idx_, ky0 = f.k1 * idy, kz0 = f.k2 * idz;
     auto column_base = [&](int col, int& ia, int& ib, float& bx, float& by, float& bz) {
         ib = __float2int_rz(((float)col + 0.5f) * invn);
@@ -971,9 +972,9 @@ __device__ __forceinline__ int count_listed_cell(const FallbackArgs& A, int s, i
                                                  const Defer* df) {
     const SolidK& k = A.sk[s];
     const SolidPlan& pl = A.plan[s];
-    const int local = (int)(idx - k.scratch_off);  // < bbox cells of one solid
-    const int row = local / k.ext[0], lc = row / k.ext[1];
-    const int la = local - row * k.ext[0], lb = row - lc * k.ext[1];
+    const uint32_t local = (uint32_t)(idx - k.scratch_off);  // < bbox cells of one solid (< 2^31)
+    const int row = (int)fdiv(local, k.div_e0), lc = (int)fdiv(local, k.div_e01);
+    const int la = (int)local - row * k.ext[0], lb = row - lc * k.ext[1];
     TileFrame tf;
     {
         const float sbx = (float)pl.base[0], sby = (float)pl.base[1], sbz = (float)pl.base[2];

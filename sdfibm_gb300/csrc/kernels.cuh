@@ -56,6 +56,7 @@ struct SolidK {
     int64_t scratch_off;     // byte offset of the bbox class array
     int64_t bitmap_off;      // word offset of the global bitmaps (bitmap_global == 1)
     int32_t motion_type, forcer_type, collision_id, pad;
+    FastDiv div_e0, div_e01;  // by ext[0] and by ext[0] * ext[1] (bbox index -> cell offsets)
     double radiusB;
     double rho, mass, mass_inv;
     double moi_inv[9];

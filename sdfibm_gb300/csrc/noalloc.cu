@@ -132,6 +132,8 @@ bool solid_record(const sdfibm_mesh_desc& mesh, const sdfibm_solid_desc& d, Soli
     k.tdim[1] = layer ? 8 : 4;
     k.tdim[2] = layer ? 2 : 4;
     for (int a = 0; a < 3; ++a) k.ntile[a] = (k.ext[a] + k.tdim[a] - 1) / k.tdim[a];
+    k.div_e0 = make_fastdiv((uint32_t)k.ext[0]);
+    k.div_e01 = make_fastdiv((uint32_t)((int64_t)k.ext[0] * k.ext[1]));
     k.tile_base = 0;
     k.scratch_off = 0;
     k.bitmap_global = 1;
