@@ -22,6 +22,9 @@ void launch_classify(const ClassifyArgs& A, bool flat, int grid, cudaStream_t st
 int classify_occupancy(int method, bool flat);
 __global__ void subsample_cells_kernel(FallbackArgs A);
 __global__ void recount_kernel(FallbackArgs A);
+__global__ void refgeo_cells_kernel(MeshK m, const SolidK* sk, const SolidPlan* plan, const int32_t* fref_solid,
+                                    const int64_t* fref_index, const float* rg_phi, int64_t cap, const Counters* cnt,
+                                    float* alpha);
 __global__ void recheck_kernel(MeshK m, const SolidK* sk, const sdfibm_solid_state* st, const SolidPlan* plan,
                                const Recheck* rq, int64_t cap, Counters* cnt, float* alpha);
 __global__ void connect_kernel(MeshK m, const SolidK* sk, SolidPlan* plan, const uint8_t* scratch, uint32_t* gbitmaps,
@@ -173,6 +176,7 @@ struct sdfibm_ctx {
     float tau_twist = 0.f, tau_grad = 0.f;
     bool model_set = false;
     float* d_feat = nullptr;  // [11][feat_cap]
+    float* d_rg_phi = nullptr;  // REF-GEO: [8][feat_cap] vertex distances of the listed cut cells
     int64_t feat_cap = 0;
     int32_t* d_fref_solid = nullptr;
     int64_t* d_fref_index = nullptr;
@@ -489,9 +493,10 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         dalloc(&ctx->d_sh_used, (size_t)ctx->sh_mask + 1) || dalloc(&ctx->d_step, 2) ||
         dalloc(&ctx->d_small, small_solids.size()) || dalloc(&ctx->d_big, big_solids.size()) ||
         dalloc(&ctx->d_rq, (size_t)ctx->rq_cap) || dalloc(&ctx->d_ovf, (size_t)ctx->ovf_cap) ||
-        (ctx->opt.fraction_method == SDFIBM_FRACTION_SUBSAMPLE &&
+        ((ctx->opt.fraction_method == SDFIBM_FRACTION_SUBSAMPLE || ctx->opt.fraction_method == SDFIBM_FRACTION_REFGEO) &&
          (dalloc(&ctx->d_fref_solid, (size_t)(ctx->feat_cap = std::max<int64_t>(1, scratch))) ||
           dalloc(&ctx->d_fref_index, (size_t)ctx->feat_cap))) ||
+        (ctx->opt.fraction_method == SDFIBM_FRACTION_REFGEO && dalloc(&ctx->d_rg_phi, 8 * (size_t)ctx->feat_cap)) ||
         cudaMallocHost((void**)&ctx->h_cnt, sizeof(Counters)) != cudaSuccess ||
         cudaMallocHost((void**)&ctx->h_ft, std::max<size_t>(1, 6 * (size_t)nsolids) * sizeof(double)) != cudaSuccess) {
         ctx->err = "device allocation failed";
@@ -597,6 +602,12 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
         CA.method = ctx->opt.fraction_method; CA.subsample_n = ctx->opt.subsample_n;
         const bool learned = ctx->opt.fraction_method == SDFIBM_FRACTION_LEARNED;
         const bool subsample = ctx->opt.fraction_method == SDFIBM_FRACTION_SUBSAMPLE;
+        const bool refgeo = ctx->opt.fraction_method == SDFIBM_FRACTION_REFGEO;
+        if (refgeo) {
+            // cut cells and their vertex distances listed by the classify pass, fractions by refgeo_cells_kernel
+            CA.feat_cap = ctx->feat_cap; CA.fref_solid = ctx->d_fref_solid; CA.fref_index = ctx->d_fref_index;
+            CA.rg_phi = ctx->d_rg_phi;
+        }
         if (subsample) {
             // cut cells listed by the classify pass, sampled by subsample_cells_kernel
             CA.rq = ctx->d_rq; CA.rq_cap = ctx->rq_cap;
@@ -608,6 +619,14 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
         }
         launch_classify(CA, ctx->mesh.nz <= 2, ctx->classify_grid, st);
         mark(ctx, "classify_kernel");
+        if (refgeo) {
+            refgeo_cells_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(ctx->mesh, ctx->d_sk, ctx->d_plan,
+                                                                   ctx->d_fref_solid, ctx->d_fref_index,
+                                                                   ctx->d_rg_phi, ctx->feat_cap, ctx->d_cnt,
+                                                                   ctx->d_alpha);
+            mark(ctx, "refgeo_cells_kernel");
+            ++launches;
+        }
         FallbackArgs fa{};
         if (learned) {
             // network on every cut cell, SUBSAMPLE on the cells outside its band
@@ -1160,8 +1179,8 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
                    ctx->d_lists[1][0], ctx->d_lists[1][1], ctx->d_lists[1][2], ctx->d_lists[1][3], ctx->d_cnt, ctx->d_ftacc,
                    ctx->d_ft, ctx->d_hash, ctx->d_gcount, ctx->d_gstart, ctx->d_gcursor, ctx->d_glist, ctx->d_U,
                    ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, ctx->d_alpha, ctx->d_sh_keys, ctx->d_sh_vals, ctx->d_sh_used,
-                   ctx->d_mlp, ctx->d_feat, ctx->d_fref_solid, ctx->d_fref_index, ctx->d_fb, ctx->d_fcount,
-                   ctx->d_fstart, ctx->d_fcursor, ctx->d_flist, ctx->d_planes};
+                   ctx->d_mlp, ctx->d_feat, ctx->d_rg_phi, ctx->d_fref_solid, ctx->d_fref_index, ctx->d_fb,
+                   ctx->d_fcount, ctx->d_fstart, ctx->d_fcursor, ctx->d_flist, ctx->d_planes};
     for (void* p : dev)
         if (p) cudaFree(p);
     if (ctx->d_step) cudaFree(ctx->d_step);

@@ -723,6 +723,35 @@ static __device__ __noinline__ void write_features(const ClassifyArgs& A, const 
     }
 }
 
+// REF-GEO: the tile's cut cells (one warp) appended to the cell list with the distances of their 8 vertices
+template <int TX, int TY, int TZ>
+static __device__ __noinline__ void write_refgeo_list(const ClassifyArgs& A, const uint8_t* cutlist, int ncut,
+                                                      const float* vphi, int s, int64_t tile0, int ext0, int ext1) {
+    constexpr int VX = TX + 1, VY = TY + 1;
+    const int lane = threadIdx.x & 31;
+    for (int u0 = 0; u0 < ncut; u0 += 32) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&A.cnt->n_feat, min(32, ncut - u0));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const int u = u0 + lane;
+        if (u < ncut) {
+            const int e = cutlist[u];
+            const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
+            const int v0 = a + VX * (b + VY * c);
+            const int64_t slot = (int64_t)base + lane;
+            if (slot < A.feat_cap) {
+                const int vo[8] = {0, 1, VX, VX + 1, VX * VY, VX * VY + 1, VX * VY + VX, VX * VY + VX + 1};
+#pragma unroll
+                for (int q = 0; q < 8; ++q) A.rg_phi[q * A.feat_cap + slot] = vphi[v0 + vo[q]];
+                A.fref_solid[slot] = s;
+                A.fref_index[slot] = tile0 + a + (int64_t)ext0 * (b + (int64_t)ext1 * c);
+            } else {
+                set_error(A.cnt, DERR_CAPACITY);
+            }
+        }
+    }
+}
+
 // SUBSAMPLE: the tile's cut cells (one warp) appended to the cell list as (solid, fraction index)
 template <int TX, int TY, int TZ>
 static __device__ __noinline__ void write_cut_list(const ClassifyArgs& A, const uint8_t* cutlist, int ncut, int s,
@@ -920,6 +949,13 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                     __syncwarp();
                     continue;
                 }
+                if (METHOD == SDFIBM_FRACTION_REFGEO && A.rg_phi) {
+                    // the cut cells and their vertex distances are listed; refgeo_cells_kernel computes the fractions
+                    write_refgeo_list<TX, TY, TZ>(A, cutlist, ncut, vphi, s, k.scratch_off + local_index(0, 0, 0),
+                                                  k.ext[0], k.ext[1]);
+                    __syncwarp();
+                    continue;
+                }
                 for (int u = lane; u < ncut; u += 32) {
                     const int e = cutlist[u];
                     const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
@@ -1059,6 +1095,33 @@ __global__ void __launch_bounds__(256) recount_kernel(FallbackArgs A) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);
     if (lane == 0 && rechecks) atomicAdd(&A.cnt->exact_rechecks, rechecks);
+}
+
+// REF-GEO fraction of the listed cut cells, one thread per cell (GeometricTools::calcCellVolume on the cell's vertex
+// distances, see refgeo32): the tile pass lists the cells, so every lane here has a cell.
+__global__ void __launch_bounds__(256) refgeo_cells_kernel(MeshK m, const SolidK* __restrict__ sk,
+                                                           const SolidPlan* __restrict__ plan,
+                                                           const int32_t* __restrict__ fref_solid,
+                                                           const int64_t* __restrict__ fref_index,
+                                                           const float* __restrict__ rg_phi, int64_t cap,
+                                                           const Counters* cnt, float* __restrict__ alpha) {
+    const int64_t n = min((int64_t)cnt->n_feat, cap);
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const int s = fref_solid[e];
+        const int64_t idx = fref_index[e];
+        const SolidK& k = sk[s];
+        const SolidPlan& pl = plan[s];
+        const uint32_t local = (uint32_t)(idx - k.scratch_off);
+        const int row = (int)fdiv(local, k.div_e0), lc = (int)fdiv(local, k.div_e01);
+        const int la = (int)local - row * k.ext[0], lb = row - lc * k.ext[1];
+        float ph[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) ph[q] = rg_phi[q * cap + e];
+        const int64_t K = pl.lo[2] + lc;
+        const float apz = m.twod ? (float)((0.0 - mesh_coord(m, 2, K)) / m.h[2]) : 0.f;
+        const float apz1 = m.twod ? (float)((mesh_coord(m, 2, K + 1) - 0.0) / m.h[2]) : 0.f;
+        alpha[idx] = refgeo32(m, ph, pl.lo[0] + la, pl.lo[1] + lb, K, apz, apz1);
+    }
 }
 
 // The deferred SUBSAMPLE points: one per thread, the reference's FP64 point and inside test, an inside point lowers the

@@ -194,6 +194,7 @@ struct ClassifyArgs {
     float inv_h;          // 1 / h (x spacing) of the feature scaling
     Recheck* rq;          // deferred SUBSAMPLE rechecks (nullptr: re-evaluate in place)
     int64_t rq_cap;
+    float* rg_phi;        // REF-GEO: [8][feat_cap] vertex distances of the listed cut cells (nullptr: fraction in place)
 };
 
 // SUBSAMPLE of listed cells: every listed cut cell (fb_list == nullptr), or the LEARNED cells left to SUBSAMPLE by
