@@ -361,9 +361,9 @@ __device__ inline int block_log2(int n, bool flat) {
 //   run [c1, c2] found: c1 and c2 inside, c1 - 1 and c2 + 1 outside (or off the column).  Every sample between the
 //     ends is inside (q there is at most its value at the ends) and every sample past c2 + 1 outside (q grows past a
 //     rise from an inside to an outside sample), and likewise before c1 - 1;
-//   no sample in the interval: the sample cv nearest the closest approach and its neighbours outside, with q
-//     certified to rise from cv to each neighbour (computed rise of at least 2 Egh); every sample past a neighbour
-//     is then outside.
+//   no sample in the interval: the samples cv and cv + 1 around the closest approach outside, with q certified to
+//     rise from cv to cv - 1 and from cv + 1 to cv + 2 (computed rise of at least 2 Egh); every sample past them is
+//     then outside.  For the box, a slab that holds neither end of the column (on the same side) settles it first.
 // A column that does not verify (a value within Egh of zero, a run end off by one, a flat approach) is walked sample
 // by sample with the coordinates, bound and deferral of subsample_count.  The count is therefore the exhaustive
 // lattice count.
@@ -454,19 +454,31 @@ __device__ __forceinline__ int subsample_runs_body(const MeshK& m, const ShapeK&
                 if (ok && c2 < n - 1) ok = g_at(c2 + 1) > Egh;
                 if (ok) res = c2 - c1 + 1;
             } else {
-                const float um = (T == SS_QUADRIC && !(cl <= cr)) ? ul : 0.5f * (ul + ur);
-                const int cv = min(max(__float2int_rn(fminf(fmaxf(um, 0.f), nf - 1.f)), 0), n - 1);
-                const float g0 = g_at(cv);
-                bool ok = g0 > Egh;
-                if (ok && cv + 1 < n) {
-                    const float g1 = g_at(cv + 1);
-                    ok = g1 > Egh && (cv + 2 >= n || g1 - g0 >= rise);
+                // the pair cv, cv + 1 around the closest approach: both outside, q rising from cv to cv - 1 and
+                // from cv + 1 to cv + 2 (a pair rather than one sample: with the approach halfway between two
+                // samples, the rise from the nearer one to the other would be about zero)
+                float um = (T == SS_QUADRIC && !(cl <= cr)) ? ul : 0.5f * (ul + ur);
+                bool separated = false;
+                if (T == SS_BOX) {
+                    // a slab whose coordinate is beyond it at both ends of the column, on the same side, holds no
+                    // sample (the coordinate is linear along the column; computed within Egh of q at the ends)
+                    const float last = nf - 1.f;
+                    auto beyond = [&](float w0, float d0, float k0) {
+                        const float x1 = __fmaf_rn(last, d0, w0);
+                        return (w0 > 0.f) == (x1 > 0.f) && fabsf(w0) - k0 > Egh && fabsf(x1) - k0 > Egh;
+                    };
+                    separated = beyond(wx, dx, f.k0) || beyond(wy, dy, f.k1) || beyond(wz, dz, f.k2);
                 }
-                if (ok && cv > 0) {
-                    const float g1 = g_at(cv - 1);
-                    ok = g1 > Egh && (cv < 2 || g1 - g0 >= rise);
+                if (separated) {
+                    res = 0;
+                } else {
+                    const int cv = min(max(__float2int_rd(fminf(fmaxf(um, 0.f), nf - 2.f)), 0), n - 2);
+                    const float g0 = g_at(cv), g1 = g_at(cv + 1);
+                    bool ok = g0 > Egh && g1 > Egh;
+                    if (ok && cv >= 1) ok = g_at(cv - 1) - g0 >= rise;
+                    if (ok && cv + 2 <= n - 1) ok = g_at(cv + 2) - g1 >= rise;
+                    if (ok) res = 0;
                 }
-                if (ok) res = 0;
             }
         }
         const bool walk = res < 0;
