@@ -158,6 +158,9 @@ struct sdfibm_ctx {
     int32_t* d_Ct = nullptr;
     cudaStream_t copy_st[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t ev_entry = nullptr, ev_u = nullptr, ev_done = nullptr;
+    // side stream of interact: the component pass (connect, claim, reset) runs there beside the fraction kernels
+    cudaStream_t side_st = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t u_wait = nullptr;  // set while interact_host runs: couple waits for the upload
     // interact_host on page-locked host fields: the host buffers of the last such call (their cells equal the device
     // fields after it) and the bytes the last interact_host moved each way
@@ -307,6 +310,12 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
     };
     if (cudaGetDevice(&ctx->device) != cudaSuccess) { delete ctx; return SDFIBM_ERR_CUDA; }
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (cudaStreamCreateWithFlags(&ctx->side_st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        ctx->err = "stream creation failed";
+        return bail(SDFIBM_ERR_CUDA);
+    }
     MeshK& m = ctx->mesh;
     m.nx = mesh->nx; m.ny = mesh->ny; m.nz = mesh->nz; m.twod = mesh->twod;
     for (int a = 0; a < 3; ++a) { m.o[a] = mesh->origin[a]; m.h[a] = mesh->h[a]; m.h32[a] = (float)mesh->h[a]; }
@@ -619,6 +628,35 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
         }
         launch_classify(CA, ctx->mesh.nz <= 2, ctx->classify_grid, st);
         mark(ctx, "classify_kernel");
+        // the component pass needs only the class bytes and the seeds: on the side stream, beside the fraction
+        // kernels below (one stream while timing, so that every kernel has its own events)
+        const bool fork = ctx->side_st != nullptr && !ctx->opt.timing;
+        cudaStream_t sb = fork ? ctx->side_st : st;
+        if (fork) {
+            CK(cudaEventRecord(ctx->ev_fork, st));
+            CK(cudaStreamWaitEvent(sb, ctx->ev_fork, 0));
+        }
+        if (ctx->n_small > 0)
+            connect_small_kernel<<<(ctx->n_small + 7) / 8, 256, 0, sb>>>(
+                ctx->mesh, ctx->d_sk, ctx->d_plan, ctx->d_scratch, ctx->in_cell(), ctx->in_solid(), ctx->cut_cell(),
+                ctx->cut_solid(), ctx->cap, ctx->cap, ctx->d_cnt, ctx->d_small, ctx->n_small);
+        if (ctx->n_big > 0)
+            connect_kernel<<<ctx->n_big, 512, ctx->connect_smem_bytes, sb>>>(
+                ctx->mesh, ctx->d_sk, ctx->d_plan, ctx->d_scratch, ctx->d_gbitmaps, ctx->in_cell(), ctx->in_solid(),
+                ctx->cut_cell(), ctx->cut_solid(), ctx->cap, ctx->cap, ctx->d_cnt, ctx->connect_smem_bytes / 4,
+                ctx->d_big);
+        mark(ctx, "connect_kernel");
+        claim_kernel<<<ctx->num_sms * 8, 256, 0, sb>>>(ctx->in_cell(), ctx->in_solid(), ctx->cut_cell(),
+                                                        ctx->cut_solid(), Ct, ctx->d_cnt, N);
+        mark(ctx, "claim_kernel");
+        launches += 4;
+        if (!dense) {
+            const int p = ctx->cur ^ 1;
+            reset_kernel<<<ctx->num_sms * 4, 256, 0, sb>>>(ctx->d_lists[p][0], ctx->d_lists[p][2], ctx->d_cnt, N, As,
+                                                            Fs, Ts, Ct);
+            mark(ctx, "reset_kernel");
+            ++launches;
+        }
         if (refgeo) {
             refgeo_cells_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(ctx->mesh, ctx->d_sk, ctx->d_plan,
                                                                    ctx->d_fref_solid, ctx->d_fref_index,
@@ -668,26 +706,14 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             mark(ctx, "recount_kernel");
             ++launches;
         }
-        if (ctx->n_small > 0)
-            connect_small_kernel<<<(ctx->n_small + 7) / 8, 256, 0, st>>>(
-                ctx->mesh, ctx->d_sk, ctx->d_plan, ctx->d_scratch, ctx->in_cell(), ctx->in_solid(), ctx->cut_cell(),
-                ctx->cut_solid(), ctx->cap, ctx->cap, ctx->d_cnt, ctx->d_small, ctx->n_small);
-        if (ctx->n_big > 0)
-            connect_kernel<<<ctx->n_big, 512, ctx->connect_smem_bytes, st>>>(
-                ctx->mesh, ctx->d_sk, ctx->d_plan, ctx->d_scratch, ctx->d_gbitmaps, ctx->in_cell(), ctx->in_solid(),
-                ctx->cut_cell(), ctx->cut_solid(), ctx->cap, ctx->cap, ctx->d_cnt, ctx->connect_smem_bytes / 4,
-                ctx->d_big);
-        mark(ctx, "connect_kernel");
-        claim_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(ctx->in_cell(), ctx->in_solid(), ctx->cut_cell(),
-                                                        ctx->cut_solid(), Ct, ctx->d_cnt, N);
-        mark(ctx, "claim_kernel");
-        launches += 4;
-    }
-    if (!dense) {
+        if (fork) {
+            CK(cudaEventRecord(ctx->ev_join, sb));
+            CK(cudaStreamWaitEvent(st, ctx->ev_join, 0));
+        }
+    } else if (!dense) {
         const int p = ctx->cur ^ 1;
         reset_kernel<<<ctx->num_sms * 4, 256, 0, st>>>(ctx->d_lists[p][0], ctx->d_lists[p][2], ctx->d_cnt, N, As, Fs,
                                                         Ts, Ct);
-        mark(ctx, "reset_kernel");
         ++launches;
     }
     if (ctx->u_wait) CK(cudaStreamWaitEvent(st, ctx->u_wait, 0));  // U staged on a copy stream (interact_host)
@@ -1196,6 +1222,9 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
     if (ctx->ev_entry) cudaEventDestroy(ctx->ev_entry);
     if (ctx->ev_u) cudaEventDestroy(ctx->ev_u);
     if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->side_st) cudaStreamDestroy(ctx->side_st);
     if (ctx->d_big) cudaFree(ctx->d_big);
     for (auto& g : ctx->igraph)
         if (g.valid) cudaGraphExecDestroy(g.exec);
