@@ -336,8 +336,16 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         SolidK& k = ctx->hk[s];
         std::memset(&k, 0, sizeof(k));
         k.shape.type = d.shape.type;
-        for (int i = 0; i < 8; ++i) { k.shape.p[i] = d.shape.p[i]; k.shape.p32[i] = (float)d.shape.p[i]; }
-        for (int i = 0; i < 3; ++i) { k.shape.com[i] = d.shape.com[i]; k.shape.com32[i] = (float)d.shape.com[i]; }
+        for (int i = 0; i < 8; ++i) {
+            k.shape.p[i] = d.shape.p[i];
+            k.shape.p32[i] = (float)d.shape.p[i];
+            k.shape.p_lo[i] = (float)(d.shape.p[i] - (double)k.shape.p32[i]);
+        }
+        for (int i = 0; i < 3; ++i) {
+            k.shape.com[i] = d.shape.com[i];
+            k.shape.com32[i] = (float)d.shape.com[i];
+            k.shape.com_lo[i] = (float)(d.shape.com[i] - (double)k.shape.com32[i]);
+        }
         double r;
         int prism;
         if (!bound_radius(d.shape, r, prism)) { ctx->err = "unknown shape type"; return bail(SDFIBM_ERR_ARG); }

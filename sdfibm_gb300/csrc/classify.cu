@@ -695,6 +695,95 @@ static __device__ __noinline__ float sdf_mixed(const ShapeK& s, const D3& p) {
 }
 
 // filter of sdf.h:147-150 applied to the mixed value; *exact_needed set when the value sits on the threshold
+// ---- two-float vertex distances (REF-GEO, 3-D spheres, ellipsoids and boxes) ---------------------------------------
+// Pairs hi + lo with error-free sums and products (Dekker, Knuth), explicit rounding intrinsics so that nothing is
+// contracted or reassociated; each operation errs by a few 2^-48 of its operands' magnitudes.  GB300 issues FP32 at 64
+// times the FP64 rate, so the pairs replace the FP64 local point and the cancelling differences of sdf_mixed.
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF ff_fast(float a, float b) {  // |a| >= |b|, or the pair carries the rounding of b
+    const float s = __fadd_rn(a, b);
+    return FF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_sum(float a, float b) {
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return FF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ FF ff_add(FF x, FF y) {
+    const FF t = ff_sum(x.hi, y.hi);
+    return ff_fast(t.hi, __fadd_rn(t.lo, __fadd_rn(x.lo, y.lo)));
+}
+__device__ __forceinline__ FF ff_mul(FF x, FF y) {
+    const float p = __fmul_rn(x.hi, y.hi);
+    return ff_fast(p, __fmaf_rn(x.hi, y.lo, __fmaf_rn(x.lo, y.hi, __fmaf_rn(x.hi, y.hi, -p))));
+}
+__device__ __forceinline__ FF ff_scale(FF x, float n) {  // n: a small integer, exact in FP32
+    const float p = __fmul_rn(x.hi, n);
+    return ff_fast(p, __fmaf_rn(x.lo, n, __fmaf_rn(x.hi, n, -p)));
+}
+__device__ __forceinline__ FF ff_abs(FF x) { return x.hi < 0.f ? FF{-x.hi, -x.lo} : x; }
+
+// Solid::phi of bbox vertex (da, db, dc) as sdf_mixed computes it (the same FP32 formula after the cancelling
+// differences), the local point from the plan's two-float map; err bounds the difference to the exact value with a
+// factor of 4 to spare over the operations' roundoff (2^-44 of the magnitudes).
+__device__ inline float sdf_ff(const ShapeK& s, const SolidPlan& pl, float da, float db, float dc, float& err) {
+    FF P[3];
+    float ml = 0.f;
+    const float f3[3] = {da, db, dc};
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        FF v{pl.lmap_hi[r], pl.lmap_lo[r]};
+        float mag = fabsf(pl.lmap_hi[r]);
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            const int i = 3 + 3 * t + r;
+            v = ff_add(v, ff_scale(FF{pl.lmap_hi[i], pl.lmap_lo[i]}, f3[t]));
+            mag += fabsf(f3[t] * pl.lmap_hi[i]);
+        }
+        P[r] = v;
+        ml = fmaxf(ml, mag);
+    }
+    const float U44 = 5.6843418860808015e-14f;  // 2^-44
+    const float* a = s.p32;
+    if (s.type == SDFIBM_SHAPE_ELLIPSOID) {  // the reference's ellipsoid ignores com
+        const FF xa = ff_mul(ff_mul(P[0], P[0]), FF{a[3], s.p_lo[3]});
+        const FF yb = ff_mul(ff_mul(P[1], P[1]), FF{a[4], s.p_lo[4]});
+        const FF zc = ff_mul(ff_mul(P[2], P[2]), FF{a[5], s.p_lo[5]});
+        const FF sum = ff_add(ff_add(ff_add(xa, yb), zc), FF{-1.f, 0.f});
+        const float den = sqrtf(xa.hi * a[3] + yb.hi * a[4] + zc.hi * a[5]);
+        const float am = fmaxf(a[3], fmaxf(a[4], a[5]));
+        const float pm = fmaxf(fabsf(P[0].hi), fmaxf(fabsf(P[1].hi), fabsf(P[2].hi)));
+        err = 4.f * U44 * (xa.hi + yb.hi + zc.hi + 1.f + 6.f * am * pm * (ml + pm)) / den;
+        return (0.5f * __fadd_rn(sum.hi, sum.lo)) / den;
+    }
+    FF q[3];
+    float qm = 0.f;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        q[r] = ff_add(P[r], FF{s.com32[r], s.com_lo[r]});
+        qm = fmaxf(qm, fabsf(q[r].hi));
+    }
+    const float mag = ml + fabsf(s.com32[0]) + fabsf(s.com32[1]) + fabsf(s.com32[2]) + qm;
+    if (s.type == SDFIBM_SHAPE_SPHERE) {
+        const FF qq = ff_add(ff_add(ff_mul(q[0], q[0]), ff_mul(q[1], q[1])), ff_mul(q[2], q[2]));
+        const FF num = ff_add(qq, FF{-a[1], -s.p_lo[1]});
+        const float den = sqrtf(qq.hi) + a[0];
+        err = 4.f * U44 * (qq.hi + a[1] + 6.f * qm * mag) / den;
+        return __fadd_rn(num.hi, num.lo) / den;
+    }
+    // box
+    float d[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const FF t = ff_add(ff_abs(q[r]), FF{-a[r], -s.p_lo[r]});
+        d[r] = __fadd_rn(t.hi, t.lo);
+    }
+    err = 4.f * U44 * (mag + a[0] + a[1] + a[2]);
+    const float dxp = fmaxf(0.f, d[0]), dyp = fmaxf(0.f, d[1]), dzp = fmaxf(0.f, d[2]);
+    return sqrtf(dxp * dxp + dyp * dyp + dzp * dzp) + fminf(0.f, fmaxf(d[2], fmaxf(d[0], d[1])));
+}
+
 __device__ inline float filter_mixed(const ShapeK& s, float phi, bool* exact_needed) {
     if (s.type == SDFIBM_SHAPE_PLANE) return phi;  // the plane's distance is unfiltered and exact
     const float a = fabsf(phi);
@@ -932,6 +1021,9 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                 }
                 __syncwarp();
                 const double* L = pl.lmap;
+                // 3-D spheres, ellipsoids and boxes: two-float distances (FP32 pipe); others: sdf_mixed (FP64)
+                const bool ff_shape = !sh.prism && (sh.type == SDFIBM_SHAPE_SPHERE ||
+                                                    sh.type == SDFIBM_SHAPE_ELLIPSOID || sh.type == SDFIBM_SHAPE_BOX);
                 for (int u = lane; u < nneed; u += 32) {
                     const int v = vlist[u];
                     const int a = v % VX, b = (v / VX) % VY, c = v / (VX * VY);
@@ -945,11 +1037,22 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                         vphi[v] = sdf32(sh, lx, ly, lz);
                         continue;
                     }
-                    const double da = (double)(tx * TX + a), db = (double)(ty * TY + b), dc = (double)(tz * TZ + c);
-                    const D3 plc{L[0] + da * L[3] + db * L[6] + dc * L[9], L[1] + da * L[4] + db * L[7] + dc * L[10],
-                                 L[2] + da * L[5] + db * L[8] + dc * L[11]};
                     bool exact = false;
-                    float ph = filter_mixed(sh, sdf_mixed(sh, plc), &exact);
+                    float ph;
+                    if (ff_shape) {
+                        float err;
+                        ph = sdf_ff(sh, pl, (float)(tx * TX + a), (float)(ty * TY + b), (float)(tz * TZ + c), err);
+                        const float aph = fabsf(ph);
+                        exact = fabsf(aph - 1e-8f) <= 1e-14f + err;  // the filter's decision is not certain
+                        if (aph < 1e-8f) ph = -1e-8f;
+                    } else {
+                        const double da = (double)(tx * TX + a), db = (double)(ty * TY + b),
+                                     dc = (double)(tz * TZ + c);
+                        const D3 plc{L[0] + da * L[3] + db * L[6] + dc * L[9],
+                                     L[1] + da * L[4] + db * L[7] + dc * L[10],
+                                     L[2] + da * L[5] + db * L[8] + dc * L[11]};
+                        ph = filter_mixed(sh, sdf_mixed(sh, plc), &exact);
+                    }
                     if (exact || sh.type == SDFIBM_SHAPE_PLANE) ph = exact_phi_point(sh, m, I0 + a, J0 + b, K0 + c, x, q);
                     vphi[v] = ph;
                 }

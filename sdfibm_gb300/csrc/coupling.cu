@@ -162,7 +162,11 @@ __global__ void plan_kernel(MeshK m, const SolidK* __restrict__ sk, const sdfibm
         const D3 lx = qtransform(qc, D3{m.h[0], 0, 0}), ly = qtransform(qc, D3{0, m.h[1], 0}),
                  lz = qtransform(qc, D3{0, 0, m.h[2]});
         const double l12[12] = {cl.x, cl.y, cl.z, lx.x, lx.y, lx.z, ly.x, ly.y, ly.z, lz.x, lz.y, lz.z};
-        for (int r = 0; r < 12; ++r) p.lmap[r] = l12[r];
+        for (int r = 0; r < 12; ++r) {
+            p.lmap[r] = l12[r];
+            p.lmap_hi[r] = (float)l12[r];
+            p.lmap_lo[r] = (float)(l12[r] - (double)p.lmap_hi[r]);
+        }
         const D3 pf = mesh_point(m, (int64_t)p.lo[0] + k.ext[0], (int64_t)p.lo[1] + k.ext[1], (int64_t)p.lo[2] + k.ext[2]);
         p.e64 = (float)(2e-15 * (fabs(p0.x) + fabs(p0.y) + fabs(p0.z) + fabs(pf.x) + fabs(pf.y) + fabs(pf.z) + fabs(x.x) +
                                  fabs(x.y) + fabs(x.z)));

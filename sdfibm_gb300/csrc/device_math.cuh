@@ -60,6 +60,8 @@ struct ShapeK {
     double bound_r;     // radius of a sphere (or disc for prisms) around -com holding the inside region
     float p32[8];
     float com32[3];
+    float p_lo[8];      // p - p32 and com - com32 rounded to FP32: the two-float form of the parameters
+    float com_lo[3];
 };
 
 constexpr double SDF_TOL = 1e-8;  // sdf::TOL

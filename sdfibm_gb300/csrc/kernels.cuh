@@ -77,6 +77,7 @@ struct SolidPlan {
     double cbase[3];          // centre of the seed cell minus the solid centre (FP64), origin of FP32 cell offsets
     double base[3];           // mesh point (lo) minus the solid centre: FP64 origin of the FP32 tile frames
     double lmap[12];          // world2local of mesh point (lo), then the local images of h_x e_x, h_y e_y, h_z e_z
+    float lmap_hi[12], lmap_lo[12];  // the same as FP32 pairs hi + lo (two-float vertex distances)
     float e64;                // bound of the FP64 rounding of point coordinates (see TileFrame)
     float pad2;
     double cw[3];             // centre of the bounding sphere (2-D shapes: of the bounding disc)

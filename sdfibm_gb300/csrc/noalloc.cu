@@ -109,8 +109,16 @@ bool solid_record(const sdfibm_mesh_desc& mesh, const sdfibm_solid_desc& d, Soli
     const int32_t n3[3] = {mesh.nx, mesh.ny, mesh.nz};
     std::memset(&k, 0, sizeof(k));
     k.shape.type = d.shape.type;
-    for (int i = 0; i < 8; ++i) { k.shape.p[i] = d.shape.p[i]; k.shape.p32[i] = (float)d.shape.p[i]; }
-    for (int i = 0; i < 3; ++i) { k.shape.com[i] = d.shape.com[i]; k.shape.com32[i] = (float)d.shape.com[i]; }
+    for (int i = 0; i < 8; ++i) {
+        k.shape.p[i] = d.shape.p[i];
+        k.shape.p32[i] = (float)d.shape.p[i];
+        k.shape.p_lo[i] = (float)(d.shape.p[i] - (double)k.shape.p32[i]);
+    }
+    for (int i = 0; i < 3; ++i) {
+        k.shape.com[i] = d.shape.com[i];
+        k.shape.com32[i] = (float)d.shape.com[i];
+        k.shape.com_lo[i] = (float)(d.shape.com[i] - (double)k.shape.com32[i]);
+    }
     double r;
     int prism;
     if (!shape_bound(d.shape, r, prism)) return false;
