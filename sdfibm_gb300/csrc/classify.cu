@@ -918,7 +918,7 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
         uint8_t* out = A.cls + k.scratch_off;
         float* alpha = A.alpha + k.scratch_off;
         unsigned long long wmin = ~0ull;
-        const float sb[3] = {(float)pl.base[0], (float)pl.base[1], (float)pl.base[2]};
+        const float sb[3] = {pl.base32[0], pl.base32[1], pl.base32[2]};
         for (int t = ch.y; t < t_end; ++t) {
             const int tx = t % k.ntile[0], ty = (t / k.ntile[0]) % k.ntile[1], tz = t / (k.ntile[0] * k.ntile[1]);
             const int cx = min(TX, k.ext[0] - tx * TX);
@@ -1128,7 +1128,7 @@ __device__ __forceinline__ int count_listed_cell(const FallbackArgs& A, int s, i
     const int la = (int)local - row * k.ext[0], lb = row - lc * k.ext[1];
     TileFrame tf;
     {
-        const float sbx = (float)pl.base[0], sby = (float)pl.base[1], sbz = (float)pl.base[2];
+        const float sbx = pl.base32[0], sby = pl.base32[1], sbz = pl.base32[2];
         const float ofx = (float)la * A.m.h32[0], ofy = (float)lb * A.m.h32[1], ofz = (float)lc * A.m.h32[2];
         tf.bx = sbx + ofx; tf.by = sby + ofy; tf.bz = sbz + ofz;
         tf.babs = fabsf(sbx) + fabsf(sby) + fabsf(sbz) + 2.f * (fabsf(ofx) + fabsf(ofy) + fabsf(ofz)) +

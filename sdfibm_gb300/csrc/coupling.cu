@@ -157,6 +157,8 @@ __global__ void plan_kernel(MeshK m, const SolidK* __restrict__ sk, const sdfibm
         const D3 p0 = mesh_point(m, p.lo[0], p.lo[1], p.lo[2]);
         const D3 b = p0 - x;
         p.base[0] = b.x; p.base[1] = b.y; p.base[2] = b.z;
+        p.base32[0] = (float)b.x; p.base32[1] = (float)b.y; p.base32[2] = (float)b.z;
+        p.pad4 = 0.f;
         const D3 cl = world2local(p0, x, q);
         const Q4 qc = qconj(q);
         const D3 lx = qtransform(qc, D3{m.h[0], 0, 0}), ly = qtransform(qc, D3{0, m.h[1], 0}),

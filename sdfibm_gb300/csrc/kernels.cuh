@@ -76,6 +76,8 @@ struct SolidPlan {
     int32_t pad1;
     double cbase[3];          // centre of the seed cell minus the solid centre (FP64), origin of FP32 cell offsets
     double base[3];           // mesh point (lo) minus the solid centre: FP64 origin of the FP32 tile frames
+    float base32[3];          // base rounded to FP32 (the frames' origin)
+    float pad4;
     double lmap[12];          // world2local of mesh point (lo), then the local images of h_x e_x, h_y e_y, h_z e_z
     float lmap_hi[12], lmap_lo[12];  // the same as FP32 pairs hi + lo (two-float vertex distances)
     float e64;                // bound of the FP64 rounding of point coordinates (see TileFrame)
