@@ -91,6 +91,27 @@ def test_shape_zoo(cuda_lib, torch_cuda, twod, method):
     check_interact(w, r)
 
 
+@pytest.mark.parametrize("method", [abi.FRACTION_REFGEO, abi.FRACTION_SUBSAMPLE])
+def test_filter_threshold_vertices(cuda_lib, torch_cuda, method):
+    """Surfaces 1e-8 away from mesh vertices: the vertex distances sit at the reference's filter threshold
+    (|phi| < 1e-8 -> -1e-8, sdf.h:147-150), where the FP32 and two-float paths hand over to the FP64 sequence."""
+    n = 32
+    h = 1.0 / n
+    mesh = abi.mesh_desc((n, n, n), (0.0, 0.0, 0.0), (h,) * 3, twod=0)
+    solids = []
+    for i, (t, kw, pos) in enumerate([
+            ("Sphere", dict(radius=6 * h + 1e-8), (8 * h, 8 * h, 8 * h)),
+            ("Sphere", dict(radius=5 * h - 1e-8), (24 * h, 8 * h, 8 * h)),
+            ("Box", dict(radiusa=4 * h + 1e-8, radiusb=3 * h - 1e-8, radiusc=5 * h), (8 * h, 24 * h, 8 * h)),
+            ("Ellipsoid", dict(radiusa=4 * h + 1e-8, radiusb=6 * h, radiusc=5 * h - 1e-8), (24 * h, 24 * h, 8 * h)),
+            ("Sphere", dict(radius=7 * h), (16 * h, 16 * h, 23 * h))]):
+        solids.append(make_solid(i, make_shape(t, **kw), 1.2, pos, vel=(0.1, 0.0, 0.0), omega=(0.0, 0.0, 0.5)))
+    opt = abi.options(rho_f=1.0, fraction_method=method)
+    w = Workload("threshold", mesh, solids, opt, 0.01, (0.1, 0.0, 0.0), 0.1, 3)
+    r = run_pair(torch_cuda, w)
+    check_interact(w, r)
+
+
 @pytest.mark.parametrize("cfg", ["poly3d_256", "sedimentation2d", "zoo3", "zoo2"])
 def test_mixed_precision_forcing(cuda_lib, torch_cuda, cfg):
     """exact_forcing = 0: FP64 only for the rigid-body velocity and U - us, FP32 after; same contract."""
