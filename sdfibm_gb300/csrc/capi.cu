@@ -58,11 +58,11 @@ __global__ void evolve_independent_kernel(const SolidK* sk, sdfibm_solid_state* 
                                           const StepParams* step, double rho_f, D3 g);
 __global__ void evolve_pre_kernel(const SolidK* sk, sdfibm_solid_state* st, int S, const StepParams* step, double rho_f, D3 g,
                                   GridK gk, int64_t* hashes, int32_t* counts, FineGridK fg, int32_t* fcounts, int mode,
-                                  int coarse_needed, CollRec* recs);
+                                  int coarse_needed, CollRec* recs, int move_first);
 __global__ void fine_scatter_kernel(const CollRec* recs, int S, FineGridK fg, int32_t* fcursor, int32_t* flist,
                                     Counters* cnt);
-__global__ void grid_scan_kernel(const int32_t* counts, int32_t* start, int32_t* cursor, int64_t ncell);
-__global__ void scan_blocks_kernel(const int32_t* counts, int32_t* start, int32_t* sums, int64_t ncell);
+__global__ void grid_scan_kernel(int32_t* counts, int32_t* start, int32_t* cursor, int64_t ncell);
+__global__ void scan_blocks_kernel(int32_t* counts, int32_t* start, int32_t* sums, int64_t ncell);
 __global__ void scan_add_kernel(int32_t* start, int32_t* cursor, const int32_t* sums_excl, int64_t ncell,
                                 int64_t nblocks);
 __global__ void grid_scatter_kernel(const int64_t* hashes, int32_t* cursor, int32_t* list, int S, int64_t ncell);
@@ -972,7 +972,7 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
 
 // Exclusive scan of per-cell counts into start (ncell + 1 entries, the total last) and cursor: one block for small
 // grids, else per-1024-cell block scans, one block over their sums, and the block offsets added back.
-static void scan_counts(sdfibm_ctx* ctx, const int32_t* counts, int32_t* start, int32_t* cursor, int64_t ncell) {
+static void scan_counts(sdfibm_ctx* ctx, int32_t* counts, int32_t* start, int32_t* cursor, int64_t ncell) {
     cudaStream_t st = ctx->stream;
     if (ncell <= 16384) {
         grid_scan_kernel<<<1, 1024, 0, st>>>(counts, start, cursor, ncell);
@@ -1001,11 +1001,13 @@ static int enqueue_evolve(sdfibm_ctx* ctx, double time, double dt) {
         const FineGridK& fg = ctx->fg;
         const int mode = ctx->opt.collision_mode;
         const int coarse = ctx->nplanes > 0;  // the coarse lists serve only the plane-like solids
+        // the scans zero the counts they read, so one clear serves every sub-step; Solid::move of sub-step it - 1
+        // runs at the head of sub-step it's force kernel
+        if (coarse) CK(cudaMemsetAsync(ctx->d_gcount, 0, sizeof(int32_t) * gk.ncell, st));
+        CK(cudaMemsetAsync(ctx->d_fcount, 0, sizeof(int32_t) * fg.ncell, st));
         for (int it = 0; it < nsub; ++it) {
-            if (coarse) CK(cudaMemsetAsync(ctx->d_gcount, 0, sizeof(int32_t) * gk.ncell, st));
-            CK(cudaMemsetAsync(ctx->d_fcount, 0, sizeof(int32_t) * fg.ncell, st));
             evolve_pre_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, step, ctx->opt.rho_f, g, gk, ctx->d_hash,
-                                               ctx->d_gcount, fg, ctx->d_fcount, mode, coarse, ctx->d_recs);
+                                               ctx->d_gcount, fg, ctx->d_fcount, mode, coarse, ctx->d_recs, it > 0);
             if (coarse) {
                 scan_counts(ctx, ctx->d_gcount, ctx->d_gstart, ctx->d_gcursor, gk.ncell);
                 grid_scatter_kernel<<<G, B, 0, st>>>(ctx->d_hash, ctx->d_gcursor, ctx->d_glist, S, gk.ncell);
@@ -1016,8 +1018,8 @@ static int enqueue_evolve(sdfibm_ctx* ctx, double time, double dt) {
             collide_kernel<<<GW, 256, 0, st>>>(
                 ctx->d_sk, ctx->d_st, S, gk, ctx->d_hash, ctx->d_gstart, ctx->d_glist, mode, fg, ctx->d_fstart,
                 ctx->d_flist, ctx->d_planes, ctx->nplanes, ctx->d_recs);
-            move_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, step);
         }
+        move_kernel<<<G, B, 0, st>>>(ctx->d_sk, ctx->d_st, S, step);
         store_old_kernel<<<G, B, 0, st>>>(ctx->d_st, S);
     }
     CK(cudaGetLastError());

@@ -197,9 +197,10 @@ __device__ inline int64_t fine_index(const FineGridK& fg, int i, int j, int k) {
 __global__ void evolve_pre_kernel(const SolidK* __restrict__ sk, sdfibm_solid_state* st, int S,
                                   const StepParams* step, double rho_f, D3 g, GridK gk, int64_t* __restrict__ hashes,
                                   int32_t* __restrict__ counts, FineGridK fg, int32_t* __restrict__ fcounts, int mode,
-                                  int coarse_needed, CollRec* __restrict__ recs) {
+                                  int coarse_needed, CollRec* __restrict__ recs, int move_first) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= S) return;
+    if (move_first) move_solid(sk[s], st[s], step->time, step->dt_sub);  // Solid::move of the previous sub-step
     pre_forces(sk[s], st[s], step->time, rho_f, g);
     const D3 c = ld3(st[s].pos);
     const int64_t h = grid_hash(gk, c);
@@ -241,8 +242,8 @@ __global__ void fine_scatter_kernel(const CollRec* __restrict__ recs, int S, Fin
     }
 }
 
-// exclusive scan of the per-cell counts (single block)
-__global__ void grid_scan_kernel(const int32_t* __restrict__ counts, int32_t* __restrict__ start,
+// exclusive scan of the per-cell counts (single block), zeroing them as they are read
+__global__ void grid_scan_kernel(int32_t* __restrict__ counts, int32_t* __restrict__ start,
                                  int32_t* __restrict__ cursor, int64_t ncell) {
     __shared__ int32_t warp_tot[32];
     __shared__ int32_t carry;
@@ -252,6 +253,7 @@ __global__ void grid_scan_kernel(const int32_t* __restrict__ counts, int32_t* __
     for (int64_t base = 0; base < ncell; base += blockDim.x) {
         const int64_t i = base + threadIdx.x;
         const int32_t v = i < ncell ? counts[i] : 0;
+        if (i < ncell) counts[i] = 0;  // read once: left zeroed for the next sub-step's counts
         int32_t x = v;
         for (int o = 1; o < 32; o <<= 1) {
             int32_t y = __shfl_up_sync(0xffffffffu, x, o);
@@ -277,13 +279,15 @@ __global__ void grid_scan_kernel(const int32_t* __restrict__ counts, int32_t* __
     if (threadIdx.x == 0) start[ncell] = carry;
 }
 
-// exclusive scan of large count arrays in three launches: per-1024-block scans, a scan of the block sums, offsets
-__global__ void __launch_bounds__(1024) scan_blocks_kernel(const int32_t* __restrict__ counts, int32_t* __restrict__ start,
+// exclusive scan of large count arrays in three launches: per-1024-block scans, a scan of the block sums, offsets;
+// the counts are zeroed as they are read
+__global__ void __launch_bounds__(1024) scan_blocks_kernel(int32_t* __restrict__ counts, int32_t* __restrict__ start,
                                                            int32_t* __restrict__ sums, int64_t ncell) {
     __shared__ int32_t warp_tot[32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
     const int32_t v = i < ncell ? counts[i] : 0;
+    if (i < ncell) counts[i] = 0;  // read once: left zeroed for the next sub-step's counts
     int32_t x = v;
     for (int o = 1; o < 32; o <<= 1) {
         const int32_t y = __shfl_up_sync(0xffffffffu, x, o);
