@@ -460,8 +460,12 @@ def main():
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_kind": peaks_kind,
                 "alg_bytes_per_unit": per_unit, "unit_of_work": unit_key, "units": units,
-                "note": "classify and the SUBSAMPLE fallback are FP32-ALU-bound (lattice inside tests), so their "
-                        "HBM fraction is small by construction; couple is the HBM-bound kernel",
+                "note": "the cut-cell evaluators (subsample_cells_kernel, classify, refgeo_cells_kernel) are bound "
+                        "by FP32 instruction issue, not memory: ncu reads 77 % issue active and 0.2 % DRAM throughput "
+                        "for subsample_cells_kernel (profiles/subsample_cells_kernel_poly3d_256_learned.md), so their "
+                        "HBM fraction is small by construction; couple_kernel is the HBM-bound kernel (51 % of DRAM "
+                        "peak in ncu, 220 B of traffic per coupling cell against 36 B algorithmic: the touched cells "
+                        "form short x-runs in six field planes)",
                 "kernel_ms": {k: round(v, 4) for k, v in sorted(kmean.items(), key=lambda x: -x[1])}}
     # the HBM-bound kernel of the step and the tensor-core kernel, each against its own peak
     if "couple_kernel" in kmean:
