@@ -898,12 +898,17 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
             cudaMemsetAsync(ctx->d_dirty, 0, sizeof(uint32_t) * words, st) != cudaSuccess)
             return fail(ctx, SDFIBM_ERR_CUDA, "staging allocation failed");
     }
-    // upload U on a copy stream once the previous work on the stream (which may still read d_U) is done; the
-    // enumeration and fraction kernels run meanwhile and the coupling kernel waits for it
-    CK(cudaEventRecord(ctx->ev_entry, st));
-    CK(cudaStreamWaitEvent(ctx->copy_st[0], ctx->ev_entry, 0));
-    CK(cudaMemcpyAsync(ctx->d_U, U, sizeof(float) * 3 * N, cudaMemcpyHostToDevice, ctx->copy_st[0]));
-    CK(cudaEventRecord(ctx->ev_u, ctx->copy_st[0]));
+    // U: REF-GEO's enumeration and fraction kernels take less time than copying the whole field in, so a page-locked
+    // U is read in place by the coupling kernel (only at the coupling cells); otherwise U is copied in on a second
+    // stream while those kernels run (once the previous work, which may still read d_U, is done) and the coupling
+    // kernel waits for it
+    const void* u_host = ctx->opt.fraction_method == SDFIBM_FRACTION_REFGEO ? mapped_host(U) : nullptr;
+    if (!u_host) {
+        CK(cudaEventRecord(ctx->ev_entry, st));
+        CK(cudaStreamWaitEvent(ctx->copy_st[0], ctx->ev_entry, 0));
+        CK(cudaMemcpyAsync(ctx->d_U, U, sizeof(float) * 3 * N, cudaMemcpyHostToDevice, ctx->copy_st[0]));
+        CK(cudaEventRecord(ctx->ev_u, ctx->copy_st[0]));
+    }
     // page-locked host fields take the cells that changed since the previous call, written in place (all of them on
     // the first call, after a change of buffers, and with dense_reset); other memory gets whole-field copies
     void* const hp[4] = {mapped_host(As), mapped_host(Fs), mapped_host(Ts), mapped_host(Ct)};
@@ -912,8 +917,9 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
         bool same = ctx->host_synced && !ctx->opt.dense_reset;
         for (int i = 0; i < 5; ++i) same = same && f5[i] == ctx->host_fields[i];
         ctx->host_synced = false;
-        ctx->u_wait = ctx->ev_u;
-        int rc = sdfibm_cuda_interact(ctx, time, dt, ctx->d_U, ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, nullptr);
+        ctx->u_wait = u_host ? nullptr : ctx->ev_u;
+        int rc = sdfibm_cuda_interact(ctx, time, dt, u_host ? static_cast<const float*>(u_host) : ctx->d_U, ctx->d_As,
+                                      ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, nullptr);
         ctx->u_wait = nullptr;
         if (rc) return rc;
         if (same) {
@@ -938,7 +944,7 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
         rc = sync_counters(ctx);
         if (rc) return rc;
         const Counters& c = *ctx->h_cnt;
-        ctx->host_h2d = 12 * N;
+        ctx->host_h2d = u_host ? 12 * ((int64_t)c.n_inside + c.n_cut) : 12 * N;
         ctx->host_d2h = (same ? 24 * (int64_t)export_chunk_cells() * c.n_export : 24 * N) + 48 * ctx->S;
         ctx->host_sparse = same;
         for (int i = 0; i < 5; ++i) ctx->host_fields[i] = f5[i];
@@ -947,8 +953,9 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
         return SDFIBM_OK;
     }
     ctx->host_synced = false;
-    ctx->u_wait = ctx->ev_u;
-    int rc = sdfibm_cuda_interact(ctx, time, dt, ctx->d_U, ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, nullptr);
+    ctx->u_wait = u_host ? nullptr : ctx->ev_u;
+    int rc = sdfibm_cuda_interact(ctx, time, dt, u_host ? static_cast<const float*>(u_host) : ctx->d_U, ctx->d_As,
+                                  ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, nullptr);
     ctx->u_wait = nullptr;
     if (rc) return rc;
     CK(cudaEventRecord(ctx->ev_done, st));
@@ -963,7 +970,7 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
     rc = sync_counters(ctx);
     for (auto& c : ctx->copy_st) CK(cudaStreamSynchronize(c));
     if (rc) return rc;
-    ctx->host_h2d = 12 * N;
+    ctx->host_h2d = u_host ? 12 * ((int64_t)ctx->h_cnt->n_inside + ctx->h_cnt->n_cut) : 12 * N;
     ctx->host_d2h = 24 * N + 48 * ctx->S;
     ctx->host_sparse = false;
     if (FT) std::memcpy(FT, ctx->h_ft, sizeof(double) * 6 * ctx->S);
