@@ -1,19 +1,24 @@
 // Coupling kernels: the GB300 replacement of SolidCloud::interact (src/solidcloud.cpp:361-464) and
 // SolidCloud::fixInternal (src/solidcloud.cpp:288-301).
 //
-// Pipeline of one interact (all on one stream, no host round trip until FT is read back):
-//   reset     zero As/Fs/Ts/Ct at the cells the previous call touched (sparse form of solidcloud.cpp:438-441)
-//   plan      per solid: bbox origin in cell indices, FP32 world->local matrix, nearest cell (meshSearch)
+// Pipeline of one interact (no host round trip until FT is read back):
+//   plan      per solid: bbox origin in cell indices, FP32 world->local matrix, nearest cell (meshSearch), the
+//             two-float forms used by the fraction and forcing kernels
 //   classify  persistent CTAs pulling (solid, cell-tile) items from an atomic counter; each tile evaluates the
 //             inside test once per vertex (FP32 with a guard band, FP64 re-check inside the band) and writes one
 //             class byte per cell: 0 no inside vertex, 1 all inside, 2 centre inside, 3 centre outside
-//             (CellEnumerator::_next, cellenumerator.cpp:6-34)
-//   connect   one CTA per solid: bit-parallel flood fill from the seed over cells with an inside vertex
-//             (the BFS of CellEnumerator::intersect with its seed fallback, cellenumerator.cpp:47-78), then
-//             appends the reached cells to the ALL_INSIDE list or the cut-cell list in ascending cell order
-//   couple    persistent CTAs over 256-entry chunks of both lists: alpha (1, REF-GEO, SUBSAMPLE), direct forcing,
-//             field accumulation with atomics, warp then FP64-atomic reduction of force and torque per solid
-//   finalize  Ct key -> Ct value (last solid wins, as the serial loop), As = min(As,1) (checkAlpha), FT = rho_f*sum
+//             (CellEnumerator::_next, cellenumerator.cpp:6-34), and lists the cut cells for the fraction kernels
+//   fraction  (classify.cu) REF-GEO a thread per listed cell; SUBSAMPLE a warp per listed cell; LEARNED the network,
+//             then SUBSAMPLE on the cells outside its band; FP64 rechecks of undecided sample points
+//   connect   on a side stream beside the fraction kernels: one CTA (or warp) per solid, bit-parallel flood fill
+//             from the seed over cells with an inside vertex (the BFS of CellEnumerator::intersect with its seed
+//             fallback, cellenumerator.cpp:47-78), then the reached cells appended to the ALL_INSIDE list or the
+//             cut-cell list in ascending cell order; claim of each touched cell; reset of the cells the previous call
+//             touched and this one does not (sparse form of solidcloud.cpp:438-441)
+//   couple    persistent CTAs over 256-entry chunks of both lists: alpha (1, or the fraction), direct forcing, the
+//             final fields of single-owner cells, warp then FP64-atomic reduction of force and torque per solid
+//   finalize  cells of several solids from the FP64 table: Ct of the last solid (as the serial loop), As = min(As,1)
+//             (checkAlpha); ft: FT = rho_f V / dt * sums
 #include <cstdint>
 #include <cuda_runtime.h>
 
