@@ -1,4 +1,4 @@
-// Enumeration and cut-cell solid fraction in one pass over (solid, cell-tile) work items.
+// Enumeration and cut-cell solid fraction: one pass over (solid, cell-tile) work items, then per-cell kernels.
 //
 // Each persistent CTA pulls tiles from an atomic counter.  For a tile it
 //   1. skips tiles whose box cannot meet the solid's bounding sphere (prism: bounding disc) and zero-fills them;
@@ -6,15 +6,17 @@
 //      band -- identical answers to the reference's FP64 Solid::phi01) and writes one class byte per cell
 //      (CellEnumerator::_next, src/cellenumerator.cpp:6-34): 0 no inside vertex, 1 all inside, 2 centre inside,
 //      3 centre outside;
-//   3. computes the solid fraction of every cut candidate (class 2/3) and writes it to the alpha scratch:
-//      REF-GEO   GeometricTools::calcCellVolume (src/geometrictools.cpp:13-116): the vertex signed distances are
-//                evaluated once per tile vertex next to a cut cell (FP64 wherever a difference can cancel, see
-//                sdf_mixed) and kept in shared memory; the apex/pyramid geometry then runs in FP32 in cell-local
-//                coordinates (vertices on {0,1}^3), where on an axis-aligned hexahedron every term is a product of
-//                non-negative factors and no subtraction cancels, so the result keeps ~1e-7 relative accuracy;
-//      SUBSAMPLE one warp per cut cell, n^3 (3-D) or n^2 (2-D) midpoint samples, each with the same exact inside
-//                test as the vertices.
-// Candidates that the flood fill later leaves out simply have their alpha ignored.
+//   3. lists every cut candidate (class 2/3) for the fraction kernels:
+//      REF-GEO   with the signed distances of its 8 vertices (two-float for 3-D spheres, ellipsoids and boxes, FP64
+//                numerators elsewhere, see sdf_ff / sdf_mixed); refgeo_cells_kernel then runs
+//                GeometricTools::calcCellVolume (src/geometrictools.cpp:13-116) in FP32 in cell-local coordinates
+//                (vertices on {0,1}^3, every term a product of non-negative factors), a thread per cell;
+//      SUBSAMPLE as (solid, fraction index); subsample_cells_kernel counts the n^3 (2-D: n^2) midpoint lattice of
+//                each listed cell, a warp per cell, with the same exact inside test as the vertices (run counting
+//                along lattice columns for the convex shapes), undecided points rechecked in FP64 by recheck_kernel;
+//      LEARNED   with the network's features; the cells outside its band go to subsample_cells_kernel.
+// The allocation-free entry point computes the fractions inside the tile pass instead.  Candidates that the flood
+// fill later leaves out simply have their alpha ignored.
 #include <cstdint>
 #include <cuda_runtime.h>
 
