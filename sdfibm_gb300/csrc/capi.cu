@@ -498,7 +498,10 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         }
     }
 
-    // device allocations
+    // device allocations; REF-GEO and SUBSAMPLE list their cut cells (one entry per bbox cell at most)
+    const bool cell_list = ctx->opt.fraction_method == SDFIBM_FRACTION_SUBSAMPLE ||
+                           ctx->opt.fraction_method == SDFIBM_FRACTION_REFGEO;
+    if (cell_list) ctx->feat_cap = std::max<int64_t>(1, scratch);
     if (dalloc(&ctx->d_sk, nsolids) || dalloc(&ctx->d_st, nsolids) || dalloc(&ctx->d_plan, nsolids) ||
         dalloc(&ctx->d_chunks, (size_t)ctx->total_tiles) || dalloc(&ctx->d_scratch, scratch) || dalloc(&ctx->d_alpha, scratch) ||
         dalloc(&ctx->d_gbitmaps, gwords) || dalloc(&ctx->d_lists[0][0], ctx->cap) || dalloc(&ctx->d_lists[0][1], ctx->cap) ||
@@ -510,9 +513,8 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         dalloc(&ctx->d_sh_used, (size_t)ctx->sh_mask + 1) || dalloc(&ctx->d_step, 2) ||
         dalloc(&ctx->d_small, small_solids.size()) || dalloc(&ctx->d_big, big_solids.size()) ||
         dalloc(&ctx->d_rq, (size_t)ctx->rq_cap) || dalloc(&ctx->d_ovf, (size_t)ctx->ovf_cap) ||
-        ((ctx->opt.fraction_method == SDFIBM_FRACTION_SUBSAMPLE || ctx->opt.fraction_method == SDFIBM_FRACTION_REFGEO) &&
-         (dalloc(&ctx->d_fref_solid, (size_t)(ctx->feat_cap = std::max<int64_t>(1, scratch))) ||
-          dalloc(&ctx->d_fref_index, (size_t)ctx->feat_cap))) ||
+        (cell_list &&
+         (dalloc(&ctx->d_fref_solid, (size_t)ctx->feat_cap) || dalloc(&ctx->d_fref_index, (size_t)ctx->feat_cap))) ||
         (ctx->opt.fraction_method == SDFIBM_FRACTION_REFGEO && dalloc(&ctx->d_rg_phi, 8 * (size_t)ctx->feat_cap)) ||
         cudaMallocHost((void**)&ctx->h_cnt, sizeof(Counters)) != cudaSuccess ||
         cudaMallocHost((void**)&ctx->h_ft, std::max<size_t>(1, 6 * (size_t)nsolids) * sizeof(double)) != cudaSuccess) {
