@@ -507,7 +507,7 @@ def main():
         # page-locked fields: U copied in during the fraction kernels, the changed cells written back in place
         e2e = {"value": mean_cells * world / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": h2d // reps,
                "d2h_bytes_per_step": d2h // reps, "ms_per_step": e2e_s * 1e3,
-               "host_fields": ("page-locked; U read in place at the coupling cells" if args.method == "refgeo" else
+               "host_fields": ("page-locked; U read in place at the coupling cells" if h2d // reps < 12 * N else
                                "page-locked; U copied in while the fraction kernels run") +
                               ", changed 8-cell chunks written back in place"
                if st["host_sparse"] else "staged through whole-field copies"}

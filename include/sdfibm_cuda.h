@@ -179,8 +179,9 @@ int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U
                          int32_t* Ct, double* FT);
 
 /* Same as sdfibm_cuda_interact but every field pointer is a HOST pointer (the path an OpenFOAM-resident caller
- * takes).  U is copied in on a second stream while the enumeration and fraction kernels run (REF-GEO, whose
- * kernels take less time than the copy, reads a page-locked U in place at the coupling cells).  Page-locked fields
+ * takes).  U is copied in on a second stream while the enumeration and fraction kernels run; a page-locked U is
+ * read in place at the coupling cells instead with REF-GEO (whose kernels take less time than the copy) and, after
+ * two calls whose copy outlasted those kernels, with the other methods.  Page-locked fields
  * (cudaHostAlloc / cudaHostRegister) are written in place with the cells this call or the previous one touched,
  * while the call gets the same five buffers as the previous one and the caller leaves the four fields alone in
  * between (the first call, other buffers, or dense_reset copy the whole fields); other host memory receives

@@ -162,6 +162,12 @@ struct sdfibm_ctx {
     cudaStream_t side_st = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t u_wait = nullptr;  // set while interact_host runs: couple waits for the upload
+    // interact_host: U copied in whole while the fraction kernels run, unless the copy outlasts them on this machine
+    // (measured on the calls, events t0 -> copy done and t0 -> the coupling kernel's wait): then a page-locked U is
+    // read in place at the coupling cells
+    bool u_probe = false, u_in_place = false;
+    int u_slow = 0;
+    cudaEvent_t ev_t0 = nullptr, ev_tu = nullptr, ev_tpre = nullptr;
     // interact_host on page-locked host fields: the host buffers of the last such call (their cells equal the device
     // fields after it) and the bytes the last interact_host moved each way
     const void* host_fields[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -726,7 +732,10 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
                                                         Ts, Ct);
         ++launches;
     }
-    if (ctx->u_wait) CK(cudaStreamWaitEvent(st, ctx->u_wait, 0));  // U staged on a copy stream (interact_host)
+    if (ctx->u_wait) {  // U staged on a copy stream (interact_host)
+        if (ctx->u_probe) CK(cudaEventRecord(ctx->ev_tpre, st));
+        CK(cudaStreamWaitEvent(st, ctx->u_wait, 0));
+    }
     if (S > 0) {
         CoupleArgs A{};
         A.m = ctx->mesh; A.sk = ctx->d_sk; A.st = ctx->d_st; A.plan = ctx->d_plan;
@@ -891,6 +900,9 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
         CK(cudaEventCreateWithFlags(&ctx->ev_entry, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&ctx->ev_u, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming));
+        CK(cudaEventCreate(&ctx->ev_t0));
+        CK(cudaEventCreate(&ctx->ev_tu));
+        CK(cudaEventCreate(&ctx->ev_tpre));
     }
     if (!ctx->d_As) {
         // one bit per chunk of export_chunk_cells() cells, 32 chunks per word
@@ -904,13 +916,31 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
     // U is read in place by the coupling kernel (only at the coupling cells); otherwise U is copied in on a second
     // stream while those kernels run (once the previous work, which may still read d_U, is done) and the coupling
     // kernel waits for it
-    const void* u_host = ctx->opt.fraction_method == SDFIBM_FRACTION_REFGEO ? mapped_host(U) : nullptr;
+    const void* u_host =
+        ctx->opt.fraction_method == SDFIBM_FRACTION_REFGEO || ctx->u_in_place ? mapped_host(U) : nullptr;
+    ctx->u_probe = !u_host;
     if (!u_host) {
         CK(cudaEventRecord(ctx->ev_entry, st));
+        CK(cudaEventRecord(ctx->ev_t0, st));
         CK(cudaStreamWaitEvent(ctx->copy_st[0], ctx->ev_entry, 0));
         CK(cudaMemcpyAsync(ctx->d_U, U, sizeof(float) * 3 * N, cudaMemcpyHostToDevice, ctx->copy_st[0]));
         CK(cudaEventRecord(ctx->ev_u, ctx->copy_st[0]));
+        CK(cudaEventRecord(ctx->ev_tu, ctx->copy_st[0]));
     }
+    // after the call: a copy that outlasted the kernels before the coupling by more than the in-place reads cost
+    // there (about 1 ms at 512^3), twice in a row, switches a page-locked U to in-place reads
+    auto judge_copy = [&]() {
+        if (!ctx->u_probe) return;
+        ctx->u_probe = false;
+        float t_copy = 0.f, t_pre = 0.f;
+        if (cudaEventElapsedTime(&t_copy, ctx->ev_t0, ctx->ev_tu) != cudaSuccess ||
+            cudaEventElapsedTime(&t_pre, ctx->ev_t0, ctx->ev_tpre) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        ctx->u_slow = t_copy > t_pre + 1.0f ? ctx->u_slow + 1 : 0;
+        if (ctx->u_slow >= 2 && mapped_host(U)) ctx->u_in_place = true;
+    };
     // page-locked host fields take the cells that changed since the previous call, written in place (all of them on
     // the first call, after a change of buffers, and with dense_reset); other memory gets whole-field copies
     void* const hp[4] = {mapped_host(As), mapped_host(Fs), mapped_host(Ts), mapped_host(Ct)};
@@ -951,6 +981,7 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
         ctx->host_sparse = same;
         for (int i = 0; i < 5; ++i) ctx->host_fields[i] = f5[i];
         ctx->host_synced = true;
+        judge_copy();
         if (FT) std::memcpy(FT, ctx->h_ft, sizeof(double) * 6 * ctx->S);
         return SDFIBM_OK;
     }
@@ -975,6 +1006,7 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
     ctx->host_h2d = u_host ? 12 * ((int64_t)ctx->h_cnt->n_inside + ctx->h_cnt->n_cut) : 12 * N;
     ctx->host_d2h = 24 * N + 48 * ctx->S;
     ctx->host_sparse = false;
+    judge_copy();
     if (FT) std::memcpy(FT, ctx->h_ft, sizeof(double) * 6 * ctx->S);
     return SDFIBM_OK;
 }
@@ -1242,6 +1274,9 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
     if (ctx->ev_u) cudaEventDestroy(ctx->ev_u);
     if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_t0) cudaEventDestroy(ctx->ev_t0);
+    if (ctx->ev_tu) cudaEventDestroy(ctx->ev_tu);
+    if (ctx->ev_tpre) cudaEventDestroy(ctx->ev_tpre);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->side_st) cudaStreamDestroy(ctx->side_st);
     if (ctx->d_big) cudaFree(ctx->d_big);
