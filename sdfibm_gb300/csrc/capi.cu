@@ -929,7 +929,7 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
     }
     // after the call: a copy that outlasted the kernels before the coupling by more than the in-place reads cost
     // there (about 1 ms at 512^3), twice in a row, switches a page-locked U to in-place reads
-    auto judge_copy = [&]() {
+    auto assess_u_copy = [&]() {
         if (!ctx->u_probe) return;
         ctx->u_probe = false;
         float t_copy = 0.f, t_pre = 0.f;
@@ -981,7 +981,7 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
         ctx->host_sparse = same;
         for (int i = 0; i < 5; ++i) ctx->host_fields[i] = f5[i];
         ctx->host_synced = true;
-        judge_copy();
+        assess_u_copy();
         if (FT) std::memcpy(FT, ctx->h_ft, sizeof(double) * 6 * ctx->S);
         return SDFIBM_OK;
     }
@@ -1006,7 +1006,7 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
     ctx->host_h2d = u_host ? 12 * ((int64_t)ctx->h_cnt->n_inside + ctx->h_cnt->n_cut) : 12 * N;
     ctx->host_d2h = 24 * N + 48 * ctx->S;
     ctx->host_sparse = false;
-    judge_copy();
+    assess_u_copy();
     if (FT) std::memcpy(FT, ctx->h_ft, sizeof(double) * 6 * ctx->S);
     return SDFIBM_OK;
 }
