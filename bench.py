@@ -53,6 +53,19 @@ MLP_FLOPS_PER_CELL = 2 * (2 * 16 * 64) + 2 * (2 * 64 * 64)
 METHODS = {"refgeo": 0, "subsample": 1, "learned": 2}
 
 
+def over_ranks(dist, ms_step, cells, device):
+    """(max of ms_step, sum of cells) over the ranks of the default process group; unchanged without one.  Each rank
+    runs its own replica of the workload, so the job's time is the slowest rank's and its work the sum."""
+    if dist is None:
+        return ms_step, cells
+    import torch
+    t = torch.tensor([ms_step], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    c = torch.tensor([cells], dtype=torch.float64, device=device)
+    dist.all_reduce(c, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(c.item())
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -356,12 +369,9 @@ def main():
     del ft_
     tm["kernel_ms"] = tk["kernel_ms"]
     ms_step = tm["ms_step"]
-    if dist:
-        tt = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_step = float(tt.item())
     mean_cells = tm["cells"]
-    value = mean_cells * world / (ms_step * 1e-3)
+    ms_step, job_cells = over_ranks(dist, ms_step, mean_cells, "cuda")
+    value = job_cells / (ms_step * 1e-3)
     launches = tm["launches"]
     bbox = [tm["bbox"]]
     kt = {k: [v] for k, v in tm["kernel_ms"].items()}
