@@ -43,6 +43,34 @@ int sdfibm_host_make_solid(int32_t id, const sdfibm_shape_desc* shape, double rh
 int sdfibm_host_parse_soliddict(const char* text, double rho_f, sdfibm_solid_desc* solids, int32_t capacity,
                                 int32_t* nsolids, sdfibm_options* opt, int32_t* on_twod, char* msg, int32_t msg_len);
 
+/* ---- output: the state file and the restart dictionary --------------------------------------------------------------
+ * Text results go to buf: at most cap bytes including the terminating NUL; *len receives the length of the whole
+ * text (without the NUL).  buf == NULL with cap == 0 only measures; a buffer of cap <= *len returns
+ * SDFIBM_ERR_CAPACITY. */
+
+/* quaternion::eulerAngles(quaternion::XYZ) (OpenFOAM 12, as called at src/solid.cpp:12 and src/solidcloud.cpp:638):
+ * the angles (radians) a, b, c with quat = qx(a) qy(b) qz(c), the inverse of sdfibm_host_quat_from_euler_deg for
+ * |b| < 90 degrees and |a|, |c| < 180 degrees. */
+void sdfibm_host_euler_from_quat(const double* quat_wxyz, double* euler_rad);
+
+/* The records one SolidCloud::saveState appends to cloud.out (operator<<(SolidCloud) src/solidcloud.cpp:595-614,
+ * operator<<(Solid) and write2D src/solid.cpp:5-29), a line per solid, every number as std::scientific with 6 digits:
+ *   3-D: time pos.xyz vel.xyz force.xyz euler.xyz(radians) omega.xyz torque.xyz        (19 columns)
+ *   2-D: time pos.x pos.y vel.x vel.y force.x force.y euler.z omega.z torque.z         (10 columns)
+ * time is the time of the last SolidCloud::evolve (the construction time before the first). */
+int sdfibm_host_format_state(double time, int32_t twod, const sdfibm_solid_state* states, int32_t n, char* buf,
+                             int64_t cap, int64_t* len);
+
+/* SolidCloud::saveRestart (src/solidcloud.cpp:616-665): the solidDict text with pos, vel, euler (degrees) and omega
+ * of the i-th entry of its `solids` sub-dictionary set from states[i] (2-D: pos.z, vel.z, omega.x and omega.y
+ * written as 0), the tree written in OpenFOAM's dictionary layout with `precision` significant digits (the case's
+ * writePrecision; 0: 6) after the solidDict file header, and a last line "// <stamp>" (NULL: the local time as
+ * strftime "%y/%m/%d %X").  n must equal the number of entries of `solids`; errors return SDFIBM_ERR_ARG with a
+ * message in msg (may be NULL). */
+int sdfibm_host_write_restart(const char* dict_text, const sdfibm_solid_state* states, int32_t n, int32_t twod,
+                              int32_t precision, const char* stamp, char* buf, int64_t cap, int64_t* len, char* msg,
+                              int32_t msg_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -4,7 +4,9 @@
     FT = cloud.interact(t, dt, U, fields)              # SolidCloud::interact   (fields: As, Fs, Ts, Ct)
     cloud.evolve(t, dt)                                # SolidCloud::evolve
     cloud.fix_internal(fields["Ct"], U)                # SolidCloud::fixInternal
-    cloud.states() / cloud.set_states(st)              # Solid getters / setters (saveState, saveRestart)
+    cloud.states() / cloud.set_states(st)              # Solid getters / setters
+    cloud.save_state(state_file)                       # SolidCloud::saveState   (state_file: host.StateFile)
+    cloud.save_restart(dict_text, path)                # SolidCloud::saveRestart
 
 Fields are CUDA tensors in the cell-major layout of include/sdfibm_cuda.h: U and Fs have shape (3, N) float32,
 As and Ts (N,) float32, Ct (N,) int32.  Every call goes through libsdfibm_cuda.so; errors raise CouplingError
@@ -15,6 +17,7 @@ import ctypes as C
 import numpy as np
 
 from . import abi
+from . import host
 from ._lib import load
 
 
@@ -29,9 +32,10 @@ def _ptr(t):
 
 
 class SolidCloud:
-    def __init__(self, mesh, solids, opt=None, stream=None):
+    def __init__(self, mesh, solids, opt=None, stream=None, time=0.0):
         self._L = load()
         self.mesh = mesh
+        self.time = float(time)  # m_time: the construction time, then the time of the last evolve
         self.nsolids = len(solids)
         self.ncells = int(mesh.nx) * int(mesh.ny) * int(mesh.nz)
         self._solids = (abi.SolidDesc * max(1, len(solids)))(*solids)
@@ -87,6 +91,7 @@ class SolidCloud:
 
     def evolve(self, time, dt):
         self._check(self._L.sdfibm_cuda_evolve(self._h, float(time), float(dt)))
+        self.time = float(time)
 
     def fix_internal(self, Ct, U):
         self._check(self._L.sdfibm_cuda_fix_internal(self._h, _ptr(Ct), _ptr(U)))
@@ -99,6 +104,17 @@ class SolidCloud:
     def set_states(self, states):
         arr = (abi.SolidState * max(1, self.nsolids))(*states)
         self._check(self._L.sdfibm_cuda_set_solids(self._h, arr, self.nsolids))
+
+    def save_state(self, state_file):
+        """SolidCloud::saveState: appends this step's records to a host.StateFile (cloud.out)."""
+        state_file.save(self.time, self.states())
+
+    def save_restart(self, dict_text, path, precision=6, stamp=None):
+        """SolidCloud::saveRestart: writes the solidDict read at construction (dict_text) with every solid's pos,
+        vel, euler and omega set to its current state."""
+        text = host.write_restart(dict_text, self.states(), bool(self.mesh.twod), precision, stamp)
+        with open(path, "w") as f:
+            f.write(text)
 
     def touched(self, s):
         n = C.c_int64(0)

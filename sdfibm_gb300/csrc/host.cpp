@@ -10,7 +10,10 @@
 #include <algorithm>
 #include <cctype>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <ctime>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -235,6 +238,7 @@ struct Node {
     bool is_dict = false;
     std::vector<std::pair<std::string, std::shared_ptr<Node>>> entries;
     std::vector<std::string> tokens;
+    std::vector<char> quoted;  // per token: read as a "string"
 
     const Node* find(const std::string& k) const {
         for (auto& e : entries)
@@ -251,6 +255,7 @@ struct Node {
 struct Lexer {
     const std::string& s;
     size_t i = 0;
+    bool quoted = false;  // the last token was a "string"
     explicit Lexer(const std::string& t) : s(t) {}
     void skip() {
         for (;;) {
@@ -269,6 +274,7 @@ struct Lexer {
         skip();
         if (i >= s.size()) return false;
         const char c = s[i];
+        quoted = c == '"';
         if (c == '{' || c == '}' || c == '(' || c == ')' || c == ';' || c == '[' || c == ']') {
             tok = std::string(1, c);
             ++i;
@@ -312,6 +318,7 @@ std::shared_ptr<Node> parse_dict(Lexer& lx, bool top) {
             if (tok == ";" && depth == 0) break;
             if (tok == "{" || tok == "}") throw std::runtime_error("unexpected brace in value of " + key);
             v->tokens.push_back(tok);
+            v->quoted.push_back(lx.quoted);
             if (!lx.next(tok)) throw std::runtime_error("unexpected end in value of " + key);
         }
         n->entries.emplace_back(key, v);
@@ -524,5 +531,214 @@ extern "C" int sdfibm_host_parse_soliddict(const char* text, double rho_f, sdfib
     } catch (const std::exception& e) {
         return err(e.what());
     }
+    return SDFIBM_OK;
+}
+
+// ---- state records and restart dictionary ------------------------------------------------------------------------------
+//   euler      OpenFOAM 12 quaternion::eulerAngles(quaternion::XYZ), used by src/solid.cpp:12 and
+//              src/solidcloud.cpp:638: for q = qx(a) qy(b) qz(c), R = Rx(a) Ry(b) Rz(c), so
+//              R02 = sin b, R12 = -sin a cos b, R22 = cos a cos b, R01 = -cos b sin c, R00 = cos b cos c
+//   state      SolidCloud::saveState / operator<<(SolidCloud) src/solidcloud.cpp:578-614 on a stream set to
+//              std::scientific (src/solidcloud.cpp:235-236), operator<<(Solid) and write2D src/solid.cpp:5-29
+//   restart    SolidCloud::saveRestart src/solidcloud.cpp:616-665: dictionary::set of pos / vel / euler / omega in
+//              every solids entry, then dictionary::write of the whole tree in OpenFOAM's ascii layout
+namespace {
+
+void euler_xyz(const double* q, double* e) {
+    const double w = q[0], x = q[1], y = q[2], z = q[3];
+    e[0] = std::atan2(-2 * (y * z - w * x), w * w - x * x - y * y + z * z);
+    e[1] = std::asin(2 * (x * z + w * y));
+    e[2] = std::atan2(-2 * (x * y - w * z), w * w + x * x - y * y - z * z);
+}
+
+void put_sci(std::string& out, double v) {  // std::ostream << double under std::scientific, precision 6
+    char b[40];
+    std::snprintf(b, sizeof(b), "%.6e", v);
+    out += b;
+}
+
+std::string put_g(double v, int prec) {  // std::ostream << double in the default float format
+    char b[48];
+    std::snprintf(b, sizeof(b), "%.*g", prec, v);
+    return b;
+}
+
+// OpenFOAM's tokeniser reads a word that starts like a number as a label (digits only) or a scalar
+bool is_number_token(const std::string& t) {
+    if (t.empty()) return false;
+    const char c = t[0];
+    if (!(std::isdigit((unsigned char)c) || c == '-' || c == '+' || c == '.')) return false;
+    char* end = nullptr;
+    std::strtod(t.c_str(), &end);
+    return end == t.c_str() + t.size();
+}
+bool is_label_token(const std::string& t) {
+    size_t i = (t[0] == '-' || t[0] == '+') ? 1 : 0;
+    if (i == t.size() || t.size() - i > 18) return false;
+    for (; i < t.size(); ++i)
+        if (!std::isdigit((unsigned char)t[i])) return false;
+    return true;
+}
+std::string format_token(const std::string& t, bool quoted, int prec) {
+    if (quoted) return "\"" + t + "\"";
+    if (!is_number_token(t)) return t;
+    if (is_label_token(t)) return std::to_string(std::stoll(t));
+    return put_g(std::strtod(t.c_str(), nullptr), prec);
+}
+
+// dictionary::set: replace the value of an existing keyword in place, else append the entry
+void set_vector(Node& d, const std::string& key, const double v[3], int prec) {
+    auto n = std::make_shared<Node>();
+    n->tokens = {"(", put_g(v[0], prec), put_g(v[1], prec), put_g(v[2], prec), ")"};
+    n->quoted.assign(n->tokens.size(), 0);
+    for (auto& e : d.entries)
+        if (e.first == key) {
+            e.second = n;
+            return;
+        }
+    d.entries.emplace_back(key, n);
+}
+
+// dictionary::write: primitive entries as the keyword padded to 16 columns, the tokens separated by one space and
+// ';'; sub-dictionaries as the keyword, then '{' ... '}' on lines of their own; 4 spaces of indent per level; an
+// empty line between the entries of the top level
+void write_dict(std::string& out, const Node& d, int level, int prec) {
+    std::vector<const std::pair<std::string, std::shared_ptr<Node>>*> list;
+    for (auto& e : d.entries)
+        if (!(level == 0 && e.first == "FoamFile")) list.push_back(&e);  // read without its header entry
+    const std::string ind(4 * level, ' ');
+    for (size_t k = 0; k < list.size(); ++k) {
+        const std::string& key = list[k]->first;
+        const Node& n = *list[k]->second;
+        if (n.is_dict) {
+            out += ind + key + "\n" + ind + "{\n";
+            write_dict(out, n, level + 1, prec);
+            out += ind + "}\n";
+        } else {
+            out += ind + key;
+            out.append(std::max<int>(16 - (int)key.size(), 1), ' ');
+            for (size_t i = 0; i < n.tokens.size(); ++i) {
+                if (i) out += ' ';
+                out += format_token(n.tokens[i], i < n.quoted.size() && n.quoted[i], prec);
+            }
+            out += ";\n";
+        }
+        if (level == 0 && k + 1 < list.size()) out += "\n";
+    }
+}
+
+const char* const kRestartHeader =
+    "/*--------------------------------*- C++ -*----------------------------------*\\\n"
+    "| =========                 |                                                 |\n"
+    "| \\\\      /  F ield         | OpenFOAM: The Open Source CFD Toolbox           |\n"
+    "|  \\\\    /   O peration     | Version:  6.0.0                                 |\n"
+    "|   \\\\  /    A nd           | Web:      www.OpenFOAM.org                      |\n"
+    "|    \\\\/     M anipulation  |                                                 |\n"
+    "\\*---------------------------------------------------------------------------*/\n"
+    "FoamFile\n{\n"
+    "    version     2.0;\n    format      ascii;\n    class       dictionary;\n    object      solidDict;\n}\n"
+    "// * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * //\n";
+
+int emit(const std::string& text, char* buf, int64_t cap, int64_t* len) {
+    if (len) *len = (int64_t)text.size();
+    if (!buf) return cap > 0 ? SDFIBM_ERR_ARG : SDFIBM_OK;
+    if (cap <= (int64_t)text.size()) return SDFIBM_ERR_CAPACITY;
+    std::memcpy(buf, text.data(), text.size());
+    buf[text.size()] = 0;
+    return SDFIBM_OK;
+}
+
+}  // namespace
+
+extern "C" void sdfibm_host_euler_from_quat(const double* quat_wxyz, double* euler_rad) {
+    euler_xyz(quat_wxyz, euler_rad);
+}
+
+extern "C" int sdfibm_host_format_state(double time, int32_t twod, const sdfibm_solid_state* st, int32_t n, char* buf,
+                                        int64_t cap, int64_t* len) {
+    if (n < 0 || (n > 0 && !st) || !len) return SDFIBM_ERR_ARG;
+    std::string out;
+    out.reserve((size_t)n * (twod ? 140 : 260));
+    for (int32_t i = 0; i < n; ++i) {
+        const sdfibm_solid_state& s = st[i];
+        double e[3];
+        euler_xyz(s.quat, e);
+        put_sci(out, time);
+        out += ' ';
+        if (twod) {
+            const double v[9] = {s.pos[0], s.pos[1], s.vel[0], s.vel[1], s.force[0], s.force[1], e[2], s.omega[2],
+                                 s.torque[2]};
+            for (int k = 0; k < 9; ++k) {
+                put_sci(out, v[k]);
+                out += k < 8 ? ' ' : '\n';
+            }
+        } else {
+            const double* g[6] = {s.pos, s.vel, s.force, e, s.omega, s.torque};
+            for (int k = 0; k < 18; ++k) {
+                put_sci(out, g[k / 3][k % 3]);
+                out += k < 17 ? ' ' : '\n';
+            }
+        }
+    }
+    return emit(out, buf, cap, len);
+}
+
+extern "C" int sdfibm_host_write_restart(const char* dict_text, const sdfibm_solid_state* st, int32_t n, int32_t twod,
+                                         int32_t precision, const char* stamp, char* buf, int64_t cap, int64_t* len,
+                                         char* msg, int32_t msg_len) {
+    auto err = [&](const std::string& m, int code) {
+        if (msg && msg_len > 0) {
+            std::strncpy(msg, m.c_str(), msg_len - 1);
+            msg[msg_len - 1] = 0;
+        }
+        return code;
+    };
+    if (!dict_text || (n > 0 && !st) || n < 0 || !len || precision < 0 || precision > 17)
+        return err("bad argument", SDFIBM_ERR_ARG);
+    std::string out;
+    try {
+        const std::string src(dict_text);
+        Lexer lx(src);
+        auto root = parse_dict(lx, true);
+        Node* solids = nullptr;
+        for (auto& e : root->entries)
+            if (e.first == "solids" && e.second->is_dict) solids = e.second.get();
+        if (!solids) throw std::runtime_error("missing sub-dictionary solids");
+        if ((int32_t)solids->entries.size() != n)
+            throw std::runtime_error("solids holds " + std::to_string(solids->entries.size()) + " entries, " +
+                                     std::to_string(n) + " states given");
+        const int prec = precision ? precision : 6;
+        for (int32_t i = 0; i < n; ++i) {
+            Node& d = *solids->entries[i].second;
+            if (!d.is_dict) throw std::runtime_error("solids entry " + solids->entries[i].first + " is not a dictionary");
+            const sdfibm_solid_state& s = st[i];
+            double pos[3] = {s.pos[0], s.pos[1], s.pos[2]}, vel[3] = {s.vel[0], s.vel[1], s.vel[2]};
+            double om[3] = {s.omega[0], s.omega[1], s.omega[2]}, e[3];
+            if (twod) pos[2] = vel[2] = om[0] = om[1] = 0.0;
+            euler_xyz(s.quat, e);
+            for (int a = 0; a < 3; ++a) e[a] = e[a] * 180.0 / M_PI;
+            set_vector(d, "pos", pos, prec);
+            set_vector(d, "vel", vel, prec);
+            set_vector(d, "euler", e, prec);
+            set_vector(d, "omega", om, prec);
+        }
+        out = kRestartHeader;
+        write_dict(out, *root, 0, prec);
+        char tb[80] = {0};
+        if (!stamp) {
+            std::time_t t = std::time(nullptr);
+            std::tm tmv;
+            localtime_r(&t, &tmv);
+            std::strftime(tb, sizeof(tb), "%y/%m/%d %X", &tmv);
+            stamp = tb;
+        }
+        out += "\n// ";
+        out += stamp;
+        out += "\n";
+    } catch (const std::exception& e) {
+        return err(e.what(), SDFIBM_ERR_ARG);
+    }
+    const int rc = emit(out, buf, cap, len);
+    if (rc != SDFIBM_OK) return err("buffer too small", rc);
     return SDFIBM_OK;
 }

@@ -4,6 +4,8 @@ libsdfibm_cuda.so (include/sdfibm_host.h).  Mirrors the reference's object model
     make_shape("Sphere", radius=0.01)                ShapeFactory / IShape constructors
     make_solid(i, shape, rho, pos, euler_deg, ...)   Solid + IMaterial (Solid::setMaterial, setOrientation)
     parse_soliddict(text, rho_f)                     SolidCloud::initFromDictionary
+    format_state(time, states, twod), StateFile      SolidCloud::saveState (cloud.out)
+    write_restart(dict_text, states, twod)           SolidCloud::saveRestart (restart solidDict)
 """
 import ctypes as C
 
@@ -112,3 +114,71 @@ def parse_soliddict(text, rho_f=1.0, capacity=1 << 20):
     if rc != abi.OK:
         raise HostError(msg.value.decode())
     return list(arr)[:n.value], opt, tw.value
+
+
+def euler_from_quat(quat_wxyz):
+    """quaternion::eulerAngles(quaternion::XYZ): radians (a, b, c) with q = qx(a) qy(b) qz(c)."""
+    q = np.ascontiguousarray(quat_wxyz, dtype=np.float64)
+    e = np.zeros(3)
+    load().sdfibm_host_euler_from_quat(_p(q), _p(e))
+    return e
+
+
+def _state_array(states):
+    return (abi.SolidState * max(1, len(states)))(*states)
+
+
+def _text(call):
+    """Runs a text-producing entry point twice: once to measure, once into a buffer of that size."""
+    n = C.c_int64(0)
+    rc = call(None, 0, C.byref(n))
+    if rc != abi.OK:
+        return rc, None
+    buf = C.create_string_buffer(n.value + 1)
+    rc = call(buf, n.value + 1, C.byref(n))
+    return rc, buf.raw[:n.value].decode()
+
+
+def format_state(time, states, twod):
+    """The cloud.out records of one SolidCloud::saveState (src/solidcloud.cpp:595-614): a line per solid."""
+    arr = _state_array(states)
+    rc, text = _text(lambda b, cap, n: load().sdfibm_host_format_state(float(time), int(bool(twod)), arr,
+                                                                         len(states), b, cap, n))
+    if rc != abi.OK:
+        raise HostError("format_state failed (status %d)" % rc)
+    return text
+
+
+def write_restart(dict_text, states, twod, precision=6, stamp=None):
+    """SolidCloud::saveRestart (src/solidcloud.cpp:616-665): the solidDict text updated to the solids' states."""
+    arr = _state_array(states)
+    msg = C.create_string_buffer(512)
+    st = stamp.encode() if stamp is not None else None
+    rc, text = _text(lambda b, cap, n: load().sdfibm_host_write_restart(
+        dict_text.encode(), arr, len(states), int(bool(twod)), int(precision), st, b, cap, n, msg, 512))
+    if rc != abi.OK:
+        raise HostError(msg.value.decode() or "write_restart failed (status %d)" % rc)
+    return text
+
+
+class StateFile:
+    """cloud.out as SolidCloud keeps it: opened (truncated) at construction (src/solidcloud.cpp:234-236), and every
+    saveState call (src/solidcloud.cpp:578-593) appends one block of records when its call counter is a multiple of
+    meta.writeFrequency (default 1), then flushes."""
+
+    def __init__(self, path="cloud.out", twod=False, write_frequency=1):
+        if int(write_frequency) < 1:
+            raise HostError("writeFrequency must be positive")
+        self.f = open(path, "w")
+        self.twod = bool(twod)
+        self.write_frequency = int(write_frequency)
+        self.counter = 0
+
+    def save(self, time, states):
+        if self.counter % self.write_frequency == 0:
+            self.f.write(format_state(time, states, self.twod))
+            self.f.flush()
+        self.counter += 1
+
+    def close(self):
+        self.f.close()
