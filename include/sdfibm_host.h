@@ -7,6 +7,7 @@
  *   IMaterial (General) + Solid::setMaterial   src/solidcloud.cpp:127-143, src/solid.h:95-103
  *   Solid::setOrientation (euler degrees)      src/solidcloud.cpp:176-177, src/solid.h:76-80
  *   SolidCloud::initFromDictionary             src/solidcloud.cpp:14-206
+ * and its output path: SolidCloud::saveState (cloud.out) and SolidCloud::saveRestart (src/solidcloud.cpp:578-665).
  * Every function returns an sdfibm_status; messages go to the caller-provided buffer (never to stdout/exit).
  */
 #ifndef SDFIBM_HOST_H
@@ -42,6 +43,12 @@ int sdfibm_host_make_solid(int32_t id, const sdfibm_shape_desc* shape, double rh
  * (0 is used when on_fluid is off).  msg (may be NULL) receives an error text. */
 int sdfibm_host_parse_soliddict(const char* text, double rho_f, sdfibm_solid_desc* solids, int32_t capacity,
                                 int32_t* nsolids, sdfibm_options* opt, int32_t* on_twod, char* msg, int32_t msg_len);
+
+/* One entry of a solidDict by its '/'-separated path (e.g. "meta/writeFrequency", the reference's
+ * meta.lookupOrDefault at src/solidcloud.cpp:37): its value tokens joined by single spaces, quotes removed, into buf as
+ * the output functions below write text.  *len = -1 when the entry is absent (the caller's default applies); a path
+ * that names a sub-dictionary, or text that does not parse, returns SDFIBM_ERR_ARG. */
+int sdfibm_host_soliddict_lookup(const char* text, const char* path, char* buf, int64_t cap, int64_t* len);
 
 /* ---- output: the state file and the restart dictionary --------------------------------------------------------------
  * Text results go to buf: at most cap bytes including the terminating NUL; *len receives the length of the whole

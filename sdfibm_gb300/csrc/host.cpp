@@ -742,3 +742,36 @@ extern "C" int sdfibm_host_write_restart(const char* dict_text, const sdfibm_sol
     if (rc != SDFIBM_OK) return err("buffer too small", rc);
     return SDFIBM_OK;
 }
+
+extern "C" int sdfibm_host_soliddict_lookup(const char* text, const char* path, char* buf, int64_t cap, int64_t* len) {
+    if (!text || !path || !len) return SDFIBM_ERR_ARG;
+    try {
+        const std::string src(text);
+        Lexer lx(src);
+        auto root = parse_dict(lx, true);
+        const Node* n = root.get();
+        std::string p(path);
+        size_t b = 0;
+        for (;;) {
+            const size_t e = p.find('/', b);
+            const std::string key = p.substr(b, e == std::string::npos ? std::string::npos : e - b);
+            if (!n->is_dict) return SDFIBM_ERR_ARG;
+            n = n->find(key);
+            if (!n) {
+                *len = -1;
+                return SDFIBM_OK;
+            }
+            if (e == std::string::npos) break;
+            b = e + 1;
+        }
+        if (n->is_dict) return SDFIBM_ERR_ARG;
+        std::string out;
+        for (size_t i = 0; i < n->tokens.size(); ++i) {
+            if (i) out += ' ';
+            out += n->tokens[i];
+        }
+        return emit(out, buf, cap, len);
+    } catch (const std::exception&) {
+        return SDFIBM_ERR_ARG;
+    }
+}

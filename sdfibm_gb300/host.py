@@ -6,6 +6,7 @@ libsdfibm_cuda.so (include/sdfibm_host.h).  Mirrors the reference's object model
     parse_soliddict(text, rho_f)                     SolidCloud::initFromDictionary
     format_state(time, states, twod), StateFile      SolidCloud::saveState (cloud.out)
     write_restart(dict_text, states, twod)           SolidCloud::saveRestart (restart solidDict)
+    soliddict_lookup(text, "meta/writeFrequency")    dictionary::lookupOrDefault
 """
 import ctypes as C
 
@@ -159,6 +160,20 @@ def write_restart(dict_text, states, twod, precision=6, stamp=None):
     if rc != abi.OK:
         raise HostError(msg.value.decode() or "write_restart failed (status %d)" % rc)
     return text
+
+
+def soliddict_lookup(text, path, default=None):
+    """The value of one solidDict entry ("meta/writeFrequency"), as text; default when the entry is absent."""
+    L = load()
+    n = C.c_int64(0)
+    if L.sdfibm_host_soliddict_lookup(text.encode(), path.encode(), None, 0, C.byref(n)) != abi.OK:
+        raise HostError("cannot look up %s" % path)
+    if n.value < 0:
+        return default
+    buf = C.create_string_buffer(n.value + 1)
+    if L.sdfibm_host_soliddict_lookup(text.encode(), path.encode(), buf, n.value + 1, C.byref(n)) != abi.OK:
+        raise HostError("cannot look up %s" % path)
+    return buf.raw[:n.value].decode()
 
 
 class StateFile:

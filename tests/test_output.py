@@ -217,3 +217,16 @@ def test_restart_of_a_real_cloud_description(cuda_lib):
     text = write_restart(src, [st], False, precision=17)
     e = re.search(r"euler +\( ([^)]*) \)", text).group(1).split()
     assert np.allclose([float(v) for v in e], (15, -30, 45), atol=1e-12)
+
+
+def test_soliddict_lookup(cuda_lib):
+    from sdfibm_gb300.host import soliddict_lookup
+    assert soliddict_lookup(DICT_3D, "meta/writeFrequency") == "2"
+    assert soliddict_lookup(DICT_3D, "meta/gravity") == "( 0.0 -9.81 0.0 )"
+    assert soliddict_lookup(DICT_3D, "solids/b/note") == "kept as written"
+    assert soliddict_lookup(DICT_3D, "meta/sampler", "none") == "none"
+    assert soliddict_lookup(DICT_3D, "nothing/here") is None
+    with pytest.raises(HostError):
+        soliddict_lookup(DICT_3D, "meta")
+    with pytest.raises(HostError):
+        soliddict_lookup("meta { on_fluid 1;", "meta/on_fluid")
