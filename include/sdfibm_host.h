@@ -68,6 +68,12 @@ void sdfibm_host_euler_from_quat(const double* quat_wxyz, double* euler_rad);
 int sdfibm_host_format_state(double time, int32_t twod, const sdfibm_solid_state* states, int32_t n, char* buf,
                              int64_t cap, int64_t* len);
 
+/* The line one SolidCloud::writeMeanField appends to meanfield.out (src/solidcloud.cpp:303-313): the mean field of
+ * every solid (mean3[3*i .. 3*i+2]) as std::scientific with 6 digits, each number followed by a space, then a newline.
+ * The means themselves come from the coupling (sdfibm_gb300.cloud.SolidCloud.mean_field: two forcing passes of the
+ * sampler-shaped solids at rest). */
+int sdfibm_host_format_mean_field(const double* mean3, int32_t n, char* buf, int64_t cap, int64_t* len);
+
 /* SolidCloud::saveRestart (src/solidcloud.cpp:616-665): the solidDict text with pos, vel, euler (degrees) and omega
  * of the i-th entry of its `solids` sub-dictionary set from states[i] (2-D: pos.z, vel.z, omega.x and omega.y
  * written as 0), the tree written in OpenFOAM's dictionary layout with `precision` significant digits (the case's

@@ -5,6 +5,7 @@
 // It follows the reference line by line:
 //   SolidCloud::interact / solidFluidInteract / checkAlpha / fixInternal / evolve / addMidEnvironment /
 //   solidSolidInteract / solidSolidCollision   src/solidcloud.cpp:288-301, 361-433, 435-464, 466-570
+//   SolidCloud::calcMeanField                   src/solidcloud.cpp:315-359
 //   CellEnumerator                              src/cellenumerator.cpp:6-78, src/cellenumerator.h:41-52
 //   GeometricTools                              src/geometrictools.cpp:6-116
 //   Solid                                       src/solid.h:109-202
@@ -132,6 +133,7 @@ struct CloudBase {
     virtual int64_t nCells() const = 0;
     virtual void cellCentre(int64_t c, double* out) const = 0;
     virtual double cellFraction(int s, int64_t c, int method) = 0;
+    virtual int meanField(const sdfibm_shape_desc& sampler, const double* U, int32_t* Ct, double* out) = 0;
 
     std::vector<Solid> solids;
     sdfibm_options opt{};
@@ -417,12 +419,14 @@ struct Cloud : CloudBase {
     // conservative cell-index box of the cells that can hold an inside vertex (fast mode); false = whole mesh
     bool bboxCells(const Solid& s, int64_t lo[3], int64_t hi[3]) const;
 
-    // CellEnumerator: returns the three sorted sets
+    // CellEnumerator: returns the three sorted sets; order (optional) receives the touched cells with their types in
+    // the enumerator's queue order (CellEnumerator::Next / GetCurCellInd, cellenumerator.h:41-60)
     void enumerate(const Solid& s, std::vector<int64_t>& inside, std::vector<int64_t>& cin,
-                   std::vector<int64_t>& cout) const {
+                   std::vector<int64_t>& cout, std::vector<std::pair<int64_t, int8_t>>* order = nullptr) const {
         auto pred = [&](const V3& v) { return s.phi01(v); };
         int64_t seed = findNearestCell(s.center);
         inside.clear(); cin.clear(); cout.clear();
+        if (order) order->clear();
         if (faithful) {
             std::function<bool(const V3&)> fpred = pred;
             std::vector<int> m_ct(mesh.nCells(), UNVISITED);  // cellenumerator.cpp:49
@@ -444,6 +448,7 @@ struct Cloud : CloudBase {
             }
             while (!q.empty()) {
                 int64_t icur = q.front();
+                if (order) order->emplace_back(icur, (int8_t)m_ct[icur]);
                 int64_t nb[6];
                 int nn = cellCellsOf(icur, nb);
                 int64_t tmp[8];
@@ -513,6 +518,7 @@ struct Cloud : CloudBase {
         }
         for (int64_t c : q) {
             int8_t t = ct[c];
+            if (order) order->emplace_back(c, t);
             if (t == ALL_INSIDE) inside.push_back(c); else if (t == CENTER_INSIDE) cin.push_back(c); else cout.push_back(c);
         }
         std::sort(inside.begin(), inside.end());
@@ -655,6 +661,41 @@ struct Cloud : CloudBase {
                 put3(FT + 6 * si, solids[si].fluid_force);
                 put3(FT + 6 * si + 3, solids[si].fluid_torque);
             }
+        }
+        return 0;
+    }
+
+    // SolidCloud::calcMeanField<vector> for every solid (solidcloud.cpp:303-359): a copy of the solid with the sampler
+    // shape (Solid::setShape keeps the pose), its cells in the enumerator's queue order, alpha = 1 inside and the
+    // REF-GEO fraction on cut cells, mean = sum(alpha V U) / sum(alpha V).  Like the reference it writes Ct for every
+    // cell it visits (id + 4 inside, the cell type otherwise); Ct may be NULL.
+    int meanField(const sdfibm_shape_desc& sampler, const double* U, int32_t* Ct, double* out) override {
+        const int64_t N = mesh.nCells();
+        std::vector<int64_t> ins, cin, cout;
+        std::vector<std::pair<int64_t, int8_t>> order;
+        for (size_t si = 0; si < solids.size(); ++si) {
+            Solid tmp = solids[si];
+            tmp.d.shape = sampler;
+            Geo geo(*this);
+            V3 mean{0, 0, 0};
+            double volume = 0.0;
+            enumerate(tmp, ins, cin, cout, &order);
+            const int insideType = tmp.id + 4;
+            for (auto& ct : order) {
+                const int64_t c = ct.first;
+                double alpha;
+                if (ct.second == ALL_INSIDE) {
+                    alpha = 1.0;
+                    if (Ct) Ct[c] = insideType;
+                } else {
+                    if (Ct) Ct[c] = ct.second;
+                    alpha = geo.cellVolume(c, tmp, twod != 0) / vol(c);
+                }
+                const double dV = alpha * vol(c);
+                volume += dV;
+                mean += dV * V3{U[c], U[N + c], U[2 * N + c]};
+            }
+            put3(out + 3 * si, V3{mean.x / volume, mean.y / volume, mean.z / volume});
         }
         return 0;
     }
@@ -897,6 +938,9 @@ int oracle_interact_threads(void* h, double dt, const double* U, double* As, dou
 }
 int64_t oracle_last_pairs(void* h) { return static_cast<CloudBase*>(h)->last_pairs; }
 
+int oracle_mean_field(void* h, const sdfibm_shape_desc* sampler, const double* U, int32_t* Ct, double* out) {
+    return static_cast<CloudBase*>(h)->meanField(*sampler, U, Ct, out);
+}
 int64_t oracle_touched(void* h, int s, int64_t* cells, int8_t* types, int64_t cap) {
     return static_cast<CloudBase*>(h)->touched(s, cells, types, cap);
 }

@@ -63,6 +63,7 @@ def lib():
         L.oracle_interact_threads.argtypes = [vp, C.c_double] + [vp] * 6 + [C.c_int]
         L.oracle_sample_cell.restype = C.c_int64
         L.oracle_sample_cell.argtypes = [C.POINTER(abi.ShapeDesc), vp, vp, C.c_double, C.c_int, vp]
+        L.oracle_mean_field.argtypes = [vp, C.POINTER(abi.ShapeDesc), vp, vp, vp]
         _lib = L
     return _lib
 
@@ -181,6 +182,16 @@ class OracleCloud:
 
     def set_state(self, st):
         lib().oracle_set_state(self.h, st, self.nsolids)
+
+    def mean_field(self, sampler, U, Ct=None):
+        """SolidCloud::calcMeanField of U for every solid with the sampler shape: (S, 3).  Ct (int32, updated in
+        place) receives the reference's writes for the visited cells."""
+        U = np.ascontiguousarray(U, dtype=np.float64).reshape(-1)
+        out = np.zeros(3 * max(1, self.nsolids))
+        if Ct is not None:
+            assert Ct.dtype == np.int32 and Ct.flags.c_contiguous
+        lib().oracle_mean_field(self.h, C.byref(sampler), _p(U), _p(Ct) if Ct is not None else None, _p(out))
+        return out[:3 * self.nsolids].reshape(self.nsolids, 3)
 
     def cell_fraction(self, s, c, method):
         return lib().oracle_cell_fraction(self.h, s, c, method)

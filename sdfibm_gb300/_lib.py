@@ -26,6 +26,7 @@ HOST_SYMBOLS = [
     "sdfibm_host_make_shape", "sdfibm_host_make_motion", "sdfibm_host_make_forcer", "sdfibm_host_quat_from_euler_deg",
     "sdfibm_host_make_solid", "sdfibm_host_parse_soliddict", "sdfibm_host_euler_from_quat",
     "sdfibm_host_format_state", "sdfibm_host_write_restart", "sdfibm_host_soliddict_lookup",
+    "sdfibm_host_format_mean_field",
 ]
 
 
@@ -84,5 +85,6 @@ def load():
     L.sdfibm_host_write_restart.argtypes = [C.c_char_p, P(abi.SolidState), i32, i32, i32, C.c_char_p, C.c_char_p,
                                             i64, P(i64), C.c_char_p, i32]
     L.sdfibm_host_soliddict_lookup.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, i64, P(i64)]
+    L.sdfibm_host_format_mean_field.argtypes = [vp, i32, C.c_char_p, i64, P(i64)]
     _lib = L
     return L

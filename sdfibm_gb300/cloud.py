@@ -5,7 +5,8 @@
     cloud.evolve(t, dt)                                # SolidCloud::evolve
     cloud.fix_internal(fields["Ct"], U)                # SolidCloud::fixInternal
     cloud.states() / cloud.set_states(st)              # Solid getters / setters
-    cloud.save_state(state_file)                       # SolidCloud::saveState   (state_file: host.StateFile)
+    cloud.save_state(state_file, U, Ct)                # SolidCloud::saveState   (state_file: host.StateFile)
+    cloud.set_sampler(shape); cloud.mean_field(U, Ct)  # meta.sampler, SolidCloud::calcMeanField
     cloud.save_restart(dict_text, path)                # SolidCloud::saveRestart
 
 Fields are CUDA tensors in the cell-major layout of include/sdfibm_cuda.h: U and Fs have shape (3, N) float32,
@@ -36,6 +37,9 @@ class SolidCloud:
         self._L = load()
         self.mesh = mesh
         self.time = float(time)  # m_time: the construction time, then the time of the last evolve
+        self._stream = stream
+        self._sampler = None     # (shape, SolidCloud of the solids with that shape) for mean_field
+        self._sampler_fields = None
         self.nsolids = len(solids)
         self.ncells = int(mesh.nx) * int(mesh.ny) * int(mesh.nz)
         self._solids = (abi.SolidDesc * max(1, len(solids)))(*solids)
@@ -52,6 +56,10 @@ class SolidCloud:
             raise CouplingError(rc, self._L.sdfibm_cuda_last_error(self._h).decode())
 
     def close(self):
+        if getattr(self, "_sampler", None) is not None:
+            self._sampler[1].close()
+            self._sampler = None
+            self._sampler_fields = None
         if getattr(self, "_h", None) and self._h.value:
             self._L.sdfibm_cuda_destroy(self._h)
             self._h = C.c_void_p()
@@ -105,9 +113,58 @@ class SolidCloud:
         arr = (abi.SolidState * max(1, self.nsolids))(*states)
         self._check(self._L.sdfibm_cuda_set_solids(self._h, arr, self.nsolids))
 
-    def save_state(self, state_file):
-        """SolidCloud::saveState: appends this step's records to a host.StateFile (cloud.out)."""
-        state_file.save(self.time, self.states())
+    def set_sampler(self, shape):
+        """meta.sampler: the shape (a host.make_shape descriptor) that mean_field puts on every solid."""
+        if self._sampler is not None:
+            self._sampler[1].close()
+            self._sampler_fields = None
+        solids = []
+        for d in self._solids[:self.nsolids]:
+            e = abi.SolidDesc.from_buffer_copy(d)
+            e.shape = shape
+            solids.append(e)
+        # at rest, rho_f = 1, FP64 forcing, the reference's REF-GEO fraction (calcMeanField calls calcCellVolume)
+        opt = abi.options(rho_f=1.0, fraction_method=abi.FRACTION_REFGEO, exact_forcing=1)
+        self._sampler = (shape, SolidCloud(self.mesh, solids, opt, stream=self._stream))
+
+    def mean_field(self, U, Ct=None):
+        """SolidCloud::calcMeanField (src/solidcloud.cpp:315-359) of U for every solid, with the sampler shape in
+        the solid's pose: sum(alpha V U) / sum(alpha V) over the cells the sampler touches, alpha the REF-GEO fraction
+        (1 inside).  Returns (S, 3) float64.
+
+        Computed by the coupling itself: the sampler-shaped solids at rest, with rho_f = 1 and dt = 1, receive the
+        force sum(alpha V (U - 0)); a second pass on U = 1 gives sum(alpha V).  Like the reference (writeMeanField
+        runs before fixInternal), Ct, when given, is overwritten on every cell a sampler touches: id + 4 inside, the
+        cell type on cut cells."""
+        if self._sampler is None:
+            raise CouplingError(5, "mean_field needs a sampler shape (set_sampler)")
+        import torch
+        sc = self._sampler[1]
+        st = self.states()
+        for x in st:
+            for a in range(3):
+                x.vel[a] = 0.0
+                x.omega[a] = 0.0
+        sc.set_states(st)
+        if self._sampler_fields is None or self._sampler_fields["As"].device != U.device:
+            self._sampler_fields = sc.new_fields(device=U.device)
+        f = self._sampler_fields
+        F = sc.interact(self.time, 1.0, U, f)
+        W = sc.interact(self.time, 1.0, torch.ones_like(U), f)
+        if Ct is not None:
+            sct = f["Ct"]
+            Ct.copy_(torch.where(sct != 0, sct, Ct))
+        return F[:, :3] / W[:, :1]
+
+    def save_state(self, state_file, U=None, Ct=None):
+        """SolidCloud::saveState: appends this step's records to a host.StateFile (cloud.out) and, when the file
+        keeps the mean field and a sampler is set, the mean of U around every solid (meanfield.out)."""
+        mf = None
+        if state_file.keeps_mean_field and self._sampler is not None:
+            if U is None:
+                raise CouplingError(1, "the mean field needs U")
+            mf = self.mean_field(U, Ct)
+        state_file.save(self.time, self.states(), mf)
 
     def save_restart(self, dict_text, path, precision=6, stamp=None):
         """SolidCloud::saveRestart: writes the solidDict read at construction (dict_text) with every solid's pos,

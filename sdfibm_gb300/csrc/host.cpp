@@ -775,3 +775,16 @@ extern "C" int sdfibm_host_soliddict_lookup(const char* text, const char* path, 
         return SDFIBM_ERR_ARG;
     }
 }
+
+// SolidCloud::writeMeanField (src/solidcloud.cpp:303-313) on a stream set to std::scientific (:31-33)
+extern "C" int sdfibm_host_format_mean_field(const double* mean3, int32_t n, char* buf, int64_t cap, int64_t* len) {
+    if (n < 0 || (n > 0 && !mean3) || !len) return SDFIBM_ERR_ARG;
+    std::string out;
+    out.reserve((size_t)n * 42 + 1);
+    for (int64_t i = 0; i < 3 * (int64_t)n; ++i) {
+        put_sci(out, mean3[i]);
+        out += ' ';
+    }
+    out += '\n';
+    return emit(out, buf, cap, len);
+}

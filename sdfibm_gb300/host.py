@@ -4,7 +4,8 @@ libsdfibm_cuda.so (include/sdfibm_host.h).  Mirrors the reference's object model
     make_shape("Sphere", radius=0.01)                ShapeFactory / IShape constructors
     make_solid(i, shape, rho, pos, euler_deg, ...)   Solid + IMaterial (Solid::setMaterial, setOrientation)
     parse_soliddict(text, rho_f)                     SolidCloud::initFromDictionary
-    format_state(time, states, twod), StateFile      SolidCloud::saveState (cloud.out)
+    format_state(time, states, twod), StateFile      SolidCloud::saveState (cloud.out, meanfield.out)
+    format_mean_field(means)                         SolidCloud::writeMeanField
     write_restart(dict_text, states, twod)           SolidCloud::saveRestart (restart solidDict)
     soliddict_lookup(text, "meta/writeFrequency")    dictionary::lookupOrDefault
 """
@@ -150,6 +151,15 @@ def format_state(time, states, twod):
     return text
 
 
+def format_mean_field(means):
+    """The meanfield.out line of one SolidCloud::writeMeanField (src/solidcloud.cpp:303-313)."""
+    m = np.ascontiguousarray(means, dtype=np.float64).reshape(-1, 3)
+    rc, text = _text(lambda b, cap, n: load().sdfibm_host_format_mean_field(_p(m), len(m), b, cap, n))
+    if rc != abi.OK:
+        raise HostError("format_mean_field failed (status %d)" % rc)
+    return text
+
+
 def write_restart(dict_text, states, twod, precision=6, stamp=None):
     """SolidCloud::saveRestart (src/solidcloud.cpp:616-665): the solidDict text updated to the solids' states."""
     arr = _state_array(states)
@@ -177,23 +187,34 @@ def soliddict_lookup(text, path, default=None):
 
 
 class StateFile:
-    """cloud.out as SolidCloud keeps it: opened (truncated) at construction (src/solidcloud.cpp:234-236), and every
-    saveState call (src/solidcloud.cpp:578-593) appends one block of records when its call counter is a multiple of
-    meta.writeFrequency (default 1), then flushes."""
+    """cloud.out (and meanfield.out) as SolidCloud keeps them: opened (truncated) at construction
+    (src/solidcloud.cpp:29-33, 234-236); every saveState call (src/solidcloud.cpp:578-593) appends one block of records
+    when its call counter is a multiple of meta.writeFrequency (default 1), and a mean-field line on every call when
+    meta.on_meanfield is present (mean_field_path), then flushes."""
 
-    def __init__(self, path="cloud.out", twod=False, write_frequency=1):
+    def __init__(self, path="cloud.out", twod=False, write_frequency=1, mean_field_path=None):
         if int(write_frequency) < 1:
             raise HostError("writeFrequency must be positive")
         self.f = open(path, "w")
+        self.mf = open(mean_field_path, "w") if mean_field_path else None
         self.twod = bool(twod)
         self.write_frequency = int(write_frequency)
         self.counter = 0
 
-    def save(self, time, states):
+    @property
+    def keeps_mean_field(self):
+        return self.mf is not None
+
+    def save(self, time, states, mean_field=None):
         if self.counter % self.write_frequency == 0:
             self.f.write(format_state(time, states, self.twod))
             self.f.flush()
+        if self.mf is not None and mean_field is not None:
+            self.mf.write(format_mean_field(mean_field))
+            self.mf.flush()
         self.counter += 1
 
     def close(self):
         self.f.close()
+        if self.mf is not None:
+            self.mf.close()
