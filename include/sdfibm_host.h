@@ -84,6 +84,31 @@ int sdfibm_host_write_restart(const char* dict_text, const sdfibm_solid_state* s
                               int32_t precision, const char* stamp, char* buf, int64_t cap, int64_t* len, char* msg,
                               int32_t msg_len);
 
+/* ---- the VOF initializer (tool_vof): a smooth phase field from the solids' fractions ------------------------------
+ * The field itself is one coupling pass: sdfibm_cuda_interact of these solids (REF-GEO fraction) leaves
+ * As = min(sum of fractions, 1), the value tool_vof's SolidCloud::writeVOF accumulates with its clamp after every
+ * solid (tool_vof/solidcloud.cpp:117-173). */
+
+/* tool_vof's solidDict (tool_vof/solidcloud.cpp:12-112): meta.on_twod, the shapes library (a repeated name keeps the
+ * last), and a solid of density 1 at rest per entry of "solids" (pos, euler in degrees, shp_name; 2-D: pos.z must
+ * be 0), followed, when with_planes is set, by the entries of "planes" (as the shipped example's phase field
+ * includes them).  Writes up to capacity solids; *nsolids receives the count. */
+int sdfibm_host_parse_vofdict(const char* text, int32_t with_planes, sdfibm_solid_desc* solids, int32_t capacity,
+                              int32_t* nsolids, int32_t* on_twod, char* msg, int32_t msg_len);
+
+/* The uniform mesh of a blockMeshDict holding one axis-aligned hex block with simpleGrading (1 1 1): origin = the
+ * block's lowest vertex, h = extent / cells, convertToMeters (or scale) applied; twod = 1 when nz == 1. */
+int sdfibm_host_parse_blockmesh(const char* text, sdfibm_mesh_desc* mesh, char* msg, int32_t msg_len);
+
+/* An OpenFOAM volScalarField file (file_len bytes, ascii or binary per its FoamFile format) with its internalField
+ * replaced by `nonuniform List<scalar>` of the n values.  format: -1 keeps the file's, 0 ascii, 1 binary (the
+ * case's writeFormat; the header's format word follows); ascii values carry `precision` significant digits (the
+ * case's writePrecision; 0: 6).  Everything else in the file is kept byte for byte.  The result (binary fields hold
+ * NUL bytes) goes to buf as the text functions above write it. */
+int sdfibm_host_write_scalar_field(const char* file, int64_t file_len, const double* values, int64_t n,
+                                   int32_t format, int32_t precision, char* buf, int64_t cap, int64_t* len, char* msg,
+                                   int32_t msg_len);
+
 #ifdef __cplusplus
 }
 #endif

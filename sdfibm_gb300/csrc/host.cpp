@@ -360,6 +360,44 @@ bool bool_of(const Node& d, const std::string& k) {
     throw std::runtime_error("bad bool " + k);
 }
 
+// The shapes library of a solidDict: one ShapeFactory::create per entry of "shapes".  keep_first: the coupling's
+// EntityLibrary::emplace keeps the first of duplicate names (src/solidcloud.cpp:66, src/entitylibrary.h:22); the
+// VOF initializer assigns, keeping the last (tool_vof/solidcloud.cpp:57-60).
+std::map<std::string, sdfibm_shape_desc> parse_shapes(const Node& shapes_dict, bool keep_first) {
+    static const std::map<std::string, int> shape_ids = {
+        {"Circle", SDFIBM_SHAPE_CIRCLE}, {"Sphere", SDFIBM_SHAPE_SPHERE}, {"Ellipse", SDFIBM_SHAPE_ELLIPSE},
+        {"Ellipsoid", SDFIBM_SHAPE_ELLIPSOID}, {"Rectangle", SDFIBM_SHAPE_RECTANGLE}, {"Box", SDFIBM_SHAPE_BOX},
+        {"Plane", SDFIBM_SHAPE_PLANE}, {"Circle_Tail", SDFIBM_SHAPE_CIRCLE_TAIL},
+        {"Circle_TwoTail", SDFIBM_SHAPE_CIRCLE_TWOTAIL}};
+    std::map<std::string, sdfibm_shape_desc> shapes;
+    for (auto& e : shapes_dict.entries) {
+        const Node& sd = *e.second;
+        const std::string type = word_of(sd, "type"), name = word_of(sd, "name");
+        auto it = shape_ids.find(type);
+        if (it == shape_ids.end()) throw std::runtime_error("Cannot create unrecognized object: " + type);
+        double raw[8] = {0}, com[3] = {0, 0, 0};
+        switch (it->second) {
+            case SDFIBM_SHAPE_CIRCLE: case SDFIBM_SHAPE_SPHERE: raw[0] = scalar_of(sd, "radius"); break;
+            case SDFIBM_SHAPE_ELLIPSE: case SDFIBM_SHAPE_RECTANGLE:
+                raw[0] = scalar_of(sd, "radiusa"); raw[1] = scalar_of(sd, "radiusb"); break;
+            case SDFIBM_SHAPE_ELLIPSOID: case SDFIBM_SHAPE_BOX:
+                raw[0] = scalar_of(sd, "radiusa"); raw[1] = scalar_of(sd, "radiusb"); raw[2] = scalar_of(sd, "radiusc");
+                break;
+            case SDFIBM_SHAPE_CIRCLE_TAIL: case SDFIBM_SHAPE_CIRCLE_TWOTAIL:
+                raw[0] = scalar_of(sd, "radius"); raw[1] = scalar_of(sd, "ratio"); raw[2] = scalar_of(sd, "thickness");
+                break;
+            default: break;
+        }
+        vector_of(sd, "com", com);
+        sdfibm_shape_desc s;
+        if (sdfibm_host_make_shape(it->second, raw, com, &s) != SDFIBM_OK)
+            throw std::runtime_error("bad parameters for shape " + name);
+        if (keep_first) shapes.emplace(name, s);
+        else shapes[name] = s;
+    }
+    return shapes;
+}
+
 }  // namespace
 
 extern "C" int sdfibm_host_parse_soliddict(const char* text, double rho_f, sdfibm_solid_desc* solids, int32_t capacity,
@@ -387,36 +425,7 @@ extern "C" int sdfibm_host_parse_soliddict(const char* text, double rho_f, sdfib
         opt->rho_f = on_fluid ? rho_f : 0.0;
         if (on_twod) *on_twod = twod ? 1 : 0;
 
-        static const std::map<std::string, int> shape_ids = {
-            {"Circle", SDFIBM_SHAPE_CIRCLE}, {"Sphere", SDFIBM_SHAPE_SPHERE}, {"Ellipse", SDFIBM_SHAPE_ELLIPSE},
-            {"Ellipsoid", SDFIBM_SHAPE_ELLIPSOID}, {"Rectangle", SDFIBM_SHAPE_RECTANGLE}, {"Box", SDFIBM_SHAPE_BOX},
-            {"Plane", SDFIBM_SHAPE_PLANE}, {"Circle_Tail", SDFIBM_SHAPE_CIRCLE_TAIL},
-            {"Circle_TwoTail", SDFIBM_SHAPE_CIRCLE_TWOTAIL}};
-        std::map<std::string, sdfibm_shape_desc> shapes;
-        for (auto& e : root->sub("shapes").entries) {
-            const Node& sd = *e.second;
-            const std::string type = word_of(sd, "type"), name = word_of(sd, "name");
-            auto it = shape_ids.find(type);
-            if (it == shape_ids.end()) throw std::runtime_error("Cannot create unrecognized object: " + type);
-            double raw[8] = {0}, com[3] = {0, 0, 0};
-            switch (it->second) {
-                case SDFIBM_SHAPE_CIRCLE: case SDFIBM_SHAPE_SPHERE: raw[0] = scalar_of(sd, "radius"); break;
-                case SDFIBM_SHAPE_ELLIPSE: case SDFIBM_SHAPE_RECTANGLE:
-                    raw[0] = scalar_of(sd, "radiusa"); raw[1] = scalar_of(sd, "radiusb"); break;
-                case SDFIBM_SHAPE_ELLIPSOID: case SDFIBM_SHAPE_BOX:
-                    raw[0] = scalar_of(sd, "radiusa"); raw[1] = scalar_of(sd, "radiusb"); raw[2] = scalar_of(sd, "radiusc");
-                    break;
-                case SDFIBM_SHAPE_CIRCLE_TAIL: case SDFIBM_SHAPE_CIRCLE_TWOTAIL:
-                    raw[0] = scalar_of(sd, "radius"); raw[1] = scalar_of(sd, "ratio"); raw[2] = scalar_of(sd, "thickness");
-                    break;
-                default: break;
-            }
-            vector_of(sd, "com", com);
-            sdfibm_shape_desc s;
-            if (sdfibm_host_make_shape(it->second, raw, com, &s) != SDFIBM_OK)
-                throw std::runtime_error("bad parameters for shape " + name);
-            shapes[name] = s;  // EntityLibrary::emplace keeps the first of duplicate names
-        }
+        const std::map<std::string, sdfibm_shape_desc> shapes = parse_shapes(root->sub("shapes"), true);
         struct Fr { int type; double p[8]; };
         std::map<std::string, Fr> forcers;
         if (const Node* fd = root->find("forces")) {
@@ -787,4 +796,267 @@ extern "C" int sdfibm_host_format_mean_field(const double* mean3, int32_t n, cha
     }
     out += '\n';
     return emit(out, buf, cap, len);
+}
+
+// ---- VOF initializer front end (tool_vof) ------------------------------------------------------------------------------
+//   solidDict   tool_vof/solidcloud.cpp:12-112: meta.on_twod, the shapes library, material rho = 1, every "solids"
+//               entry as Solid(i, pos, identity) + euler + shape; the example's "planes" entries follow the solids
+//   blockMesh   a single uniform hex block (the mesh of the uniform-grid path)
+//   field file  the internalField of a volScalarField rewritten in the file's own format (ascii or binary), the rest
+//               of the file kept as it is (IOobject MUST_READ + field.write(), tool_vof/solidcloud.cpp:143-164)
+namespace {
+
+void read_vof_entries(const Node& list, const std::map<std::string, sdfibm_shape_desc>& shapes, bool twod,
+                      std::vector<sdfibm_solid_desc>& out) {
+    for (auto& e : list.entries) {
+        const Node& d = *e.second;
+        if (!d.is_dict) throw std::runtime_error("entry " + e.first + " is not a dictionary");
+        const int32_t i = (int32_t)out.size();
+        double pos[3], euler[3] = {0, 0, 0};
+        if (!vector_of(d, "pos", pos)) throw std::runtime_error("solid without pos");
+        if (twod && pos[2] != 0)
+            throw std::runtime_error("Solid must has z=0 in 2D simulation, violated by solid # " + std::to_string(i));
+        vector_of(d, "euler", euler);
+        const std::string shp = word_of(d, "shp_name");
+        auto si = shapes.find(shp);
+        if (si == shapes.end()) throw std::runtime_error("unknown shape name " + shp);
+        sdfibm_solid_desc s;
+        if (sdfibm_host_make_solid(i, &si->second, 1.0, SDFIBM_MOTION_FREE, nullptr, SDFIBM_FORCER_NONE, nullptr, pos,
+                                   euler, nullptr, nullptr, &s) != SDFIBM_OK)
+            throw std::runtime_error("bad solid " + std::to_string(i));
+        out.push_back(s);
+    }
+}
+
+int set_msg(char* msg, int32_t msg_len, const std::string& m, int code) {
+    if (msg && msg_len > 0) {
+        std::strncpy(msg, m.c_str(), msg_len - 1);
+        msg[msg_len - 1] = 0;
+    }
+    return code;
+}
+
+// the value tokens of a list entry of a dictionary that the solidDict grammar does not cover (blockMeshDict's
+// "boundary" holds sub-dictionaries inside a list): scan for `key` at brace depth 0 and collect to its ';'
+bool raw_entry(const std::string& src, const std::string& key, std::vector<std::string>& toks) {
+    Lexer lx(src);
+    std::string t;
+    int depth = 0;
+    while (lx.next(t)) {
+        if (t == "{") ++depth;
+        else if (t == "}") --depth;
+        else if (depth == 0 && t == key && !lx.quoted) {
+            toks.clear();
+            int par = 0;
+            while (lx.next(t)) {
+                if (t == "(") ++par;
+                if (t == ")") --par;
+                if (t == ";" && par == 0) return true;
+                toks.push_back(t);
+            }
+            throw std::runtime_error("unterminated entry " + key);
+        }
+    }
+    return false;
+}
+
+}  // namespace
+
+extern "C" int sdfibm_host_parse_vofdict(const char* text, int32_t with_planes, sdfibm_solid_desc* solids,
+                                         int32_t capacity, int32_t* nsolids, int32_t* on_twod, char* msg,
+                                         int32_t msg_len) {
+    if (!text || !nsolids) return set_msg(msg, msg_len, "null argument", SDFIBM_ERR_ARG);
+    try {
+        const std::string src(text);
+        Lexer lx(src);
+        auto root = parse_dict(lx, true);
+        const bool twod = bool_of(root->sub("meta"), "on_twod");
+        if (on_twod) *on_twod = twod ? 1 : 0;
+        const auto shapes = parse_shapes(root->sub("shapes"), false);
+        std::vector<sdfibm_solid_desc> out;
+        read_vof_entries(root->sub("solids"), shapes, twod, out);
+        if (with_planes)
+            if (const Node* pl = root->find("planes")) {
+                if (!pl->is_dict) throw std::runtime_error("planes is not a dictionary");
+                read_vof_entries(*pl, shapes, twod, out);
+            }
+        *nsolids = (int32_t)out.size();
+        if ((int32_t)out.size() > capacity) return set_msg(msg, msg_len, "solid capacity too small", SDFIBM_ERR_ARG);
+        if (solids)
+            for (size_t i = 0; i < out.size(); ++i) solids[i] = out[i];
+    } catch (const std::exception& e) {
+        return set_msg(msg, msg_len, e.what(), SDFIBM_ERR_ARG);
+    }
+    return SDFIBM_OK;
+}
+
+extern "C" int sdfibm_host_parse_blockmesh(const char* text, sdfibm_mesh_desc* mesh, char* msg, int32_t msg_len) {
+    if (!text || !mesh) return set_msg(msg, msg_len, "null argument", SDFIBM_ERR_ARG);
+    try {
+        const std::string src(text);
+        std::vector<std::string> t;
+        double scale = 1.0;
+        if (raw_entry(src, "convertToMeters", t) || raw_entry(src, "scale", t)) {
+            if (t.size() != 1) throw std::runtime_error("bad convertToMeters");
+            scale = to_num(t[0]);
+        }
+        if (!raw_entry(src, "vertices", t)) throw std::runtime_error("missing vertices");
+        std::vector<double> v;
+        for (auto& x : t)
+            if (x != "(" && x != ")") v.push_back(to_num(x) * scale);
+        if (v.empty() || v.size() % 3) throw std::runtime_error("bad vertices");
+        if (!raw_entry(src, "blocks", t)) throw std::runtime_error("missing blocks");
+        // ( hex ( 8 labels ) ( nx ny nz ) simpleGrading ( 1 1 1 ) )
+        std::vector<std::string> w;
+        for (auto& x : t)
+            if (x != "(" && x != ")") w.push_back(x);
+        if (w.size() != 16 || w[0] != "hex" || w[12] != "simpleGrading")
+            throw std::runtime_error("one hex block with simpleGrading expected");
+        for (int k = 13; k < 16; ++k)
+            if (to_num(w[k]) != 1.0) throw std::runtime_error("graded block: only uniform grading is supported");
+        int lab[8];
+        const int nv = (int)(v.size() / 3);
+        for (int k = 0; k < 8; ++k) {
+            lab[k] = (int)to_num(w[1 + k]);
+            if (lab[k] < 0 || lab[k] >= nv) throw std::runtime_error("block vertex label out of range");
+        }
+        const long long n[3] = {std::stoll(w[9]), std::stoll(w[10]), std::stoll(w[11])};
+        for (int a = 0; a < 3; ++a)
+            if (n[a] < 1 || n[a] > (1 << 30)) throw std::runtime_error("bad cell count");
+        // the hex's local axes: x = v0->v1, y = v0->v3, z = v0->v4 (blockMesh's vertex order), axis-aligned
+        auto P = [&](int k, int a) { return v[3 * lab[k] + a]; };
+        double lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) lo[a] = P(0, a);
+        const int far[3] = {1, 3, 4};
+        for (int a = 0; a < 3; ++a) {
+            hi[a] = P(far[a], a);
+            for (int b = 0; b < 3; ++b)
+                if (b != a && P(far[a], b) != P(0, b)) throw std::runtime_error("the block is not axis-aligned");
+            if (!(hi[a] > lo[a])) throw std::runtime_error("the block's local axes must point along +x, +y, +z");
+        }
+        // the remaining corners must close the box
+        const int corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+        for (int k = 0; k < 8; ++k)
+            for (int a = 0; a < 3; ++a)
+                if (P(k, a) != (corner[k][a] ? hi[a] : lo[a])) throw std::runtime_error("the block is not a box");
+        mesh->nx = (int32_t)n[0];
+        mesh->ny = (int32_t)n[1];
+        mesh->nz = (int32_t)n[2];
+        mesh->twod = n[2] == 1 ? 1 : 0;
+        for (int a = 0; a < 3; ++a) {
+            mesh->origin[a] = lo[a];
+            mesh->h[a] = (hi[a] - lo[a]) / (double)n[a];
+        }
+    } catch (const std::exception& e) {
+        return set_msg(msg, msg_len, e.what(), SDFIBM_ERR_ARG);
+    }
+    return SDFIBM_OK;
+}
+
+extern "C" int sdfibm_host_write_scalar_field(const char* file, int64_t file_len, const double* values, int64_t n,
+                                              int32_t format, int32_t precision, char* buf, int64_t cap, int64_t* len,
+                                              char* msg, int32_t msg_len) {
+    if (!file || file_len < 0 || (n > 0 && !values) || n < 0 || !len || precision < 0 || precision > 17 ||
+        format < -1 || format > 1)
+        return set_msg(msg, msg_len, "bad argument", SDFIBM_ERR_ARG);
+    const std::string src(file, (size_t)file_len);
+    try {
+        // the header's format (FoamFile { format ascii|binary; }): the text before the first binary byte
+        const size_t hdr = src.find("FoamFile");
+        if (hdr == std::string::npos) throw std::runtime_error("no FoamFile header");
+        const size_t hend = src.find('}', hdr);
+        if (hend == std::string::npos) throw std::runtime_error("unterminated FoamFile header");
+        bool binary = false;
+        {
+            std::vector<std::string> t;
+            const std::string header = src.substr(hdr, hend - hdr + 1);
+            if (raw_entry(header.substr(header.find('{') + 1, header.rfind('}') - header.find('{') - 1), "format", t))
+                binary = t.size() == 1 && t[0] == "binary";
+        }
+        // the header's format word, rewritten when the output format differs from the file's
+        std::string head = src.substr(0, hend + 1);
+        if (format >= 0 && (format == 1) != binary) {
+            size_t f = head.find("format", hdr);
+            while (f != std::string::npos &&
+                   !(std::isspace((unsigned char)head[f - 1]) && std::isspace((unsigned char)head[f + 6])))
+                f = head.find("format", f + 6);
+            if (f == std::string::npos) throw std::runtime_error("no format entry in the FoamFile header");
+            size_t b = f + 6;
+            while (b < head.size() && std::isspace((unsigned char)head[b])) ++b;
+            const size_t e = head.find(';', b);
+            if (e == std::string::npos) throw std::runtime_error("bad format entry");
+            head.replace(b, e - b, format == 1 ? "binary" : "ascii");
+        }
+        const bool out_binary = format < 0 ? binary : format == 1;
+        // internalField after the header, at brace depth 0
+        size_t at = hend + 1;
+        int depth = 0;
+        size_t key = std::string::npos;
+        for (size_t i = at; i + 13 <= src.size(); ++i) {
+            const char c = src[i];
+            if (c == '{') ++depth;
+            else if (c == '}') --depth;
+            else if (c == '/' && i + 1 < src.size() && src[i + 1] == '/') {
+                i = src.find('\n', i);
+                if (i == std::string::npos) break;
+            } else if (depth == 0 && src.compare(i, 13, "internalField") == 0 &&
+                       (i == 0 || std::isspace((unsigned char)src[i - 1])) &&
+                       (i + 13 == src.size() || std::isspace((unsigned char)src[i + 13]))) {
+                key = i;
+                break;
+            }
+        }
+        if (key == std::string::npos) throw std::runtime_error("no internalField");
+        // the end of its value: ';' after `uniform v`, or after the closing ')' of a nonuniform list (binary lists
+        // are skipped by their byte count)
+        size_t p = key + 13;
+        auto skip_ws = [&]() { while (p < src.size() && std::isspace((unsigned char)src[p])) ++p; };
+        auto word = [&]() {
+            skip_ws();
+            size_t b = p;
+            while (p < src.size() && !std::isspace((unsigned char)src[p]) && src[p] != '(' && src[p] != ';') ++p;
+            return src.substr(b, p - b);
+        };
+        const std::string kind = word();
+        size_t end;
+        if (kind == "uniform") {
+            end = src.find(';', p);
+        } else if (kind == "nonuniform") {
+            const std::string lt = word();
+            if (lt != "List<scalar>") throw std::runtime_error("internalField is not a List<scalar>");
+            const std::string cnt = word();
+            const long long m = std::stoll(cnt);
+            skip_ws();
+            if (p >= src.size() || src[p] != '(') throw std::runtime_error("bad internalField list");
+            if (binary) {
+                p += 1 + (size_t)m * 8;
+                if (p >= src.size() || src[p] != ')') throw std::runtime_error("bad binary internalField list");
+            } else {
+                p = src.find(')', p);
+                if (p == std::string::npos) throw std::runtime_error("unterminated internalField list");
+            }
+            end = src.find(';', p);
+        } else {
+            throw std::runtime_error("unknown internalField form " + kind);
+        }
+        if (end == std::string::npos) throw std::runtime_error("unterminated internalField");
+        std::string out = head + src.substr(hend + 1, key - hend - 1);
+        out += "internalField   nonuniform List<scalar> \n" + std::to_string(n) + "\n(";
+        if (out_binary) {
+            out.append(reinterpret_cast<const char*>(values), (size_t)n * 8);  // little-endian doubles, as read
+        } else {
+            const int prec = precision ? precision : 6;
+            out += "\n";
+            for (int64_t i = 0; i < n; ++i) {
+                out += put_g(values[i], prec);
+                out += "\n";
+            }
+        }
+        out += ")\n";
+        out += src.substr(end);
+        const int rc = emit(out, buf, cap, len);
+        return rc == SDFIBM_OK ? SDFIBM_OK : set_msg(msg, msg_len, "buffer too small", rc);
+    } catch (const std::exception& e) {
+        return set_msg(msg, msg_len, e.what(), SDFIBM_ERR_ARG);
+    }
 }

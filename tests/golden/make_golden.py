@@ -6,6 +6,8 @@
   falling_ellipse.npz   the oracle run on the reference's own OpenFOAM polyMesh of examples/falling_ellipse
                         (100x200x1 cells, ellipse 0.3x0.15 at (0.5,3.5), euler z=-45 deg): touched cells, As, forcing.
                         It pins the uniform-mesh ordering conventions against a real OpenFOAM mesh.
+  tool_vof_alpha.npz    the smooth phase field the reference's VOF initializer wrote for tool_vof/example
+                        (0/alpha.water: 200x200x1 cells on [0,4]^2, twelve shapes and two planes of its solidDict).
 Usage: python tests/golden/make_golden.py /path/to/reference
 """
 import os
@@ -69,7 +71,12 @@ def main(ref):
     cells, types = oc.touched(0)
     np.savez_compressed(os.path.join(HERE, "falling_ellipse.npz"), cells=cells, types=types, As=f["As"][cells],
                         Fs=f["Fs"].reshape(3, N)[:, cells], FT=FT, U_seed=7, U_std=0.1, dt=0.01)
-    print("re200: %d nonzero; falling_ellipse: %d touched cells, FT=%s" % ((centre > 0).sum(), len(cells), FT))
+    vof, _ = read_foam_list(os.path.join(ref, "tool_vof/example/0/alpha.water"), "<f8")
+    assert len(vof) == 40000
+    np.savez_compressed(os.path.join(HERE, "tool_vof_alpha.npz"), alpha=np.ascontiguousarray(vof), nx=200, ny=200,
+                        origin=np.array([0.0, 0.0, -0.5]), h=np.array([0.02, 0.02, 1.0]))
+    print("re200: %d nonzero; falling_ellipse: %d touched cells, FT=%s; tool_vof: %d nonzero"
+          % ((centre > 0).sum(), len(cells), FT, (vof > 0).sum()))
 
 
 if __name__ == "__main__":
