@@ -109,3 +109,14 @@ def test_unknown_motion_name_is_free(cuda_lib):
     # m_libmotion[name] of an unknown name yields a null motion (solidcloud.cpp:185-186)
     solids, _, _ = parse_soliddict(DICT.replace("mot_name rot;", "mot_name nothing;"), rho_f=1.0)
     assert solids[1].motion_type == abi.MOTION_FREE
+
+
+def test_repeated_names(cuda_lib):
+    """Shapes and forcers come from EntityLibrary (emplace: the first of a repeated name stays,
+    src/entitylibrary.h:22); motions and materials are assigned into a map (the last stays, solidcloud.cpp:116, 137)."""
+    text = DICT.replace("shape3 {", "shape4 { name circle1; type Circle; radius 0.9; }\n    shape3 {").replace(
+        "material1 { name mat1; type General; rho 3.0; }",
+        "material1 { name mat1; type General; rho 3.0; } material2 { name mat1; type General; rho 5.0; }")
+    solids, _, _ = parse_soliddict(text, rho_f=1.0)
+    assert solids[0].shape.radiusB == 0.15   # first circle1
+    assert solids[0].rho == 5.0              # last mat1
