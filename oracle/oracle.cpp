@@ -27,6 +27,7 @@
 #include <cstdint>
 #include <cstring>
 #include <functional>
+#include <limits>
 #include <memory>
 #include <queue>
 #include <set>
@@ -63,6 +64,15 @@ struct Solid {
 };
 
 inline V3 arr3(const double* a) { return V3{a[0], a[1], a[2]}; }
+
+// double -> integer by truncation with the device's conversion rules (NaN -> 0, out of range -> the nearest limit):
+// a non-finite or far-off solid position then has one defined result on every host (a plain cast is undefined there)
+template <class I> inline I to_int_rz(double t) {
+    if (!(t == t)) return 0;
+    if (t >= (double)std::numeric_limits<I>::max()) return std::numeric_limits<I>::max();
+    if (t <= (double)std::numeric_limits<I>::min()) return std::numeric_limits<I>::min();
+    return (I)t;
+}
 inline void put3(double* a, const V3& v) { a[0] = v.x; a[1] = v.y; a[2] = v.z; }
 
 // ---- motions: IMotion::constraint ----------------------------------------------------------------------------
@@ -221,19 +231,20 @@ struct CloudBase {
         double rB = -1.0;
         for (const Solid& s : solids) rB = std::max(rB, s.d.shape.radiusB);
         double delta = 2 * rB;
+        if (!(delta > 0)) return;
         double dINV = 1.0 / delta;
         double low[3] = {bmin.x, bmin.y, bmin.z}, high[3] = {bmax.x, bmax.y, bmax.z};
-        int nx = (int)std::ceil((high[0] - low[0]) * dINV);
-        int ny = (int)std::ceil((high[1] - low[1]) * dINV);
-        int nz = (int)std::ceil((high[2] - low[2]) * dINV);
-        if (!(delta > 0) || nx <= 0 || ny <= 0 || nz <= 0) return;
-        int nynz = ny * nz;
+        int nx = to_int_rz<int>(std::ceil((high[0] - low[0]) * dINV));
+        int ny = to_int_rz<int>(std::ceil((high[1] - low[1]) * dINV));
+        int nz = to_int_rz<int>(std::ceil((high[2] - low[2]) * dINV));
+        if (nx <= 0 || ny <= 0 || nz <= 0) return;
+        int64_t nynz = (int64_t)ny * nz;
         int64_t ncell = (int64_t)nx * ny * nz;
         std::unordered_map<int64_t, std::vector<int>> map;
         for (const Solid& s : solids) {
-            int i = (int)std::floor((s.center.x - low[0]) * dINV);
-            int j = (int)std::floor((s.center.y - low[1]) * dINV);
-            int k = (int)std::floor((s.center.z - low[2]) * dINV);
+            int i = to_int_rz<int>(std::floor((s.center.x - low[0]) * dINV));
+            int j = to_int_rz<int>(std::floor((s.center.y - low[1]) * dINV));
+            int k = to_int_rz<int>(std::floor((s.center.z - low[2]) * dINV));
             map[(int64_t)i * nynz + (int64_t)j * nz + k].push_back(s.id);
         }
         std::vector<std::pair<int, int>> pairs;
@@ -756,7 +767,7 @@ template <> int64_t Cloud<UniformMesh>::findNearestCell(const V3& p) const {
     int64_t lo[3], hi[3];
     for (int a = 0; a < 3; ++a) {
         double t = std::floor((pc[a] - o[a]) / h[a]);
-        int64_t e = t < 0 ? 0 : (t > (double)(n[a] - 1) ? n[a] - 1 : (int64_t)t);
+        int64_t e = !(t >= 0) ? 0 : (t > (double)(n[a] - 1) ? n[a] - 1 : (int64_t)t);  // NaN: 0, as the device
         lo[a] = std::max<int64_t>(0, e - 1); hi[a] = std::min<int64_t>(n[a] - 1, e + 1);
     }
     int64_t best = -1;
@@ -811,8 +822,8 @@ template <> bool Cloud<UniformMesh>::bboxCells(const Solid& s, int64_t lo[3], in
         if (prism && a == 2) { lo[a] = 0; hi[a] = n[a] - 1; continue; }
         double l = std::floor((c3[a] - r - mesh.d.origin[a]) / mesh.d.h[a]) - 1;
         double u = std::floor((c3[a] + r - mesh.d.origin[a]) / mesh.d.h[a]) + 1;
-        lo[a] = (int64_t)std::max(0.0, l);
-        hi[a] = (int64_t)std::min((double)(n[a] - 1), u);
+        lo[a] = (int64_t)std::min(std::max(0.0, l), (double)n[a]);
+        hi[a] = (int64_t)std::max(std::min((double)(n[a] - 1), u), -1.0);
     }
     return true;
 }

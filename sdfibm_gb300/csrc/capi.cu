@@ -261,16 +261,6 @@ const char* sdfibm_cuda_version(void) { return "sdfibm-gb300 1.0 (sm_103a)"; }
 
 const char* sdfibm_cuda_last_error(const sdfibm_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
-void sdfibm_options_default(sdfibm_options* o) {
-    if (!o) return;
-    std::memset(o, 0, sizeof(*o));
-    o->rho_f = 1.0;
-    o->collision_mode = SDFIBM_COLLISION_OFF;
-    o->fraction_method = SDFIBM_FRACTION_REFGEO;
-    o->subsample_n = 10;
-    o->exact_forcing = 1;
-}
-
 // radius around -com of a sphere (or, for 2-D shapes, a disc in the local x-y plane) that holds every point the
 // shape's isInside accepts (IShape::m_radiusB is not such a bound for rectangles, boxes and tails)
 static bool bound_radius(const sdfibm_shape_desc& s, double& r, int& prism) {

@@ -55,6 +55,16 @@ Qh axis_angle(double dx, double dy, double dz, double th) {
 
 extern "C" {
 
+void sdfibm_options_default(sdfibm_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->rho_f = 1.0;
+    o->collision_mode = SDFIBM_COLLISION_OFF;
+    o->fraction_method = SDFIBM_FRACTION_REFGEO;
+    o->subsample_n = 10;
+    o->exact_forcing = 1;
+}
+
 int sdfibm_host_make_shape(int32_t type, const double* raw, const double* com_in, sdfibm_shape_desc* out) {
     if (!out || (!raw && type != SDFIBM_SHAPE_PLANE)) return SDFIBM_ERR_ARG;
     sdfibm_shape_desc s;
@@ -1028,6 +1038,7 @@ extern "C" int sdfibm_host_write_scalar_field(const char* file, int64_t file_len
             const long long m = std::stoll(cnt);
             skip_ws();
             if (p >= src.size() || src[p] != '(') throw std::runtime_error("bad internalField list");
+            if (m < 0 || (uint64_t)m > (uint64_t)(src.size() - p) / 8) throw std::runtime_error("bad internalField size");
             if (binary) {
                 p += 1 + (size_t)m * 8;
                 if (p >= src.size() || src[p] != ')') throw std::runtime_error("bad binary internalField list");

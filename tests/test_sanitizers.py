@@ -1,0 +1,58 @@
+"""Address and undefined-behaviour sanitizer builds of the host code, on CPU.
+
+Two drivers are compiled with g++ -fsanitize=address,undefined and run; a sanitizer report aborts them:
+  - tests/sanitize/host_driver.cpp drives the host half of the library (sdfibm_gb300/csrc/host.cpp). Inputs are
+    the solidDict, VOF-dict, blockMesh and field-file front ends and writers: every prefix of each input,
+    byte-mutated copies, and output buffers of every capacity below what is needed;
+  - tests/sanitize/oracle_driver.cpp drives the oracle: both modes, 2-D and 3-D, every shape, interact, evolve with
+    collisions (solids that coincide, leave the mesh or go non-finite), fixInternal and the mean field.
+The device half has no sanitizer run here."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SAN = ["-std=c++17", "-O1", "-g", "-fsanitize=address,undefined", "-fno-omit-frame-pointer", "-ffp-contract=off",
+       "-I", os.path.join(ROOT, "include")]
+ENV = dict(os.environ, UBSAN_OPTIONS="halt_on_error=1:print_stacktrace=1", ASAN_OPTIONS="detect_leaks=1")
+
+
+def _compile(out, sources, extra=()):
+    cxx = shutil.which(os.environ.get("CXX", "g++"))
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    r = subprocess.run([cxx] + SAN + [os.path.join(ROOT, s) for s in sources] + ["-o", out] + list(extra),
+                       capture_output=True, text=True)
+    if r.returncode != 0 and "sanitize" in r.stderr:
+        pytest.skip("the compiler has no sanitizer runtime")
+    assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_host_code_under_sanitizers(cuda_lib, tmp_path):
+    from test_host import DICT
+    from test_vof import BLOCKMESH, FIELD, vof_dict_text
+    from sdfibm_gb300.vof import write_scalar_field
+    d = tmp_path / "in"
+    d.mkdir()
+    (d / "soliddict.txt").write_text(DICT)
+    (d / "vofdict.txt").write_text(vof_dict_text())
+    (d / "blockmesh.txt").write_text(BLOCKMESH)
+    (d / "field_ascii").write_text(FIELD)
+    (d / "field_binary").write_bytes(write_scalar_field(FIELD.encode(), np.linspace(0, 1, 50), "binary"))
+    exe = str(tmp_path / "host_driver")
+    _compile(exe, ["tests/sanitize/host_driver.cpp", "sdfibm_gb300/csrc/host.cpp"])
+    r = subprocess.run([exe, str(d)], capture_output=True, text=True, env=ENV, timeout=600)
+    assert r.returncode == 0, (r.stdout + r.stderr)[-4000:]
+    assert "calls clean" in r.stdout
+
+
+def test_oracle_under_sanitizers(tmp_path):
+    exe = str(tmp_path / "oracle_driver")
+    _compile(exe, ["tests/sanitize/oracle_driver.cpp", "oracle/oracle.cpp", "sdfibm_gb300/csrc/host.cpp"],
+             ["-pthread"])
+    r = subprocess.run([exe], capture_output=True, text=True, env=ENV, timeout=600)
+    assert r.returncode == 0, (r.stdout + r.stderr)[-4000:]
+    assert "calls clean" in r.stdout
