@@ -172,16 +172,44 @@ def test_oracle_matches_the_tools_field():
     assert (np.abs(f2["As"] - g["alpha"]) > 0.5).sum() > 4000
 
 
-@pytest.mark.gpu
-def test_run_case_gpu(cuda_lib, torch_cuda, tmp_path):
-    from sdfibm_gb300.vof import run_case
-    case = tmp_path / "case"
+def _write_case(case):
     for d in ("system", "0"):
         (case / d).mkdir(parents=True)
     (case / "solidDict").write_text(vof_dict_text())
     (case / "system" / "blockMeshDict").write_text(BLOCKMESH)
     (case / "system" / "controlDict").write_text("application interFoam;\nwriteFormat binary;\nwritePrecision 6;\n")
     (case / "0" / "alpha.water").write_text(FIELD)
+
+
+def test_run_case_host_logic(cuda_lib, tmp_path, monkeypatch):
+    """run_case's host logic (dictionaries, mesh, template, writer) with the coupling pass answered by the oracle."""
+    from sdfibm_gb300 import vof
+
+    def oracle_vof(mesh, solids, device="cuda"):
+        oc = OracleCloud(mesh, solids, abi.options(rho_f=1.0), faithful=False)
+        f = oc.new_fields()
+        oc.interact(0.0, 1.0, np.zeros(3 * oc.N), f)
+        return f["As"]
+
+    monkeypatch.setattr(vof, "smooth_vof", oracle_vof)
+    case = tmp_path / "case"
+    _write_case(case)
+    logs = []
+    alpha = vof.run_case(str(case), log=logs.append)
+    data = (case / "0" / "alpha.water").read_bytes()
+    assert b"format      binary;" in data
+    got, _ = read_field(data)
+    assert np.array_equal(got, alpha)
+    g = golden("tool_vof_alpha.npz")["alpha"]
+    assert np.abs(got - g).max() < 3.5e-5
+    assert re.match(r"\* Write smooth phase field \[alpha.water\] to \./0, total volume = 5\.2017", logs[-1])
+
+
+@pytest.mark.gpu
+def test_run_case_gpu(cuda_lib, torch_cuda, tmp_path):
+    from sdfibm_gb300.vof import run_case
+    case = tmp_path / "case"
+    _write_case(case)
     logs = []
     alpha = run_case(str(case), log=logs.append)
     got, _ = read_field((case / "0" / "alpha.water").read_bytes())
