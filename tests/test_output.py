@@ -230,3 +230,23 @@ def test_soliddict_lookup(cuda_lib):
         soliddict_lookup(DICT_3D, "meta")
     with pytest.raises(HostError):
         soliddict_lookup("meta { on_fluid 1;", "meta/on_fluid")
+
+
+def test_cloud_writers_host_logic(cuda_lib, tmp_path):
+    """SolidCloud.save_state / save_restart with the device state read answered on the host."""
+    from sdfibm_gb300.cloud import SolidCloud
+    st = _states(2, 11)
+    cloud = SolidCloud.__new__(SolidCloud)
+    cloud.time = 0.25
+    cloud.mesh = abi.mesh_desc((4, 4, 4), (0, 0, 0), (0.25, 0.25, 0.25), twod=0)
+    cloud._sampler = None
+    cloud._sampler_fields = None
+    cloud.states = lambda: st
+    f = StateFile(str(tmp_path / "cloud.out"), twod=False, mean_field_path=str(tmp_path / "meanfield.out"))
+    cloud.save_state(f)           # no sampler: no mean-field line
+    f.close()
+    assert open(tmp_path / "cloud.out").read() == format_state(0.25, st, False)
+    assert open(tmp_path / "meanfield.out").read() == ""
+    cloud.save_restart(DICT_3D, str(tmp_path / "solidDict"), precision=17, stamp="s")
+    again, _, _ = parse_soliddict(open(tmp_path / "solidDict").read(), 1.0)
+    assert [list(d.pos) for d in again] == [list(s.pos) for s in st]
