@@ -7,6 +7,7 @@
     cloud.states() / cloud.set_states(st)              # Solid getters / setters
     cloud.save_state(state_file, U, Ct)                # SolidCloud::saveState   (state_file: host.StateFile)
     cloud.set_sampler(shape); cloud.mean_field(U, Ct)  # meta.sampler, SolidCloud::calcMeanField
+    cloud.initial_correct(U, fields), cloud.total_solid_volume(fields), cloud[i], cloud.is_on_twod()
     cloud.save_restart(dict_text, path)                # SolidCloud::saveRestart
 
 Fields are CUDA tensors in the cell-major layout of include/sdfibm_cuda.h: U and Fs have shape (3, N) float32,
@@ -96,6 +97,41 @@ class SolidCloud:
                                                p(fields["Ts"]), p(fields["Ct"]), p(FT))
         self._check(rc)
         return FT[:self.nsolids]
+
+    def initial_correct(self, U, fields):
+        """SolidCloud::initialCorrect (src/solidcloud.cpp:276-286): interact(0, 1), then every solid's force and
+        torque cleared (the fluid force of that pass stays, as in the reference).  Returns the per-solid force and
+        torque of the pass."""
+        FT = self.interact(0.0, 1.0, U, fields)
+        st = self.states()
+        for x in st:
+            for a in range(3):
+                x.force[a] = 0.0
+                x.torque[a] = 0.0
+        self.set_states(st)
+        return FT
+
+    def total_solid_volume(self, fields):
+        """SolidCloud::totalSolidVolume (src/solidcloud.cpp:572-576): sum of As times the cell volume."""
+        V = float(self.mesh.h[0]) * float(self.mesh.h[1]) * float(self.mesh.h[2])
+        return float(fields["As"].double().sum()) * V
+
+    def is_on_fluid(self):
+        """SolidCloud::isOnFluid: meta.on_fluid (a cloud without fluid coupling has rho_f = 0)."""
+        return self.opt.rho_f != 0.0
+
+    def is_on_twod(self):
+        """SolidCloud::isOnTwoD: meta.on_twod."""
+        return bool(self.mesh.twod)
+
+    def __getitem__(self, i):
+        """SolidCloud::operator[] (src/solidcloud.cpp:667-670): the state of solid i."""
+        if not 0 <= i < self.nsolids:
+            raise IndexError(i)
+        return self.states()[i]
+
+    def __len__(self):
+        return self.nsolids
 
     def evolve(self, time, dt):
         self._check(self._L.sdfibm_cuda_evolve(self._h, float(time), float(dt)))

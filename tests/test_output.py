@@ -250,3 +250,21 @@ def test_cloud_writers_host_logic(cuda_lib, tmp_path):
     cloud.save_restart(DICT_3D, str(tmp_path / "solidDict"), precision=17, stamp="s")
     again, _, _ = parse_soliddict(open(tmp_path / "solidDict").read(), 1.0)
     assert [list(d.pos) for d in again] == [list(s.pos) for s in st]
+
+
+def test_cloud_info_host_logic(cuda_lib):
+    """SolidCloud's info methods on host tensors (totalSolidVolume, isOnTwoD, operator[])."""
+    torch = pytest.importorskip("torch")
+    from sdfibm_gb300.cloud import SolidCloud
+    cloud = SolidCloud.__new__(SolidCloud)
+    cloud.mesh = abi.mesh_desc((4, 2, 1), (0, 0, -0.5), (0.5, 0.25, 1.0), twod=1)
+    cloud.opt = abi.options(rho_f=0.0)
+    cloud.nsolids = 2
+    st = _states(2, 12)
+    cloud.states = lambda: st
+    As = torch.tensor([0.0, 1.0, 0.5, 0.25, 1.0, 0.0, 0.0, 1.0])
+    assert cloud.total_solid_volume({"As": As}) == 3.75 * 0.125
+    assert cloud.is_on_twod() and not cloud.is_on_fluid() and len(cloud) == 2
+    assert list(cloud[1].pos) == list(st[1].pos)
+    with pytest.raises(IndexError):
+        cloud[2]
