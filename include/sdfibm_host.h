@@ -50,6 +50,11 @@ int sdfibm_host_parse_soliddict(const char* text, double rho_f, sdfibm_solid_des
  * that names a sub-dictionary, or text that does not parse, returns SDFIBM_ERR_ARG. */
 int sdfibm_host_soliddict_lookup(const char* text, const char* path, char* buf, int64_t cap, int64_t* len);
 
+/* The shape named `name` in a solidDict's shapes library (meta.sampler names the mean-field sampler this way,
+ * src/solidcloud.cpp:38, 308); a repeated name keeps the first definition, as the library does. */
+int sdfibm_host_soliddict_shape(const char* text, const char* name, sdfibm_shape_desc* out, char* msg,
+                                int32_t msg_len);
+
 /* ---- output: the state file and the restart dictionary --------------------------------------------------------------
  * Text results go to buf: at most cap bytes including the terminating NUL; *len receives the length of the whole
  * text (without the NUL).  buf == NULL with cap == 0 only measures; a buffer of cap <= *len returns

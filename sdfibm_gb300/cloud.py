@@ -41,6 +41,7 @@ class SolidCloud:
         self._stream = stream
         self._sampler = None     # (shape, SolidCloud of the solids with that shape) for mean_field
         self._sampler_fields = None
+        self._sampler_ct = None  # (Ct written by mean_field, mask of its cells), zeroed before the next interact
         self.nsolids = len(solids)
         self.ncells = int(mesh.nx) * int(mesh.ny) * int(mesh.nz)
         self._solids = (abi.SolidDesc * max(1, len(solids)))(*solids)
@@ -80,6 +81,7 @@ class SolidCloud:
                     Ct=torch.zeros(N, dtype=torch.int32, device=device))
 
     def interact(self, time, dt, U, fields, want_ft=True):
+        self._clear_sampler_ct(fields["Ct"])
         FT = np.zeros((max(1, self.nsolids), 6)) if want_ft else None
         rc = self._L.sdfibm_cuda_interact(self._h, float(time), float(dt), _ptr(U), _ptr(fields["As"]),
                                           _ptr(fields["Fs"]), _ptr(fields["Ts"]), _ptr(fields["Ct"]),
@@ -190,7 +192,16 @@ class SolidCloud:
         if Ct is not None:
             sct = f["Ct"]
             Ct.copy_(torch.where(sct != 0, sct, Ct))
+            # the reference's next interact zeroes every cell (solidcloud.cpp:438-441); the sparse reset covers the
+            # coupling's own cells, so the sampler's are remembered and zeroed before that call
+            self._sampler_ct = (Ct, sct != 0)
         return F[:, :3] / W[:, :1]
+
+    def _clear_sampler_ct(self, Ct):
+        mark = getattr(self, "_sampler_ct", None)
+        if mark is not None and mark[0].data_ptr() == Ct.data_ptr():
+            Ct.masked_fill_(mark[1], 0)
+        self._sampler_ct = None
 
     def save_state(self, state_file, U=None, Ct=None):
         """SolidCloud::saveState: appends this step's records to a host.StateFile (cloud.out) and, when the file

@@ -1071,3 +1071,21 @@ extern "C" int sdfibm_host_write_scalar_field(const char* file, int64_t file_len
         return set_msg(msg, msg_len, e.what(), SDFIBM_ERR_ARG);
     }
 }
+
+// One shape of a solidDict's library by name (meta.sampler names one, src/solidcloud.cpp:38, 308)
+extern "C" int sdfibm_host_soliddict_shape(const char* text, const char* name, sdfibm_shape_desc* out, char* msg,
+                                           int32_t msg_len) {
+    if (!text || !name || !out) return set_msg(msg, msg_len, "null argument", SDFIBM_ERR_ARG);
+    try {
+        const std::string src(text);
+        Lexer lx(src);
+        auto root = parse_dict(lx, true);
+        const auto shapes = parse_shapes(root->sub("shapes"), true);
+        auto it = shapes.find(name);
+        if (it == shapes.end()) return set_msg(msg, msg_len, std::string("unknown shape name ") + name, SDFIBM_ERR_ARG);
+        *out = it->second;
+    } catch (const std::exception& e) {
+        return set_msg(msg, msg_len, e.what(), SDFIBM_ERR_ARG);
+    }
+    return SDFIBM_OK;
+}

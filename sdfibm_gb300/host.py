@@ -186,6 +186,15 @@ def soliddict_lookup(text, path, default=None):
     return buf.raw[:n.value].decode()
 
 
+def soliddict_shape(text, name):
+    """The shape named `name` in a solidDict's shapes library (e.g. the meta.sampler shape)."""
+    sh = abi.ShapeDesc()
+    msg = C.create_string_buffer(512)
+    if load().sdfibm_host_soliddict_shape(text.encode(), name.encode(), C.byref(sh), msg, 512) != abi.OK:
+        raise HostError(msg.value.decode())
+    return sh
+
+
 class StateFile:
     """cloud.out (and meanfield.out) as SolidCloud keeps them: opened (truncated) at construction
     (src/solidcloud.cpp:29-33, 234-236); every saveState call (src/solidcloud.cpp:578-593) appends one block of records

@@ -135,6 +135,15 @@ def test_mean_field_host_logic():
     ref = main.mean_field(sampler, Uo, fo["Ct"])
     assert np.abs(m - ref).max() < 1e-13
     assert np.array_equal(Ct.numpy(), fo["Ct"])
+    # before the next interact the sampler's cells return to 0, as the reference's dense reset leaves them
+    sampled = cloud._sampler_ct[1].numpy().copy()
+    assert sampled.sum() > 100
+    other = Ct.clone()
+    cloud._clear_sampler_ct(other.clone())      # another field: untouched, and the mark is consumed
+    assert cloud._sampler_ct is None
+    cloud._sampler_ct = (Ct, torch.from_numpy(sampled))
+    cloud._clear_sampler_ct(Ct)
+    assert (Ct.numpy()[sampled] == 0).all() and np.array_equal(Ct.numpy()[~sampled], other.numpy()[~sampled])
 
 
 @pytest.mark.gpu

@@ -268,3 +268,11 @@ def test_cloud_info_host_logic(cuda_lib):
     assert list(cloud[1].pos) == list(st[1].pos)
     with pytest.raises(IndexError):
         cloud[2]
+
+
+def test_soliddict_shape(cuda_lib):
+    from sdfibm_gb300.host import soliddict_shape
+    sh = soliddict_shape(DICT_3D, "brick")
+    assert bytes(sh) == bytes(make_shape("Box", radiusa=0.1, radiusb=0.05, radiusc=0.02, com=(0, 0, 0.01)))
+    with pytest.raises(HostError, match="unknown shape name"):
+        soliddict_shape(DICT_3D, "nothing")

@@ -1,0 +1,100 @@
+"""The C++ SolidCloud of include/sdfibm_cloud.hpp (the reference's interface over the C ABI, host fields).
+
+CPU: the header and the time-loop client of tests/cpp_client/cloud_client.cpp compile with -Wall -Wextra -Werror
+and link against libsdfibm_cuda.so.  GPU: the client's cloud.out, meanfield.out and restart dictionary equal, byte
+for byte, what the Python SolidCloud writes for the same loop on device fields (the same kernels behind both)."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+DICT = """meta { on_fluid 1; on_twod 1; gravity (0 -9.81 0); writeFrequency 2; sampler probe; on_meanfield 1; }
+shapes
+{
+    disc { name disc; type Circle; radius 0.05; }
+    probe { name probe; type Circle; radius 0.1; }
+    wall { name wall; type Plane; }
+}
+materials { m { name heavy; type General; rho 1.5; } }
+motions { f { name fixed; type Motion01Mask; mask b000000; } }
+solids
+{
+    a { shp_name disc; mot_name free; mat_name heavy; pos (0.3 0.5 0); vel (0.1 0 0); omega (0 0 1); }
+    b { shp_name disc; mot_name free; mat_name heavy; pos (0.62 0.45 0); vel (-0.1 0.05 0); }
+    c { shp_name disc; mot_name free; mat_name heavy; pos (0.5 0.8 0); euler (0 0 30); }
+    w { shp_name wall; mot_name fixed; mat_name heavy; pos (0 0.1 0); }
+}
+"""
+MESH = (128, 128, 1, 0.0, 0.0, -0.5, 0.0078125, 0.0078125, 1.0)
+STEPS, DT = 3, 0.002
+
+
+def _client(tmp_path):
+    cxx = shutil.which(os.environ.get("CXX", "g++"))
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    from sdfibm_gb300._lib import LIB_PATH
+    libdir = os.path.dirname(LIB_PATH)
+    exe = str(tmp_path / "cloud_client")
+    r = subprocess.run([cxx, "-std=c++17", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp_client", "cloud_client.cpp"), "-o", exe, "-L", libdir,
+                        "-l:libsdfibm_cuda.so", "-Wl,-rpath," + libdir], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_cpp_cloud_compiles(cuda_lib, tmp_path):
+    _client(tmp_path)
+
+
+@pytest.mark.gpu
+def test_cpp_cloud_matches_python(cuda_lib, torch_cuda, tmp_path):
+    torch = torch_cuda
+    from sdfibm_gb300 import abi
+    from sdfibm_gb300.cloud import SolidCloud
+    from sdfibm_gb300.host import StateFile, parse_soliddict, soliddict_shape
+    exe = _client(tmp_path)
+    N = MESH[0] * MESH[1] * MESH[2]
+    rng = np.random.default_rng(3)
+    U = (rng.standard_normal((3, N)) * 0.05).astype(np.float32)
+    U[0] += np.float32(0.2)
+    out = tmp_path / "cpp"
+    out.mkdir()
+    (tmp_path / "solidDict").write_text(DICT)
+    (tmp_path / "mesh.txt").write_text(" ".join(repr(v) for v in MESH))
+    U.tofile(str(tmp_path / "U.bin"))
+    r = subprocess.run([exe, str(tmp_path / "solidDict"), str(tmp_path / "mesh.txt"), str(tmp_path / "U.bin"),
+                        str(STEPS), repr(DT), str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+
+    # the same loop through the Python binding, device fields
+    solids, opt, twod = parse_soliddict(DICT, 1.0)
+    mesh = abi.mesh_desc(MESH[:3], MESH[3:6], MESH[6:], twod=twod)
+    cloud = SolidCloud(mesh, solids, opt)
+    cloud.set_sampler(soliddict_shape(DICT, "probe"))
+    Ud = torch.from_numpy(U).cuda()
+    f = cloud.new_fields()
+    py = tmp_path / "py"
+    py.mkdir()
+    sf = StateFile(str(py / "cloud.out"), twod, 2, mean_field_path=str(py / "meanfield.out"))
+    cloud.initial_correct(Ud, f)
+    cloud.save_state(sf, Ud, f["Ct"])
+    for s in range(1, STEPS + 1):
+        t = s * DT
+        cloud.interact(t, DT, Ud, f)
+        cloud.evolve(t, DT)
+        cloud.save_state(sf, Ud, f["Ct"])
+    sf.close()
+    cloud.save_restart(DICT, str(py / "solidDict.restart"), precision=17)
+    cloud.close()
+
+    assert (out / "cloud.out").read_text() == (py / "cloud.out").read_text()
+    assert len((py / "cloud.out").read_text().splitlines()) == 2 * 4   # calls 0 and 2 of 4
+    assert (out / "meanfield.out").read_text() == (py / "meanfield.out").read_text()
+    assert len((py / "meanfield.out").read_text().splitlines()) == STEPS + 1
+    a = (out / "solidDict.restart").read_text().splitlines()
+    b = (py / "solidDict.restart").read_text().splitlines()
+    assert a[:-1] == b[:-1]                                  # all but the time stamp
