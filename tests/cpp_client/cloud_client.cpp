@@ -8,6 +8,7 @@
 // meanfield.out (when the dictionary asks for it) and solidDict.restart; stdout the total solid volume and the
 // force on solid 0 of the last step.
 #include <cstdio>
+#include <cstdlib>
 #include <fstream>
 #include <iterator>
 #include <sstream>

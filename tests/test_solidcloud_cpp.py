@@ -1,8 +1,8 @@
 """The C++ SolidCloud of include/sdfibm_cloud.hpp (the reference's interface over the C ABI, host fields).
 
 CPU: the header and the time-loop client of tests/cpp_client/cloud_client.cpp compile with -Wall -Wextra -Werror
-and link against libsdfibm_cuda.so.  GPU: the client's cloud.out, meanfield.out and restart dictionary equal, byte
-for byte, what the Python SolidCloud writes for the same loop on device fields (the same kernels behind both)."""
+and link against libsdfibm_cuda.so.  GPU: the client's cloud.out, meanfield.out and restart dictionary agree with
+what the Python SolidCloud writes for the same loop on device fields (the same kernels behind both)."""
 import os
 import shutil
 import subprocess
@@ -91,10 +91,28 @@ def test_cpp_cloud_matches_python(cuda_lib, torch_cuda, tmp_path):
     cloud.save_restart(DICT, str(py / "solidDict.restart"), precision=17)
     cloud.close()
 
-    assert (out / "cloud.out").read_text() == (py / "cloud.out").read_text()
-    assert len((py / "cloud.out").read_text().splitlines()) == 2 * 4   # calls 0 and 2 of 4
-    assert (out / "meanfield.out").read_text() == (py / "meanfield.out").read_text()
-    assert len((py / "meanfield.out").read_text().splitlines()) == STEPS + 1
-    a = (out / "solidDict.restart").read_text().splitlines()
-    b = (py / "solidDict.restart").read_text().splitlines()
-    assert a[:-1] == b[:-1]                                  # all but the time stamp
+    # the per-solid force sums are FP64 atomics whose order varies from run to run, so the two runs agree to the last
+    # bits of the force and what follows from it: the 7-digit records within one unit of their last digit, the
+    # 17-digit restart within 1e-12
+    def numbers(text):
+        return np.array([[float(v) for v in line.split()] for line in text.splitlines()])
+
+    def close(a, b):  # per column: one unit of the 7th digit, or 1e-9 of the column's scale (sums that cancel)
+        scale = np.maximum(np.abs(a).max(axis=0), np.abs(b).max(axis=0))
+        return np.all(np.abs(a - b) <= 2e-6 * np.abs(b) + 1e-9 * scale)
+    a, b = numbers((out / "cloud.out").read_text()), numbers((py / "cloud.out").read_text())
+    assert a.shape == b.shape == (2 * 4, 10)                 # calls 0 and 2 of 4, four solids, 2-D columns
+    assert close(a, b)
+    a, b = numbers((out / "meanfield.out").read_text()), numbers((py / "meanfield.out").read_text())
+    assert a.shape == b.shape == (STEPS + 1, 3 * 4)
+    assert close(a, b)
+    ra = (out / "solidDict.restart").read_text().splitlines()[:-1]   # all but the time stamp
+    rb = (py / "solidDict.restart").read_text().splitlines()[:-1]
+    assert len(ra) == len(rb)
+    for x, y in zip(ra, rb):
+        if "(" in x:
+            vx = [float(v) for v in x[x.index("(") + 1:x.index(")")].split()]
+            vy = [float(v) for v in y[y.index("(") + 1:y.index(")")].split()]
+            assert x[:x.index("(")] == y[:y.index("(")] and np.allclose(vx, vy, rtol=1e-12, atol=1e-15), (x, y)
+        else:
+            assert x == y
