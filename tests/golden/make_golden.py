@@ -8,6 +8,7 @@
                         It pins the uniform-mesh ordering conventions against a real OpenFOAM mesh.
   tool_vof_alpha.npz    the smooth phase field the reference's VOF initializer wrote for tool_vof/example
                         (0/alpha.water: 200x200x1 cells on [0,4]^2, twelve shapes and two planes of its solidDict).
+It also checks that the host front ends read every solidDict the reference ships (no fixture is written for that).
 Usage: python tests/golden/make_golden.py /path/to/reference
 """
 import os
@@ -44,6 +45,24 @@ def read_faces(path):
     return off, lab
 
 
+def check_example_dicts(ref):
+    """The host front ends read every solidDict the reference ships: the solid count, and the positions in order
+    against a plain-text extraction of the pos entries of the solids block."""
+    import glob
+    from sdfibm_gb300.host import parse_soliddict
+    from sdfibm_gb300.vof import parse_vofdict
+    for path in sorted(glob.glob(os.path.join(ref, "examples", "**", "solidDict"), recursive=True)):
+        text = open(path).read()
+        solids, _, _ = parse_soliddict(text, 1.0)
+        block = text[text.index("solids"):]
+        pos = [tuple(float(v) for v in m.split()) for m in re.findall(r"\bpos\s*\(([^)]*)\)", block)]
+        assert [tuple(d.pos) for d in solids] == pos, path
+        print("%s: %d solids" % (os.path.relpath(path, ref), len(solids)))
+    solids, _ = parse_vofdict(open(os.path.join(ref, "tool_vof", "example", "solidDict")).read())
+    assert len(solids) == 14
+    print("tool_vof/example/solidDict: %d solids and planes" % len(solids))
+
+
 def main(ref):
     from oracle.oracle import OracleCloud
     from sdfibm_gb300 import abi
@@ -77,6 +96,7 @@ def main(ref):
                         origin=np.array([0.0, 0.0, -0.5]), h=np.array([0.02, 0.02, 1.0]))
     print("re200: %d nonzero; falling_ellipse: %d touched cells, FT=%s; tool_vof: %d nonzero"
           % ((centre > 0).sum(), len(cells), FT, (vof > 0).sum()))
+    check_example_dicts(ref)
 
 
 if __name__ == "__main__":
