@@ -201,7 +201,8 @@ public:
             o.rho_f = 1.0;
             o.fraction_method = SDFIBM_FRACTION_REFGEO;
             o.exact_forcing = 1;
-            check(sdfibm_cuda_create(&mesh_, ss.data(), (int32_t)ss.size(), &o, nullptr, &sampler_ctx_), "create");
+            check(sdfibm_cuda_create(&mesh_, ss.data(), (int32_t)ss.size(), &o, nullptr, &sampler_ctx_), "create",
+                  sampler_ctx_);
             sAs_.assign((size_t)N_, 0.0f);
             sFs_.assign((size_t)(3 * N_), 0.0f);
             sTs_.assign((size_t)N_, 0.0f);
@@ -211,14 +212,14 @@ public:
         std::vector<sdfibm_solid_state> st = states();
         for (auto& s : st)
             for (int a = 0; a < 3; ++a) s.vel[a] = s.omega[a] = 0.0;
-        check(sdfibm_cuda_set_solids(sampler_ctx_, st.data(), (int32_t)st.size()), "set_solids");
+        check(sdfibm_cuda_set_solids(sampler_ctx_, st.data(), (int32_t)st.size()), "set_solids", sampler_ctx_);
         std::vector<double> F(6 * st.size() + 6), W(6 * st.size() + 6);
         check(sdfibm_cuda_interact_host(sampler_ctx_, time_, 1.0, U_.data(), sAs_.data(), sFs_.data(), sTs_.data(),
                                         sCt_.data(), F.data()),
-              "interact");
+              "interact", sampler_ctx_);
         check(sdfibm_cuda_interact_host(sampler_ctx_, time_, 1.0, ones_.data(), sAs_.data(), sFs_.data(),
                                         sTs_.data(), sCt_.data(), W.data()),
-              "interact");
+              "interact", sampler_ctx_);
         for (int64_t c = 0; c < N_; ++c)
             if (sCt_[(size_t)c] != 0) Ct_[(size_t)c] = sCt_[(size_t)c];
         std::vector<double> m(3 * st.size());
@@ -249,9 +250,10 @@ public:
     sdfibm_ctx* context() const { return ctx_; }
 
 private:
-    void check(int rc, const char* what) const {
-        if (rc != SDFIBM_OK)
-            throw std::runtime_error(std::string(what) + ": " + (ctx_ ? sdfibm_cuda_last_error(ctx_) : "failed"));
+    void check(int rc, const char* what, const sdfibm_ctx* on = nullptr) const {
+        if (rc == SDFIBM_OK) return;
+        const sdfibm_ctx* c = on ? on : ctx_;
+        throw std::runtime_error(std::string(what) + ": " + (c ? sdfibm_cuda_last_error(c) : "failed"));
     }
     static void check_host(int rc, const char* msg) {
         if (rc != SDFIBM_OK) throw std::runtime_error(msg);
