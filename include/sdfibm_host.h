@@ -114,6 +114,29 @@ int sdfibm_host_write_scalar_field(const char* file, int64_t file_len, const dou
                                    int32_t format, int32_t precision, char* buf, int64_t cap, int64_t* len, char* msg,
                                    int32_t msg_len);
 
+/* ---- OpenFOAM list files: polyMesh points / faces / owner / neighbour and field internalFields ---------------------
+ * file: the file's bytes (ascii or binary per its FoamFile format; binary lists hold little-endian 8-byte scalars and
+ * 4-byte labels, the reference's build).  out == NULL only measures. */
+enum sdfibm_foam_kind { SDFIBM_FOAM_SCALAR = 0, SDFIBM_FOAM_VECTOR = 1, SDFIBM_FOAM_LABEL = 2 };
+
+/* The list of an OpenFOAM file: for a vol*Field class the internalField (a uniform field gives *n = -1 and its value
+ * in out[0] or out[0..2]), otherwise the first list after the header (points: VECTOR, owner/neighbour: LABEL).
+ * out: doubles (SCALAR: n, VECTOR: 3 n) or int32 labels; cap in elements (vectors count once). */
+int sdfibm_host_read_foam_list(const char* file, int64_t file_len, int32_t kind, void* out, int64_t cap, int64_t* n,
+                               char* msg, int32_t msg_len);
+
+/* A polyMesh faces file, faceCompactList (ascii or binary) or ascii faceList: offsets (nfaces + 1, from 0) and the
+ * vertex labels of every face in order. */
+int sdfibm_host_read_foam_faces(const char* file, int64_t file_len, int32_t* offsets, int64_t cap_offsets,
+                                int32_t* labels, int64_t cap_labels, int64_t* nfaces, int64_t* nlabels, char* msg,
+                                int32_t msg_len);
+
+/* The uniform mesh whose point lattice these polyMesh points are (a single blockMesh block: x fastest, then y, then
+ * z), every point within rtol of the mesh extent of its lattice position and ncells = nx ny nz; otherwise
+ * SDFIBM_ERR_ARG.  Lets a case without its blockMeshDict take the uniform-mesh path. */
+int sdfibm_host_uniform_mesh(const double* points, int64_t npoints, int64_t ncells, double rtol,
+                             sdfibm_mesh_desc* mesh, char* msg, int32_t msg_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -297,8 +297,12 @@ struct Lexer {
             i = e + 1;
             return true;
         }
+        // a word runs to the next blank or punctuation; a NUL byte (binary data) is a word character, since
+        // strchr would match it against the terminator of the punctuation string
         size_t b = i;
-        while (i < s.size() && !std::isspace((unsigned char)s[i]) && std::strchr("{}();[]", s[i]) == nullptr) ++i;
+        while (i < s.size() && !std::isspace((unsigned char)s[i]) &&
+               (s[i] == '\0' || std::strchr("{}();[]", s[i]) == nullptr))
+            ++i;
         tok = s.substr(b, i - b);
         return true;
     }
@@ -1086,6 +1090,279 @@ extern "C" int sdfibm_host_soliddict_shape(const char* text, const char* name, s
         *out = it->second;
     } catch (const std::exception& e) {
         return set_msg(msg, msg_len, e.what(), SDFIBM_ERR_ARG);
+    }
+    return SDFIBM_OK;
+}
+
+// ---- OpenFOAM list files (polyMesh points / faces / owner / neighbour, field internalFields) ----------------------------
+// Layout of OpenFOAM's IOstream lists: "N" then "(" and the N elements, then ")"; in binary files the elements are the
+// raw little-endian scalars (8 bytes) or labels (4 bytes, 32-bit label builds such as the reference's) between the
+// parentheses; a faceCompactList is two lists (N + 1 offsets, then the vertex labels).
+namespace {
+
+struct FoamHeader {
+    bool binary = false;
+    std::string cls;
+    size_t body = 0;  // offset after the header's closing brace
+};
+
+FoamHeader foam_header(const std::string& src) {
+    FoamHeader h;
+    const size_t at = src.find("FoamFile");
+    if (at == std::string::npos) throw std::runtime_error("no FoamFile header");
+    const size_t open = src.find('{', at), close = open == std::string::npos ? open : src.find('}', open);
+    if (close == std::string::npos) throw std::runtime_error("unterminated FoamFile header");
+    const std::string inner = src.substr(open + 1, close - open - 1);
+    std::vector<std::string> t;
+    if (raw_entry(inner, "format", t)) h.binary = t.size() == 1 && t[0] == "binary";
+    if (raw_entry(inner, "class", t) && t.size() == 1) h.cls = t[0];
+    h.body = close + 1;
+    return h;
+}
+
+void skip_blank(const std::string& s, size_t& p) {
+    for (;;) {
+        while (p < s.size() && std::isspace((unsigned char)s[p])) ++p;
+        if (p + 1 < s.size() && s[p] == '/' && s[p + 1] == '/') {
+            p = s.find('\n', p);
+            if (p == std::string::npos) p = s.size();
+        } else if (p + 1 < s.size() && s[p] == '/' && s[p + 1] == '*') {
+            const size_t e = s.find("*/", p + 2);
+            p = e == std::string::npos ? s.size() : e + 2;
+        } else {
+            return;
+        }
+    }
+}
+
+std::string next_word(const std::string& s, size_t& p) {
+    skip_blank(s, p);
+    const size_t b = p;
+    while (p < s.size() && !std::isspace((unsigned char)s[p]) && s[p] != '(' && s[p] != ')' && s[p] != ';') ++p;
+    return s.substr(b, p - b);
+}
+
+// "N (" at p: returns N and leaves p after the '('
+int64_t list_open(const std::string& s, size_t& p) {
+    const std::string w = next_word(s, p);
+    if (w.empty() || !std::isdigit((unsigned char)w[0])) throw std::runtime_error("list size expected");
+    const long long n = std::stoll(w);
+    skip_blank(s, p);
+    if (p >= s.size() || s[p] != '(') throw std::runtime_error("'(' expected");
+    ++p;
+    if (n < 0) throw std::runtime_error("negative list size");
+    // every element takes at least one byte: a size beyond the rest of the file is corrupt (and is refused before
+    // anyone allocates for it)
+    if ((uint64_t)n > (uint64_t)(s.size() - p)) throw std::runtime_error("list size exceeds the file");
+    return (int64_t)n;
+}
+
+// n values of `width` numbers each (width 3: "(x y z)" elements in ascii) into out (doubles or int32 labels)
+void read_items(const std::string& s, size_t& p, bool binary, int64_t n, int width, bool labels, double* dout,
+                int32_t* iout) {
+    const size_t esize = labels ? 4 : 8;
+    if (binary) {
+        const uint64_t bytes = (uint64_t)n * (uint64_t)width * esize;
+        if (bytes > s.size() - p) throw std::runtime_error("binary list shorter than its size");
+        if (dout) std::memcpy(dout, s.data() + p, (size_t)bytes);
+        if (iout) std::memcpy(iout, s.data() + p, (size_t)bytes);
+        p += (size_t)bytes;
+    } else {
+        for (int64_t i = 0; i < n; ++i) {
+            if (width > 1) {
+                skip_blank(s, p);
+                if (p >= s.size() || s[p] != '(') throw std::runtime_error("'(' of a list element expected");
+                ++p;
+            }
+            for (int a = 0; a < width; ++a) {
+                const std::string w = next_word(s, p);
+                if (w.empty()) throw std::runtime_error("number expected");
+                if (labels) {
+                    const long long v = std::stoll(w);
+                    if (iout) iout[i * width + a] = (int32_t)v;
+                } else if (dout) {
+                    dout[i * width + a] = to_num(w);
+                } else {
+                    to_num(w);
+                }
+            }
+            if (width > 1) {
+                skip_blank(s, p);
+                if (p >= s.size() || s[p] != ')') throw std::runtime_error("')' of a list element expected");
+                ++p;
+            }
+        }
+    }
+    skip_blank(s, p);
+    if (p >= s.size() || s[p] != ')') throw std::runtime_error("')' expected after the list");
+    ++p;
+}
+
+// the position after the "internalField" keyword at brace depth 0 after the header
+size_t internal_field(const std::string& src, size_t from) {
+    int depth = 0;
+    for (size_t i = from; i + 13 <= src.size(); ++i) {
+        const char c = src[i];
+        if (c == '{') ++depth;
+        else if (c == '}') --depth;
+        else if (c == '/' && i + 1 < src.size() && (src[i + 1] == '/' || src[i + 1] == '*')) {
+            size_t q = i;
+            skip_blank(src, q);
+            i = q - 1;
+        } else if (depth == 0 && src.compare(i, 13, "internalField") == 0 &&
+                   (i == 0 || std::isspace((unsigned char)src[i - 1])) &&
+                   (i + 13 == src.size() || std::isspace((unsigned char)src[i + 13]))) {
+            return i + 13;
+        }
+    }
+    throw std::runtime_error("no internalField");
+}
+
+}  // namespace
+
+extern "C" int sdfibm_host_read_foam_list(const char* file, int64_t file_len, int32_t kind, void* out, int64_t cap,
+                                          int64_t* n, char* msg, int32_t msg_len) {
+    if (!file || file_len < 0 || !n || kind < SDFIBM_FOAM_SCALAR || kind > SDFIBM_FOAM_LABEL)
+        return set_msg(msg, msg_len, "bad argument", SDFIBM_ERR_ARG);
+    try {
+        const std::string src(file, (size_t)file_len);
+        const FoamHeader h = foam_header(src);
+        const int width = kind == SDFIBM_FOAM_VECTOR ? 3 : 1;
+        const bool labels = kind == SDFIBM_FOAM_LABEL;
+        size_t p = h.body;
+        if (h.cls.compare(0, 3, "vol") == 0) {
+            p = internal_field(src, h.body);
+            const std::string form = next_word(src, p);
+            if (form == "uniform") {
+                if (labels) throw std::runtime_error("a uniform field holds no labels");
+                double v[3];
+                size_t q = p;
+                skip_blank(src, q);
+                if (width == 3) {
+                    if (q >= src.size() || src[q] != '(') throw std::runtime_error("uniform vector expected");
+                    p = q + 1;
+                    for (int a = 0; a < 3; ++a) v[a] = to_num(next_word(src, p));
+                } else {
+                    v[0] = to_num(next_word(src, p));
+                }
+                *n = -1;  // uniform: the value only
+                if (out && cap >= 1) std::memcpy(out, v, sizeof(double) * width);
+                return SDFIBM_OK;
+            }
+            if (form != "nonuniform") throw std::runtime_error("unknown internalField form " + form);
+            const std::string lt = next_word(src, p);
+            if (lt != (width == 3 ? "List<vector>" : "List<scalar>"))
+                throw std::runtime_error("internalField is a " + lt);
+        }
+        const int64_t m = list_open(src, p);
+        *n = m;
+        if (!out) return SDFIBM_OK;
+        if (cap < m) return set_msg(msg, msg_len, "output capacity too small", SDFIBM_ERR_CAPACITY);
+        read_items(src, p, h.binary, m, width, labels, labels ? nullptr : static_cast<double*>(out),
+                   labels ? static_cast<int32_t*>(out) : nullptr);
+    } catch (const std::exception& e) {
+        return set_msg(msg, msg_len, e.what(), SDFIBM_ERR_ARG);
+    }
+    return SDFIBM_OK;
+}
+
+extern "C" int sdfibm_host_read_foam_faces(const char* file, int64_t file_len, int32_t* offsets, int64_t cap_offsets,
+                                           int32_t* labels, int64_t cap_labels, int64_t* nfaces, int64_t* nlabels,
+                                           char* msg, int32_t msg_len) {
+    if (!file || file_len < 0 || !nfaces || !nlabels) return set_msg(msg, msg_len, "bad argument", SDFIBM_ERR_ARG);
+    try {
+        const std::string src(file, (size_t)file_len);
+        const FoamHeader h = foam_header(src);
+        size_t p = h.body;
+        const bool measure = !offsets || !labels;
+        if (h.cls == "faceCompactList") {
+            const int64_t no = list_open(src, p);
+            if (no < 1) throw std::runtime_error("empty offset list");
+            std::vector<int32_t> off((size_t)no);
+            read_items(src, p, h.binary, no, 1, true, nullptr, off.data());
+            const int64_t nl = list_open(src, p);
+            *nfaces = no - 1;
+            *nlabels = nl;
+            if (off[0] != 0 || off.back() != nl) throw std::runtime_error("offsets do not match the label list");
+            for (int64_t i = 0; i + 1 < no; ++i)
+                if (off[(size_t)i + 1] < off[(size_t)i]) throw std::runtime_error("decreasing face offsets");
+            if (measure) return SDFIBM_OK;
+            if (cap_offsets < no || cap_labels < nl)
+                return set_msg(msg, msg_len, "output capacity too small", SDFIBM_ERR_CAPACITY);
+            std::memcpy(offsets, off.data(), sizeof(int32_t) * (size_t)no);
+            read_items(src, p, h.binary, nl, 1, true, nullptr, labels);
+        } else if (h.cls == "faceList") {
+            if (h.binary) throw std::runtime_error("binary faceList: write the mesh as faceCompactList");
+            const int64_t nf = list_open(src, p);
+            std::vector<int32_t> off(1, 0), lab;
+            for (int64_t f = 0; f < nf; ++f) {
+                const int64_t k = list_open(src, p);
+                const size_t b = lab.size();
+                lab.resize(b + (size_t)k);
+                read_items(src, p, false, k, 1, true, nullptr, lab.data() + b);
+                off.push_back((int32_t)lab.size());
+            }
+            skip_blank(src, p);
+            if (p >= src.size() || src[p] != ')') throw std::runtime_error("')' expected after the faces");
+            *nfaces = nf;
+            *nlabels = (int64_t)lab.size();
+            if (measure) return SDFIBM_OK;
+            if (cap_offsets < nf + 1 || cap_labels < (int64_t)lab.size())
+                return set_msg(msg, msg_len, "output capacity too small", SDFIBM_ERR_CAPACITY);
+            std::memcpy(offsets, off.data(), sizeof(int32_t) * off.size());
+            if (!lab.empty()) std::memcpy(labels, lab.data(), sizeof(int32_t) * lab.size());
+        } else {
+            throw std::runtime_error("not a face list: class " + h.cls);
+        }
+    } catch (const std::exception& e) {
+        return set_msg(msg, msg_len, e.what(), SDFIBM_ERR_ARG);
+    }
+    return SDFIBM_OK;
+}
+
+extern "C" int sdfibm_host_uniform_mesh(const double* points, int64_t npoints, int64_t ncells, double rtol,
+                                        sdfibm_mesh_desc* mesh, char* msg, int32_t msg_len) {
+    if (!points || npoints < 8 || !mesh || !(rtol >= 0)) return set_msg(msg, msg_len, "bad argument", SDFIBM_ERR_ARG);
+    auto P = [&](int64_t i, int a) { return points[3 * i + a]; };
+    // single-block numbering: x fastest, then y, then z (a row ends where x falls back, a layer where y does; the
+    // lattice check below bounds every coordinate, blockMesh's points being within rounding of the lattice)
+    int64_t px = 1;
+    while (px < npoints && P(px, 0) > P(px - 1, 0)) ++px;
+    if (px < 2 || npoints % px) return set_msg(msg, msg_len, "points are not a lattice row by row", SDFIBM_ERR_ARG);
+    int64_t py = 1;
+    while (py * px < npoints && P(py * px, 1) > P((py - 1) * px, 1)) ++py;
+    if (py < 2 || npoints % (px * py)) return set_msg(msg, msg_len, "points are not a lattice layer by layer", SDFIBM_ERR_ARG);
+    const int64_t pz = npoints / (px * py);
+    if (pz < 2) return set_msg(msg, msg_len, "one layer of points", SDFIBM_ERR_ARG);
+    const int64_t n[3] = {px - 1, py - 1, pz - 1};
+    if (n[0] * n[1] * n[2] != ncells)
+        return set_msg(msg, msg_len, "the point lattice does not match the cell count", SDFIBM_ERR_ARG);
+    if (n[0] > INT32_MAX || n[1] > INT32_MAX || n[2] > INT32_MAX) return set_msg(msg, msg_len, "too many cells", SDFIBM_ERR_ARG);
+    const int64_t last = npoints - 1;
+    double o[3], h[3], ext = 0;
+    for (int a = 0; a < 3; ++a) {
+        o[a] = P(0, a);
+        h[a] = (P(last, a) - o[a]) / (double)n[a];
+        if (!(h[a] > 0)) return set_msg(msg, msg_len, "the lattice does not grow along +x, +y, +z", SDFIBM_ERR_ARG);
+        ext = std::max(ext, std::fabs(P(last, a) - o[a]) + std::fabs(o[a]));
+    }
+    const double tol = rtol * ext;
+    for (int64_t k = 0, i3 = 0; k < pz; ++k)
+        for (int64_t j = 0; j < py; ++j)
+            for (int64_t i = 0; i < px; ++i, ++i3) {
+                const double want[3] = {o[0] + (double)i * h[0], o[1] + (double)j * h[1], o[2] + (double)k * h[2]};
+                for (int a = 0; a < 3; ++a)
+                    if (std::fabs(P(i3, a) - want[a]) > tol)
+                        return set_msg(msg, msg_len, "point " + std::to_string(i3) + " is off the uniform lattice",
+                                       SDFIBM_ERR_ARG);
+            }
+    mesh->nx = (int32_t)n[0];
+    mesh->ny = (int32_t)n[1];
+    mesh->nz = (int32_t)n[2];
+    mesh->twod = n[2] == 1 ? 1 : 0;
+    for (int a = 0; a < 3; ++a) {
+        mesh->origin[a] = o[a];
+        mesh->h[a] = h[a];
     }
     return SDFIBM_OK;
 }

@@ -4,7 +4,8 @@ GB300 coupling library: a smooth phase field, the solids' volume fraction per ce
     python -m sdfibm_gb300.vof [CASE] [--name alpha.water] [--no-planes]
 
 reads CASE/solidDict (the tool's format: meta.on_twod, shapes, solids and planes with pos / euler / shp_name),
-the single uniform block of CASE/system/blockMeshDict (or constant/polyMesh/blockMeshDict) and CASE/0/<name>, and
+the single uniform block of CASE/system/blockMeshDict (or constant/polyMesh/blockMeshDict, or the polyMesh itself
+when it is one uniform block) and CASE/0/<name>, and
 writes CASE/0/<name> with its internalField set to the field, in the case's writeFormat and writePrecision.
 
 The field is one coupling pass on the GPU: sdfibm_cuda_interact of the solids at rest with the REF-GEO fraction
@@ -88,13 +89,17 @@ def _read(path, mode="r"):
 def run_case(case, name="alpha.water", with_planes=True, log=print):
     """tool_vof's main: writes CASE/0/<name>; returns the field."""
     solids, twod = parse_vofdict(_read(os.path.join(case, "solidDict")), with_planes)
+    pm = os.path.join(case, "constant", "polyMesh")
     for sub in ("system", os.path.join("constant", "polyMesh")):
         bm = os.path.join(case, sub, "blockMeshDict")
         if os.path.exists(bm):
+            mesh = parse_blockmesh(_read(bm))
             break
     else:
-        raise HostError("no blockMeshDict under %s/system or %s/constant/polyMesh" % (case, case))
-    mesh = parse_blockmesh(_read(bm))
+        if not os.path.exists(os.path.join(pm, "points")):
+            raise HostError("no blockMeshDict and no polyMesh in %s" % case)
+        from .foam_io import uniform_mesh_from_polymesh
+        mesh = uniform_mesh_from_polymesh(pm)  # a single uniform block, or HostError
     mesh.twod = int(twod)
     ctrl = _read(os.path.join(case, "system", "controlDict"))
     fmt = soliddict_lookup(ctrl, "writeFormat", "ascii")

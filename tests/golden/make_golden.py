@@ -8,7 +8,8 @@
                         It pins the uniform-mesh ordering conventions against a real OpenFOAM mesh.
   tool_vof_alpha.npz    the smooth phase field the reference's VOF initializer wrote for tool_vof/example
                         (0/alpha.water: 200x200x1 cells on [0,4]^2, twelve shapes and two planes of its solidDict).
-It also checks that the host front ends read every solidDict the reference ships (no fixture is written for that).
+It also checks that the host front ends read every solidDict the reference ships, and that the library's OpenFOAM
+readers agree with this script's on the reference's binary mesh and field files (no fixture is written for those).
 Usage: python tests/golden/make_golden.py /path/to/reference
 """
 import os
@@ -63,6 +64,27 @@ def check_example_dicts(ref):
     print("tool_vof/example/solidDict: %d solids and planes" % len(solids))
 
 
+def check_foam_readers(ref):
+    """The library's OpenFOAM readers (sdfibm_gb300.foam_io) give the arrays this script's readers give on the
+    reference's binary files, and the falling_ellipse polyMesh is the uniform 100 x 200 x 1 mesh the tests use."""
+    from sdfibm_gb300 import foam_io
+    pm = os.path.join(ref, "examples/falling_ellipse/constant/polyMesh")
+    assert np.array_equal(foam_io.read_list(os.path.join(pm, "points"), "vector")[0],
+                          read_foam_list(os.path.join(pm, "points"), "<f8", 3)[0])
+    for name in ("owner", "neighbour"):
+        assert np.array_equal(foam_io.read_list(os.path.join(pm, name), "label")[0],
+                              read_foam_list(os.path.join(pm, name), "<i4")[0])
+    off, lab = foam_io.read_faces(os.path.join(pm, "faces"))
+    off2, lab2 = read_faces(os.path.join(pm, "faces"))
+    assert np.array_equal(off, off2) and np.array_equal(lab, lab2)
+    m = foam_io.uniform_mesh_from_polymesh(pm)
+    assert (m.nx, m.ny, m.nz) == (100, 200, 1) and list(m.origin) == [0.0, 0.0, -0.5] and list(m.h) == [0.02, 0.02, 1.0]
+    for f in ("examples/flow_past_cylinder/re200/0/As", "tool_vof/example/0/alpha.water"):
+        assert np.array_equal(foam_io.read_list(os.path.join(ref, f), "scalar")[0],
+                              read_foam_list(os.path.join(ref, f), "<f8")[0])
+    print("OpenFOAM readers agree on the falling_ellipse polyMesh, re200 As and tool_vof alpha.water")
+
+
 def main(ref):
     from oracle.oracle import OracleCloud
     from sdfibm_gb300 import abi
@@ -97,6 +119,7 @@ def main(ref):
     print("re200: %d nonzero; falling_ellipse: %d touched cells, FT=%s; tool_vof: %d nonzero"
           % ((centre > 0).sum(), len(cells), FT, (vof > 0).sum()))
     check_example_dicts(ref)
+    check_foam_readers(ref)
 
 
 if __name__ == "__main__":

@@ -1,9 +1,10 @@
 // Drives the host half of libsdfibm_cuda.so (sdfibm_gb300/csrc/host.cpp: the solidDict, VOF-dict and blockMesh
-// front ends, the field and restart writers) under -fsanitize=address,undefined, on CPU.
+// front ends, the OpenFOAM list readers, the field and restart writers) under -fsanitize=address,undefined, on CPU.
 //
 //   host_driver DIR
 //
-// DIR holds soliddict.txt, vofdict.txt, blockmesh.txt, field_ascii and field_binary.  Every entry point runs on the
+// DIR holds soliddict.txt, vofdict.txt, blockmesh.txt, field_ascii, field_binary, points_binary, faces_binary and
+// faces_ascii.  Every entry point runs on the
 // whole input, on every prefix of it and on byte-mutated copies, with output and message buffers allocated to their
 // exact capacity (so a write past the end is reported).  Any sanitizer report aborts the process; exit 0 = clean.
 #include <algorithm>
@@ -64,7 +65,33 @@ static void parse_all(const std::string& t, int n_states) {
     }
 }
 
+static void read_all(const std::string& f) {
+    std::vector<char> msg(40);
+    for (int kind = SDFIBM_FOAM_SCALAR; kind <= SDFIBM_FOAM_LABEL; ++kind) {
+        int64_t n = 0;
+        if (sdfibm_host_read_foam_list(f.data(), (int64_t)f.size(), kind, nullptr, 0, &n, msg.data(),
+                                       (int32_t)msg.size()) != SDFIBM_OK)
+            continue;
+        const int64_t m = n < 0 ? 1 : n;
+        std::vector<double> d((size_t)(3 * m + 1));
+        std::vector<int32_t> l((size_t)(m + 1));
+        void* out = kind == SDFIBM_FOAM_LABEL ? (void*)l.data() : (void*)d.data();
+        sdfibm_host_read_foam_list(f.data(), (int64_t)f.size(), kind, out, m, &n, msg.data(), (int32_t)msg.size());
+        if (m > 1) sdfibm_host_read_foam_list(f.data(), (int64_t)f.size(), kind, out, m - 1, &n, msg.data(), 8);
+    }
+    int64_t nf = 0, nl = 0;
+    if (sdfibm_host_read_foam_faces(f.data(), (int64_t)f.size(), nullptr, 0, nullptr, 0, &nf, &nl, msg.data(),
+                                    (int32_t)msg.size()) == SDFIBM_OK) {
+        std::vector<int32_t> off((size_t)nf + 1), lab((size_t)nl + 1);
+        sdfibm_host_read_foam_faces(f.data(), (int64_t)f.size(), off.data(), nf + 1, lab.data(), nl, &nf, &nl,
+                                    msg.data(), (int32_t)msg.size());
+        sdfibm_host_read_foam_faces(f.data(), (int64_t)f.size(), off.data(), nf, lab.data(), nl, &nf, &nl,
+                                    msg.data(), (int32_t)msg.size());
+    }
+}
+
 static void field_all(const std::string& f) {
+    read_all(f);
     std::vector<char> msg(40);
     const int64_t n = 37;
     std::vector<double> v((size_t)n);
@@ -91,7 +118,9 @@ int main(int argc, char** argv) {
     const std::string dir = argv[1];
     const std::string texts[3] = {slurp(dir + "/soliddict.txt"), slurp(dir + "/vofdict.txt"),
                                   slurp(dir + "/blockmesh.txt")};
-    const std::string fields[2] = {slurp(dir + "/field_ascii"), slurp(dir + "/field_binary")};
+    const std::string fields[5] = {slurp(dir + "/field_ascii"), slurp(dir + "/field_binary"),
+                                   slurp(dir + "/points_binary"), slurp(dir + "/faces_binary"),
+                                   slurp(dir + "/faces_ascii")};
     // states for the restart writer: as many as the full solidDict has solids
     sdfibm_solid_desc solids[32];
     int32_t ns = 0, twod = 0;
@@ -116,6 +145,26 @@ int main(int argc, char** argv) {
             std::string m = f;
             for (int j = 0; j < 2; ++j) m[(size_t)(lcg(seed) >> 33) % m.size()] = (char)(lcg(seed) >> 56);
             field_all(m);
+        }
+    }
+    // the lattice test on a small block and on points that are not one
+    {
+        std::vector<double> pts;
+        for (int k = 0; k < 3; ++k)
+            for (int j = 0; j < 3; ++j)
+                for (int i = 0; i < 4; ++i) {
+                    pts.push_back(0.5 * i);
+                    pts.push_back(0.25 * j);
+                    pts.push_back((double)k);
+                }
+        sdfibm_mesh_desc m;
+        std::vector<char> msg(24);
+        for (int64_t np = 0; np <= (int64_t)pts.size() / 3; ++np, ++calls)
+            sdfibm_host_uniform_mesh(pts.data(), np, 12, 1e-9, &m, msg.data(), (int32_t)msg.size());
+        for (int k = 0; k < 100; ++k, ++calls) {
+            std::vector<double> q = pts;
+            q[(size_t)(lcg(seed) >> 33) % q.size()] = (double)((lcg(seed) >> 40) % 7) - 3.0;
+            sdfibm_host_uniform_mesh(q.data(), (int64_t)q.size() / 3, 12, 1e-9, &m, msg.data(), (int32_t)msg.size());
         }
     }
     // the record writers at every capacity below what they need

@@ -2,7 +2,7 @@
 
 Two drivers are compiled with g++ -fsanitize=address,undefined and run; a sanitizer report aborts them:
   - tests/sanitize/host_driver.cpp drives the host half of the library (sdfibm_gb300/csrc/host.cpp). Inputs are
-    the solidDict, VOF-dict, blockMesh and field-file front ends and writers: every prefix of each input,
+    the solidDict, VOF-dict, blockMesh, OpenFOAM list and field-file front ends and writers: every prefix of each input,
     byte-mutated copies, and output buffers of every capacity below what is needed;
   - tests/sanitize/oracle_driver.cpp drives the oracle: both modes, 2-D and 3-D, every shape, interact, evolve with
     collisions (solids that coincide, leave the mesh or go non-finite), fixInternal and the mean field.
@@ -42,6 +42,14 @@ def test_host_code_under_sanitizers(cuda_lib, tmp_path):
     (d / "blockmesh.txt").write_text(BLOCKMESH)
     (d / "field_ascii").write_text(FIELD)
     (d / "field_binary").write_bytes(write_scalar_field(FIELD.encode(), np.linspace(0, 1, 50), "binary"))
+    from test_foam_io import _header, _list, lattice
+    (d / "points_binary").write_bytes(_header("binary", "vectorField", "points") +
+                                      _list(lattice((3, 2, 2)), "binary", "vector"))
+    off, lab = np.array([0, 4, 8, 11], np.int32), np.array([0, 1, 5, 4, 1, 2, 6, 5, 3, 7, 8], np.int32)
+    (d / "faces_binary").write_bytes(_header("binary", "faceCompactList", "faces") + _list(off, "binary", "label") +
+                                     _list(lab, "binary", "label"))
+    (d / "faces_ascii").write_bytes(_header("ascii", "faceList", "faces") +
+                                    b"3\n(\n4(0 1 5 4)\n4(1 2 6 5)\n3(3 7 8)\n)\n")
     exe = str(tmp_path / "host_driver")
     _compile(exe, ["tests/sanitize/host_driver.cpp", "sdfibm_gb300/csrc/host.cpp"])
     r = subprocess.run([exe, str(d)], capture_output=True, text=True, env=ENV, timeout=600)
