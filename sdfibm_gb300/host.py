@@ -227,3 +227,10 @@ class StateFile:
         self.f.close()
         if self.mf is not None:
             self.mf.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+        return False

@@ -126,10 +126,10 @@ def test_state_records(cuda_lib, twod):
 
 def test_state_file_frequency(cuda_lib, tmp_path):
     st = _states(3, 4)
-    f = StateFile(str(tmp_path / "cloud.out"), twod=False, write_frequency=2)
-    for k in range(5):
-        f.save(0.1 * k, st)
-    f.close()
+    with StateFile(str(tmp_path / "cloud.out"), twod=False, write_frequency=2) as f:
+        for k in range(5):
+            f.save(0.1 * k, st)
+    assert f.f.closed
     rows = [l.split() for l in open(tmp_path / "cloud.out").read().splitlines()]
     # calls 0, 2 and 4 write: three blocks of three solids
     assert len(rows) == 9
