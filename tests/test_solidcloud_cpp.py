@@ -1,8 +1,9 @@
 """The C++ SolidCloud of include/sdfibm_cloud.hpp (the reference's interface over the C ABI, host fields).
 
 CPU: the header and the time-loop client of tests/cpp_client/cloud_client.cpp compile with -Wall -Wextra -Werror
-and link against libsdfibm_cuda.so.  GPU: the client's cloud.out, meanfield.out and restart dictionary agree with
-what the Python SolidCloud writes for the same loop on device fields (the same kernels behind both)."""
+and link against libsdfibm_cuda.so; linked instead against a stand-in library that the oracle answers, the client
+writes what the same loop written with the oracle directly writes.  GPU: the client's cloud.out, meanfield.out and
+restart dictionary agree with what the Python SolidCloud writes for the same loop on device fields."""
 import os
 import shutil
 import subprocess
@@ -50,6 +51,83 @@ def test_cpp_cloud_compiles(cuda_lib, tmp_path):
     _client(tmp_path)
 
 
+def _case_files(tmp_path):
+    N = MESH[0] * MESH[1] * MESH[2]
+    rng = np.random.default_rng(3)
+    U = (rng.standard_normal((3, N)) * 0.05).astype(np.float32)
+    U[0] += np.float32(0.2)
+    (tmp_path / "solidDict").write_text(DICT)
+    (tmp_path / "mesh.txt").write_text(" ".join(repr(v) for v in MESH))
+    U.tofile(str(tmp_path / "U.bin"))
+    return U
+
+
+def _run(exe, tmp_path, out):
+    out.mkdir()
+    r = subprocess.run([exe, str(tmp_path / "solidDict"), str(tmp_path / "mesh.txt"), str(tmp_path / "U.bin"),
+                        str(STEPS), repr(DT), str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    return r.stdout
+
+
+def test_cpp_cloud_on_the_oracle(cuda_lib, tmp_path):
+    """The C++ SolidCloud's own logic (construction with initialCorrect, saveState every writeFrequency calls, the
+    mean field from two passes of a sampler context with its Ct writes, the host fixInternal, saveRestart) on CPU:
+    the time-loop client linked against a stand-in library whose entry points the oracle answers
+    (tests/cpp_client/oracle_abi_shim.cpp), against the same loop written with the oracle directly."""
+    cxx = shutil.which(os.environ.get("CXX", "g++"))
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    from oracle.oracle import OracleCloud
+    from sdfibm_gb300 import abi
+    from sdfibm_gb300.host import format_mean_field, format_state, parse_soliddict, soliddict_shape, write_restart
+    shim = tmp_path / "shim"
+    shim.mkdir()
+    inc = ["-I", os.path.join(ROOT, "include")]
+    r = subprocess.run([cxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off"] + inc +
+                       [os.path.join(ROOT, f) for f in ("tests/cpp_client/oracle_abi_shim.cpp", "oracle/oracle.cpp",
+                                                        "sdfibm_gb300/csrc/host.cpp")] +
+                       ["-o", str(shim / "libsdfibm_cuda.so"), "-pthread"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    exe = str(shim / "client")
+    r = subprocess.run([cxx, "-std=c++17", "-Wall", "-Wextra", "-Werror"] + inc +
+                       [os.path.join(ROOT, "tests", "cpp_client", "cloud_client.cpp"), "-o", exe, "-L", str(shim),
+                        "-l:libsdfibm_cuda.so", "-Wl,-rpath," + str(shim)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    U = _case_files(tmp_path)
+    stdout = _run(exe, tmp_path, tmp_path / "cpp")
+    assert "solids 4" in stdout
+
+    # the same loop on the oracle, written out directly
+    solids, opt, twod = parse_soliddict(DICT, 1.0)
+    mesh = abi.mesh_desc(MESH[:3], MESH[3:6], MESH[6:], twod=twod)
+    oc = OracleCloud(mesh, solids, opt, faithful=False)
+    f = oc.new_fields()
+    Uo = U.astype(np.float64).reshape(-1)
+    oc.interact(0.0, 1.0, Uo, f)                                  # initialCorrect
+    st = oc.get_state()
+    for x in st:
+        for a in range(3):
+            x.force[a] = x.torque[a] = 0.0
+    oc.set_state(st)
+    sampler = soliddict_shape(DICT, "probe")
+    state, means = [], []
+    for call in range(STEPS + 1):
+        t = call * DT
+        if call:
+            oc.interact(t, DT, Uo, f)
+            oc.evolve(t, DT)
+        if call % 2 == 0:                                         # writeFrequency 2
+            state.append(format_state(t, list(oc.get_state()), True))
+        means.append(oc.mean_field(sampler, Uo))
+    assert (tmp_path / "cpp" / "cloud.out").read_text() == "".join(state)
+    got = np.array([[float(v) for v in l.split()] for l in (tmp_path / "cpp" / "meanfield.out").read_text().splitlines()])
+    want = np.array([[float(v) for v in format_mean_field(m).split()] for m in means])
+    assert got.shape == want.shape and np.allclose(got, want, rtol=2e-6, atol=1e-12)
+    restart = write_restart(DICT, list(oc.get_state()), True, precision=17, stamp="x").splitlines()[:-1]
+    assert (tmp_path / "cpp" / "solidDict.restart").read_text().splitlines()[:-1] == restart
+
+
 @pytest.mark.gpu
 def test_cpp_cloud_matches_python(cuda_lib, torch_cuda, tmp_path):
     torch = torch_cuda
@@ -57,18 +135,9 @@ def test_cpp_cloud_matches_python(cuda_lib, torch_cuda, tmp_path):
     from sdfibm_gb300.cloud import SolidCloud
     from sdfibm_gb300.host import StateFile, parse_soliddict, soliddict_shape
     exe = _client(tmp_path)
-    N = MESH[0] * MESH[1] * MESH[2]
-    rng = np.random.default_rng(3)
-    U = (rng.standard_normal((3, N)) * 0.05).astype(np.float32)
-    U[0] += np.float32(0.2)
+    U = _case_files(tmp_path)
     out = tmp_path / "cpp"
-    out.mkdir()
-    (tmp_path / "solidDict").write_text(DICT)
-    (tmp_path / "mesh.txt").write_text(" ".join(repr(v) for v in MESH))
-    U.tofile(str(tmp_path / "U.bin"))
-    r = subprocess.run([exe, str(tmp_path / "solidDict"), str(tmp_path / "mesh.txt"), str(tmp_path / "U.bin"),
-                        str(STEPS), repr(DT), str(out)], capture_output=True, text=True, timeout=300)
-    assert r.returncode == 0, r.stderr
+    _run(exe, tmp_path, out)
 
     # the same loop through the Python binding, device fields
     solids, opt, twod = parse_soliddict(DICT, 1.0)
