@@ -992,7 +992,7 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                     }
                     out[local_index(a, b, c)] = cls;
                 }
-                // compact the cut candidates of this round
+                // compact the cut candidates of this pass
                 const bool is_cut = (cls == 2 || cls == 3) && METHOD >= 0;
                 const unsigned bal = __ballot_sync(FULL, is_cut);
                 if (is_cut) {
