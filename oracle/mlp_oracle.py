@@ -1,6 +1,6 @@
 """CPU oracle of the learned cut-cell fraction model: TEST INFRASTRUCTURE ONLY.
 
-Only tests, the smoke check and the bench's CPU legs import this module, as the checker of the GPU kernels in
+Only tests, the smoke check and the bench's CPU legs import this module, to check the GPU kernels in
 sdfibm_gb300/csrc/mlp.cu.  It has no counterpart in the reference, which computes As only with the apex/pyramid
 geometry (geometrictools.cpp:47-116).  It restates the model so that the GPU forward pass, backward pass and
 trainer can be compared term by term:

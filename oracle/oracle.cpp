@@ -1,7 +1,7 @@
 // TEST INFRASTRUCTURE ONLY (the oracle).
 //
 // CPU FP64 restatement of sdfibm's fluid-solid coupling path, used by tests/, __graft_entry__.smoke() and the
-// cpu_baseline leg of bench.py as the checker and as the timed CPU baseline; nothing in the product loads it.
+// cpu_baseline leg of bench.py to check the GPU path and as the timed CPU baseline; nothing in the product loads it.
 // It follows the reference line by line:
 //   SolidCloud::interact / solidFluidInteract / checkAlpha / fixInternal / evolve / addMidEnvironment /
 //   solidSolidInteract / solidSolidCollision   src/solidcloud.cpp:288-301, 361-433, 435-464, 466-570

@@ -1,4 +1,4 @@
-"""The oracle's fast mode (the checker of every GPU parity test) against its faithful mode (the reference's own data
+"""The oracle's fast mode (the reference side of every GPU parity test) against its faithful mode (the reference's own data
 structures: per-solid cell-type arrays, std::set, the phi cache, the full-mesh nearest-cell search), on CPU.
 Both must give the same bits for interact, evolve and fixInternal."""
 import numpy as np
