@@ -1,11 +1,13 @@
 """Address and undefined-behaviour sanitizer builds of the host code, on CPU.
 
-Two drivers are compiled with g++ -fsanitize=address,undefined and run; a sanitizer report aborts them:
+Three drivers are compiled with g++ -fsanitize=address,undefined and run; a sanitizer report aborts them:
   - tests/sanitize/host_driver.cpp drives the host half of the library (sdfibm_gb300/csrc/host.cpp). Inputs are
     the solidDict, VOF-dict, blockMesh, OpenFOAM list and field-file front ends and writers: every prefix of each input,
     byte-mutated copies, and output buffers of every capacity below what is needed;
   - tests/sanitize/oracle_driver.cpp drives the oracle: both modes, 2-D and 3-D, every shape, interact, evolve with
-    collisions (solids that coincide, leave the mesh or go non-finite), fixInternal and the mean field.
+    collisions (solids that coincide, leave the mesh or go non-finite), fixInternal and the mean field;
+  - tests/cpp_client/cloud_client.cpp drives the C++ SolidCloud (include/sdfibm_cloud.hpp) through the reference's
+    time loop, the device entry points answered by the oracle.
 The device half has no sanitizer run here."""
 import os
 import shutil
@@ -64,3 +66,19 @@ def test_oracle_under_sanitizers(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, env=ENV, timeout=600)
     assert r.returncode == 0, (r.stdout + r.stderr)[-4000:]
     assert "calls clean" in r.stdout
+
+
+def test_cpp_solidcloud_under_sanitizers(tmp_path):
+    """The C++ SolidCloud of include/sdfibm_cloud.hpp through its time-loop client, with the device entry points
+    answered by the oracle (tests/cpp_client/oracle_abi_shim.cpp), everything built with the sanitizers."""
+    from test_solidcloud_cpp import STEPS, DT, _case_files
+    exe = str(tmp_path / "client")
+    _compile(exe, ["tests/cpp_client/cloud_client.cpp", "tests/cpp_client/oracle_abi_shim.cpp", "oracle/oracle.cpp",
+                   "sdfibm_gb300/csrc/host.cpp"], ["-pthread"])
+    _case_files(tmp_path)
+    (tmp_path / "out").mkdir()
+    r = subprocess.run([exe, str(tmp_path / "solidDict"), str(tmp_path / "mesh.txt"), str(tmp_path / "U.bin"),
+                        str(STEPS), repr(DT), str(tmp_path / "out")], capture_output=True, text=True, env=ENV,
+                       timeout=600)
+    assert r.returncode == 0, (r.stdout + r.stderr)[-4000:]
+    assert "solids 4" in r.stdout and (tmp_path / "out" / "meanfield.out").exists()
