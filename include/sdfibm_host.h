@@ -114,6 +114,12 @@ int sdfibm_host_write_scalar_field(const char* file, int64_t file_len, const dou
                                    int32_t format, int32_t precision, char* buf, int64_t cap, int64_t* len, char* msg,
                                    int32_t msg_len);
 
+/* The same for a volVectorField file: values holds n (x, y, z) triples (e.g. Fs or U transposed from the cell-major
+ * planes), written as `nonuniform List<vector>`. */
+int sdfibm_host_write_vector_field(const char* file, int64_t file_len, const double* values, int64_t n,
+                                   int32_t format, int32_t precision, char* buf, int64_t cap, int64_t* len, char* msg,
+                                   int32_t msg_len);
+
 /* ---- OpenFOAM list files: polyMesh points / faces / owner / neighbour and field internalFields ---------------------
  * file: the file's bytes (ascii or binary per its FoamFile format; binary lists hold little-endian 8-byte scalars and
  * 4-byte labels, the reference's build).  out == NULL only measures. */

@@ -28,7 +28,7 @@ HOST_SYMBOLS = [
     "sdfibm_host_format_state", "sdfibm_host_write_restart", "sdfibm_host_soliddict_lookup",
     "sdfibm_host_format_mean_field", "sdfibm_host_parse_vofdict", "sdfibm_host_parse_blockmesh",
     "sdfibm_host_write_scalar_field", "sdfibm_host_soliddict_shape", "sdfibm_host_read_foam_list",
-    "sdfibm_host_read_foam_faces", "sdfibm_host_uniform_mesh",
+    "sdfibm_host_read_foam_faces", "sdfibm_host_uniform_mesh", "sdfibm_host_write_vector_field",
 ]
 
 
@@ -89,6 +89,8 @@ def load():
     L.sdfibm_host_soliddict_lookup.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, i64, P(i64)]
     L.sdfibm_host_format_mean_field.argtypes = [vp, i32, C.c_char_p, i64, P(i64)]
     L.sdfibm_host_parse_vofdict.argtypes = [C.c_char_p, i32, P(abi.SolidDesc), i32, P(i32), P(i32), C.c_char_p, i32]
+    L.sdfibm_host_write_vector_field.argtypes = [C.c_char_p, i64, vp, i64, i32, i32, C.c_char_p, i64, P(i64),
+                                                 C.c_char_p, i32]
     L.sdfibm_host_read_foam_list.argtypes = [C.c_char_p, i64, i32, vp, i64, P(i64), C.c_char_p, i32]
     L.sdfibm_host_read_foam_faces.argtypes = [C.c_char_p, i64, vp, i64, vp, i64, P(i64), P(i64), C.c_char_p, i32]
     L.sdfibm_host_uniform_mesh.argtypes = [vp, i64, i64, dbl, P(abi.MeshDesc), C.c_char_p, i32]

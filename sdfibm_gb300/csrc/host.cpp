@@ -967,13 +967,16 @@ extern "C" int sdfibm_host_parse_blockmesh(const char* text, sdfibm_mesh_desc* m
     return SDFIBM_OK;
 }
 
-extern "C" int sdfibm_host_write_scalar_field(const char* file, int64_t file_len, const double* values, int64_t n,
-                                              int32_t format, int32_t precision, char* buf, int64_t cap, int64_t* len,
-                                              char* msg, int32_t msg_len) {
+namespace {
+
+// the internalField of a vol<Type>Field file replaced by n values of `width` components (1: scalar, 3: vector)
+int write_field(const char* file, int64_t file_len, const double* values, int64_t n, int width, int32_t format,
+                int32_t precision, char* buf, int64_t cap, int64_t* len, char* msg, int32_t msg_len) {
     if (!file || file_len < 0 || (n > 0 && !values) || n < 0 || !len || precision < 0 || precision > 17 ||
         format < -1 || format > 1)
         return set_msg(msg, msg_len, "bad argument", SDFIBM_ERR_ARG);
     const std::string src(file, (size_t)file_len);
+    const std::string list_type = width == 3 ? "List<vector>" : "List<scalar>";
     try {
         // the header's format (FoamFile { format ascii|binary; }): the text before the first binary byte
         const size_t hdr = src.find("FoamFile");
@@ -1037,18 +1040,25 @@ extern "C" int sdfibm_host_write_scalar_field(const char* file, int64_t file_len
             end = src.find(';', p);
         } else if (kind == "nonuniform") {
             const std::string lt = word();
-            if (lt != "List<scalar>") throw std::runtime_error("internalField is not a List<scalar>");
+            if (lt != list_type) throw std::runtime_error("internalField is not a " + list_type);
             const std::string cnt = word();
             const long long m = std::stoll(cnt);
             skip_ws();
             if (p >= src.size() || src[p] != '(') throw std::runtime_error("bad internalField list");
-            if (m < 0 || (uint64_t)m > (uint64_t)(src.size() - p) / 8) throw std::runtime_error("bad internalField size");
+            // an element takes 8 bytes per component in binary, and at least 2 bytes in ascii
+            if (m < 0 || (uint64_t)m > (uint64_t)(src.size() - p) / (binary ? 8 * (uint64_t)width : 2))
+                throw std::runtime_error("bad internalField size");
             if (binary) {
-                p += 1 + (size_t)m * 8;
+                p += 1 + (size_t)m * 8 * (size_t)width;
                 if (p >= src.size() || src[p] != ')') throw std::runtime_error("bad binary internalField list");
             } else {
-                p = src.find(')', p);
-                if (p == std::string::npos) throw std::runtime_error("unterminated internalField list");
+                // the closing parenthesis of the list (vector elements hold their own)
+                int depth = 0;
+                for (++p; p < src.size(); ++p) {
+                    if (src[p] == '(') ++depth;
+                    else if (src[p] == ')' && depth-- == 0) break;
+                }
+                if (p >= src.size()) throw std::runtime_error("unterminated internalField list");
             }
             end = src.find(';', p);
         } else {
@@ -1056,14 +1066,23 @@ extern "C" int sdfibm_host_write_scalar_field(const char* file, int64_t file_len
         }
         if (end == std::string::npos) throw std::runtime_error("unterminated internalField");
         std::string out = head + src.substr(hend + 1, key - hend - 1);
-        out += "internalField   nonuniform List<scalar> \n" + std::to_string(n) + "\n(";
+        out += "internalField   nonuniform " + list_type + " \n" + std::to_string(n) + "\n(";
         if (out_binary) {
-            out.append(reinterpret_cast<const char*>(values), (size_t)n * 8);  // little-endian doubles, as read
+            out.append(reinterpret_cast<const char*>(values), (size_t)(n * width) * 8);  // little-endian doubles
         } else {
             const int prec = precision ? precision : 6;
             out += "\n";
             for (int64_t i = 0; i < n; ++i) {
-                out += put_g(values[i], prec);
+                if (width == 1) {
+                    out += put_g(values[i], prec);
+                } else {
+                    out += "(";
+                    for (int a = 0; a < width; ++a) {
+                        if (a) out += ' ';
+                        out += put_g(values[i * width + a], prec);
+                    }
+                    out += ")";
+                }
                 out += "\n";
             }
         }
@@ -1074,6 +1093,20 @@ extern "C" int sdfibm_host_write_scalar_field(const char* file, int64_t file_len
     } catch (const std::exception& e) {
         return set_msg(msg, msg_len, e.what(), SDFIBM_ERR_ARG);
     }
+}
+
+}  // namespace
+
+extern "C" int sdfibm_host_write_scalar_field(const char* file, int64_t file_len, const double* values, int64_t n,
+                                              int32_t format, int32_t precision, char* buf, int64_t cap, int64_t* len,
+                                              char* msg, int32_t msg_len) {
+    return write_field(file, file_len, values, n, 1, format, precision, buf, cap, len, msg, msg_len);
+}
+
+extern "C" int sdfibm_host_write_vector_field(const char* file, int64_t file_len, const double* values, int64_t n,
+                                              int32_t format, int32_t precision, char* buf, int64_t cap, int64_t* len,
+                                              char* msg, int32_t msg_len) {
+    return write_field(file, file_len, values, n, 3, format, precision, buf, cap, len, msg, msg_len);
 }
 
 // One shape of a solidDict's library by name (meta.sampler names one, src/solidcloud.cpp:38, 308)

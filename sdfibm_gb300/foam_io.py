@@ -1,8 +1,10 @@
-"""OpenFOAM file input through the host half of libsdfibm_cuda.so (include/sdfibm_host.h): the lists of polyMesh files
-and field internalFields, ascii or binary, and the uniform mesh a single-block polyMesh describes.
+"""OpenFOAM file input and field output through the host half of libsdfibm_cuda.so (include/sdfibm_host.h): the
+lists of polyMesh files and field internalFields, ascii or binary, vol field files with a new internalField, and the
+uniform mesh a single-block polyMesh describes.
 
     read_list(path, "vector")            points (N, 3); "label" for owner / neighbour; "scalar" for scalar fields
     read_faces(path)                     (offsets, labels) of a faceCompactList or faceList
+    write_field(template, values)        a vol field file with its internalField set (scalars or vectors)
     uniform_mesh_from_polymesh(dir)      abi.MeshDesc of constant/polyMesh when it is one uniform block
 """
 import ctypes as C
@@ -58,6 +60,29 @@ def read_faces(path_or_bytes):
                                      512) != abi.OK:
         raise HostError(msg.value.decode())
     return off, lab[:nl.value]
+
+
+def write_field(template, values, fmt=None, precision=6):
+    """The bytes of an OpenFOAM vol field file: template (bytes of a volScalarField or volVectorField file) with its
+    internalField set to values, (N,) scalars or (N, 3) vectors (a cell-major (3, N) field is transposed first).
+    fmt: None keeps the template's format, else "ascii" or "binary"."""
+    v = np.asarray(values, dtype=np.float64)
+    if v.ndim == 2 and v.shape[0] == 3 and v.shape[1] != 3:
+        v = v.T
+    vector = v.ndim == 2
+    v = np.ascontiguousarray(v)
+    f = {None: -1, "ascii": 0, "binary": 1}[fmt]
+    L = load()
+    fn = L.sdfibm_host_write_vector_field if vector else L.sdfibm_host_write_scalar_field
+    n = C.c_int64(0)
+    msg = C.create_string_buffer(512)
+    args = (template, len(template), v.ctypes.data_as(C.c_void_p), len(v), f, int(precision))
+    if fn(*args, None, 0, C.byref(n), msg, 512) != abi.OK:
+        raise HostError(msg.value.decode())
+    buf = C.create_string_buffer(n.value + 1)
+    if fn(*args, buf, n.value + 1, C.byref(n), msg, 512) != abi.OK:
+        raise HostError(msg.value.decode())
+    return buf.raw[:n.value]
 
 
 def uniform_mesh(points, ncells, rtol=1e-9):

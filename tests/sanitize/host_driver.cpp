@@ -107,6 +107,12 @@ static void field_all(const std::string& f) {
         std::vector<char> s((size_t)len);
         sdfibm_host_write_scalar_field(f.data(), (int64_t)f.size(), v.data(), n, fmt, 9, s.data(), (int64_t)s.size(),
                                        &len, msg.data(), (int32_t)msg.size());
+        if (sdfibm_host_write_vector_field(f.data(), (int64_t)f.size(), v.data(), n / 3, fmt, 9, nullptr, 0, &len,
+                                           msg.data(), (int32_t)msg.size()) == SDFIBM_OK) {
+            std::vector<char> vb((size_t)len);
+            sdfibm_host_write_vector_field(f.data(), (int64_t)f.size(), v.data(), n / 3, fmt, 9, vb.data(),
+                                           (int64_t)vb.size(), &len, msg.data(), (int32_t)msg.size());
+        }
     }
 }
 

@@ -150,3 +150,29 @@ def test_nul_bytes_in_the_header(cuda_lib):
     from test_vof import FIELD
     data = FIELD.replace("version     2.0;", "version \x00 2.0;").encode()
     assert b"\n3\n(" in write_scalar_field(data, [0.5, 0.25, 1.0], "ascii")
+
+
+@pytest.mark.parametrize("fmt", ["ascii", "binary"])
+def test_vector_field_writer(cuda_lib, fmt):
+    from sdfibm_gb300.foam_io import read_list, write_field
+    from test_vof import FIELD
+    template = FIELD.replace("volScalarField", "volVectorField").replace("uniform 0;", "uniform (0 0 0);").encode()
+    Fs = np.random.default_rng(6).normal(size=(3, 40))          # cell-major planes, as the coupling returns them
+    data = write_field(template, Fs, fmt, precision=17)
+    got, uniform = read_list(data, "vector")
+    assert not uniform and np.array_equal(got, Fs.T)
+    again = write_field(data, Fs.T[::-1], None, precision=17)   # the written file as the next template
+    assert np.array_equal(read_list(again, "vector")[0], Fs.T[::-1])
+    assert again.endswith(b"boundaryField\n{\n    left { type zeroGradient; }\n    right { type zeroGradient; }\n"
+                          b"    frontAndBack { type empty; }\n}\n")
+
+
+def test_ascii_rewrite_of_short_entries(cuda_lib):
+    """A VOF field written at 6 digits is mostly "0" and "1": rewriting it must not take its size as too large."""
+    from sdfibm_gb300.foam_io import read_list, write_field
+    from test_vof import FIELD
+    v = np.zeros(5000)
+    v[::7] = 1.0
+    data = write_field(FIELD.encode(), v, "ascii")
+    again = write_field(data, v[::-1], "ascii")
+    assert np.array_equal(read_list(again, "scalar")[0], v[::-1])
