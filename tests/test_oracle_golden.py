@@ -1,5 +1,7 @@
-"""The oracle pinned against the reference's shipped artefacts (CPU)."""
+"""The oracle pinned against the reference's shipped artefacts (CPU), and the library against the same artefacts
+(GPU)."""
 import numpy as np
+import pytest
 
 from conftest import golden
 from oracle.oracle import OracleCloud
@@ -61,3 +63,65 @@ def test_falling_ellipse_uniform_matches_polymesh():
     assert np.abs(f["As"][cells] - g["As"]).max() < 1e-12
     assert np.abs(f["Fs"].reshape(3, N)[:, cells] - g["Fs"]).max() < 1e-9
     assert np.abs(FT - g["FT"]).max() < 1e-12 * np.abs(g["FT"]).max() + 1e-15
+
+
+@pytest.mark.gpu
+def test_re200_golden_on_the_gpu(cuda_lib, torch_cuda):
+    """The library's initialCorrect pass (interact(0, 1), REF-GEO) against the As the reference ships for re200: the
+    same cells as the oracle, FP32 fractions within the coupling tolerance of the shipped FP64 values."""
+    torch = torch_cuda
+    from sdfibm_gb300.cloud import SolidCloud
+    g = golden("re200_As.npz")
+    mesh = abi.mesh_desc((120, 120, 1), g["origin"], g["h"], twod=1)
+    solid = make_solid(0, make_shape("Circle", radius=1.0), 1.0, (0, 0, 0), motion=mask_motion("b000000"))
+    cloud = SolidCloud(mesh, [solid], abi.options(rho_f=1.0))
+    f = cloud.new_fields()
+    cloud.interact(0.0, 1.0, torch.zeros((3, 14400), dtype=torch.float32, device="cuda"), f)
+    got = f["As"].cpu().numpy().astype(np.float64).reshape(120, 120)
+    cells, _ = cloud.touched(0)
+    cloud.close()
+    _, orc = re200_case(faithful=False)
+    assert len(cells) == (orc > 0).sum() == 346
+    ref = g["As"].reshape(120, 120)
+    mask = np.ones_like(ref, dtype=bool)
+    for j, i in RE200_FLAGGED:
+        mask[j, i] = False
+    # the 5 cells at blockMesh rounding level hold < 1e-9 in the shipped field and 0 here, as in the oracle
+    assert (np.abs(got - ref)[mask] <= 1e-5 * ref[mask] + 1e-9).all()
+    # 344 cells above 1e-9 (two cut cells hold 3.5e-11 in FP64), 276 of them at 1
+    assert (got > 1e-9).sum() == 344 and (got == 1).sum() == 276
+    assert 0.6 < got[50, 57] < 0.7
+
+
+@pytest.mark.gpu
+def test_falling_ellipse_golden_on_the_gpu(cuda_lib, torch_cuda):
+    """The library on the uniform form of examples/falling_ellipse against the oracle's run on the reference's own
+    polyMesh: touched cells and types exact, As and Fs within the coupling tolerance, force and torque within 1e-6."""
+    torch = torch_cuda
+    from sdfibm_gb300.cloud import SolidCloud
+    g = golden("falling_ellipse.npz")
+    shape = make_shape("Ellipse", radiusa=0.3, radiusb=0.15)
+    solid = make_solid(0, shape, 2.0, (0.5, 3.5, 0.0), (0.0, 0.0, -45.0), motion=mask_motion("b111111"))
+    mesh = abi.mesh_desc((100, 200, 1), (0.0, 0.0, -0.5), (0.02, 0.02, 1.0), twod=1)
+    N = 20000
+    rng = np.random.default_rng(int(g["U_seed"]))
+    U = rng.standard_normal((3, N), dtype=np.float32) * np.float32(g["U_std"])
+    cloud = SolidCloud(mesh, [solid], abi.options(rho_f=1.0))
+    f = cloud.new_fields()
+    FT = cloud.interact(0.0, float(g["dt"]), torch.from_numpy(U).cuda(), f)
+    cells, types = cloud.touched(0)
+    As = f["As"].cpu().numpy().astype(np.float64)
+    Fs = f["Fs"].cpu().numpy().astype(np.float64).reshape(3, N)
+    cloud.close()
+    assert np.array_equal(cells, g["cells"]) and np.array_equal(types, g["types"])
+    assert (np.abs(As[cells] - g["As"]) <= 1e-5 * np.abs(g["As"]) + 1e-9).all()
+    assert (np.abs(Fs[:, cells] - g["Fs"]) <= 1e-5 * np.abs(g["Fs"]) + 1e-7 * np.abs(g["Fs"]).max()).all()
+    # force and torque normwise within 1e-6 of the sum of the per-cell contributions' magnitudes (the coupling's bar)
+    V = 0.02 * 0.02 * 1.0
+    i, j = cells % 100, cells // 100
+    r = np.stack([(i + 0.5) * 0.02 - 0.5, (j + 0.5) * 0.02 - 3.5, np.zeros(len(cells))])
+    dF = g["Fs"] * V
+    scale_f = np.linalg.norm(dF, axis=0).sum()
+    scale_t = np.linalg.norm(np.cross(r.T, dF.T), axis=1).sum()
+    assert np.linalg.norm(FT[0, :3] - g["FT"][0, :3]) <= 1e-6 * scale_f
+    assert np.linalg.norm(FT[0, 3:] - g["FT"][0, 3:]) <= 1e-6 * scale_t
