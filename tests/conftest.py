@@ -11,6 +11,12 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built libsdfibm_cuda.so")
+    config.addinivalue_line("markers", "first_gpu_run: a GPU test that has not yet run on a GPU (ordered last)")
+
+
+def pytest_collection_modifyitems(config, items):
+    # tests that have not yet run on a GPU go last, so that under -x a failure there hides no other result
+    items.sort(key=lambda it: it.get_closest_marker("first_gpu_run") is not None)
 
 
 @pytest.fixture(scope="session")
