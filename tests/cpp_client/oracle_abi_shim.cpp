@@ -1,12 +1,14 @@
-// TEST DOUBLE: the host-field entry points of sdfibm_cuda.h answered by the oracle (oracle/oracle.cpp, the FP64 CPU
-// restatement) instead of the GPU, so that the C++ SolidCloud of include/sdfibm_cloud.hpp and its time-loop client
-// run on a machine without a GPU.  Linked with oracle.cpp and host.cpp into a stand-in libsdfibm_cuda.so that only
-// tests load; the product library is never replaced by it.
+// TEST DOUBLE: the entry points of sdfibm_cuda.h answered by the oracle (oracle/oracle.cpp, the FP64 CPU restatement)
+// instead of the GPU, with every field in host memory, so that the C++ SolidCloud of include/sdfibm_cloud.hpp, its
+// time-loop client and the Python SolidCloud (on CPU tensors) run on a machine without a GPU.  Linked with
+// oracle.cpp and host.cpp into a stand-in libsdfibm_cuda.so that only tests load; the product library is never
+// replaced by it.  Entry points the tests do not use return SDFIBM_ERR_STATE.
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "sdfibm_cuda.h"
+#include "sdfibm_mlp.h"
 
 extern "C" {
 void* oracle_create_uniform(const sdfibm_mesh_desc*, const sdfibm_solid_desc*, int, const sdfibm_options*, int);
@@ -15,6 +17,8 @@ int oracle_interact(void*, double, double, const double*, double*, double*, doub
 int oracle_evolve(void*, double, double);
 int oracle_get_state(void*, sdfibm_solid_state*, int);
 int oracle_set_state(void*, const sdfibm_solid_state*, int);
+int64_t oracle_touched(void*, int, int64_t*, int8_t*, int64_t);
+int oracle_fix_internal(void*, const int32_t*, double*);
 }
 
 struct sdfibm_ctx {
@@ -64,6 +68,70 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* c, double time, double dt, const float
     }
     for (size_t i = 0; i < c->Fs.size(); ++i) Fs[i] = (float)c->Fs[i];
     return SDFIBM_OK;
+}
+
+/* the device-pointer entry point: here every pointer is host memory */
+int sdfibm_cuda_interact(sdfibm_ctx* c, double time, double dt, const float* U, float* As, float* Fs, float* Ts,
+                         int32_t* Ct, double* FT) {
+    return sdfibm_cuda_interact_host(c, time, dt, U, As, Fs, Ts, Ct, FT);
+}
+
+int sdfibm_cuda_fix_internal(sdfibm_ctx* c, const int32_t* Ct, float* U) {
+    if (!c || !Ct || !U) return SDFIBM_ERR_ARG;
+    std::vector<double> u(c->U.size());
+    for (size_t i = 0; i < u.size(); ++i) u[i] = U[i];
+    oracle_fix_internal(c->oc, Ct, u.data());
+    for (size_t i = 0; i < u.size(); ++i) U[i] = (float)u[i];
+    return SDFIBM_OK;
+}
+
+int sdfibm_cuda_touched(sdfibm_ctx* c, int32_t s, int64_t* cells, int8_t* types, int64_t capacity, int64_t* n) {
+    if (!c || !n || s < 0 || s >= c->S) return SDFIBM_ERR_ARG;
+    *n = oracle_touched(c->oc, s, cells, types, cells && types ? capacity : 0);
+    return SDFIBM_OK;
+}
+
+int sdfibm_cuda_stats(sdfibm_ctx* c, int64_t* out, int32_t n) {
+    if (!c || !out) return SDFIBM_ERR_ARG;
+    for (int32_t i = 0; i < n; ++i) out[i] = 0;
+    return SDFIBM_OK;
+}
+
+const char* sdfibm_cuda_version(void) { return "oracle stand-in (no GPU)"; }
+
+int64_t sdfibm_abi_sizeof(int which) {
+    switch (which) {
+        case 0: return sizeof(sdfibm_mesh_desc);
+        case 1: return sizeof(sdfibm_shape_desc);
+        case 2: return sizeof(sdfibm_solid_desc);
+        case 3: return sizeof(sdfibm_solid_state);
+        case 4: return sizeof(sdfibm_options);
+        case 5: return sizeof(sdfibm_mlp_data_desc);
+        case 6: return sizeof(sdfibm_mlp_train_desc);
+        default: return -1;
+    }
+}
+
+// not answered here
+int sdfibm_cuda_kernel_times(sdfibm_ctx*, const char**, double*, int32_t, int32_t*) { return SDFIBM_ERR_STATE; }
+int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc*, const sdfibm_solid_desc*, void*, int32_t*, int8_t*, int64_t,
+                                int64_t*) {
+    return SDFIBM_ERR_STATE;
+}
+int sdfibm_cuda_set_fraction_model(sdfibm_ctx*, const float*, float, float) { return SDFIBM_ERR_STATE; }
+int sdfibm_cuda_autotune(sdfibm_ctx*, double, const float*, float*, float*, float*, int32_t*, int32_t*) {
+    return SDFIBM_ERR_STATE;
+}
+int sdfibm_mlp_dataset(uint64_t, int64_t, const sdfibm_mlp_data_desc*, float*, float*, double*, void*) {
+    return SDFIBM_ERR_STATE;
+}
+int sdfibm_mlp_forward(const float*, const float*, int64_t, int64_t, float*, void*) { return SDFIBM_ERR_STATE; }
+int sdfibm_mlp_loss_grad(const float*, const float*, const float*, int64_t, int64_t, float*, void*) {
+    return SDFIBM_ERR_STATE;
+}
+int sdfibm_mlp_adam(float*, const float*, float*, float*, int32_t, float, void*) { return SDFIBM_ERR_STATE; }
+int sdfibm_mlp_train(float*, const float*, const float*, int64_t, const sdfibm_mlp_train_desc*, float*, void*) {
+    return SDFIBM_ERR_STATE;
 }
 
 int sdfibm_cuda_evolve(sdfibm_ctx* c, double time, double dt) { return c ? oracle_evolve(c->oc, time, dt) : 1; }

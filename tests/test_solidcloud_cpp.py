@@ -2,7 +2,8 @@
 
 CPU: the header and the time-loop client of tests/cpp_client/cloud_client.cpp compile with -Wall -Wextra -Werror
 and link against libsdfibm_cuda.so; linked instead against a stand-in library that the oracle answers, the client
-writes what the same loop written with the oracle directly writes.  GPU: the client's cloud.out, meanfield.out and
+writes what the same loop written with the oracle directly writes, and the Python SolidCloud loaded on that
+stand-in writes the same files.  GPU: the client's cloud.out, meanfield.out and
 restart dictionary agree with what the Python SolidCloud writes for the same loop on device fields."""
 import os
 import shutil
@@ -70,17 +71,11 @@ def _run(exe, tmp_path, out):
     return r.stdout
 
 
-def test_cpp_cloud_on_the_oracle(cuda_lib, tmp_path):
-    """The C++ SolidCloud's own logic (construction with initialCorrect, saveState every writeFrequency calls, the
-    mean field from two passes of a sampler context with its Ct writes, the host fixInternal, saveRestart) on CPU:
-    the time-loop client linked against a stand-in library whose entry points the oracle answers
-    (tests/cpp_client/oracle_abi_shim.cpp), against the same loop written with the oracle directly."""
+def _shim_client(tmp_path):
+    """The stand-in library (the oracle behind the entry points) and the time-loop client linked against it."""
     cxx = shutil.which(os.environ.get("CXX", "g++"))
     if cxx is None:
         pytest.skip("no C++ compiler")
-    from oracle.oracle import OracleCloud
-    from sdfibm_gb300 import abi
-    from sdfibm_gb300.host import format_mean_field, format_state, parse_soliddict, soliddict_shape, write_restart
     shim = tmp_path / "shim"
     shim.mkdir()
     inc = ["-I", os.path.join(ROOT, "include")]
@@ -94,6 +89,62 @@ def test_cpp_cloud_on_the_oracle(cuda_lib, tmp_path):
                        [os.path.join(ROOT, "tests", "cpp_client", "cloud_client.cpp"), "-o", exe, "-L", str(shim),
                         "-l:libsdfibm_cuda.so", "-Wl,-rpath," + str(shim)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+    return exe
+
+
+def _python_loop(torch, U, out, device):
+    """The client's loop through the Python SolidCloud: initialCorrect, saveState (with the mean field), then per
+    step interact, evolve, saveState; a restart dictionary at the end."""
+    from sdfibm_gb300 import abi
+    from sdfibm_gb300.cloud import SolidCloud
+    from sdfibm_gb300.host import StateFile, parse_soliddict, soliddict_shape
+    solids, opt, twod = parse_soliddict(DICT, 1.0)
+    mesh = abi.mesh_desc(MESH[:3], MESH[3:6], MESH[6:], twod=twod)
+    cloud = SolidCloud(mesh, solids, opt)
+    cloud.set_sampler(soliddict_shape(DICT, "probe"))
+    Ud = torch.from_numpy(U).to(device)
+    f = cloud.new_fields(device=device)
+    out.mkdir()
+    with StateFile(str(out / "cloud.out"), twod, 2, mean_field_path=str(out / "meanfield.out")) as sf:
+        cloud.initial_correct(Ud, f)
+        cloud.save_state(sf, Ud, f["Ct"])
+        for s in range(1, STEPS + 1):
+            t = s * DT
+            cloud.interact(t, DT, Ud, f)
+            cloud.evolve(t, DT)
+            cloud.save_state(sf, Ud, f["Ct"])
+    cloud.save_restart(DICT, str(out / "solidDict.restart"), precision=17)
+    cloud.close()
+
+
+def test_python_cloud_on_the_oracle(cuda_lib, tmp_path, monkeypatch):
+    """The Python SolidCloud's orchestration (initial_correct, save_state with the mean field and its Ct writes,
+    save_restart) on CPU tensors, with the stand-in library loaded in place of libsdfibm_cuda.so: its files equal the
+    C++ client's on the same stand-in, byte for byte (the same FP64 arithmetic behind both)."""
+    torch = pytest.importorskip("torch")
+    from sdfibm_gb300 import _lib
+    exe = _shim_client(tmp_path)
+    U = _case_files(tmp_path)
+    _run(exe, tmp_path, tmp_path / "cpp")
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "shim" / "libsdfibm_cuda.so"))
+    monkeypatch.setattr(_lib, "_lib", None)
+    assert b"oracle" in _lib.load().sdfibm_cuda_version()
+    _python_loop(torch, U, tmp_path / "py", "cpu")
+    for name in ("cloud.out", "meanfield.out"):
+        assert (tmp_path / "py" / name).read_text() == (tmp_path / "cpp" / name).read_text(), name
+    a = (tmp_path / "py" / "solidDict.restart").read_text().splitlines()[:-1]
+    assert a == (tmp_path / "cpp" / "solidDict.restart").read_text().splitlines()[:-1]
+
+
+def test_cpp_cloud_on_the_oracle(cuda_lib, tmp_path):
+    """The C++ SolidCloud's own logic (construction with initialCorrect, saveState every writeFrequency calls, the
+    mean field from two passes of a sampler context with its Ct writes, the host fixInternal, saveRestart) on CPU:
+    the time-loop client linked against a stand-in library whose entry points the oracle answers
+    (tests/cpp_client/oracle_abi_shim.cpp), against the same loop written with the oracle directly."""
+    from oracle.oracle import OracleCloud
+    from sdfibm_gb300 import abi
+    from sdfibm_gb300.host import format_mean_field, format_state, parse_soliddict, soliddict_shape, write_restart
+    exe = _shim_client(tmp_path)
     U = _case_files(tmp_path)
     stdout = _run(exe, tmp_path, tmp_path / "cpp")
     assert "solids 4" in stdout
@@ -132,34 +183,14 @@ def test_cpp_cloud_on_the_oracle(cuda_lib, tmp_path):
 @pytest.mark.first_gpu_run
 def test_cpp_cloud_matches_python(cuda_lib, torch_cuda, tmp_path):
     torch = torch_cuda
-    from sdfibm_gb300 import abi
-    from sdfibm_gb300.cloud import SolidCloud
-    from sdfibm_gb300.host import StateFile, parse_soliddict, soliddict_shape
     exe = _client(tmp_path)
     U = _case_files(tmp_path)
     out = tmp_path / "cpp"
     _run(exe, tmp_path, out)
 
     # the same loop through the Python binding, device fields
-    solids, opt, twod = parse_soliddict(DICT, 1.0)
-    mesh = abi.mesh_desc(MESH[:3], MESH[3:6], MESH[6:], twod=twod)
-    cloud = SolidCloud(mesh, solids, opt)
-    cloud.set_sampler(soliddict_shape(DICT, "probe"))
-    Ud = torch.from_numpy(U).cuda()
-    f = cloud.new_fields()
     py = tmp_path / "py"
-    py.mkdir()
-    sf = StateFile(str(py / "cloud.out"), twod, 2, mean_field_path=str(py / "meanfield.out"))
-    cloud.initial_correct(Ud, f)
-    cloud.save_state(sf, Ud, f["Ct"])
-    for s in range(1, STEPS + 1):
-        t = s * DT
-        cloud.interact(t, DT, Ud, f)
-        cloud.evolve(t, DT)
-        cloud.save_state(sf, Ud, f["Ct"])
-    sf.close()
-    cloud.save_restart(DICT, str(py / "solidDict.restart"), precision=17)
-    cloud.close()
+    _python_loop(torch, U, py, "cuda")
 
     # the per-solid force sums are FP64 atomics whose order varies from run to run, so the two runs agree to the last
     # bits of the force and what follows from it: the 7-digit records within one unit of their last digit, the
