@@ -66,6 +66,8 @@ public:
         if (write_frequency_ < 1) throw std::runtime_error("meta.writeFrequency must be positive");
         const std::string sampler = lookup("meta/sampler", "");
         on_meanfield_ = lookup("meta/on_meanfield", "\x01") != "\x01";  // meta.found("on_meanfield")
+        const std::string fl = lookup("meta/on_fluid", "0");                // Foam::readBool
+        on_fluid_ = fl == "1" || fl == "true" || fl == "yes" || fl == "on" || fl == "y" || fl == "t";
         if (!sampler.empty()) {
             if (sdfibm_host_soliddict_shape(dict_.c_str(), sampler.c_str(), &sampler_shape_, msg, sizeof msg) !=
                 SDFIBM_OK)
@@ -239,7 +241,7 @@ public:
         if (i < 0 || i >= size()) throw std::out_of_range("solid index");
         return states()[(size_t)i];
     }
-    bool isOnFluid() const { return opt_.rho_f != 0.0; }
+    bool isOnFluid() const { return on_fluid_; }
     bool isOnTwoD() const { return mesh_.twod != 0; }
 
     std::vector<sdfibm_solid_state> states() const {
@@ -282,7 +284,7 @@ private:
     sdfibm_ctx* ctx_ = nullptr;
     sdfibm_ctx* sampler_ctx_ = nullptr;
     sdfibm_shape_desc sampler_shape_{};
-    bool has_sampler_ = false, on_meanfield_ = false;
+    bool has_sampler_ = false, on_meanfield_ = false, on_fluid_ = false;
     int write_frequency_ = 1;
     unsigned counter_ = 0;
     double time_ = 0.0;
