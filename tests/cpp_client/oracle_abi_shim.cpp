@@ -1,7 +1,7 @@
 // TEST DOUBLE: the entry points of sdfibm_cuda.h answered by the oracle (oracle/oracle.cpp, the FP64 CPU restatement)
 // instead of the GPU, with every field in host memory, so that the C++ SolidCloud of include/sdfibm_cloud.hpp, its
 // time-loop client and the Python SolidCloud (on CPU tensors) run on a machine without a GPU.  Linked with
-// oracle.cpp and host.cpp into a stand-in libsdfibm_cuda.so that only tests load; the product library is never
+// oracle.cpp and the host sources into a stand-in libsdfibm_cuda.so that only tests load; the product library is never
 // replaced by it.  Entry points the tests do not use return SDFIBM_ERR_STATE.
 #include <cstring>
 #include <string>

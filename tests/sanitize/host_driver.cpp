@@ -1,4 +1,4 @@
-// Drives the host half of libsdfibm_cuda.so (sdfibm_gb300/csrc/host.cpp: the solidDict, VOF-dict and blockMesh
+// Drives the host half of libsdfibm_cuda.so (sdfibm_gb300/csrc/host*.cpp: the solidDict, VOF-dict and blockMesh
 // front ends, the OpenFOAM list readers, the field and restart writers) under -fsanitize=address,undefined, on CPU.
 //
 //   host_driver DIR

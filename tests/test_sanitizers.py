@@ -1,7 +1,7 @@
 """Address and undefined-behaviour sanitizer builds of the host code, on CPU.
 
 Three drivers are compiled with g++ -fsanitize=address,undefined and run; a sanitizer report aborts them:
-  - tests/sanitize/host_driver.cpp drives the host half of the library (sdfibm_gb300/csrc/host.cpp). Inputs are
+  - tests/sanitize/host_driver.cpp drives the host half of the library (sdfibm_gb300/csrc/host*.cpp). Inputs are
     the solidDict, VOF-dict, blockMesh, OpenFOAM list and field-file front ends and writers: every prefix of each input,
     byte-mutated copies, and output buffers of every capacity below what is needed;
   - tests/sanitize/oracle_driver.cpp drives the oracle: both modes, 2-D and 3-D, every shape, interact, evolve with
@@ -15,6 +15,8 @@ import subprocess
 
 import numpy as np
 import pytest
+
+from sdfibm_gb300.build import HOST_SOURCES
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SAN = ["-std=c++17", "-O1", "-g", "-fsanitize=address,undefined", "-fno-omit-frame-pointer", "-ffp-contract=off",
@@ -53,7 +55,7 @@ def test_host_code_under_sanitizers(cuda_lib, tmp_path):
     (d / "faces_ascii").write_bytes(_header("ascii", "faceList", "faces") +
                                     b"3\n(\n4(0 1 5 4)\n4(1 2 6 5)\n3(3 7 8)\n)\n")
     exe = str(tmp_path / "host_driver")
-    _compile(exe, ["tests/sanitize/host_driver.cpp", "sdfibm_gb300/csrc/host.cpp"])
+    _compile(exe, ["tests/sanitize/host_driver.cpp"] + HOST_SOURCES)
     r = subprocess.run([exe, str(d)], capture_output=True, text=True, env=ENV, timeout=600)
     assert r.returncode == 0, (r.stdout + r.stderr)[-4000:]
     assert "calls clean" in r.stdout
@@ -61,8 +63,7 @@ def test_host_code_under_sanitizers(cuda_lib, tmp_path):
 
 def test_oracle_under_sanitizers(tmp_path):
     exe = str(tmp_path / "oracle_driver")
-    _compile(exe, ["tests/sanitize/oracle_driver.cpp", "oracle/oracle.cpp", "sdfibm_gb300/csrc/host.cpp"],
-             ["-pthread"])
+    _compile(exe, ["tests/sanitize/oracle_driver.cpp", "oracle/oracle.cpp"] + HOST_SOURCES, ["-pthread"])
     r = subprocess.run([exe], capture_output=True, text=True, env=ENV, timeout=600)
     assert r.returncode == 0, (r.stdout + r.stderr)[-4000:]
     assert "calls clean" in r.stdout
@@ -73,8 +74,8 @@ def test_cpp_solidcloud_under_sanitizers(tmp_path):
     answered by the oracle (tests/cpp_client/oracle_abi_shim.cpp), everything built with the sanitizers."""
     from test_solidcloud_cpp import STEPS, DT, _case_files
     exe = str(tmp_path / "client")
-    _compile(exe, ["tests/cpp_client/cloud_client.cpp", "tests/cpp_client/oracle_abi_shim.cpp", "oracle/oracle.cpp",
-                   "sdfibm_gb300/csrc/host.cpp"], ["-pthread"])
+    _compile(exe, ["tests/cpp_client/cloud_client.cpp", "tests/cpp_client/oracle_abi_shim.cpp", "oracle/oracle.cpp"] +
+             HOST_SOURCES, ["-pthread"])
     _case_files(tmp_path)
     (tmp_path / "out").mkdir()
     r = subprocess.run([exe, str(tmp_path / "solidDict"), str(tmp_path / "mesh.txt"), str(tmp_path / "U.bin"),

@@ -12,6 +12,8 @@ import subprocess
 import numpy as np
 import pytest
 
+from sdfibm_gb300.build import HOST_SOURCES
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 DICT = """meta { on_fluid 1; on_twod 1; gravity (0 -9.81 0); writeFrequency 2; sampler probe; on_meanfield 1; }
 shapes
@@ -80,8 +82,8 @@ def _shim_client(tmp_path):
     shim.mkdir()
     inc = ["-I", os.path.join(ROOT, "include")]
     r = subprocess.run([cxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off"] + inc +
-                       [os.path.join(ROOT, f) for f in ("tests/cpp_client/oracle_abi_shim.cpp", "oracle/oracle.cpp",
-                                                        "sdfibm_gb300/csrc/host.cpp")] +
+                       [os.path.join(ROOT, f) for f in ["tests/cpp_client/oracle_abi_shim.cpp", "oracle/oracle.cpp"] +
+                        HOST_SOURCES] +
                        ["-o", str(shim / "libsdfibm_cuda.so"), "-pthread"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     exe = str(shim / "client")
