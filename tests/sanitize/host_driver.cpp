@@ -1,7 +1,7 @@
 // Drives the host half of libsdfibm_cuda.so (sdfibm_gb300/csrc/host*.cpp: the solidDict, VOF-dict and blockMesh
 // front ends, the OpenFOAM list readers, the field and restart writers) under -fsanitize=address,undefined, on CPU.
 //
-//   host_driver DIR
+//   host_driver DIR [MUTATIONS [SEED]]
 //
 // DIR holds soliddict.txt, vofdict.txt, blockmesh.txt, field_ascii, field_binary, points_binary, faces_binary and
 // faces_ascii.  Every entry point runs on the
@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <sstream>
@@ -135,11 +136,12 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "the solidDict input does not parse\n");
         return 3;
     }
-    uint64_t seed = 12345;
+    const int mutations = argc > 2 ? std::atoi(argv[2]) : 300;  // mutated copies per input
+    uint64_t seed = argc > 3 ? (uint64_t)std::strtoull(argv[3], nullptr, 10) : 12345;
     long calls = 0;
     for (const std::string& t : texts) {
         for (size_t l = 0; l <= t.size(); ++l, ++calls) parse_all(t.substr(0, l), ns);
-        for (int k = 0; k < 300; ++k, ++calls) {
+        for (int k = 0; k < mutations; ++k, ++calls) {
             std::string m = t;
             for (int j = 0; j < 3; ++j) m[(size_t)(lcg(seed) >> 33) % m.size()] = "{}();\"/ *0a.-#\n"[(lcg(seed) >> 33) % 15];
             parse_all(m, ns);
@@ -147,7 +149,7 @@ int main(int argc, char** argv) {
     }
     for (const std::string& f : fields) {
         for (size_t l = 0; l <= f.size(); ++l, ++calls) field_all(f.substr(0, l));
-        for (int k = 0; k < 300; ++k, ++calls) {
+        for (int k = 0; k < mutations; ++k, ++calls) {
             std::string m = f;
             for (int j = 0; j < 2; ++j) m[(size_t)(lcg(seed) >> 33) % m.size()] = (char)(lcg(seed) >> 56);
             field_all(m);
