@@ -5,15 +5,17 @@ Workload (default): 512^3 uniform hex mesh on [0,1]^3, 16384 spheres / ellipsoid
 median 0.004), FP32 fields resident in HBM (seeded synthetic data).  One step = one interact: sparse reset,
 enumeration of every solid's touched cells, solid fraction, direct forcing and force/torque reduction.
 value = sum over solids of |touched cells| / device time of the step (CUDA events, L2 flushed between steps).
-e2e = the same metric through the host-buffer entry point (U copied in, As/Fs/Ts/Ct + force/torque copied out).
+e2e = the same metric through the host-buffer entry point (U copied in, As/Fs/Ts/Ct + force/torque copied out),
+timed over every step.  refgeo_gpu: the reference's own fraction on the GPU, beside the CPU reference arm.
 
 The default method is the learned cut-cell fraction (network + SUBSAMPLE(16^3) fallback outside its band).  The
 same run times the plain SUBSAMPLE(10^3) path ("plain") and measures the learned As and per-solid force against a
 SUBSAMPLE(16^3) step ("accuracy"; that evaluator's classifications equal the FP64 oracle's).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--config poly3d_512] [--method learned|subsample|refgeo]
-  python bench.py --impl reference ...   the CPU restatement of the reference's coupling (faithful data
-                                          structures, single thread), timed on a bounded sample of solids
+  python bench.py --impl reference ...   the CPU restatement of the reference's coupling (its data structures
+                                          and REF-GEO fraction), on a bounded sample of the solids spread over
+                                          every host thread
 With N > 1 (torchrun) every rank runs an independent replica: the path has no exchange step on one mesh per GPU
 (replicas only), value = sum over ranks, time = max over ranks.
 """
@@ -47,6 +49,13 @@ NCU_BYTES_PER_UNIT = {
     "couple_kernel": 220.1,    # 293.3 MB for 1,332,670 coupling cells: short x-runs of scattered cells in 6 field planes
     "classify_kernel": 1.40,   # 11.0 MB for 7,825,801 bbox cells (the learned features stay in L2 for the network)
     "subsample_cells_kernel": 39.6,  # 18.2 MB for 460,073 sampled cells
+}
+# Warp instructions per unit (ncu smsp__inst_executed.sum of one launch / its units), per (kernel, method); the
+# sampling and classification kernels are bound by instruction issue, and these counts give their issue roofline
+INST_PER_UNIT = {
+    ("subsample_cells_kernel", "learned"): ("sampled_cells", 1680.2),  # 773.0 M for 460,073 16^3 cells
+    ("classify_kernel", "learned"): ("bbox_cells", 21.62),            # 169.2 M for 7,825,801 bbox cells
+    ("classify_kernel", "refgeo"): ("bbox_cells", 24.02),             # 187.9 M for the same bbox cells
 }
 # FLOPs of the two tensor-core layers per predicted cell: hi and lo BF16 halves of an 11(16)x64 and a 64x64 product
 MLP_FLOPS_PER_CELL = 2 * (2 * 16 * 64) + 2 * (2 * 64 * 64)
@@ -127,9 +136,11 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_workload(args):
-    from sdfibm_gb300 import abi, workloads
-    w = workloads.CONFIGS[args.config](scale=args.scale)
+def make_workload(args, lower=None):
+    """The workload of --config at --scale with the fraction method of --method.  lower: the solid construction
+    (default: the library's host lowering; the CPU reference leg passes the oracle's restatement)."""
+    from sdfibm_gb300 import workloads
+    w = workloads.CONFIGS[args.config](scale=args.scale, lower=lower)
     w.opt.fraction_method = METHODS[args.method]
     w.opt.exact_forcing = 1 if getattr(args, "exact_forcing", False) else 0
     if args.method == "learned":
@@ -138,6 +149,21 @@ def make_workload(args):
     elif args.method == "subsample":
         w.opt.subsample_n = args.subsample_n
     return w
+
+
+def workload_config(w):
+    """The `config` of both arms' lines: the workload alone (mesh, solids, fields), identical for the GPU arm and the
+    CPU reference arm."""
+    kinds = sorted({abi_shape_name(d.shape.type) for d in w.solids})
+    return {"workload": "%s: %dx%dx%d uniform hex mesh, %d solids (%s), FP32 velocity field, seeded synthetic"
+                        % (w.name, w.mesh.nx, w.mesh.ny, w.mesh.nz, len(w.solids), "/".join(kinds)),
+            "n_cells": w.ncells, "n_solids": len(w.solids),
+            "l2": "GPU arm: flushed (256 MB write) before every timed step; CPU arm: inputs far above its caches"}
+
+
+def abi_shape_name(t):
+    from sdfibm_gb300 import abi
+    return {v: k for k, v in abi.SHAPE_NAMES.items()}.get(int(t), str(t))
 
 
 def make_cloud(w, method, subsample_n=None, stream=None, timing=False, band=None):
@@ -281,9 +307,15 @@ def cpu_baseline(w, solids_per_thread, threads=None):
 
 
 def run_reference(args, rank, world):
+    """The CPU reference arm: the oracle's restatement of the reference's own coupling (its data structures and its
+    REF-GEO fraction, the only fraction the reference has) on the workload built by the oracle's own lowering, so
+    that this process maps no library of the product.  Rank 0 alone runs it."""
     if rank != 0:
         return
-    w = make_workload(args)
+    from oracle.oracle import Lowering
+    a = argparse.Namespace(**vars(args))
+    a.method = "refgeo"
+    w = make_workload(a, lower=Lowering)
     ref = CpuReference(w, args.cpu_solids)
     vals = []
     last = None
@@ -296,11 +328,80 @@ def run_reference(args, rank, world):
     line = {"impl": "reference", "metric": "IBM coupling cells/s", "value": v, "unit": "cells/s", "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": last[1] * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": w.name, "n_cells": w.ncells, "n_solids": len(w.solids),
-                       "fraction_method": "refgeo (the reference's apex/pyramid fraction)"},
+            "method": "refgeo (GeometricTools::calcCellVolume, the reference's only cut-cell fraction)",
+            "config": workload_config(w),
             "cpu_baseline": ref.describe(v, *last),
             "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def issue_peak(clocks, sms):
+    """Warp instructions per second the GPU can issue: 4 per cycle per SM (one per sub-partition) at the median SM
+    clock sampled during the timed region (the maximum clock when no sample was taken)."""
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    return 4.0 * sms * mhz * 1e6
+
+
+def kernel_rooflines(kmean, units, method, peaks, clocks, sms):
+    """Roofline entries of the step's kernels, each against the limit that bounds it: warp-instruction issue for the
+    sampling and classification kernels (INST_PER_UNIT, from ncu), HBM for the coupling kernel, the tensor cores for
+    the network.  achieved = work per launch (per-unit figure x units) / average launch time."""
+    out = {}
+    ip = issue_peak(clocks, sms) / 1e9
+    for k, t in kmean.items():
+        key = (k, method)
+        if key in INST_PER_UNIT and t > 0:
+            unit, per = INST_PER_UNIT[key]
+            a = per * units[unit] / (t * 1e-3) / 1e9
+            out[k] = {"bound": "issue", "achieved": a, "peak": ip, "unit": "G warp-instructions/s", "frac": a / ip,
+                      "per_unit": per, "unit_of_work": unit, "units": units[unit], "ms": t,
+                      "traffic": NCU_BYTES_PER_UNIT.get(k, 0.0) * units[unit] if k in NCU_BYTES_PER_UNIT else None}
+    if kmean.get("couple_kernel", 0) > 0:
+        a = ALG_BYTES["couple_kernel"][1] * units["coupling_cells"] / (kmean["couple_kernel"] * 1e-3) / 1e9
+        out["couple_kernel"] = {"bound": "hbm", "achieved": a, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                                "frac": a / peaks["hbm_gbs"], "ms": kmean["couple_kernel"],
+                                "traffic": NCU_BYTES_PER_UNIT["couple_kernel"] * units["coupling_cells"]}
+    if kmean.get("mlp_infer_kernel", 0) > 0 and units["learned_cells"]:
+        tf = MLP_FLOPS_PER_CELL * units["learned_cells"] / (kmean["mlp_infer_kernel"] * 1e-3) / 1e12
+        out["mlp_infer_kernel"] = {"bound": "tensor", "achieved": tf, "peak": peaks["bf16_tflops"],
+                                   "unit": "TFLOP/s", "frac": tf / peaks["bf16_tflops"],
+                                   "ms": kmean["mlp_infer_kernel"]}
+    return out
+
+
+def e2e_host(torch, cloud, w, steps, cells):
+    """The step through the host-buffer entry point with page-locked FP32 host fields, timed over `steps` calls
+    after two untimed ones (wall clock around each call: the U upload, the kernels, the write-back of the changed
+    cells and the force/torque download)."""
+    import numpy as np
+    N = w.ncells
+    Uh = torch.from_numpy(w.U_numpy()).pin_memory()
+    hf = {"As": torch.empty(N, dtype=torch.float32, pin_memory=True),
+          "Fs": torch.empty(3 * N, dtype=torch.float32, pin_memory=True),
+          "Ts": torch.empty(N, dtype=torch.float32, pin_memory=True),
+          "Ct": torch.empty(N, dtype=torch.int32, pin_memory=True)}
+    hn = {k: v.numpy() for k, v in hf.items()}
+    Uhn = Uh.numpy()
+    for i in range(2):
+        cloud.interact_host(0.0, w.dt, Uhn, hn)
+    h2d = d2h = 0
+    ts = []
+    st = None
+    for i in range(steps):
+        t0 = time.perf_counter()
+        cloud.interact_host(i * w.dt, w.dt, Uhn, hn)
+        ts.append(time.perf_counter() - t0)
+        st = cloud.stats()  # outside the timed span
+        h2d += st["host_h2d_bytes"]
+        d2h += st["host_d2h_bytes"]
+    s = sum(ts) / len(ts)
+    return {"value": cells / s, "unit": "cells/s", "h2d_bytes_per_step": h2d // steps,
+            "d2h_bytes_per_step": d2h // steps, "ms_per_step": s * 1e3, "steps": steps,
+            "ms_min_max": [min(ts) * 1e3, max(ts) * 1e3],
+            "host_fields": ("page-locked FP32; U read in place at the coupling cells" if h2d // steps < 12 * N else
+                            "page-locked FP32; U copied in while the fraction kernels run") +
+                           (", changed 8-cell chunks written back in place" if st["host_sparse"]
+                            else ", whole fields copied back")}
 
 
 def main():
@@ -312,7 +413,8 @@ def main():
     ap.add_argument("--config", default="poly3d_512")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--method", default="learned", choices=sorted(METHODS))
-    ap.add_argument("--no-compare", action="store_true", help="skip the plain SUBSAMPLE timing and the accuracy step")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the plain SUBSAMPLE and REF-GEO timings and the accuracy steps")
     ap.add_argument("--subsample-n", type=int, default=10, help="samples per axis of --method subsample")
     ap.add_argument("--cpu-solids", type=int, default=2, help="solids per host thread in the CPU timing sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -327,7 +429,6 @@ def main():
     if args.impl == "reference":
         return run_reference(args, rank, world)
 
-    import numpy as np
     import torch
 
     torch.cuda.set_device(local)
@@ -335,12 +436,11 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    from sdfibm_gb300 import abi
-    from sdfibm_gb300.cloud import SolidCloud
 
     w = make_workload(args)
     U = w.U_torch()
     stream = torch.cuda.Stream()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
     cloud = make_cloud(w, args.method, stream=stream)
     with torch.cuda.stream(stream):
         f = cloud.new_fields()
@@ -367,16 +467,40 @@ def main():
     tk = time_steps(torch, ct, w, U, ft_, min(args.steps, 3), 2, flush, kernel_times=True)
     ct.close()
     del ft_
-    tm["kernel_ms"] = tk["kernel_ms"]
     ms_step = tm["ms_step"]
     mean_cells = tm["cells"]
     ms_step, job_cells = over_ranks(dist, ms_step, mean_cells, "cuda")
     value = job_cells / (ms_step * 1e-3)
     launches = tm["launches"]
-    bbox = [tm["bbox"]]
-    kt = {k: [v] for k, v in tm["kernel_ms"].items()}
+    st = tm["stats"]
+    kmean = tk["kernel_ms"]
+    units = {"coupling_cells": mean_cells, "bbox_cells": tm["bbox"],
+             "learned_cells": st.get("learned_cells", 0) if args.method == "learned" else 0,
+             "sampled_cells": st.get("learned_fallback_cells", 0) if args.method == "learned"
+             else (st.get("learned_cells", 0) if args.method == "subsample" else 0),
+             "cut_cells": st.get("learned_cells", 0)}
 
     compare = None
+    refgeo = None
+    if not args.no_compare:
+        # the reference's own fraction (REF-GEO) on the GPU, same workload: the like-for-like figure beside the CPU
+        # reference arm
+        rg = make_cloud(w, "refgeo", stream=stream)
+        with torch.cuda.stream(stream):
+            fr_ = rg.new_fields()
+        trg = time_steps(torch, rg, w, U, fr_, args.steps, args.warmup, flush, stream=stream)
+        rgt = make_cloud(w, "refgeo", timing=True)
+        frt = rgt.new_fields()
+        krg = time_steps(torch, rgt, w, U, frt, min(args.steps, 3), 2, flush, kernel_times=True)["kernel_ms"]
+        rgt.close()
+        del frt
+        refgeo = {"method": "refgeo (the reference's apex/pyramid fraction; As within 1e-5 of the oracle)",
+                  "value": trg["cells"] * world / (trg["ms_step"] * 1e-3), "ms_per_step": trg["ms_step"],
+                  "kernel_ms": {k: round(v, 4) for k, v in sorted(krg.items(), key=lambda x: -x[1])}}
+        if not args.no_e2e:
+            refgeo["e2e"] = e2e_host(torch, rg, w, args.steps, trg["cells"] * world)
+        rg.close()
+        del fr_
     if args.method == "learned" and not args.no_compare:
         ref = reference16(w, U)
         plain = make_cloud(w, "subsample", subsample_n=10, stream=stream)
@@ -391,7 +515,6 @@ def main():
         tp["kernel_ms"] = time_steps(torch, pt, w, U, fpt, min(args.steps, 3), 2, flush, kernel_times=True)["kernel_ms"]
         pt.close()
         del fpt
-        # the smallest plain lattice whose As error is under the 1e-3 bar on this workload
         plain12 = make_cloud(w, "subsample", subsample_n=12, stream=stream)
         with torch.cuda.stream(stream):
             f12 = plain12.new_fields()
@@ -400,11 +523,10 @@ def main():
         plain12.close()
         del f12
         acc = accuracy(torch, w, cloud, U, ref)
-        st = tm["stats"]
         # other operating points of the same model: the open band and the 10^3 fallback
         points = []
         for label, band, fb in (("open band (network on every cut cell)", (1e30, 1e30), None),
-                                ("tau_twist 0.1, tau_grad 0.05, SUBSAMPLE 10^3 fallback", (0.1, 0.05), 10)):
+                                ("same band, SUBSAMPLE 10^3 fallback", None, 10)):
             import copy
             w2 = copy.copy(w)
             w2.opt = copy.copy(w.opt)
@@ -415,26 +537,23 @@ def main():
                 f2 = c2.new_fields()
             t2 = time_steps(torch, c2, w2, U, f2, args.steps, args.warmup, flush, stream=stream)
             a2 = accuracy(torch, w2, c2, U, ref)
-            points.append({"band": label, "ms_per_step": t2["ms_step"],
-                           "value": t2["cells"] * world / (t2["ms_step"] * 1e-3),
-                           "fallback_cells": t2["stats"].get("learned_fallback_cells"),
-                           "as_abs_err_mean": a2["as_abs_err_mean"], "as_abs_err_p99": a2["as_abs_err_p99"],
-                           "force_rel_err_median": a2["force_rel_err_median"]})
+            points.append(dict({"band": label, "ms_per_step": t2["ms_step"],
+                                "value": t2["cells"] * world / (t2["ms_step"] * 1e-3),
+                                "fallback_cells": t2["stats"].get("learned_fallback_cells")}, **a2))
             c2.close()
             del f2
         del ref
-        compare = {"plain": {"method": "SUBSAMPLE 10^3 samples per cut cell", "ms_per_step": tp["ms_step"],
-                             "value": tp["cells"] * world / (tp["ms_step"] * 1e-3),
-                             "as_abs_err_mean": acc_plain["as_abs_err_mean"],
-                             "as_abs_err_p99": acc_plain["as_abs_err_p99"],
-                             "kernel_ms": {k: round(v, 4) for k, v in tp["kernel_ms"].items()}},
+        pick = lambda a: {k: v for k, v in a.items() if k.startswith("as_") or k.startswith("force_")}
+        compare = {"plain": dict({"method": "SUBSAMPLE 10^3 samples per cut cell", "ms_per_step": tp["ms_step"],
+                                  "value": tp["cells"] * world / (tp["ms_step"] * 1e-3),
+                                  "kernel_ms": {k: round(v, 4) for k, v in tp["kernel_ms"].items()}},
+                                 **pick(acc_plain)),
                    "speedup_vs_plain": tp["ms_step"] / tm["ms_step"],
-                   "plain_12": {"method": "SUBSAMPLE 12^3 samples per cut cell", "ms_per_step": t12["ms_step"],
-                                "value": t12["cells"] * world / (t12["ms_step"] * 1e-3),
-                                "as_abs_err_mean": a12["as_abs_err_mean"], "as_abs_err_p99": a12["as_abs_err_p99"],
-                                "force_rel_err_median": a12["force_rel_err_median"]},
+                   "plain_12": dict({"method": "SUBSAMPLE 12^3 samples per cut cell", "ms_per_step": t12["ms_step"],
+                                     "value": t12["cells"] * world / (t12["ms_step"] * 1e-3)}, **pick(a12)),
                    "speedup_vs_plain_12": t12["ms_step"] / tm["ms_step"],
                    "learned_cells": st.get("learned_cells"), "fallback_cells": st.get("learned_fallback_cells"),
+                   "fallback_share": (st.get("learned_fallback_cells") or 0) / max(1, st.get("learned_cells") or 1),
                    "accuracy": acc, "other_operating_points": points}
 
     # full time step (interact + evolve with its sub-steps and collisions + fixInternal), device time, graphs
@@ -454,73 +573,22 @@ def main():
     full_ms = e0.elapsed_time(e2)
     evolve_ms = e1.elapsed_time(e2)
 
-    # roofline of the dominant kernel
+    # roofline of the dominant kernel (the one with the largest share of the step), against the limit that binds it
     peaks, peaks_kind = load_peaks()
-    kmean = {k: sum(v) / len(v) for k, v in kt.items()}
+    kr = kernel_rooflines(kmean, units, args.method, peaks, clk, sms)
     dom = max(kmean, key=lambda k: kmean[k])
-    st = tm["stats"]
-    unit_counts = {"coupling_cells": mean_cells, "bbox_cells": sum(bbox) / len(bbox),
-                   "learned_cells": st.get("learned_cells", 0) if args.method == "learned" else 0,
-                   "sampled_cells": st.get("learned_fallback_cells", 0) if args.method == "learned"
-                   else st.get("learned_cells", 0)}
-    unit_key, per_unit = ALG_BYTES.get(dom, ("coupling_cells", 0.0))
-    units = unit_counts[unit_key]
-    achieved = per_unit * units / (kmean[dom] * 1e-3) / 1e9
-    traffic = NCU_BYTES_PER_UNIT[dom] * units if dom in NCU_BYTES_PER_UNIT else None
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_kind": peaks_kind,
-                "alg_bytes_per_unit": per_unit, "unit_of_work": unit_key, "units": units,
-                "note": "the cut-cell evaluators (subsample_cells_kernel, classify, refgeo_cells_kernel) are bound "
-                        "by FP32 instruction issue, not memory: ncu reads 77 % issue active and 0.2 % DRAM throughput "
-                        "for subsample_cells_kernel (profiles/subsample_cells_kernel_poly3d_256_learned.md), so their "
-                        "HBM fraction is small by construction; couple_kernel is the HBM-bound kernel (51 % of DRAM "
-                        "peak in ncu, 220 B of traffic per coupling cell against 36 B algorithmic: the touched cells "
-                        "form short x-runs in six field planes)",
-                "kernel_ms": {k: round(v, 4) for k, v in sorted(kmean.items(), key=lambda x: -x[1])}}
-    # the HBM-bound kernel of the step and the tensor-core kernel, each against its own peak
-    if "couple_kernel" in kmean:
-        a = ALG_BYTES["couple_kernel"][1] * mean_cells / (kmean["couple_kernel"] * 1e-3) / 1e9
-        roofline["couple_kernel"] = {"bound": "hbm", "achieved": a, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                                     "frac": a / peaks["hbm_gbs"],
-                                     "traffic": NCU_BYTES_PER_UNIT["couple_kernel"] * mean_cells
-                                     if "couple_kernel" in NCU_BYTES_PER_UNIT else None}
-    if "mlp_infer_kernel" in kmean and unit_counts["learned_cells"]:
-        tf = MLP_FLOPS_PER_CELL * unit_counts["learned_cells"] / (kmean["mlp_infer_kernel"] * 1e-3) / 1e12
-        roofline["mlp_infer_kernel"] = {"bound": "tensor", "achieved": tf, "peak": peaks["bf16_tflops"],
-                                        "unit": "TFLOP/s", "frac": tf / peaks["bf16_tflops"]}
+    roofline = dict(kr.get(dom, {"bound": "hbm", "achieved": None, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                                 "frac": None, "traffic": None}))
+    roofline.update({"kernel": dom, "peak_kind": peaks_kind + (" (HBM, bf16)" if peaks_kind == "measured" else ""),
+                     "kernels": kr,
+                     "note": "issue = warp instructions per second against 4 per cycle per SM at the sampled SM clock "
+                             "(per-unit instruction counts from ncu smsp__inst_executed.sum); the sampling and "
+                             "classification kernels are instruction-bound, the coupling kernel HBM-bound, the "
+                             "network tensor-core-bound"})
 
-    # end to end through the host-buffer entry point (pinned host fields)
     e2e = None
     if not args.no_e2e:
-        N = w.ncells
-        Uh = torch.empty((3, N), dtype=torch.float32, pin_memory=True)
-        Uh.copy_(U)
-        hf = {"As": torch.empty(N, dtype=torch.float32, pin_memory=True),
-              "Fs": torch.empty(3 * N, dtype=torch.float32, pin_memory=True),
-              "Ts": torch.empty(N, dtype=torch.float32, pin_memory=True),
-              "Ct": torch.empty(N, dtype=torch.int32, pin_memory=True)}
-        hn = {k: v.numpy() for k, v in hf.items()}
-        Uhn = Uh.numpy()
-        for i in range(2):
-            cloud.interact_host(0.0, w.dt, Uhn, hn)
-        reps = max(2, min(args.steps, 5))
-        h2d = d2h = 0
-        e2e_s = 0.0
-        for i in range(reps):
-            t0 = time.perf_counter()
-            cloud.interact_host(i * w.dt, w.dt, Uhn, hn)
-            e2e_s += time.perf_counter() - t0
-            st = cloud.stats()  # outside the timed span
-            h2d += st["host_h2d_bytes"]
-            d2h += st["host_d2h_bytes"]
-        e2e_s /= reps
-        # page-locked fields: U copied in during the fraction kernels, the changed cells written back in place
-        e2e = {"value": mean_cells * world / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": h2d // reps,
-               "d2h_bytes_per_step": d2h // reps, "ms_per_step": e2e_s * 1e3,
-               "host_fields": ("page-locked; U read in place at the coupling cells" if h2d // reps < 12 * N else
-                               "page-locked; U copied in while the fraction kernels run") +
-                              ", changed 8-cell chunks written back in place"
-               if st["host_sparse"] else "staged through whole-field copies"}
+        e2e = e2e_host(torch, cloud, w, args.steps, mean_cells * world)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -530,18 +598,20 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 fields, f64 geometry and reductions",
                 "data": "synthetic",
-                "config": {"workload": "%s: %dx%dx%d mesh, %d solids, %s solid fraction, %s forcing, HBM-resident fields"
-                                       % (w.name, w.mesh.nx, w.mesh.ny, w.mesh.nz, len(w.solids), args.method,
-                                          "FP64" if args.exact_forcing else "mixed FP64/FP32"),
-                           "n_cells": w.ncells, "n_solids": len(w.solids), "coupling_cells": mean_cells,
-                           "bbox_cells": sum(bbox) / len(bbox), "fraction_method": args.method,
-                           "fp64_rechecks": tm["stats"].get("fp64_rechecks"),
-                           "learned_cells": unit_counts["learned_cells"], "sampled_cells": unit_counts["sampled_cells"],
-                           "l2": "flushed (256 MB write) before every timed step", "full_step_ms": full_ms,
-                           "evolve_fix_ms": evolve_ms, "cuda_graphs": True,
-                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "method": {"learned": "learned cut-cell fraction (tensor-core network, SUBSAMPLE fallback outside "
+                                      "its band)",
+                           "subsample": "SUBSAMPLE %d^3" % args.subsample_n,
+                           "refgeo": "refgeo (the reference's apex/pyramid fraction)"}[args.method],
+                "config": workload_config(w),
+                "details": {"coupling_cells": mean_cells, "bbox_cells": tm["bbox"],
+                            "fp64_rechecks": st.get("fp64_rechecks"), "learned_cells": units["learned_cells"],
+                            "sampled_cells": units["sampled_cells"], "full_step_ms": full_ms,
+                            "evolve_fix_ms": evolve_ms, "cuda_graphs": True,
+                            "forcing": "FP64" if args.exact_forcing else "mixed FP64/FP32",
+                            "parallelism": "replicas" if world > 1 else "single GPU"},
+                "kernel_ms": {k: round(v, 4) for k, v in sorted(kmean.items(), key=lambda x: -x[1])},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-                "gpu_launches": launches, "learned_vs_plain": compare}
+                "gpu_launches": launches, "refgeo_gpu": refgeo, "learned_vs_plain": compare}
         print(json.dumps(line))
     cloud.close()
     if dist:

@@ -211,11 +211,13 @@ int sdfibm_cuda_touched(sdfibm_ctx* ctx, int32_t solid, int64_t* cells, int8_t* 
  * returns after an interact) computed without allocating any device memory, for callers that cannot call
  * cudaMalloc: hosts whose device memory is owned entirely by their own pool allocator, or latency-critical loops
  * that cannot afford the device-wide synchronisation of cudaMalloc/cudaFree.  The work space is one file-scope
- * device array of about 10 MiB, reserved on every GPU that loads the library until the process exits.
- * Limit: the solid's bounding box may hold at most 524288 cells (and 262144 flood-fill bitmap words); larger solids
- * are rejected with SDFIBM_ERR_CAPACITY.  The first call on a device looks up the array's address with that device
- * current: make it before any stream capture.  Calls share the array, so calls that overlap on the GPU race; issue
- * them on one stream.  cells (int32) and types (int8, 1/2/3) are device buffers of `capacity` entries; *n_device
+ * device array of about 10 MiB, held on every GPU that uses it until the process exits.  With lazy module loading
+ * (the default of recent CUDA releases) the driver reserves the array during the first call on each device: make
+ * that first call at start-up, before a pool allocator takes the device's memory, and before any stream capture
+ * (it also looks up the array's address, which stays cached for the process; cudaDeviceReset between calls is not
+ * supported).  Limit: the solid's bounding box may hold at most 524288 cells (and 262144 flood-fill bitmap words);
+ * larger solids are rejected with SDFIBM_ERR_CAPACITY before anything is launched.  Calls share the array and a call
+ * keeps its contents, so calls that overlap on the GPU race; issue them on one stream.  cells (int32) and types (int8, 1/2/3) are device buffers of `capacity` entries; *n_device
  * (device int64) receives the full count, or -(status) when the enumeration failed on the device.  Asynchronous on
  * cuda_stream (NULL: the legacy default stream). */
 int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* solid, void* cuda_stream,

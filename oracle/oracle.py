@@ -195,3 +195,61 @@ class OracleCloud:
 
     def cell_fraction(self, s, c, method):
         return lib().oracle_cell_fraction(self.h, s, c, method)
+
+
+class Lowering:
+    """The solid construction of the reference (shape constructors, quaternion(XYZ, euler), Solid::setMaterial)
+    through the oracle's own restatement, with the call signatures of sdfibm_gb300.host.  The CPU reference leg of
+    the benchmark builds its workload with this, so that it maps no library of the product."""
+
+    SHAPE_PARAMS = {
+        abi.SHAPE_CIRCLE: ("radius",), abi.SHAPE_SPHERE: ("radius",), abi.SHAPE_ELLIPSE: ("radiusa", "radiusb"),
+        abi.SHAPE_ELLIPSOID: ("radiusa", "radiusb", "radiusc"), abi.SHAPE_RECTANGLE: ("radiusa", "radiusb"),
+        abi.SHAPE_BOX: ("radiusa", "radiusb", "radiusc"), abi.SHAPE_PLANE: (),
+        abi.SHAPE_CIRCLE_TAIL: ("radius", "ratio", "thickness"),
+        abi.SHAPE_CIRCLE_TWOTAIL: ("radius", "ratio", "thickness"),
+    }
+
+    @staticmethod
+    def make_shape(type_name, com=(0.0, 0.0, 0.0), **params):
+        t = abi.SHAPE_NAMES[type_name] if isinstance(type_name, str) else int(type_name)
+        return make_shape(t, [float(params[k]) for k in Lowering.SHAPE_PARAMS[t]], com)
+
+    @staticmethod
+    def mask_motion(mask):
+        """Motion01Mask from its 'b######' word (motion01mask.h:21-48)."""
+        if not (isinstance(mask, str) and len(mask) == 7 and mask[0] == "b" and set(mask[1:]) <= {"0", "1"}):
+            raise ValueError("bad mask %r" % (mask,))
+        p = np.zeros(8)
+        p[:6] = [float(ch) for ch in mask[1:]]
+        return abi.MOTION_01MASK, p
+
+    @staticmethod
+    def make_solid(sid, shape, rho, pos, euler_deg=(0, 0, 0), vel=(0, 0, 0), omega=(0, 0, 0), motion=None,
+                   forcer=None):
+        """Solid + IMaterial: Solid::setMaterial (solid.h:95-103), setOrientation from XYZ Euler angles."""
+        mt, mp = motion if motion is not None else (abi.MOTION_FREE, np.zeros(8))
+        ft, fp = forcer if forcer is not None else (abi.FORCER_NONE, np.zeros(8))
+        d = abi.SolidDesc()
+        d.id = int(sid)
+        d.shape = shape
+        d.motion_type, d.forcer_type = int(mt), int(ft)
+        for i in range(8):
+            d.motion_p[i] = float(mp[i])
+            d.forcer_p[i] = float(fp[i])
+        d.rho = float(rho)
+        d.mass = shape.volume * rho
+        d.mass_inv = shape.volume_inv / rho
+        for i in range(9):
+            d.moi_inv[i] = shape.moi_inv[i] / rho
+        e = [float(x) for x in euler_deg] + [0.0] * (3 - len(euler_deg))
+        q = np.zeros(4)
+        a = np.array([e[0] * np.pi / 180.0, e[1] * np.pi / 180.0, e[2] * np.pi / 180.0])
+        lib().oracle_quat_from_euler(_p(a), _p(q))
+        for i in range(3):
+            d.pos[i] = float(pos[i])
+            d.vel[i] = float(vel[i])
+            d.omega[i] = float(omega[i])
+        for i in range(4):
+            d.quat[i] = float(q[i])
+        return d

@@ -5,14 +5,19 @@
 // allocator (a cudaMalloc beside it fails or fragments the pool), and callers on latency-critical loops where the
 // device-wide synchronisation of cudaMalloc/cudaFree is not acceptable.  For them this file keeps the work space of
 // one enumeration -- the solid's record, its plan, the counters, the bbox class bytes, the flood-fill bitmaps and the
-// two touched-cell lists -- in one file-scope device array that the library reserves when it is loaded.
+// two touched-cell lists -- in one file-scope device array that the driver reserves with the library's device code
+// (under lazy module loading: during the first call on each device).
 //
 // Limits and rules:
 //  * the solid's bounding box may hold at most NA_MAX_BBOX_CELLS cells (and NA_MAX_BITMAP_WORDS bitmap words);
 //    larger boxes are rejected with SDFIBM_ERR_CAPACITY before anything is launched;
-//  * the array (about 10 MiB) stays reserved on every GPU that loads the library until the process exits;
-//  * the first call on a device looks up the array's device address (cudaGetSymbolAddress) with that device
-//    current; make that first call before any stream capture;
+//  * the array (about 10 MiB) stays reserved on every GPU that uses it until the process exits.  With lazy module
+//    loading (CUDA_MODULE_LOADING=LAZY, the default of recent CUDA releases) the driver reserves it during the
+//    first call on each device, so make that first call at start-up, before a pool allocator takes the device's
+//    memory;
+//  * the first call on a device also looks up the array's device address (cudaGetSymbolAddress) with that device
+//    current and keeps it for the life of the process; make that first call before any stream capture.  The kept
+//    address belongs to the device's primary context: cudaDeviceReset between calls is not supported;
 //  * every call reuses the same array: two calls whose work overlaps on the GPU (different streams, or different
 //    host threads on one device) race and corrupt each other's results.  Serialise them (same stream) instead.
 #include <cmath>
@@ -157,10 +162,22 @@ bool solid_record(const sdfibm_mesh_desc& mesh, const sdfibm_solid_desc& d, Soli
 
 namespace sdfibm_dev {
 
-// classify work items of the single solid: (0, first tile of each chunk)
-__global__ void noalloc_chunks_kernel(int2* chunks, int n) {
+// Set-up of one call inside the array: the solid's record, its state and zeroed counters (passed by value, so that
+// nothing on the call's stack is read after the call returns), and the classify work items of the single solid,
+// (0, first tile of each chunk).
+static_assert(sizeof(SolidK) + sizeof(sdfibm_solid_state) + sizeof(int64_t) + 16 <= 4096,
+              "records passed as kernel arguments");
+__global__ void noalloc_init_kernel(SolidK k, sdfibm_solid_state x, int64_t list_cap, int nchunks) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) chunks[i] = make_int2(0, i * CHUNK_TILES);
+    if (i == 0) {
+        *reinterpret_cast<SolidK*>(g_noalloc_scratch + OFF_SK) = k;
+        *reinterpret_cast<sdfibm_solid_state*>(g_noalloc_scratch + OFF_ST) = x;
+        Counters c;
+        memset(&c, 0, sizeof(c));
+        c.list_cap = list_cap;
+        *reinterpret_cast<Counters*>(g_noalloc_scratch + OFF_CNT) = c;
+    }
+    if (i < nchunks) reinterpret_cast<int2*>(g_noalloc_scratch + OFF_CHUNKS)[i] = make_int2(0, i * CHUNK_TILES);
 }
 
 // Writes the enumeration result in the order of sdfibm_cuda_touched: ALL_INSIDE cells ascending, then
@@ -267,20 +284,13 @@ extern "C" int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc* mesh, const s
     std::memset(&x, 0, sizeof(x));
     for (int a = 0; a < 3; ++a) { x.pos[a] = solid->pos[a]; x.vel[a] = solid->vel[a]; x.omega[a] = solid->omega[a]; }
     for (int a = 0; a < 4; ++a) x.quat[a] = solid->quat[a];
-    Counters c0;
-    std::memset(&c0, 0, sizeof(c0));
-    c0.list_cap = NA_MAX_BBOX_CELLS;  // counters start from zero on every call
-
     SolidK* d_sk = reinterpret_cast<SolidK*>(b + OFF_SK);
     sdfibm_solid_state* d_st = reinterpret_cast<sdfibm_solid_state*>(b + OFF_ST);
     SolidPlan* d_plan = reinterpret_cast<SolidPlan*>(b + OFF_PLAN);
     Counters* d_cnt = reinterpret_cast<Counters*>(b + OFF_CNT);
     int2* d_chunks = reinterpret_cast<int2*>(b + OFF_CHUNKS);
-    if (cudaMemcpyAsync(d_sk, &k, sizeof(k), cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaMemcpyAsync(d_st, &x, sizeof(x), cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaMemcpyAsync(d_cnt, &c0, sizeof(c0), cudaMemcpyHostToDevice, st) != cudaSuccess)
-        return SDFIBM_ERR_CUDA;
-    noalloc_chunks_kernel<<<(nchunks + 255) / 256, 256, 0, st>>>(d_chunks, nchunks);
+    // the records travel as kernel arguments (counters start from zero on every call)
+    noalloc_init_kernel<<<(nchunks + 255) / 256, 256, 0, st>>>(k, x, NA_MAX_BBOX_CELLS, nchunks);
     plan_kernel<<<1, 32, 0, st>>>(m, d_sk, d_st, d_plan, 1, d_cnt);
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return SDFIBM_ERR_CUDA;

@@ -15,13 +15,20 @@ The sedimentation radius is 0.03: 100 circles of radius 0.05 with a 0.01 gap can
 (they would cover 95% of it, more than the densest hexagonal packing).
 A ``scale`` < 1 shrinks meshes and solid counts for tests while keeping the per-solid resolution (r/h).
 The reference's public benchmark inputs are not used: these seeded inputs stand in for them.
+Every builder takes ``lower``: the object whose make_shape / make_solid / mask_motion build the solids (default: the
+C++ lowering of include/sdfibm_host.h, i.e. sdfibm_gb300.host); any lowering with the same signatures that restates
+the reference's constructors gives the same descriptors bit for bit.
 """
 import math
 
 import numpy as np
 
 from . import abi
-from .host import make_shape, make_solid, mask_motion
+
+
+def _host_lowering():
+    from . import host
+    return host
 
 
 class Workload:
@@ -109,39 +116,42 @@ def place_spheres(rng, radii, lo, hi, gap, twod=False, max_tries=20000):
     return pos
 
 
-def cylinder2d(scale=1.0):
+def cylinder2d(scale=1.0, lower=None):
+    L = lower or _host_lowering()
     nx, ny = max(8, int(round(400 * scale))), max(4, int(round(200 * scale)))
     mesh = abi.mesh_desc((nx, ny, 1), (-10.0, -10.0, -0.5), (40.0 / nx, 20.0 / ny, 1.0), twod=1)
-    shape = make_shape("Circle", radius=0.5)
-    solids = [make_solid(0, shape, 1.0, (0.0, 0.0, 0.0))]
+    shape = L.make_shape("Circle", radius=0.5)
+    solids = [L.make_solid(0, shape, 1.0, (0.0, 0.0, 0.0))]
     opt = abi.options(rho_f=1.0)
     return Workload("cylinder2d", mesh, solids, opt, 0.005, (1.0, 0.0, 0.0), 0.05, 1)
 
 
-def sedimentation2d(scale=1.0, ncircles=None, collision=abi.COLLISION_REFERENCE):
+def sedimentation2d(scale=1.0, ncircles=None, collision=abi.COLLISION_REFERENCE, lower=None):
+    L = lower or _host_lowering()
     n = max(16, int(round(1024 * scale)))
     mesh = abi.mesh_desc((n, n, 1), (0.0, 0.0, -0.5), (1.0 / n, 1.0 / n, 1.0), twod=1)
     rng = np.random.default_rng(2)
     nc = ncircles if ncircles is not None else 100
     r = 0.03
     pos = place_spheres(rng, np.full(nc, r), (0, 0, 0), (1, 1, 0), 0.01, twod=True)
-    wall = make_shape("Plane")
+    wall = L.make_shape("Plane")
     walls = [((0.0, 0.5, 0.0), (0, 0, -90.0)), ((1.0, 0.5, 0.0), (0, 0, 90.0)),
              ((0.5, 0.0, 0.0), (0, 0, 0.0)), ((0.5, 1.0, 0.0), (0, 0, 180.0))]
-    fixed = mask_motion("b000000")
-    planar = mask_motion("b110001")
-    solids = [make_solid(i, wall, 1.5, p, e, motion=fixed) for i, (p, e) in enumerate(walls)]
-    circle = make_shape("Circle", radius=r)
+    fixed = L.mask_motion("b000000")
+    planar = L.mask_motion("b110001")
+    solids = [L.make_solid(i, wall, 1.5, p, e, motion=fixed) for i, (p, e) in enumerate(walls)]
+    circle = L.make_shape("Circle", radius=r)
     vel = rng.normal(0.0, 0.1, (nc, 2))
     om = rng.normal(0.0, 1.0, nc)
     for i in range(nc):
-        solids.append(make_solid(len(solids), circle, 1.5, pos[i], vel=(vel[i, 0], vel[i, 1], 0.0),
+        solids.append(L.make_solid(len(solids), circle, 1.5, pos[i], vel=(vel[i, 0], vel[i, 1], 0.0),
                                  omega=(0.0, 0.0, om[i]), motion=planar))
     opt = abi.options(rho_f=1.0, gravity=(0.0, -10.0, 0.0), collision_mode=collision)
     return Workload("sedimentation2d", mesh, solids, opt, 1e-3, (0.0, 0.0, 0.0), 0.1, 3)
 
 
-def _poly3d(name, n, nsolids, r_median, sigma, kinds, seed, collision):
+def _poly3d(name, n, nsolids, r_median, sigma, kinds, seed, collision, lower):
+    L = lower or _host_lowering()
     mesh = abi.mesh_desc((n, n, n), (0.0, 0.0, 0.0), (1.0 / n,) * 3, twod=0)
     rng = np.random.default_rng(seed)
     r = np.exp(rng.normal(math.log(r_median), sigma, nsolids))
@@ -159,12 +169,12 @@ def _poly3d(name, n, nsolids, r_median, sigma, kinds, seed, collision):
     solids = []
     for i in range(nsolids):
         if kind[i] == "Sphere":
-            sh = make_shape("Sphere", radius=r[i])
+            sh = L.make_shape("Sphere", radius=r[i])
         elif kind[i] == "Ellipsoid":
-            sh = make_shape("Ellipsoid", radiusa=r[i], radiusb=r[i] * a[i], radiusc=r[i] * b[i])
+            sh = L.make_shape("Ellipsoid", radiusa=r[i], radiusb=r[i] * a[i], radiusc=r[i] * b[i])
         else:
-            sh = make_shape("Box", radiusa=r[i], radiusb=r[i] * a[i], radiusc=r[i] * b[i])
-        d = make_solid(i, sh, 1.5, pos[i], vel=vel[i])
+            sh = L.make_shape("Box", radiusa=r[i], radiusb=r[i] * a[i], radiusc=r[i] * b[i])
+        d = L.make_solid(i, sh, 1.5, pos[i], vel=vel[i])
         for c in range(4):
             d.quat[c] = float(quat[i, c])
         solids.append(d)
@@ -172,16 +182,16 @@ def _poly3d(name, n, nsolids, r_median, sigma, kinds, seed, collision):
     return Workload(name, mesh, solids, opt, 1e-3, (0.0, 0.0, 0.0), 0.1, seed + 100)
 
 
-def poly3d_256(scale=1.0, collision=abi.COLLISION_OFF):
+def poly3d_256(scale=1.0, collision=abi.COLLISION_OFF, lower=None):
     n = max(16, int(round(256 * scale)))
     ns = max(4, int(round(4096 * scale ** 3)))
-    return _poly3d("poly3d_256", n, ns, 0.01 * 256 / n, 0.4, ["Sphere", "Ellipsoid"], 4, collision)
+    return _poly3d("poly3d_256", n, ns, 0.01 * 256 / n, 0.4, ["Sphere", "Ellipsoid"], 4, collision, lower)
 
 
-def poly3d_512(scale=1.0, collision=abi.COLLISION_SPHERES):
+def poly3d_512(scale=1.0, collision=abi.COLLISION_SPHERES, lower=None):
     n = max(16, int(round(512 * scale)))
     ns = max(6, int(round(16384 * scale ** 3)))
-    return _poly3d("poly3d_512", n, ns, 0.004 * 512 / n, 0.5, ["Sphere", "Ellipsoid", "Box"], 5, collision)
+    return _poly3d("poly3d_512", n, ns, 0.004 * 512 / n, 0.5, ["Sphere", "Ellipsoid", "Box"], 5, collision, lower)
 
 
 CONFIGS = {"cylinder2d": cylinder2d, "sedimentation2d": sedimentation2d, "poly3d_256": poly3d_256,

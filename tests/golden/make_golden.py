@@ -123,4 +123,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SDFIBM_REFERENCE")
+    if not src:
+        sys.exit("usage: make_golden.py REFERENCE_CHECKOUT  (or set SDFIBM_REFERENCE)")
+    main(src)

@@ -66,7 +66,6 @@ def test_falling_ellipse_uniform_matches_polymesh():
 
 
 @pytest.mark.gpu
-@pytest.mark.first_gpu_run
 def test_re200_golden_on_the_gpu(cuda_lib, torch_cuda):
     """The library's initialCorrect pass (interact(0, 1), REF-GEO) against the As the reference ships for re200: the
     same cells as the oracle, FP32 fractions within the coupling tolerance of the shipped FP64 values."""
@@ -95,7 +94,6 @@ def test_re200_golden_on_the_gpu(cuda_lib, torch_cuda):
 
 
 @pytest.mark.gpu
-@pytest.mark.first_gpu_run
 def test_falling_ellipse_golden_on_the_gpu(cuda_lib, torch_cuda):
     """The library on the uniform form of examples/falling_ellipse against the oracle's run on the reference's own
     polyMesh: touched cells and types exact, As and Fs within the coupling tolerance, force and torque within 1e-6."""

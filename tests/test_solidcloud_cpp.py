@@ -182,7 +182,6 @@ def test_cpp_cloud_on_the_oracle(cuda_lib, tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.first_gpu_run
 def test_cpp_cloud_matches_python(cuda_lib, torch_cuda, tmp_path):
     torch = torch_cuda
     exe = _client(tmp_path)

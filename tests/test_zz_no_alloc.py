@@ -73,3 +73,35 @@ def test_noalloc_rejects_oversized_bbox(cuda_lib, torch_cuda):
     rc = cuda_lib.sdfibm_cuda_touched_noalloc(C.byref(mesh), C.byref(big), None, C.c_void_p(cells.data_ptr()),
                                               C.c_void_p(types.data_ptr()), 16, C.c_void_p(n.data_ptr()))
     assert rc == abi.ERR_CAPACITY
+
+
+def test_noalloc_allocates_nothing_and_counts_without_buffers(cuda_lib, torch_cuda):
+    """After a first call (which, under lazy module loading, is when the driver reserves the array), ten more calls
+    leave the device's free memory unchanged; a call with capacity 0 and no output buffers still reports the
+    count."""
+    w = workloads.poly3d_512(scale=0.125)
+    d = w.solids[0]
+    ref_cells, _ = _context(w, d)
+    n = torch_cuda.full((1,), -99, dtype=torch_cuda.int64, device="cuda")
+    cells = torch_cuda.zeros((1 << 16,), dtype=torch_cuda.int32, device="cuda")
+    types = torch_cuda.zeros((1 << 16,), dtype=torch_cuda.int8, device="cuda")
+
+    def call(capacity, with_buffers=True):
+        return cuda_lib.sdfibm_cuda_touched_noalloc(
+            C.byref(w.mesh), C.byref(d), None, C.c_void_p(cells.data_ptr()) if with_buffers else None,
+            C.c_void_p(types.data_ptr()) if with_buffers else None, capacity, C.c_void_p(n.data_ptr()))
+
+    assert call(1 << 16) == abi.OK
+    torch_cuda.cuda.synchronize()
+    free0 = torch_cuda.cuda.mem_get_info()[0]
+    alloc0 = torch_cuda.cuda.memory_allocated()
+    for _ in range(10):
+        assert call(1 << 16) == abi.OK
+    torch_cuda.cuda.synchronize()
+    assert torch_cuda.cuda.mem_get_info()[0] == free0
+    assert torch_cuda.cuda.memory_allocated() == alloc0
+    assert int(n.item()) == len(ref_cells)
+    n.fill_(-99)
+    assert call(0, with_buffers=False) == abi.OK
+    torch_cuda.cuda.synchronize()
+    assert int(n.item()) == len(ref_cells)
