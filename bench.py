@@ -5,8 +5,8 @@ Workload (default): 512^3 uniform hex mesh on [0,1]^3, 16384 spheres / ellipsoid
 median 0.004), FP32 fields resident in HBM (seeded synthetic data).  One step = one interact: sparse reset,
 enumeration of every solid's touched cells, solid fraction, direct forcing and force/torque reduction.
 value = sum over solids of |touched cells| / device time of the step (CUDA events, L2 flushed between steps).
-e2e = the same metric through the host-buffer entry point (U copied in, As/Fs/Ts/Ct + force/torque copied out),
-timed over every step.  refgeo_gpu: the reference's own fraction on the GPU, beside the CPU reference arm.
+e2e = the same metric through the host-buffer entry point with FP64 fields in OpenFOAM's layout (U read in, As/Fs/Ts/Ct
+and force/torque written out), timed over every step.  refgeo_gpu: the reference's own fraction on the GPU, beside the CPU reference arm.
 
 The default method is the learned cut-cell fraction (network + SUBSAMPLE(16^3) fallback outside its band).  The
 same run times the plain SUBSAMPLE(10^3) path ("plain") and measures the learned As and per-solid force against a
@@ -404,6 +404,42 @@ def e2e_host(torch, cloud, w, steps, cells):
                             else ", whole fields copied back")}
 
 
+def e2e_host64(torch, cloud, w, steps, cells):
+    """The step through sdfibm_cuda_interact_host64: FP64 host fields in OpenFOAM's own layout (U and Fs one x,y,z
+    triple per cell, As / Ts / Ct one double per cell), page-locked as a solver would register its field storage,
+    timed over `steps` calls after two untimed ones.  This is the drop-in's host cost: the solver passes its fields as
+    they are, with no conversion loop on the host."""
+    import numpy as np
+    N = w.ncells
+    U64 = torch.from_numpy(np.ascontiguousarray(w.U_numpy().T, dtype=np.float64)).pin_memory()
+    hf = {"As": torch.empty(N, dtype=torch.float64, pin_memory=True),
+          "Fs": torch.empty((N, 3), dtype=torch.float64, pin_memory=True),
+          "Ts": torch.empty(N, dtype=torch.float64, pin_memory=True),
+          "Ct": torch.empty(N, dtype=torch.float64, pin_memory=True)}
+    hn = {k: v.numpy() for k, v in hf.items()}
+    Un = U64.numpy()
+    for i in range(2):
+        cloud.interact_host64(0.0, w.dt, Un, hn)
+    h2d = d2h = 0
+    ts = []
+    st = None
+    for i in range(steps):
+        t0 = time.perf_counter()
+        cloud.interact_host64(i * w.dt, w.dt, Un, hn)
+        ts.append(time.perf_counter() - t0)
+        st = cloud.stats()  # outside the timed span
+        h2d += st["host_h2d_bytes"]
+        d2h += st["host_d2h_bytes"]
+    s = sum(ts) / len(ts)
+    return {"value": cells / s, "unit": "cells/s", "h2d_bytes_per_step": h2d // steps,
+            "d2h_bytes_per_step": d2h // steps, "ms_per_step": s * 1e3, "steps": steps,
+            "ms_min_max": [min(ts) * 1e3, max(ts) * 1e3],
+            "host_fields": "page-locked FP64 in OpenFOAM's layout (volVectorField U/Fs, volScalarField As/Ts/Ct); "
+                           "U read at the coupling cells, " +
+                           ("changed 8-cell chunks written back in place" if st["host_sparse"]
+                            else "whole fields written back")}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -419,6 +455,7 @@ def main():
     ap.add_argument("--cpu-solids", type=int, default=2, help="solids per host thread in the CPU timing sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch configuration (no autotuner)")
     ap.add_argument("--exact-forcing", action="store_true",
                     help="the reference's FP64 forcing sequence per cell (default: FP64 for the rigid-body "
                          "velocity and U - us, FP32 after it, FP64 force/torque sums)")
@@ -446,6 +483,12 @@ def main():
         f = cloud.new_fields()
         flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
     torch.cuda.synchronize()
+    # launch configuration from the project's autotuner (per-kernel CTA counts, classify work-item size), before any
+    # timed work; contexts of the same shape below take it from its cache
+    tuning = None
+    if not args.no_autotune:
+        cloud.autotune(w.dt, U, f)
+        tuning = cloud.tuning()
 
     def step(t):
         return cloud.interact(t, w.dt, U, f, want_ft=False)
@@ -464,6 +507,8 @@ def main():
     # per-kernel device times from a second context that records events around every launch (no graphs)
     ct = make_cloud(w, args.method, timing=True)
     ft_ = ct.new_fields()
+    if not args.no_autotune:
+        ct.autotune(w.dt, U, ft_)
     tk = time_steps(torch, ct, w, U, ft_, min(args.steps, 3), 2, flush, kernel_times=True)
     ct.close()
     del ft_
@@ -488,17 +533,23 @@ def main():
         rg = make_cloud(w, "refgeo", stream=stream)
         with torch.cuda.stream(stream):
             fr_ = rg.new_fields()
+        torch.cuda.synchronize()
+        if not args.no_autotune:
+            rg.autotune(w.dt, U, fr_)
         trg = time_steps(torch, rg, w, U, fr_, args.steps, args.warmup, flush, stream=stream)
         rgt = make_cloud(w, "refgeo", timing=True)
         frt = rgt.new_fields()
+        if not args.no_autotune:
+            rgt.autotune(w.dt, U, frt)
         krg = time_steps(torch, rgt, w, U, frt, min(args.steps, 3), 2, flush, kernel_times=True)["kernel_ms"]
         rgt.close()
         del frt
         refgeo = {"method": "refgeo (the reference's apex/pyramid fraction; As within 1e-5 of the oracle)",
                   "value": trg["cells"] * world / (trg["ms_step"] * 1e-3), "ms_per_step": trg["ms_step"],
+                  "tuning": rg.tuning(),
                   "kernel_ms": {k: round(v, 4) for k, v in sorted(krg.items(), key=lambda x: -x[1])}}
         if not args.no_e2e:
-            refgeo["e2e"] = e2e_host(torch, rg, w, args.steps, trg["cells"] * world)
+            refgeo["e2e"] = e2e_host64(torch, rg, w, args.steps, trg["cells"] * world)
         rg.close()
         del fr_
     if args.method == "learned" and not args.no_compare:
@@ -506,12 +557,18 @@ def main():
         plain = make_cloud(w, "subsample", subsample_n=10, stream=stream)
         with torch.cuda.stream(stream):
             fp = plain.new_fields()
+        torch.cuda.synchronize()
+        if not args.no_autotune:
+            plain.autotune(w.dt, U, fp)
+        plain_tuning = plain.tuning()
         tp = time_steps(torch, plain, w, U, fp, args.steps, args.warmup, flush, stream=stream)
         acc_plain = accuracy(torch, w, plain, U, ref)
         plain.close()
         del fp
         pt = make_cloud(w, "subsample", subsample_n=10, timing=True)
         fpt = pt.new_fields()
+        if not args.no_autotune:
+            pt.autotune(w.dt, U, fpt)
         tp["kernel_ms"] = time_steps(torch, pt, w, U, fpt, min(args.steps, 3), 2, flush, kernel_times=True)["kernel_ms"]
         pt.close()
         del fpt
@@ -545,6 +602,7 @@ def main():
         del ref
         pick = lambda a: {k: v for k, v in a.items() if k.startswith("as_") or k.startswith("force_")}
         compare = {"plain": dict({"method": "SUBSAMPLE 10^3 samples per cut cell", "ms_per_step": tp["ms_step"],
+                                  "tuning": plain_tuning,
                                   "value": tp["cells"] * world / (tp["ms_step"] * 1e-3),
                                   "kernel_ms": {k: round(v, 4) for k, v in tp["kernel_ms"].items()}},
                                  **pick(acc_plain)),
@@ -588,7 +646,8 @@ def main():
 
     e2e = None
     if not args.no_e2e:
-        e2e = e2e_host(torch, cloud, w, args.steps, mean_cells * world)
+        e2e = e2e_host64(torch, cloud, w, args.steps, mean_cells * world)
+        e2e["fp32_host_fields"] = e2e_host(torch, cloud, w, args.steps, mean_cells * world)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -611,7 +670,7 @@ def main():
                             "parallelism": "replicas" if world > 1 else "single GPU"},
                 "kernel_ms": {k: round(v, 4) for k, v in sorted(kmean.items(), key=lambda x: -x[1])},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-                "gpu_launches": launches, "refgeo_gpu": refgeo, "learned_vs_plain": compare}
+                "gpu_launches": launches, "tuning": tuning, "refgeo_gpu": refgeo, "learned_vs_plain": compare}
         print(json.dumps(line))
     cloud.close()
     if dist:

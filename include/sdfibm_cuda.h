@@ -189,6 +189,17 @@ int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U
 int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs,
                               float* Ts, int32_t* Ct, double* FT);
 
+/* Same as sdfibm_cuda_interact_host with the fields in OpenFOAM's own types and layout, so that a solver passes its
+ * volField storage as it is (the reference's field members, createFields.h:19-35): U and Fs are volVectorFields
+ * (double[ncells][3], one x,y,z triple per cell), As, Ts and Ct volScalarFields (double[ncells]; Ct holds the
+ * integer cell codes as doubles, as the reference stores them).  Page-locked fields (cudaHostRegister on the
+ * solver's arrays) are read and written in place by the GPU: U only at the coupling cells, after the enumeration,
+ * and the result fields at the cells this call or the previous one touched (every cell on the first call with a
+ * set of buffers, after other buffers, or with dense_reset).  Other host memory goes through whole-field copies
+ * staged in a device FP64 buffer.  U is rounded to FP32 on the device, as the device-field path reads it. */
+int sdfibm_cuda_interact_host64(sdfibm_ctx* ctx, double time, double dt, const double* U, double* As, double* Fs,
+                                double* Ts, double* Ct, double* FT);
+
 /* SolidCloud::evolve (solidcloud.cpp:521-562): n_subiter sub-steps of AB2 forcer and fluid force, buoyancy-reduced
  * gravity, solid-solid collision and Solid::move (solid.h:181-202), then storeOldForce. */
 int sdfibm_cuda_evolve(sdfibm_ctx* ctx, double time, double dt);
@@ -231,12 +242,22 @@ int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc* mesh, const sdfibm_solid
  * the touched cells only.  n: entries of out (at most 11 are written). */
 int sdfibm_cuda_stats(sdfibm_ctx* ctx, int64_t* out, int32_t n);
 
-/* No counterpart in the reference.  Autotuner of the classify work queue: times a few dense interacts (on the given
- * device fields, which it overwrites) with each candidate work-item size (2, 4, 8, 16 or 32 tiles of one solid per
- * item) and keeps the fastest; results do not depend on the choice.  *chosen_tiles (host, may be NULL) receives it
- * and options.tile_cells reports it in cells.  Captured graphs are re-captured on their next use.  Synchronises. */
+/* No counterpart in the reference.  Autotuner of the launch configuration: times dense interacts (on the given
+ * device fields, which it overwrites) with per-kernel events, first over the classify work-item size (2, 4, 8, 16 or
+ * 32 tiles of one solid per item), then over the CTA count of every work-stealing or grid-strided launch
+ * (classification: 1 .. occupancy x SMs; cut-cell sampling, REF-GEO fractions: 2 .. 16 x SMs; coupling: 1 ..
+ * occupancy x SMs; network: 1 .. 8 x SMs), and keeps the fastest of each; results do not depend on the choice.
+ * The choice is kept for the life of the process per workload shape (mesh, solid count, bounding-box tiles, fraction
+ * method and lattice, SM count): a later call on a context of the same shape applies it without timing.
+ * *chosen_tiles (host, may be NULL) receives the work-item size and options.tile_cells reports it in cells.  Captured
+ * graphs are re-captured on their next use.  Synchronises. */
 int sdfibm_cuda_autotune(sdfibm_ctx* ctx, double dt, const float* U, float* As, float* Fs, float* Ts, int32_t* Ct,
                          int32_t* chosen_tiles);
+
+/* No counterpart in the reference.  The launch configuration in use: out[0] classify tiles per work item, out[1..5]
+ * CTA counts of the classification, cut-cell sampling, coupling, network and REF-GEO fraction kernels, out[6] 1 when
+ * the last sdfibm_cuda_autotune took it from the per-shape cache.  n: entries of out (at most 7 are written). */
+int sdfibm_cuda_tuning(sdfibm_ctx* ctx, int32_t* out, int32_t n);
 
 /* No counterpart in the reference (which has only the apex/pyramid fraction).  Installs the learned cut-cell
  * fraction model used when options.fraction_method is SDFIBM_FRACTION_LEARNED: params is a HOST array of

@@ -14,10 +14,12 @@ _lib = None
 
 CUDA_SYMBOLS = [
     "sdfibm_options_default", "sdfibm_cuda_create", "sdfibm_cuda_interact", "sdfibm_cuda_interact_host",
+    "sdfibm_cuda_interact_host64",
     "sdfibm_cuda_evolve", "sdfibm_cuda_fix_internal", "sdfibm_cuda_get_solids", "sdfibm_cuda_set_solids",
     "sdfibm_cuda_touched", "sdfibm_cuda_stats", "sdfibm_cuda_kernel_times", "sdfibm_cuda_last_error",
     "sdfibm_cuda_version",
     "sdfibm_cuda_destroy", "sdfibm_cuda_touched_noalloc", "sdfibm_cuda_set_fraction_model", "sdfibm_cuda_autotune",
+    "sdfibm_cuda_tuning",
 ]
 MLP_SYMBOLS = [
     "sdfibm_mlp_dataset", "sdfibm_mlp_forward", "sdfibm_mlp_loss_grad", "sdfibm_mlp_adam", "sdfibm_mlp_train",
@@ -50,6 +52,7 @@ def load():
     L.sdfibm_cuda_create.argtypes = [P(abi.MeshDesc), P(abi.SolidDesc), i32, P(abi.Options), vp, P(vp)]
     L.sdfibm_cuda_interact.argtypes = [vp, dbl, dbl, vp, vp, vp, vp, vp, vp]
     L.sdfibm_cuda_interact_host.argtypes = [vp, dbl, dbl, vp, vp, vp, vp, vp, vp]
+    L.sdfibm_cuda_interact_host64.argtypes = [vp, dbl, dbl, vp, vp, vp, vp, vp, vp]
     L.sdfibm_cuda_evolve.argtypes = [vp, dbl, dbl]
     L.sdfibm_cuda_fix_internal.argtypes = [vp, vp, vp]
     L.sdfibm_cuda_get_solids.argtypes = [vp, P(abi.SolidState), i32]
@@ -58,6 +61,7 @@ def load():
     L.sdfibm_cuda_stats.argtypes = [vp, P(i64), i32]
     L.sdfibm_cuda_set_fraction_model.argtypes = [vp, vp, C.c_float, C.c_float]
     L.sdfibm_cuda_autotune.argtypes = [vp, dbl, vp, vp, vp, vp, vp, P(i32)]
+    L.sdfibm_cuda_tuning.argtypes = [vp, P(i32), i32]
     L.sdfibm_cuda_kernel_times.argtypes = [vp, P(C.c_char_p), P(dbl), i32, P(i32)]
     L.sdfibm_cuda_touched_noalloc.argtypes = [P(abi.MeshDesc), P(abi.SolidDesc), vp, vp, vp, i64, vp]
     L.sdfibm_cuda_last_error.argtypes = [vp]

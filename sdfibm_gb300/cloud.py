@@ -100,6 +100,20 @@ class SolidCloud:
         self._check(rc)
         return FT[:self.nsolids]
 
+    def interact_host64(self, time, dt, U, fields):
+        """FP64 host (numpy) fields in OpenFOAM's layout: U and Fs [N, 3], As, Ts, Ct [N] (Ct as float64).
+        Page-locked arrays are read and written in place by the GPU; other arrays are staged through whole-field
+        copies."""
+        FT = np.zeros((max(1, self.nsolids), 6))
+        for k, a in (("U", U),) + tuple(fields.items()):
+            if a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError("interact_host64: %s must be a C-contiguous float64 array" % k)
+        p = lambda a: a.ctypes.data_as(C.c_void_p)
+        rc = self._L.sdfibm_cuda_interact_host64(self._h, float(time), float(dt), p(U), p(fields["As"]),
+                                                 p(fields["Fs"]), p(fields["Ts"]), p(fields["Ct"]), p(FT))
+        self._check(rc)
+        return FT[:self.nsolids]
+
     def initial_correct(self, U, fields):
         """SolidCloud::initialCorrect (src/solidcloud.cpp:276-286): interact(0, 1), then every solid's force and
         torque cleared (the fluid force of that pass stays, as in the reference).  Returns the per-solid force and
@@ -249,11 +263,20 @@ class SolidCloud:
         return dict(zip(keys, list(out)))
 
     def autotune(self, dt, U, fields):
-        """Chooses the classify work-item size by timing dense interacts on these fields; returns tiles per item."""
+        """Chooses the launch configuration (classify work-item size, CTA counts) by timing dense interacts on these
+        fields (or takes it from the per-shape cache); returns tiles per item."""
         out = C.c_int32(0)
         self._check(self._L.sdfibm_cuda_autotune(self._h, float(dt), _ptr(U), _ptr(fields["As"]), _ptr(fields["Fs"]),
                                                  _ptr(fields["Ts"]), _ptr(fields["Ct"]), C.byref(out)))
         return out.value
+
+    def tuning(self):
+        """The launch configuration in use (what the autotuner chose, or the defaults)."""
+        out = (C.c_int32 * 7)()
+        self._check(self._L.sdfibm_cuda_tuning(self._h, out, 7))
+        keys = ("classify_tiles_per_item", "classify_ctas", "subsample_ctas", "couple_ctas", "mlp_ctas",
+                "refgeo_ctas", "from_cache")
+        return dict(zip(keys, list(out)))
 
     def set_fraction_model(self, params, tau_twist, tau_grad):
         """Installs the learned cut-cell fraction model (options.fraction_method = FRACTION_LEARNED)."""

@@ -5,6 +5,8 @@
 #include <cstring>
 #include <functional>
 #include <string>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -48,6 +50,15 @@ __global__ void mark_export_kernel(const int32_t* in_cell, const int32_t* cut_ce
                                    const int32_t* prev_cut_cell, const Counters* cnt, int64_t N, uint32_t* dirty);
 __global__ void export_kernel(Counters* cnt, int64_t N, uint32_t* dirty, const float* As, const float* Fs,
                               const float* Ts, const int32_t* Ct, float* hAs, float* hFs, float* hTs, int32_t* hCt);
+__global__ void gather_u64_kernel(const int32_t* in_cell, const int32_t* cut_cell, const Counters* cnt, int64_t N,
+                                  const double* hU, float* U);
+__global__ void mark_all_kernel(uint32_t* dirty, int64_t words);
+__global__ void export64_kernel(Counters* cnt, int64_t N, uint32_t* dirty, const float* As, const float* Fs,
+                                const float* Ts, const int32_t* Ct, double* hAs, double* hFs, double* hTs,
+                                double* hCt);
+__global__ void u64_to_planes_kernel(const double* U64, int64_t N, float* U);
+__global__ void fields_to_f64_kernel(int64_t N, const float* As, const float* Fs, const float* Ts, const int32_t* Ct,
+                                     double* out);
 __global__ void reset_kernel(const int32_t* in_cell, const int32_t* cut_cell, const Counters* cnt, int64_t N,
                              float* As, float* Fs, float* Ts, int32_t* Ct);
 __global__ void fix_internal_kernel(MeshK m, const sdfibm_solid_state* st, const int32_t* in_cell,
@@ -175,7 +186,17 @@ struct sdfibm_ctx {
     bool host_sparse = false;  // the last interact_host exported the touched cells only
     int64_t host_h2d = 0, host_d2h = 0;
     uint32_t* d_dirty = nullptr;  // changed 8-cell chunks of the fields, one bit each (cleared by export_kernel)
-    int classify_grid = 0, couple_grid = 0;
+    // interact_host64 (FP64 fields in OpenFOAM's layout): device address of the page-locked U while a call runs
+    // (gathered at the coupling cells after the enumeration), the host buffers of the last call, and the device
+    // staging of the whole-field path for memory the GPU cannot address
+    const double* u64_dev = nullptr;
+    const void* host64_fields[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool host64_synced = false;
+    double* d_f64 = nullptr;  // [3N] U, then [6N] As, Fs, Ts, Ct
+    // CTA counts of the launches the autotuner sets (defaults from the occupancy at create)
+    int classify_grid = 0, couple_grid = 0, subsample_grid = 0, mlp_grid = 0, refgeo_grid = 0;
+    int classify_occ = 1, couple_occ = 1;  // resident CTAs per SM
+    bool tuned_from_cache = false;
     // per-kernel events (options.timing)
     static constexpr int MAXEV = 24;
     cudaEvent_t ev[MAXEV + 1] = {};
@@ -203,6 +224,7 @@ struct sdfibm_ctx {
         cudaKernelNodeParams step_params{};
         int cur = -1, dense = -1;
         const void* fields[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+        const double* u64 = nullptr;
         int launches = 0;
     };
     Graph igraph[4];
@@ -561,9 +583,14 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
     int occ = 0;
     occ = classify_occupancy(ctx->opt.fraction_method, mesh->nz <= 2);
     ctx->classify_grid = std::max(1, occ) * ctx->num_sms;
+    ctx->classify_occ = std::max(1, occ);
     occ = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, couple_kernel, 256, 0);
     ctx->couple_grid = std::max(1, occ) * ctx->num_sms;
+    ctx->couple_occ = std::max(1, occ);
+    ctx->subsample_grid = 8 * ctx->num_sms;
+    ctx->mlp_grid = 4 * ctx->num_sms;
+    ctx->refgeo_grid = 8 * ctx->num_sms;
     *out = ctx;
     return SDFIBM_OK;
 }
@@ -656,6 +683,12 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
                                                         ctx->cut_solid(), Ct, ctx->d_cnt, N);
         mark(ctx, "claim_kernel");
         launches += 4;
+        if (ctx->u64_dev) {  // interact_host64: U read at the coupling cells from the page-locked FP64 field
+            gather_u64_kernel<<<ctx->num_sms * 8, 256, 0, sb>>>(ctx->in_cell(), ctx->cut_cell(), ctx->d_cnt, N,
+                                                                 ctx->u64_dev, const_cast<float*>(U));
+            mark(ctx, "gather_u64_kernel");
+            ++launches;
+        }
         if (!dense) {
             const int p = ctx->cur ^ 1;
             reset_kernel<<<ctx->num_sms * 4, 256, 0, sb>>>(ctx->d_lists[p][0], ctx->d_lists[p][2], ctx->d_cnt, N, As,
@@ -664,7 +697,7 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             ++launches;
         }
         if (refgeo) {
-            refgeo_cells_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(ctx->mesh, ctx->d_sk, ctx->d_plan,
+            refgeo_cells_kernel<<<ctx->refgeo_grid, 256, 0, st>>>(ctx->mesh, ctx->d_sk, ctx->d_plan,
                                                                    ctx->d_fref_solid, ctx->d_fref_index,
                                                                    ctx->d_rg_phi, ctx->feat_cap, ctx->d_cnt,
                                                                    ctx->d_alpha);
@@ -679,7 +712,7 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             ia.ref_solid = ctx->d_fref_solid; ia.ref_index = ctx->d_fref_index; ia.alpha = ctx->d_alpha;
             ia.fb_list = ctx->d_fb; ia.fb_count = &ctx->d_cnt->n_fb; ia.tau_twist = ctx->tau_twist;
             ia.tau_grad = ctx->tau_grad; ia.error = &ctx->d_cnt->error;
-            launch_mlp_infer(ia, 4 * ctx->num_sms, st);
+            launch_mlp_infer(ia, ctx->mlp_grid, st);
             mark(ctx, "mlp_infer_kernel");
             fa.m = ctx->mesh; fa.sk = ctx->d_sk; fa.st = ctx->d_st; fa.plan = ctx->d_plan; fa.fb_list = ctx->d_fb;
             fa.fref_solid = ctx->d_fref_solid; fa.fref_index = ctx->d_fref_index; fa.cap = ctx->feat_cap;
@@ -687,7 +720,7 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             fa.n = ctx->opt.learned_fallback_n > 0 ? ctx->opt.learned_fallback_n : 16;
             fa.rq = ctx->d_rq; fa.rq_cap = ctx->rq_cap;
             fa.ovf = ctx->d_ovf; fa.ovf_cap = ctx->ovf_cap;
-            subsample_cells_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(fa);
+            subsample_cells_kernel<<<ctx->subsample_grid, 256, 0, st>>>(fa);
             mark(ctx, "subsample_cells_kernel");
             launches += 2;
         } else if (subsample) {
@@ -697,7 +730,7 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             fa.n = ctx->opt.subsample_n;
             fa.rq = ctx->d_rq; fa.rq_cap = ctx->rq_cap;
             fa.ovf = ctx->d_ovf; fa.ovf_cap = ctx->ovf_cap;
-            subsample_cells_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(fa);
+            subsample_cells_kernel<<<ctx->subsample_grid, 256, 0, st>>>(fa);
             mark(ctx, "subsample_cells_kernel");
             ++launches;
         }
@@ -836,7 +869,7 @@ int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U
     int rc = -1;
     if (graphs_on(ctx)) {
         sdfibm_ctx::Graph& g = ctx->igraph[ctx->cur * 2 + (dense ? 1 : 0)];
-        bool changed = g.cur != ctx->cur || g.dense != (int)dense;
+        bool changed = g.cur != ctx->cur || g.dense != (int)dense || g.u64 != ctx->u64_dev;
         for (int i = 0; i < 5; ++i) changed = changed || g.fields[i] != f5[i];
         int counted = 0;
         rc = run_graph(ctx, g, changed,
@@ -850,6 +883,7 @@ int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U
         } else {
             g.cur = ctx->cur;
             g.dense = (int)dense;
+            g.u64 = ctx->u64_dev;
             for (int i = 0; i < 5; ++i) g.fields[i] = f5[i];
             if (counted) g.launches = counted;
             launches = g.launches;
@@ -878,13 +912,103 @@ static void* mapped_host(const void* p) {
     return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
+static int64_t dirty_words(int64_t N) {
+    // one bit per chunk of export_chunk_cells() cells, 32 chunks per word
+    return (N + 32 * (int64_t)export_chunk_cells() - 1) / (32 * (int64_t)export_chunk_cells());
+}
+
+// device copies of the four result fields and of U for the host-buffer entry points
+static int ensure_staging(sdfibm_ctx* ctx) {
+    const int64_t N = ctx->mesh.ncells;
+    if (!ctx->d_U && dalloc(&ctx->d_U, 3 * N)) return fail(ctx, SDFIBM_ERR_CUDA, "staging allocation failed");
+    if (!ctx->d_As) {
+        const int64_t words = dirty_words(N);
+        if (dalloc(&ctx->d_As, N) || dalloc(&ctx->d_Fs, 3 * N) || dalloc(&ctx->d_Ts, N) || dalloc(&ctx->d_Ct, N) ||
+            dalloc(&ctx->d_dirty, words) ||
+            cudaMemsetAsync(ctx->d_dirty, 0, sizeof(uint32_t) * words, ctx->stream) != cudaSuccess)
+            return fail(ctx, SDFIBM_ERR_CUDA, "staging allocation failed");
+    }
+    return SDFIBM_OK;
+}
+
+int sdfibm_cuda_interact_host64(sdfibm_ctx* ctx, double time, double dt, const double* U, double* As, double* Fs,
+                                double* Ts, double* Ct, double* FT) {
+    if (!ctx) return SDFIBM_ERR_ARG;
+    if (!U || !As || !Fs || !Ts || !Ct) return fail(ctx, SDFIBM_ERR_ARG, "null field pointer");
+    const int64_t N = ctx->mesh.ncells;
+    cudaStream_t st = ctx->stream;
+    if (int rc = ensure_staging(ctx)) return rc;
+    const void* hU = mapped_host(U);
+    void* const hp[4] = {mapped_host(As), mapped_host(Fs), mapped_host(Ts), mapped_host(Ct)};
+    const void* f5[5] = {U, As, Fs, Ts, Ct};
+    ctx->host_synced = false;  // the FP32 host path's buffers no longer follow the device fields
+    if (hU && hp[0] && hp[1] && hp[2] && hp[3]) {
+        // page-locked: U gathered at the coupling cells, changed chunks written back in place (every chunk on the
+        // first call on these buffers, after other buffers, and with dense_reset)
+        bool same = ctx->host64_synced && !ctx->opt.dense_reset;
+        for (int i = 0; i < 5; ++i) same = same && f5[i] == ctx->host64_fields[i];
+        ctx->host64_synced = false;
+        ctx->u64_dev = static_cast<const double*>(hU);
+        int rc = sdfibm_cuda_interact(ctx, time, dt, ctx->d_U, ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, nullptr);
+        ctx->u64_dev = nullptr;
+        if (rc) return rc;
+        CK(cudaMemsetAsync(&ctx->d_cnt->n_export, 0, sizeof(int32_t), st));
+        if (same) {
+            const int p = ctx->cur ^ 1;
+            mark_export_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(ctx->in_cell(), ctx->cut_cell(), ctx->d_lists[p][0],
+                                                                  ctx->d_lists[p][2], ctx->d_cnt, N, ctx->d_dirty);
+        } else {
+            mark_all_kernel<<<ctx->num_sms * 4, 256, 0, st>>>(ctx->d_dirty, dirty_words(N));
+        }
+        export64_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(
+            ctx->d_cnt, N, ctx->d_dirty, ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, static_cast<double*>(hp[0]),
+            static_cast<double*>(hp[1]), static_cast<double*>(hp[2]), static_cast<double*>(hp[3]));
+        CK(cudaGetLastError());
+        mark(ctx, "export64_kernel");
+        if (ctx->S > 0)
+            CK(cudaMemcpyAsync(ctx->h_ft, ctx->d_ft, sizeof(double) * 6 * ctx->S, cudaMemcpyDeviceToHost, st));
+        rc = sync_counters(ctx);
+        if (rc) return rc;
+        const Counters& c = *ctx->h_cnt;
+        ctx->host_h2d = 24 * ((int64_t)clamp_len(c.n_inside, c.list_cap) + clamp_len(c.n_cut, c.list_cap));
+        ctx->host_d2h = 48 * (int64_t)export_chunk_cells() * c.n_export + 48 * ctx->S;
+        ctx->host_sparse = same;
+        for (int i = 0; i < 5; ++i) ctx->host64_fields[i] = f5[i];
+        ctx->host64_synced = true;
+        if (FT) std::memcpy(FT, ctx->h_ft, sizeof(double) * 6 * ctx->S);
+        return SDFIBM_OK;
+    }
+    // other host memory: whole fields staged through a device FP64 buffer
+    ctx->host64_synced = false;
+    if (!ctx->d_f64 && dalloc(&ctx->d_f64, 9 * N)) return fail(ctx, SDFIBM_ERR_CUDA, "staging allocation failed");
+    CK(cudaMemcpyAsync(ctx->d_f64, U, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
+    u64_to_planes_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(ctx->d_f64, N, ctx->d_U);
+    int rc = sdfibm_cuda_interact(ctx, time, dt, ctx->d_U, ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, nullptr);
+    if (rc) return rc;
+    double* out = ctx->d_f64 + 3 * N;
+    fields_to_f64_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(N, ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, out);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(As, out, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(Fs, out + N, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(Ts, out + 4 * N, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(Ct, out + 5 * N, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+    if (ctx->S > 0) CK(cudaMemcpyAsync(ctx->h_ft, ctx->d_ft, sizeof(double) * 6 * ctx->S, cudaMemcpyDeviceToHost, st));
+    rc = sync_counters(ctx);
+    if (rc) return rc;
+    ctx->host_h2d = 24 * N;
+    ctx->host_d2h = 48 * N + 48 * ctx->S;
+    ctx->host_sparse = false;
+    if (FT) std::memcpy(FT, ctx->h_ft, sizeof(double) * 6 * ctx->S);
+    return SDFIBM_OK;
+}
+
 int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs,
                               float* Ts, int32_t* Ct, double* FT) {
     if (!ctx) return SDFIBM_ERR_ARG;
     if (!U || !As || !Fs || !Ts || !Ct) return fail(ctx, SDFIBM_ERR_ARG, "null field pointer");
     const int64_t N = ctx->mesh.ncells;
     cudaStream_t st = ctx->stream;
-    if (!ctx->d_U && dalloc(&ctx->d_U, 3 * N)) return fail(ctx, SDFIBM_ERR_CUDA, "staging allocation failed");
+    if (int rc = ensure_staging(ctx)) return rc;
     if (!ctx->ev_u) {
         for (auto& c : ctx->copy_st) CK(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&ctx->ev_entry, cudaEventDisableTiming));
@@ -893,14 +1017,6 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
         CK(cudaEventCreate(&ctx->ev_t0));
         CK(cudaEventCreate(&ctx->ev_tu));
         CK(cudaEventCreate(&ctx->ev_tpre));
-    }
-    if (!ctx->d_As) {
-        // one bit per chunk of export_chunk_cells() cells, 32 chunks per word
-        const int64_t words = (N + 32 * (int64_t)export_chunk_cells() - 1) / (32 * (int64_t)export_chunk_cells());
-        if (dalloc(&ctx->d_As, N) || dalloc(&ctx->d_Fs, 3 * N) || dalloc(&ctx->d_Ts, N) || dalloc(&ctx->d_Ct, N) ||
-            dalloc(&ctx->d_dirty, words) ||
-            cudaMemsetAsync(ctx->d_dirty, 0, sizeof(uint32_t) * words, st) != cudaSuccess)
-            return fail(ctx, SDFIBM_ERR_CUDA, "staging allocation failed");
     }
     // U: REF-GEO's enumeration and fraction kernels take less time than copying the whole field in, so a page-locked
     // U is read in place by the coupling kernel (only at the coupling cells); otherwise U is copied in on a second
@@ -934,6 +1050,7 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
     // page-locked host fields take the cells that changed since the previous call, written in place (all of them on
     // the first call, after a change of buffers, and with dense_reset); other memory gets whole-field copies
     void* const hp[4] = {mapped_host(As), mapped_host(Fs), mapped_host(Ts), mapped_host(Ct)};
+    ctx->host64_synced = false;  // the FP64 host path's buffers no longer follow the device fields
     if (hp[0] && hp[1] && hp[2] && hp[3]) {
         const void* f5[5] = {U, As, Fs, Ts, Ct};
         bool same = ctx->host_synced && !ctx->opt.dense_reset;
@@ -1148,6 +1265,49 @@ int sdfibm_cuda_kernel_times(sdfibm_ctx* ctx, const char** names, double* ms, in
     return SDFIBM_OK;
 }
 
+// Launch configuration chosen by the autotuner, kept per workload shape for the life of the process so that a second
+// context of the same shape (a restart, a second solver instance) starts from it without timing again.
+struct Tuning {
+    int chunk_tiles, classify_grid, subsample_grid, couple_grid, mlp_grid, refgeo_grid;
+};
+static std::mutex g_tune_mu;
+static std::map<std::string, Tuning> g_tune_cache;
+
+static std::string tune_key(const sdfibm_ctx* ctx) {
+    char b[256];
+    std::snprintf(b, sizeof(b), "%d.%d.%d/%d/%d.%d.%d/%d/%d/%d", ctx->mesh.nx, ctx->mesh.ny, ctx->mesh.nz, ctx->S,
+                  ctx->opt.fraction_method, ctx->opt.subsample_n, ctx->opt.learned_fallback_n, ctx->total_tiles,
+                  ctx->num_sms, (int)ctx->model_set);
+    return b;
+}
+
+static int apply_tuning(sdfibm_ctx* ctx, const Tuning& t) {
+    std::vector<int2> ch = make_chunks(ctx->hk, t.chunk_tiles);
+    if ((int64_t)ch.size() > ctx->chunks_cap) return fail(ctx, SDFIBM_ERR_CAPACITY, "chunk table too small");
+    CK(cudaMemcpy(ctx->d_chunks, ch.data(), sizeof(int2) * ch.size(), cudaMemcpyHostToDevice));
+    ctx->chunk_tiles = t.chunk_tiles;
+    ctx->total_chunks = (int)ch.size();
+    ctx->opt.tile_cells = t.chunk_tiles * (ctx->mesh.nz <= 2 ? 8 * 8 * 2 : 4 * 4 * 4);
+    ctx->classify_grid = t.classify_grid;
+    ctx->subsample_grid = t.subsample_grid;
+    ctx->couple_grid = t.couple_grid;
+    ctx->mlp_grid = t.mlp_grid;
+    ctx->refgeo_grid = t.refgeo_grid;
+    for (auto& g : ctx->igraph) g.cur = -1;  // captured graphs hold the old launch shapes: recapture on next use
+    return SDFIBM_OK;
+}
+
+// per-kernel device times (ms) of the last interact run with timing on
+static std::map<std::string, float> last_kernel_ms(sdfibm_ctx* ctx) {
+    std::map<std::string, float> r;
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return r;
+    for (int i = 0; i < ctx->nev; ++i) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, ctx->ev[i], ctx->ev[i + 1]) == cudaSuccess) r[ctx->ev_name[i]] += t;
+    }
+    return r;
+}
+
 int sdfibm_cuda_autotune(sdfibm_ctx* ctx, double dt, const float* U, float* As, float* Fs, float* Ts, int32_t* Ct,
                          int32_t* chosen_tiles) {
     if (!ctx) return SDFIBM_ERR_ARG;
@@ -1155,51 +1315,111 @@ int sdfibm_cuda_autotune(sdfibm_ctx* ctx, double dt, const float* U, float* As, 
     if (ctx->S == 0) return SDFIBM_OK;
     if (ctx->opt.fraction_method == SDFIBM_FRACTION_LEARNED && !ctx->model_set)
         return fail(ctx, SDFIBM_ERR_STATE, "LEARNED fraction without a model: call sdfibm_cuda_set_fraction_model");
-    static const int cand[] = {2, 4, 8, 16, 32};
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
-    const int saved_timing = ctx->opt.timing;
-    ctx->opt.timing = 0;
-    int best = ctx->chunk_tiles;
-    float best_ms = 1e30f;
-    int rc = SDFIBM_OK;
-    for (int ci = 0; ci < (int)(sizeof(cand) / sizeof(cand[0])) && rc == SDFIBM_OK; ++ci) {
-        std::vector<int2> ch = make_chunks(ctx->hk, cand[ci]);
-        if ((int64_t)ch.size() > ctx->chunks_cap) continue;
-        if (cudaMemcpy(ctx->d_chunks, ch.data(), sizeof(int2) * ch.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
-            rc = fail(ctx, SDFIBM_ERR_CUDA, "chunk table upload failed");
-            break;
+    const std::string key = tune_key(ctx);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            const int rc = apply_tuning(ctx, it->second);
+            if (rc) return rc;
+            ctx->tuned_from_cache = true;
+            if (chosen_tiles) *chosen_tiles = ctx->chunk_tiles;
+            return SDFIBM_OK;
         }
-        ctx->chunk_tiles = cand[ci];
-        ctx->total_chunks = (int)ch.size();
-        float ms = 1e30f;
-        for (int rep = 0; rep < 3 && rc == SDFIBM_OK; ++rep) {
-            cudaEventRecord(e0, ctx->stream);
-            int launches = 0;
-            rc = enqueue_interact(ctx, 0.0, dt, U, As, Fs, Ts, Ct, true, launches);
-            cudaEventRecord(e1, ctx->stream);
-            if (cudaEventSynchronize(e1) != cudaSuccess) rc = fail(ctx, SDFIBM_ERR_CUDA, "autotune timing failed");
-            float t = 0.f;
-            cudaEventElapsedTime(&t, e0, e1);
-            if (rep > 0) ms = std::min(ms, t);  // the first run of each size is a warm-up
-        }
-        if (ms < best_ms) { best_ms = ms; best = cand[ci]; }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    const int sms = ctx->num_sms;
+    // candidates: classify work-item size, then the CTA count of every grid-strided or work-stealing launch (the
+    // results do not depend on any of them; each kernel is timed by its own events in the same interacts)
+    static const int tiles_cand[] = {2, 4, 8, 16, 32};
+    std::vector<int> cls_cand, cpl_cand;
+    for (int k = 1; k <= ctx->classify_occ; ++k) cls_cand.push_back(k * sms);
+    for (int k = 1; k <= ctx->couple_occ; k *= 2) cpl_cand.push_back(k * sms);
+    if (cpl_cand.back() != ctx->couple_occ * sms) cpl_cand.push_back(ctx->couple_occ * sms);
+    const std::vector<int> sub_cand = {2 * sms, 4 * sms, 8 * sms, 16 * sms};
+    const std::vector<int> mlp_cand = {1 * sms, 2 * sms, 4 * sms, 8 * sms};
+    const std::vector<int> rg_cand = {2 * sms, 4 * sms, 8 * sms, 16 * sms};
+    const int saved_timing = ctx->opt.timing;
+    ctx->opt.timing = 1;
+    Tuning best{ctx->chunk_tiles, ctx->classify_grid, ctx->subsample_grid, ctx->couple_grid, ctx->mlp_grid,
+                ctx->refgeo_grid};
+    int rc = SDFIBM_OK;
+    // min over two timed interacts (after one warm-up) of each kernel's time under configuration t
+    auto measure = [&](const Tuning& t, std::map<std::string, float>& out) {
+        int r = apply_tuning(ctx, t);
+        for (int rep = 0; rep < 3 && r == SDFIBM_OK; ++rep) {
+            int launches = 0;
+            ctx->cur ^= 1;
+            mark_begin(ctx);
+            r = enqueue_interact(ctx, 0.0, dt, U, As, Fs, Ts, Ct, true, launches);
+            if (r) break;
+            auto ms = last_kernel_ms(ctx);
+            if (rep == 0) continue;
+            for (auto& kv : ms) out[kv.first] = out.count(kv.first) ? std::min(out[kv.first], kv.second) : kv.second;
+        }
+        return r;
+    };
+    // 1. work-item size of the classify queue (classify time)
+    float best_cls = 1e30f;
+    for (int tc : tiles_cand) {
+        Tuning t = best;
+        t.chunk_tiles = tc;
+        if ((int64_t)make_chunks(ctx->hk, tc).size() > ctx->chunks_cap) continue;
+        std::map<std::string, float> ms;
+        if ((rc = measure(t, ms))) break;
+        if (ms.count("classify_kernel") && ms["classify_kernel"] < best_cls) {
+            best_cls = ms["classify_kernel"];
+            best.chunk_tiles = tc;
+        }
+    }
+    // 2. CTA counts: candidate i of every list at once, each kernel keeps its fastest
+    struct Knob {
+        const char* kernel;
+        const std::vector<int>* cand;
+        int Tuning::*grid;
+    };
+    const Knob knobs[5] = {{"classify_kernel", &cls_cand, &Tuning::classify_grid},
+                           {"subsample_cells_kernel", &sub_cand, &Tuning::subsample_grid},
+                           {"couple_kernel", &cpl_cand, &Tuning::couple_grid},
+                           {"mlp_infer_kernel", &mlp_cand, &Tuning::mlp_grid},
+                           {"refgeo_cells_kernel", &rg_cand, &Tuning::refgeo_grid}};
+    float bt[5] = {1e30f, 1e30f, 1e30f, 1e30f, 1e30f};
+    size_t rounds = 0;
+    for (const Knob& kb : knobs) rounds = std::max(rounds, kb.cand->size());
+    Tuning chosen = best;
+    for (size_t i = 0; i < rounds && rc == SDFIBM_OK; ++i) {
+        Tuning t = best;
+        for (const Knob& kb : knobs) t.*kb.grid = (*kb.cand)[std::min(i, kb.cand->size() - 1)];
+        std::map<std::string, float> ms;
+        if ((rc = measure(t, ms))) break;
+        for (int k = 0; k < 5; ++k) {
+            auto it = ms.find(knobs[k].kernel);
+            if (it != ms.end() && it->second < bt[k]) {
+                bt[k] = it->second;
+                chosen.*knobs[k].grid = t.*knobs[k].grid;
+            }
+        }
+    }
     ctx->opt.timing = saved_timing;
     if (rc != SDFIBM_OK) return rc;
-    std::vector<int2> ch = make_chunks(ctx->hk, best);
-    CK(cudaMemcpy(ctx->d_chunks, ch.data(), sizeof(int2) * ch.size(), cudaMemcpyHostToDevice));
-    ctx->chunk_tiles = best;
-    ctx->total_chunks = (int)ch.size();
-    ctx->opt.tile_cells = best * (ctx->mesh.nz <= 2 ? 8 * 8 * 2 : 4 * 4 * 4);
-    for (auto& g : ctx->igraph) g.cur = -1;  // captured graphs hold the old table size: recapture on next use
+    rc = apply_tuning(ctx, chosen);
+    if (rc) return rc;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = chosen;
+    }
+    ctx->tuned_from_cache = false;
     // the fields hold a complete dense interact of the current state; the next call starts from the same buffers
     ctx->interacted = false;
-    if (chosen_tiles) *chosen_tiles = best;
+    if (chosen_tiles) *chosen_tiles = chosen.chunk_tiles;
     return sync_counters(ctx);
+}
+
+int sdfibm_cuda_tuning(sdfibm_ctx* ctx, int32_t* out, int32_t n) {
+    if (!ctx || !out) return SDFIBM_ERR_ARG;
+    const int32_t v[7] = {ctx->chunk_tiles, ctx->classify_grid, ctx->subsample_grid, ctx->couple_grid, ctx->mlp_grid,
+                          ctx->refgeo_grid, (int32_t)ctx->tuned_from_cache};
+    for (int i = 0; i < n && i < 7; ++i) out[i] = v[i];
+    return SDFIBM_OK;
 }
 
 int sdfibm_cuda_set_fraction_model(sdfibm_ctx* ctx, const float* params, float tau_twist, float tau_grad) {
@@ -1255,6 +1475,7 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
     if (ctx->d_rq) cudaFree(ctx->d_rq);
     if (ctx->d_ovf) cudaFree(ctx->d_ovf);
     if (ctx->d_dirty) cudaFree(ctx->d_dirty);
+    if (ctx->d_f64) cudaFree(ctx->d_f64);
     if (ctx->d_fsums) cudaFree(ctx->d_fsums);
     if (ctx->d_recs) cudaFree(ctx->d_recs);
     if (ctx->d_fsums_excl) cudaFree(ctx->d_fsums_excl);

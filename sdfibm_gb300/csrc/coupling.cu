@@ -913,6 +913,82 @@ __global__ void export_kernel(Counters* cnt, int64_t N, uint32_t* __restrict__ d
     if (lane == 0 && chunks) atomicAdd(&cnt->n_export, chunks);
 }
 
+// ---- FP64 host fields in OpenFOAM's own layout (sdfibm_cuda_interact_host64) -------------------------------------
+// U is a volVectorField (one x,y,z triple per cell), As / Ts / Ct volScalarFields and Fs a volVectorField, all FP64
+// in page-locked host memory.  gather_u64_kernel reads U at the coupling cells only (24 contiguous bytes per cell)
+// into the FP32 device plane layout the coupling kernel reads; export64_kernel writes the marked 8-cell chunks of
+// the four result fields back in FP64.
+__global__ void gather_u64_kernel(const int32_t* __restrict__ in_cell, const int32_t* __restrict__ cut_cell,
+                                  const Counters* cnt, int64_t N, const double* __restrict__ hU,
+                                  float* __restrict__ U) {
+    const int64_t n0 = clamp_len(cnt->n_inside, cnt->list_cap), n1 = clamp_len(cnt->n_cut, cnt->list_cap);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n0 + n1; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = e < n0 ? in_cell[e] : cut_cell[e - n0];
+        if (c < 0 || c >= N) continue;
+        const double x = hU[3 * c], y = hU[3 * c + 1], z = hU[3 * c + 2];
+        U[c] = (float)x;
+        U[N + c] = (float)y;
+        U[2 * N + c] = (float)z;
+    }
+}
+
+// all chunks marked (the first call on a set of host fields writes every cell)
+__global__ void mark_all_kernel(uint32_t* __restrict__ dirty, int64_t words) {
+    for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < words; w += (int64_t)gridDim.x * blockDim.x)
+        dirty[w] = 0xffffffffu;
+}
+
+__global__ void export64_kernel(Counters* cnt, int64_t N, uint32_t* __restrict__ dirty, const float* __restrict__ As,
+                                const float* __restrict__ Fs, const float* __restrict__ Ts,
+                                const int32_t* __restrict__ Ct, double* hAs, double* hFs, double* hTs, double* hCt) {
+    const int lane = threadIdx.x & 31;
+    const int64_t words = (N + 32 * EXPORT_CHUNK - 1) >> (EXPORT_LG + 5);
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    int chunks = 0;
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += nw) {
+        const uint32_t word = dirty[w];
+        if (!word) continue;
+        chunks += __popc(word);
+#pragma unroll
+        for (int t = 0; t < EXPORT_CHUNK; ++t) {
+            const int64_t c = (w << (EXPORT_LG + 5)) + 32 * t + lane;
+            if (((word >> ((32 * t + lane) >> EXPORT_LG)) & 1u) && c < N) {
+                hAs[c] = (double)As[c];
+                hTs[c] = (double)Ts[c];
+                hCt[c] = (double)Ct[c];
+                hFs[3 * c] = (double)Fs[c];
+                hFs[3 * c + 1] = (double)Fs[N + c];
+                hFs[3 * c + 2] = (double)Fs[2 * N + c];
+            }
+        }
+        __syncwarp();
+        if (lane == 0) dirty[w] = 0u;
+    }
+    if (lane == 0 && chunks) atomicAdd(&cnt->n_export, chunks);
+}
+
+// whole-field conversions of the FP64 path for host memory the GPU cannot address (staged through device copies)
+__global__ void u64_to_planes_kernel(const double* __restrict__ U64, int64_t N, float* __restrict__ U) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < N; c += (int64_t)gridDim.x * blockDim.x) {
+        U[c] = (float)U64[3 * c];
+        U[N + c] = (float)U64[3 * c + 1];
+        U[2 * N + c] = (float)U64[3 * c + 2];
+    }
+}
+__global__ void fields_to_f64_kernel(int64_t N, const float* __restrict__ As, const float* __restrict__ Fs,
+                                     const float* __restrict__ Ts, const int32_t* __restrict__ Ct,
+                                     double* __restrict__ out) {
+    // out: As[N], Fs[N][3], Ts[N], Ct[N]
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < N; c += (int64_t)gridDim.x * blockDim.x) {
+        out[c] = (double)As[c];
+        out[N + 3 * c] = (double)Fs[c];
+        out[N + 3 * c + 1] = (double)Fs[N + c];
+        out[N + 3 * c + 2] = (double)Fs[2 * N + c];
+        out[4 * N + c] = (double)Ts[c];
+        out[5 * N + c] = (double)Ct[c];
+    }
+}
+
 // SolidCloud::fixInternal over the ALL_INSIDE list: U = rigid velocity of the solid that owns the cell
 __global__ void fix_internal_kernel(MeshK m, const sdfibm_solid_state* __restrict__ st,
                                     const int32_t* __restrict__ in_cell, const int32_t* __restrict__ in_solid,

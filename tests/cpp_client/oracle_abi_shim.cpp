@@ -70,6 +70,27 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* c, double time, double dt, const float
     return SDFIBM_OK;
 }
 
+/* FP64 fields in OpenFOAM's layout (U and Fs one x,y,z triple per cell), U rounded to FP32 first as the GPU does */
+int sdfibm_cuda_interact_host64(sdfibm_ctx* c, double time, double dt, const double* U, double* As, double* Fs,
+                                double* Ts, double* Ct, double* FT) {
+    if (!c || !U || !As || !Fs || !Ts || !Ct) return SDFIBM_ERR_ARG;
+    const int64_t N = c->N;
+    for (int64_t i = 0; i < N; ++i)
+        for (int a = 0; a < 3; ++a) c->U[(size_t)(a * N + i)] = (double)(float)U[3 * i + a];
+    if (oracle_interact(c->oc, time, dt, c->U.data(), c->As.data(), c->Fs.data(), c->Ts.data(), c->Ct.data(), FT) !=
+        0) {
+        c->err = "oracle interact failed";
+        return SDFIBM_ERR_ARG;
+    }
+    for (int64_t i = 0; i < N; ++i) {
+        As[i] = (double)(float)c->As[(size_t)i];
+        Ts[i] = (double)(float)c->Ts[(size_t)i];
+        Ct[i] = (double)c->Ct[(size_t)i];
+        for (int a = 0; a < 3; ++a) Fs[3 * i + a] = (double)(float)c->Fs[(size_t)(a * N + i)];
+    }
+    return SDFIBM_OK;
+}
+
 /* the device-pointer entry point: here every pointer is host memory */
 int sdfibm_cuda_interact(sdfibm_ctx* c, double time, double dt, const float* U, float* As, float* Fs, float* Ts,
                          int32_t* Ct, double* FT) {

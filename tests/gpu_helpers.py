@@ -41,13 +41,24 @@ def run_pair(torch, w, steps=1, evolve=False, fix=False, U=None, gpu_opt=None, g
     return dict(gpu=gpu, orc=orc, fd=fd, fo=fo, FT=out, Ud=Ud, Uo=Uo)
 
 
-def ft_scale(w, orc, fo_U, s):
+def centres(m, cells):
+    """Cell centres [3, n] of cell labels (numpy)."""
+    cells = np.asarray(cells, dtype=np.int64)
+    i = cells % m.nx
+    j = (cells // m.nx) % m.ny
+    k = cells // (m.nx * m.ny)
+    return np.stack([m.origin[0] + (i + 0.5) * m.h[0], m.origin[1] + (j + 0.5) * m.h[1],
+                     m.origin[2] + (k + 0.5) * m.h[2]])
+
+
+def ft_scale(w, orc, fo_U, s, cells=None, st=None):
     """rho_f * V/dt * sum over the solid's cells of |U - u_s| (and of |C-x| |U - u_s| for the torque)."""
-    cells, _ = orc.touched(s)
+    if cells is None:
+        cells, _ = orc.touched(s)
     N = orc.N
     U = fo_U.reshape(3, N)[:, cells]
-    st = orc.get_state()[s]
-    C = np.array([_centre(w.mesh, c) for c in cells]).T if len(cells) else np.zeros((3, 0))
+    st = (st if st is not None else orc.get_state())[s]
+    C = centres(w.mesh, cells)
     x = np.array(st.pos)[:, None]
     v = np.array(st.vel)[:, None]
     om = np.array(st.omega)
@@ -60,10 +71,7 @@ def ft_scale(w, orc, fo_U, s):
 
 
 def _centre(m, c):
-    i = c % m.nx
-    j = (c // m.nx) % m.ny
-    k = c // (m.nx * m.ny)
-    return (m.origin[0] + (i + 0.5) * m.h[0], m.origin[1] + (j + 0.5) * m.h[1], m.origin[2] + (k + 0.5) * m.h[2])
+    return tuple(centres(m, [c])[:, 0])
 
 
 def check_interact(w, r, U_used=None):
@@ -90,15 +98,19 @@ def check_interact(w, r, U_used=None):
     # Fs is relative-accurate per contribution; where several solids touch one cell their contributions can cancel,
     # so there the bound is taken against the sum of the contributions' magnitudes
     scale = np.abs(o).copy()
+    touched = [orc.touched(s)[0] for s in range(S)]
+    allc = np.concatenate(touched) if S else np.zeros(0, np.int64)
+    alls = np.concatenate([np.full(len(t), s) for s, t in enumerate(touched)]) if S else np.zeros(0, np.int64)
+    uc, cnt = np.unique(allc, return_counts=True)
+    shared = set(uc[cnt > 1].tolist())
     owners = {}
-    for s in range(S):
-        for c in orc.touched(s)[0]:
-            owners.setdefault(int(c), []).append(s)
+    if shared:
+        for c, s in zip(allc.tolist(), alls.tolist()):
+            if c in shared:
+                owners.setdefault(c, []).append(s)
     Uo = r["Uo"].reshape(3, N) if U_used is None else U_used.reshape(3, N)
     st = orc.get_state()
     for c, ss in owners.items():
-        if len(ss) < 2:
-            continue
         C = np.array(_centre(w.mesh, c))
         mag = np.zeros(3)
         for s in ss:
@@ -112,8 +124,9 @@ def check_interact(w, r, U_used=None):
     FTg, FTo = r["FT"][-1]
     Uo = r["Uo"] if U_used is None else U_used
     worst = 0.0
+    states = orc.get_state()
     for s in range(S):
-        sf, st = ft_scale(w, orc, Uo, s)
+        sf, st = ft_scale(w, orc, Uo, s, cells=touched[s], st=states)
         ef = np.linalg.norm(FTg[s, :3] - FTo[s, :3]) / sf
         et = np.linalg.norm(FTg[s, 3:] - FTo[s, 3:]) / st
         worst = max(worst, ef, et)

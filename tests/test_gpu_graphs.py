@@ -57,7 +57,8 @@ def test_graph_replay_is_bit_identical(cuda_lib, torch_cuda, cfg):
 
 
 def test_autotune_keeps_results(cuda_lib, torch_cuda):
-    """The autotuner only changes the classify work-item size: fields and forces equal an untuned context's."""
+    """The autotuner only changes the launch configuration (classify work-item size, CTA counts): fields and forces
+    equal an untuned context's, and a second context of the same shape takes the choice from the cache."""
     torch = torch_cuda
     w = workloads.poly3d_256(scale=0.25)
     w.opt.fraction_method = abi.FRACTION_SUBSAMPLE
@@ -73,5 +74,21 @@ def test_autotune_keeps_results(cuda_lib, torch_cuda):
     for k in fa:
         assert torch.equal(fa[k], fb[k]), k
     np.testing.assert_allclose(FTa, FTb, rtol=1e-12, atol=1e-14)
+    t = b.tuning()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert t["classify_tiles_per_item"] == chosen and t["from_cache"] == 0
+    for k in ("classify_ctas", "subsample_ctas", "couple_ctas", "mlp_ctas", "refgeo_ctas"):
+        assert t[k] > 0 and t[k] % sms == 0, (k, t)
+    c = SolidCloud(w.mesh, w.solids, w.opt)
+    fc = c.new_fields()
+    assert c.autotune(w.dt, U, fc) == chosen
+    tc = c.tuning()
+    assert tc["from_cache"] == 1 and {k: v for k, v in tc.items() if k != "from_cache"} == \
+        {k: v for k, v in t.items() if k != "from_cache"}
+    FTc = c.interact(0.0, w.dt, U, fc)
+    for k in fa:
+        assert torch.equal(fa[k], fc[k]), k
+    np.testing.assert_allclose(FTa, FTc, rtol=1e-12, atol=1e-14)
     a.close()
     b.close()
+    c.close()

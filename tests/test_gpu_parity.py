@@ -203,3 +203,52 @@ def test_interact_host_pinned_in_place(cuda_lib, torch_cuda, cfg):
         a.evolve(t, w.dt)
         b.evolve(t, w.dt)
         t += w.dt
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_interact_host64_matches_device(cuda_lib, torch_cuda, pinned):
+    """FP64 host fields in OpenFOAM's layout (U and Fs one x,y,z triple per cell, Ct as doubles), page-locked (read
+    and written in place) or pageable (staged): every step equals the device-field path on the same U, and a change
+    of buffers writes every cell again."""
+    from sdfibm_gb300.cloud import SolidCloud
+    torch = torch_cuda
+    w = workloads.poly3d_512(scale=0.0625)
+    N = w.ncells
+    U32 = w.U_numpy()                                    # [3][N] FP32
+    U64 = np.ascontiguousarray(U32.T.astype(np.float64))  # [N][3]: the FP32 values, exactly
+    a = SolidCloud(w.mesh, w.solids, w.opt)
+    b = SolidCloud(w.mesh, w.solids, w.opt)
+    fd = a.new_fields()
+    Ud = torch.from_numpy(U32).cuda()
+
+    def host(shape, fill):
+        t = torch.full(shape, fill, dtype=torch.float64)
+        return (t.pin_memory() if pinned else t).numpy()
+
+    def fields():
+        return {"As": host((N,), 7.0), "Fs": host((N, 3), 7.0), "Ts": host((N,), 7.0), "Ct": host((N,), 7.0)}
+
+    Uh = torch.from_numpy(U64)
+    Uh = (Uh.pin_memory() if pinned else Uh).numpy()
+    hn = fields()
+    t = 0.0
+    for step in range(4):
+        if step == 3:
+            hn = fields()
+        FTa = a.interact(t, w.dt, Ud, fd)
+        FTb = b.interact_host64(t, w.dt, Uh, hn)
+        assert np.array_equal(fd["As"].cpu().numpy().astype(np.float64), hn["As"]), step
+        assert np.array_equal(fd["Ts"].cpu().numpy().astype(np.float64), hn["Ts"]), step
+        assert np.array_equal(fd["Ct"].cpu().numpy().astype(np.float64), hn["Ct"]), step
+        assert np.array_equal(fd["Fs"].cpu().numpy().astype(np.float64).T, hn["Fs"]), step
+        assert np.allclose(FTa, FTb, rtol=1e-12, atol=1e-14)
+        st = b.stats()
+        assert st["host_sparse"] == (1 if pinned and step in (1, 2) else 0), step
+        if st["host_sparse"]:
+            assert st["host_h2d_bytes"] == 24 * st["coupling_cells"]
+            assert 0 < st["host_d2h_bytes"] < 48 * N
+        a.evolve(t, w.dt)
+        b.evolve(t, w.dt)
+        t += w.dt
+    a.close()
+    b.close()
