@@ -166,9 +166,10 @@ def abi_shape_name(t):
     return {v: k for k, v in abi.SHAPE_NAMES.items()}.get(int(t), str(t))
 
 
-def make_cloud(w, method, subsample_n=None, stream=None, timing=False, band=None):
-    """A coupling context of workload w with the given fraction method (the learned model loaded if needed).
-    With a stream the context replays CUDA graphs of its steps; with timing it records per-kernel events instead."""
+def make_cloud(w, method, subsample_n=None, stream=None, timing=False, band=None, params=None):
+    """A coupling context of workload w with the given fraction method (the learned model loaded if needed: its
+    shipped band, or band = (tau_refine, rho_min); its parameters, or `params`).  With a stream the context replays
+    CUDA graphs of its steps; with timing it records per-kernel events instead."""
     import copy
 
     from sdfibm_gb300 import abi, learned
@@ -181,10 +182,10 @@ def make_cloud(w, method, subsample_n=None, stream=None, timing=False, band=None
     opt.graphs = 0 if timing else 1
     cloud = SolidCloud(w.mesh, w.solids, opt, stream=stream)
     if method == "learned":
-        params, tt, tg, meta = learned.load_model()
+        p, tau, rho, meta = learned.load_model()
         if band is not None:
-            tt, tg = band[0], band[1]
-        cloud.set_fraction_model(params, tt, tg)
+            tau, rho = band
+        cloud.set_fraction_model(p if params is None else params, tau, rho)
     return cloud
 
 
@@ -217,40 +218,43 @@ def time_steps(torch, cloud, w, U, f, steps, warmup, flush, stream=None, kernel_
                 launches=launches, kernel_ms={k: sum(v) / len(v) for k, v in kt.items()}, stats=st)
 
 
-def reference16(w, U):
-    """Fields and forces of one SUBSAMPLE(16^3) step (its classifications equal the FP64 oracle's)."""
-    ref = make_cloud(w, "subsample", subsample_n=16)
+def reference16(w, U, n=16):
+    """Fields and forces of one SUBSAMPLE(n^3) step (its classifications equal the FP64 oracle's)."""
+    import copy
+    if n > 16:  # about 3 undecided points per 32^3 cell: a recheck list that holds them
+        w = copy.copy(w)
+        w.opt = copy.copy(w.opt)
+        w.opt.recheck_cap = 1 << 26
+    ref = make_cloud(w, "subsample", subsample_n=n)
     fr = ref.new_fields()
     FTr = ref.interact(0.0, w.dt, U, fr)
     ref.close()
     return fr, FTr
 
 
-def accuracy(torch, w, cloud, U, ref):
-    """Learned As and per-solid force against SUBSAMPLE(16^3) on the same step."""
-    import numpy as np
+def converged(torch, w, U, methods):
+    """As and per-solid force of each method against a SUBSAMPLE 32^3 step (32768 samples per cut cell)."""
+    ref = reference16(w, U, n=32)
+    out = {}
+    for name, m in methods.items():
+        if isinstance(m, tuple):
+            c = make_cloud(w, m[0], subsample_n=m[1])
+            a = accuracy(torch, w, c, U, ref, reference="SUBSAMPLE 32^3 (32768 samples), same step")
+            c.close()
+        else:
+            a = accuracy(torch, w, m, U, ref, reference="SUBSAMPLE 32^3 (32768 samples), same step")
+        out[name] = {k: v for k, v in a.items() if k.startswith("as_") or k.startswith("force_")}
+    return out
+
+
+def accuracy(torch, w, cloud, U, ref, reference="SUBSAMPLE 16^3 (4096 samples), same step"):
+    """As and per-solid force of one step of `cloud` against the reference step `ref` (learned.accuracy)."""
+    from sdfibm_gb300 import learned
     fr, FTr = ref
     fl = cloud.new_fields()
     torch.cuda.synchronize()  # the fields are zeroed on torch's stream; the context may run on another
     FTl = cloud.interact(0.0, w.dt, U, fl)
-    touched = fr["Ct"] != 0
-    cut = touched & ~((fr["As"] == 1.0) & (fl["As"] == 1.0))
-    err = (fl["As"] - fr["As"]).abs()[cut].double()
-    q = torch.quantile(err[: 1 << 24], torch.tensor([0.5, 0.99, 0.999], dtype=torch.float64, device=err.device))
-    # force error per solid, normwise against rho_f / dt * volume * (|U| rms + |v| + |omega| r): the magnitude of the
-    # sum of the cell contributions
-    u_rms = float(U.square().mean().sqrt())
-    rel = []
-    for s, d in enumerate(w.solids):
-        v = np.linalg.norm(np.array(d.vel[:])) + np.linalg.norm(np.array(d.omega[:])) * d.shape.radiusB
-        scale = w.opt.rho_f / w.dt * d.shape.volume * (u_rms + v)
-        rel.append(np.linalg.norm(FTl[s, :3] - FTr[s, :3]) / scale)
-    rel = np.array(rel)
-    return {"reference": "SUBSAMPLE 16^3 (4096 samples), same step", "cut_cells": int(cut.sum()),
-            "as_abs_err_mean": float(err.mean()), "as_abs_err_p50": float(q[0]), "as_abs_err_p99": float(q[1]),
-            "as_abs_err_p999": float(q[2]), "as_abs_err_max": float(err.max()),
-            "force_rel_err_median": float(np.median(rel)), "force_rel_err_p90": float(np.percentile(rel, 90)),
-            "force_rel_err_max": float(rel.max())}
+    return learned.accuracy(torch, w, fl, FTl, fr, FTr, U, reference=reference)
 
 
 class CpuReference:
@@ -580,25 +584,32 @@ def main():
         plain12.close()
         del f12
         acc = accuracy(torch, w, cloud, U, ref)
-        # other operating points of the same model: the open band and the 10^3 fallback
+        # other operating points of the same model: the open band, and its prior alone (what the network adds)
+        from sdfibm_gb300 import learned
+        p_model = learned.load_model()[0]
+        p_prior = p_model.copy()
+        p_prior[-65:] = 0.0  # network output zero: a = clamp(P4), the 4^3 sub-cell planar reconstruction
         points = []
-        for label, band, fb in (("open band (network on every cut cell)", (1e30, 1e30), None),
-                                ("same band, SUBSAMPLE 10^3 fallback", None, 10)):
-            import copy
-            w2 = copy.copy(w)
-            w2.opt = copy.copy(w.opt)
-            if fb:
-                w2.opt.learned_fallback_n = fb
-            c2 = make_cloud(w2, "learned", stream=stream, band=band)
+        for label, band, params in (("open band (network on every cut cell)", (1e30, 0.0), None),
+                                    ("prior alone (4^3 sub-cell planar reconstruction, no network), open band",
+                                     (1e30, 0.0), p_prior)):
+            c2 = make_cloud(w, "learned", stream=stream, band=band, params=params)
             with torch.cuda.stream(stream):
                 f2 = c2.new_fields()
-            t2 = time_steps(torch, c2, w2, U, f2, args.steps, args.warmup, flush, stream=stream)
-            a2 = accuracy(torch, w2, c2, U, ref)
+            torch.cuda.synchronize()
+            if not args.no_autotune:
+                c2.autotune(w.dt, U, f2)
+            t2 = time_steps(torch, c2, w, U, f2, args.steps, args.warmup, flush, stream=stream)
+            a2 = accuracy(torch, w, c2, U, ref)
             points.append(dict({"band": label, "ms_per_step": t2["ms_step"],
                                 "value": t2["cells"] * world / (t2["ms_step"] * 1e-3),
                                 "fallback_cells": t2["stats"].get("learned_fallback_cells")}, **a2))
             c2.close()
             del f2
+        # every method against a converged lattice (SUBSAMPLE 32^3, 32768 samples per cut cell): how close each is
+        # to the true solid fraction, beside the contract's 16^3 judge
+        conv = converged(torch, w, U, {"learned": cloud, "plain_10": ("subsample", 10),
+                                       "plain_12": ("subsample", 12), "plain_16": ("subsample", 16)})
         del ref
         pick = lambda a: {k: v for k, v in a.items() if k.startswith("as_") or k.startswith("force_")}
         compare = {"plain": dict({"method": "SUBSAMPLE 10^3 samples per cut cell", "ms_per_step": tp["ms_step"],
@@ -612,7 +623,8 @@ def main():
                    "speedup_vs_plain_12": t12["ms_step"] / tm["ms_step"],
                    "learned_cells": st.get("learned_cells"), "fallback_cells": st.get("learned_fallback_cells"),
                    "fallback_share": (st.get("learned_fallback_cells") or 0) / max(1, st.get("learned_cells") or 1),
-                   "accuracy": acc, "other_operating_points": points}
+                   "accuracy": acc, "other_operating_points": points,
+                   "against_converged_32": conv}
 
     # full time step (interact + evolve with its sub-steps and collisions + fixInternal), device time, graphs
     with torch.cuda.stream(stream):

@@ -86,7 +86,7 @@ typedef enum sdfibm_collision_mode {
 typedef enum sdfibm_fraction_method {
     SDFIBM_FRACTION_REFGEO = 0,     /* GeometricTools::calcCellVolume (geometrictools.cpp:47-116), FP64 */
     SDFIBM_FRACTION_SUBSAMPLE = 1,  /* stratified midpoint lattice of n^3 (3D) / n^2 (2D) isInside samples */
-    SDFIBM_FRACTION_LEARNED = 2     /* 11-64-64-1 MLP on vertex SDFs, SUBSAMPLE fallback outside the band */
+    SDFIBM_FRACTION_LEARNED = 2     /* sub-cell planar prior + 16-64-64-1 network, SUBSAMPLE outside the band */
 } sdfibm_fraction_method;
 
 typedef struct sdfibm_mesh_desc {
@@ -169,6 +169,22 @@ void sdfibm_options_default(sdfibm_options* opt);
  * reserves device work space.  stream may be NULL (legacy default stream). */
 int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* solids, int32_t nsolids,
                        const sdfibm_options* opt, void* cuda_stream, sdfibm_ctx** out);
+
+/* SolidCloud::SolidCloud on an explicit OpenFOAM polyMesh (graded, multi-block or polyhedral meshes; MeshInfo,
+ * src/meshinfo.h:20-29), from the polyMesh lists: points [npoints][3]; faces as a compact list, face f having the
+ * point labels face_lab[face_off[f] .. face_off[f + 1]); owner [nfaces]; neighbour [ninternal] (internal faces
+ * first).  twod as in sdfibm_mesh_desc.  Face and cell geometry follow OpenFOAM's primitiveMesh (triangle fan and
+ * pyramid decompositions); cellPoints are in ascending label order.  The same entry points then serve the context:
+ * interact (the reference's breadth-first enumeration from the nearest cell centre, CellEnumerator, and its
+ * REF-GEO fraction over the cells' faces, GeometricTools::calcCellVolume; fields reset over the whole mesh as
+ * the reference does), evolve, fix_internal (with the mesh's cell centres), the host-field entry points (whole
+ * fields copied) and touched.  Only SDFIBM_FRACTION_REFGEO is offered; graphs are off.  Limit: cells x solids
+ * <= 2^28 (the per-solid search lists). */
+int sdfibm_cuda_create_polymesh(const double* points, int64_t npoints, const int32_t* face_off,
+                                const int32_t* face_lab, int64_t nfaces, const int32_t* owner,
+                                const int32_t* neighbour, int64_t ninternal, int32_t twod,
+                                const sdfibm_solid_desc* solids, int32_t nsolids, const sdfibm_options* opt,
+                                void* cuda_stream, sdfibm_ctx** out);
 
 /* SolidCloud::interact (solidcloud.cpp:435-464): resets As/Fs/Ts/Ct, enumerates the touched cells of every solid
  * (CellEnumerator, cellenumerator.cpp:6-78), computes As (REF-GEO / SUBSAMPLE / LEARNED), the direct forcing
@@ -261,11 +277,12 @@ int sdfibm_cuda_tuning(sdfibm_ctx* ctx, int32_t* out, int32_t n);
 
 /* No counterpart in the reference (which has only the apex/pyramid fraction).  Installs the learned cut-cell
  * fraction model used when options.fraction_method is SDFIBM_FRACTION_LEARNED: params is a HOST array of
- * SDFIBM_MLP_NPARAM floats in the layout of include/sdfibm_mlp.h; cells whose features fall outside the band
- * (face twist sum > tau_twist or | |trilinear gradient| - 1 | > tau_grad) are evaluated by SUBSAMPLE with
- * options.learned_fallback_n samples per axis (a negative limit closes the band: every cut cell falls back).
- * Reserves the per-cell feature buffers on first use. */
-int sdfibm_cuda_set_fraction_model(sdfibm_ctx* ctx, const float* params, float tau_twist, float tau_grad);
+ * SDFIBM_MLP_NPARAM floats in the layout of include/sdfibm_mlp.h.  Confidence band: a cut cell takes the model's
+ * fraction when its two sub-cell planar reconstructions agree, |P4 - P2| <= tau_refine, and its solid's bounding
+ * radius spans at least rho_min cells; other cells are evaluated by SUBSAMPLE with options.learned_fallback_n samples
+ * per axis (a negative tau_refine closes the band: every cut cell falls back).  Reserves the per-cell input buffers
+ * on first use. */
+int sdfibm_cuda_set_fraction_model(sdfibm_ctx* ctx, const float* params, float tau_refine, float rho_min);
 
 /* Per-kernel device time (milliseconds, CUDA events on the context's stream) of the last interact when
  * options.timing is set: names[i] receives a static kernel name, ms[i] its time; returns the count through *n. */

@@ -2,19 +2,26 @@
  *
  * No counterpart in the reference: sdfibm computes the solid fraction of a cut cell only with the apex / pyramid
  * geometry of GeometricTools::calcCellVolume (src/geometrictools.cpp:47-116).  These entry points build, train and
- * run a small network that predicts the SUBSAMPLE fraction (a stratified n^3 lattice of Shape::isInside tests,
- * SDFIBM_FRACTION_SUBSAMPLE in sdfibm_cuda.h) from the signed distances at the cell's vertices.  The coupling path
- * uses it with options.fraction_method = SDFIBM_FRACTION_LEARNED after sdfibm_cuda_set_fraction_model.
+ * run a model that predicts the SUBSAMPLE fraction (a stratified n^3 lattice of Shape::isInside tests,
+ * SDFIBM_FRACTION_SUBSAMPLE in sdfibm_cuda.h) from signed distances sampled in the cell.  The coupling path uses it
+ * with options.fraction_method = SDFIBM_FRACTION_LEARNED after sdfibm_cuda_set_fraction_model.
  *
- * Network: 11 features -> 64 -> 64 -> 1, SiLU hidden units, sigmoid output.
- *   features: phi(v)/h at the 8 vertices (OpenFOAM cellPoints order of a hex: (i,j,k) (i+1,j,k) (i,j+1,k)
- *             (i+1,j+1,k), then the same at k+1), then the unit trilinear gradient of those values at the centre.
- *   numerics: the hidden layers run on the tensor cores (tcgen05, BF16 x BF16 -> FP32 in tensor memory) with W1, W2
- *             rounded to BF16; features and first-layer activations are split into a hi + lo pair of BF16 values, so
- *             the products keep about 16 significant bits; biases, the output layer and the sigmoid are FP32.
- * Parameters: one FP32 array of SDFIBM_MLP_NPARAM values, W1[64][11], b1[64], W2[64][64], b2[64], w3[64], b3
+ * Model: a = sigmoid(logit(P4) + network(x)).
+ *   stencil: Shape::signedDistance at the 5 x 5 x 5 lattice of the cell (spacing h/4 per axis, vertices included).
+ *   P4, P2: sub-cell planar reconstructions of the fraction: the cell cut into 4^3 (2^3) sub-cells, each sub-cell's
+ *           fraction the exact cube-plane volume under the plane fitted to its 8 corner distances (Scardovelli &
+ *           Zaleski, J. Comput. Phys. 164 (2000)), averaged; both clamped to [1e-4, 1 - 1e-4].
+ *   x (16 network inputs): phi/h at the 8 vertices (OpenFOAM cellPoints order of a hex: (i,j,k) (i+1,j,k) (i,j+1,k)
+ *           (i+1,j+1,k), then the same at k+1), at the 6 face centres (-x, +x, -y, +y, -z, +z), at the cell centre,
+ *           then logit(P2).
+ *   network: 16 -> 64 -> 64 -> 1, SiLU hidden units; the hidden layers run on the tensor cores (tcgen05, BF16 x BF16
+ *           -> FP32 in tensor memory) with W1, W2 rounded to BF16; inputs and first-layer activations are split into
+ *           a hi + lo pair of BF16 values, so the products keep about 16 significant bits; biases, the output layer
+ *           and the sigmoid are FP32.
+ * Parameters: one FP32 array of SDFIBM_MLP_NPARAM values, W1[64][16], b1[64], W2[64][64], b2[64], w3[64], b3
  *             (row = output unit).
- * Features are stored structure-of-arrays: feature f of cell c at feat[f * stride + c].
+ * Feature buffers are structure-of-arrays with SDFIBM_MLP_NFEAT rows: row f < 16 is input f, row 16 the prior
+ * logit(P4); row f of cell c at feat[f * stride + c].
  *
  * All pointers named *_dev are device memory owned by the caller; `stream` is a cudaStream_t (NULL: the legacy
  * default stream).  Functions return 0 (SDFIBM_OK) or a negative sdfibm_status; they synchronise the stream
@@ -29,9 +36,10 @@
 extern "C" {
 #endif
 
-#define SDFIBM_MLP_NIN 11
+#define SDFIBM_MLP_NIN 16
+#define SDFIBM_MLP_NFEAT 17 /* rows of a feature buffer: the 16 network inputs, then the prior logit(P4) */
 #define SDFIBM_MLP_NHIDDEN 64
-#define SDFIBM_MLP_NPARAM 4993
+#define SDFIBM_MLP_NPARAM 5313
 #define SDFIBM_MLP_ERR_TIMEOUT 7 /* device error code: an MMA completion was not observed within the wait limit */
 
 /* Shape families of the generated training cells (bit mask in sdfibm_mlp_data_desc.families). */
@@ -51,14 +59,16 @@ typedef struct sdfibm_mlp_data_desc {
     double z_axis_frac;      /* fraction of Circle / Ellipse cells whose axis is the mesh z axis (2-D meshes) */
 } sdfibm_mlp_data_desc;
 
-/* Generates n labelled cut cells (cells with 1..7 vertices inside).  feat_dev: [11][n]; label_dev: [n], the
- * fraction of the n_sub^3 lattice points inside; recipe_dev (may be NULL): [n][20] FP64 description of each cell
- * for checking: shape type, 8 shape parameters (sdfibm_shape_desc.p), quaternion (w,x,y,z), cell corner (3), h,
- * inside-vertex count, attempts.  Shapes sit at the origin; the cell size is h = 1. */
+/* Generates n labelled cut cells (cells with 1..7 vertices inside).  feat_dev: [SDFIBM_MLP_NFEAT][n] (inputs and
+ * prior, computed in FP32 as the coupling path computes them); label_dev: [n], the fraction of the n_sub^3 lattice
+ * points inside (FP64 inside tests); recipe_dev (may be NULL): [n][20] FP64 description of each cell for checking:
+ * shape type, 8 shape parameters (sdfibm_shape_desc.p), quaternion (w,x,y,z), cell corner (3), h, inside-vertex
+ * count, attempts.  Shapes sit at the origin; the cell size is h = 1. */
 int sdfibm_mlp_dataset(uint64_t seed, int64_t n, const sdfibm_mlp_data_desc* desc, float* feat_dev, float* label_dev,
                        double* recipe_dev, void* stream);
 
-/* Predicted fraction of n cells: out_dev[c] = network(feat[:, c]); params_dev is FP32 [SDFIBM_MLP_NPARAM]. */
+/* Predicted fraction of n cells: out_dev[c] = sigmoid(feat[16][c] + network(feat[0..15][c])); params_dev is FP32
+ * [SDFIBM_MLP_NPARAM]; feat_dev holds SDFIBM_MLP_NFEAT rows of `stride` entries. */
 int sdfibm_mlp_forward(const float* params_dev, const float* feat_dev, int64_t stride, int64_t n, float* out_dev,
                        void* stream);
 

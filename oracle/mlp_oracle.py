@@ -1,19 +1,20 @@
 """CPU oracle of the learned cut-cell fraction model: TEST INFRASTRUCTURE ONLY.
 
 Only tests, the smoke check and the bench's CPU legs import this module, to check the GPU kernels in
-sdfibm_gb300/csrc/mlp.cu.  It has no counterpart in the reference, which computes As only with the apex/pyramid
-geometry (geometrictools.cpp:47-116).  It restates the model so that the GPU forward pass, backward pass and
-trainer can be compared term by term:
+sdfibm_gb300/csrc/mlp.cu and classify.cu.  It has no counterpart in the reference, which computes As only with the
+apex/pyramid geometry (geometrictools.cpp:47-116).  It restates the model so that the GPU inputs, forward pass,
+backward pass and trainer can be compared term by term:
 
-* features of a cut cell (11): the signed distance at its 8 vertices divided by the cell size, in the vertex
-  order of OpenFOAM's cellPoints for a hex, (i,j,k) (i+1,j,k) (i,j+1,k) (i+1,j+1,k), then the same at k+1; then
-  the trilinear gradient of those 8 values at the cell centre, normalised to unit length;
-* network 11 -> 64 -> 64 -> 1 with SiLU hidden activations; the predicted fraction is
-  sigmoid(logit(clamp(P, 1e-4, 1 - 1e-4)) + g * o) with o the network output, P the exact solid fraction of the cell
-  under the plane fitted to its vertex distances (Scardovelli & Zaleski, J. Comput. Phys. 164 (2000), cube-plane
-  volume) and g = tw / (1 + tw), tw the sum of the six face twists of the vertex distances;
+* stencil: the signed distance at the 5 x 5 x 5 lattice of the cell (spacing h/4, vertices included), divided by h;
+* P4, P2: the cell cut into 4^3 (2^3) sub-cells, each sub-cell's fraction the exact cube-plane volume under the plane
+  fitted to its 8 corner distances (Scardovelli & Zaleski, J. Comput. Phys. 164 (2000)), averaged;
+* inputs (16): the stencil values at the 8 vertices (OpenFOAM cellPoints order of a hex, (i,j,k) (i+1,j,k)
+  (i,j+1,k) (i+1,j+1,k), then the same at k+1), at the 6 face centres (-x +x -y +y -z +z) and at the centre, then
+  logit(clamp(P2)); the prior is logit(clamp(P4)), clamp to [1e-4, 1 - 1e-4];
+* network 16 -> 64 -> 64 -> 1 with SiLU hidden activations; the predicted fraction is sigmoid(prior + o) with o the
+  network output;
 * numerics of the GPU kernels: the two hidden layers are BF16 x BF16 tensor-core products with FP32
-  accumulation, W1 and W2 are rounded to BF16, and the features and the first hidden activations are carried
+  accumulation, W1 and W2 are rounded to BF16, and the inputs and the first hidden activations are carried
   as a hi + lo pair of BF16 values (so they keep ~16 significant bits); biases, the 64 -> 1 output layer and
   the sigmoid are FP32;
 * the loss is the mean squared error of the predicted fraction; the backward pass rounds the operands of its
@@ -23,12 +24,13 @@ The pure-Python parts are vectorised numpy; sizes used by the tests are a few th
 """
 import numpy as np
 
-N_IN = 11
+N_IN = 16
+N_FEAT = 17     # rows of a feature record: the 16 inputs, then the prior logit
 N_H = 64
-N_PARAM = N_H * N_IN + N_H + N_H * N_H + N_H + N_H + 1  # 4993
+N_PARAM = N_H * N_IN + N_H + N_H * N_H + N_H + N_H + 1  # 5313
 
 # flat parameter layout, shared with include/sdfibm_mlp.h
-OFF_W1 = 0                        # W1[64][11], row = hidden unit
+OFF_W1 = 0                        # W1[64][16], row = hidden unit
 OFF_B1 = OFF_W1 + N_H * N_IN      # b1[64]
 OFF_W2 = OFF_B1 + N_H             # W2[64][64], row = output unit
 OFF_B2 = OFF_W2 + N_H * N_H       # b2[64]
@@ -88,38 +90,6 @@ def dsilu(z):
     return s * (1.0 + z * (1.0 - s))
 
 
-def features(phi, inv_h):
-    """phi: [n, 8] float32 vertex signed distances; inv_h: float32 1/h.  Returns [n, 11] float32.
-
-    Same FP32 operation order as the device function cell_features in mlp.cu."""
-    f = (np.asarray(phi, np.float32) * np.float32(inv_h)).astype(np.float32)
-    q = np.float32(0.25)
-    gx = q * (((f[:, 1] - f[:, 0]) + (f[:, 3] - f[:, 2])) + ((f[:, 5] - f[:, 4]) + (f[:, 7] - f[:, 6])))
-    gy = q * (((f[:, 2] - f[:, 0]) + (f[:, 3] - f[:, 1])) + ((f[:, 6] - f[:, 4]) + (f[:, 7] - f[:, 5])))
-    gz = q * (((f[:, 4] - f[:, 0]) + (f[:, 5] - f[:, 1])) + ((f[:, 6] - f[:, 2]) + (f[:, 7] - f[:, 3])))
-    gn = np.sqrt(gx * gx + gy * gy + gz * gz).astype(np.float32)
-    ok = gn > np.float32(1e-12)
-    den = np.where(ok, gn, np.float32(1.0)).astype(np.float32)
-    g = np.stack([np.where(ok, gx / den, 0), np.where(ok, gy / den, 0), np.where(ok, gz / den, 0)], 1)
-    return np.concatenate([f, g.astype(np.float32)], 1).astype(np.float32)
-
-
-def band_scores(feat):
-    """Confidence-band scores of a cell from its features: (twist, |grad| - 1).
-
-    twist = sum over the 6 faces of |f_a - f_b - f_c + f_d| (zero for a linear field); the gradient magnitude of
-    the trilinear interpolant is 1 for a true distance field away from edges and the medial axis."""
-    f = np.asarray(feat, np.float32)[:, :8]
-    tw = (np.abs(f[:, 0] - f[:, 1] - f[:, 2] + f[:, 3]) + np.abs(f[:, 4] - f[:, 5] - f[:, 6] + f[:, 7]) +
-          np.abs(f[:, 0] - f[:, 1] - f[:, 4] + f[:, 5]) + np.abs(f[:, 2] - f[:, 3] - f[:, 6] + f[:, 7]) +
-          np.abs(f[:, 0] - f[:, 2] - f[:, 4] + f[:, 6]) + np.abs(f[:, 1] - f[:, 3] - f[:, 5] + f[:, 7]))
-    q = 0.25
-    gx = q * (((f[:, 1] - f[:, 0]) + (f[:, 3] - f[:, 2])) + ((f[:, 5] - f[:, 4]) + (f[:, 7] - f[:, 6])))
-    gy = q * (((f[:, 2] - f[:, 0]) + (f[:, 3] - f[:, 1])) + ((f[:, 6] - f[:, 4]) + (f[:, 7] - f[:, 5])))
-    gz = q * (((f[:, 4] - f[:, 0]) + (f[:, 5] - f[:, 1])) + ((f[:, 6] - f[:, 2]) + (f[:, 7] - f[:, 3])))
-    return tw, np.abs(np.sqrt(gx * gx + gy * gy + gz * gz) - 1.0)
-
-
 PRIOR_CLAMP = 1e-4
 
 
@@ -157,39 +127,68 @@ def plane_fraction(X):
     return np.where(ok, v, out)
 
 
-def face_twist(X):
-    f = np.asarray(X, np.float64)[:, :8]
-    return (np.abs(f[:, 0] - f[:, 1] - f[:, 2] + f[:, 3]) + np.abs(f[:, 4] - f[:, 5] - f[:, 6] + f[:, 7]) +
-            np.abs(f[:, 0] - f[:, 1] - f[:, 4] + f[:, 5]) + np.abs(f[:, 2] - f[:, 3] - f[:, 6] + f[:, 7]) +
-            np.abs(f[:, 0] - f[:, 2] - f[:, 4] + f[:, 6]) + np.abs(f[:, 1] - f[:, 3] - f[:, 5] + f[:, 7]))
+def _idx(i, j, k):
+    return i + 5 * (j + 5 * k)
 
 
-def prior(X):
-    """(logit of the clamped planar fraction, gate) of every cell."""
-    v = np.clip(plane_fraction(X), PRIOR_CLAMP, 1 - PRIOR_CLAMP)
-    tw = face_twist(X)
-    return np.log(v / (1 - v)), tw / (1 + tw)
+# stencil points of the 15 distance inputs: vertices (cellPoints order), face centres -x +x -y +y -z +z, centre
+INPUT_POINTS = ([_idx(4 * (v & 1), 4 * ((v >> 1) & 1), 4 * (v >> 2)) for v in range(8)] +
+                [_idx(0, 2, 2), _idx(4, 2, 2), _idx(2, 0, 2), _idx(2, 4, 2), _idx(2, 2, 0), _idx(2, 2, 4)] +
+                [_idx(2, 2, 2)])
+
+
+def subcell_prior(phi125, n):
+    """Mean planar fraction of the n^3 sub-cells (n = 1, 2 or 4) of cells given by their 5^3 stencils [m, 125]."""
+    G = np.asarray(phi125, np.float64).reshape(-1, 5, 5, 5)   # [cell][k][j][i]
+    d = 4 // n
+    tot = np.zeros(G.shape[0])
+    for c in range(n):
+        for b in range(n):
+            for a in range(n):
+                f = np.stack([G[:, (c + dk) * d, (b + dj) * d, (a + di) * d]
+                              for dk in (0, 1) for dj in (0, 1) for di in (0, 1)], 1)
+                tot += plane_fraction(f)
+    return tot / n ** 3
+
+
+def _logit_clamped(v):
+    v = np.clip(v, PRIOR_CLAMP, 1 - PRIOR_CLAMP)
+    return np.log(v / (1 - v))
+
+
+def features(phi125):
+    """Feature records [m, 17] (16 inputs, then the prior) of cells given by their stencils [m, 125] (phi / h)."""
+    phi = np.asarray(phi125, np.float64)
+    p4, p2 = subcell_prior(phi, 4), subcell_prior(phi, 2)
+    return np.concatenate([phi[:, INPUT_POINTS], _logit_clamped(p2)[:, None], _logit_clamped(p4)[:, None]],
+                          1).astype(np.float32)
+
+
+def band_score(X):
+    """|P4 - P2| of the clamped reconstructions, from feature records [m, 17]."""
+    X = np.asarray(X, np.float64)
+    return np.abs(sigmoid(X[:, 16]) - sigmoid(X[:, 15]))
 
 
 def forward(p, X, return_all=False, exact=False):
-    """Predicted fraction of each cell.  X: [n, 11] float32.  FP64 accumulation of the FP32-exact products.
+    """Predicted fraction of each cell.  X: [n, 17] float32 feature records (inputs, prior).  FP64 accumulation of
+    the FP32-exact products.
 
     exact=True drops every rounding (FP64 throughout): the plain function, used to check the backward algebra."""
     W1, b1, W2, b2, w3, b3 = unpack(p) if not exact else [np.asarray(t, np.float64) for t in unpack_f64(p)]
     if exact:
-        z1 = np.asarray(X, np.float64) @ W1.T + b1
+        z1 = np.asarray(X, np.float64)[:, :N_IN] @ W1.T + b1
         h1 = silu(z1)
         z2 = h1 @ W2.T + b2
         h2 = silu(z2)
         o = h2 @ w3 + b3
-        pl, g = prior(X)
-        a = sigmoid(pl + g * o)
+        a = sigmoid(np.asarray(X, np.float64)[:, N_IN] + o)
         if return_all:
-            return dict(z1=z1, h1=h1, z2=z2, h2=h2, o=o, a=a, gate=g)
+            return dict(z1=z1, h1=h1, z2=z2, h2=h2, o=o, a=a)
         return a
     W1b = bf16(W1).astype(np.float64)
     W2b = bf16(W2).astype(np.float64)
-    xh, xl = split(X)
+    xh, xl = split(np.asarray(X, np.float32)[:, :N_IN])
     z1 = (xh.astype(np.float64) + xl.astype(np.float64)) @ W1b.T + b1
     h1 = silu(z1.astype(np.float32)).astype(np.float32)
     hh, hl = split(h1)
@@ -197,10 +196,9 @@ def forward(p, X, return_all=False, exact=False):
     z2 = z2.astype(np.float32)
     h2 = silu(z2).astype(np.float32)
     o = h2.astype(np.float64) @ w3.astype(np.float64) + b3
-    pl, g = prior(X)
-    a = sigmoid(pl + g * o)
+    a = sigmoid(np.asarray(X, np.float32)[:, N_IN].astype(np.float64) + o)
     if return_all:
-        return dict(z1=z1.astype(np.float32), h1=h1, z2=z2, h2=h2, o=o, a=a, gate=g)
+        return dict(z1=z1.astype(np.float32), h1=h1, z2=z2, h2=h2, o=o, a=a)
     return a
 
 
@@ -220,10 +218,10 @@ def loss_grad(p, X, y, exact=False):
         r = forward(p, X, return_all=True, exact=True)
         a = r["a"]
         d = a - y
-        dz3 = (2.0 / n) * d * a * (1.0 - a) * r["gate"]
+        dz3 = (2.0 / n) * d * a * (1.0 - a)
         dZ2 = dz3[:, None] * w3[None, :] * dsilu(r["z2"])
         dZ1 = (dZ2 @ W2) * dsilu(r["z1"])
-        g = np.concatenate([(dZ1.T @ np.asarray(X, np.float64)).ravel(), dZ1.sum(0), (dZ2.T @ r["h1"]).ravel(),
+        g = np.concatenate([(dZ1.T @ np.asarray(X, np.float64)[:, :N_IN]).ravel(), dZ1.sum(0), (dZ2.T @ r["h1"]).ravel(),
                             dZ2.sum(0), r["h2"].T @ dz3, [dz3.sum()]])
         return float(np.mean(d * d)), g
     W1, b1, W2, b2, w3, b3 = unpack(p)
@@ -232,7 +230,7 @@ def loss_grad(p, X, y, exact=False):
     a = r["a"]
     d = a - y
     loss = float(np.mean(d * d))
-    dz3 = (2.0 / n) * d * a * (1.0 - a) * r["gate"]                       # [n]
+    dz3 = (2.0 / n) * d * a * (1.0 - a)                                   # [n]
     dw3 = r["h2"].astype(np.float64).T @ dz3
     db3 = dz3.sum()
     dZ2 = (dz3[:, None] * w3[None, :].astype(np.float64) * dsilu(r["z2"].astype(np.float64))).astype(np.float32)
@@ -242,7 +240,7 @@ def loss_grad(p, X, y, exact=False):
     dH1 = dZ2b @ bf16(W2).astype(np.float64)
     dZ1 = (dH1 * dsilu(r["z1"].astype(np.float64))).astype(np.float32)
     db1 = dZ1.astype(np.float64).sum(0)
-    dW1 = bf16(dZ1).astype(np.float64).T @ bf16(X).astype(np.float64)
+    dW1 = bf16(dZ1).astype(np.float64).T @ bf16(np.asarray(X, np.float32)[:, :N_IN]).astype(np.float64)
     g = np.concatenate([dW1.ravel(), db1, dW2.ravel(), db2, dw3, [db3]])
     return loss, g
 

@@ -993,16 +993,18 @@ double oracle_phi(const sdfibm_solid_desc* s, const double* p) {
 }
 
 // One labelled training cell of the learned fraction (sdfibm_mlp_dataset): the shape at the origin with rotation q4,
-// the cell [o, o + h]^3; writes the filtered signed distance at the 8 vertices (cellPoints order) and returns the
-// number of n^3 midpoint-lattice samples inside.
+// the cell [o, o + h]^3; writes the signed distance divided by h at the 5 x 5 x 5 lattice of the cell (spacing h/4,
+// index i + 5 (j + 5 k)) and returns the number of n^3 midpoint-lattice samples inside.
 int64_t oracle_sample_cell(const sdfibm_shape_desc* s, const double* q4, const double* o, double h, int n,
-                           double* phi8) {
+                           double* phi125) {
     const Quat q{q4[0], V3{q4[1], q4[2], q4[3]}};
     const V3 zero{0.0, 0.0, 0.0};
-    for (int v = 0; v < 8; ++v) {
-        const V3 p{o[0] + (double)(v & 1) * h, o[1] + (double)((v >> 1) & 1) * h, o[2] + (double)((v >> 2) & 1) * h};
-        phi8[v] = shapeSDF(*s, world2local(p, zero, q));
-    }
+    for (int k = 0; k < 5; ++k)
+        for (int j = 0; j < 5; ++j)
+            for (int i = 0; i < 5; ++i) {
+                const V3 p{o[0] + 0.25 * i * h, o[1] + 0.25 * j * h, o[2] + 0.25 * k * h};
+                phi125[i + 5 * (j + 5 * k)] = shapeSDF(*s, world2local(p, zero, q)) / h;
+            }
     int64_t cnt = 0;
     for (int c = 0; c < n; ++c)
         for (int b = 0; b < n; ++b)

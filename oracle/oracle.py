@@ -84,7 +84,7 @@ def make_shape(type_id, raw, com=(0.0, 0.0, 0.0)):
 
 def sample_cell(recipe, n_sub):
     """Recomputes one generated training cell from its FP64 recipe (the 20-value record of sdfibm_mlp_dataset):
-    returns (phi at the 8 vertices, inside count of the n_sub^3 lattice)."""
+    returns (phi / h at the cell's 5 x 5 x 5 lattice [125], inside count of the n_sub^3 lattice)."""
     r = np.asarray(recipe, dtype=np.float64)
     s = abi.ShapeDesc()
     s.type = int(r[0])
@@ -92,7 +92,7 @@ def sample_cell(recipe, n_sub):
         s.p[k] = r[1 + k]
     q = np.ascontiguousarray(r[9:13])
     o = np.ascontiguousarray(r[13:16])
-    phi = np.zeros(8)
+    phi = np.zeros(125)
     cnt = lib().oracle_sample_cell(C.byref(s), _p(q), _p(o), float(r[16]), int(n_sub), _p(phi))
     return phi, int(cnt)
 

@@ -14,7 +14,7 @@ _lib = None
 
 CUDA_SYMBOLS = [
     "sdfibm_options_default", "sdfibm_cuda_create", "sdfibm_cuda_interact", "sdfibm_cuda_interact_host",
-    "sdfibm_cuda_interact_host64",
+    "sdfibm_cuda_interact_host64", "sdfibm_cuda_create_polymesh",
     "sdfibm_cuda_evolve", "sdfibm_cuda_fix_internal", "sdfibm_cuda_get_solids", "sdfibm_cuda_set_solids",
     "sdfibm_cuda_touched", "sdfibm_cuda_stats", "sdfibm_cuda_kernel_times", "sdfibm_cuda_last_error",
     "sdfibm_cuda_version",
@@ -50,6 +50,8 @@ def load():
     L.sdfibm_options_default.argtypes = [P(abi.Options)]
     L.sdfibm_options_default.restype = None
     L.sdfibm_cuda_create.argtypes = [P(abi.MeshDesc), P(abi.SolidDesc), i32, P(abi.Options), vp, P(vp)]
+    L.sdfibm_cuda_create_polymesh.argtypes = [vp, i64, vp, vp, i64, vp, vp, i64, i32, P(abi.SolidDesc), i32,
+                                              P(abi.Options), vp, P(vp)]
     L.sdfibm_cuda_interact.argtypes = [vp, dbl, dbl, vp, vp, vp, vp, vp, vp]
     L.sdfibm_cuda_interact_host.argtypes = [vp, dbl, dbl, vp, vp, vp, vp, vp, vp]
     L.sdfibm_cuda_interact_host64.argtypes = [vp, dbl, dbl, vp, vp, vp, vp, vp, vp]

@@ -74,7 +74,9 @@ class MlpTrainDesc(C.Structure):
                 ("warmup_steps", C.c_int32), ("reserved", C.c_int32)]
 
 
-MLP_NPARAM = 4993
+MLP_NIN = 16
+MLP_NFEAT = 17  # rows of a feature buffer: the 16 network inputs, then the prior logit
+MLP_NPARAM = 5313
 MLP_SPHERE, MLP_ELLIPSOID, MLP_BOX, MLP_PLANE, MLP_CYLINDER, MLP_ELLIPTIC_CYL = 1, 2, 4, 8, 16, 32
 
 

@@ -14,8 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libsdfibm_cuda.so")
 BUILD_DIR = os.path.join(HERE, "_build")
-CU_SOURCES = ["classify.cu", "coupling.cu", "evolve.cu", "capi.cu", "noalloc.cu", "mlp.cu"]
-CXX_SOURCES = ["host.cpp", "host_dict.cpp", "host_io.cpp"]
+CU_SOURCES = ["classify.cu", "coupling.cu", "evolve.cu", "capi.cu", "noalloc.cu", "mlp.cu", "poly.cu"]
+CXX_SOURCES = ["host.cpp", "host_dict.cpp", "host_io.cpp", "host_poly.cpp"]
 # the host half alone (no CUDA): what CPU-only builds of the host code (sanitizer runs, test doubles) compile
 HOST_SOURCES = [os.path.join("sdfibm_gb300", "csrc", f) for f in CXX_SOURCES]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -30,7 +30,8 @@ def nvcc():
 
 def _sources():
     return [os.path.join(CSRC, f) for f in CU_SOURCES + CXX_SOURCES + ["device_math.cuh", "kernels.cuh", "common.cuh",
-                                                                   "host_text.hpp"]] + [
+                                                                   "host_text.hpp", "mlp.cuh", "poly.hpp",
+                                                                   "poly_dev.cuh"]] + [
         os.path.join(HERE, "..", "include", h) for h in ("sdfibm_cuda.h", "sdfibm_host.h")]
 
 

@@ -53,6 +53,37 @@ class SolidCloud:
         if rc != abi.OK:
             raise CouplingError(rc, "create failed")
 
+    @classmethod
+    def from_polymesh(cls, points, face_off, face_lab, owner, neighbour, solids, opt=None, twod=False, stream=None):
+        """SolidCloud on an explicit OpenFOAM polyMesh (graded, multi-block or polyhedral): the polyMesh lists as
+        read from constant/polyMesh (points [P, 3], faces as offsets [F + 1] and labels, owner [F], neighbour [F_int]).
+        The reference's REF-GEO fraction; fields are cell-major as for the uniform mesh, ncells = max label + 1."""
+        self = cls.__new__(cls)
+        self._L = load()
+        self.mesh = None
+        self.time = 0.0
+        self._stream = stream
+        self._sampler = None
+        self._sampler_fields = None
+        self._sampler_ct = None
+        self.nsolids = len(solids)
+        self._solids = (abi.SolidDesc * max(1, len(solids)))(*solids)
+        self.opt = opt if opt is not None else abi.options()
+        self._poly = tuple(np.ascontiguousarray(a, dt) for a, dt in ((points, np.float64), (face_off, np.int32),
+                                                                     (face_lab, np.int32), (owner, np.int32),
+                                                                     (neighbour, np.int32)))
+        pts, fo, fl, ow, nb = self._poly
+        self.ncells = int(max(ow.max(initial=-1), nb.max(initial=-1))) + 1
+        self._h = C.c_void_p()
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        p = lambda a: a.ctypes.data_as(C.c_void_p)
+        rc = self._L.sdfibm_cuda_create_polymesh(p(pts), len(pts), p(fo), p(fl), len(fo) - 1, p(ow), p(nb), len(nb),
+                                                 int(bool(twod)), self._solids, len(solids), C.byref(self.opt), s,
+                                                 C.byref(self._h))
+        if rc != abi.OK:
+            raise CouplingError(rc, "polyMesh create failed")
+        return self
+
     def _check(self, rc):
         if rc != abi.OK:
             raise CouplingError(rc, self._L.sdfibm_cuda_last_error(self._h).decode())
@@ -278,10 +309,12 @@ class SolidCloud:
                 "refgeo_ctas", "from_cache")
         return dict(zip(keys, list(out)))
 
-    def set_fraction_model(self, params, tau_twist, tau_grad):
-        """Installs the learned cut-cell fraction model (options.fraction_method = FRACTION_LEARNED)."""
+    def set_fraction_model(self, params, tau_refine, rho_min):
+        """Installs the learned cut-cell fraction model (options.fraction_method = FRACTION_LEARNED) and its band:
+        cells whose planar reconstructions disagree by more than tau_refine, or whose solid's bounding radius spans
+        fewer than rho_min cells, take the SUBSAMPLE fallback."""
         p = np.ascontiguousarray(params, dtype=np.float32)
         if p.shape != (abi.MLP_NPARAM,):
             raise ValueError("fraction model needs %d parameters" % abi.MLP_NPARAM)
         self._check(self._L.sdfibm_cuda_set_fraction_model(self._h, p.ctypes.data_as(C.c_void_p),
-                                                           C.c_float(tau_twist), C.c_float(tau_grad)))
+                                                           C.c_float(tau_refine), C.c_float(rho_min)))

@@ -5,6 +5,7 @@
 #include <cstring>
 #include <functional>
 #include <string>
+#include <type_traits>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -14,6 +15,8 @@
 #include "../../include/sdfibm_cuda.h"
 #include "kernels.cuh"
 #include "mlp.cuh"
+#include "poly.hpp"
+#include "poly_dev.cuh"
 #include "../../include/sdfibm_mlp.h"
 
 namespace sdfibm_dev {
@@ -24,6 +27,7 @@ void launch_classify(const ClassifyArgs& A, bool flat, int grid, cudaStream_t st
 int classify_occupancy(int method, bool flat);
 __global__ void subsample_cells_kernel(FallbackArgs A);
 __global__ void recount_kernel(FallbackArgs A);
+__global__ void learned_stencil_kernel(StencilArgs A);
 __global__ void refgeo_cells_kernel(MeshK m, const SolidK* sk, const SolidPlan* plan, const int32_t* fref_solid,
                                     const int64_t* fref_index, const float* rg_phi, int64_t cap, const Counters* cnt,
                                     float* alpha);
@@ -194,7 +198,7 @@ struct sdfibm_ctx {
     bool host64_synced = false;
     double* d_f64 = nullptr;  // [3N] U, then [6N] As, Fs, Ts, Ct
     // CTA counts of the launches the autotuner sets (defaults from the occupancy at create)
-    int classify_grid = 0, couple_grid = 0, subsample_grid = 0, mlp_grid = 0, refgeo_grid = 0;
+    int classify_grid = 0, couple_grid = 0, subsample_grid = 0, mlp_grid = 0, refgeo_grid = 0, stencil_grid = 0;
     int classify_occ = 1, couple_occ = 1;  // resident CTAs per SM
     bool tuned_from_cache = false;
     // per-kernel events (options.timing)
@@ -203,9 +207,9 @@ struct sdfibm_ctx {
     const char* ev_name[MAXEV] = {};
     // learned fraction (SDFIBM_FRACTION_LEARNED): model and per-cut-cell feature buffers
     float* d_mlp = nullptr;
-    float tau_twist = 0.f, tau_grad = 0.f;
+    float tau_refine = 0.f, rho_min = 0.f;  // confidence band of the learned fraction
     bool model_set = false;
-    float* d_feat = nullptr;  // [11][feat_cap]
+    float* d_feat = nullptr;  // [SDFIBM_MLP_NFEAT][feat_cap]: model inputs and prior of the listed cut cells
     float* d_rg_phi = nullptr;  // REF-GEO: [8][feat_cap] vertex distances of the listed cut cells
     int64_t feat_cap = 0;
     int32_t* d_fref_solid = nullptr;
@@ -231,6 +235,20 @@ struct sdfibm_ctx {
     Graph egraph;
     bool graphs_failed = false;
     std::vector<cudaGraph_t> graphs_keep;
+    // explicit (unstructured) polyMesh: set by sdfibm_cuda_create_polymesh, which builds the rest of the context
+    // over a one-cell box of the mesh's extent (solid records, states, collision grid); only the poly kernels then
+    // touch the fields
+    struct Poly {
+        int64_t N = 0;
+        PolyK k{};
+        PolyWork w{};
+        std::vector<void*> allocs;
+        float *dU = nullptr, *dAs = nullptr, *dFs = nullptr, *dTs = nullptr;  // host-entry staging
+        int32_t* dCt = nullptr;
+        double* d64 = nullptr;
+        std::vector<int32_t> counts;
+    };
+    Poly* poly = nullptr;
 };
 
 // event bracketing of each launch when timing is on: mark(ctx, name) after a launch records its end
@@ -275,6 +293,29 @@ static std::vector<int2> make_chunks(const std::vector<SolidK>& hk, int chunk_ti
 template <class T>
 static cudaError_t dalloc(T** p, size_t n) {
     return cudaMalloc((void**)p, std::max<size_t>(1, n) * sizeof(T));
+}
+
+// ---- explicit polyMesh (unstructured) contexts: helpers ----------------------------------------------------------
+__global__ void poly_ft_kernel(const double* ftacc, double* ft, int S, double rho_f) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    for (int r = 0; r < 6; ++r) ft[6 * s + r] = ftacc[6 * s + r] * rho_f;  // force *= m_rhof (solidcloud.cpp:423)
+}
+
+template <typename T>
+static cudaError_t poly_alloc(sdfibm_ctx::Poly& P, T** p, size_t n) {
+    const cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(1, n) * sizeof(T));
+    if (e == cudaSuccess) P.allocs.push_back((void*)*p);
+    else *p = nullptr;
+    return e;
+}
+
+template <typename T>
+static bool poly_upload(sdfibm_ctx::Poly& P, const T** dst, const std::vector<T>& v) {
+    T* d = nullptr;
+    if (poly_alloc(P, &d, v.size()) != cudaSuccess) return false;
+    *dst = d;
+    return v.empty() || cudaMemcpy(d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice) == cudaSuccess;
 }
 
 extern "C" {
@@ -591,6 +632,7 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
     ctx->subsample_grid = 8 * ctx->num_sms;
     ctx->mlp_grid = 4 * ctx->num_sms;
     ctx->refgeo_grid = 8 * ctx->num_sms;
+    ctx->stencil_grid = 8 * ctx->num_sms;
     *out = ctx;
     return SDFIBM_OK;
 }
@@ -656,8 +698,8 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             CA.feat_cap = ctx->feat_cap; CA.fref_solid = ctx->d_fref_solid; CA.fref_index = ctx->d_fref_index;
         }
         if (learned) {
-            CA.feat = ctx->d_feat; CA.feat_cap = ctx->feat_cap; CA.fref_solid = ctx->d_fref_solid;
-            CA.fref_index = ctx->d_fref_index; CA.inv_h = (float)(1.0 / ctx->mdesc.h[0]);
+            // cut cells listed by the classify pass; learned_stencil_kernel computes the model's inputs
+            CA.feat_cap = ctx->feat_cap; CA.fref_solid = ctx->d_fref_solid; CA.fref_index = ctx->d_fref_index;
         }
         launch_classify(CA, ctx->mesh.nz <= 2, ctx->classify_grid, st);
         mark(ctx, "classify_kernel");
@@ -706,12 +748,18 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
         }
         FallbackArgs fa{};
         if (learned) {
-            // network on every cut cell, SUBSAMPLE on the cells outside its band
+            // model inputs and band of every cut cell, the network on the cells inside the band, SUBSAMPLE on the
+            // others
+            StencilArgs sa{};
+            sa.m = ctx->mesh; sa.sk = ctx->d_sk; sa.plan = ctx->d_plan; sa.fref_solid = ctx->d_fref_solid;
+            sa.fref_index = ctx->d_fref_index; sa.cap = ctx->feat_cap; sa.feat = ctx->d_feat; sa.fb_list = ctx->d_fb;
+            sa.cnt = ctx->d_cnt; sa.tau_refine = ctx->tau_refine; sa.rho_min = ctx->rho_min;
+            learned_stencil_kernel<<<ctx->stencil_grid, 256, 0, st>>>(sa);
+            mark(ctx, "learned_stencil_kernel");
+            ++launches;
             MlpInferArgs ia{};
             ia.params = ctx->d_mlp; ia.feat = ctx->d_feat; ia.stride = ctx->feat_cap; ia.n_dev = &ctx->d_cnt->n_feat;
-            ia.ref_solid = ctx->d_fref_solid; ia.ref_index = ctx->d_fref_index; ia.alpha = ctx->d_alpha;
-            ia.fb_list = ctx->d_fb; ia.fb_count = &ctx->d_cnt->n_fb; ia.tau_twist = ctx->tau_twist;
-            ia.tau_grad = ctx->tau_grad; ia.error = &ctx->d_cnt->error;
+            ia.ref_index = ctx->d_fref_index; ia.alpha = ctx->d_alpha; ia.error = &ctx->d_cnt->error;
             launch_mlp_infer(ia, ctx->mlp_grid, st);
             mark(ctx, "mlp_infer_kernel");
             fa.m = ctx->mesh; fa.sk = ctx->d_sk; fa.st = ctx->d_st; fa.plan = ctx->d_plan; fa.fb_list = ctx->d_fb;
@@ -848,11 +896,15 @@ static bool graphs_on(const sdfibm_ctx* ctx) {
     return ctx->opt.graphs && ctx->stream != nullptr && !ctx->opt.timing && !ctx->graphs_failed && !ctx->u_wait;
 }
 
+static int poly_interact(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs, float* Ts,
+                         int32_t* Ct, double* FT);
+
 int sdfibm_cuda_interact(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs, float* Ts,
                          int32_t* Ct, double* FT) {
     if (!ctx) return SDFIBM_ERR_ARG;
     if (!U || !As || !Fs || !Ts || !Ct) return fail(ctx, SDFIBM_ERR_ARG, "null field pointer");
     if (!(dt != 0.0)) return fail(ctx, SDFIBM_ERR_ARG, "dt must be nonzero");
+    if (ctx->poly) return poly_interact(ctx, time, dt, U, As, Fs, Ts, Ct, FT);
     const int S = ctx->S;
     cudaStream_t st = ctx->stream;
     int launches = 0;
@@ -931,10 +983,14 @@ static int ensure_staging(sdfibm_ctx* ctx) {
     return SDFIBM_OK;
 }
 
+static int poly_interact_host(sdfibm_ctx* ctx, double time, double dt, const void* U, void* As, void* Fs, void* Ts,
+                              void* Ct, double* FT, bool f64);
+
 int sdfibm_cuda_interact_host64(sdfibm_ctx* ctx, double time, double dt, const double* U, double* As, double* Fs,
                                 double* Ts, double* Ct, double* FT) {
     if (!ctx) return SDFIBM_ERR_ARG;
     if (!U || !As || !Fs || !Ts || !Ct) return fail(ctx, SDFIBM_ERR_ARG, "null field pointer");
+    if (ctx->poly) return poly_interact_host(ctx, time, dt, U, As, Fs, Ts, Ct, FT, true);
     const int64_t N = ctx->mesh.ncells;
     cudaStream_t st = ctx->stream;
     if (int rc = ensure_staging(ctx)) return rc;
@@ -1006,6 +1062,7 @@ int sdfibm_cuda_interact_host(sdfibm_ctx* ctx, double time, double dt, const flo
                               float* Ts, int32_t* Ct, double* FT) {
     if (!ctx) return SDFIBM_ERR_ARG;
     if (!U || !As || !Fs || !Ts || !Ct) return fail(ctx, SDFIBM_ERR_ARG, "null field pointer");
+    if (ctx->poly) return poly_interact_host(ctx, time, dt, U, As, Fs, Ts, Ct, FT, false);
     const int64_t N = ctx->mesh.ncells;
     cudaStream_t st = ctx->stream;
     if (int rc = ensure_staging(ctx)) return rc;
@@ -1190,6 +1247,11 @@ int sdfibm_cuda_fix_internal(sdfibm_ctx* ctx, const int32_t* Ct, float* U) {
     if (!ctx) return SDFIBM_ERR_ARG;
     if (!Ct || !U) return fail(ctx, SDFIBM_ERR_ARG, "null field pointer");
     if (!ctx->interacted) return fail(ctx, SDFIBM_ERR_STATE, "fix_internal needs a previous interact");
+    if (ctx->poly) {
+        poly_fix_kernel<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(ctx->poly->k, ctx->d_st, ctx->S, Ct, U);
+        CK(cudaGetLastError());
+        return SDFIBM_OK;
+    }
     fix_internal_kernel<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(ctx->mesh, ctx->d_st, ctx->in_cell(),
                                                                     ctx->in_solid(), Ct, U, ctx->d_cnt);
     CK(cudaGetLastError());
@@ -1219,6 +1281,25 @@ int sdfibm_cuda_touched(sdfibm_ctx* ctx, int32_t solid, int64_t* cells, int8_t* 
     if (!ctx->interacted) return fail(ctx, SDFIBM_ERR_STATE, "no interact yet");
     int rc = sync_counters(ctx);
     if (rc) return rc;
+    if (ctx->poly) {
+        sdfibm_ctx::Poly& P = *ctx->poly;
+        int32_t cnt = 0;
+        CK(cudaMemcpy(&cnt, P.w.count + solid, sizeof(int32_t), cudaMemcpyDeviceToHost));
+        std::vector<int32_t> qc(cnt);
+        std::vector<int8_t> qt(cnt);
+        if (cnt) {
+            CK(cudaMemcpy(qc.data(), P.w.queue + (int64_t)solid * P.w.qcap, sizeof(int32_t) * cnt,
+                          cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(qt.data(), P.w.qtype + (int64_t)solid * P.w.qcap, cnt, cudaMemcpyDeviceToHost));
+        }
+        std::vector<std::pair<int, int32_t>> tc(cnt);
+        for (int32_t i = 0; i < cnt; ++i) tc[i] = {qt[i], qc[i]};
+        std::sort(tc.begin(), tc.end());
+        for (int64_t i = 0; i < cnt; ++i)
+            if (i < capacity && cells) { cells[i] = tc[i].second; if (types) types[i] = (int8_t)tc[i].first; }
+        *n = cnt;
+        return SDFIBM_OK;
+    }
     const int nin = clamp_len(ctx->h_cnt->n_inside, ctx->cap), ncut = clamp_len(ctx->h_cnt->n_cut, ctx->cap);
     std::vector<int32_t> ic(nin), is(nin), cc(ncut), cs(ncut);
     if (nin) {
@@ -1422,16 +1503,16 @@ int sdfibm_cuda_tuning(sdfibm_ctx* ctx, int32_t* out, int32_t n) {
     return SDFIBM_OK;
 }
 
-int sdfibm_cuda_set_fraction_model(sdfibm_ctx* ctx, const float* params, float tau_twist, float tau_grad) {
+int sdfibm_cuda_set_fraction_model(sdfibm_ctx* ctx, const float* params, float tau_refine, float rho_min) {
     if (!ctx) return SDFIBM_ERR_ARG;
     if (!params) return fail(ctx, SDFIBM_ERR_ARG, "null model parameters");
-    if (std::isnan(tau_twist) || std::isnan(tau_grad)) return fail(ctx, SDFIBM_ERR_ARG, "band limits are NaN");
+    if (std::isnan(tau_refine) || std::isnan(rho_min)) return fail(ctx, SDFIBM_ERR_ARG, "band limits are NaN");
     for (int i = 0; i < SDFIBM_MLP_NPARAM; ++i)
         if (!std::isfinite(params[i])) return fail(ctx, SDFIBM_ERR_ARG, "non-finite model parameter");
     if (!ctx->d_mlp) {
-        // one feature record per bbox cell: every cut cell of a call fits
+        // one input record per bbox cell: every cut cell of a call fits
         ctx->feat_cap = std::max<int64_t>(1, ctx->scratch_bytes);
-        if (dalloc(&ctx->d_mlp, SDFIBM_MLP_NPARAM) || dalloc(&ctx->d_feat, (size_t)SDFIBM_MLP_NIN * ctx->feat_cap) ||
+        if (dalloc(&ctx->d_mlp, SDFIBM_MLP_NPARAM) || dalloc(&ctx->d_feat, (size_t)SDFIBM_MLP_NFEAT * ctx->feat_cap) ||
             (!ctx->d_fref_solid && dalloc(&ctx->d_fref_solid, ctx->feat_cap)) ||
             (!ctx->d_fref_index && dalloc(&ctx->d_fref_index, ctx->feat_cap)) || dalloc(&ctx->d_fb, ctx->feat_cap))
             return fail(ctx, SDFIBM_ERR_CUDA, "allocation of the learned-fraction buffers failed");
@@ -1439,8 +1520,8 @@ int sdfibm_cuda_set_fraction_model(sdfibm_ctx* ctx, const float* params, float t
     mlp_prepare();
     CK(cudaMemcpyAsync(ctx->d_mlp, params, sizeof(float) * SDFIBM_MLP_NPARAM, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    ctx->tau_twist = tau_twist;
-    ctx->tau_grad = tau_grad;
+    ctx->tau_refine = tau_refine;
+    ctx->rho_min = rho_min;
     ctx->model_set = true;
     return SDFIBM_OK;
 }
@@ -1450,6 +1531,17 @@ int sdfibm_cuda_stats(sdfibm_ctx* ctx, int64_t* out, int32_t n) {
     int rc = sync_counters(ctx);
     if (rc) return rc;
     const Counters& c = *ctx->h_cnt;
+    if (ctx->poly && ctx->interacted) {
+        sdfibm_ctx::Poly& P = *ctx->poly;
+        P.counts.resize(std::max(1, ctx->S));
+        if (ctx->S) CK(cudaMemcpy(P.counts.data(), P.w.count, sizeof(int32_t) * ctx->S, cudaMemcpyDeviceToHost));
+        int64_t tot = 0;
+        for (int s = 0; s < ctx->S; ++s) tot += P.counts[s];
+        const int64_t v[11] = {tot, 0, (int64_t)P.N * ctx->S, 0, 0, (int64_t)ctx->launches_last, 0, 0, ctx->host_h2d,
+                               ctx->host_d2h, 0};
+        for (int i = 0; i < n && i < 11; ++i) out[i] = v[i];
+        return SDFIBM_OK;
+    }
     const int64_t v[11] = {(int64_t)c.n_inside + c.n_cut, (int64_t)c.n_cut, (int64_t)c.bbox_cells,
                            (int64_t)c.exact_rechecks, (int64_t)ctx->total_chunks, (int64_t)ctx->launches_last,
                            (int64_t)c.n_feat, (int64_t)c.n_fb, ctx->host_h2d, ctx->host_d2h,
@@ -1476,6 +1568,11 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
     if (ctx->d_ovf) cudaFree(ctx->d_ovf);
     if (ctx->d_dirty) cudaFree(ctx->d_dirty);
     if (ctx->d_f64) cudaFree(ctx->d_f64);
+    if (ctx->poly) {
+        for (void* p : ctx->poly->allocs)
+            if (p) cudaFree(p);
+        delete ctx->poly;
+    }
     if (ctx->d_fsums) cudaFree(ctx->d_fsums);
     if (ctx->d_recs) cudaFree(ctx->d_recs);
     if (ctx->d_fsums_excl) cudaFree(ctx->d_fsums_excl);
@@ -1500,6 +1597,161 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
     if (ctx->h_cnt) cudaFreeHost(ctx->h_cnt);
     if (ctx->h_ft) cudaFreeHost(ctx->h_ft);
     delete ctx;
+}
+
+// ---- explicit polyMesh (unstructured) contexts ------------------------------------------------------------------
+int sdfibm_cuda_create_polymesh(const double* points, int64_t npoints, const int32_t* face_off,
+                                const int32_t* face_lab, int64_t nfaces, const int32_t* owner,
+                                const int32_t* neighbour, int64_t ninternal, int32_t twod,
+                                const sdfibm_solid_desc* solids, int32_t nsolids, const sdfibm_options* opt,
+                                void* cuda_stream, sdfibm_ctx** out) {
+    if (!out) return SDFIBM_ERR_ARG;
+    *out = nullptr;
+    sdfibm_poly::PolyHostMesh hm;
+    std::string err;
+    if (!sdfibm_poly::build_polymesh(points, npoints, face_off, face_lab, nfaces, owner, neighbour, ninternal, hm, err))
+        return SDFIBM_ERR_ARG;
+    sdfibm_options o;
+    if (opt) o = *opt; else sdfibm_options_default(&o);
+    if (o.fraction_method != SDFIBM_FRACTION_REFGEO) return SDFIBM_ERR_ARG;  // the reference's own fraction only
+    o.graphs = 0;
+    sdfibm_mesh_desc box{};
+    box.nx = box.ny = box.nz = 1;
+    box.twod = twod;
+    for (int a = 0; a < 3; ++a) {
+        box.origin[a] = hm.bmin[a];
+        box.h[a] = std::max(hm.bmax[a] - hm.bmin[a], 1e-300);
+    }
+    int rc = sdfibm_cuda_create(&box, solids, nsolids, &o, cuda_stream, out);
+    if (rc) return rc;
+    sdfibm_ctx* ctx = *out;
+    auto* Pp = new sdfibm_ctx::Poly();
+    ctx->poly = Pp;
+    sdfibm_ctx::Poly& P = *Pp;
+    const int64_t N = hm.ncells;
+    P.N = N;
+    const int64_t S = std::max(1, nsolids);
+    // search lists: every cell of the mesh for every solid, at most 2^28 entries
+    if ((double)N * (double)S > (double)(1 << 28)) {
+        ctx->err = "polyMesh: cells x solids above the search-list limit (2^28)";
+        sdfibm_cuda_destroy(ctx);
+        *out = nullptr;
+        return SDFIBM_ERR_CAPACITY;
+    }
+    PolyK& k = P.k;
+    k.ncells = (int32_t)N; k.npoints = (int32_t)hm.npoints; k.nfaces = (int32_t)hm.nfaces; k.twod = twod;
+    const bool ok_up =
+        poly_upload(P, &k.points, hm.points) && poly_upload(P, &k.face_off, hm.face_off) &&
+        poly_upload(P, &k.face_lab, hm.face_lab) && poly_upload(P, &k.cf_off, hm.cell_faces_off) &&
+        poly_upload(P, &k.cf, hm.cell_faces) && poly_upload(P, &k.cp_off, hm.cell_pts_off) &&
+        poly_upload(P, &k.cp, hm.cell_pts) && poly_upload(P, &k.cc_off, hm.cell_cells_off) &&
+        poly_upload(P, &k.ccl, hm.cell_cells) && poly_upload(P, &k.Cf, hm.Cf) && poly_upload(P, &k.Sf, hm.Sf) &&
+        poly_upload(P, &k.Cc, hm.Cc) && poly_upload(P, &k.Vc, hm.Vc);
+    PolyWork& w = P.w;
+    w.words = (N + 31) / 32;
+    w.qcap = N;
+    const bool ok = ok_up && poly_alloc(P, &w.visited, (size_t)(S * w.words)) == cudaSuccess &&
+         poly_alloc(P, &w.queue, (size_t)(S * w.qcap)) == cudaSuccess &&
+         poly_alloc(P, &w.qtype, (size_t)(S * w.qcap)) == cudaSuccess &&
+         poly_alloc(P, &w.count, (size_t)S) == cudaSuccess && poly_alloc(P, &w.acc, (size_t)(5 * N)) == cudaSuccess &&
+         poly_alloc(P, &w.claim, (size_t)N) == cudaSuccess &&
+         cudaMemset(w.count, 0, sizeof(int32_t) * S) == cudaSuccess;
+    w.err = &ctx->d_cnt->error;
+    if (!ok) {
+        ctx->err = "polyMesh: device allocation failed";
+        sdfibm_cuda_destroy(ctx);
+        *out = nullptr;
+        return SDFIBM_ERR_CUDA;
+    }
+    return SDFIBM_OK;
+}
+
+static int poly_interact(sdfibm_ctx* ctx, double time, double dt, const float* U, float* As, float* Fs, float* Ts,
+                         int32_t* Ct, double* FT) {
+    sdfibm_ctx::Poly& P = *ctx->poly;
+    const int64_t N = P.N;
+    const int S = ctx->S;
+    cudaStream_t st = ctx->stream;
+    int launches = 0;
+    mark_begin(ctx);
+    set_step_kernel<<<1, 1, 0, st>>>(ctx->d_step, time, dt, 1, 0.0);
+    // SolidCloud::interact zeroes the four fields over the whole mesh (solidcloud.cpp:438-441)
+    CK(cudaMemsetAsync(As, 0, sizeof(float) * N, st));
+    CK(cudaMemsetAsync(Fs, 0, sizeof(float) * 3 * N, st));
+    CK(cudaMemsetAsync(Ts, 0, sizeof(float) * N, st));
+    CK(cudaMemsetAsync(Ct, 0, sizeof(int32_t) * N, st));
+    CK(cudaMemsetAsync(P.w.acc, 0, sizeof(double) * 5 * N, st));
+    CK(cudaMemsetAsync(P.w.claim, 0xff, sizeof(int32_t) * N, st));
+    launches = 1;
+    if (S > 0) {
+        CK(cudaMemsetAsync(P.w.visited, 0, sizeof(uint32_t) * P.w.words * S, st));
+        CK(cudaMemsetAsync(ctx->d_ftacc, 0, sizeof(double) * 6 * S, st));
+        poly_enum_kernel<<<S, 256, 0, st>>>(P.k, ctx->d_sk, ctx->d_st, P.w);
+        mark(ctx, "poly_enum_kernel");
+        poly_couple_kernel<<<dim3(8, S), 256, 0, st>>>(P.k, ctx->d_sk, ctx->d_st, P.w, U, ctx->d_ftacc, ctx->d_step);
+        mark(ctx, "poly_couple_kernel");
+        launches += 2;
+    }
+    poly_finalize_kernel<<<ctx->num_sms * 4, 256, 0, st>>>(P.w, (int32_t)N, As, Fs, Ts, Ct);
+    mark(ctx, "poly_finalize_kernel");
+    ++launches;
+    if (S > 0) {
+        poly_ft_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->d_ftacc, ctx->d_ft, S, ctx->opt.rho_f);
+        ft_to_state_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->d_ft, ctx->d_st, S);
+        launches += 2;
+    }
+    CK(cudaGetLastError());
+    ctx->launches_last = launches;
+    ctx->interacted = true;
+    if (FT) {
+        if (S > 0) CK(cudaMemcpyAsync(ctx->h_ft, ctx->d_ft, sizeof(double) * 6 * S, cudaMemcpyDeviceToHost, st));
+        const int rs = sync_counters(ctx);
+        if (rs) return rs;
+        std::memcpy(FT, ctx->h_ft, sizeof(double) * 6 * S);
+    }
+    return SDFIBM_OK;
+}
+
+// host fields of a polyMesh context: whole-field copies through device staging (FP32 planes, or FP64 in OpenFOAM's
+// layout converted on the device)
+static int poly_interact_host(sdfibm_ctx* ctx, double time, double dt, const void* U, void* As, void* Fs, void* Ts,
+                              void* Ct, double* FT, bool f64) {
+    sdfibm_ctx::Poly& P = *ctx->poly;
+    const int64_t N = P.N;
+    cudaStream_t st = ctx->stream;
+    if (!P.dU && (poly_alloc(P, &P.dU, 3 * N) || poly_alloc(P, &P.dAs, N) || poly_alloc(P, &P.dFs, 3 * N) ||
+                  poly_alloc(P, &P.dTs, N) || poly_alloc(P, &P.dCt, N)))
+        return fail(ctx, SDFIBM_ERR_CUDA, "staging allocation failed");
+    if (f64 && !P.d64 && poly_alloc(P, &P.d64, 9 * N)) return fail(ctx, SDFIBM_ERR_CUDA, "staging allocation failed");
+    if (f64) {
+        CK(cudaMemcpyAsync(P.d64, U, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
+        u64_to_planes_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(P.d64, N, P.dU);
+    } else {
+        CK(cudaMemcpyAsync(P.dU, U, sizeof(float) * 3 * N, cudaMemcpyHostToDevice, st));
+    }
+    int rc = poly_interact(ctx, time, dt, P.dU, P.dAs, P.dFs, P.dTs, P.dCt, nullptr);
+    if (rc) return rc;
+    if (f64) {
+        double* o = P.d64 + 3 * N;
+        fields_to_f64_kernel<<<ctx->num_sms * 8, 256, 0, st>>>(N, P.dAs, P.dFs, P.dTs, P.dCt, o);
+        CK(cudaMemcpyAsync(As, o, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(Fs, o + N, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(Ts, o + 4 * N, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(Ct, o + 5 * N, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+    } else {
+        CK(cudaMemcpyAsync(As, P.dAs, sizeof(float) * N, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(Fs, P.dFs, sizeof(float) * 3 * N, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(Ts, P.dTs, sizeof(float) * N, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(Ct, P.dCt, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, st));
+    }
+    if (ctx->S > 0) CK(cudaMemcpyAsync(ctx->h_ft, ctx->d_ft, sizeof(double) * 6 * ctx->S, cudaMemcpyDeviceToHost, st));
+    rc = sync_counters(ctx);
+    if (rc) return rc;
+    ctx->host_h2d = (f64 ? 24 : 12) * N;
+    ctx->host_d2h = (f64 ? 48 : 24) * N + 48 * ctx->S;
+    ctx->host_sparse = false;
+    if (FT) std::memcpy(FT, ctx->h_ft, sizeof(double) * 6 * ctx->S);
+    return SDFIBM_OK;
 }
 
 // sizes of the ABI structs as compiled, for binding checks

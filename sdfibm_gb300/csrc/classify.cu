@@ -795,37 +795,6 @@ __device__ inline float filter_mixed(const ShapeK& s, float phi, bool* exact_nee
 
 // LEARNED: the features of the tile's cut cells (one warp), appended to the network's input buffer with the index of
 // the cell's fraction; out of line to keep the tile loop small.  tile0 = fraction index of the tile's cell (0,0,0).
-template <int TX, int TY, int TZ>
-static __device__ __noinline__ void write_features(const ClassifyArgs& A, const uint8_t* cutlist, int ncut,
-                                                   const float* vphi, int s, int64_t tile0, int ext0, int ext1) {
-    constexpr int VX = TX + 1, VY = TY + 1;
-    const int lane = threadIdx.x & 31;
-    for (int u0 = 0; u0 < ncut; u0 += 32) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(&A.cnt->n_feat, min(32, ncut - u0));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        const int u = u0 + lane;
-        if (u < ncut) {
-            const int e = cutlist[u];
-            const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
-            const int v0 = a + VX * (b + VY * c);
-            const float ph[8] = {vphi[v0], vphi[v0 + 1], vphi[v0 + VX], vphi[v0 + VX + 1], vphi[v0 + VX * VY],
-                                 vphi[v0 + VX * VY + 1], vphi[v0 + VX * VY + VX], vphi[v0 + VX * VY + VX + 1]};
-            float fe[MLP_IN];
-            cell_features(ph, A.inv_h, fe);
-            const int64_t slot = (int64_t)base + lane;
-            if (slot < A.feat_cap) {
-#pragma unroll
-                for (int q = 0; q < MLP_IN; ++q) A.feat[q * A.feat_cap + slot] = fe[q];
-                A.fref_solid[slot] = s;
-                A.fref_index[slot] = tile0 + a + (int64_t)ext0 * (b + (int64_t)ext1 * c);
-            } else {
-                set_error(A.cnt, DERR_CAPACITY);
-            }
-        }
-    }
-}
-
 // REF-GEO: the tile's cut cells (one warp) appended to the cell list with the distances of their 8 vertices
 template <int TX, int TY, int TZ>
 static __device__ __noinline__ void write_refgeo_list(const ClassifyArgs& A, const uint8_t* cutlist, int ncut,
@@ -997,7 +966,7 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                 const unsigned bal = __ballot_sync(FULL, is_cut);
                 if (is_cut) {
                     cutlist[ncut + __popc(bal & ((1u << lane) - 1u))] = (uint8_t)e;
-                    if (METHOD == SDFIBM_FRACTION_REFGEO || METHOD == SDFIBM_FRACTION_LEARNED) {
+                    if (METHOD == SDFIBM_FRACTION_REFGEO) {
                         const int v0 = a + VX * (b + VY * c);
                         vneed[v0] = 1; vneed[v0 + 1] = 1; vneed[v0 + VX] = 1; vneed[v0 + VX + 1] = 1;
                         vneed[v0 + VX * VY] = 1; vneed[v0 + VX * VY + 1] = 1; vneed[v0 + VX * VY + VX] = 1;
@@ -1008,7 +977,7 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
             }
             if (ncut == 0) continue;
             __syncwarp();
-            if (METHOD == SDFIBM_FRACTION_REFGEO || METHOD == SDFIBM_FRACTION_LEARNED) {
+            if (METHOD == SDFIBM_FRACTION_REFGEO) {
                 // Solid::phi once per vertex next to a cut candidate.  The needed vertices are compacted first so
                 // every FP64 instruction runs on a full warp; the local point is the solid's FP64 local map applied to
                 // small integer offsets from the bbox corner.
@@ -1029,16 +998,6 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                 for (int u = lane; u < nneed; u += 32) {
                     const int v = vlist[u];
                     const int a = v % VX, b = (v / VX) % VY, c = v / (VX * VY);
-                    if (METHOD == SDFIBM_FRACTION_LEARNED) {
-                        // the network's features need ~1e-6 relative accuracy: FP32 local point and distance
-                        const float dx = tf.bx + (float)a * m.h32[0], dy = tf.by + (float)b * m.h32[1],
-                                    dz = tf.bz + (float)c * m.h32[2];
-                        const float lx = __fmaf_rn(M[0], dx, __fmaf_rn(M[1], dy, M[2] * dz));
-                        const float ly = __fmaf_rn(M[3], dx, __fmaf_rn(M[4], dy, M[5] * dz));
-                        const float lz = __fmaf_rn(M[6], dx, __fmaf_rn(M[7], dy, M[8] * dz));
-                        vphi[v] = sdf32(sh, lx, ly, lz);
-                        continue;
-                    }
                     bool exact = false;
                     float ph;
                     if (ff_shape) {
@@ -1059,13 +1018,6 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                     vphi[v] = ph;
                 }
                 __syncwarp();
-                if (METHOD == SDFIBM_FRACTION_LEARNED) {
-                    // features of every cut cell into the network's input buffer; the fraction comes later
-                    write_features<TX, TY, TZ>(A, cutlist, ncut, vphi, s,
-                                               k.scratch_off + local_index(0, 0, 0), k.ext[0], k.ext[1]);
-                    __syncwarp();
-                    continue;
-                }
                 if (METHOD == SDFIBM_FRACTION_REFGEO && A.rg_phi) {
                     // the cut cells and their vertex distances are listed; refgeo_cells_kernel computes the fractions
                     write_refgeo_list<TX, TY, TZ>(A, cutlist, ncut, vphi, s, k.scratch_off + local_index(0, 0, 0),
@@ -1086,7 +1038,8 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                     alpha[local_index(a, b, c)] = refgeo32(m, ph, I0 + a, J0 + b, K, apz, apz1);
                 }
             } else if (A.fref_index) {
-                // SUBSAMPLE: the cut cells are listed; subsample_cells_kernel samples them, a warp per cell
+                // SUBSAMPLE and LEARNED: the cut cells are listed; subsample_cells_kernel samples them (LEARNED:
+                // learned_stencil_kernel computes the model's inputs), a warp per cell
                 write_cut_list<TX, TY, TZ>(A, cutlist, ncut, s, k.scratch_off + local_index(0, 0, 0), k.ext[0],
                                            k.ext[1]);
             } else {
@@ -1212,6 +1165,60 @@ __global__ void __launch_bounds__(256) recount_kernel(FallbackArgs A) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);
     if (lane == 0 && rechecks) atomicAdd(&A.cnt->exact_rechecks, rechecks);
+}
+
+// LEARNED: the model inputs of every listed cut cell, one warp per cell (cell_stencil on the cell's FP32 frame, built
+// as the classify pass builds a tile's), written at the cell's list position; cells outside the band get a NaN prior
+// and their list positions go to the fallback list.  Each warp stages the inputs of 32 consecutive cells in shared
+// memory and writes every row as 32 consecutive floats.
+__global__ void __launch_bounds__(256) learned_stencil_kernel(StencilArgs A) {
+    __shared__ float s_phi[8][STENCIL_PTS];
+    __shared__ float s_out[8][MLP_NFEAT][33];
+    const int lane = threadIdx.x & 31, w = (threadIdx.x >> 5) & 7;
+    const int64_t n = min((int64_t)A.cnt->n_feat, A.cap);
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const float inv_h = 1.f / A.m.h32[0];
+    const float qx = 0.25f * A.m.h32[0], qy = 0.25f * A.m.h32[1], qz = 0.25f * A.m.h32[2];
+    const float nan = __int_as_float(0x7fc00000);
+    for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < n; base += warps * 32) {
+        int s_l = 0;
+        int64_t idx_l = 0;
+        if (base + lane < n) {
+            s_l = A.fref_solid[base + lane];
+            idx_l = A.fref_index[base + lane];
+        }
+        const int batch = (int)min((int64_t)32, n - base);
+        for (int t = 0; t < batch; ++t) {
+            const int s = __shfl_sync(0xffffffffu, s_l, t);
+            const int64_t idx = __shfl_sync(0xffffffffu, idx_l, t);
+            const SolidK& k = A.sk[s];
+            bool ok = (float)k.radiusB * inv_h >= A.rho_min;  // the solid-size half of the band: no stencil needed
+            float feat = 0.f;
+            if (ok) {
+                const SolidPlan& pl = A.plan[s];
+                const uint32_t local = (uint32_t)(idx - k.scratch_off);
+                const int row = (int)fdiv(local, k.div_e0), lc = (int)fdiv(local, k.div_e01);
+                const int la = (int)local - row * k.ext[0], lb = row - lc * k.ext[1];
+                const float bx = pl.base32[0] + (float)la * A.m.h32[0], by = pl.base32[1] + (float)lb * A.m.h32[1],
+                            bz = pl.base32[2] + (float)lc * A.m.h32[2];
+                float M[9];
+#pragma unroll
+                for (int r = 0; r < 9; ++r) M[r] = pl.M[r];
+                const StencilOut so = cell_stencil(k.shape, M, bx, by, bz, qx, qy, qz, inv_h, s_phi[w]);
+                ok = in_band(so.p4, so.p2, A.tau_refine);
+                feat = so.feat;
+            }
+            if (lane < MLP_NFEAT) s_out[w][lane][t] = (lane == MLP_IN && !ok) ? nan : feat;
+            if (!ok && lane == 0) {
+                const int slot = atomicAdd(&A.cnt->n_fb, 1);
+                A.fb_list[slot] = (int32_t)(base + t);  // n_fb <= n <= cap entries
+            }
+        }
+        __syncwarp();
+        if (lane < batch)
+            for (int f = 0; f < MLP_NFEAT; ++f) A.feat[f * A.cap + base + lane] = s_out[w][f][lane];
+        __syncwarp();
+    }
 }
 
 // REF-GEO fraction of the listed cut cells, one thread per cell (GeometricTools::calcCellVolume on the cell's vertex

@@ -38,16 +38,7 @@ __global__ void plan_kernel(MeshK m, const SolidK* __restrict__ sk, const sdfibm
     const Q4 q = state_quat(st[s]);
     const D3 x = state_pos(st[s]);
     SolidPlan p;
-    // |q|^2 R(q)^T: the linear map of world2local (quaternion::R of OpenFOAM, transposed)
-    {
-        const double w2 = q.w * q.w, x2 = q.v.x * q.v.x, y2 = q.v.y * q.v.y, z2 = q.v.z * q.v.z;
-        const double txy = 2 * q.v.x * q.v.y, twz = 2 * q.w * q.v.z, txz = 2 * q.v.x * q.v.z;
-        const double twy = 2 * q.w * q.v.y, tyz = 2 * q.v.y * q.v.z, twx = 2 * q.w * q.v.x;
-        double R[9] = {w2 + x2 - y2 - z2, txy - twz, txz + twy, txy + twz, w2 - x2 + y2 - z2,
-                       tyz - twx, txz - twy, tyz + twx, w2 - x2 - y2 + z2};
-        for (int r = 0; r < 3; ++r)
-            for (int c = 0; c < 3; ++c) p.M[3 * r + c] = (float)R[3 * c + r];
-    }
+    local_matrix32(q, p.M);  // |q|^2 R(q)^T: the linear map of world2local
     p.err = 0;
     const int32_t n[3] = {m.nx, m.ny, m.nz};
     p.cw[0] = p.cw[1] = p.cw[2] = 0.0;

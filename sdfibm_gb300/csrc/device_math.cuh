@@ -51,6 +51,17 @@ __host__ __device__ inline D3 qtransform(const Q4& q, const D3& u) {
 // IShape::world2local
 __host__ __device__ inline D3 world2local(const D3& p, const D3& t, const Q4& q) { return qtransform(qconj(q), p - t); }
 
+// |q|^2 R(q)^T in FP32: the linear map of world2local (quaternion::R of OpenFOAM, transposed), row-major
+__host__ __device__ inline void local_matrix32(const Q4& q, float* M) {
+    const double w2 = q.w * q.w, x2 = q.v.x * q.v.x, y2 = q.v.y * q.v.y, z2 = q.v.z * q.v.z;
+    const double txy = 2 * q.v.x * q.v.y, twz = 2 * q.w * q.v.z, txz = 2 * q.v.x * q.v.z;
+    const double twy = 2 * q.w * q.v.y, tyz = 2 * q.v.y * q.v.z, twx = 2 * q.w * q.v.x;
+    const double R[9] = {w2 + x2 - y2 - z2, txy - twz, txz + twy, txy + twz, w2 - x2 + y2 - z2,
+                         tyz - twx, txz - twy, tyz + twx, w2 - x2 - y2 + z2};
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) M[3 * r + c] = (float)R[3 * c + r];
+}
+
 // Per-solid shape record used by the kernels (lowered from sdfibm_solid_desc).
 struct ShapeK {
     int32_t type;

@@ -189,12 +189,10 @@ struct ClassifyArgs {
     Counters* cnt;
     int method;        // sdfibm_fraction_method, or -1: classification only
     int subsample_n;
-    // LEARNED: features of every cut cell ([11][feat_cap]) and where its fraction goes
-    float* feat;
+    // SUBSAMPLE, LEARNED, REF-GEO: the list of cut cells (solid, index into alpha), feat_cap entries
     int64_t feat_cap;
     int32_t* fref_solid;
     int64_t* fref_index;  // index into alpha
-    float inv_h;          // 1 / h (x spacing) of the feature scaling
     Recheck* rq;          // deferred SUBSAMPLE rechecks (nullptr: re-evaluate in place)
     int64_t rq_cap;
     float* rg_phi;        // REF-GEO: [8][feat_cap] vertex distances of the listed cut cells (nullptr: fraction in place)
@@ -218,6 +216,21 @@ struct FallbackArgs {
     int64_t rq_cap;
     Recheck* ovf;              // cells to recount (idx, solid), see recount_kernel
     int64_t ovf_cap;
+};
+
+// LEARNED: the model inputs of the listed cut cells (learned_stencil_kernel)
+struct StencilArgs {
+    MeshK m;
+    const SolidK* sk;
+    const SolidPlan* plan;
+    const int32_t* fref_solid;
+    const int64_t* fref_index;
+    int64_t cap;
+    float* feat;          // [SDFIBM_MLP_NFEAT][cap]: network inputs, then the prior logit (NaN outside the band)
+    int32_t* fb_list;     // list positions of the cells outside the band (SUBSAMPLE fallback)
+    Counters* cnt;
+    float tau_refine;     // band: |P4 - P2| limit
+    float rho_min;        // band: smallest bounding radius / h of a solid whose cells the network takes
 };
 
 // UGrid (src/libcollision/ugrid.h:14-58): bbox of the mesh, spacing 2*max radiusB, row-major i*ny*nz + j*nz + k

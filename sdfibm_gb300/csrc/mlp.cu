@@ -1,7 +1,8 @@
 // Learned cut-cell fraction on the Blackwell tensor cores: inference, training (forward + backward), Adam, and the
 // generator of labelled training cells.  Parameter layout, features and numerics: include/sdfibm_mlp.h.
 //
-// Model output: a = sigmoid(logit(planar fraction) + gate * network), see model_prior in mlp.cuh.
+// Model output: a = sigmoid(prior + network), the prior logit(P4) of the sub-cell planar reconstruction (row 16 of the
+// feature buffer, see cell_stencil in mlp.cuh).
 // One CTA of 128 threads works on tiles of 128 cells; thread t owns cell t of the tile, row t of every M = 128
 // operand and lane t of tensor memory.  Thread 0 issues the tcgen05.mma instructions and commits them to one
 // mbarrier; every wait on it is bounded and a timeout ends the CTA's work with an error code.
@@ -168,6 +169,7 @@ __global__ void __launch_bounds__(MLP_THREADS) mlp_infer_kernel(MlpInferArgs A) 
         float x[MLP_IN];
 #pragma unroll
         for (int f = 0; f < MLP_IN; ++f) x[f] = valid ? A.feat[f * A.stride + c] : 0.f;
+        const float prior = valid ? A.feat[MLP_IN * A.stride + c] : 0.f;
         store_a1(sA1, tid, x);
         tc::fence_smem_async();
         __syncthreads();
@@ -201,24 +203,10 @@ __global__ void __launch_bounds__(MLP_THREADS) mlp_infer_kernel(MlpInferArgs A) 
             const float zz = z[j] + sb2[j];
             o += sw3[j] * (zz * sigm(zz));
         }
-        float prior, gate;
-        model_prior(x, prior, gate);
-        const float a = sigm(prior + gate * o);
+        const float a = sigm(prior + o);
         if (valid) {
-            if (!A.ref_solid) {
-                A.out[c] = a;
-            } else {
-                const bool ok = in_band(x, A.tau_twist, A.tau_grad);
-                if (ok) A.alpha[A.ref_index[c]] = a;
-                const unsigned fb = __ballot_sync(__activemask(), !ok);
-                if (!ok) {
-                    const int leader = __ffs(fb) - 1;
-                    int base = 0;
-                    if (lane == leader) base = atomicAdd(A.fb_count, __popc(fb));
-                    base = __shfl_sync(fb, base, leader);
-                    A.fb_list[base + __popc(fb & ((1u << lane) - 1u))] = (int32_t)c;
-                }
-            }
+            if (!A.ref_index) A.out[c] = a;
+            else if (prior == prior) A.alpha[A.ref_index[c]] = a;  // NaN prior: outside the band (fallback)
         }
         tc::fence_before_sync();
         __syncthreads();
@@ -280,8 +268,8 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) mlp_grad_kernel(MlpGradArgs A)
 
     stage_weights(A.params, sW1, sW2, sW2T, sb1, sb2, sw3, sb3);
     for (int e = tid; e < 3 * 64 + 2; e += MLP_THREADS) acc[e] = 0.f;
-    // GB rows 75..79 (padding of the feature block) stay zero
-    for (int e = tid; e < 5 * 128; e += MLP_THREADS) store_bf16(sGB, 75 + e / 128, e % 128, 128, 0.f);
+    // GB rows 64 + MLP_IN .. 79 (padding of the input block, when there are fewer than 16 inputs) stay zero
+    for (int e = tid; e < (16 - MLP_IN) * 128; e += MLP_THREADS) store_bf16(sGB, 64 + MLP_IN + e / 128, e % 128, 128, 0.f);
     if (tid == 0) {
         tc::mbar_init(bar, 1);
         tc::fence_mbar_init();
@@ -305,6 +293,7 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) mlp_grad_kernel(MlpGradArgs A)
         float x[MLP_IN];
 #pragma unroll
         for (int f = 0; f < MLP_IN; ++f) x[f] = valid ? A.feat[f * A.stride + c] : 0.f;
+        const float prior = valid ? A.feat[MLP_IN * A.stride + c] : 0.f;
         const float y = valid ? A.label[c] : 0.f;
         store_a1(sA1, tid, x);
 #pragma unroll
@@ -343,11 +332,9 @@ __global__ void __launch_bounds__(MLP_THREADS, 1) mlp_grad_kernel(MlpGradArgs A)
             const float zz = v[j] + sb2[j];
             o += sw3[j] * (zz * sigm(zz));
         }
-        float prior, gate;
-        model_prior(x, prior, gate);
-        const float a = sigm(prior + gate * o);
+        const float a = sigm(prior + o);
         const float d = valid ? a - y : 0.f;
-        const float dz3 = A.scale * d * a * (1.f - a) * gate;
+        const float dz3 = A.scale * d * a * (1.f - a);
         float w[64];
 #pragma unroll
         for (int j = 0; j < 64; ++j) {
@@ -550,9 +537,15 @@ __device__ D3 surface_point(const ShapeK& sh, Rng& g, double h) {
     return D3{s * d.x, s * d.y, s * d.z};
 }
 
-__global__ void mlp_dataset_kernel(DataArgs A) {
+// One labelled cut cell per thread: the thread draws the shape, pose and cell (FP64) and counts the label lattice in
+// FP64; the inputs come from cell_stencil, as in the coupling path: the warp computes its 32 cells' stencils one after
+// the other from the FP32 frame (cell corner as the offset from the shape centre, the rotation's local map).
+__global__ void __launch_bounds__(128) mlp_dataset_kernel(DataArgs A) {
+    __shared__ ShapeK s_sh[128];
+    __shared__ float s_fr[128][12];  // local map M (9), cell corner (3)
+    __shared__ float s_phi[4][STENCIL_PTS];
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= A.n) return;
+    const bool valid = i < A.n;
     // the family is uniform over a warp: fewer divergent FP64 paths
     Rng gw{mix64(A.seed ^ mix64((uint64_t)(i >> 5) + 0x51ull))};
     const int fam = A.fam[min((int)(gw.uni() * A.nfam), A.nfam - 1)];
@@ -560,8 +553,8 @@ __global__ void mlp_dataset_kernel(DataArgs A) {
     const double h = 1.0;
     const D3 zero{0.0, 0.0, 0.0};
     ShapeK sh;
-    Q4 q;
-    D3 o;
+    Q4 q{1.0, D3{0.0, 0.0, 0.0}};
+    D3 o{0.0, 0.0, 0.0};
     int inside_cnt = 0, attempt = 0;
     for (attempt = 1; attempt <= 256; ++attempt) {
         const double r = h / exp(A.lhr_min + (A.lhr_max - A.lhr_min) * g.uni());
@@ -583,15 +576,29 @@ __global__ void mlp_dataset_kernel(DataArgs A) {
             const D3 pv{o.x + (double)(v & 1) * h, o.y + (double)((v >> 1) & 1) * h, o.z + (double)((v >> 2) & 1) * h};
             inside_cnt += inside64(sh, world2local(pv, zero, q)) ? 1 : 0;
         }
-        if (inside_cnt > 0 && inside_cnt < 8) break;
+        if (!valid || (inside_cnt > 0 && inside_cnt < 8)) break;
     }
-    float ph[8];
-    for (int v = 0; v < 8; ++v) {
-        const D3 pv{o.x + (double)(v & 1) * h, o.y + (double)((v >> 1) & 1) * h, o.z + (double)((v >> 2) & 1) * h};
-        ph[v] = (float)sdf64(sh, world2local(pv, zero, q));
+    for (int k = 0; k < 8; ++k) sh.p32[k] = (float)sh.p[k];
+    for (int k = 0; k < 3; ++k) sh.com32[k] = (float)sh.com[k];
+    s_sh[threadIdx.x] = sh;
+    local_matrix32(q, s_fr[threadIdx.x]);
+    s_fr[threadIdx.x][9] = (float)o.x;
+    s_fr[threadIdx.x][10] = (float)o.y;
+    s_fr[threadIdx.x][11] = (float)o.z;
+    __syncwarp();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int t = 0; t < 32; ++t) {
+        const int src = (w << 5) + t;
+        const int64_t ci = (int64_t)blockIdx.x * blockDim.x + src;
+        if (ci >= A.n) break;  // uniform over the warp
+        float M[9];
+#pragma unroll
+        for (int r = 0; r < 9; ++r) M[r] = s_fr[src][r];
+        const StencilOut so = cell_stencil(s_sh[src], M, s_fr[src][9], s_fr[src][10], s_fr[src][11], 0.25f, 0.25f,
+                                           0.25f, 1.f, s_phi[w]);
+        if (lane < MLP_NFEAT) A.feat[lane * A.n + ci] = so.feat;
     }
-    float f[MLP_IN];
-    cell_features(ph, (float)(1.0 / h), f);
+    if (!valid) return;
     const int n = A.n_sub;
     int cnt = 0;
     for (int c3 = 0; c3 < n; ++c3)
@@ -602,7 +609,6 @@ __global__ void mlp_dataset_kernel(DataArgs A) {
                 const D3 p{o.x + ta * h, o.y + tb * h, o.z + tc3 * h};
                 cnt += inside64(sh, world2local(p, zero, q)) ? 1 : 0;
             }
-    for (int k = 0; k < MLP_IN; ++k) A.feat[k * A.n + i] = f[k];
     A.label[i] = (float)((double)cnt / (double)(n * n * n));
     if (A.recipe) {
         double* r = A.recipe + i * 20;

@@ -2,8 +2,9 @@
 and the model file.
 
 Every function calls libsdfibm_cuda.so; tensors are CUDA torch tensors (torch only holds device memory and the
-stream).  Features are [11, n] float32 (structure of arrays), labels and predictions [n] float32, parameters
-[4993] float32 in the layout W1[64][11], b1, W2[64][64], b2, w3, b3.
+stream).  Feature records are [17, n] float32 (structure of arrays: the 16 network inputs, then the prior
+logit(P4)), labels and predictions [n] float32, parameters [5313] float32 in the layout W1[64][16], b1, W2[64][64],
+b2, w3, b3.  The model: a = sigmoid(prior + network(inputs)), see include/sdfibm_mlp.h.
 """
 import ctypes as C
 import json
@@ -48,8 +49,8 @@ def data_desc(hr=(0.01, 1.5), families=ALL_FAMILIES, n_sub=16, z_axis_frac=0.25)
 
 
 def make_dataset(torch, n, seed, recipe=False, **kw):
-    """n labelled cut cells on the GPU: (features [11, n], labels [n], recipe [n, 20] float64 or None)."""
-    feat = torch.empty((11, n), dtype=torch.float32, device="cuda")
+    """n labelled cut cells on the GPU: (feature records [17, n], labels [n], recipe [n, 20] float64 or None)."""
+    feat = torch.empty((abi.MLP_NFEAT, n), dtype=torch.float32, device="cuda")
     label = torch.empty(n, dtype=torch.float32, device="cuda")
     rec = torch.empty((n, 20), dtype=torch.float64, device="cuda") if recipe else None
     d = data_desc(**kw)
@@ -93,21 +94,46 @@ def train(torch, params, feat, label, epochs=10, batch=16384, lr=2e-3, lr_final_
 
 
 def init_params(seed=0):
-    """Fan-in scaled uniform initialisation (zero biases)."""
+    """Fan-in scaled uniform initialisation (zero biases), output layer small: the model starts near its prior."""
     rng = np.random.default_rng(seed)
-    W1 = rng.uniform(-1, 1, (64, 11)) * np.sqrt(3.0 / 11)
+    n_in = abi.MLP_NIN
+    W1 = rng.uniform(-1, 1, (64, n_in)) * np.sqrt(3.0 / n_in)
     W2 = rng.uniform(-1, 1, (64, 64)) * np.sqrt(3.0 / 64)
-    w3 = rng.uniform(-1, 1, 64) * np.sqrt(3.0 / 64) * 0.1  # start near the planar prior
+    w3 = rng.uniform(-1, 1, 64) * np.sqrt(3.0 / 64) * 0.1
     return np.concatenate([W1.ravel(), np.zeros(64), W2.ravel(), np.zeros(64), w3, [0.0]]).astype(np.float32)
 
 
-def save_model(params, tau_twist, tau_grad, meta, path=MODEL_PATH):
+def save_model(params, tau_refine, rho_min, meta, path=MODEL_PATH):
     os.makedirs(os.path.dirname(path), exist_ok=True)
-    np.savez(path, params=np.asarray(params, np.float32), tau_twist=np.float32(tau_twist),
-             tau_grad=np.float32(tau_grad), meta=json.dumps(meta))
+    np.savez(path, params=np.asarray(params, np.float32), tau_refine=np.float32(tau_refine),
+             rho_min=np.float32(rho_min), meta=json.dumps(meta))
 
 
 def load_model(path=MODEL_PATH):
-    """(params float32 [4993], tau_twist, tau_grad, meta dict) of a trained model file."""
+    """(params float32 [5313], tau_refine, rho_min, meta dict) of a trained model file: the network and its
+    confidence band (|P4 - P2| limit, smallest solid bounding radius in cells)."""
     z = np.load(path)
-    return z["params"].astype(np.float32), float(z["tau_twist"]), float(z["tau_grad"]), json.loads(str(z["meta"]))
+    return z["params"].astype(np.float32), float(z["tau_refine"]), float(z["rho_min"]), json.loads(str(z["meta"]))
+
+
+def accuracy(torch, w, f, FT, fr, FTr, U, reference="SUBSAMPLE 16^3 (4096 samples), same step"):
+    """As of a coupling step (fields f, force/torque FT) against a reference step (fr, FTr) of workload w on the same
+    velocity U: absolute As error over the cut cells (mean and quantiles) and the per-solid force error, normwise
+    against rho_f / dt * volume * (|U| rms + |v| + |omega| r_B), the magnitude of the sum of the cell contributions
+    (median, 90th percentile, max)."""
+    touched = fr["Ct"] != 0
+    cut = touched & ~((fr["As"] == 1.0) & (f["As"] == 1.0))
+    err = (f["As"] - fr["As"]).abs()[cut].double()
+    q = torch.quantile(err[: 1 << 24], torch.tensor([0.5, 0.99, 0.999], dtype=torch.float64, device=err.device))
+    u_rms = float(U.square().mean().sqrt())
+    rel = []
+    for s, d in enumerate(w.solids):
+        v = np.linalg.norm(np.array(d.vel[:])) + np.linalg.norm(np.array(d.omega[:])) * d.shape.radiusB
+        scale = w.opt.rho_f / w.dt * d.shape.volume * (u_rms + v)
+        rel.append(np.linalg.norm(FT[s, :3] - FTr[s, :3]) / scale)
+    rel = np.array(rel)
+    return {"reference": reference, "cut_cells": int(cut.sum()),
+            "as_abs_err_mean": float(err.mean()), "as_abs_err_p50": float(q[0]), "as_abs_err_p99": float(q[1]),
+            "as_abs_err_p999": float(q[2]), "as_abs_err_max": float(err.max()),
+            "force_rel_err_median": float(np.median(rel)), "force_rel_err_p90": float(np.percentile(rel, 90)),
+            "force_rel_err_max": float(rel.max())}

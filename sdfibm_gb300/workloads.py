@@ -13,7 +13,9 @@
                   rho_s=1.5, U~N(0,0.1^2), dt=1e-3, soft-sphere collisions on bounding spheres
 The sedimentation radius is 0.03: 100 circles of radius 0.05 with a 0.01 gap cannot be placed in the unit square
 (they would cover 95% of it, more than the densest hexagonal packing).
-A ``scale`` < 1 shrinks meshes and solid counts for tests while keeping the per-solid resolution (r/h).
+A ``scale`` < 1 shrinks meshes and solid counts for tests while keeping the per-solid resolution (r/h); ``seed``
+draws another instance of the same distribution (the learned fraction's band is calibrated on one that the
+benchmark does not use).
 The reference's public benchmark inputs are not used: these seeded inputs stand in for them.
 Every builder takes ``lower``: the object whose make_shape / make_solid / mask_motion build the solids (default: the
 C++ lowering of include/sdfibm_host.h, i.e. sdfibm_gb300.host); any lowering with the same signatures that restates
@@ -182,16 +184,16 @@ def _poly3d(name, n, nsolids, r_median, sigma, kinds, seed, collision, lower):
     return Workload(name, mesh, solids, opt, 1e-3, (0.0, 0.0, 0.0), 0.1, seed + 100)
 
 
-def poly3d_256(scale=1.0, collision=abi.COLLISION_OFF, lower=None):
+def poly3d_256(scale=1.0, collision=abi.COLLISION_OFF, lower=None, seed=4):
     n = max(16, int(round(256 * scale)))
     ns = max(4, int(round(4096 * scale ** 3)))
-    return _poly3d("poly3d_256", n, ns, 0.01 * 256 / n, 0.4, ["Sphere", "Ellipsoid"], 4, collision, lower)
+    return _poly3d("poly3d_256", n, ns, 0.01 * 256 / n, 0.4, ["Sphere", "Ellipsoid"], seed, collision, lower)
 
 
-def poly3d_512(scale=1.0, collision=abi.COLLISION_SPHERES, lower=None):
+def poly3d_512(scale=1.0, collision=abi.COLLISION_SPHERES, lower=None, seed=5):
     n = max(16, int(round(512 * scale)))
     ns = max(6, int(round(16384 * scale ** 3)))
-    return _poly3d("poly3d_512", n, ns, 0.004 * 512 / n, 0.5, ["Sphere", "Ellipsoid", "Box"], 5, collision, lower)
+    return _poly3d("poly3d_512", n, ns, 0.004 * 512 / n, 0.5, ["Sphere", "Ellipsoid", "Box"], seed, collision, lower)
 
 
 CONFIGS = {"cylinder2d": cylinder2d, "sedimentation2d": sedimentation2d, "poly3d_256": poly3d_256,

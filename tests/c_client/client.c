@@ -29,6 +29,7 @@ int main(int argc, char** argv) {
     typedef void (*entry_fn)(void);
     entry_fn entry[] = {(entry_fn)sdfibm_cuda_create, (entry_fn)sdfibm_cuda_interact,
                         (entry_fn)sdfibm_cuda_interact_host, (entry_fn)sdfibm_cuda_interact_host64,
+                        (entry_fn)sdfibm_cuda_create_polymesh, (entry_fn)sdfibm_cuda_tuning,
                         (entry_fn)sdfibm_cuda_evolve,
                         (entry_fn)sdfibm_cuda_fix_internal, (entry_fn)sdfibm_cuda_get_solids,
                         (entry_fn)sdfibm_cuda_set_solids, (entry_fn)sdfibm_cuda_touched, (entry_fn)sdfibm_cuda_stats,

@@ -140,6 +140,12 @@ int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc*, const sdfibm_solid_desc
     return SDFIBM_ERR_STATE;
 }
 int sdfibm_cuda_set_fraction_model(sdfibm_ctx*, const float*, float, float) { return SDFIBM_ERR_STATE; }
+int sdfibm_cuda_tuning(sdfibm_ctx*, int32_t*, int32_t) { return SDFIBM_ERR_STATE; }
+int sdfibm_cuda_create_polymesh(const double*, int64_t, const int32_t*, const int32_t*, int64_t, const int32_t*,
+                                const int32_t*, int64_t, int32_t, const sdfibm_solid_desc*, int32_t,
+                                const sdfibm_options*, void*, sdfibm_ctx**) {
+    return SDFIBM_ERR_STATE;
+}
 int sdfibm_cuda_autotune(sdfibm_ctx*, double, const float*, float*, float*, float*, int32_t*, int32_t*) {
     return SDFIBM_ERR_STATE;
 }

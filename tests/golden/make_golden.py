@@ -6,6 +6,9 @@
   falling_ellipse.npz   the oracle run on the reference's own OpenFOAM polyMesh of examples/falling_ellipse
                         (100x200x1 cells, ellipse 0.3x0.15 at (0.5,3.5), euler z=-45 deg): touched cells, As, forcing.
                         It pins the uniform-mesh ordering conventions against a real OpenFOAM mesh.
+  re200_blocks.npz      the block structure of examples/flow_past_cylinder/re200/system/blockMeshDict (32 vertices,
+                        9 hex blocks with their cell counts and simpleGrading): the tests rebuild the graded
+                        multi-block mesh from it (tests/polymesh_gen.py) for the unstructured-mesh path.
   tool_vof_alpha.npz    the smooth phase field the reference's VOF initializer wrote for tool_vof/example
                         (0/alpha.water: 200x200x1 cells on [0,4]^2, twelve shapes and two planes of its solidDict).
 It also checks that the host front ends read every solidDict the reference ships, and that the library's OpenFOAM
@@ -44,6 +47,23 @@ def read_faces(path):
     n2 = int(m2.group(1))
     lab = np.frombuffer(rest[m2.end():m2.end() + n2 * 4], dtype="<i4")
     return off, lab
+
+
+def read_block_mesh_dict(path):
+    """vertices [V, 3], hex labels [B, 8], cell counts [B, 3] and simpleGrading [B, 3] of a blockMeshDict (straight
+    edges, uniform expansion per direction), comments removed."""
+    text = open(path).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    vblock = text[text.index("vertices"):text.index("blocks")]
+    verts = np.array([[float(v) for v in m.split()] for m in re.findall(r"\(([^()]*)\)", vblock)])
+    bblock = text[text.index("blocks"):text.index("edges")]
+    hexes, counts, grades = [], [], []
+    for m in re.finditer(r"hex\s*\(([^)]*)\)\s*\(([^)]*)\)\s*simpleGrading\s*\(([^)]*)\)", bblock):
+        hexes.append([int(v) for v in m.group(1).split()])
+        counts.append([int(v) for v in m.group(2).split()])
+        grades.append([float(v) for v in m.group(3).split()])
+    return verts, np.array(hexes), np.array(counts), np.array(grades)
 
 
 def check_example_dicts(ref):
@@ -112,6 +132,11 @@ def main(ref):
     cells, types = oc.touched(0)
     np.savez_compressed(os.path.join(HERE, "falling_ellipse.npz"), cells=cells, types=types, As=f["As"][cells],
                         Fs=f["Fs"].reshape(3, N)[:, cells], FT=FT, U_seed=7, U_std=0.1, dt=0.01)
+    verts, hexes, counts, grades = read_block_mesh_dict(
+        os.path.join(ref, "examples/flow_past_cylinder/re200/system/blockMeshDict"))
+    assert verts.shape == (32, 3) and hexes.shape == (9, 8) and counts.prod(1).sum() == 78400
+    np.savez_compressed(os.path.join(HERE, "re200_blocks.npz"), vertices=verts, hexes=hexes, counts=counts,
+                        grading=grades)
     vof, _ = read_foam_list(os.path.join(ref, "tool_vof/example/0/alpha.water"), "<f8")
     assert len(vof) == 40000
     np.savez_compressed(os.path.join(HERE, "tool_vof_alpha.npz"), alpha=np.ascontiguousarray(vof), nx=200, ny=200,

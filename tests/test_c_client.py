@@ -34,7 +34,7 @@ def test_c_client(cuda_lib, tmp_path):
     r = subprocess.run([exe, str(tmp_path / "solidDict")], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, r.stderr
     lines = r.stdout.split("\n")
-    assert lines[0] == "linked 13" and lines[1] == "solids 2 twod 0 rho_f 1000"
+    assert lines[0] == "linked 15" and lines[1] == "solids 2 twod 0 rho_f 1000"
     assert int(lines[2].split()[1]) > 500
     # the same records through the Python binding
     solids, _, _ = parse_soliddict(DICT, 1000.0)

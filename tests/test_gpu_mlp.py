@@ -23,20 +23,35 @@ def _params(seed, bias=0.1):
 
 
 def test_dataset_matches_oracle(cuda_lib, torch_cuda):
+    """Generated cells against the oracle: labels exactly (FP64 inside tests on both sides), inputs and prior within
+    the FP32 rounding of the device's stencil (distances from FP32 local coordinates, FP32 sub-cell planes)."""
     torch = torch_cuda
     n = 2048  # 64 warps: every family drawn (the family is chosen per warp)
     feat, label, rec = learned.make_dataset(torch, n, seed=7, recipe=True, n_sub=8)
     feat, label, rec = feat.cpu().numpy(), label.cpu().numpy(), rec.cpu().numpy()
+    assert feat.shape == (abi.MLP_NFEAT, n)
     types = set()
+    phis = []
     for i in range(n):
         phi, cnt = O.sample_cell(rec[i], 8)
         assert 0 < rec[i, 17] < 8, "cell %d is not cut" % i
         assert label[i] == np.float32(cnt / 512.0), "label of cell %d: %r vs %r" % (i, label[i], cnt / 512.0)
-        f = MO.features(phi.astype(np.float32)[None, :], np.float32(1.0))[0]
-        np.testing.assert_array_equal(feat[:, i], f)
+        phis.append(phi)
         types.add(int(rec[i, 0]))
+    ref = MO.features(np.array(phis))
+    # distance inputs: FP32 local coordinates of points up to ~20 cells from the origin (the inputs need 1e-4: BF16
+    # hi + lo pairs keep about 16 bits)
+    d = np.abs(feat[:15].T - ref[:, :15]) / (1 + np.abs(ref[:, :15]))
+    assert d.max() <= 1e-4, "distance inputs: max scaled difference %g" % d.max()
+    # P2 and P4 through their logits: compare the fractions
+    sig = lambda z: 1.0 / (1.0 + np.exp(-z.astype(np.float64)))
+    assert np.abs(sig(feat[15]) - sig(ref[:, 15])).max() <= 2e-5
+    assert np.abs(sig(feat[16]) - sig(ref[:, 16])).max() <= 2e-5
     assert types == {abi.SHAPE_SPHERE, abi.SHAPE_ELLIPSOID, abi.SHAPE_BOX, abi.SHAPE_PLANE, abi.SHAPE_CIRCLE,
                      abi.SHAPE_ELLIPSE}
+    # the prior is a good estimate already: planes are exact up to the 8^3 label's own lattice error
+    plane = rec[:, 0] == abi.SHAPE_PLANE
+    assert np.abs(sig(feat[16][plane]) - label[plane]).mean() < 5e-3
 
 
 def test_forward_matches_oracle(cuda_lib, torch_cuda):
@@ -45,12 +60,15 @@ def test_forward_matches_oracle(cuda_lib, torch_cuda):
     feat, _, _ = learned.make_dataset(torch, n, seed=11)
     p = _params(3)
     out = learned.forward(torch, torch.from_numpy(p).cuda(), feat).cpu().numpy()
-    ref = MO.forward(p, feat.cpu().numpy().T)
+    X = feat.cpu().numpy().T
+    ref = MO.forward(p, X)
     err = np.abs(out - ref)
     assert err.max() <= FWD_ABS, "max |GPU - oracle| = %g at cell %d" % (err.max(), int(err.argmax()))
-    # the hi/lo split matters: a single-BF16 forward is far off
-    lo = MO.forward(p, MO.bf16(feat.cpu().numpy().T))
-    assert np.abs(lo - ref).max() > FWD_ABS
+    # the hi/lo split matters: single-BF16 inputs are several times further off
+    Xb = X.copy()
+    Xb[:, :MO.N_IN] = MO.bf16(X[:, :MO.N_IN])
+    lo = MO.forward(p, Xb)
+    assert np.abs(lo - ref).max() > 3 * err.max()
 
 
 def test_forward_strided_features(cuda_lib, torch_cuda):
@@ -110,10 +128,10 @@ def test_training_lowers_the_error(cuda_lib, torch_cuda):
     p = torch.from_numpy(learned.init_params(1)).cuda()
     before = (learned.forward(torch, p, tf) - tl).abs().mean().item()
     p0 = p.clone()
-    p0[-65:] = 0.0  # network output zero: the planar prior alone
+    p0[-65:] = 0.0  # network output zero: the prior alone (4^3 sub-cell planar reconstruction)
     prior_only = (learned.forward(torch, p0, tf) - tl).abs().mean().item()
     losses = learned.train(torch, p, feat, label, epochs=10, batch=4096, lr=2e-3, warmup_steps=50)
     after = (learned.forward(torch, p, tf) - tl).abs().mean().item()
     assert np.all(np.isfinite(losses)) and losses[-1] < losses[0]
-    # what the trained network gains over the model without it (the planar prior)
-    assert after < 0.9 * prior_only and after < before, (before, prior_only, after, losses)
+    # what the trained network gains over the model without it (the sub-cell planar prior)
+    assert after < 0.7 * prior_only and after < before, (before, prior_only, after, losses)

@@ -1,75 +1,72 @@
-"""Host-side parts of the learned cut-cell fraction, on CPU: the confidence-band scores (the formulas of the device's
-in_band), the band calibration of the trainer, and the shipped model file."""
+"""Host-side parts of the learned cut-cell fraction, on CPU: the sub-cell planar reconstructions of the oracle's
+restatement (exact on planes, converging on curved surfaces), the band score of the trainer against the oracle's,
+and the model file."""
 import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")
 
-# the 8 vertices of a unit cell in cellPoints order (x fastest, then y, then z)
-CORNERS = np.array([[i, j, k] for k in (0, 1) for j in (0, 1) for i in (0, 1)], dtype=np.float64)
+
+def _stencil(fn):
+    """phi at the 5^3 lattice of the unit cell (index i + 5 (j + 5 k))."""
+    g = np.array([[i / 4, j / 4, k / 4] for k in range(5) for j in range(5) for i in range(5)])
+    return fn(g)
 
 
-def _features(phi):
-    f = torch.zeros((11, phi.shape[1]), dtype=torch.float32)
-    f[:8] = torch.from_numpy(phi.astype(np.float32))
-    return f
-
-
-def test_band_scores_of_planes_and_spheres():
-    from sdfibm_gb300.train_fraction import band_scores
+def test_subcell_priors_exact_on_planes():
+    from oracle import mlp_oracle as MO
     rng = np.random.default_rng(0)
-    n = rng.normal(size=(3, 500))
-    n /= np.linalg.norm(n, axis=0)
-    d = rng.uniform(-0.8, 0.8, 500)
-    phi = CORNERS @ n + d                                    # a plane's signed distance, in cell sizes
-    tw, gd = band_scores(torch, _features(phi))
-    assert tw.abs().max().item() < 1e-5 and gd.max().item() < 1e-5   # no twist, unit gradient
-    # spheres through the cell centre, seen along a diagonal: twisted, more so the smaller the radius
-    u = np.ones(3) / np.sqrt(3.0)
-    tws = []
-    for r in (1.5, 3.0, 12.0):
-        centre = np.array([0.5, 0.5, 0.5]) - r * u
-        phi = np.linalg.norm(CORNERS - centre, axis=1)[:, None] - r
-        tws.append(band_scores(torch, _features(phi))[0].item())
-    assert tws[0] > tws[1] > tws[2] > 0
+    for _ in range(200):
+        n = rng.normal(size=3)
+        n /= np.linalg.norm(n)
+        d = rng.uniform(-0.9, 0.9)
+        phi = _stencil(lambda g: g @ n + d)[None, :]
+        exact = MO.plane_fraction(phi[:, [0, 4, 20, 24, 100, 104, 120, 124]])
+        for k in (1, 2, 4):
+            assert abs(MO.subcell_prior(phi, k)[0] - exact[0]) < 1e-12
 
 
-def test_band_scores_match_the_oracle():
-    """The trainer's scores and the oracle's restatement of the device's in_band give the same FP32 values."""
-    from oracle import mlp_oracle
-    from sdfibm_gb300.train_fraction import band_scores
-    feat = np.random.default_rng(2).normal(size=(11, 4096)).astype(np.float32)
-    tw, gd = band_scores(torch, torch.from_numpy(feat))
-    tw_o, gd_o = mlp_oracle.band_scores(feat.T)
-    assert np.allclose(tw.numpy(), tw_o, rtol=1e-6, atol=1e-6) and np.allclose(gd.numpy(), gd_o, rtol=1e-6, atol=1e-6)
+def test_subcell_priors_converge_on_spheres():
+    """Finer sub-cells track a curved surface better: |P4 - exact| < |P2 - exact| < |P1 - exact| on average."""
+    from oracle import mlp_oracle as MO
+    rng = np.random.default_rng(1)
+    errs = {1: [], 2: [], 4: []}
+    lat = (np.arange(64) + 0.5) / 64
+    L = np.stack(np.meshgrid(lat, lat, lat, indexing="ij"), -1).reshape(-1, 3)
+    for _ in range(60):
+        r = rng.uniform(1.0, 3.0)
+        c = np.array([0.5, 0.5, 0.5]) + rng.normal(size=3) * 0.2
+        u = rng.normal(size=3)
+        c = c - r * u / np.linalg.norm(u)          # the surface passes near the cell centre
+        phi = _stencil(lambda g: np.linalg.norm(g - c, axis=1) - r)[None, :]
+        exact = (np.linalg.norm(L - c, axis=1) < r).mean()
+        for k in (1, 2, 4):
+            errs[k].append(abs(MO.subcell_prior(phi, k)[0] - exact))
+    m = {k: np.mean(v) for k, v in errs.items()}
+    assert m[4] < 0.5 * m[2] < 0.5 * m[1], m
 
 
-def test_calibration_keeps_the_error_limits():
-    from sdfibm_gb300.train_fraction import calibrate
-    g = torch.Generator().manual_seed(1)
-    n = 200000
-    tw = torch.rand(n, generator=g)
-    gd = torch.rand(n, generator=g) * 0.1
-    # the error grows with the twist: cells above 0.5 are far off
-    err = torch.where(tw < 0.5, 2e-4 * torch.rand(n, generator=g), 5e-2 * torch.ones(n))
-    frac, a, b, m, p = calibrate(torch, err, tw, gd, 1e-3, 1e-2)
-    acc = (tw <= a) & (gd <= b)
-    assert 0.3 < frac <= 0.5 + 1e-3 and abs(acc.float().mean().item() - frac) < 1e-6
-    assert err[acc].mean().item() <= 1e-3 and m <= 1e-3 and p <= 1e-2
-    # limits that nothing meets leave the band empty
-    assert calibrate(torch, err, tw, gd, 1e-9, 1e-9)[0] == 0.0
+def test_band_score_matches_the_oracle():
+    from oracle import mlp_oracle as MO
+    from sdfibm_gb300.train_fraction import band_score
+    feat = np.random.default_rng(2).normal(size=(17, 4096)).astype(np.float32) * 3
+    s = band_score(torch, torch.from_numpy(feat)).numpy()
+    assert np.allclose(s, MO.band_score(feat.T), rtol=1e-6, atol=1e-9)
 
 
 def test_shipped_model_file():
     from sdfibm_gb300 import abi, learned
-    params, tau_twist, tau_grad, meta = learned.load_model()
+    params, tau_refine, rho_min, meta = learned.load_model()
     assert params.dtype == np.float32 and params.shape == (abi.MLP_NPARAM,) and np.isfinite(params).all()
-    assert tau_twist > 0 and tau_grad > 0 and "band" in meta
+    assert tau_refine > 0 and rho_min >= 0 and "band" in meta
+    cal = meta["band"]["calibration"]
+    # the band is calibrated on a workload the benchmark does not use
+    assert "seed 6" in cal["workload"] and cal["chosen"]["tau_refine"] == pytest.approx(tau_refine)
 
 
 def test_model_file_round_trip(tmp_path):
     from sdfibm_gb300 import learned
     p = learned.init_params(3)
-    learned.save_model(p, 0.25, 0.05, {"note": "test"}, path=str(tmp_path / "m.npz"))
+    learned.save_model(p, 0.25, 1.5, {"note": "test"}, path=str(tmp_path / "m.npz"))
     q, a, b, meta = learned.load_model(str(tmp_path / "m.npz"))
-    assert np.array_equal(p, q) and a == np.float32(0.25) and b == np.float32(0.05) and meta == {"note": "test"}
+    assert np.array_equal(p, q) and a == np.float32(0.25) and b == np.float32(1.5) and meta == {"note": "test"}

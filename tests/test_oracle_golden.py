@@ -125,3 +125,54 @@ def test_falling_ellipse_golden_on_the_gpu(cuda_lib, torch_cuda):
     scale_t = np.linalg.norm(np.cross(r.T, dF.T), axis=1).sum()
     assert np.linalg.norm(FT[0, :3] - g["FT"][0, :3]) <= 1e-6 * scale_f
     assert np.linalg.norm(FT[0, 3:] - g["FT"][0, 3:]) <= 1e-6 * scale_t
+
+
+def test_polymesh_generator_single_block_equals_the_uniform_mesh():
+    """tests/polymesh_gen.py writes the uniform mesh as OpenFOAM lists: the oracle's polyMesh path on them gives the
+    uniform path's touched sets and fields (to the rounding of the triangle-fan face geometry)."""
+    from oracle.oracle import Lowering as L
+    from polymesh_gen import uniform_block
+    n, origin, h = (24, 20, 16), (-1.0, -0.8, -0.6), (2 / 24, 1.6 / 20, 1.2 / 16)
+    pts, fo, fl, ow, nb, nc = uniform_block(n, origin, h)
+    sol = [L.make_solid(0, L.make_shape("Sphere", radius=0.4), 1.0, (0.05, 0.02, -0.03), vel=(0.1, 0, 0),
+                        omega=(0, 0, 1)),
+           L.make_solid(1, L.make_shape("Box", radiusa=0.2, radiusb=0.3, radiusc=0.25), 1.0, (0.5, 0.3, 0.1),
+                        (10, 20, 30))]
+    opt = abi.options(rho_f=1.0)
+    ou = OracleCloud(abi.mesh_desc(n, origin, h), sol, opt, faithful=False)
+    op = OracleCloud(abi.mesh_desc(n, origin, h), sol, opt, faithful=False, polymesh=(pts, fo, fl, ow, nb))
+    U = np.random.default_rng(0).normal(size=3 * nc)
+    fu, fp = ou.new_fields(), op.new_fields()
+    FTu = ou.interact(0.0, 0.01, U, fu)
+    FTp = op.interact(0.0, 0.01, U, fp)
+    for s in range(2):
+        cu, tu = ou.touched(s)
+        cp, tp = op.touched(s)
+        assert np.array_equal(cu, cp) and np.array_equal(tu, tp)
+    assert np.abs(fu["As"] - fp["As"]).max() < 1e-12
+    assert np.abs(FTu - FTp).max() < 1e-12 * np.abs(FTu).max()
+
+
+def test_re200_multiblock_mesh_reproduces_the_shipped_As():
+    """The re200 case on its own 9-block graded mesh (rebuilt from the reference's blockMeshDict by
+    tests/polymesh_gen.py) through the oracle's polyMesh path: every cell outside the centre block stays 0 and the
+    centre block reproduces the shipped As (the flagged cell aside) to 1e-9."""
+    from oracle.oracle import Lowering as L
+    from polymesh_gen import block_mesh
+    g = golden("re200_blocks.npz")
+    pts, fo, fl, ow, nb, nc = block_mesh(g["vertices"], g["hexes"], g["counts"], g["grading"])
+    assert nc == 78400
+    solid = L.make_solid(0, L.make_shape("Circle", radius=1.0), 1.0, (0, 0, 0), motion=L.mask_motion("b000000"))
+    oc = OracleCloud(abi.mesh_desc((1, 1, 1), (0, 0, 0), (1, 1, 1), twod=1), [solid], abi.options(rho_f=1.0),
+                     faithful=False, polymesh=(pts, fo, fl, ow, nb))
+    f = oc.new_fields()
+    oc.interact(0.0, 1.0, np.zeros(3 * oc.N), f)
+    As = f["As"]
+    assert (np.delete(As, np.arange(20800, 20800 + 14400)) == 0).all()
+    centre = As[20800:20800 + 14400].reshape(120, 120)
+    ref = golden("re200_As.npz")["As"].reshape(120, 120)
+    mask = np.ones_like(ref, dtype=bool)
+    for j, i in RE200_FLAGGED:
+        mask[j, i] = False
+    assert np.abs(centre - ref)[mask].max() < 1e-9
+    assert (centre > 1e-9).sum() >= 344 and 0.6 < centre[50, 57] < 0.7
