@@ -902,9 +902,25 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                 return (int64_t)(tx * TX + a) + (int64_t)k.ext[0] * ((ty * TY + b) + (int64_t)k.ext[1] * (tz * TZ + c));
             };
             // whole tile outside the mesh or outside the solid's oriented bounding box: no cell has an inside vertex
-            const bool cull = pl.err != 0 || I0 + cx <= 0 || J0 + cy <= 0 || K0 + cz <= 0 || I0 >= m.nx ||
-                              J0 >= m.ny || K0 >= m.nz || I0 + cx < vlo0 || I0 > vhi0 || J0 + cy < vlo1 ||
-                              J0 > vhi1 || K0 + cz < vlo2 || K0 > vhi2;
+            bool cull = pl.err != 0 || I0 + cx <= 0 || J0 + cy <= 0 || K0 + cz <= 0 || I0 >= m.nx ||
+                        J0 >= m.ny || K0 >= m.nz || I0 + cx < vlo0 || I0 > vhi0 || J0 + cy < vlo1 ||
+                        J0 > vhi1 || K0 + cz < vlo2 || K0 > vhi2;
+            if (!cull && pl.cull_box) {
+                // separating axes of the solid's local box: the tile's centre and half extents seen in the local
+                // frame (FP32 with a relative margin of 1e-4 on both sides of every comparison)
+                const float hx = 0.5f * (float)cx * m.h32[0], hy = 0.5f * (float)cy * m.h32[1],
+                            hz = 0.5f * (float)cz * m.h32[2];
+                const float tcx = sb[0] + (float)(tx * TX) * m.h32[0] + hx;
+                const float tcy = sb[1] + (float)(ty * TY) * m.h32[1] + hy;
+                const float tcz = sb[2] + (float)(tz * TZ) * m.h32[2] + hz;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const float lc = __fmaf_rn(M[3 * a], tcx, __fmaf_rn(M[3 * a + 1], tcy, M[3 * a + 2] * tcz));
+                    const float rad = fabsf(M[3 * a]) * hx + fabsf(M[3 * a + 1]) * hy + fabsf(M[3 * a + 2]) * hz;
+                    const float gap = fabsf(lc - pl.lbox_c[a]) - pl.lbox_s[a] - rad;
+                    cull = cull || gap > 1e-4f * (fabsf(lc) + fabsf(pl.lbox_c[a]) + pl.lbox_s[a] + rad) + 1e-30f;
+                }
+            }
             if (cull) {
                 for (int e = lane; e < NC; e += 32) {
                     const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
@@ -1173,6 +1189,7 @@ __global__ void __launch_bounds__(256) recount_kernel(FallbackArgs A) {
 // memory and writes every row as 32 consecutive floats.
 __global__ void __launch_bounds__(256) learned_stencil_kernel(StencilArgs A) {
     __shared__ float s_phi[8][STENCIL_PTS];
+    __shared__ uint8_t s_list[8][72];
     __shared__ float s_out[8][MLP_NFEAT][33];
     const int lane = threadIdx.x & 31, w = (threadIdx.x >> 5) & 7;
     const int64_t n = min((int64_t)A.cnt->n_feat, A.cap);
@@ -1204,7 +1221,7 @@ __global__ void __launch_bounds__(256) learned_stencil_kernel(StencilArgs A) {
                 float M[9];
 #pragma unroll
                 for (int r = 0; r < 9; ++r) M[r] = pl.M[r];
-                const StencilOut so = cell_stencil(k.shape, M, bx, by, bz, qx, qy, qz, inv_h, s_phi[w]);
+                const StencilOut so = cell_stencil(k.shape, M, bx, by, bz, qx, qy, qz, inv_h, s_phi[w], s_list[w]);
                 ok = in_band(so.p4, so.p2, A.tau_refine);
                 feat = so.feat;
             }

@@ -40,6 +40,22 @@ __global__ void plan_kernel(MeshK m, const SolidK* __restrict__ sk, const sdfibm
     SolidPlan p;
     local_matrix32(q, p.M);  // |q|^2 R(q)^T: the linear map of world2local
     p.err = 0;
+    // local box holding the inside region (widened far beyond FP32 rounding): tiles of the classify pass that lie
+    // outside it hold no inside vertex
+    p.cull_box = 0;
+    if (!k.shape.prism && !k.infinite &&
+        (k.shape.type == SDFIBM_SHAPE_SPHERE || k.shape.type == SDFIBM_SHAPE_ELLIPSOID ||
+         k.shape.type == SDFIBM_SHAPE_BOX)) {
+        const double* sp = k.shape.p;
+        const bool ell = k.shape.type == SDFIBM_SHAPE_ELLIPSOID;  // ignores com
+        const bool sph = k.shape.type == SDFIBM_SHAPE_SPHERE;
+        for (int a = 0; a < 3; ++a) {
+            const double half = sph ? sp[0] : sp[a];
+            p.lbox_c[a] = ell ? 0.f : (float)(-k.shape.com[a]);
+            p.lbox_s[a] = (float)(half * (1.0 + 1e-4) + 1e-4 * fabs(k.shape.com[a]) + 1e-30);
+        }
+        p.cull_box = 1;
+    }
     const int32_t n[3] = {m.nx, m.ny, m.nz};
     p.cw[0] = p.cw[1] = p.cw[2] = 0.0;
     p.rcull = 0.0;
@@ -145,7 +161,6 @@ __global__ void plan_kernel(MeshK m, const SolidK* __restrict__ sk, const sdfibm
             p.ds_hi[r] = (float)d6[r];
             p.ds_lo[r] = (float)(d6[r] - (double)p.ds_hi[r]);
         }
-        p.pad3 = 0.f;
     }
     // FP64 origin of the tile frames and the local map (world2local of the bbox corner plus the images of the cell
     // edge vectors), so tiles build their frames without per-tile FP64 work

@@ -91,7 +91,8 @@ struct SolidPlan {
     float us_hi[3], us_lo[3];
     float ds_hi[6], ds_lo[6];
     float cb32[3];
-    float pad3;
+    int32_t cull_box;         // 1: the inside region lies in the local box below (3-D spheres, ellipsoids, boxes)
+    float lbox_c[3], lbox_s[3];  // that box in the local frame: centre and half extents (FP32, widened)
 };
 
 // Global counters / flags (one record per context, device memory).

@@ -544,6 +544,7 @@ __global__ void __launch_bounds__(128) mlp_dataset_kernel(DataArgs A) {
     __shared__ ShapeK s_sh[128];
     __shared__ float s_fr[128][12];  // local map M (9), cell corner (3)
     __shared__ float s_phi[4][STENCIL_PTS];
+    __shared__ uint8_t s_list[4][72];
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < A.n;
     // the family is uniform over a warp: fewer divergent FP64 paths
@@ -595,7 +596,7 @@ __global__ void __launch_bounds__(128) mlp_dataset_kernel(DataArgs A) {
 #pragma unroll
         for (int r = 0; r < 9; ++r) M[r] = s_fr[src][r];
         const StencilOut so = cell_stencil(s_sh[src], M, s_fr[src][9], s_fr[src][10], s_fr[src][11], 0.25f, 0.25f,
-                                           0.25f, 1.f, s_phi[w]);
+                                           0.25f, 1.f, s_phi[w], s_list[w]);
         if (lane < MLP_NFEAT) A.feat[lane * A.n + ci] = so.feat;
     }
     if (!valid) return;
