@@ -224,6 +224,16 @@ int sdfibm_cuda_evolve(sdfibm_ctx* ctx, double time, double dt);
  * cell with Ct[c] >= 4.  Visits only the cells the last interact touched. */
 int sdfibm_cuda_fix_internal(sdfibm_ctx* ctx, const int32_t* Ct, float* U);
 
+/* Optional, for a fluid solver whose fields live on the GPU: the forcing update the reference's solver applies after
+ * interact (main.cpp:70-77, its cell fields): U = U - Fs dt per component and, when T is not null,
+ * T = (1 - As) T + Ts, computed in FP64 and rounded once to the FP32 fields.  As, Fs and Ts must be the fields the
+ * last interact on this context wrote (SDFIBM_ERR_STATE otherwise); only the cells that interact touched are
+ * visited (elsewhere As = Fs = Ts = 0 and U, T keep their values, as in the dense update).  The face-flux update
+ * (phi -= dt (interpolate(Fs) & Sf)) and the boundary corrections belong to the solver's mesh and stay there.
+ * Enqueued on the context's stream. */
+int sdfibm_cuda_apply_forcing(sdfibm_ctx* ctx, double dt, const float* As, const float* Fs, const float* Ts,
+                              float* U, float* T);
+
 /* Solid state download / upload for saveState, saveRestart and restarts (solidcloud.cpp:578-665). */
 int sdfibm_cuda_get_solids(sdfibm_ctx* ctx, sdfibm_solid_state* out, int32_t nsolids);
 int sdfibm_cuda_set_solids(sdfibm_ctx* ctx, const sdfibm_solid_state* in, int32_t nsolids);

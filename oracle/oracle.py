@@ -181,6 +181,9 @@ class OracleCloud:
         return st
 
     def set_state(self, st):
+        """Solid states from a ctypes array or a sequence of abi.SolidState (e.g. SolidCloud.states())."""
+        if not isinstance(st, C.Array):
+            st = (abi.SolidState * max(1, self.nsolids))(*st)
         lib().oracle_set_state(self.h, st, self.nsolids)
 
     def mean_field(self, sampler, U, Ct=None):

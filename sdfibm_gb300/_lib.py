@@ -15,7 +15,8 @@ _lib = None
 CUDA_SYMBOLS = [
     "sdfibm_options_default", "sdfibm_cuda_create", "sdfibm_cuda_interact", "sdfibm_cuda_interact_host",
     "sdfibm_cuda_interact_host64", "sdfibm_cuda_create_polymesh",
-    "sdfibm_cuda_evolve", "sdfibm_cuda_fix_internal", "sdfibm_cuda_get_solids", "sdfibm_cuda_set_solids",
+    "sdfibm_cuda_evolve", "sdfibm_cuda_fix_internal", "sdfibm_cuda_apply_forcing", "sdfibm_cuda_get_solids",
+    "sdfibm_cuda_set_solids",
     "sdfibm_cuda_touched", "sdfibm_cuda_stats", "sdfibm_cuda_kernel_times", "sdfibm_cuda_last_error",
     "sdfibm_cuda_version",
     "sdfibm_cuda_destroy", "sdfibm_cuda_touched_noalloc", "sdfibm_cuda_set_fraction_model", "sdfibm_cuda_autotune",
@@ -57,6 +58,7 @@ def load():
     L.sdfibm_cuda_interact_host64.argtypes = [vp, dbl, dbl, vp, vp, vp, vp, vp, vp]
     L.sdfibm_cuda_evolve.argtypes = [vp, dbl, dbl]
     L.sdfibm_cuda_fix_internal.argtypes = [vp, vp, vp]
+    L.sdfibm_cuda_apply_forcing.argtypes = [vp, dbl, vp, vp, vp, vp, vp]
     L.sdfibm_cuda_get_solids.argtypes = [vp, P(abi.SolidState), i32]
     L.sdfibm_cuda_set_solids.argtypes = [vp, P(abi.SolidState), i32]
     L.sdfibm_cuda_touched.argtypes = [vp, i32, vp, vp, i64, P(i64)]

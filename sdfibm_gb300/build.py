@@ -2,7 +2,8 @@
 
 ``python -m sdfibm_gb300.build`` or ``sdfibm_gb300.build.build()``.  Translation units are compiled in parallel
 with nvcc; ``-fmad=false`` keeps every FP64 operation unfused so the exact path reproduces host FP64 arithmetic
-(FP32 hot loops use explicit fused multiply-add intrinsics).
+(FP32 hot loops use explicit fused multiply-add intrinsics), except in the translation units of CONTRACT_SOURCES,
+which hold FP32 arithmetic only.
 """
 import concurrent.futures as cf
 import os
@@ -14,7 +15,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libsdfibm_cuda.so")
 BUILD_DIR = os.path.join(HERE, "_build")
-CU_SOURCES = ["classify.cu", "coupling.cu", "evolve.cu", "capi.cu", "noalloc.cu", "mlp.cu", "poly.cu"]
+CU_SOURCES = ["classify.cu", "coupling.cu", "evolve.cu", "capi.cu", "noalloc.cu", "mlp.cu", "poly.cu", "stencil.cu"]
+# pure FP32 kernels with no exact path: compiled with multiply-add contraction
+CONTRACT_SOURCES = {"stencil.cu"}
 CXX_SOURCES = ["host.cpp", "host_dict.cpp", "host_io.cpp", "host_poly.cpp"]
 # the host half alone (no CUDA): what CPU-only builds of the host code (sanitizer runs, test doubles) compile
 HOST_SOURCES = [os.path.join("sdfibm_gb300", "csrc", f) for f in CXX_SOURCES]
@@ -51,8 +54,9 @@ def build(force=False, verbose=False):
     jobs = []
     for f in CU_SOURCES:
         obj = os.path.join(BUILD_DIR, f + ".o")
-        cmd = [nv] + ARCH + common + ["-lineinfo", "-fmad=false", "-Xptxas", "-warn-spills", "-c",
-                                      os.path.join(CSRC, f), "-o", obj]
+        fmad = [] if f in CONTRACT_SOURCES else ["-fmad=false"]
+        cmd = [nv] + ARCH + common + ["-lineinfo"] + fmad + ["-Xptxas", "-warn-spills", "-c", os.path.join(CSRC, f),
+                                                             "-o", obj]
         jobs.append((cmd, obj))
     for f in CXX_SOURCES:
         obj = os.path.join(BUILD_DIR, f + ".o")

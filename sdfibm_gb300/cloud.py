@@ -187,6 +187,13 @@ class SolidCloud:
     def fix_internal(self, Ct, U):
         self._check(self._L.sdfibm_cuda_fix_internal(self._h, _ptr(Ct), _ptr(U)))
 
+    def apply_forcing(self, dt, fields, U, T=None):
+        """The solver's forcing update on device fields (main.cpp:70-77): U -= Fs dt, T = (1 - As) T + Ts, from the
+        fields the last interact wrote (sdfibm_cuda_apply_forcing)."""
+        self._check(self._L.sdfibm_cuda_apply_forcing(self._h, float(dt), _ptr(fields["As"]), _ptr(fields["Fs"]),
+                                                       _ptr(fields["Ts"]), _ptr(U),
+                                                       _ptr(T) if T is not None else None))
+
     def states(self):
         st = (abi.SolidState * max(1, self.nsolids))()
         self._check(self._L.sdfibm_cuda_get_solids(self._h, st, self.nsolids))

@@ -41,12 +41,18 @@ __global__ void connect_small_kernel(MeshK m, const SolidK* sk, SolidPlan* plan,
                                      int64_t cap_in, int64_t cap_cut, Counters* cnt, const int32_t* solids,
                                      int nsolids);
 
-__global__ void couple_kernel(CoupleArgs A);
+__global__ void couple_shared_kernel(CoupleArgs A);
+__global__ void shared_scan_kernel(const int32_t* in_cell, const int32_t* cut_cell, const int32_t* Ct, Counters* cnt,
+                                   int64_t N, const uint32_t* sbits, uint32_t* shent, int64_t shent_cap);
+__global__ void couple_chunks_kernel(CoupleArgs A);
+__global__ void apply_forcing_kernel(int64_t N, const uint32_t* cbits, double dt, const float* As, const float* Fs,
+                                     const float* Ts, float* U, float* T);
 __global__ void finalize_kernel(float* As, float* Ts, float* Fs, int32_t* Ct, const Counters* cnt, int64_t N,
                                 int32_t* sh_keys, double* sh_vals, const int32_t* sh_used, int32_t sh_mask);
 __global__ void begin_kernel(Counters* cnt);
 __global__ void claim_kernel(const int32_t* in_cell, const int32_t* in_solid, const int32_t* cut_cell,
-                             const int32_t* cut_solid, int32_t* Ct, const Counters* cnt, int64_t N);
+                             const int32_t* cut_solid, int32_t* Ct, Counters* cnt, int64_t N, uint32_t* cbits,
+                             uint32_t* sbits);
 __global__ void ft_kernel(const double* ftacc, double* ft, int S, const StepParams* step);
 __global__ void set_step_kernel(StepParams* p, double time, double dt, int nsub, double rho_V);
 int export_chunk_cells();
@@ -64,7 +70,7 @@ __global__ void u64_to_planes_kernel(const double* U64, int64_t N, float* U);
 __global__ void fields_to_f64_kernel(int64_t N, const float* As, const float* Fs, const float* Ts, const int32_t* Ct,
                                      double* out);
 __global__ void reset_kernel(const int32_t* in_cell, const int32_t* cut_cell, const Counters* cnt, int64_t N,
-                             float* As, float* Fs, float* Ts, int32_t* Ct);
+                             float* As, float* Fs, float* Ts, int32_t* Ct, const uint32_t* cbits);
 __global__ void fix_internal_kernel(MeshK m, const sdfibm_solid_state* st, const int32_t* in_cell,
                                     const int32_t* in_solid, const int32_t* Ct, float* U, const Counters* cnt);
 // evolve.cu
@@ -125,6 +131,10 @@ struct sdfibm_ctx {
     float* d_alpha = nullptr;  // solid fraction per bbox cell (same indexing as d_scratch)
     int64_t scratch_bytes = 0;
     uint32_t* d_gbitmaps = nullptr;
+    // chunked coupling: one bit per 8-cell chunk holding a claimed cell / a cell claimed twice (cleared as used)
+    uint32_t *d_cbits = nullptr, *d_sbits = nullptr;
+    uint32_t* d_shent = nullptr;  // list entries on shared cells, compacted by shared_scan_kernel
+    int64_t shent_cap = 0;
     int64_t gbitmap_words = 0;
     int connect_smem_bytes = 0;
     // flood-fill work: solids with small bbox bitmaps (one warp each) and the others (one CTA each)
@@ -477,6 +487,7 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         int64_t t = 1;
         while (t < 2 * want) t <<= 1;
         ctx->sh_mask = (int32_t)(t - 1);
+        ctx->shent_cap = 2 * t;  // a shared cell has two or more entries
     }
     ctx->chunk_tiles = CHUNK_TILES;
     if (ctx->opt.tile_cells > 0) {
@@ -570,6 +581,8 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         dalloc(&ctx->d_ftacc, 6 * (size_t)nsolids) || dalloc(&ctx->d_ft, 6 * (size_t)nsolids) ||
         dalloc(&ctx->d_sh_keys, (size_t)ctx->sh_mask + 1) || dalloc(&ctx->d_sh_vals, 5 * ((size_t)ctx->sh_mask + 1)) ||
         dalloc(&ctx->d_sh_used, (size_t)ctx->sh_mask + 1) || dalloc(&ctx->d_step, 2) ||
+        dalloc(&ctx->d_cbits, (size_t)(ctx->mesh.ncells + 255) / 256) ||
+        dalloc(&ctx->d_sbits, (size_t)(ctx->mesh.ncells + 255) / 256) || dalloc(&ctx->d_shent, (size_t)ctx->shent_cap) ||
         dalloc(&ctx->d_small, small_solids.size()) || dalloc(&ctx->d_big, big_solids.size()) ||
         dalloc(&ctx->d_rq, (size_t)ctx->rq_cap) || dalloc(&ctx->d_ovf, (size_t)ctx->ovf_cap) ||
         (cell_list &&
@@ -610,6 +623,8 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         cudaMemset(c->d_cnt, 0, sizeof(Counters)) != cudaSuccess ||
         cudaMemset(c->d_sh_keys, 0xff, sizeof(int32_t) * ((size_t)c->sh_mask + 1)) != cudaSuccess ||
         cudaMemset(c->d_sh_vals, 0, sizeof(double) * 5 * ((size_t)c->sh_mask + 1)) != cudaSuccess ||
+        cudaMemset(c->d_cbits, 0, sizeof(uint32_t) * ((size_t)(c->mesh.ncells + 255) / 256)) != cudaSuccess ||
+        cudaMemset(c->d_sbits, 0, sizeof(uint32_t) * ((size_t)(c->mesh.ncells + 255) / 256)) != cudaSuccess ||
         up(&c->d_cnt->list_cap, &c->cap, sizeof(int64_t))) {
         ctx->err = "upload failed";
         return bail(SDFIBM_ERR_CUDA);
@@ -626,7 +641,7 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
     ctx->classify_grid = std::max(1, occ) * ctx->num_sms;
     ctx->classify_occ = std::max(1, occ);
     occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, couple_kernel, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, couple_chunks_kernel, 256, 0);
     ctx->couple_grid = std::max(1, occ) * ctx->num_sms;
     ctx->couple_occ = std::max(1, occ);
     ctx->subsample_grid = 8 * ctx->num_sms;
@@ -677,6 +692,9 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
     }
     if (S > 0) {
         CK(cudaMemsetAsync(ctx->d_ftacc, 0, sizeof(double) * 6 * S, st));
+        // chunk marks of this call's claims (they stay after the call for sdfibm_cuda_apply_forcing)
+        CK(cudaMemsetAsync(ctx->d_cbits, 0, sizeof(uint32_t) * (size_t)((N + 255) / 256), st));
+        CK(cudaMemsetAsync(ctx->d_sbits, 0, sizeof(uint32_t) * (size_t)((N + 255) / 256), st));
         plan_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->mesh, ctx->d_sk, ctx->d_st, ctx->d_plan, S, ctx->d_cnt);
         mark(ctx, "plan_kernel");
         ClassifyArgs CA{};
@@ -722,9 +740,13 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
                 ctx->d_big);
         mark(ctx, "connect_kernel");
         claim_kernel<<<ctx->num_sms * 8, 256, 0, sb>>>(ctx->in_cell(), ctx->in_solid(), ctx->cut_cell(),
-                                                        ctx->cut_solid(), Ct, ctx->d_cnt, N);
+                                                        ctx->cut_solid(), Ct, ctx->d_cnt, N, ctx->d_cbits,
+                                                        ctx->d_sbits);
         mark(ctx, "claim_kernel");
-        launches += 4;
+        shared_scan_kernel<<<ctx->num_sms * 8, 256, 0, sb>>>(ctx->in_cell(), ctx->cut_cell(), Ct, ctx->d_cnt, N,
+                                                              ctx->d_sbits, ctx->d_shent, ctx->shent_cap);
+        mark(ctx, "shared_scan_kernel");
+        launches += 5;
         if (ctx->u64_dev) {  // interact_host64: U read at the coupling cells from the page-locked FP64 field
             gather_u64_kernel<<<ctx->num_sms * 8, 256, 0, sb>>>(ctx->in_cell(), ctx->cut_cell(), ctx->d_cnt, N,
                                                                  ctx->u64_dev, const_cast<float*>(U));
@@ -734,7 +756,7 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
         if (!dense) {
             const int p = ctx->cur ^ 1;
             reset_kernel<<<ctx->num_sms * 4, 256, 0, sb>>>(ctx->d_lists[p][0], ctx->d_lists[p][2], ctx->d_cnt, N, As,
-                                                            Fs, Ts, Ct);
+                                                            Fs, Ts, Ct, ctx->d_cbits);
             mark(ctx, "reset_kernel");
             ++launches;
         }
@@ -800,7 +822,7 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
     } else if (!dense) {
         const int p = ctx->cur ^ 1;
         reset_kernel<<<ctx->num_sms * 4, 256, 0, st>>>(ctx->d_lists[p][0], ctx->d_lists[p][2], ctx->d_cnt, N, As, Fs,
-                                                        Ts, Ct);
+                                                        Ts, Ct, ctx->d_cbits);
         ++launches;
     }
     if (ctx->u_wait) {  // U staged on a copy stream (interact_host)
@@ -822,15 +844,19 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             A.count_samples = nc * nc * (ctx->mesh.twod ? 1 : nc);
         }
         A.sh_keys = ctx->d_sh_keys; A.sh_vals = ctx->d_sh_vals; A.sh_used = ctx->d_sh_used; A.sh_mask = ctx->sh_mask;
-        couple_kernel<<<ctx->couple_grid, 256, 0, st>>>(A);
-        mark(ctx, "couple_kernel");
+        A.cbits = ctx->d_cbits; A.sbits = ctx->d_sbits; A.shent = ctx->d_shent; A.shent_cap = ctx->shent_cap;
+        // the compacted entries on shared cells (their FP64 sums), then every cell of the marked chunks
+        couple_shared_kernel<<<ctx->num_sms, 256, 0, st>>>(A);
+        mark(ctx, "couple_shared_kernel");
+        couple_chunks_kernel<<<ctx->couple_grid, 256, 0, st>>>(A);
+        mark(ctx, "couple_chunks_kernel");
         finalize_kernel<<<ctx->num_sms, 256, 0, st>>>(As, Ts, Fs, Ct, ctx->d_cnt, N, ctx->d_sh_keys, ctx->d_sh_vals,
                                                        ctx->d_sh_used, ctx->sh_mask);
         mark(ctx, "finalize_kernel");
         ft_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->d_ftacc, ctx->d_ft, S, ctx->d_step);
         ft_to_state_kernel<<<(S + 127) / 128, 128, 0, st>>>(ctx->d_ft, ctx->d_st, S);
         mark(ctx, "ft_kernel");
-        launches += 4;
+        launches += 5;
     }
     CK(cudaGetLastError());
     return SDFIBM_OK;
@@ -1258,6 +1284,23 @@ int sdfibm_cuda_fix_internal(sdfibm_ctx* ctx, const int32_t* Ct, float* U) {
     return SDFIBM_OK;
 }
 
+int sdfibm_cuda_apply_forcing(sdfibm_ctx* ctx, double dt, const float* As, const float* Fs, const float* Ts,
+                              float* U, float* T) {
+    if (!ctx) return SDFIBM_ERR_ARG;
+    if (!As || !Fs || !Ts || !U) return fail(ctx, SDFIBM_ERR_ARG, "null field pointer");
+    if (!ctx->interacted) return fail(ctx, SDFIBM_ERR_STATE, "apply_forcing needs a previous interact");
+    const uint32_t* marks = nullptr;
+    if (!ctx->poly) {
+        if (As != ctx->last_fields[1] || Fs != ctx->last_fields[2] || Ts != ctx->last_fields[3])
+            return fail(ctx, SDFIBM_ERR_STATE, "apply_forcing takes the fields the last interact wrote");
+        marks = ctx->d_cbits;
+    }
+    const int64_t N = ctx->poly ? ctx->poly->k.ncells : ctx->mesh.ncells;
+    apply_forcing_kernel<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(N, marks, dt, As, Fs, Ts, U, T);
+    CK(cudaGetLastError());
+    return SDFIBM_OK;
+}
+
 int sdfibm_cuda_get_solids(sdfibm_ctx* ctx, sdfibm_solid_state* out, int32_t n) {
     if (!ctx) return SDFIBM_ERR_ARG;
     if (!out || n != ctx->S) return fail(ctx, SDFIBM_ERR_ARG, "state array size must equal the solid count");
@@ -1460,7 +1503,7 @@ int sdfibm_cuda_autotune(sdfibm_ctx* ctx, double dt, const float* U, float* As, 
     };
     const Knob knobs[5] = {{"classify_kernel", &cls_cand, &Tuning::classify_grid},
                            {"subsample_cells_kernel", &sub_cand, &Tuning::subsample_grid},
-                           {"couple_kernel", &cpl_cand, &Tuning::couple_grid},
+                           {"couple_chunks_kernel", &cpl_cand, &Tuning::couple_grid},
                            {"mlp_infer_kernel", &mlp_cand, &Tuning::mlp_grid},
                            {"refgeo_cells_kernel", &rg_cand, &Tuning::refgeo_grid}};
     float bt[5] = {1e30f, 1e30f, 1e30f, 1e30f, 1e30f};
@@ -1567,6 +1610,9 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
     if (ctx->d_rq) cudaFree(ctx->d_rq);
     if (ctx->d_ovf) cudaFree(ctx->d_ovf);
     if (ctx->d_dirty) cudaFree(ctx->d_dirty);
+    if (ctx->d_cbits) cudaFree(ctx->d_cbits);
+    if (ctx->d_sbits) cudaFree(ctx->d_sbits);
+    if (ctx->d_shent) cudaFree(ctx->d_shent);
     if (ctx->d_f64) cudaFree(ctx->d_f64);
     if (ctx->poly) {
         for (void* p : ctx->poly->allocs)

@@ -196,17 +196,28 @@ __global__ void plan_kernel(MeshK m, const SolidK* __restrict__ sk, const sdfibm
 // below CT_KEY_BASE -- zero, or the decoded Ct a previous call left -- is an unclaimed cell.
 // One atomicMax claims the cell (any previous value is below every claim word); seeing another claim of this call
 // in its return value, the claimer raises the word to the larger claim with CT_SHARED set.
-__device__ inline void claim_cell(int32_t* Ct, int32_t cell, int32_t s, int type) {
+__device__ inline bool claim_cell(int32_t* Ct, int32_t cell, int32_t s, int type) {
     uint32_t* C = reinterpret_cast<uint32_t*>(Ct) + cell;
     const uint32_t key = CT_KEY_BASE | ((uint32_t)s << 2) | (uint32_t)type;
     const uint32_t old = atomicMax(C, key);
-    if (old >= CT_KEY_BASE) atomicMax(C, max(key, old & ~CT_SHARED) | CT_SHARED);
+    if (old < CT_KEY_BASE) return false;
+    atomicMax(C, max(key, old & ~CT_SHARED) | CT_SHARED);
+    return true;
 }
 
-// claim pass over this call's lists
+// set bit (c >> 3) of a chunk bitmap (one bit per 8 consecutive cells)
+__device__ inline void mark_chunk(uint32_t* bits, int64_t c) {
+    uint32_t* w = bits + (c >> 8);
+    const uint32_t b = 1u << ((c >> 3) & 31);
+    if (!(*w & b)) atomicOr(w, b);
+}
+
+// claim pass over this call's lists; marks the chunks of the claimed cells in cbits and, for a cell claimed more than
+// once, in sbits (every claimer after the first sees an earlier claim, so each shared cell's chunk is marked)
 __global__ void claim_kernel(const int32_t* __restrict__ in_cell, const int32_t* __restrict__ in_solid,
                              const int32_t* __restrict__ cut_cell, const int32_t* __restrict__ cut_solid,
-                             int32_t* __restrict__ Ct, const Counters* cnt, int64_t N) {
+                             int32_t* __restrict__ Ct, Counters* cnt, int64_t N, uint32_t* __restrict__ cbits,
+                             uint32_t* __restrict__ sbits) {
     const int n_in = clamp_len(cnt->n_inside, cnt->list_cap), n_cut = clamp_len(cnt->n_cut, cnt->list_cap);
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)n_in + n_cut;
          e += (int64_t)gridDim.x * blockDim.x) {
@@ -215,7 +226,14 @@ __global__ void claim_kernel(const int32_t* __restrict__ in_cell, const int32_t*
         const int32_t c = cut ? cut_cell[ee] : in_cell[ee];
         const int32_t sw = cut ? cut_solid[ee] : in_solid[ee];
         if (c < 0 || c >= N) continue;
-        claim_cell(Ct, c, sw & LIST_SOLID_MASK, list_type(sw));
+        const bool shared = claim_cell(Ct, c, sw & LIST_SOLID_MASK, list_type(sw));
+        if (cbits) {
+            mark_chunk(cbits, c);
+            if (shared) {
+                mark_chunk(sbits, c);
+                atomicAdd(&cnt->shared_marks, 1);
+            }
+        }
     }
 }
 
@@ -684,118 +702,258 @@ __device__ __forceinline__ float ff_u_minus_us(float U, float u0h, float u0l, fl
     return __fadd_rn(d, __fsub_rn(g, lo));
 }
 
-// Per-cell forcing (pcHydrodynamicInteraction, solidcloud.cpp:384-390) and the force/torque sums (:411-421).
-// ftacc receives sum f and sum (C - x) x f; ft_kernel applies rho_f * V / dt once per solid.
-__global__ void __launch_bounds__(CPL_THREADS) couple_kernel(CoupleArgs A) {
-    __shared__ int s_item;
+// Per-cell forcing of solid s on cell c with fluid velocity U (pcHydrodynamicInteraction, solidcloud.cpp:384-390):
+// alpha, the FP32 Fs and the cell's contributions to the force/torque sums (:411-421), FP64 in f6 (exact mode) or
+// FP32 in g6.
+__device__ __forceinline__ float cell_forcing(const CoupleArgs& A, int64_t c, int s, int type, float dtINV32,
+                                              double dtINV, float fs[3], double f6[8], float g6[8], float Ux,
+                                              float Uy, float Uz) {
     const MeshK& m = A.m;
-    const int64_t N = m.ncells;
-    const int tid = threadIdx.x, lane = tid & 31;
-    const int n_in = clamp_len(A.cnt->n_inside, A.cnt->list_cap), n_cut = clamp_len(A.cnt->n_cut, A.cnt->list_cap);
-    const int in_chunks = (n_in + CPL_THREADS - 1) / CPL_THREADS;
-    const int cut_chunks = (n_cut + CPL_THREADS - 1) / CPL_THREADS;
+    int i, j, k;
+    cell_ijk(m, c, i, j, k);
+    float alpha = 1.f;
+    if (type != 1) {
+        // computed by the fraction pass for every cut candidate of the solid's bbox
+        const SolidK& ks = A.sk[s];
+        const int32_t* lo = A.plan[s].lo;
+        const int64_t li = (i - lo[0]) + (int64_t)ks.ext[0] * ((j - lo[1]) + (int64_t)ks.ext[1] * (k - lo[2]));
+        alpha = A.alpha[ks.scratch_off + li];
+        // a SUBSAMPLE count whose undecided points were rechecked on full warps
+        if (alpha < 0.f) alpha = __fdiv_rn(-alpha - 1.f, (float)A.count_samples);
+    }
+    if (A.exact_forcing) {
+        // the reference's FP64 sequence
+        const sdfibm_solid_state& st = A.st[s];
+        const D3 x = state_pos(st);
+        const D3 cc = mesh_C(m, i, j, k);
+        const D3 vel{st.vel[0], st.vel[1], st.vel[2]}, om{st.omega[0], st.omega[1], st.omega[2]};
+        const D3 uf{(double)Ux, (double)Uy, (double)Uz};
+        const D3 us = vel + cross(om, cc - x);
+        const D3 f_ = (double)alpha * (uf - us);
+        const D3 t_ = cross(cc - x, f_);
+        f6[0] = f_.x; f6[1] = f_.y; f6[2] = f_.z; f6[3] = t_.x; f6[4] = t_.y; f6[5] = t_.z;
+        fs[0] = (float)(f_.x * dtINV); fs[1] = (float)(f_.y * dtINV); fs[2] = (float)(f_.z * dtINV);
+    } else {
+        // U - us in two-float arithmetic (the difference can cancel; about 2^-46 of the magnitudes, against 2^-24 of
+        // the difference for the FP32 rounding that follows), FP32 after it.  The cell offsets from the seed are
+        // exact small integers.
+        const SolidPlan& pl = A.plan[s];
+        const float di = (float)(i - pl.seed_ijk[0]), dj = (float)(j - pl.seed_ijk[1]), dk = (float)(k - pl.seed_ijk[2]);
+        const float fx = alpha * ff_u_minus_us(Ux, pl.us_hi[0], pl.us_lo[0], dj, pl.ds_hi[0], pl.ds_lo[0], dk,
+                                               pl.ds_hi[1], pl.ds_lo[1]);
+        const float fy = alpha * ff_u_minus_us(Uy, pl.us_hi[1], pl.us_lo[1], di, pl.ds_hi[2], pl.ds_lo[2], dk,
+                                               pl.ds_hi[3], pl.ds_lo[3]);
+        const float fz = alpha * ff_u_minus_us(Uz, pl.us_hi[2], pl.us_lo[2], di, pl.ds_hi[4], pl.ds_lo[4], dj,
+                                               pl.ds_hi[5], pl.ds_lo[5]);
+        const float dx = __fmaf_rn(di, m.h32[0], pl.cb32[0]), dy = __fmaf_rn(dj, m.h32[1], pl.cb32[1]),
+                    dz = __fmaf_rn(dk, m.h32[2], pl.cb32[2]);
+        g6[0] = fx; g6[1] = fy; g6[2] = fz;
+        g6[3] = dy * fz - dz * fy; g6[4] = dz * fx - dx * fz; g6[5] = dx * fy - dy * fx;
+        fs[0] = fx * dtINV32; fs[1] = fy * dtINV32; fs[2] = fz * dtINV32;
+    }
+    return alpha;
+}
+
+// The cell's FP64 sums in the shared table (As, Ts, Fs of every solid on a cell several solids touch).
+__device__ __forceinline__ void add_shared(const CoupleArgs& A, int64_t c, float alpha, const float fs[3]) {
+    const int slot = shared_slot(A, (int32_t)c);
+    if (slot >= 0) {
+        double* v = A.sh_vals + 5 * (int64_t)slot;
+        atomicAdd(v + 0, (double)alpha);
+        atomicAdd(v + 1, (double)alpha);
+        atomicAdd(v + 2, (double)fs[0]);
+        atomicAdd(v + 3, (double)fs[1]);
+        atomicAdd(v + 4, (double)fs[2]);
+    }
+}
+
+// Shared pass of the coupling, first half (on the side stream after the claims, beside the fraction kernels): the list
+// entries on cells that several solids claimed, compacted into shent (entry index into the in list then the cut list).
+// Only the chunks marked in sbits are looked at; the kernel returns at once when no cell was claimed twice.
+__global__ void shared_scan_kernel(const int32_t* __restrict__ in_cell, const int32_t* __restrict__ cut_cell,
+                                   const int32_t* __restrict__ Ct, Counters* cnt, int64_t N,
+                                   const uint32_t* __restrict__ sbits, uint32_t* __restrict__ shent,
+                                   int64_t shent_cap) {
+    if (cnt->shared_marks == 0) return;
+    const int64_t n_in = clamp_len(cnt->n_inside, cnt->list_cap), n_cut = clamp_len(cnt->n_cut, cnt->list_cap);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_in + n_cut;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t c = e < n_in ? in_cell[e] : cut_cell[e - n_in];
+        if (c < 0 || c >= N) continue;
+        if (!((sbits[c >> 8] >> ((c >> 3) & 31)) & 1u)) continue;  // no cell of this chunk is shared
+        if (!(reinterpret_cast<const uint32_t*>(Ct)[c] & CT_SHARED)) continue;
+        const int32_t slot = atomicAdd(&cnt->n_shent, 1);
+        if (slot < shent_cap) shent[slot] = (uint32_t)e;
+        else set_error(cnt, DERR_SHARED_TABLE);
+    }
+}
+
+// Shared pass, second half (after the fraction kernels): every compacted entry adds its solid's As / Ts / Fs to the
+// cell's FP64 sums in the shared table (finalize_kernel writes them) and its force/torque contribution to the solid's
+// sums.
+__global__ void __launch_bounds__(CPL_THREADS) couple_shared_kernel(CoupleArgs A) {
+    const int64_t N = A.m.ncells;
+    const int64_t n = min((int64_t)A.cnt->n_shent, A.shent_cap);
+    if (n == 0) return;
+    const int64_t n_in = clamp_len(A.cnt->n_inside, A.cnt->list_cap);
     const double dtINV = A.step->dtINV;
     const float dtINV32 = (float)dtINV;
-    for (;;) {
-        if (tid == 0) s_item = atomicAdd(&A.cnt->couple_next, 1);
-        __syncthreads();
-        const int item = s_item;
-        __syncthreads();
-        if (item >= in_chunks + cut_chunks) break;
-        const bool is_cut = item >= in_chunks;
-        const int e = (is_cut ? item - in_chunks : item) * CPL_THREADS + tid;
-        const bool valid = e < (is_cut ? n_cut : n_in);
-        int s = -1;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = A.shent[q];
+        const bool is_cut = e >= n_in;
+        const int32_t c = is_cut ? A.cut_cell[e - n_in] : A.in_cell[e];
+        const int32_t sw = is_cut ? A.cut_solid[e - n_in] : A.in_solid[e];
+        const int s = sw & LIST_SOLID_MASK;
         double f6[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         float g6[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        if (valid) {
-            const int32_t c32 = is_cut ? A.cut_cell[e] : A.in_cell[e];
-            const int32_t sw = is_cut ? A.cut_solid[e] : A.in_solid[e];
-            s = sw & LIST_SOLID_MASK;
-            const int type = list_type(sw);
-            const int64_t c = (c32 >= 0 && c32 < N) ? c32 : 0;
-            if (c32 != c) set_error(A.cnt, DERR_CAPACITY);
-            int i, j, k;
-            cell_ijk(m, c, i, j, k);
-            const sdfibm_solid_state& st = A.st[s];
-            float alpha = 1.f;
-            if (is_cut) {
-                // computed by the classify pass for every cut candidate of the solid's bbox
-                const SolidK& ks = A.sk[s];
-                const int32_t* lo = A.plan[s].lo;
-                const int64_t li = (i - lo[0]) + (int64_t)ks.ext[0] * ((j - lo[1]) + (int64_t)ks.ext[1] * (k - lo[2]));
-                alpha = A.alpha[ks.scratch_off + li];
-                // a SUBSAMPLE count whose undecided points were rechecked on full warps
-                if (alpha < 0.f) alpha = __fdiv_rn(-alpha - 1.f, (float)A.count_samples);
-            }
-            const float Ux = A.U[c], Uy = A.U[N + c], Uz = A.U[2 * N + c];
-            float fsx, fsy, fsz;
-            if (A.exact_forcing) {
-                // the reference's FP64 sequence
-                const D3 x = state_pos(st);
-                const D3 cc = mesh_C(m, i, j, k);
-                const D3 vel{st.vel[0], st.vel[1], st.vel[2]}, om{st.omega[0], st.omega[1], st.omega[2]};
-                const D3 uf{(double)Ux, (double)Uy, (double)Uz};
-                const D3 us = vel + cross(om, cc - x);
-                const D3 f_ = (double)alpha * (uf - us);
-                const D3 t_ = cross(cc - x, f_);
-                f6[0] = f_.x; f6[1] = f_.y; f6[2] = f_.z; f6[3] = t_.x; f6[4] = t_.y; f6[5] = t_.z;
-                fsx = (float)(f_.x * dtINV); fsy = (float)(f_.y * dtINV); fsz = (float)(f_.z * dtINV);
-            } else {
-                // U - us in two-float arithmetic (the difference can cancel; about 2^-46 of the magnitudes, against
-                // 2^-24 of the difference for the FP32 rounding that follows), FP32 after it.  The cell offsets from
-                // the seed are exact small integers.
-                const SolidPlan& pl = A.plan[s];
-                const float di = (float)(i - pl.seed_ijk[0]), dj = (float)(j - pl.seed_ijk[1]),
-                            dk = (float)(k - pl.seed_ijk[2]);
-                const float fx = alpha * ff_u_minus_us(Ux, pl.us_hi[0], pl.us_lo[0], dj, pl.ds_hi[0], pl.ds_lo[0], dk,
-                                                       pl.ds_hi[1], pl.ds_lo[1]);
-                const float fy = alpha * ff_u_minus_us(Uy, pl.us_hi[1], pl.us_lo[1], di, pl.ds_hi[2], pl.ds_lo[2], dk,
-                                                       pl.ds_hi[3], pl.ds_lo[3]);
-                const float fz = alpha * ff_u_minus_us(Uz, pl.us_hi[2], pl.us_lo[2], di, pl.ds_hi[4], pl.ds_lo[4], dj,
-                                                       pl.ds_hi[5], pl.ds_lo[5]);
-                const float dx = __fmaf_rn(di, m.h32[0], pl.cb32[0]), dy = __fmaf_rn(dj, m.h32[1], pl.cb32[1]),
-                            dz = __fmaf_rn(dk, m.h32[2], pl.cb32[2]);
-                g6[0] = fx; g6[1] = fy; g6[2] = fz;
-                g6[3] = dy * fz - dz * fy; g6[4] = dz * fx - dx * fz; g6[5] = dx * fy - dy * fx;
-                fsx = fx * dtINV32; fsy = fy * dtINV32; fsz = fz * dtINV32;
-            }
-            const uint32_t claim = reinterpret_cast<const uint32_t*>(A.Ct)[c];
-            if (!(claim & CT_SHARED)) {
-                // the only solid on this cell: the final values (As += alpha on a zeroed field, checkAlpha, Ct)
-                A.As[c] = fminf(alpha, 1.0f);
-                A.Ts[c] = alpha;
-                A.Fs[c] = fsx;
-                A.Fs[N + c] = fsy;
-                A.Fs[2 * N + c] = fsz;
-                A.Ct[c] = type == 1 ? s + 4 : type;
-            } else {
-                const int slot = shared_slot(A, (int32_t)c);
-                if (slot >= 0) {
-                    double* v = A.sh_vals + 5 * (int64_t)slot;
-                    atomicAdd(v + 0, (double)alpha);
-                    atomicAdd(v + 1, (double)alpha);
-                    atomicAdd(v + 2, (double)fsx);
-                    atomicAdd(v + 3, (double)fsy);
-                    atomicAdd(v + 4, (double)fsz);
+        float fs[3];
+        const float alpha = cell_forcing(A, c, s, list_type(sw), dtINV32, dtINV, fs, f6, g6, A.U[c], A.U[N + c],
+                                         A.U[2 * N + c]);
+        add_shared(A, c, alpha, fs);
+        for (int r = 0; r < 6; ++r) atomicAdd(A.ftacc + 6 * s + r, A.exact_forcing ? f6[r] : (double)g6[r]);
+    }
+}
+
+// Chunked coupling.  The claim pass marks in cbits every chunk of 8 consecutive cells that holds a claimed cell (and
+// in sbits the chunks of cells claimed more than once).  This kernel runs over the marked chunks in memory order, a
+// warp per bitmap word (256 cells), four chunks at a time with 8 lanes each, and writes the four fields of every
+// cell of a marked chunk: zero for an unclaimed cell (a cell that no solid touches, or one the previous call touched:
+// the sparse reset inside these chunks), zero As / Ts / Fs and the claim word kept in Ct for a shared cell
+// (finalize_kernel writes its sums and decodes its Ct), and for a cell claimed once the forcing of its solid.  The
+// cells claimed once are queued per warp in shared memory and computed 32 at a time on full warps; their values
+// land in the same sectors a few instructions after the zeros, so every 32-byte sector of a field is written whole
+// while L2 holds it and DRAM takes no read-modify-write, and U / Ct sectors are read once whatever the lists' order.
+// The force/torque sums are reduced per solid over the lanes of the warp (segmented by solid) before one FP64
+// atomic per (solid, component).  The marks stay until the next interact clears them (sdfibm_cuda_apply_forcing
+// visits the same chunks).
+constexpr int CPL_WARPS = CPL_THREADS / 32;
+
+// forcing of the first `count` queued cells (lane l takes entry l), written to the fields, F/T summed per solid
+__device__ __forceinline__ void couple_queued(const CoupleArgs& A, const int32_t* qc, const uint32_t* qk, int count,
+                                              float dtINV32, double dtINV) {
+    const int lane = threadIdx.x & 31;
+    const int64_t N = A.m.ncells;
+    int s = -1;
+    double f6[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    float g6[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (lane < count) {
+        const int64_t c = qc[lane];
+        const uint32_t key = qk[lane] - CT_KEY_BASE;
+        s = (int)(key >> 2);
+        const int type = (int)(key & 3u);
+        float fs[3];
+        const float alpha = cell_forcing(A, c, s, type, dtINV32, dtINV, fs, f6, g6, A.U[c], A.U[N + c],
+                                         A.U[2 * N + c]);
+        A.As[c] = fminf(alpha, 1.0f);
+        A.Ts[c] = alpha;
+        A.Fs[c] = fs[0];
+        A.Fs[N + c] = fs[1];
+        A.Fs[2 * N + c] = fs[2];
+        A.Ct[c] = type == 1 ? s + 4 : type;
+    }
+    uint32_t pend = __ballot_sync(0xffffffffu, s >= 0);
+    while (pend) {
+        const int sl = __shfl_sync(0xffffffffu, s, __ffs(pend) - 1);
+        const bool mine = s == sl;
+        pend &= ~__ballot_sync(0xffffffffu, mine);
+        double v;
+        if (A.exact_forcing) {
+            double t[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) t[r] = mine ? f6[r] : 0.0;
+            v = warp_total4(reduce_scatter8(t, lane));
+        } else {
+            float t[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) t[r] = mine ? g6[r] : 0.f;
+            v = warp_total4((double)reduce_scatter8(t, lane));
+        }
+        const int slot = lane >> 2;
+        if ((lane & 3) == 0 && slot < 6) atomicAdd(A.ftacc + 6 * sl + slot, v);
+    }
+}
+
+__global__ void __launch_bounds__(CPL_THREADS) couple_chunks_kernel(CoupleArgs A) {
+    __shared__ int32_t s_qc[CPL_WARPS][64];   // per warp: queued cells claimed once, and their claim words
+    __shared__ uint32_t s_qk[CPL_WARPS][64];
+    const int64_t N = A.m.ncells;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, grp = lane >> 3, sub = lane & 7;
+    int32_t* qc = s_qc[wib];
+    uint32_t* qk = s_qk[wib];
+    const int64_t words = (N + 255) >> 8;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const double dtINV = A.step->dtINV;
+    const float dtINV32 = (float)dtINV;
+    const uint32_t* C = reinterpret_cast<const uint32_t*>(A.Ct);
+    int nq = 0;  // warp-uniform
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += nw) {
+        uint32_t rem = A.cbits[w];
+        while (rem) {  // warp-uniform: four marked chunks per pass
+            uint32_t x = rem;
+            for (int q = 0; q < grp; ++q) x &= x - 1;  // this group's chunk: the grp-th lowest mark left
+#pragma unroll
+            for (int q = 0; q < 4; ++q) rem &= rem - 1;
+            const int64_t c = (((w << 5) + (__ffs(x) - 1)) << 3) + sub;
+            bool single = false;
+            uint32_t claim = 0;
+            if (x != 0 && c < N) {
+                claim = C[c];
+                single = claim >= CT_KEY_BASE && !(claim & CT_SHARED);
+                if (!single) {
+                    A.As[c] = 0.f;
+                    A.Ts[c] = 0.f;
+                    A.Fs[c] = 0.f;
+                    A.Fs[N + c] = 0.f;
+                    A.Fs[2 * N + c] = 0.f;
+                    A.Ct[c] = (claim & CT_SHARED) ? (int32_t)claim : 0;
                 }
             }
-        }
-        // force/torque: a reduce-scatter over the warp and one FP64 atomic per (solid, component) when the warp
-        // serves a single solid
-        const int s0 = __shfl_sync(0xffffffffu, s, 0);
-        const bool uniform = __all_sync(0xffffffffu, s == s0 || s < 0);
-        if (uniform) {
-            double v;
-            if (A.exact_forcing) {
-                v = warp_total4(reduce_scatter8(f6, lane));
-            } else {
-                v = warp_total4((double)reduce_scatter8(g6, lane));
+            const uint32_t m = __ballot_sync(0xffffffffu, single);
+            if (single) {
+                const int pos = nq + __popc(m & ((1u << lane) - 1u));
+                qc[pos] = (int32_t)c;
+                qk[pos] = claim;
             }
-            const int slot = lane >> 2;
-            if ((lane & 3) == 0 && slot < 6 && s0 >= 0) atomicAdd(A.ftacc + 6 * s0 + slot, v);
-        } else if (s >= 0) {
-            for (int r = 0; r < 6; ++r) atomicAdd(A.ftacc + 6 * s + r, A.exact_forcing ? f6[r] : (double)g6[r]);
+            nq += __popc(m);
+            __syncwarp();
+            if (nq >= 32) {
+                couple_queued(A, qc, qk, 32, dtINV32, dtINV);
+                __syncwarp();
+                if (lane < nq - 32) {
+                    qc[lane] = qc[32 + lane];
+                    qk[lane] = qk[32 + lane];
+                }
+                nq -= 32;
+                __syncwarp();
+            }
+        }
+    }
+    if (nq > 0) couple_queued(A, qc, qk, nq, dtINV32, dtINV);
+}
+
+// Forcing applied to a GPU-resident fluid (main.cpp:70-77, its cell fields): U = U - Fs dt and T = (1 - As) T + Ts,
+// in FP64 and rounded once to the FP32 fields, over the chunks the last interact marked in cbits.  Every other cell
+// has As = Fs = Ts = 0 there and keeps its values, as in the dense update.  With cbits == nullptr (unstructured
+// meshes) every cell is visited.  A warp per bitmap word, each store instruction covering 32 consecutive cells.
+__global__ void apply_forcing_kernel(int64_t N, const uint32_t* __restrict__ cbits, double dt,
+                                     const float* __restrict__ As, const float* __restrict__ Fs,
+                                     const float* __restrict__ Ts, float* __restrict__ U, float* __restrict__ T) {
+    const int lane = threadIdx.x & 31;
+    const int64_t words = (N + 255) >> 8;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += nw) {
+        const uint32_t word = cbits ? cbits[w] : 0xffffffffu;
+        if (!word) continue;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int idx = 32 * t + lane;
+            const int64_t c = (w << 8) + idx;
+            if (((word >> (idx >> 3)) & 1u) && c < N) {
+                // separate roundings, as the solver's own field operations (no contraction into FMAs)
+                for (int a = 0; a < 3; ++a)
+                    U[a * N + c] = (float)__dsub_rn((double)U[a * N + c], __dmul_rn((double)Fs[a * N + c], dt));
+                if (T) T[c] = (float)__dadd_rn(__dmul_rn(__dsub_rn(1.0, (double)As[c]), (double)T[c]), (double)Ts[c]);
+            }
         }
     }
 }
@@ -830,9 +988,9 @@ __global__ void begin_kernel(Counters* cnt) {
     cnt->prev_n_inside = cnt->n_inside;
     cnt->prev_n_cut = cnt->n_cut;
     cnt->classify_next = 0; cnt->couple_next = 0; cnt->finalize_next = 0;
-    cnt->n_inside = 0; cnt->n_cut = 0; cnt->n_shared = 0;
+    cnt->n_inside = 0; cnt->n_cut = 0; cnt->n_shared = 0; cnt->shared_marks = 0;
     cnt->exact_rechecks = 0; cnt->bbox_cells = 0;
-    cnt->n_feat = 0; cnt->n_fb = 0; cnt->n_recheck = 0; cnt->n_ovf = 0;
+    cnt->n_feat = 0; cnt->n_fb = 0; cnt->n_recheck = 0; cnt->n_ovf = 0; cnt->n_shent = 0;
 }
 
 // F = rho_f * V / dt * sum f, T = rho_f * V / dt * sum (C - x) x f  (solidcloud.cpp:411-421)
@@ -851,16 +1009,19 @@ __global__ void set_step_kernel(StepParams* p, double time, double dt, int nsub,
     p->ft_scale = rho_V / dt;
 }
 
-// sparse reset: the cells the previous call touched and this call does not (after this call's claims, before the
-// couple pass writes the claimed cells) go back to zero -- the sparse form of solidcloud.cpp:438-441
+// sparse reset: the cells the previous call touched and this call does not (after this call's claims) go back to
+// zero -- the sparse form of solidcloud.cpp:438-441.  Cells in the chunks marked in cbits are left to
+// couple_chunks_kernel, which writes every cell of those chunks.
 __global__ void reset_kernel(const int32_t* __restrict__ prev_in_cell, const int32_t* __restrict__ prev_cut_cell,
-                             const Counters* cnt, int64_t N, float* As, float* Fs, float* Ts, int32_t* Ct) {
+                             const Counters* cnt, int64_t N, float* As, float* Fs, float* Ts, int32_t* Ct,
+                             const uint32_t* __restrict__ cbits) {
     const int n_in = clamp_len(cnt->prev_n_inside, cnt->list_cap), n_cut = clamp_len(cnt->prev_n_cut, cnt->list_cap);
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)n_in + n_cut;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t c = e < n_in ? prev_in_cell[e] : prev_cut_cell[e - n_in];
         if (c < 0 || c >= N) continue;
-        if (reinterpret_cast<const uint32_t*>(Ct)[c] >= CT_KEY_BASE) continue;  // claimed now: rewritten below
+        if ((cbits[c >> 8] >> ((c >> 3) & 31)) & 1u) continue;  // written by the chunked coupling
+        if (reinterpret_cast<const uint32_t*>(Ct)[c] >= CT_KEY_BASE) continue;
         As[c] = 0.f; Ts[c] = 0.f; Ct[c] = 0;
         Fs[c] = 0.f; Fs[N + c] = 0.f; Fs[2 * N + c] = 0.f;
     }

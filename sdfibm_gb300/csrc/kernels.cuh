@@ -106,7 +106,7 @@ struct Counters {
     int32_t prev_n_inside;    // list lengths of the previous call (its lists stay for the sparse reset)
     int32_t prev_n_cut;
     int32_t error;            // first error code seen on the device
-    int32_t pad0;
+    int32_t shared_marks;     // claims that found the cell already claimed this call
     unsigned long long exact_rechecks;  // FP32-undecided points re-evaluated in FP64
     unsigned long long bbox_cells;
     int32_t launches;
@@ -116,6 +116,8 @@ struct Counters {
     int32_t n_fb;             // LEARNED: of those, cells outside the model's band (SUBSAMPLE fallback)
     int32_t n_recheck;        // SUBSAMPLE points left to recheck_kernel this call
     int32_t n_ovf;            // LEARNED: fallback cells whose points overflowed the recheck list (recount_kernel)
+    int32_t n_shent;          // list entries on cells several solids claimed (shared_scan_kernel)
+    int32_t pad1;
 };
 
 // list lengths clamped to the capacity (a capacity error leaves the counters above what was written)
@@ -166,6 +168,11 @@ struct CoupleArgs {
     double* sh_vals;   // [slot][5]: As, Ts, Fs.x, Fs.y, Fs.z
     int32_t* sh_used;  // slots filled this call
     int32_t sh_mask;
+    // chunked coupling: marks of the 8-cell chunks with claimed cells / with shared cells (one bit per chunk)
+    uint32_t* cbits;
+    uint32_t* sbits;
+    const uint32_t* shent;  // list entries on shared cells (shared_scan_kernel)
+    int64_t shent_cap;
 };
 
 // Ct during a call holds claim words: CT_KEY_BASE | (solid << 2 | type), with CT_SHARED set once a second solid

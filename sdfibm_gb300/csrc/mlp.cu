@@ -68,33 +68,40 @@ __device__ void stage_weights(const float* P, uint8_t* sW1, uint8_t* sW2, uint8_
     if (threadIdx.x == 0) *sb3 = P[MLP_OFF_B3];
 }
 
-// A1 row: hi of the 11 features (+5 zeros) in K 0..15, lo in K 16..31
+// BF16 hi + lo halves of two values, packed as the K-major operands hold them (a in the low 16 bits): one
+// two-value round-to-nearest conversion per half, the same bits as two single conversions.
+__device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t& lo) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(a - __uint_as_float(hi << 16), b - __uint_as_float(hi & 0xffff0000u));
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+
+// A1 row: hi of the 16 inputs in K 0..15, lo in K 16..31
+static_assert(MLP_IN == 16, "the layer-1 operand holds 16 inputs");
 __device__ __forceinline__ void store_a1(uint8_t* sA1, int row, const float* x) {
-    uint32_t hi[16], lo[16];
-#pragma unroll
-    for (int k = 0; k < 16; ++k) {
-        const float v = k < MLP_IN ? x[k] : 0.f;
-        hi[k] = bf16_bits(v);
-        lo[k] = bf16_bits(v - bf16_value(hi[k]));
-    }
-    store_row8(sA1, row, 0, 32, hi);
-    store_row8(sA1, row, 8, 32, hi + 8);
-    store_row8(sA1, row, 16, 32, lo);
-    store_row8(sA1, row, 24, 32, lo + 8);
+    uint4 h0, h1, l0, l1;
+    split2(x[0], x[1], h0.x, l0.x); split2(x[2], x[3], h0.y, l0.y);
+    split2(x[4], x[5], h0.z, l0.z); split2(x[6], x[7], h0.w, l0.w);
+    split2(x[8], x[9], h1.x, l1.x); split2(x[10], x[11], h1.y, l1.y);
+    split2(x[12], x[13], h1.z, l1.z); split2(x[14], x[15], h1.w, l1.w);
+    *reinterpret_cast<uint4*>(sA1 + tc::kmajor_offset(row, 0, 32)) = h0;
+    *reinterpret_cast<uint4*>(sA1 + tc::kmajor_offset(row, 8, 32)) = h1;
+    *reinterpret_cast<uint4*>(sA1 + tc::kmajor_offset(row, 16, 32)) = l0;
+    *reinterpret_cast<uint4*>(sA1 + tc::kmajor_offset(row, 24, 32)) = l1;
 }
 
 // A2 row: hi of h1 in K 0..63, lo in K 64..127
 __device__ __forceinline__ void store_a2(uint8_t* sA2, int row, const float* h) {
 #pragma unroll
     for (int g = 0; g < 8; ++g) {
-        uint32_t hi[8], lo[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            hi[i] = bf16_bits(h[8 * g + i]);
-            lo[i] = bf16_bits(h[8 * g + i] - bf16_value(hi[i]));
-        }
-        store_row8(sA2, row, 8 * g, 128, hi);
-        store_row8(sA2, row, 64 + 8 * g, 128, lo);
+        uint4 hw, lw;
+        split2(h[8 * g], h[8 * g + 1], hw.x, lw.x);
+        split2(h[8 * g + 2], h[8 * g + 3], hw.y, lw.y);
+        split2(h[8 * g + 4], h[8 * g + 5], hw.z, lw.z);
+        split2(h[8 * g + 6], h[8 * g + 7], hw.w, lw.w);
+        *reinterpret_cast<uint4*>(sA2 + tc::kmajor_offset(row, 8 * g, 128)) = hw;
+        *reinterpret_cast<uint4*>(sA2 + tc::kmajor_offset(row, 64 + 8 * g, 128)) = lw;
     }
 }
 
@@ -588,6 +595,7 @@ __global__ void __launch_bounds__(128) mlp_dataset_kernel(DataArgs A) {
     s_fr[threadIdx.x][11] = (float)o.z;
     __syncwarp();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const StencilLane SL = stencil_lane();
     for (int t = 0; t < 32; ++t) {
         const int src = (w << 5) + t;
         const int64_t ci = (int64_t)blockIdx.x * blockDim.x + src;
@@ -595,8 +603,8 @@ __global__ void __launch_bounds__(128) mlp_dataset_kernel(DataArgs A) {
         float M[9];
 #pragma unroll
         for (int r = 0; r < 9; ++r) M[r] = s_fr[src][r];
-        const StencilOut so = cell_stencil(s_sh[src], M, s_fr[src][9], s_fr[src][10], s_fr[src][11], 0.25f, 0.25f,
-                                           0.25f, 1.f, s_phi[w], s_list[w]);
+        const StencilOut so = cell_stencil(s_sh[src], SL, M, s_fr[src][9], s_fr[src][10], s_fr[src][11], 0.25f,
+                                           0.25f, 0.25f, 1.f, s_phi[w], s_list[w]);
         if (lane < MLP_NFEAT) A.feat[lane * A.n + ci] = so.feat;
     }
     if (!valid) return;

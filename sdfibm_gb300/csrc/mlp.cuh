@@ -162,13 +162,37 @@ __device__ __forceinline__ int subcell_v0(int sc) {
                    : stn(2 * ((sc - 64) & 1), 2 * (((sc - 64) >> 1) & 1), 2 * ((sc - 64) >> 2));
 }
 
+// What a lane does in every cell's stencil, fixed by its lane index and computed once per kernel: the lattice
+// coordinates of its points l + 32 r, the lowest corners of its sub-cubes l + 32 r (rounds 0 and 1: the 4^3 division,
+// round 2: lanes 0..7 the 2^3 one) and the stencil point of its network input.
+struct StencilLane {
+    float fi[4], fj[4], fk[4];
+    int v0[3];
+    int inp;
+};
+__device__ inline StencilLane stencil_lane() {
+    const int lane = threadIdx.x & 31;
+    StencilLane L;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int p = min(lane + 32 * r, STENCIL_PTS - 1);
+        const int k = p / 25, j = (p - 25 * k) / 5, i = p - 25 * k - 5 * j;
+        L.fi[r] = (float)i; L.fj[r] = (float)j; L.fk[r] = (float)k;
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) L.v0[r] = subcell_v0(min(lane + 32 * r, 71));
+    L.inp = input_point(min(lane, 14));
+    return L;
+}
+
 // Shape::signedDistance / h at the 125 lattice points, lane l taking points l, l + 32, ...: the 3-D shapes of the
 // coupling workloads with the hardware's approximate square root and reciprocal (a few units in the last place; the
 // reference's filter kept), any other shape through sdf32.
 __device__ __forceinline__ float fast_sqrt(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
 template <int TYPE>
-__device__ __forceinline__ void stencil_points(const ShapeK& sh, const float* L0, const float* Li, const float* Lj,
-                                               const float* Lk, float inv_h, float* sphi) {
+__device__ __forceinline__ void stencil_points(const ShapeK& sh, const StencilLane& SL, const float* L0,
+                                               const float* Li, const float* Lj, const float* Lk, float inv_h,
+                                               float* sphi) {
     const int lane = threadIdx.x & 31;
     const float* a = sh.p32;
     const float c0 = sh.com32[0], c1 = sh.com32[1], c2 = sh.com32[2];
@@ -176,8 +200,7 @@ __device__ __forceinline__ void stencil_points(const ShapeK& sh, const float* L0
     for (int r = 0; r < 4; ++r) {
         const int p = lane + 32 * r;
         if (p >= STENCIL_PTS) break;
-        const int k = p / 25, j = (p - 25 * k) / 5, i = p - 25 * k - 5 * j;
-        const float fi = (float)i, fj = (float)j, fk = (float)k;
+        const float fi = SL.fi[r], fj = SL.fj[r], fk = SL.fk[r];
         const float lx = __fmaf_rn(fk, Lk[0], __fmaf_rn(fj, Lj[0], __fmaf_rn(fi, Li[0], L0[0])));
         const float ly = __fmaf_rn(fk, Lk[1], __fmaf_rn(fj, Lj[1], __fmaf_rn(fi, Li[1], L0[1])));
         const float lz = __fmaf_rn(fk, Lk[2], __fmaf_rn(fj, Lj[2], __fmaf_rn(fi, Li[2], L0[2])));
@@ -209,8 +232,9 @@ __device__ __forceinline__ void stencil_points(const ShapeK& sh, const float* L0
 struct StencilOut {
     float p4, p2, feat;
 };
-__device__ inline StencilOut cell_stencil(const ShapeK& sh, const float* M, float bx, float by, float bz, float qx,
-                                          float qy, float qz, float inv_h, float* sphi, uint8_t* slist) {
+__device__ inline StencilOut cell_stencil(const ShapeK& sh, const StencilLane& SL, const float* M, float bx, float by,
+                                          float bz, float qx, float qy, float qz, float inv_h, float* sphi,
+                                          uint8_t* slist) {
     const int lane = threadIdx.x & 31;
     // local coordinates of lattice point (i, j, k): L0 + i Li + j Lj + k Lk
     const float L0[3] = {__fmaf_rn(M[0], bx, __fmaf_rn(M[1], by, M[2] * bz)),
@@ -219,10 +243,10 @@ __device__ inline StencilOut cell_stencil(const ShapeK& sh, const float* M, floa
     const float Li[3] = {M[0] * qx, M[3] * qx, M[6] * qx}, Lj[3] = {M[1] * qy, M[4] * qy, M[7] * qy},
                 Lk[3] = {M[2] * qz, M[5] * qz, M[8] * qz};
     switch (sh.type) {
-        case SDFIBM_SHAPE_SPHERE: stencil_points<SDFIBM_SHAPE_SPHERE>(sh, L0, Li, Lj, Lk, inv_h, sphi); break;
-        case SDFIBM_SHAPE_ELLIPSOID: stencil_points<SDFIBM_SHAPE_ELLIPSOID>(sh, L0, Li, Lj, Lk, inv_h, sphi); break;
-        case SDFIBM_SHAPE_BOX: stencil_points<SDFIBM_SHAPE_BOX>(sh, L0, Li, Lj, Lk, inv_h, sphi); break;
-        default: stencil_points<0>(sh, L0, Li, Lj, Lk, inv_h, sphi); break;
+        case SDFIBM_SHAPE_SPHERE: stencil_points<SDFIBM_SHAPE_SPHERE>(sh, SL, L0, Li, Lj, Lk, inv_h, sphi); break;
+        case SDFIBM_SHAPE_ELLIPSOID: stencil_points<SDFIBM_SHAPE_ELLIPSOID>(sh, SL, L0, Li, Lj, Lk, inv_h, sphi); break;
+        case SDFIBM_SHAPE_BOX: stencil_points<SDFIBM_SHAPE_BOX>(sh, SL, L0, Li, Lj, Lk, inv_h, sphi); break;
+        default: stencil_points<0>(sh, SL, L0, Li, Lj, Lk, inv_h, sphi); break;
     }
     __syncwarp();
     float s4 = 0.f, s2 = 0.f;
@@ -232,7 +256,7 @@ __device__ inline StencilOut cell_stencil(const ShapeK& sh, const float* M, floa
         const int sc = lane + 32 * r;
         int t = 0;
         if (sc < 72) {
-            t = subcell_trivial(sphi, subcell_v0(sc), sc < 64 ? 1 : 2);
+            t = subcell_trivial(sphi, SL.v0[r], r < 2 ? 1 : 2);
             if (t == 1) {
                 if (sc < 64) s4 += 1.f; else s2 += 1.f;
             }
@@ -257,7 +281,7 @@ __device__ inline StencilOut cell_stencil(const ShapeK& sh, const float* M, floa
     out.p2 = s2 * (1.f / 8.f);
     // network inputs: 8 vertices, 6 face centres, centre, logit(P2); then the prior logit(P4)
     float f = 0.f;
-    if (lane < 15) f = sphi[input_point(lane)];
+    if (lane < 15) f = sphi[SL.inp];
     else if (lane == 15) f = logit_frac(clamp_frac(out.p2));
     else if (lane == 16) f = logit_frac(clamp_frac(out.p4));
     out.feat = f;

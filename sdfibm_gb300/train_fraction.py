@@ -12,10 +12,12 @@ Steps, all through libsdfibm_cuda.so:
   3. held-out cells of the same distribution: the model's error against the label, and the error of its prior alone
      (the 4^3 sub-cell planar reconstruction, network output zero), per shape family;
   4. the confidence band, calibrated on a coupling workload that the benchmark does not use: the 512^3 workload's
-     distribution of spheres / ellipsoids / boxes drawn with another seed, at half scale per axis.  For a grid of
+     distribution of spheres / ellipsoids / boxes drawn with another seed (16384 solids on 512^3).  For a grid of
      (tau_refine, rho_min) the learned step's As and per-solid force are compared with a SUBSAMPLE 16^3 step; the band
      kept is the one with the smallest fallback share whose As mean, As 99th percentile and per-solid force median
-     and 90th percentile stay within the limits;
+     and 90th percentile stay within the limits.  The force limits default to 0.9 of the contract's 1e-4: the 90th
+     percentile moves by a few per cent between draws of the same distribution, and a band chosen exactly at the
+     limit on one draw can land above it on another;
   5. the model file, with the training record (data description, losses, held-out errors, calibration table,
      timings) in `meta`.
 """
@@ -28,7 +30,7 @@ import numpy as np
 from . import learned
 
 TAU_GRID = (1e30, 0.1, 0.05, 0.04, 0.03, 0.02, 0.01, 0.005)
-RHO_GRID = (0.0, 1.0, 1.5, 2.0, 2.5, 3.0, 3.5, 4.0, 5.0, 6.0)
+RHO_GRID = (0.0, 1.0, 1.5, 2.0, 2.5, 3.0, 3.5, 4.0, 4.5, 5.0, 6.0)
 
 
 def band_score(torch, feat):
@@ -61,7 +63,7 @@ def heldout_report(torch, params, tf, tl, rec):
     return out
 
 
-def calibrate_band(torch, params_np, limits, scale=0.5, seed=6):
+def calibrate_band(torch, params_np, limits, scale=1.0, seed=6):
     """Band on a coupling workload the benchmark does not use; returns (tau_refine, rho_min, table)."""
     from . import abi, workloads
     from .cloud import SolidCloud
@@ -118,8 +120,8 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--band-mean", type=float, default=1e-3)
     ap.add_argument("--band-p99", type=float, default=1e-2)
-    ap.add_argument("--band-force", type=float, default=1e-4, help="limit of the per-solid force error median")
-    ap.add_argument("--band-force-p90", type=float, default=1e-4, help="limit of its 90th percentile")
+    ap.add_argument("--band-force", type=float, default=0.9e-4, help="limit of the per-solid force error median")
+    ap.add_argument("--band-force-p90", type=float, default=0.9e-4, help="limit of its 90th percentile")
     ap.add_argument("--no-calibrate", action="store_true")
     ap.add_argument("--out", default=learned.MODEL_PATH)
     a = ap.parse_args(argv)

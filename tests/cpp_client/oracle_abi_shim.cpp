@@ -141,6 +141,16 @@ int sdfibm_cuda_touched_noalloc(const sdfibm_mesh_desc*, const sdfibm_solid_desc
 }
 int sdfibm_cuda_set_fraction_model(sdfibm_ctx*, const float*, float, float) { return SDFIBM_ERR_STATE; }
 int sdfibm_cuda_tuning(sdfibm_ctx*, int32_t*, int32_t) { return SDFIBM_ERR_STATE; }
+/* the solver's forcing update on host fields (every pointer is host memory here) */
+int sdfibm_cuda_apply_forcing(sdfibm_ctx* c, double dt, const float* As, const float* Fs, const float* Ts, float* U,
+                              float* T) {
+    if (!c || !As || !Fs || !Ts || !U) return SDFIBM_ERR_ARG;
+    const int64_t N = c->N;
+    for (int64_t i = 0; i < 3 * N; ++i) U[i] = (float)((double)U[i] - (double)Fs[i] * dt);
+    if (T)
+        for (int64_t i = 0; i < N; ++i) T[i] = (float)((1.0 - (double)As[i]) * (double)T[i] + (double)Ts[i]);
+    return SDFIBM_OK;
+}
 int sdfibm_cuda_create_polymesh(const double*, int64_t, const int32_t*, const int32_t*, int64_t, const int32_t*,
                                 const int32_t*, int64_t, int32_t, const sdfibm_solid_desc*, int32_t,
                                 const sdfibm_options*, void*, sdfibm_ctx**) {

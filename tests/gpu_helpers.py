@@ -10,11 +10,13 @@ AS_REL, AS_ABS = 1e-5, 1e-9      # As, Ts and Fs per cell: |d| <= 1e-5 |ref| + 1
 FT_REL = 1e-6                    # force/torque per solid, normwise against the sum of |contributions|
 
 
-def run_pair(torch, w, steps=1, evolve=False, fix=False, U=None, gpu_opt=None, gpu_setup=None):
+def run_pair(torch, w, steps=1, evolve=False, fix=False, U=None, gpu_opt=None, gpu_setup=None, sync_states=False):
     """Runs `steps` interact (+evolve, +fixInternal) on the GPU and on the fast oracle; returns both sides.
 
     gpu_opt: options of the GPU side when they differ from the oracle's (w.opt); gpu_setup(cloud) runs after
-    the GPU cloud is created."""
+    the GPU cloud is created.  sync_states: the oracle takes the GPU's solid states before every interact, so that
+    each step compares the coupling on the same states (the FP32 forcing's force sums, within their 1e-6 bound, move
+    the solids by a little through evolve, and U - us can cancel at a cell)."""
     Uh = w.U_numpy() if U is None else U
     gpu = SolidCloud(w.mesh, w.solids, gpu_opt if gpu_opt is not None else w.opt)
     if gpu_setup is not None:
@@ -27,6 +29,8 @@ def run_pair(torch, w, steps=1, evolve=False, fix=False, U=None, gpu_opt=None, g
     out = []
     t = 0.0
     for _ in range(steps):
+        if sync_states:
+            orc.set_state(gpu.states())
         FTg = gpu.interact(t, w.dt, Ud, fd)
         FTo = orc.interact(t, w.dt, Uo, fo)
         out.append((FTg, FTo))

@@ -43,10 +43,11 @@ def test_dataset_matches_oracle(cuda_lib, torch_cuda):
     # hi + lo pairs keep about 16 bits)
     d = np.abs(feat[:15].T - ref[:, :15]) / (1 + np.abs(ref[:, :15]))
     assert d.max() <= 1e-4, "distance inputs: max scaled difference %g" % d.max()
-    # P2 and P4 through their logits: compare the fractions
+    # P2 and P4 through their logits: compare the fractions.  A sub-cell's fraction moves by the distances' FP32
+    # rounding over the sub-cell's width (h/2 for P2) and by the fast reciprocals of the closed form: about 2e-5
     sig = lambda z: 1.0 / (1.0 + np.exp(-z.astype(np.float64)))
-    assert np.abs(sig(feat[15]) - sig(ref[:, 15])).max() <= 2e-5
-    assert np.abs(sig(feat[16]) - sig(ref[:, 16])).max() <= 2e-5
+    assert np.abs(sig(feat[15]) - sig(ref[:, 15])).max() <= 5e-5
+    assert np.abs(sig(feat[16]) - sig(ref[:, 16])).max() <= 5e-5
     assert types == {abi.SHAPE_SPHERE, abi.SHAPE_ELLIPSOID, abi.SHAPE_BOX, abi.SHAPE_PLANE, abi.SHAPE_CIRCLE,
                      abi.SHAPE_ELLIPSE}
     # the prior is a good estimate already: planes are exact up to the 8^3 label's own lattice error

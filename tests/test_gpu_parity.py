@@ -134,6 +134,54 @@ def test_sparse_reset_and_repeat(cuda_lib, torch_cuda):
     check_interact(w, r)
 
 
+def _cluster(exact, twod):
+    """Solids overlapping in a cluster (cells touched by two to four solids), some crossing the high corner of a mesh
+    whose cell count is not a multiple of 8, moving about two cells per step."""
+    rng = np.random.default_rng(21 if twod else 22)
+    if twod:
+        n = (45, 37, 1)
+        mesh = abi.mesh_desc(n, (0.0, 0.0, -0.5), (1.0 / 45, 1.0 / 45, 1.0), twod=1)
+        kinds = [("Circle", dict(radius=0.09)), ("Ellipse", dict(radiusa=0.12, radiusb=0.05)),
+                 ("Rectangle", dict(radiusa=0.1, radiusb=0.04))]
+    else:
+        n = (37, 29, 23)
+        mesh = abi.mesh_desc(n, (0.0, 0.0, 0.0), (1.0 / 37,) * 3, twod=0)
+        kinds = [("Sphere", dict(radius=0.09)), ("Ellipsoid", dict(radiusa=0.12, radiusb=0.05, radiusc=0.07)),
+                 ("Box", dict(radiusa=0.1, radiusb=0.04, radiusc=0.06))]
+    hi = np.array([n[0] / 37 if not twod else 1.0, n[1] / (37 if not twod else 45), n[2] / 37 if not twod else 0.0])
+    centre = 0.45 * hi
+    solids = []
+    for i in range(10):
+        t, kw = kinds[i % 3]
+        if i < 7:
+            pos = centre + rng.uniform(-0.08, 0.08, 3)
+        else:  # at the high corner: the last chunk of the mesh is partly outside it
+            pos = hi - rng.uniform(0.0, 0.05, 3)
+        if twod:
+            pos[2] = 0.0
+        vel = rng.normal(0, 3.0, 3) * ((1, 1, 0) if twod else 1)
+        om = rng.normal(0, 5.0, 3) * ((0, 0, 1) if twod else 1)
+        solids.append(make_solid(i, make_shape(t, **kw), 1.1, pos, vel=vel, omega=om))
+    opt = abi.options(rho_f=1.2, fraction_method=abi.FRACTION_SUBSAMPLE, exact_forcing=exact)
+    return Workload("cluster", mesh, solids, opt, 0.01, (0.3, -0.2, 0.1), 0.2, 5)
+
+
+@pytest.mark.parametrize("twod", [False, True])
+@pytest.mark.parametrize("exact", [1, 0])
+def test_clustered_solids_shared_cells(cuda_lib, torch_cuda, twod, exact):
+    """Cells shared by several solids (their FP64 sums through the shared table), chunks of 8 cells split between
+    solids and untouched cells, the partial last chunk of the mesh, and cells left behind by fast motion (the sparse
+    reset outside the chunks written this call), over three coupled steps."""
+    w = _cluster(exact, twod)
+    assert w.ncells % 8 != 0
+    r = run_pair(torch_cuda, w, steps=3, evolve=True, sync_states=not exact)
+    check_interact(w, r)
+    touched = np.concatenate([r["orc"].touched(s)[0] for s in range(len(w.solids))])
+    _, cnt = np.unique(touched, return_counts=True)
+    assert (cnt > 1).sum() > 20 and cnt.max() >= 3
+    assert (touched == w.ncells - 1).any() or (touched >= w.ncells - 8).any()
+
+
 def test_fix_internal(cuda_lib, torch_cuda):
     w = workloads.cylinder2d(scale=0.5)
     w.solids[0].vel[0] = 0.3
@@ -141,6 +189,37 @@ def test_fix_internal(cuda_lib, torch_cuda):
     r = run_pair(torch_cuda, w, steps=2, evolve=True, fix=True)
     Ug = r["Ud"].cpu().numpy().astype(np.float64).reshape(-1)
     assert np.abs(Ug - r["Uo"]).max() <= 1e-6 * np.abs(r["Uo"]).max()
+
+
+@pytest.mark.parametrize("cfg", ["poly3d_512", "sedimentation2d"])
+def test_apply_forcing(cuda_lib, torch_cuda, cfg):
+    """The solver's forcing update on device fields after each of three moving steps: U -= Fs dt and
+    T = (1 - As) T + Ts equal the dense FP64 update of every cell, rounded once to FP32; other fields are refused."""
+    from sdfibm_gb300.cloud import SolidCloud
+    torch = torch_cuda
+    w = workloads.poly3d_512(scale=0.0625) if cfg == "poly3d_512" else workloads.sedimentation2d(scale=0.125)
+    N = w.ncells
+    c = SolidCloud(w.mesh, w.solids, w.opt)
+    f = c.new_fields()
+    U = torch.from_numpy(w.U_numpy()).cuda()
+    T = torch.from_numpy(np.random.default_rng(4).uniform(0.0, 2.0, N).astype(np.float32)).cuda()
+    t = 0.0
+    for step in range(3):
+        c.interact(t, w.dt, U, f)
+        U0, T0 = U.cpu().numpy().astype(np.float64), T.cpu().numpy().astype(np.float64)
+        As, Fs, Ts = (f[k].cpu().numpy().astype(np.float64) for k in ("As", "Fs", "Ts"))
+        c.apply_forcing(w.dt, f, U, T if step != 1 else None)
+        Ue = (U0.reshape(-1) - Fs.reshape(-1) * w.dt).astype(np.float32)
+        assert np.array_equal(U.cpu().numpy().reshape(-1), Ue), step
+        Te = ((1.0 - As) * T0 + Ts).astype(np.float32) if step != 1 else T0.astype(np.float32)
+        assert np.array_equal(T.cpu().numpy(), Te), step
+        assert (As > 0).sum() > 0
+        c.evolve(t, w.dt)
+        t += w.dt
+    g = c.new_fields()
+    with pytest.raises(RuntimeError):
+        c.apply_forcing(w.dt, g, U, T)
+    c.close()
 
 
 def test_interact_host_matches_device(cuda_lib, torch_cuda):
