@@ -40,23 +40,28 @@ ALG_BYTES = {
     "reset_kernel": ("coupling_cells", 24.0),      # previous cells zeroed
     "classify_kernel": ("bbox_cells", 1.0),        # one class byte per bbox cell (+ the cut-cell outputs below)
     "connect_kernel": ("bbox_cells", 1.0),         # class bytes read once
-    "mlp_infer_kernel": ("learned_cells", 56.0),   # 11 features + destination read, fraction written
+    "mlp_infer_kernel": ("network_cells", 80.0),   # 16 inputs + prior + destination read, fraction written
     "subsample_cells_kernel": ("sampled_cells", 16.0),  # list entry and destination read, fraction written
 }
 # DRAM bytes per unit measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum of one launch / its units) on the
-# 256^3 / 2048-solid learned workload; profiles/<kernel>_poly3d_256_learned.md records the captures
+# 256^3 / 2048-solid learned workload (the full-size workload's distribution at half scale per axis);
+# profiles/<kernel>_poly3d_256_learned.md and profiles/launches_poly3d_256_learned.md record the captures
 NCU_BYTES_PER_UNIT = {
-    "classify_kernel": 1.40,   # 11.0 MB for 7,825,801 bbox cells (the learned features stay in L2 for the network)
-    "subsample_cells_kernel": 39.6,  # 18.2 MB for 460,073 sampled cells
+    "couple_chunks_kernel": 121.1,  # 161.4 MB for 1,332,670 coupling cells: whole 32-byte sectors of the marked chunks
+    "classify_kernel": 1.35,        # 5.8 MB for 4,282,843 bbox cells left after the box test
+    "subsample_cells_kernel": 60.9,  # 9.4 MB for 154,364 sampled cells
+    "learned_stencil_kernel": 14.3,  # 10.9 MB for 760,774 listed cut cells
 }
 # Warp instructions per unit (ncu smsp__inst_executed.sum of one launch / its units), per (kernel, method); the
-# sampling and classification kernels are bound by instruction issue, and these counts give their issue roofline
+# stencil, sampling and classification kernels are bound by instruction issue, and these counts give their issue
+# roofline
 INST_PER_UNIT = {
-    ("subsample_cells_kernel", "learned"): ("sampled_cells", 1680.2),  # 773.0 M for 460,073 16^3 cells
-    ("classify_kernel", "learned"): ("bbox_cells", 21.62),            # 169.2 M for 7,825,801 bbox cells
-    ("classify_kernel", "refgeo"): ("bbox_cells", 24.02),             # 187.9 M for the same bbox cells
+    ("learned_stencil_kernel", "learned"): ("learned_cells", 679.3),  # 516.8 M for 760,774 listed cut cells
+    ("subsample_cells_kernel", "learned"): ("sampled_cells", 1709.3),  # 263.9 M for 154,364 16^3 cells
+    ("classify_kernel", "learned"): ("bbox_cells", 31.51),            # 134.9 M for 4,282,843 bbox cells
+    ("classify_kernel", "refgeo"): ("bbox_cells", 37.82),             # 162.0 M for the same bbox cells
 }
-# FLOPs of the two tensor-core layers per predicted cell: hi and lo BF16 halves of an 11(16)x64 and a 64x64 product
+# FLOPs of the two tensor-core layers per predicted cell: hi and lo BF16 halves of a 16x64 and a 64x64 product
 MLP_FLOPS_PER_CELL = 2 * (2 * 16 * 64) + 2 * (2 * 64 * 64)
 METHODS = {"refgeo": 0, "subsample": 1, "learned": 2}
 
@@ -347,8 +352,8 @@ def issue_peak(clocks, sms):
 
 def kernel_rooflines(kmean, units, method, peaks, clocks, sms):
     """Roofline entries of the step's kernels, each against the limit that bounds it: warp-instruction issue for the
-    sampling and classification kernels (INST_PER_UNIT, from ncu), HBM for the coupling kernel, the tensor cores for
-    the network.  achieved = work per launch (per-unit figure x units) / average launch time."""
+    stencil, sampling and classification kernels (INST_PER_UNIT, from ncu), HBM for the coupling kernel, the tensor
+    cores for the network.  achieved = work per launch (per-unit figure x units) / average launch time."""
     out = {}
     ip = issue_peak(clocks, sms) / 1e9
     for k, t in kmean.items():
@@ -365,8 +370,8 @@ def kernel_rooflines(kmean, units, method, peaks, clocks, sms):
         out[k] = {"bound": "hbm", "achieved": a, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": a / peaks["hbm_gbs"],
                   "ms": kmean[k], "traffic": NCU_BYTES_PER_UNIT[k] * units["coupling_cells"]
                   if k in NCU_BYTES_PER_UNIT else None}
-    if kmean.get("mlp_infer_kernel", 0) > 0 and units["learned_cells"]:
-        tf = MLP_FLOPS_PER_CELL * units["learned_cells"] / (kmean["mlp_infer_kernel"] * 1e-3) / 1e12
+    if kmean.get("mlp_infer_kernel", 0) > 0 and units["network_cells"]:
+        tf = MLP_FLOPS_PER_CELL * units["network_cells"] / (kmean["mlp_infer_kernel"] * 1e-3) / 1e12
         out["mlp_infer_kernel"] = {"bound": "tensor", "achieved": tf, "peak": peaks["bf16_tflops"],
                                    "unit": "TFLOP/s", "frac": tf / peaks["bf16_tflops"],
                                    "ms": kmean["mlp_infer_kernel"]}
@@ -527,7 +532,10 @@ def main():
              "learned_cells": st.get("learned_cells", 0) if args.method == "learned" else 0,
              "sampled_cells": st.get("learned_fallback_cells", 0) if args.method == "learned"
              else (st.get("learned_cells", 0) if args.method == "subsample" else 0),
-             "cut_cells": st.get("learned_cells", 0)}
+             "cut_cells": st.get("learned_cells", 0),
+             # the cells the network predicts (the stencil kernel compacts the in-band cells for it)
+             "network_cells": (st.get("learned_cells", 0) - st.get("learned_fallback_cells", 0))
+             if args.method == "learned" else 0}
 
     compare = None
     refgeo = None
@@ -666,9 +674,9 @@ def main():
     roofline.update({"kernel": dom, "peak_kind": peaks_kind + (" (HBM, bf16)" if peaks_kind == "measured" else ""),
                      "kernels": kr,
                      "note": "issue = warp instructions per second against 4 per cycle per SM at the sampled SM clock "
-                             "(per-unit instruction counts from ncu smsp__inst_executed.sum); the sampling and "
-                             "classification kernels are instruction-bound, the coupling kernel HBM-bound, the "
-                             "network tensor-core-bound"})
+                             "(per-unit instruction counts from ncu smsp__inst_executed.sum); the stencil, sampling "
+                             "and classification kernels are instruction-bound, the coupling kernel HBM/latency-bound, "
+                             "the network tensor-core-bound"})
 
     e2e = None
     if not args.no_e2e:

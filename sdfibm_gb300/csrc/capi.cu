@@ -219,7 +219,8 @@ struct sdfibm_ctx {
     float* d_mlp = nullptr;
     float tau_refine = 0.f, rho_min = 0.f;  // confidence band of the learned fraction
     bool model_set = false;
-    float* d_feat = nullptr;  // [SDFIBM_MLP_NFEAT][feat_cap]: model inputs and prior of the listed cut cells
+    float* d_feat = nullptr;  // [SDFIBM_MLP_NFEAT][feat_cap]: model inputs and prior of the in-band cut cells
+    int64_t* d_mlp_index = nullptr;  // fraction index of each of those cells
     float* d_rg_phi = nullptr;  // REF-GEO: [8][feat_cap] vertex distances of the listed cut cells
     int64_t feat_cap = 0;
     int32_t* d_fref_solid = nullptr;
@@ -775,13 +776,14 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             StencilArgs sa{};
             sa.m = ctx->mesh; sa.sk = ctx->d_sk; sa.plan = ctx->d_plan; sa.fref_solid = ctx->d_fref_solid;
             sa.fref_index = ctx->d_fref_index; sa.cap = ctx->feat_cap; sa.feat = ctx->d_feat; sa.fb_list = ctx->d_fb;
+            sa.mlp_index = ctx->d_mlp_index;
             sa.cnt = ctx->d_cnt; sa.tau_refine = ctx->tau_refine; sa.rho_min = ctx->rho_min;
             learned_stencil_kernel<<<ctx->stencil_grid, 256, 0, st>>>(sa);
             mark(ctx, "learned_stencil_kernel");
             ++launches;
             MlpInferArgs ia{};
-            ia.params = ctx->d_mlp; ia.feat = ctx->d_feat; ia.stride = ctx->feat_cap; ia.n_dev = &ctx->d_cnt->n_feat;
-            ia.ref_index = ctx->d_fref_index; ia.alpha = ctx->d_alpha; ia.error = &ctx->d_cnt->error;
+            ia.params = ctx->d_mlp; ia.feat = ctx->d_feat; ia.stride = ctx->feat_cap; ia.n_dev = &ctx->d_cnt->n_inband;
+            ia.ref_index = ctx->d_mlp_index; ia.alpha = ctx->d_alpha; ia.error = &ctx->d_cnt->error;
             launch_mlp_infer(ia, ctx->mlp_grid, st);
             mark(ctx, "mlp_infer_kernel");
             fa.m = ctx->mesh; fa.sk = ctx->d_sk; fa.st = ctx->d_st; fa.plan = ctx->d_plan; fa.fb_list = ctx->d_fb;
@@ -1557,7 +1559,8 @@ int sdfibm_cuda_set_fraction_model(sdfibm_ctx* ctx, const float* params, float t
         ctx->feat_cap = std::max<int64_t>(1, ctx->scratch_bytes);
         if (dalloc(&ctx->d_mlp, SDFIBM_MLP_NPARAM) || dalloc(&ctx->d_feat, (size_t)SDFIBM_MLP_NFEAT * ctx->feat_cap) ||
             (!ctx->d_fref_solid && dalloc(&ctx->d_fref_solid, ctx->feat_cap)) ||
-            (!ctx->d_fref_index && dalloc(&ctx->d_fref_index, ctx->feat_cap)) || dalloc(&ctx->d_fb, ctx->feat_cap))
+            (!ctx->d_fref_index && dalloc(&ctx->d_fref_index, ctx->feat_cap)) || dalloc(&ctx->d_fb, ctx->feat_cap) ||
+            dalloc(&ctx->d_mlp_index, ctx->feat_cap))
             return fail(ctx, SDFIBM_ERR_CUDA, "allocation of the learned-fraction buffers failed");
     }
     mlp_prepare();
@@ -1601,7 +1604,7 @@ void sdfibm_cuda_destroy(sdfibm_ctx* ctx) {
                    ctx->d_lists[1][0], ctx->d_lists[1][1], ctx->d_lists[1][2], ctx->d_lists[1][3], ctx->d_cnt, ctx->d_ftacc,
                    ctx->d_ft, ctx->d_hash, ctx->d_gcount, ctx->d_gstart, ctx->d_gcursor, ctx->d_glist, ctx->d_U,
                    ctx->d_As, ctx->d_Fs, ctx->d_Ts, ctx->d_Ct, ctx->d_alpha, ctx->d_sh_keys, ctx->d_sh_vals, ctx->d_sh_used,
-                   ctx->d_mlp, ctx->d_feat, ctx->d_rg_phi, ctx->d_fref_solid, ctx->d_fref_index, ctx->d_fb,
+                   ctx->d_mlp, ctx->d_feat, ctx->d_rg_phi, ctx->d_fref_solid, ctx->d_fref_index, ctx->d_fb, ctx->d_mlp_index,
                    ctx->d_fcount, ctx->d_fstart, ctx->d_fcursor, ctx->d_flist, ctx->d_planes};
     for (void* p : dev)
         if (p) cudaFree(p);

@@ -43,6 +43,7 @@ __global__ void plan_kernel(MeshK m, const SolidK* __restrict__ sk, const sdfibm
     // local box holding the inside region (widened far beyond FP32 rounding): tiles of the classify pass that lie
     // outside it hold no inside vertex
     p.cull_box = 0;
+    p.radius_cells = (float)k.radiusB * (1.f / m.h32[0]);
     if (!k.shape.prism && !k.infinite &&
         (k.shape.type == SDFIBM_SHAPE_SPHERE || k.shape.type == SDFIBM_SHAPE_ELLIPSOID ||
          k.shape.type == SDFIBM_SHAPE_BOX)) {
@@ -991,6 +992,7 @@ __global__ void begin_kernel(Counters* cnt) {
     cnt->n_inside = 0; cnt->n_cut = 0; cnt->n_shared = 0; cnt->shared_marks = 0;
     cnt->exact_rechecks = 0; cnt->bbox_cells = 0;
     cnt->n_feat = 0; cnt->n_fb = 0; cnt->n_recheck = 0; cnt->n_ovf = 0; cnt->n_shent = 0;
+    cnt->n_inband = 0;
 }
 
 // F = rho_f * V / dt * sum f, T = rho_f * V / dt * sum (C - x) x f  (solidcloud.cpp:411-421)

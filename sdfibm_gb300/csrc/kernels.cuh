@@ -93,6 +93,7 @@ struct SolidPlan {
     float cb32[3];
     int32_t cull_box;         // 1: the inside region lies in the local box below (3-D spheres, ellipsoids, boxes)
     float lbox_c[3], lbox_s[3];  // that box in the local frame: centre and half extents (FP32, widened)
+    float radius_cells;       // bounding radius / h (FP32): the solid-size half of the learned fraction's band
 };
 
 // Global counters / flags (one record per context, device memory).
@@ -117,7 +118,7 @@ struct Counters {
     int32_t n_recheck;        // SUBSAMPLE points left to recheck_kernel this call
     int32_t n_ovf;            // LEARNED: fallback cells whose points overflowed the recheck list (recount_kernel)
     int32_t n_shent;          // list entries on cells several solids claimed (shared_scan_kernel)
-    int32_t pad1;
+    int32_t n_inband;         // LEARNED: listed cut cells inside the band, compacted for the network
 };
 
 // list lengths clamped to the capacity (a capacity error leaves the counters above what was written)
@@ -234,8 +235,10 @@ struct StencilArgs {
     const int32_t* fref_solid;
     const int64_t* fref_index;
     int64_t cap;
-    float* feat;          // [SDFIBM_MLP_NFEAT][cap]: network inputs, then the prior logit (NaN outside the band)
+    float* feat;          // [SDFIBM_MLP_NFEAT][cap]: network inputs, then the prior logit, of the in-band cells
+                          // (compacted, n_inband of them)
     int32_t* fb_list;     // list positions of the cells outside the band (SUBSAMPLE fallback)
+    int64_t* mlp_index;   // fraction index of each compacted in-band cell (the network's destination)
     Counters* cnt;
     float tau_refine;     // band: |P4 - P2| limit
     float rho_min;        // band: smallest bounding radius / h of a solid whose cells the network takes

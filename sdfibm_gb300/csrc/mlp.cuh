@@ -163,11 +163,11 @@ __device__ __forceinline__ int subcell_v0(int sc) {
 }
 
 // What a lane does in every cell's stencil, fixed by its lane index and computed once per kernel: the lattice
-// coordinates of its points l + 32 r, the lowest corners of its sub-cubes l + 32 r (rounds 0 and 1: the 4^3 division,
-// round 2: lanes 0..7 the 2^3 one) and the stencil point of its network input.
+// coordinates of its points l + 32 r, the lowest corners of its 4^3 sub-cubes l + 32 r and the stencil point of its
+// network input.
 struct StencilLane {
     float fi[4], fj[4], fk[4];
-    int v0[3];
+    int v0[2];
     int inp;
 };
 __device__ inline StencilLane stencil_lane() {
@@ -180,7 +180,7 @@ __device__ inline StencilLane stencil_lane() {
         L.fi[r] = (float)i; L.fj[r] = (float)j; L.fk[r] = (float)k;
     }
 #pragma unroll
-    for (int r = 0; r < 3; ++r) L.v0[r] = subcell_v0(min(lane + 32 * r, 71));
+    for (int r = 0; r < 2; ++r) L.v0[r] = subcell_v0(lane + 32 * r);
     L.inp = input_point(min(lane, 14));
     return L;
 }
@@ -227,8 +227,8 @@ __device__ __forceinline__ void stencil_points(const ShapeK& sh, const StencilLa
 // (i, j, k) lies at world offset (bx + i*qx, by + j*qy, bz + k*qz) from the solid centre (q = h/4 per axis, FP32), its
 // local coordinates are M times that offset.  sphi: 125 floats and slist: 72 bytes of shared memory of this warp.
 // Every lane returns P4 and P2 (unclamped); lane f < 16 returns input f in *feat, lane 16 the prior logit(clamp(P4)).
-// The 72 sub-cubes are first sorted by the cheap test of subcell_trivial; only those the fitted plane crosses (about a
-// third) take the closed form, spread over the lanes.
+// The 64 sub-cubes of P4 are first sorted by the cheap test of subcell_trivial; only those the fitted plane crosses
+// (about a third), and the 8 of P2, take the closed form, spread over the lanes.
 struct StencilOut {
     float p4, p2, feat;
 };
@@ -252,19 +252,18 @@ __device__ inline StencilOut cell_stencil(const ShapeK& sh, const StencilLane& S
     float s4 = 0.f, s2 = 0.f;
     int ncross = 0;
 #pragma unroll
-    for (int r = 0; r < 3; ++r) {
+    for (int r = 0; r < 2; ++r) {
         const int sc = lane + 32 * r;
-        int t = 0;
-        if (sc < 72) {
-            t = subcell_trivial(sphi, SL.v0[r], r < 2 ? 1 : 2);
-            if (t == 1) {
-                if (sc < 64) s4 += 1.f; else s2 += 1.f;
-            }
-        }
-        const unsigned need = __ballot_sync(0xffffffffu, sc < 72 && t < 0);
-        if (sc < 72 && t < 0) slist[ncross + __popc(need & ((1u << lane) - 1u))] = (uint8_t)sc;
+        const int t = subcell_trivial(sphi, SL.v0[r], 1);
+        if (t == 1) s4 += 1.f;
+        const unsigned need = __ballot_sync(0xffffffffu, t < 0);
+        if (t < 0) slist[ncross + __popc(need & ((1u << lane) - 1u))] = (uint8_t)sc;
         ncross += __popc(need);
     }
+    // the eight 2^3 sub-cubes go to the closed form directly (its own early exits settle the uncrossed ones): a
+    // round of the cheap test would keep 24 of the 32 lanes idle
+    if (lane < 8) slist[ncross + lane] = (uint8_t)(64 + lane);
+    ncross += 8;
     __syncwarp();
     for (int e = lane; e < ncross; e += 32) {
         const int sc = slist[e];
@@ -297,8 +296,8 @@ __device__ __forceinline__ bool in_band(float p4, float p2, float tau_refine) {
 }
 
 // Inference over a list of cells: feat holds MLP_NFEAT rows (inputs, then the prior logit).  Standalone mode
-// (ref_index == nullptr): out[c] = predicted fraction.  Coupling mode: alpha[ref_index[c]] = predicted fraction for
-// every cell whose prior is a number (cells outside the band carry NaN there and are left to the fallback).
+// (ref_index == nullptr): out[c] = predicted fraction.  Coupling mode: alpha[ref_index[c]] = predicted fraction (the
+// in-band cells, compacted by learned_stencil_kernel; a NaN prior is skipped).
 struct MlpInferArgs {
     const float* params;     // FP32 [MLP_NPARAM], device
     const float* feat;       // [MLP_NFEAT][stride]

@@ -19,12 +19,12 @@ __global__ void __launch_bounds__(256) learned_stencil_kernel(StencilArgs A) {
     __shared__ float s_phi[8][STENCIL_PTS];
     __shared__ uint8_t s_list[8][72];
     __shared__ float s_out[8][MLP_NFEAT][33];
+    __shared__ bool s_ok[8][32];
     const int lane = threadIdx.x & 31, w = (threadIdx.x >> 5) & 7;
     const int64_t n = min((int64_t)A.cnt->n_feat, A.cap);
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     const float inv_h = 1.f / A.m.h32[0];
     const float qx = 0.25f * A.m.h32[0], qy = 0.25f * A.m.h32[1], qz = 0.25f * A.m.h32[2];
-    const float nan = __int_as_float(0x7fc00000);
     const StencilLane SL = stencil_lane();
     for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < n; base += warps * 32) {
         int s_l = 0;
@@ -38,10 +38,10 @@ __global__ void __launch_bounds__(256) learned_stencil_kernel(StencilArgs A) {
             const int s = __shfl_sync(0xffffffffu, s_l, t);
             const int64_t idx = __shfl_sync(0xffffffffu, idx_l, t);
             const SolidK& k = A.sk[s];
-            bool ok = (float)k.radiusB * inv_h >= A.rho_min;  // the solid-size half of the band: no stencil needed
+            const SolidPlan& pl = A.plan[s];
+            bool ok = pl.radius_cells >= A.rho_min;  // the solid-size half of the band: no stencil needed
             float feat = 0.f;
             if (ok) {
-                const SolidPlan& pl = A.plan[s];
                 const uint32_t local = (uint32_t)(idx - k.scratch_off);
                 const int row = (int)fdiv(local, k.div_e0), lc = (int)fdiv(local, k.div_e01);
                 const int la = (int)local - row * k.ext[0], lb = row - lc * k.ext[1];
@@ -54,15 +54,25 @@ __global__ void __launch_bounds__(256) learned_stencil_kernel(StencilArgs A) {
                 ok = in_band(so.p4, so.p2, A.tau_refine);
                 feat = so.feat;
             }
-            if (lane < MLP_NFEAT) s_out[w][lane][t] = (lane == MLP_IN && !ok) ? nan : feat;
+            if (lane < MLP_NFEAT) s_out[w][lane][t] = feat;
+            if (lane == 0) s_ok[w][t] = ok;
             if (!ok && lane == 0) {
                 const int slot = atomicAdd(&A.cnt->n_fb, 1);
                 A.fb_list[slot] = (int32_t)(base + t);  // n_fb <= n <= cap entries
             }
         }
         __syncwarp();
-        if (lane < batch)
-            for (int f = 0; f < MLP_NFEAT; ++f) A.feat[f * A.cap + base + lane] = s_out[w][f][lane];
+        // the batch's in-band cells, compacted for the network: one atomic per warp, rows of consecutive cells
+        const bool in = lane < batch && s_ok[w][lane];
+        const unsigned mask = __ballot_sync(0xffffffffu, in);
+        int64_t p0 = 0;
+        if (lane == 0 && mask) p0 = atomicAdd(&A.cnt->n_inband, __popc(mask));
+        p0 = __shfl_sync(0xffffffffu, p0, 0);
+        if (in) {
+            const int64_t pos = p0 + __popc(mask & ((1u << lane) - 1u));  // n_inband <= n <= cap
+            for (int f = 0; f < MLP_NFEAT; ++f) A.feat[f * A.cap + pos] = s_out[w][f][lane];
+            A.mlp_index[pos] = idx_l;
+        }
         __syncwarp();
     }
 }

@@ -3,7 +3,9 @@ SUBSAMPLE with the 16^3 lattice the model is trained on and falls back to.
 
 Gates of the shipped model (the learned path's contract; the oracle's 16^3 lattice is the judge):
   * As, mean absolute error over the cut cells <= 1e-3 (the target's bar), 99th percentile <= 1e-2;
-  * per-solid force, normwise against the sum of |contributions|: median <= 1e-4, 90th percentile <= 1e-3.
+  * per-solid force, normwise: median <= 1e-4; 90th percentile <= 1e-4 on the benchmarked workload (16384 solids,
+    test_trained_model_full_size), <= 1e-3 on the small scaled workloads, where 32 to 64 solids make the percentile
+    a statement about two or three solids.
 The mean and the median are the gated statistics because the judge itself is a lattice count: its own error against
 the converged fraction is about 6e-4 per cut cell (mean), with a tail, so no smooth estimate meets 1e-3 in every
 cell, and a per-solid force bar of 1e-4 at the 90th percentile is below the 16^3 lattice's own noise for solids of
@@ -101,3 +103,34 @@ def test_trained_model_accuracy(cuda_lib, torch_cuda, cfg):
     rel = np.array(rel)
     assert np.median(rel) <= F_REL, "median per-solid force error %g" % np.median(rel)
     assert np.percentile(rel, 90) <= F_REL_P90, "90th percentile per-solid force error %g" % np.percentile(rel, 90)
+
+
+@pytest.mark.skipif(not os.path.exists(learned.MODEL_PATH), reason="no trained fraction model")
+def test_trained_model_full_size(cuda_lib, torch_cuda):
+    """The shipped model on the benchmarked workload itself (512^3 mesh, 16384 spheres / ellipsoids / boxes; its band
+    was calibrated on another draw of that distribution), against SUBSAMPLE 16^3 on the GPU (whose classifications are
+    the FP64 oracle's, as the SUBSAMPLE parity tests show): As mean <= 1e-3 and 99th percentile <= 1e-2 over the cut
+    cells, per-solid force median and 90th percentile <= 1e-4; the maxima are reported."""
+    from sdfibm_gb300.cloud import SolidCloud
+    torch = torch_cuda
+    params, tau, rho, _ = learned.load_model()
+    w = workloads.poly3d_512(collision=abi.COLLISION_OFF)
+    U = w.U_torch()
+    ref = SolidCloud(w.mesh, w.solids, abi.options(rho_f=w.opt.rho_f, fraction_method=abi.FRACTION_SUBSAMPLE,
+                                                   subsample_n=16))
+    fr = ref.new_fields()
+    FTr = ref.interact(0.0, w.dt, U, fr)
+    ref.close()
+    c = SolidCloud(w.mesh, w.solids, abi.options(rho_f=w.opt.rho_f, fraction_method=abi.FRACTION_LEARNED,
+                                                 learned_fallback_n=16))
+    c.set_fraction_model(params, tau, rho)
+    f = c.new_fields()
+    FT = c.interact(0.0, w.dt, U, f)
+    st = c.stats()
+    c.close()
+    a = learned.accuracy(torch, w, f, FT, fr, FTr, U)
+    msg = "%r" % a
+    assert a["as_abs_err_mean"] <= AS_MEAN and a["as_abs_err_p99"] <= AS_P99, msg
+    assert a["force_rel_err_median"] <= F_REL and a["force_rel_err_p90"] <= 1e-4, msg
+    assert a["as_abs_err_max"] < 0.1 and a["force_rel_err_max"] < 1e-2, msg
+    assert st["learned_fallback_cells"] <= 0.25 * st["learned_cells"]
