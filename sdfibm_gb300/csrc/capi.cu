@@ -28,6 +28,7 @@ int classify_occupancy(int method, bool flat);
 __global__ void subsample_cells_kernel(FallbackArgs A);
 __global__ void recount_kernel(FallbackArgs A);
 __global__ void learned_stencil_kernel(StencilArgs A);
+int stencil_block();
 __global__ void refgeo_cells_kernel(MeshK m, const SolidK* sk, const SolidPlan* plan, const int32_t* fref_solid,
                                     const int64_t* fref_index, const float* rg_phi, int64_t cap, const Counters* cnt,
                                     float* alpha);
@@ -648,7 +649,9 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
     ctx->subsample_grid = 8 * ctx->num_sms;
     ctx->mlp_grid = 4 * ctx->num_sms;
     ctx->refgeo_grid = 8 * ctx->num_sms;
-    ctx->stencil_grid = 8 * ctx->num_sms;
+    occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, learned_stencil_kernel, stencil_block(), 0);
+    ctx->stencil_grid = std::max(1, occ) * ctx->num_sms;  // persistent: every resident CTA, grid-strided
     *out = ctx;
     return SDFIBM_OK;
 }
@@ -778,7 +781,7 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             sa.fref_index = ctx->d_fref_index; sa.cap = ctx->feat_cap; sa.feat = ctx->d_feat; sa.fb_list = ctx->d_fb;
             sa.mlp_index = ctx->d_mlp_index;
             sa.cnt = ctx->d_cnt; sa.tau_refine = ctx->tau_refine; sa.rho_min = ctx->rho_min;
-            learned_stencil_kernel<<<ctx->stencil_grid, 256, 0, st>>>(sa);
+            learned_stencil_kernel<<<ctx->stencil_grid, stencil_block(), 0, st>>>(sa);
             mark(ctx, "learned_stencil_kernel");
             ++launches;
             MlpInferArgs ia{};

@@ -1059,8 +1059,9 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                 // learned_stencil_kernel computes the model's inputs), a warp per cell
                 write_cut_list<TX, TY, TZ>(A, cutlist, ncut, s, k.scratch_off + local_index(0, 0, 0), k.ext[0],
                                            k.ext[1]);
-            } else {
+            } else if (METHOD == SDFIBM_FRACTION_SUBSAMPLE) {
                 // SUBSAMPLE without a cell list (allocation-free entry): the warp shares the samples of one cut cell
+                // (LEARNED always lists its cut cells, so its classify pass carries no sampling code)
                 for (int u = 0; u < ncut; ++u) {
                     const int e = cutlist[u];
                     const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
@@ -1233,9 +1234,11 @@ __global__ void __launch_bounds__(256) recheck_kernel(MeshK m, const SolidK* __r
 }
 
 // 3-D meshes: 4x4x4-cell tiles; one- and two-layer meshes: 8x8x2
-// one instantiation per fraction method (-1: classification only), so each kernel carries only its own path
+// one instantiation per fraction method (-1: classification only), so each kernel carries only its own path.  The
+// LEARNED pass (no fraction of its own) runs three CTAs per SM in 80 registers (ncu at 512^3: 1.45 -> 1.14 ms); the
+// REF-GEO pass, whose vertex distances need more, is faster at two (1.84 ms against 2.48 ms at three).
 template <int METHOD>
-__global__ void __launch_bounds__(CLS_WARPS * 32) classify_kernel_3d(ClassifyArgs A) { classify_body<4, 4, 4, METHOD>(A); }
+__global__ void __launch_bounds__(CLS_WARPS * 32, METHOD == SDFIBM_FRACTION_LEARNED ? 3 : 2) classify_kernel_3d(ClassifyArgs A) { classify_body<4, 4, 4, METHOD>(A); }
 template <int METHOD>
 __global__ void __launch_bounds__(CLS_WARPS * 32) classify_kernel_2d(ClassifyArgs A) { classify_body<8, 8, 2, METHOD>(A); }
 template __global__ void classify_kernel_3d<-1>(ClassifyArgs);

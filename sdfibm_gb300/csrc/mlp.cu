@@ -143,7 +143,7 @@ __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
 constexpr int INF_W1 = 0, INF_W2 = 2048, INF_A1 = 10240, INF_A2 = 18432, INF_F = 51200;
 constexpr int INF_SMEM = INF_F + 4 * 64 * 4 + 64 + 1024;
 
-__global__ void __launch_bounds__(MLP_THREADS) mlp_infer_kernel(MlpInferArgs A) {
+__global__ void __launch_bounds__(MLP_THREADS, 4) mlp_infer_kernel(MlpInferArgs A) {
     extern __shared__ uint8_t smraw[];
     uint8_t* sm = align1024(smraw);
     uint8_t *sW1 = sm + INF_W1, *sW2 = sm + INF_W2, *sA1 = sm + INF_A1, *sA2 = sm + INF_A2;
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(MLP_THREADS) mlp_infer_kernel(MlpInferArgs A) 
     float *sb2 = sb1 + 64, *sw3 = sb2 + 64, *sb3 = sw3 + 64;
     uint64_t* bar = reinterpret_cast<uint64_t*>(sb3 + 64);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tid = threadIdx.x, warp = tid >> 5;
 
     stage_weights(A.params, sW1, sW2, nullptr, sb1, sb2, sw3, sb3);
     if (tid == 0) {
@@ -170,13 +170,20 @@ __global__ void __launch_bounds__(MLP_THREADS) mlp_infer_kernel(MlpInferArgs A) 
     const int64_t n = A.n_dev ? min((int64_t)*A.n_dev, A.stride) : A.n;
     const int64_t ntiles = (n + MLP_TILE - 1) / MLP_TILE;
     uint32_t phase = 0;
-    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    // this thread's cell of a tile: inputs, prior and destination, loaded one tile ahead so that the loads of tile
+    // t + gridDim.x overlap the MMAs and the epilogues of tile t
+    float x[MLP_IN], prior = 0.f;
+    int64_t dst = -1;
+    auto load_cell = [&](int64_t t, float* xv, float& pv, int64_t& dv) {
         const int64_t c = t * MLP_TILE + tid;
-        const bool valid = c < n;
-        float x[MLP_IN];
+        const bool valid = t < ntiles && c < n;
 #pragma unroll
-        for (int f = 0; f < MLP_IN; ++f) x[f] = valid ? A.feat[f * A.stride + c] : 0.f;
-        const float prior = valid ? A.feat[MLP_IN * A.stride + c] : 0.f;
+        for (int f = 0; f < MLP_IN; ++f) xv[f] = valid ? A.feat[f * A.stride + c] : 0.f;
+        pv = valid ? A.feat[MLP_IN * A.stride + c] : 0.f;
+        dv = !valid ? -1 : (A.ref_index ? A.ref_index[c] : c);
+    };
+    load_cell(blockIdx.x, x, prior, dst);
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         store_a1(sA1, tid, x);
         tc::fence_smem_async();
         __syncthreads();
@@ -185,6 +192,9 @@ __global__ void __launch_bounds__(MLP_THREADS) mlp_infer_kernel(MlpInferArgs A) 
             issue_layer1(D1, sA1, sW1);
             tc::mma_commit(bar);
         }
+        const float prior_t = prior;
+        const int64_t dst_t = dst;
+        load_cell(t + gridDim.x, x, prior, dst);  // the next tile (sA1 holds this one's inputs)
         if (!cta_wait(bar, phase, A.error)) break;
         float z[64];
         tmem_ld64(D1, warp, 0, z);
@@ -210,10 +220,10 @@ __global__ void __launch_bounds__(MLP_THREADS) mlp_infer_kernel(MlpInferArgs A) 
             const float zz = z[j] + sb2[j];
             o += sw3[j] * (zz * sigm(zz));
         }
-        const float a = sigm(prior + o);
-        if (valid) {
-            if (!A.ref_index) A.out[c] = a;
-            else if (prior == prior) A.alpha[A.ref_index[c]] = a;  // NaN prior: outside the band (fallback)
+        const float a = sigm(prior_t + o);
+        if (dst_t >= 0) {
+            if (!A.ref_index) A.out[dst_t] = a;
+            else if (prior_t == prior_t) A.alpha[dst_t] = a;  // a NaN prior: outside the band (fallback)
         }
         tc::fence_before_sync();
         __syncthreads();

@@ -162,23 +162,15 @@ __device__ __forceinline__ int subcell_v0(int sc) {
                    : stn(2 * ((sc - 64) & 1), 2 * (((sc - 64) >> 1) & 1), 2 * ((sc - 64) >> 2));
 }
 
-// What a lane does in every cell's stencil, fixed by its lane index and computed once per kernel: the lattice
-// coordinates of its points l + 32 r, the lowest corners of its 4^3 sub-cubes l + 32 r and the stencil point of its
-// network input.
+// What a lane does in every cell's stencil, fixed by its lane index and computed once per kernel: the lowest corners
+// of its 4^3 sub-cubes l + 32 r and the stencil point of its network input.
 struct StencilLane {
-    float fi[4], fj[4], fk[4];
     int v0[2];
     int inp;
 };
 __device__ inline StencilLane stencil_lane() {
     const int lane = threadIdx.x & 31;
     StencilLane L;
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        const int p = min(lane + 32 * r, STENCIL_PTS - 1);
-        const int k = p / 25, j = (p - 25 * k) / 5, i = p - 25 * k - 5 * j;
-        L.fi[r] = (float)i; L.fj[r] = (float)j; L.fk[r] = (float)k;
-    }
 #pragma unroll
     for (int r = 0; r < 2; ++r) L.v0[r] = subcell_v0(lane + 32 * r);
     L.inp = input_point(min(lane, 14));
@@ -200,7 +192,8 @@ __device__ __forceinline__ void stencil_points(const ShapeK& sh, const StencilLa
     for (int r = 0; r < 4; ++r) {
         const int p = lane + 32 * r;
         if (p >= STENCIL_PTS) break;
-        const float fi = SL.fi[r], fj = SL.fj[r], fk = SL.fk[r];
+        const int k = p / 25, j = (p - 25 * k) / 5, i = p - 25 * k - 5 * j;
+        const float fi = (float)i, fj = (float)j, fk = (float)k;
         const float lx = __fmaf_rn(fk, Lk[0], __fmaf_rn(fj, Lj[0], __fmaf_rn(fi, Li[0], L0[0])));
         const float ly = __fmaf_rn(fk, Lk[1], __fmaf_rn(fj, Lj[1], __fmaf_rn(fi, Li[1], L0[1])));
         const float lz = __fmaf_rn(fk, Lk[2], __fmaf_rn(fj, Lj[2], __fmaf_rn(fi, Li[2], L0[2])));
