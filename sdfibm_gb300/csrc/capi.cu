@@ -720,8 +720,10 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             CA.feat_cap = ctx->feat_cap; CA.fref_solid = ctx->d_fref_solid; CA.fref_index = ctx->d_fref_index;
         }
         if (learned) {
-            // cut cells listed by the classify pass; learned_stencil_kernel computes the model's inputs
+            // cut cells listed by the classify pass; learned_stencil_kernel computes the model's inputs (the cells of
+            // solids under rho_min cells, listed from the back, go to the fallback whole)
             CA.feat_cap = ctx->feat_cap; CA.fref_solid = ctx->d_fref_solid; CA.fref_index = ctx->d_fref_index;
+            CA.rho_min = ctx->rho_min;
         }
         launch_classify(CA, ctx->mesh.nz <= 2, ctx->classify_grid, st);
         mark(ctx, "classify_kernel");
@@ -1593,7 +1595,7 @@ int sdfibm_cuda_stats(sdfibm_ctx* ctx, int64_t* out, int32_t n) {
     }
     const int64_t v[11] = {(int64_t)c.n_inside + c.n_cut, (int64_t)c.n_cut, (int64_t)c.bbox_cells,
                            (int64_t)c.exact_rechecks, (int64_t)ctx->total_chunks, (int64_t)ctx->launches_last,
-                           (int64_t)c.n_feat, (int64_t)c.n_fb, ctx->host_h2d, ctx->host_d2h,
+                           (int64_t)c.n_feat + c.n_small, (int64_t)c.n_fb + c.n_small, ctx->host_h2d, ctx->host_d2h,
                            (int64_t)ctx->host_sparse};
     for (int i = 0; i < n && i < 11; ++i) out[i] = v[i];
     return SDFIBM_OK;

@@ -830,16 +830,18 @@ template <int TX, int TY, int TZ>
 static __device__ __noinline__ void write_cut_list(const ClassifyArgs& A, const uint8_t* cutlist, int ncut, int s,
                                                    int64_t tile0, int ext0, int ext1) {
     const int lane = threadIdx.x & 31;
+    // LEARNED, a solid under rho_min cells: from the back of the list, for the fallback
+    const bool back = A.method == SDFIBM_FRACTION_LEARNED && A.plan[s].radius_cells < A.rho_min;
     for (int u0 = 0; u0 < ncut; u0 += 32) {
         int base = 0;
-        if (lane == 0) base = atomicAdd(&A.cnt->n_feat, min(32, ncut - u0));
+        if (lane == 0) base = atomicAdd(back ? &A.cnt->n_small : &A.cnt->n_feat, min(32, ncut - u0));
         base = __shfl_sync(0xffffffffu, base, 0);
         const int u = u0 + lane;
         if (u < ncut) {
             const int e = cutlist[u];
             const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
-            const int64_t slot = (int64_t)base + lane;
-            if (slot < A.feat_cap) {
+            const int64_t slot = back ? A.feat_cap - 1 - ((int64_t)base + lane) : (int64_t)base + lane;
+            if (slot >= 0 && slot < A.feat_cap) {
                 A.fref_solid[slot] = s;
                 A.fref_index[slot] = tile0 + a + (int64_t)ext0 * (b + (int64_t)ext1 * c);
             } else {
@@ -1129,7 +1131,13 @@ __global__ void __launch_bounds__(256, 4) subsample_cells_kernel(FallbackArgs A)
     __shared__ int32_t s_overflow[8];
     const int lane = threadIdx.x & 31;
     int32_t* overflow = s_overflow + ((threadIdx.x >> 5) & 7);
-    const int64_t nfb = min((int64_t)(A.fb_list ? A.cnt->n_fb : A.cnt->n_feat), A.cap);
+    // LEARNED: the band's rejects (fb_list), then the cells listed from the back; a front and a back that overlap
+    // (more cut cells than the list holds) are a capacity error
+    const int64_t n_fb = A.fb_list ? min((int64_t)A.cnt->n_fb, A.cap) : 0;
+    const int64_t n_back = A.fb_list ? (int64_t)A.cnt->n_small : 0;
+    if (A.fb_list && (int64_t)A.cnt->n_feat + n_back > A.cap && threadIdx.x == 0 && blockIdx.x == 0)
+        set_error(A.cnt, DERR_CAPACITY);
+    const int64_t nfb = A.fb_list ? min(n_fb + n_back, A.cap) : min((int64_t)A.cnt->n_feat, A.cap);
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     unsigned long long rechecks = 0;
     if (lane == 0) *overflow = 0;
@@ -1140,7 +1148,8 @@ __global__ void __launch_bounds__(256, 4) subsample_cells_kernel(FallbackArgs A)
         int s_l = 0;
         int64_t idx_l = 0;
         if (base + lane < nfb) {
-            const int32_t slot = A.fb_list ? A.fb_list[base + lane] : (int32_t)(base + lane);
+            const int64_t q = base + lane;
+            const int64_t slot = !A.fb_list ? q : (q < n_fb ? (int64_t)A.fb_list[q] : A.cap - 1 - (q - n_fb));
             s_l = A.fref_solid[slot];
             idx_l = A.fref_index[slot];
         }

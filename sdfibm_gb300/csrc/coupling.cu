@@ -992,7 +992,7 @@ __global__ void begin_kernel(Counters* cnt) {
     cnt->n_inside = 0; cnt->n_cut = 0; cnt->n_shared = 0; cnt->shared_marks = 0;
     cnt->exact_rechecks = 0; cnt->bbox_cells = 0;
     cnt->n_feat = 0; cnt->n_fb = 0; cnt->n_recheck = 0; cnt->n_ovf = 0; cnt->n_shent = 0;
-    cnt->n_inband = 0;
+    cnt->n_inband = 0; cnt->n_small = 0;
 }
 
 // F = rho_f * V / dt * sum f, T = rho_f * V / dt * sum (C - x) x f  (solidcloud.cpp:411-421)

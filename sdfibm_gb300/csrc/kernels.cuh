@@ -119,6 +119,8 @@ struct Counters {
     int32_t n_ovf;            // LEARNED: fallback cells whose points overflowed the recheck list (recount_kernel)
     int32_t n_shent;          // list entries on cells several solids claimed (shared_scan_kernel)
     int32_t n_inband;         // LEARNED: listed cut cells inside the band, compacted for the network
+    int32_t n_small;          // LEARNED: cut cells of solids under rho_min, listed from the back (fallback)
+    int32_t pad2;
 };
 
 // list lengths clamped to the capacity (a capacity error leaves the counters above what was written)
@@ -205,6 +207,9 @@ struct ClassifyArgs {
     Recheck* rq;          // deferred SUBSAMPLE rechecks (nullptr: re-evaluate in place)
     int64_t rq_cap;
     float* rg_phi;        // REF-GEO: [8][feat_cap] vertex distances of the listed cut cells (nullptr: fraction in place)
+    // LEARNED: solids whose bounding radius spans fewer cells (SolidPlan::radius_cells) list their cut cells from the
+    // back of the list (positions feat_cap - 1 - i, n_small of them): the band sends them to the fallback whole
+    float rho_min;
 };
 
 // SUBSAMPLE of listed cells: every listed cut cell (fb_list == nullptr), or the LEARNED cells left to SUBSAMPLE by
@@ -214,7 +219,8 @@ struct FallbackArgs {
     const SolidK* sk;
     const sdfibm_solid_state* st;
     const SolidPlan* plan;
-    const int32_t* fb_list;    // positions into the feature buffer (nullptr: every listed cell)
+    const int32_t* fb_list;    // positions into the feature buffer (nullptr: every listed cell); LEARNED: then the
+                               // n_small positions listed from the back
     const int32_t* fref_solid;
     const int64_t* fref_index;
     int64_t cap;

@@ -61,12 +61,15 @@ __device__ __forceinline__ void stencil_points_thread(const ShapeK& sh, const fl
     }
 }
 
-// LEARNED: the model inputs of every listed cut cell (the cell's FP32 frame built as the classify pass builds a
-// tile's): the 5^3 distance stencil in shared memory (a thread's 125 floats at an odd stride, so the threads of a
-// warp reading the same point hit distinct banks), the 64 sub-cubes of P4 sorted by the cheap test of
-// subcell_trivial with the crossed ones listed for the closed form, the 8 of P2 through the closed form, the band.
-// The in-band cells are compacted for the network (one atomic per warp, rows of consecutive cells, with their
-// fraction index in mlp_index); the others' list positions go to the fallback list.
+// LEARNED: the model inputs of every cut cell listed from the front (the solids of at least rho_min cells; the
+// classify pass lists the others' cells from the back, for the fallback), in the cell's FP32 frame built as the
+// classify pass builds a tile's: the 5^3 distance stencil in shared memory (a thread's 125 floats at an odd stride,
+// so the threads of a warp reading the same point hit distinct banks), the 64 sub-cubes of P4 sorted by the cheap
+// test of subcell_trivial with the crossed ones listed for the closed form, the 8 of P2 through the closed form, the
+// band.  (Spreading the closed forms of a warp's 32 cells over its lanes as one flat list was slower: the lanes then
+// read other threads' stencils at scattered banks.)  The in-band cells are compacted for the network (one atomic
+// per warp, rows of consecutive cells, with their fraction index in mlp_index); the others' list positions go to
+// the fallback list.
 __global__ void __launch_bounds__(STN_THREADS) learned_stencil_kernel(StencilArgs A) {
     __shared__ float s_phi[STN_THREADS][STENCIL_PTS];
     __shared__ uint8_t s_cross[64][STN_THREADS];  // [entry][thread]: a warp reading entry q reads 32 consecutive bytes
@@ -86,8 +89,7 @@ __global__ void __launch_bounds__(STN_THREADS) learned_stencil_kernel(StencilArg
             idx = A.fref_index[e];
             const SolidK& k = A.sk[s];
             const SolidPlan& pl = A.plan[s];
-            ok = pl.radius_cells >= A.rho_min;  // the solid-size half of the band: no stencil needed
-            if (ok) {
+            {
                 const uint32_t local = (uint32_t)(idx - k.scratch_off);
                 const int row = (int)fdiv(local, k.div_e0), lc = (int)fdiv(local, k.div_e01);
                 const int la = (int)local - row * k.ext[0], lb = row - lc * k.ext[1];
