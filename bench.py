@@ -48,17 +48,17 @@ ALG_BYTES = {
 # profiles/<kernel>_poly3d_256_learned.md and profiles/launches_poly3d_256_learned.md record the captures
 NCU_BYTES_PER_UNIT = {
     "couple_chunks_kernel": 121.1,  # 161.4 MB for 1,332,670 coupling cells: whole 32-byte sectors of the marked chunks
-    "classify_kernel": 1.35,        # 5.8 MB for 4,282,843 bbox cells left after the box test
-    "subsample_cells_kernel": 60.9,  # 9.4 MB for 154,364 sampled cells
-    "learned_stencil_kernel": 14.5,  # 11.0 MB for 760,774 listed cut cells
+    "classify_kernel": 0.84,        # 3.6 MB for 4,282,843 bbox cells left after the box test
+    "subsample_cells_kernel": 52.5,  # 8.1 MB for 154,364 sampled cells
+    "learned_stencil_kernel": 11.8,  # 9.0 MB for 760,774 listed cut cells
 }
 # Warp instructions per unit (ncu smsp__inst_executed.sum of one launch / its units), per (kernel, method); the
 # stencil, sampling and classification kernels are bound by instruction issue, and these counts give their issue
 # roofline
 INST_PER_UNIT = {
-    ("learned_stencil_kernel", "learned"): ("learned_cells", 539.0),  # 410.0 M for 760,774 listed cut cells
-    ("subsample_cells_kernel", "learned"): ("sampled_cells", 1709.3),  # 263.9 M for 154,364 16^3 cells
-    ("classify_kernel", "learned"): ("bbox_cells", 31.51),            # 134.9 M for 4,282,843 bbox cells
+    ("learned_stencil_kernel", "learned"): ("learned_cells", 433.7),  # 329.9 M for 760,774 listed cut cells
+    ("subsample_cells_kernel", "learned"): ("sampled_cells", 1716.3),  # 264.9 M for 154,364 16^3 cells
+    ("classify_kernel", "learned"): ("bbox_cells", 31.08),            # 133.1 M for 4,282,843 bbox cells
     ("classify_kernel", "refgeo"): ("bbox_cells", 37.82),             # 162.0 M for the same bbox cells
 }
 # FLOPs of the two tensor-core layers per predicted cell: hi and lo BF16 halves of a 16x64 and a 64x64 product

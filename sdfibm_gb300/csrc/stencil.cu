@@ -112,15 +112,36 @@ __global__ void __launch_bounds__(STN_THREADS) learned_stencil_kernel(StencilArg
                         stencil_points_thread<SDFIBM_SHAPE_BOX>(k.shape, L0, Li, Lj, Lk, inv_h, ph); break;
                     default: stencil_points_thread<0>(k.shape, L0, Li, Lj, Lk, inv_h, ph); break;
                 }
-                // P4: uncrossed sub-cubes from the cheap test, the crossed ones listed for the closed form
+                // P4: the cheap test of subcell_trivial row by row (four sub-cubes along x share the five corner
+                // columns of the row: their sums and y / z differences), the crossed ones listed for the closed form
                 float s4 = 0.f;
                 int nc = 0;
-#pragma unroll 4
-                for (int sc = 0; sc < 64; ++sc) {
-                    const int v0 = (sc & 3) + STENCIL_N * ((sc >> 2) & 3) + STENCIL_N * STENCIL_N * (sc >> 4);
-                    const int t = subcell_trivial(ph, v0, 1);
-                    if (t == 1) s4 += 1.f;
-                    else if (t < 0) s_cross[nc++][tid] = (uint8_t)v0;
+#pragma unroll 1
+                for (int r = 0; r < 16; ++r) {
+                    const int v_row = STENCIL_N * (r & 3) + STENCIL_N * STENCIL_N * (r >> 2);
+                    float sm[STENCIL_N], dy[STENCIL_N], dz[STENCIL_N];
+#pragma unroll
+                    for (int i = 0; i < STENCIL_N; ++i) {
+                        const float a = ph[v_row + i], b = ph[v_row + i + STENCIL_N],
+                                    c = ph[v_row + i + STENCIL_N * STENCIL_N],
+                                    d = ph[v_row + i + STENCIL_N * STENCIL_N + STENCIL_N];
+                        sm[i] = (a + b) + (c + d);
+                        dy[i] = (b + d) - (a + c);
+                        dz[i] = (c + d) - (a + b);
+                    }
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const float mean = 0.125f * (sm[i] + sm[i + 1]);
+                        const float half = 0.125f * (fabsf(sm[i + 1] - sm[i]) + fabsf(dy[i] + dy[i + 1]) +
+                                                     fabsf(dz[i] + dz[i + 1]));  // half the plane's |normal|_1
+                        if (!(half > 0.f)) {
+                            if (mean < 0.f) s4 += 1.f;
+                        } else if (-mean >= half) {
+                            s4 += 1.f;  // the fitted plane leaves the sub-cube inside
+                        } else if (mean < half) {
+                            s_cross[nc++][tid] = (uint8_t)(v_row + i);  // crossed: the closed form
+                        }
+                    }
                 }
                 for (int q = 0; q < nc; ++q) s4 += subcell_fraction(ph, s_cross[q][tid], 1);
                 float s2 = 0.f;
