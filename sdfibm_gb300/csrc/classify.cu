@@ -924,15 +924,10 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                     cull = cull || gap > 1e-4f * (fabsf(lc) + fabsf(pl.lbox_c[a]) + pl.lbox_s[a] + rad) + 1e-30f;
                 }
             }
-            // a partial tile at the bbox edge: its cells and vertices are walked compactly (u -> a, b, c by
-            // multiplications with 16-bit reciprocals, exact for these small counts), so that a 2x2x2 remainder takes
-            // one pass over the lanes instead of the full tile's passes
-            const int ncx = cx * cy, nce = ncx * cz;
-            const uint32_t rcx = (65536u + cx - 1) / cx, rcxy = (65536u + ncx - 1) / ncx;
             if (cull) {
-                for (int u = lane; u < nce; u += 32) {
-                    const int c = (int)((u * rcxy) >> 16), rm = u - c * ncx, b = (int)((rm * rcx) >> 16), a = rm - b * cx;
-                    out[local_index(a, b, c)] = 0;
+                for (int e = lane; e < NC; e += 32) {
+                    const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
+                    if (a < cx && b < cy && c < cz) out[local_index(a, b, c)] = 0;
                 }
                 continue;
             }
@@ -946,15 +941,12 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                           fabsf(tf.bx) + fabsf(tf.by) + fabsf(tf.bz);
                 tf.e64 = pl.e64;
             }
-            const int nvx = cx + 1, nvxy = nvx * (cy + 1), nve = nvxy * (cz + 1);
-            const uint32_t rvx = (65536u + nvx - 1) / nvx, rvxy = (65536u + nvxy - 1) / nvxy;
-            for (int u = lane; u < nve; u += 32) {
-                const int c = (int)((u * rvxy) >> 16), rm = u - c * nvxy, b = (int)((rm * rvx) >> 16), a = rm - b * nvx;
-                const int v = a + VX * (b + VY * c);
+            for (int v = lane; v < NV; v += 32) {
+                const int a = v % VX, b = (v / VX) % VY, c = v / (VX * VY);
                 const int64_t I = I0 + a, J = J0 + b, K = K0 + c;
                 uint8_t r = 0;
-                if (I >= vlo0 && I <= vhi0 && J >= vlo1 && J <= vhi1 && K >= vlo2 && K <= vhi2 && I >= 0 && J >= 0 &&
-                    K >= 0 && I <= m.nx && J <= m.ny && K <= m.nz) {
+                if (a <= cx && b <= cy && c <= cz && I >= vlo0 && I <= vhi0 && J >= vlo1 && J <= vhi1 && K >= vlo2 &&
+                    K <= vhi2 && I >= 0 && J >= 0 && K >= 0 && I <= m.nx && J <= m.ny && K <= m.nz) {
                     const float ox = (float)a * m.h32[0], oy = (float)b * m.h32[1], oz = (float)c * m.h32[2];
                     r = (uint8_t)classify_point(sh, M, tf, ox, oy, oz, m, I, J, K, 0, x, q, &rechecks);
                 }
@@ -964,12 +956,11 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
             __syncwarp();
             int ncut = 0;
 #pragma unroll 1
-            for (int base = 0; base < nce; base += 32) {
-                const int u = base + lane;
-                const int c = (int)((u * rcxy) >> 16), rm = u - c * ncx, b = (int)((rm * rcx) >> 16), a = rm - b * cx;
-                const int e = a + TX * (b + TY * c);  // the cell's index in the full tile (the cut lists' encoding)
+            for (int base = 0; base < NC; base += 32) {
+                const int e = base + lane;
+                const int a = e % TX, b = (e / TX) % TY, c = e / (TX * TY);
                 uint8_t cls = 0;
-                const bool in_tile = u < nce;
+                const bool in_tile = e < NC && a < cx && b < cy && c < cz;
                 if (in_tile) {
                     const int64_t I = I0 + a, J = J0 + b, K = K0 + c;
                     if (I >= 0 && J >= 0 && K >= 0 && I < m.nx && J < m.ny && K < m.nz) {
@@ -1011,12 +1002,9 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                 // small integer offsets from the bbox corner.
                 uint8_t* vlist = s_vlist[w];
                 int nneed = 0;
-                for (int base = 0; base < nve; base += 32) {
-                    const int u = base + lane;
-                    const int c = (int)((u * rvxy) >> 16), rm = u - c * nvxy, b = (int)((rm * rvx) >> 16),
-                              a = rm - b * nvx;
-                    const int v = a + VX * (b + VY * c);
-                    const bool need = u < nve && vneed[v];
+                for (int base = 0; base < NV; base += 32) {
+                    const int v = base + lane;
+                    const bool need = v < NV && vneed[v];
                     const unsigned bal = __ballot_sync(FULL, need);
                     if (need) vlist[nneed + __popc(bal & ((1u << lane) - 1u))] = (uint8_t)v;
                     nneed += __popc(bal);
