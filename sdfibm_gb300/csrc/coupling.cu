@@ -349,41 +349,61 @@ __global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const Sol
         R[srow * W + (sx >> 5)] |= 1u << (sx & 31);
     }
     __syncthreads();
-    // Propagation until nothing changes: each thread owns rows (j, k) and, per round, ors into every word of its row
-    // the reached words of the four rows next to it in y and z (a step in y or z), masks with the candidates and
-    // fills along x within the row (carries across words).  Every round is parallel over the rows and needs one
-    // barrier; the rows are updated in place (the reached set only grows, so a neighbour word read before or after
-    // its update in the same round is equally valid).  A shortest path moves along x within a row for free, so the
-    // rounds needed are at most the rows it visits, plus one to see that nothing changed.
-    const int max_rounds = 2 + rows;
-    volatile uint32_t* RV = R;
+    // directional sweeps until nothing changes
+    const int max_rounds = 8 + 2 * (ex + ey + ez);
     int round = 0;
     for (;; ++round) {
         int changed = 0;
+        // x: carry fill along each row
         for (int row = tid; row < rows; row += CON_THREADS) {
-            const int jj = row % ey, kk = row / ey;
+            uint32_t* r = R + row * W;
             const uint32_t* c = C + row * W;
             uint32_t carry = 0;
             for (int w = 0; w < W; ++w) {
-                const int q = row * W + w;
-                uint32_t nb = RV[q];
-                if (jj > 0) nb |= RV[q - W];
-                if (jj + 1 < ey) nb |= RV[q + W];
-                if (kk > 0) nb |= RV[q - ey * W];
-                if (kk + 1 < ez) nb |= RV[q + ey * W];
-                const uint32_t seeds = (nb | (carry & 1u)) & c[w];
+                const uint32_t seeds = (r[w] | (carry & 1u)) & c[w];
                 const uint32_t f = fill_up(c[w], seeds);
-                if (f != RV[q]) { changed = 1; RV[q] = f; }
+                if (f != r[w]) { changed = 1; r[w] = f; }
                 carry = f >> 31;
             }
             carry = 0;
             for (int w = W - 1; w >= 0; --w) {
-                const int q = row * W + w;
-                const uint32_t r = RV[q];
-                const uint32_t seeds = (r | (carry << 31)) & c[w];
+                const uint32_t seeds = (r[w] | (carry << 31)) & c[w];
                 const uint32_t f = fill_down(c[w], seeds);
-                if (f != r) { changed = 1; RV[q] = f; }
+                if (f != r[w]) { changed = 1; r[w] = f; }
                 carry = f & 1u;
+            }
+        }
+        __syncthreads();
+        // y: forward and backward scans along j for every (k, word)
+        for (int col = tid; col < ez * W; col += CON_THREADS) {
+            const int kk = col / W, w = col - kk * W;
+            uint32_t* r = R + (kk * ey) * W + w;
+            const uint32_t* c = C + (kk * ey) * W + w;
+            for (int j = 1; j < ey; ++j) {
+                const uint32_t f = r[j * W] | (r[(j - 1) * W] & c[j * W]);
+                if (f != r[j * W]) { changed = 1; r[j * W] = f; }
+            }
+            for (int j = ey - 2; j >= 0; --j) {
+                const uint32_t f = r[j * W] | (r[(j + 1) * W] & c[j * W]);
+                if (f != r[j * W]) { changed = 1; r[j * W] = f; }
+            }
+        }
+        __syncthreads();
+        // z: forward and backward scans along k for every (j, word)
+        if (ez > 1) {
+            for (int col = tid; col < ey * W; col += CON_THREADS) {
+                const int jj = col / W, w = col - jj * W;
+                uint32_t* r = R + jj * W + w;
+                const uint32_t* c = C + jj * W + w;
+                const int stride = ey * W;
+                for (int kk = 1; kk < ez; ++kk) {
+                    const uint32_t f = r[kk * stride] | (r[(kk - 1) * stride] & c[kk * stride]);
+                    if (f != r[kk * stride]) { changed = 1; r[kk * stride] = f; }
+                }
+                for (int kk = ez - 2; kk >= 0; --kk) {
+                    const uint32_t f = r[kk * stride] | (r[(kk + 1) * stride] & c[kk * stride]);
+                    if (f != r[kk * stride]) { changed = 1; r[kk * stride] = f; }
+                }
             }
         }
         changed = __syncthreads_or(changed);
