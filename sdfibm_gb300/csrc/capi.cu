@@ -788,7 +788,7 @@ static int enqueue_interact(sdfibm_ctx* ctx, double time, double dt, const float
             sa.m = ctx->mesh; sa.sk = ctx->d_sk; sa.plan = ctx->d_plan; sa.fref_solid = ctx->d_fref_solid;
             sa.fref_index = ctx->d_fref_index; sa.cap = ctx->feat_cap; sa.feat = ctx->d_feat; sa.fb_list = ctx->d_fb;
             sa.mlp_index = ctx->d_mlp_index;
-            sa.cnt = ctx->d_cnt; sa.tau_refine = ctx->tau_refine; sa.rho_min = ctx->rho_min;
+            sa.cnt = ctx->d_cnt; sa.tau_refine = ctx->tau_refine;
             learned_stencil_kernel<<<ctx->stencil_grid, stencil_block(), 0, st>>>(sa);
             mark(ctx, "learned_stencil_kernel");
             ++launches;

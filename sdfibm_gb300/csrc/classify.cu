@@ -1058,7 +1058,7 @@ __device__ __forceinline__ void classify_body(const ClassifyArgs& A) {
                 }
             } else if (A.fref_index) {
                 // SUBSAMPLE and LEARNED: the cut cells are listed; subsample_cells_kernel samples them (LEARNED:
-                // learned_stencil_kernel computes the model's inputs), a warp per cell
+                // learned_stencil_kernel computes the model's inputs, a thread per cell), a warp per cell
                 write_cut_list<TX, TY, TZ>(A, cutlist, ncut, s, k.scratch_off + local_index(0, 0, 0), k.ext[0],
                                            k.ext[1]);
             } else if (METHOD == SDFIBM_FRACTION_SUBSAMPLE) {

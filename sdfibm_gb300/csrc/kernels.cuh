@@ -246,8 +246,7 @@ struct StencilArgs {
     int32_t* fb_list;     // list positions of the cells outside the band (SUBSAMPLE fallback)
     int64_t* mlp_index;   // fraction index of each compacted in-band cell (the network's destination)
     Counters* cnt;
-    float tau_refine;     // band: |P4 - P2| limit
-    float rho_min;        // band: smallest bounding radius / h of a solid whose cells the network takes
+    float tau_refine;     // band: |P4 - P2| limit (the solid-size half, rho_min, is applied by the classify pass)
 };
 
 // UGrid (src/libcollision/ugrid.h:14-58): bbox of the mesh, spacing 2*max radiusB, row-major i*ny*nz + j*nz + k

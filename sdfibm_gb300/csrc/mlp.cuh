@@ -216,7 +216,8 @@ __device__ __forceinline__ void stencil_points(const ShapeK& sh, const StencilLa
     }
 }
 
-// The model inputs of one cell, computed by all 32 lanes of a warp together.  The cell's frame: lattice point
+// The model inputs of one cell, computed by all 32 lanes of a warp together (the training cells of mlp.cu; the
+// coupling path computes the same quantities a thread per cell in stencil.cu).  The cell's frame: lattice point
 // (i, j, k) lies at world offset (bx + i*qx, by + j*qy, bz + k*qz) from the solid centre (q = h/4 per axis, FP32), its
 // local coordinates are M times that offset.  sphi: 125 floats and slist: 72 bytes of shared memory of this warp.
 // Every lane returns P4 and P2 (unclamped); lane f < 16 returns input f in *feat, lane 16 the prior logit(clamp(P4)).
@@ -283,7 +284,8 @@ __device__ inline StencilOut cell_stencil(const ShapeK& sh, const StencilLane& S
 
 // Confidence band: the network's answer is kept where the two planar reconstructions agree (|P4 - P2| at most
 // tau_refine: the sub-cell planes resolve the surface) and the solid spans at least rho_min cells (bounding radius /
-// h, tested before the stencil); other cells take the SUBSAMPLE fallback.
+// h, tested by the classify pass, which lists the other solids' cells for the fallback); other cells take the
+// SUBSAMPLE fallback.
 __device__ __forceinline__ bool in_band(float p4, float p2, float tau_refine) {
     return fabsf(clamp_frac(p4) - clamp_frac(p2)) <= tau_refine;
 }

@@ -18,12 +18,13 @@ namespace sdfibm_dev {
 constexpr int STN_THREADS = 64;
 int stencil_block() { return STN_THREADS; }
 
-// Shape::signedDistance / h at the 125 lattice points of one cell (local coordinates L0 + i Li + j Lj + k Lk): the
-// 3-D shapes of the coupling workloads with the hardware's approximate square root and reciprocal, any other shape
-// through sdf32.  ph: this thread's 125 floats.
+// Shape::signedDistance at the 125 lattice points of one cell (local coordinates L0 + i Li + j Lj + k Lk), in world
+// units: the sub-cube fractions do not depend on the scale, and the 15 network inputs are divided by h when they are
+// written.  The 3-D shapes of the coupling workloads with the hardware's approximate square root and reciprocal, any
+// other shape through sdf32.  ph: this thread's 125 floats.
 template <int TYPE>
 __device__ __forceinline__ void stencil_points_thread(const ShapeK& sh, const float* L0, const float* Li,
-                                                      const float* Lj, const float* Lk, float inv_h, float* ph) {
+                                                      const float* Lj, const float* Lk, float* ph) {
     const float* a = sh.p32;
     const float c0 = sh.com32[0], c1 = sh.com32[1], c2 = sh.com32[2];
 #pragma unroll 1
@@ -55,7 +56,7 @@ __device__ __forceinline__ void stencil_points_thread(const ShapeK& sh, const fl
                 } else {
                     phi = sdf32(sh, lx, ly, lz);
                 }
-                ph[stn(i, j, k)] = phi * inv_h;
+                ph[stn(i, j, k)] = phi;
             }
         }
     }
@@ -105,12 +106,12 @@ __global__ void __launch_bounds__(STN_THREADS) learned_stencil_kernel(StencilArg
                             Lk[3] = {M[2] * qz, M[5] * qz, M[8] * qz};
                 switch (k.shape.type) {
                     case SDFIBM_SHAPE_SPHERE:
-                        stencil_points_thread<SDFIBM_SHAPE_SPHERE>(k.shape, L0, Li, Lj, Lk, inv_h, ph); break;
+                        stencil_points_thread<SDFIBM_SHAPE_SPHERE>(k.shape, L0, Li, Lj, Lk, ph); break;
                     case SDFIBM_SHAPE_ELLIPSOID:
-                        stencil_points_thread<SDFIBM_SHAPE_ELLIPSOID>(k.shape, L0, Li, Lj, Lk, inv_h, ph); break;
+                        stencil_points_thread<SDFIBM_SHAPE_ELLIPSOID>(k.shape, L0, Li, Lj, Lk, ph); break;
                     case SDFIBM_SHAPE_BOX:
-                        stencil_points_thread<SDFIBM_SHAPE_BOX>(k.shape, L0, Li, Lj, Lk, inv_h, ph); break;
-                    default: stencil_points_thread<0>(k.shape, L0, Li, Lj, Lk, inv_h, ph); break;
+                        stencil_points_thread<SDFIBM_SHAPE_BOX>(k.shape, L0, Li, Lj, Lk, ph); break;
+                    default: stencil_points_thread<0>(k.shape, L0, Li, Lj, Lk, ph); break;
                 }
                 // P4: the cheap test of subcell_trivial row by row (four sub-cubes along x share the five corner
                 // columns of the row: their sums and y / z differences), the crossed ones listed for the closed form
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(STN_THREADS) learned_stencil_kernel(StencilArg
         if (in) {
             const int64_t pos = p0 + __popc(mask & below);  // n_inband <= n <= cap
 #pragma unroll
-            for (int f = 0; f < 15; ++f) A.feat[f * A.cap + pos] = ph[input_point(f)];
+            for (int f = 0; f < 15; ++f) A.feat[f * A.cap + pos] = ph[input_point(f)] * inv_h;
             A.feat[15 * A.cap + pos] = logit_frac(clamp_frac(p2));
             A.feat[16 * A.cap + pos] = logit_frac(clamp_frac(p4));
             A.mlp_index[pos] = idx;
