@@ -47,7 +47,7 @@ ALG_BYTES = {
 # 256^3 / 2048-solid learned workload (the full-size workload's distribution at half scale per axis);
 # profiles/<kernel>_poly3d_256_learned.md and profiles/launches_poly3d_256_learned.md record the captures
 NCU_BYTES_PER_UNIT = {
-    "couple_chunks_kernel": 121.1,  # 161.4 MB for 1,332,670 coupling cells: whole 32-byte sectors of the marked chunks
+    "couple_chunks_kernel": 121.3,  # 161.6 MB for 1,332,670 coupling cells: whole 32-byte sectors of the marked chunks
     "classify_kernel": 0.84,        # 3.6 MB for 4,282,843 bbox cells left after the box test
     "subsample_cells_kernel": 52.5,  # 8.1 MB for 154,364 sampled cells
     "learned_stencil_kernel": 11.8,  # 9.0 MB for 760,774 listed cut cells
@@ -56,7 +56,7 @@ NCU_BYTES_PER_UNIT = {
 # stencil, sampling and classification kernels are bound by instruction issue, and these counts give their issue
 # roofline
 INST_PER_UNIT = {
-    ("learned_stencil_kernel", "learned"): ("learned_cells", 433.7),  # 329.9 M for 760,774 listed cut cells
+    ("learned_stencil_kernel", "learned"): ("learned_cells", 373.0),  # 283.8 M for 760,774 listed cut cells
     ("subsample_cells_kernel", "learned"): ("sampled_cells", 1716.3),  # 264.9 M for 154,364 16^3 cells
     ("classify_kernel", "learned"): ("bbox_cells", 31.08),            # 133.1 M for 4,282,843 bbox cells
     ("classify_kernel", "refgeo"): ("bbox_cells", 37.82),             # 162.0 M for the same bbox cells
