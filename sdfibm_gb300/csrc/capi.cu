@@ -407,7 +407,9 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
     int64_t scratch = 0, gwords = 0, bbox_total = 0;
     int64_t tiles = 0;
     int max_smem_words = 0;
-    const int SMEM_CAP_BYTES = 200 * 1024;
+    // the flood fill's bitmaps stay in shared memory up to this size (every CTA of the launch reserves the largest, so
+    // the cap keeps two 512-thread CTAs per SM); larger ones live in global memory
+    const int SMEM_CAP_BYTES = 96 * 1024;
     for (int s = 0; s < nsolids; ++s) {
         const sdfibm_solid_desc& d = solids[s];
         SolidK& k = ctx->hk[s];
@@ -455,8 +457,9 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
         k.scratch_off = scratch;
         scratch += (cells + 15) & ~(int64_t)15;
         bbox_total += std::min<int64_t>(cells, N);
-        const int64_t words = 2 * (int64_t)k.ext[1] * k.ext[2] * ((k.ext[0] + 31) / 32);
-        if (words / 2 <= 256) {
+        // connect_kernel: four bitmaps (candidates, reached, inside, centre inside) of ext[1] * ext[2] rows
+        const int64_t words = 4 * (int64_t)k.ext[1] * k.ext[2] * ((k.ext[0] + 31) / 32);
+        if (words / 4 <= 256) {
             small_solids.push_back(s);  // warp-per-solid flood fill (connect_small_kernel)
         } else if (words * 4 > SMEM_CAP_BYTES) {
             k.bitmap_global = 1;

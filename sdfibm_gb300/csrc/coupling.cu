@@ -317,8 +317,10 @@ __global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const Sol
     const int W = (ex + 31) >> 5;
     const int rows = ey * ez;
     const int nwords = rows * W;
-    uint32_t* C = k.bitmap_global ? gbitmaps + k.bitmap_off : dsm;
-    uint32_t* R = C + nwords;
+    uint32_t* C = k.bitmap_global ? gbitmaps + k.bitmap_off : dsm;  // candidates (class != 0)
+    uint32_t* R = C + nwords;                                        // reached
+    uint32_t* I = R + nwords;                                        // class 1 (all inside)
+    uint32_t* T = I + nwords;                                        // class 2 (centre inside)
     const uint8_t* cls = scratch + k.scratch_off;
     if (pl.err) {
         if (tid == 0) { pl.n_inside = 0; pl.n_cut = 0; }
@@ -333,15 +335,30 @@ __global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const Sol
         if (tid == 0) { pl.n_inside = 0; pl.n_cut = 0; }
         return;
     }
-    // candidate and reached bitmaps
-    for (int w = tid; w < nwords; w += CON_THREADS) {
-        const int row = w / W, wi = w - row * W;
-        const uint8_t* rp = cls + (int64_t)row * ex;
-        uint32_t bits = 0;
-        const int x0 = wi << 5, x1 = min(ex, x0 + 32);
-        for (int xx = x0; xx < x1; ++xx) bits |= (rp[xx] ? 1u : 0u) << (xx - x0);
-        C[w] = bits;
-        R[w] = 0;
+    // the bitmaps from the class bytes: a warp per group of four words, each word one coalesced 32-byte load and
+    // three ballots (the emission below then reads no class byte again)
+    {
+        const int lane = tid & 31;
+        for (int w0 = (tid >> 5) * 4; w0 < nwords; w0 += CON_THREADS / 32 * 4) {
+            uint8_t v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int w = w0 + u;
+                const int row = w / W, xx = ((w - row * W) << 5) + lane;
+                v[u] = (w < nwords && xx < ex) ? cls[(int64_t)row * ex + xx] : (uint8_t)0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t bc = __ballot_sync(0xffffffffu, v[u] != 0), bi = __ballot_sync(0xffffffffu, v[u] == 1),
+                               bt = __ballot_sync(0xffffffffu, v[u] == 2);
+                if (lane == 0 && w0 + u < nwords) {
+                    C[w0 + u] = bc;
+                    I[w0 + u] = bi;
+                    T[w0 + u] = bt;
+                    R[w0 + u] = 0;
+                }
+            }
+        }
     }
     __syncthreads();
     if (tid == 0) {
@@ -419,13 +436,9 @@ __global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const Sol
     int nin = 0, ncut = 0;
     for (int row = r0; row < r1; ++row)
         for (int w = 0; w < W; ++w) {
-            uint32_t bits = R[row * W + w];
-            while (bits) {
-                const int b = __ffs(bits) - 1;
-                bits &= bits - 1;
-                const uint8_t cc = cls[(int64_t)row * ex + (w << 5) + b];
-                if (cc == 1) ++nin; else ++ncut;
-            }
+            const uint32_t bits = R[row * W + w], in = I[row * W + w];
+            nin += __popc(bits & in);
+            ncut += __popc(bits & ~in);
         }
     int tot_in, tot_cut;
     const int off_in = block_excl_scan(nin, warp_sums, tot_in);
@@ -447,11 +460,12 @@ __global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const Sol
         const int jj = row % ey, kk = row / ey;
         for (int w = 0; w < W; ++w) {
             uint32_t bits = R[row * W + w];
+            const uint32_t in = I[row * W + w], ci = T[row * W + w];
             while (bits) {
                 const int b = __ffs(bits) - 1;
                 bits &= bits - 1;
                 const int xx = (w << 5) + b;
-                const uint8_t cc = cls[(int64_t)row * ex + xx];
+                const uint8_t cc = ((in >> b) & 1u) ? 1 : (((ci >> b) & 1u) ? 2 : 3);
                 const int64_t gi = pl.lo[0] + xx, gj = pl.lo[1] + jj, gk = pl.lo[2] + kk;
                 const int32_t cell = (int32_t)(gi + (int64_t)m.nx * (gj + (int64_t)m.ny * gk));
                 if (cc == 1) { in_cell[pin] = cell; in_solid[pin] = list_word(s, 1); ++pin; }
