@@ -396,13 +396,17 @@ __global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const Sol
             const int kk = col / W, w = col - kk * W;
             uint32_t* r = R + (kk * ey) * W + w;
             const uint32_t* c = C + (kk * ey) * W + w;
+            // the running value stays in a register: the loads of r and c do not depend on the previous step
+            uint32_t prev = r[0];
             for (int j = 1; j < ey; ++j) {
-                const uint32_t f = r[j * W] | (r[(j - 1) * W] & c[j * W]);
-                if (f != r[j * W]) { changed = 1; r[j * W] = f; }
+                const uint32_t cur = r[j * W], f = cur | (prev & c[j * W]);
+                if (f != cur) { changed = 1; r[j * W] = f; }
+                prev = f;
             }
             for (int j = ey - 2; j >= 0; --j) {
-                const uint32_t f = r[j * W] | (r[(j + 1) * W] & c[j * W]);
-                if (f != r[j * W]) { changed = 1; r[j * W] = f; }
+                const uint32_t cur = r[j * W], f = cur | (prev & c[j * W]);
+                if (f != cur) { changed = 1; r[j * W] = f; }
+                prev = f;
             }
         }
         __syncthreads();
@@ -413,13 +417,16 @@ __global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const Sol
                 uint32_t* r = R + jj * W + w;
                 const uint32_t* c = C + jj * W + w;
                 const int stride = ey * W;
+                uint32_t prev = r[0];
                 for (int kk = 1; kk < ez; ++kk) {
-                    const uint32_t f = r[kk * stride] | (r[(kk - 1) * stride] & c[kk * stride]);
-                    if (f != r[kk * stride]) { changed = 1; r[kk * stride] = f; }
+                    const uint32_t cur = r[kk * stride], f = cur | (prev & c[kk * stride]);
+                    if (f != cur) { changed = 1; r[kk * stride] = f; }
+                    prev = f;
                 }
                 for (int kk = ez - 2; kk >= 0; --kk) {
-                    const uint32_t f = r[kk * stride] | (r[(kk + 1) * stride] & c[kk * stride]);
-                    if (f != r[kk * stride]) { changed = 1; r[kk * stride] = f; }
+                    const uint32_t cur = r[kk * stride], f = cur | (prev & c[kk * stride]);
+                    if (f != cur) { changed = 1; r[kk * stride] = f; }
+                    prev = f;
                 }
             }
         }
@@ -552,13 +559,17 @@ __global__ void __launch_bounds__(CON_SMALL_WARPS * 32) connect_small_kernel(
             const int kk = col / W, w = col - kk * W;
             uint32_t* r = R + (kk * ey) * W + w;
             const uint32_t* c = C + (kk * ey) * W + w;
+            // the running value stays in a register: the loads of r and c do not depend on the previous step
+            uint32_t prev = r[0];
             for (int j = 1; j < ey; ++j) {
-                const uint32_t f = r[j * W] | (r[(j - 1) * W] & c[j * W]);
-                if (f != r[j * W]) { changed = 1; r[j * W] = f; }
+                const uint32_t cur = r[j * W], f = cur | (prev & c[j * W]);
+                if (f != cur) { changed = 1; r[j * W] = f; }
+                prev = f;
             }
             for (int j = ey - 2; j >= 0; --j) {
-                const uint32_t f = r[j * W] | (r[(j + 1) * W] & c[j * W]);
-                if (f != r[j * W]) { changed = 1; r[j * W] = f; }
+                const uint32_t cur = r[j * W], f = cur | (prev & c[j * W]);
+                if (f != cur) { changed = 1; r[j * W] = f; }
+                prev = f;
             }
         }
         __syncwarp();
@@ -568,13 +579,16 @@ __global__ void __launch_bounds__(CON_SMALL_WARPS * 32) connect_small_kernel(
                 uint32_t* r = R + jj * W + w;
                 const uint32_t* c = C + jj * W + w;
                 const int stride = ey * W;
+                uint32_t prev = r[0];
                 for (int kk = 1; kk < ez; ++kk) {
-                    const uint32_t f = r[kk * stride] | (r[(kk - 1) * stride] & c[kk * stride]);
-                    if (f != r[kk * stride]) { changed = 1; r[kk * stride] = f; }
+                    const uint32_t cur = r[kk * stride], f = cur | (prev & c[kk * stride]);
+                    if (f != cur) { changed = 1; r[kk * stride] = f; }
+                    prev = f;
                 }
                 for (int kk = ez - 2; kk >= 0; --kk) {
-                    const uint32_t f = r[kk * stride] | (r[(kk + 1) * stride] & c[kk * stride]);
-                    if (f != r[kk * stride]) { changed = 1; r[kk * stride] = f; }
+                    const uint32_t cur = r[kk * stride], f = cur | (prev & c[kk * stride]);
+                    if (f != cur) { changed = 1; r[kk * stride] = f; }
+                    prev = f;
                 }
             }
         }
