@@ -335,20 +335,21 @@ __global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const Sol
         if (tid == 0) { pl.n_inside = 0; pl.n_cut = 0; }
         return;
     }
-    // the bitmaps from the class bytes: a warp per group of four words, each word one coalesced 32-byte load and
-    // three ballots (the emission below then reads no class byte again)
+    // the bitmaps from the class bytes: a warp per group of eight words (eight independent loads in flight per lane),
+    // each word one coalesced 32-byte load and three ballots (the emission below then reads no class byte again)
     {
         const int lane = tid & 31;
-        for (int w0 = (tid >> 5) * 4; w0 < nwords; w0 += CON_THREADS / 32 * 4) {
-            uint8_t v[4];
+        constexpr int GW = 8;
+        for (int w0 = (tid >> 5) * GW; w0 < nwords; w0 += CON_THREADS / 32 * GW) {
+            uint8_t v[GW];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < GW; ++u) {
                 const int w = w0 + u;
                 const int row = w / W, xx = ((w - row * W) << 5) + lane;
                 v[u] = (w < nwords && xx < ex) ? cls[(int64_t)row * ex + xx] : (uint8_t)0;
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < GW; ++u) {
                 const uint32_t bc = __ballot_sync(0xffffffffu, v[u] != 0), bi = __ballot_sync(0xffffffffu, v[u] == 1),
                                bt = __ballot_sync(0xffffffffu, v[u] == 2);
                 if (lane == 0 && w0 + u < nwords) {
