@@ -297,7 +297,7 @@ __device__ inline int seed_local(const MeshK& m, const SolidPlan& pl, const uint
     return sl;
 }
 
-__global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const SolidK* __restrict__ sk,
+__global__ void __launch_bounds__(CON_THREADS, 2) connect_kernel(MeshK m, const SolidK* __restrict__ sk,
                                                               SolidPlan* __restrict__ plan,
                                                               const uint8_t* __restrict__ scratch,
                                                               uint32_t* __restrict__ gbitmaps,
@@ -335,11 +335,11 @@ __global__ void __launch_bounds__(CON_THREADS) connect_kernel(MeshK m, const Sol
         if (tid == 0) { pl.n_inside = 0; pl.n_cut = 0; }
         return;
     }
-    // the bitmaps from the class bytes: a warp per group of eight words (eight independent loads in flight per lane),
+    // the bitmaps from the class bytes: a warp per group of 16 words (16 independent loads in flight per lane),
     // each word one coalesced 32-byte load and three ballots (the emission below then reads no class byte again)
     {
         const int lane = tid & 31;
-        constexpr int GW = 8;
+        constexpr int GW = 16;
         for (int w0 = (tid >> 5) * GW; w0 < nwords; w0 += CON_THREADS / 32 * GW) {
             uint8_t v[GW];
 #pragma unroll
