@@ -591,7 +591,7 @@ def main():
         a12 = accuracy(torch, w, plain12, U, ref)
         plain12.close()
         del f12
-        # the plain path at the learned path's accuracy: SUBSAMPLE 16^3, the judge's own lattice (against the
+        # the plain path at the learned path's accuracy: SUBSAMPLE 16^3, the accuracy reference's own lattice (against the
         # converged 32^3 lattice below, learned and plain 16^3 carry the same As and force errors)
         plain16 = make_cloud(w, "subsample", subsample_n=16, stream=stream)
         with torch.cuda.stream(stream):
@@ -626,7 +626,7 @@ def main():
             c2.close()
             del f2
         # every method against a converged lattice (SUBSAMPLE 32^3, 32768 samples per cut cell): how close each is
-        # to the true solid fraction, beside the contract's 16^3 judge
+        # to the true solid fraction, beside the contract's 16^3 reference
         conv = converged(torch, w, U, {"learned": cloud, "plain_10": ("subsample", 10),
                                        "plain_12": ("subsample", 12), "plain_16": ("subsample", 16)})
         del ref
@@ -640,7 +640,7 @@ def main():
                    "plain_12": dict({"method": "SUBSAMPLE 12^3 samples per cut cell", "ms_per_step": t12["ms_step"],
                                      "value": t12["cells"] * world / (t12["ms_step"] * 1e-3)}, **pick(a12)),
                    "speedup_vs_plain_12": t12["ms_step"] / tm["ms_step"],
-                   "plain_16": {"method": "SUBSAMPLE 16^3 samples per cut cell (the accuracy judge's lattice)",
+                   "plain_16": {"method": "SUBSAMPLE 16^3 samples per cut cell (the accuracy reference's lattice)",
                                 "ms_per_step": t16["ms_step"], "value": t16["cells"] * world / (t16["ms_step"] * 1e-3)},
                    "speedup_vs_plain_16": t16["ms_step"] / tm["ms_step"],
                    "learned_cells": st.get("learned_cells"), "fallback_cells": st.get("learned_fallback_cells"),

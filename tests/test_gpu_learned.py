@@ -1,12 +1,12 @@
 """Coupling with the learned cut-cell fraction (options.fraction_method = LEARNED) against the FP64 oracle running
 SUBSAMPLE with the 16^3 lattice the model is trained on and falls back to.
 
-Gates of the shipped model (the learned path's contract; the oracle's 16^3 lattice is the judge):
+Gates of the shipped model (the learned path's contract; the oracle's 16^3 lattice is the reference):
   * As, mean absolute error over the cut cells <= 1e-3 (the target's bar), 99th percentile <= 1e-2;
   * per-solid force, normwise: median <= 1e-4; 90th percentile <= 1e-4 on the benchmarked workload (16384 solids,
     test_trained_model_full_size), <= 1e-3 on the small scaled workloads, where 32 to 64 solids make the percentile
     a statement about two or three solids.
-The mean and the median are the gated statistics because the judge itself is a lattice count: its own error against
+The mean and the median are the gated statistics because the reference itself is a lattice count: its own error against
 the converged fraction is about 6e-4 per cut cell (mean), with a tail, so no smooth estimate meets 1e-3 in every
 cell, and a per-solid force bar of 1e-4 at the 90th percentile is below the 16^3 lattice's own noise for solids of
 one or two cells' radius (the bench reports every quantile against 16^3 and against a converged 32^3 lattice).
