@@ -656,7 +656,7 @@ int sdfibm_cuda_create(const sdfibm_mesh_desc* mesh, const sdfibm_solid_desc* so
     ctx->couple_grid = std::max(1, occ) * ctx->num_sms;
     ctx->couple_occ = std::max(1, occ);
     ctx->subsample_grid = 8 * ctx->num_sms;
-    ctx->mlp_grid = 4 * ctx->num_sms;
+    ctx->mlp_grid = 5 * ctx->num_sms;  // mlp_infer_kernel: five CTAs per SM (shared memory, tensor memory, registers)
     ctx->refgeo_grid = 8 * ctx->num_sms;
     occ = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, learned_stencil_kernel, stencil_block(), 0);
@@ -1476,7 +1476,7 @@ int sdfibm_cuda_autotune(sdfibm_ctx* ctx, double dt, const float* U, float* As, 
     for (int k = 1; k <= ctx->couple_occ; k *= 2) cpl_cand.push_back(k * sms);
     if (cpl_cand.back() != ctx->couple_occ * sms) cpl_cand.push_back(ctx->couple_occ * sms);
     const std::vector<int> sub_cand = {2 * sms, 4 * sms, 8 * sms, 16 * sms};
-    const std::vector<int> mlp_cand = {1 * sms, 2 * sms, 4 * sms, 8 * sms};
+    const std::vector<int> mlp_cand = {1 * sms, 2 * sms, 5 * sms, 10 * sms};
     const std::vector<int> rg_cand = {2 * sms, 4 * sms, 8 * sms, 16 * sms};
     const int saved_timing = ctx->opt.timing;
     ctx->opt.timing = 1;

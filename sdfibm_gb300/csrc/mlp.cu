@@ -46,6 +46,11 @@ __device__ __forceinline__ void tmem_ld64(uint32_t base, int warp, int col, floa
     for (int j = 0; j < 4; ++j) tc::tmem_ld16(tc::tmem_addr(base, 32 * warp, col + 16 * j), v + 16 * j);
     tc::tmem_wait_ld();
 }
+__device__ __forceinline__ void tmem_ld32(uint32_t base, int warp, int col, float* v) {
+    tc::tmem_ld16(tc::tmem_addr(base, 32 * warp, col), v);
+    tc::tmem_ld16(tc::tmem_addr(base, 32 * warp, col + 16), v + 16);
+    tc::tmem_wait_ld();
+}
 
 // Stages W1 (BF16, K padded to 16) and W2 (BF16) as B operands, and the FP32 vectors.
 __device__ void stage_weights(const float* P, uint8_t* sW1, uint8_t* sW2, uint8_t* sW2T, float* sb1, float* sb2,
@@ -91,15 +96,17 @@ __device__ __forceinline__ void store_a1(uint8_t* sA1, int row, const float* x) 
     *reinterpret_cast<uint4*>(sA1 + tc::kmajor_offset(row, 24, 32)) = l1;
 }
 
-// A2 row: hi of h1 in K 0..63, lo in K 64..127
-__device__ __forceinline__ void store_a2(uint8_t* sA2, int row, const float* h) {
+// A2 row: hi of h1 in K 0..63, lo in K 64..127; h holds the units 8 * g0 .. 8 * (g0 + NG) - 1
+template <int NG = 8>
+__device__ __forceinline__ void store_a2(uint8_t* sA2, int row, const float* h, int g0 = 0) {
 #pragma unroll
-    for (int g = 0; g < 8; ++g) {
+    for (int i = 0; i < NG; ++i) {
+        const int g = g0 + i;
         uint4 hw, lw;
-        split2(h[8 * g], h[8 * g + 1], hw.x, lw.x);
-        split2(h[8 * g + 2], h[8 * g + 3], hw.y, lw.y);
-        split2(h[8 * g + 4], h[8 * g + 5], hw.z, lw.z);
-        split2(h[8 * g + 6], h[8 * g + 7], hw.w, lw.w);
+        split2(h[8 * i], h[8 * i + 1], hw.x, lw.x);
+        split2(h[8 * i + 2], h[8 * i + 3], hw.y, lw.y);
+        split2(h[8 * i + 4], h[8 * i + 5], hw.z, lw.z);
+        split2(h[8 * i + 6], h[8 * i + 7], hw.w, lw.w);
         *reinterpret_cast<uint4*>(sA2 + tc::kmajor_offset(row, 8 * g, 128)) = hw;
         *reinterpret_cast<uint4*>(sA2 + tc::kmajor_offset(row, 64 + 8 * g, 128)) = lw;
     }
@@ -140,10 +147,13 @@ __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
 }
 
 // ---- inference -----------------------------------------------------------------------------------------------------
-constexpr int INF_W1 = 0, INF_W2 = 2048, INF_A1 = 10240, INF_A2 = 18432, INF_F = 51200;
+// The layer-1 operand A1 lives in the first 8 KB of the layer-2 operand A2 (A2 is written only after the layer-1 MMA
+// has completed, and A1 only after the layer-2 MMA has), and D2 takes D1's tensor-memory columns (the layer-2 MMA is
+// issued after every thread has read D1): 45 KB of shared memory and 64 columns per CTA, five CTAs per SM.
+constexpr int INF_W1 = 0, INF_W2 = 2048, INF_A2 = 10240, INF_A1 = INF_A2, INF_F = INF_A2 + 32768;
 constexpr int INF_SMEM = INF_F + 4 * 64 * 4 + 64 + 1024;
 
-__global__ void __launch_bounds__(MLP_THREADS, 4) mlp_infer_kernel(MlpInferArgs A) {
+__global__ void __launch_bounds__(MLP_THREADS, 5) mlp_infer_kernel(MlpInferArgs A) {
     extern __shared__ uint8_t smraw[];
     uint8_t* sm = align1024(smraw);
     uint8_t *sW1 = sm + INF_W1, *sW2 = sm + INF_W2, *sA1 = sm + INF_A1, *sA2 = sm + INF_A2;
@@ -159,14 +169,14 @@ __global__ void __launch_bounds__(MLP_THREADS, 4) mlp_infer_kernel(MlpInferArgs 
         tc::fence_mbar_init();
     }
     if (warp == 0) {
-        tc::tmem_alloc(tslot, 128);
+        tc::tmem_alloc(tslot, 64);
         tc::tmem_relinquish();
     }
     tc::fence_smem_async();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tbase = *tslot, D1 = tbase, D2 = tbase + 64;
+    const uint32_t tbase = *tslot, D1 = tbase, D2 = tbase;
     const int64_t n = A.n_dev ? min((int64_t)*A.n_dev, A.stride) : A.n;
     const int64_t ntiles = (n + MLP_TILE - 1) / MLP_TILE;
     uint32_t phase = 0;
@@ -196,14 +206,18 @@ __global__ void __launch_bounds__(MLP_THREADS, 4) mlp_infer_kernel(MlpInferArgs 
         const int64_t dst_t = dst;
         load_cell(t + gridDim.x, x, prior, dst);  // the next tile (sA1 holds this one's inputs)
         if (!cta_wait(bar, phase, A.error)) break;
-        float z[64];
-        tmem_ld64(D1, warp, 0, z);
+        // the epilogues take half a row (32 units) at a time: five CTAs per SM leave 96 registers a thread
 #pragma unroll
-        for (int j = 0; j < 64; ++j) {
-            const float zz = z[j] + sb1[j];
-            z[j] = zz * sigm(zz);
+        for (int half = 0; half < 2; ++half) {
+            float z[32];
+            tmem_ld32(D1, warp, 32 * half, z);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const float zz = z[j] + sb1[32 * half + j];
+                z[j] = zz * sigm(zz);
+            }
+            store_a2<4>(sA2, tid, z, 4 * half);
         }
-        store_a2(sA2, tid, z);
         tc::fence_before_sync();
         tc::fence_smem_async();
         __syncthreads();
@@ -213,12 +227,16 @@ __global__ void __launch_bounds__(MLP_THREADS, 4) mlp_infer_kernel(MlpInferArgs 
             tc::mma_commit(bar);
         }
         if (!cta_wait(bar, phase, A.error)) break;
-        tmem_ld64(D2, warp, 0, z);
         float o = *sb3;
 #pragma unroll
-        for (int j = 0; j < 64; ++j) {
-            const float zz = z[j] + sb2[j];
-            o += sw3[j] * (zz * sigm(zz));
+        for (int half = 0; half < 2; ++half) {
+            float z[32];
+            tmem_ld32(D2, warp, 32 * half, z);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const float zz = z[j] + sb2[32 * half + j];
+                o += sw3[32 * half + j] * (zz * sigm(zz));
+            }
         }
         const float a = sigm(prior_t + o);
         if (dst_t >= 0) {
@@ -230,7 +248,7 @@ __global__ void __launch_bounds__(MLP_THREADS, 4) mlp_infer_kernel(MlpInferArgs 
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tbase, 128);
+    if (warp == 0) tc::tmem_dealloc(tbase, 64);
 }
 
 // ---- training: forward + backward of one batch, weight gradients accumulated in tensor memory -------------------------
