@@ -1136,9 +1136,16 @@ __global__ void mark_all_kernel(uint32_t* __restrict__ dirty, int64_t words) {
         dirty[w] = 0xffffffffu;
 }
 
-__global__ void export64_kernel(Counters* cnt, int64_t N, uint32_t* __restrict__ dirty, const float* __restrict__ As,
-                                const float* __restrict__ Fs, const float* __restrict__ Ts,
-                                const int32_t* __restrict__ Ct, double* hAs, double* hFs, double* hTs, double* hCt) {
+// A warp per bitmap word (256 cells, 32 chunks).  An FP64 chunk of a scalar field is 64 bytes and of Fs 192 bytes,
+// whole host cache lines: the scalar fields go out one cell per lane, Fs as the interleaved x,y,z sequence of the
+// word's cells, element e of it at lane e mod 32, so that every store instruction writes 256 contiguous bytes (a lane
+// per cell and a store per component would leave each instruction a third of each line).  The device values of a
+// group of stores are loaded before the first of them.
+__global__ void __launch_bounds__(256, 3) export64_kernel(Counters* cnt, int64_t N, uint32_t* __restrict__ dirty,
+                                                      const float* __restrict__ As, const float* __restrict__ Fs,
+                                                      const float* __restrict__ Ts, const int32_t* __restrict__ Ct,
+                                                      double* __restrict__ hAs, double* __restrict__ hFs,
+                                                      double* __restrict__ hTs, double* __restrict__ hCt) {
     const int lane = threadIdx.x & 31;
     const int64_t words = (N + 32 * EXPORT_CHUNK - 1) >> (EXPORT_LG + 5);
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -1147,17 +1154,45 @@ __global__ void export64_kernel(Counters* cnt, int64_t N, uint32_t* __restrict__
         const uint32_t word = dirty[w];
         if (!word) continue;
         chunks += __popc(word);
+        const int64_t base = w << (EXPORT_LG + 5);
+        {
+            float a[EXPORT_CHUNK], t[EXPORT_CHUNK];
+            int32_t k[EXPORT_CHUNK];
+            bool on[EXPORT_CHUNK];
 #pragma unroll
-        for (int t = 0; t < EXPORT_CHUNK; ++t) {
-            const int64_t c = (w << (EXPORT_LG + 5)) + 32 * t + lane;
-            if (((word >> ((32 * t + lane) >> EXPORT_LG)) & 1u) && c < N) {
-                hAs[c] = (double)As[c];
-                hTs[c] = (double)Ts[c];
-                hCt[c] = (double)Ct[c];
-                hFs[3 * c] = (double)Fs[c];
-                hFs[3 * c + 1] = (double)Fs[N + c];
-                hFs[3 * c + 2] = (double)Fs[2 * N + c];
+            for (int q = 0; q < EXPORT_CHUNK; ++q) {
+                const int64_t c = base + 32 * q + lane;
+                on[q] = ((word >> ((32 * q + lane) >> EXPORT_LG)) & 1u) && c < N;
+                a[q] = on[q] ? As[c] : 0.f;
+                t[q] = on[q] ? Ts[c] : 0.f;
+                k[q] = on[q] ? Ct[c] : 0;
             }
+#pragma unroll
+            for (int q = 0; q < EXPORT_CHUNK; ++q) {
+                const int64_t c = base + 32 * q + lane;
+                if (on[q]) {
+                    hAs[c] = (double)a[q];
+                    hTs[c] = (double)t[q];
+                    hCt[c] = (double)k[q];
+                }
+            }
+        }
+        // Fs: 3 x 256 elements, 24 stores per lane in three groups of eight
+#pragma unroll 1
+        for (int g = 0; g < 3; ++g) {
+            float v[8];
+            bool on[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int e = 32 * (8 * g + q) + lane;      // element of the word's interleaved sequence
+                const int cl = (int)((unsigned)e / 3u), comp = e - 3 * cl;
+                const int64_t c = base + cl;
+                on[q] = ((word >> (cl >> EXPORT_LG)) & 1u) && c < N;
+                v[q] = on[q] ? Fs[comp * N + c] : 0.f;
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (on[q]) hFs[3 * base + 32 * (8 * g + q) + lane] = (double)v[q];
         }
         __syncwarp();
         if (lane == 0) dirty[w] = 0u;
